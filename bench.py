@@ -1,0 +1,285 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the per-timestep MHD update on GB300.
+
+Workload (the metric's configuration): 256^3 periodic decaying MHD turbulence
+(seeded Gaussian-random solenoidal v and B, E(k) ~ k^-2 on 2 <= k <= 8, rms 1.0
+and 0.5, rho = 1, Ms = 0.5), PDM reconstruction + RK2, FP32 state and fluxes
+with FP64 metric and sums.  One step = one full RK2 step of the whole grid.
+
+Prints ONE JSON line (rank 0).  ``value`` = zone-updates/s over K device-timed
+steps (CUDA events on the solver's stream, graph replay, inputs resident);
+``e2e`` = the same metric through the C ABI with host FP64 buffers: mhd_init
+(H2D), K x mhd_step with tau/status read back, mhd_fetch of the output fields
+(D2H), all inside the timed region.
+
+``--impl reference`` times the reference algorithm on the host cores instead
+(the oracle port: no Fortran compiler exists to build the reference itself),
+one bounded-size RK2 step per timed step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+# Algorithmic (compulsory) HBM words per zone and stage of each launch family
+# (FP32 = 4 B per word): fluxes read 8 cell fields and write 8 face fluxes per
+# direction (3 directions); emf reads v1, v2, b1, b2, vf and writes E per edge
+# family (3 families); update reads 5 prims + 24 fluxes + 3x2 EMFs + 3 face B
+# (+8 U^n on later stages) and writes 5 prims + 3 face B.
+WORDS = {"fluxes": 48, "emf": 18, "update": 41}
+LAUNCHES = {"fluxes": 3, "emf": 3, "update": 2}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--recon", type=int, default=1)
+    ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-only", action="store_true", help="short run for ncu (no JSON extras)")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            time.sleep(0.25)
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().strip().splitlines() if r.strip()]
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload(n):
+    from mhd3d_mpi_fortran_gb300 import ics
+    s = ics.turbulence(n, seed=0)
+    return s, ics.cfl_dt(s, cfl=0.3)
+
+
+def cpu_rate(n, steps, recon=1):
+    """Oracle (FP64 restatement of the reference) zone-updates/s on the host."""
+    from mhd3d_mpi_fortran_gb300 import ics
+    from mhd3d_mpi_fortran_gb300.abi import Params
+    from oracle.oracle import OracleSolver, threads
+    s = ics.turbulence(n, seed=0)
+    prm = Params(n, n, n, reconop=recon, stepop=2, tau=ics.cfl_dt(s, cfl=0.3))
+    o = OracleSolver(prm, s)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return n ** 3 * steps / dt, dt, threads()
+
+
+def run_reference(a):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    # bounded per-step sample so that warmup + K steps stay within minutes
+    n = 64 if a.steps > 40 else 96
+    from mhd3d_mpi_fortran_gb300 import ics
+    from mhd3d_mpi_fortran_gb300.abi import Params
+    from oracle.oracle import OracleSolver, threads
+    s = ics.turbulence(n, seed=0)
+    prm = Params(n, n, n, reconop=a.recon, stepop=2, tau=ics.cfl_dt(s, cfl=0.3))
+    o = OracleSolver(prm, s)
+    o.step(max(1, min(a.warmup, 3)))
+    t0 = time.perf_counter()
+    o.step(a.steps)
+    dt = time.perf_counter() - t0
+    v = n ** 3 * a.steps / dt
+    line = {
+        "impl": "reference", "metric": "zone-updates/s", "value": v, "unit": "zone-updates/s",
+        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * dt / a.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded solenoidal turbulence (same generator)",
+        "config": {"workload": f"periodic decaying MHD turbulence, PDM + RK2 (sample {n}^3 per step "
+                               f"of the 256^3 workload)", "grid": [n, n, n]},
+        "cpu_baseline": {"value": v, "unit": "zone-updates/s", "cores": threads(), "kind": "port",
+                         "sample": f"{a.steps} RK2 steps of a {n}^3 grid, FP64 oracle restatement"},
+        "e2e": {"value": v, "unit": "zone-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(a):
+    ws, rank, local = dist_env()
+    if ws > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    from mhd3d_mpi_fortran_gb300 import MHDSolver
+    from mhd3d_mpi_fortran_gb300.abi import Params, FP32
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    n = a.n
+    s, tau = workload(n)
+    prm = Params(n, n, n, reconop=a.recon, stepop=2, precision=FP32, tau=tau)
+    graph = not a.no_graph
+    solver = MHDSolver(prm, s)
+    # warm-up (>= 3 steps), then the timed region
+    solver.time_steps(max(3, a.warmup), graph=graph)
+    if a.profile_only:
+        solver.time_steps(2, graph=False)
+        solver.close()
+        return
+    if pg:
+        pg.barrier()
+    with Clocks(0 if ws == 1 else local) as ck:
+        ms = solver.time_steps(a.steps, graph=graph)
+    clocks = ck.summary()
+    if pg:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    zu = n ** 3 * a.steps * ws / (ms * 1e-3)
+    # per-family device time (events on the solver's stream)
+    kprof = min(a.steps, 20)
+    solver.set_profiling(True)
+    solver.step_async(kprof)
+    fam = solver.timings()
+    solver.set_profiling(False)
+    _, st = solver.step(1)
+    solver.close()
+    stages = 2 * kprof
+    fam_ms = {k: v / stages for k, v in fam.items()}  # per stage
+    dom = max(("fluxes", "emf", "update"), key=lambda k: fam_ms[k])
+    hbm, peak_kind = peaks()
+    bytes_per_launch = WORDS[dom] * 4 * n ** 3 / LAUNCHES[dom]
+    launch_s = fam_ms[dom] * 1e-3 / LAUNCHES[dom]
+    achieved = bytes_per_launch / launch_s / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get(dom)
+    # e2e through the C ABI with host buffers
+    e2e = None
+    if not a.no_e2e and rank == 0:
+        ke = a.steps
+        t0 = time.perf_counter()
+        sv = MHDSolver(prm, s)
+        for _ in range(ke):
+            sv.step(1)
+        out = sv.fetch()
+        sv.close()
+        el = time.perf_counter() - t0
+        vol = (n + 9) * (n + 9) * (n + 9)
+        h2d = 8 * prm.shape[0] * prm.shape[1] * prm.shape[2] * 4
+        d2h = 11 * prm.shape[0] * prm.shape[1] * prm.shape[2] * 4 + ke * 48
+        e2e = {"value": n ** 3 * ke / el, "unit": "zone-updates/s", "h2d_bytes_per_step": int(h2d / ke),
+               "d2h_bytes_per_step": int(d2h / ke), "steps": ke, "seconds": el}
+        del out, vol
+    cpu = None
+    if not a.no_cpu_baseline and rank == 0 and ws == 1:
+        v, dt, cores = cpu_rate(128, 2, a.recon)
+        cpu = {"value": v, "unit": "zone-updates/s", "cores": cores, "kind": "port",
+               "sample": f"2 RK2 steps of the 128^3 turbulence state (same generator), PDM, FP64 oracle, {dt:.1f} s"}
+    if rank != 0:
+        return
+    launches_per_step = 2 + 1 + 2 * 10
+    line = {
+        "metric": "zone-updates/s", "value": zu, "unit": "zone-updates/s", "n_gpus": ws,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded Gaussian-random solenoidal turbulence, k^-2 on 2<=k<=8, 256^3 periodic",
+        "config": {"workload": f"{n}^3 periodic decaying MHD turbulence, PDM + RK2, FP32 state/fluxes, "
+                               f"FP64 metric and sums", "grid": [n, n, n], "recon": a.recon, "stepper": "RK2",
+                   "graph": graph, "l2": "inputs larger than L2 (FP32 state ~0.9 GB), no flush",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind},
+        "hbm_roofline_160B": {"achieved_gbs": zu * 160 / 1e9 / ws, "peak": hbm, "frac": zu * 160 / 1e9 / ws / hbm,
+                              "note": "compulsory 160 B per FP32 RK2 zone-update"},
+        "family_ms_per_stage": fam_ms,
+        "gpu_launches": launches_per_step * a.steps,
+        "clocks": clocks,
+        "status": st,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

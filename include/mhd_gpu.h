@@ -1,0 +1,165 @@
+/*
+ * mhd_gpu.h -- C ABI of the GB300 (sm_103a) per-timestep ideal-MHD update.
+ *
+ * The reference program (mhd3d3.f90, module globals + `call step`) has no
+ * plugin or FFI layer: the seam is the argument-less `call step` at
+ * mhd3d3.f90:3286, which reads and writes the module `fields` (mhd3d3.f90:251-316),
+ * the `pars` scalars (mhd3d3.f90:65-104) and the block geometry dxblock..dzblock
+ * (mhd3d3.f90:114-119).  The entry points below replace that seam one for one:
+ *
+ *   mhd_init   <- the end of `initialization` (mhd3d3.f90:3327-3377): the driver
+ *                 hands over the initialised, ghost-inclusive FP64 fields.
+ *   mhd_step   <- `call step` (mhd3d3.f90:3286 -> step, mhd3d3.f90:3585-3600).
+ *   mhd_fetch  <- the module arrays read by `outputxyz` (mhd3d3.f90:3091-3109)
+ *                 and by `diag_rho_neg` / `diag_overflow` (mhd3d3.f90:3143-3160).
+ *   mhd_free   <- `termination` / `dealloc_fields` (mhd3d3.f90:3936-3943, 319-337).
+ *
+ * Array convention (identical to the Fortran module arrays, mhd3d3.f90:287-290):
+ * FP64, column-major (x fastest), ghost-inclusive extents with ng = nord/2
+ * ghost layers per side and nx = nx0 + nord (same for y, z):
+ *   cell arrays  rho,vx,vy,vz,p,bx,by,bz : (nx, ny, nz)
+ *   face arrays  bi : (nx+1, ny, nz)   bj : (nx, ny+1, nz)   bk : (nx, ny, nz+1)
+ * Geometry: the reference's dxblock(i,j,k) depends on i only (init_geom,
+ * mhd3d3.f90:3473-3486), so it is passed as 1-D arrays dx[nx], dy[ny], dz[nz].
+ *
+ * All functions return 0 (MHD_OK) on success or a negative MHD_E* code.
+ * Nothing here blocks forever: device waits are bounded (MHD_E_TIMEOUT).
+ */
+#ifndef MHD_GPU_H
+#define MHD_GPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* reconop values (mhd3d3.f90:78-79, 833-860) plus the MC-limited TVD variant */
+enum { MHD_RECON_PDM = 1, MHD_RECON_TVD = 2, MHD_RECON_WENO5 = 3, MHD_RECON_MPWENO5 = 4,
+       MHD_RECON_TVD_MC = 5 };
+/* stepop values (mhd3d3.f90:3585-3600) */
+enum { MHD_STEP_AB2 = 1, MHD_STEP_RK2 = 2, MHD_STEP_RK3 = 3 };
+/* per-axis boundary kinds */
+enum { MHD_BC_PERIODIC = 0,   /* periodic Cartesian topology (mhd3d2.f90:3063-3064) */
+       MHD_BC_EVEN = 1,       /* even mirror of every variable (mhd3d3.f90:781-819, bc=0) */
+       MHD_BC_REFLECT = 2,    /* even mirror, normal velocity odd (mhd3d2.f90:713,720) */
+       MHD_BC_OUTFLOW = 3 };  /* zero-gradient copy of the boundary cell / face */
+enum { MHD_FP64 = 0, MHD_FP32 = 1 };
+/* dt_mode: 0 = as the reference (RK: fixed deck tau, mhd3d3.f90:3656-3661;
+ *              AB: CFL dt, mhd3d3.f90:3609), 1 = CFL dt for every stepop */
+enum { MHD_DT_REFERENCE = 0, MHD_DT_CFL = 1 };
+
+/* status bits returned by mhd_step (device-side checks of the reference's
+ * diag_rho_neg / diag_overflow, mhd3d3.f90:3143-3160, and its CFL warning,
+ * mhd3d3.f90:3658-3660) */
+enum {
+  MHD_ST_NAN        = 1u << 0,  /* NaN in rho, p or v (any cell incl. ghosts) */
+  MHD_ST_NEG_RHO    = 1u << 1,  /* rho < 0 somewhere (diag_rho_neg) */
+  MHD_ST_NEG_P      = 1u << 2,  /* p < 0 somewhere */
+  MHD_ST_CFL        = 1u << 3,  /* CFL dt < fixed tau (the reference only prints) */
+  MHD_ST_TIMEOUT    = 1u << 4,  /* a bounded device wait gave up */
+  MHD_ST_CUDA_ERROR = 1u << 5   /* a CUDA call failed; see mhd_last_error */
+};
+
+enum { MHD_OK = 0, MHD_E_ARG = -1, MHD_E_CUDA = -2, MHD_E_NOMEM = -3,
+       MHD_E_TIMEOUT = -4, MHD_E_STATE = -5 };
+
+typedef struct mhd_params {
+  int32_t nx0, ny0, nz0;   /* interior cells per axis (one rank: nx0 = nx0G) */
+  int32_t nord;            /* stencil order, ng = nord/2 (comp_pars, mhd3d3.f90:208) */
+  int32_t reconop;         /* MHD_RECON_* */
+  int32_t stepop;          /* MHD_STEP_* */
+  int32_t bc[3];           /* MHD_BC_* for x, y, z */
+  int32_t precision;       /* MHD_FP64 or MHD_FP32 */
+  int32_t dt_mode;         /* MHD_DT_* */
+  int32_t tvd_shift;       /* TVD corner stencils: 0 = shifts ignored as in
+                              mhd3d3.f90:1187-1237, 1 = honoured as in mhd3d2.f90:1152-1199 */
+  double gam;              /* 5/3 in the reference (mhd3d3.f90:51) */
+  double cfl, pdmb, eps, alpha, beta;   /* namelist `free` (mhd3d3.f90:91,156) */
+  double tau;              /* deck tau (namelist `list`); AB priming dt if > 0 */
+  int32_t reserved[8];
+} mhd_params;
+
+/* Create a solver on the current CUDA device from the driver's initialised
+ * fields.  The ghost fill and get_bxyz of `initialization`
+ * (mhd3d3.f90:3349-3351) are re-applied on the device.  Returns MHD_E_ARG for
+ * an unsupported deck (nord odd, nord < 8 with PDM, nord < 6 with WENO, ...). */
+int mhd_init(const mhd_params* prm,
+             const double* rho, const double* vx, const double* vy, const double* vz,
+             const double* p, const double* bi, const double* bj, const double* bk,
+             const double* dx, const double* dy, const double* dz, void** handle);
+
+/* One time step (replaces `call step`, mhd3d3.f90:3286).  On return *tau_out
+ * (if non-NULL) holds the dt the step used (the module `tau` after the step)
+ * and *status (if non-NULL) the MHD_ST_* bits of the checks made during it.
+ * Synchronous with respect to the handle's stream when either pointer is
+ * non-NULL. */
+int mhd_step(void* handle, double* tau_out, uint32_t* status);
+
+/* n steps back to back without host synchronisation in between (the driver's
+ * inner `do nt=1,nts` loop, mhd3d3.f90:3284-3288).  status accumulates. */
+int mhd_step_n(void* handle, int32_t nsteps, double* tau_out, uint32_t* status);
+
+/* Copy the current state back into ghost-inclusive FP64 Fortran arrays.  Any
+ * pointer may be NULL to skip that field.  Synchronous. */
+int mhd_fetch(void* handle, double* rho, double* vx, double* vy, double* vz,
+              double* p, double* bx, double* by, double* bz,
+              double* bi, double* bj, double* bk);
+
+/* FP64 diagnostics of the current state: out[0] = mass = sum rho dV,
+ * out[1] = total energy sum (rho v^2/2 + p/(gam-1) + B^2/2) dV, both with
+ * compensated (Neumaier) summation over interior cells, out[2] = max |div B|
+ * over interior cells from face B, out[3] = min rho (incl. ghosts),
+ * out[4] = CFL dt (mhd3d3.f90:1608-1639). No reference counterpart except
+ * out[3] (diag_rho_neg) and out[4] (get_dt). */
+int mhd_diagnostics(void* handle, double out[5]);
+
+/* Build a CUDA graph of n steps and replay it (graph-captured variant of
+ * mhd_step_n; same results). */
+int mhd_step_graph(void* handle, int32_t nsteps, double* tau_out, uint32_t* status);
+
+/* Set the dt used by the next RK step (the driver's deck `tau`), e.g. after a
+ * restart. */
+int mhd_set_tau(void* handle, double tau);
+
+/* Per-launch-family timing: when on, mhd_step_n brackets every launch family
+ * with CUDA events on the handle's stream (no extra synchronisation);
+ * mhd_last_timings then returns the summed device time of the last
+ * mhd_step_n call in ms: [fluxes, emf, update, fill+bxyz, dt(+save/predict)]. */
+int mhd_set_profiling(void* handle, int32_t on);
+int mhd_last_timings(void* handle, float out_ms[5]);
+
+/* Enqueue nsteps (graph-replayed when use_graph != 0) between two CUDA events
+ * recorded on the handle's stream; *ms = their elapsed device time. */
+int mhd_time_steps(void* handle, int32_t nsteps, int32_t use_graph, float* ms);
+
+int mhd_free(void* handle);
+
+/* Human-readable text of the last error on this thread. */
+const char* mhd_last_error(void);
+
+/* ---- kernel-level entry points used by the parity tests --------------- */
+
+/* Face fluxes of the current state, as get_flux_stress (mhd3d3.f90:2385-2560)
+ * leaves them: for dir d in {0,1,2} and q in {rho, rvx, rvy, rvz, eng,
+ * stress_x, stress_y, stress_z}, out[(d*8+q)*nface_d ...] with the reference's
+ * interior extents (nx0+1,ny0,nz0) / (nx0,ny0+1,nz0) / (nx0,ny0,nz0+1). */
+int mhd_debug_fluxes(void* handle, double* out);
+
+/* Edge EMFs of the current state, as get_eijk_LFM (mhd3d3.f90:1754-1856):
+ * ei (nx0,ny0+1,nz0+1), ej (nx0+1,ny0,nz0+1), ek (nx0+1,ny0+1,nz0). */
+int mhd_debug_emf(void* handle, double* ei, double* ej, double* ek);
+
+/* ---- batched ensemble of independent grids -------------------------- */
+
+/* Advance `ngrids` independent solvers (created by mhd_init, same precision,
+ * reconop and stepop, any sizes) by nsteps each, all grids of a stage in one
+ * launch per kernel family, replayed as one CUDA graph. */
+int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MHD_GPU_H */

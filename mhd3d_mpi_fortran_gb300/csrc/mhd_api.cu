@@ -1,0 +1,692 @@
+// C ABI of the GB300 MHD step (declared in include/mhd_gpu.h).  Host-side
+// sequencing of one time step on one CUDA stream; every kernel is in
+// mhd_kernels.cuh, instantiated per precision in mhd_fp32.cu / mhd_fp64.cu.
+//
+// Step sequence (reference routine -> launches):
+//   step_rk2/rk3 (mhd3d3.f90:3648-3792):
+//     get_dt -> Launch::cfl; advance_previous -> save_prev;
+//     per stage: get_eijk_LFM -> emf; get_flux_stress -> fluxes;
+//     advance_corrector1/2 + advance_bijk + combines -> update;
+//     fill_hydro_mpi/fill_mag_mpi -> fill; get_bxyz -> bxyz_vf.
+//   step_ab (mhd3d3.f90:3602-3644):
+//     get_dt -> cfl(AB); advance_predictor_ab -> predictor_ab; emf(h);
+//     fluxes(h); update; fill; bxyz.
+#include <cuda_runtime.h>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+#include <map>
+
+#include "../../include/mhd_gpu.h"
+#include "mhd_state.h"
+
+using namespace mhd;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(MHD_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
+  } while (0)
+
+constexpr double kWaitSeconds = 600.0;  // bound on any host wait for the device
+
+struct Handle {
+  mhd_params prm{};
+  Geom g{};
+  int fp32 = 0;
+  cudaStream_t st = nullptr;
+  void* buf = nullptr;
+  size_t bytes = 0;
+  double* geo = nullptr;       // dx | dy | dz (FP64)
+  Scal* sc = nullptr;          // device scalars
+  Scal* sc_h = nullptr;        // pinned mirror
+  double* diag = nullptr;      // device diagnostics buffer
+  double* diag_h = nullptr;    // pinned
+  Dev<float> df{};
+  Dev<double> dd{};
+  bool profile = false;
+  float tms[5] = {0, 0, 0, 0, 0};
+  cudaEvent_t ev[16] = {};
+  std::vector<cudaEvent_t> pool;
+  std::vector<int> fam;
+  std::map<int, cudaGraphExec_t> graphs;
+};
+
+size_t round_up(size_t a, size_t b) { return (a + b - 1) / b * b; }
+
+int wait_stream(Handle* h) {
+  cudaEvent_t e;
+  CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  CK(cudaEventRecord(e, h->st));
+  auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    cudaError_t q = cudaEventQuery(e);
+    if (q == cudaSuccess) break;
+    if (q != cudaErrorNotReady) {
+      cudaEventDestroy(e);
+      return fail(MHD_E_CUDA, std::string("device error: ") + cudaGetErrorString(q));
+    }
+    double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (el > kWaitSeconds) {
+      cudaEventDestroy(e);
+      return fail(MHD_E_TIMEOUT, "device did not finish within the wait bound");
+    }
+    std::this_thread::sleep_for(std::chrono::microseconds(el < 0.01 ? 20 : 500));
+  }
+  cudaEventDestroy(e);
+  return MHD_OK;
+}
+
+// ---- precision-generic step body -------------------------------------
+template <typename T>
+Inp<T> state_inp(const Dev<T>& d) {
+  return Inp<T>{d.rho, d.vx, d.vy, d.vz, d.p, d.bx, d.by, d.bz, d.bi, d.bj, d.bk};
+}
+template <typename T>
+Inp<T> half_inp(const Dev<T>& d) {
+  return Inp<T>{d.h[0], d.h[1], d.h[2], d.h[3], d.h[4], d.h[8], d.h[9], d.h[10], d.h[5], d.h[6], d.h[7]};
+}
+
+// Launch-family recorder: in profile mode every family is bracketed by a pair
+// of CUDA events on the stream (no synchronisation); pairs are resolved after
+// the call.  Families: 0 fluxes, 1 emf, 2 update, 3 fill+bxyz, 4 dt/save/predict.
+struct Rec {
+  Handle* h = nullptr;
+  cudaStream_t st = nullptr;
+  std::vector<cudaEvent_t>* pool = nullptr;
+  std::vector<int>* fam = nullptr;
+  size_t used = 0;
+  void begin() {
+    if (!pool) return;
+    while (pool->size() < used + 2) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      pool->push_back(e);
+    }
+    cudaEventRecord((*pool)[used], st);
+  }
+  void end(int f) {
+    if (!pool) return;
+    cudaEventRecord((*pool)[used + 1], st);
+    fam->push_back(f);
+    used += 2;
+  }
+};
+
+template <typename T>
+void enqueue_step(Handle* h, const Dev<T>& d, cudaStream_t st, Rec* r = nullptr) {
+  Rec none;
+  Rec& R = r ? *r : none;
+  const mhd_params& p = h->prm;
+  if (p.stepop == MHD_STEP_AB2) {
+    R.begin(); Launch<T>::cfl(d, 2, st); Launch<T>::predictor_ab(d, st); R.end(4);
+    Inp<T> in = half_inp(d);
+    R.begin(); Launch<T>::emf(d, in, st); R.end(1);
+    R.begin(); Launch<T>::fluxes(d, in, st); R.end(0);
+    R.begin(); Launch<T>::update(d, -1, 0.0, 1.0, st); R.end(2);
+    R.begin(); Launch<T>::fill(d, st); Launch<T>::bxyz_vf(d, false, st); R.end(3);
+    return;
+  }
+  R.begin();
+  Launch<T>::cfl(d, p.dt_mode == MHD_DT_CFL ? 1 : 0, st);
+  Launch<T>::save_prev(d, st);
+  R.end(4);
+  int nst = (p.stepop == MHD_STEP_RK2) ? 2 : 3;
+  Inp<T> in = state_inp(d);
+  for (int s = 1; s <= nst; ++s) {
+    int form = -1;
+    double c = 0.0, den = 1.0;
+    if (s > 1) {
+      if (nst == 2) { form = 0; den = 2.0; }
+      else if (s == 2) { form = 1; c = 3.0; den = 4.0; }
+      else { form = 2; c = 2.0; den = 3.0; }
+    }
+    R.begin(); Launch<T>::emf(d, in, st); R.end(1);
+    R.begin(); Launch<T>::fluxes(d, in, st); R.end(0);
+    R.begin(); Launch<T>::update(d, form, c, den, st); R.end(2);
+    R.begin(); Launch<T>::fill(d, st); Launch<T>::bxyz_vf(d, true, st); R.end(3);
+  }
+}
+
+template <typename T>
+void carve(Handle* h, Dev<T>& d, char* base) {
+  const Geom& g = h->g;
+  size_t n = (size_t)g.vol;
+  T* a = (T*)base;
+  auto next = [&]() { T* r = a; a += n; return r; };
+  d.g = g;
+  d.recon = h->prm.reconop;
+  d.stepop = h->prm.stepop;
+  d.tvd_shift = h->prm.tvd_shift;
+  d.dt_mode = h->prm.dt_mode;
+  for (int i = 0; i < 3; ++i) d.bc[i] = h->prm.bc[i];
+  d.gam = (T)h->prm.gam; d.pdmb = (T)h->prm.pdmb; d.eps = (T)h->prm.eps;
+  d.alpha = (T)h->prm.alpha; d.beta = (T)h->prm.beta; d.cfl = (T)h->prm.cfl;
+  d.rho = next(); d.vx = next(); d.vy = next(); d.vz = next(); d.p = next();
+  d.bi = next(); d.bj = next(); d.bk = next(); d.bx = next(); d.by = next(); d.bz = next();
+  int nq = (h->prm.stepop == MHD_STEP_AB2) ? 11 : 8;
+  for (int i = 0; i < 11; ++i) d.q[i] = (i < nq) ? next() : nullptr;
+  for (int i = 0; i < 11; ++i) d.h[i] = (h->prm.stepop == MHD_STEP_AB2) ? next() : nullptr;
+  for (int ax = 0; ax < 3; ++ax)
+    for (int q = 0; q < 8; ++q) d.F[ax][q] = next();
+  for (int e = 0; e < 3; ++e) d.E[e] = next();
+  d.vf = next();
+  d.dx = h->geo; d.dy = h->geo + g.nx; d.dz = h->geo + g.nx + g.ny;
+  d.sc = h->sc;
+  d.partial = nullptr;
+  d.counter = nullptr;
+}
+
+size_t n_arrays(const mhd_params& p) {
+  size_t n = 11 + ((p.stepop == MHD_STEP_AB2) ? 22 : 8) + 24 + 3 + 1;
+  return n;
+}
+
+// host FP64 Fortran array (ex,ey,ez) <-> device padded T
+template <typename T>
+void pack(const Geom& g, const double* src, int ex, int ey, int ez, T* dst) {
+  for (int k = 0; k < ez; ++k)
+    for (int j = 0; j < ey; ++j) {
+      const double* s = src + (size_t)ex * ((size_t)j + (size_t)ey * k);
+      T* d = dst + (size_t)g.px * ((size_t)j + (size_t)g.py * k);
+      for (int i = 0; i < ex; ++i) d[i] = (T)s[i];
+    }
+}
+template <typename T>
+void unpack(const Geom& g, const T* src, int ex, int ey, int ez, double* dst) {
+  for (int k = 0; k < ez; ++k)
+    for (int j = 0; j < ey; ++j) {
+      const T* s = src + (size_t)g.px * ((size_t)j + (size_t)g.py * k);
+      double* d = dst + (size_t)ex * ((size_t)j + (size_t)ey * k);
+      for (int i = 0; i < ex; ++i) d[i] = (double)s[i];
+    }
+}
+
+template <typename T>
+Dev<T>& dev(Handle* h);
+template <>
+Dev<float>& dev<float>(Handle* h) { return h->df; }
+template <>
+Dev<double>& dev<double>(Handle* h) { return h->dd; }
+
+template <typename T>
+int upload(Handle* h, const double* const* arrs) {
+  const Geom& g = h->g;
+  Dev<T>& d = dev<T>(h);
+  T* dsts[8] = {d.rho, d.vx, d.vy, d.vz, d.p, d.bi, d.bj, d.bk};
+  int ext[8][3] = {{g.nx, g.ny, g.nz}, {g.nx, g.ny, g.nz}, {g.nx, g.ny, g.nz}, {g.nx, g.ny, g.nz},
+                   {g.nx, g.ny, g.nz}, {g.nx + 1, g.ny, g.nz}, {g.nx, g.ny + 1, g.nz},
+                   {g.nx, g.ny, g.nz + 1}};
+  T* stage = nullptr;
+  CK(cudaMallocHost(&stage, (size_t)g.vol * sizeof(T)));
+  for (int a = 0; a < 8; ++a) {
+    std::memset(stage, 0, (size_t)g.vol * sizeof(T));
+    pack<T>(g, arrs[a], ext[a][0], ext[a][1], ext[a][2], stage);
+    cudaError_t e = cudaMemcpyAsync(dsts[a], stage, (size_t)g.vol * sizeof(T), cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (e != cudaSuccess) {
+      cudaFreeHost(stage);
+      return fail(MHD_E_CUDA, std::string("upload: ") + cudaGetErrorString(e));
+    }
+  }
+  cudaFreeHost(stage);
+  return MHD_OK;
+}
+
+template <typename T>
+int init_device(Handle* h) {
+  Dev<T>& d = dev<T>(h);
+  cudaStream_t st = h->st;
+  Launch<T>::fill(d, st);
+  Launch<T>::bxyz_vf(d, h->prm.stepop != MHD_STEP_AB2, st);
+  if (h->prm.stepop == MHD_STEP_AB2) {
+    if (!(h->prm.tau > 0.0)) Launch<T>::cfl(d, 1, st);  // prime with the CFL dt (mhd3d2)
+    T* x[11] = {d.rho, d.vx, d.vy, d.vz, d.p, d.bi, d.bj, d.bk, d.bx, d.by, d.bz};
+    for (int a = 0; a < 11; ++a)
+      CK(cudaMemcpyAsync(d.q[a], x[a], (size_t)h->g.vol * sizeof(T), cudaMemcpyDeviceToDevice, st));
+  }
+  CK(cudaGetLastError());
+  return wait_stream(h);
+}
+
+template <typename T>
+int do_steps(Handle* h, int n) {
+  Dev<T>& d = dev<T>(h);
+  if (h->profile) {
+    for (int i = 0; i < 5; ++i) h->tms[i] = 0;
+    Rec r;
+    r.h = h; r.st = h->st; r.pool = &h->pool; r.fam = &h->fam;
+    h->fam.clear();
+    for (int s = 0; s < n; ++s) enqueue_step<T>(h, d, h->st, &r);
+    CK(cudaGetLastError());
+    int rc = wait_stream(h);
+    if (rc) return rc;
+    for (size_t i = 0; i < h->fam.size(); ++i) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, h->pool[2 * i], h->pool[2 * i + 1]);
+      h->tms[h->fam[i]] += ms;
+    }
+    return MHD_OK;
+  }
+  for (int s = 0; s < n; ++s) enqueue_step<T>(h, d, h->st);
+  CK(cudaGetLastError());
+  return MHD_OK;
+}
+
+int finish(Handle* h, double* tau_out, uint32_t* status) {
+  if (!tau_out && !status) return MHD_OK;
+  CK(cudaMemcpyAsync(h->sc_h, h->sc, sizeof(Scal), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemsetAsync(&h->sc->status, 0, sizeof(unsigned int), h->st));
+  int rc = wait_stream(h);
+  if (rc) {
+    if (status) *status = MHD_ST_TIMEOUT | (rc == MHD_E_CUDA ? MHD_ST_CUDA_ERROR : 0);
+    return rc;
+  }
+  if (tau_out) *tau_out = h->sc_h->tau;
+  if (status) *status = h->sc_h->status;
+  return MHD_OK;
+}
+
+int validate(const mhd_params* p) {
+  if (!p) return fail(MHD_E_ARG, "null params");
+  if (p->nx0 < 1 || p->ny0 < 1 || p->nz0 < 1) return fail(MHD_E_ARG, "grid sizes must be positive");
+  if (p->nord <= 0 || (p->nord & 1)) return fail(MHD_E_ARG, "nord must be even and positive");
+  if (p->reconop < 1 || p->reconop > 5) return fail(MHD_E_ARG, "reconop must be 1..5");
+  if (p->stepop < 1 || p->stepop > 3) return fail(MHD_E_ARG, "stepop must be 1..3");
+  int need = (p->reconop == 1) ? 8 : (p->reconop == 3 || p->reconop == 4) ? 6 : 4;
+  if (p->nord < need) return fail(MHD_E_ARG, "nord too small for the reconstruction stencil");
+  int ng = p->nord / 2;
+  for (int a = 0; a < 3; ++a) {
+    if (p->bc[a] < 0 || p->bc[a] > 3) return fail(MHD_E_ARG, "bc must be 0..3");
+    int n0 = a == 0 ? p->nx0 : a == 1 ? p->ny0 : p->nz0;
+    if (n0 < ng) return fail(MHD_E_ARG, "each axis needs at least ng interior cells");
+  }
+  if (p->precision != MHD_FP32 && p->precision != MHD_FP64) return fail(MHD_E_ARG, "precision 0 or 1");
+  if (!(p->gam > 1.0)) return fail(MHD_E_ARG, "gam must exceed 1");
+  if (p->stepop != MHD_STEP_AB2 && p->dt_mode == MHD_DT_REFERENCE && !(p->tau > 0.0))
+    return fail(MHD_E_ARG, "RK with the reference dt needs tau > 0");
+  return MHD_OK;
+}
+
+}  // namespace
+
+// Entry points: C linkage comes from their declarations in mhd_gpu.h.
+
+const char* mhd_last_error(void) { return g_err.c_str(); }
+
+int mhd_init(const mhd_params* prm, const double* rho, const double* vx, const double* vy,
+             const double* vz, const double* p, const double* bi, const double* bj, const double* bk,
+             const double* dx, const double* dy, const double* dz, void** handle) {
+  if (!handle) return fail(MHD_E_ARG, "null handle pointer");
+  *handle = nullptr;
+  int rc = validate(prm);
+  if (rc) return rc;
+  if (!rho || !vx || !vy || !vz || !p || !bi || !bj || !bk || !dx || !dy || !dz)
+    return fail(MHD_E_ARG, "null field pointer");
+  Handle* h = new Handle();
+  h->prm = *prm;
+  h->fp32 = (prm->precision == MHD_FP32);
+  Geom& g = h->g;
+  g.nx0 = prm->nx0; g.ny0 = prm->ny0; g.nz0 = prm->nz0;
+  g.nord = prm->nord; g.ng = prm->nord / 2;
+  g.nx = g.nx0 + g.nord; g.ny = g.ny0 + g.nord; g.nz = g.nz0 + g.nord;
+  g.px = (int)round_up((size_t)g.nx + 1, 32);
+  g.py = g.ny + 1;
+  g.pz = g.nz + 1;
+  g.plane = (long long)g.px * g.py;
+  g.vol = g.plane * g.pz;
+  size_t es = h->fp32 ? sizeof(float) : sizeof(double);
+  h->bytes = n_arrays(*prm) * (size_t)g.vol * es;
+  auto bail = [&](int code, const std::string& m) {
+    mhd_free(h);
+    return fail(code, m);
+  };
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(MHD_E_CUDA, "stream create failed");
+  if (cudaMalloc(&h->buf, h->bytes) != cudaSuccess) return bail(MHD_E_NOMEM, "device allocation failed");
+  if (cudaMalloc(&h->geo, sizeof(double) * (g.nx + g.ny + g.nz)) != cudaSuccess ||
+      cudaMalloc(&h->sc, sizeof(Scal)) != cudaSuccess ||
+      cudaMalloc(&h->diag, sizeof(double) * (8 + 5 * 152 * 2)) != cudaSuccess)
+    return bail(MHD_E_NOMEM, "device allocation failed");
+  if (cudaMallocHost(&h->sc_h, sizeof(Scal)) != cudaSuccess ||
+      cudaMallocHost(&h->diag_h, sizeof(double) * 8) != cudaSuccess)
+    return bail(MHD_E_NOMEM, "pinned allocation failed");
+  for (int i = 0; i < 16; ++i) cudaEventCreate(&h->ev[i]);
+  if (cudaMemsetAsync(h->buf, 0, h->bytes, h->st) != cudaSuccess) return bail(MHD_E_CUDA, "memset failed");
+  std::vector<double> geo((size_t)g.nx + g.ny + g.nz);
+  std::memcpy(geo.data(), dx, sizeof(double) * g.nx);
+  std::memcpy(geo.data() + g.nx, dy, sizeof(double) * g.ny);
+  std::memcpy(geo.data() + g.nx + g.ny, dz, sizeof(double) * g.nz);
+  for (double v : geo)
+    if (!(v > 0.0)) return bail(MHD_E_ARG, "cell widths must be positive (diag_geom)");
+  if (cudaMemcpy(h->geo, geo.data(), sizeof(double) * geo.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(MHD_E_CUDA, "geometry upload failed");
+  Scal s{};
+  s.tau = prm->tau;
+  s.tau0 = prm->tau;
+  s.dt_cfl = 0.0;
+  s.ab_coef = 0.0;
+  double inf = INFINITY;
+  std::memcpy(&s.dtmin_bits, &inf, sizeof(double));
+  s.status = 0;
+  if (cudaMemcpy(h->sc, &s, sizeof(Scal), cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(MHD_E_CUDA, "scalar upload failed");
+  if (h->fp32) carve<float>(h, h->df, (char*)h->buf);
+  else carve<double>(h, h->dd, (char*)h->buf);
+  const double* arrs[8] = {rho, vx, vy, vz, p, bi, bj, bk};
+  rc = h->fp32 ? upload<float>(h, arrs) : upload<double>(h, arrs);
+  if (rc) { std::string m = g_err; mhd_free(h); return fail(rc, m); }
+  rc = h->fp32 ? init_device<float>(h) : init_device<double>(h);
+  if (rc) { std::string m = g_err; mhd_free(h); return fail(rc, m); }
+  *handle = h;
+  return MHD_OK;
+}
+
+int mhd_step_n(void* handle, int32_t nsteps, double* tau_out, uint32_t* status) {
+  Handle* h = (Handle*)handle;
+  if (!h) return fail(MHD_E_ARG, "null handle");
+  if (nsteps < 0) return fail(MHD_E_ARG, "nsteps < 0");
+  int rc = h->fp32 ? do_steps<float>(h, nsteps) : do_steps<double>(h, nsteps);
+  if (rc) {
+    if (status) *status = MHD_ST_CUDA_ERROR;
+    return rc;
+  }
+  return finish(h, tau_out, status);
+}
+
+int mhd_step(void* handle, double* tau_out, uint32_t* status) {
+  return mhd_step_n(handle, 1, tau_out, status);
+}
+
+static int graph_for(Handle* h, int nsteps, cudaGraphExec_t* out);
+
+int mhd_step_graph(void* handle, int32_t nsteps, double* tau_out, uint32_t* status) {
+  Handle* h = (Handle*)handle;
+  if (!h) return fail(MHD_E_ARG, "null handle");
+  if (nsteps <= 0) return fail(MHD_E_ARG, "nsteps must be positive");
+  cudaGraphExec_t ex = nullptr;
+  int rc = graph_for(h, nsteps, &ex);
+  if (rc) return rc;
+  CK(cudaGraphLaunch(ex, h->st));
+  return finish(h, tau_out, status);
+}
+
+static int graph_for(Handle* h, int nsteps, cudaGraphExec_t* out) {
+  auto it = h->graphs.find(nsteps);
+  if (it != h->graphs.end()) {
+    *out = it->second;
+    return MHD_OK;
+  }
+  cudaGraph_t gr;
+  cudaGraphExec_t ex;
+  CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+  for (int s = 0; s < nsteps; ++s) {
+    if (h->fp32) enqueue_step<float>(h, h->df, h->st);
+    else enqueue_step<double>(h, h->dd, h->st);
+  }
+  CK(cudaStreamEndCapture(h->st, &gr));
+  CK(cudaGraphInstantiate(&ex, gr, 0));
+  cudaGraphDestroy(gr);
+  h->graphs[nsteps] = ex;
+  *out = ex;
+  return MHD_OK;
+}
+
+int mhd_time_steps(void* handle, int32_t nsteps, int32_t use_graph, float* ms) {
+  Handle* h = (Handle*)handle;
+  if (!h || !ms || nsteps <= 0) return fail(MHD_E_ARG, "bad arguments");
+  cudaGraphExec_t ex = nullptr;
+  if (use_graph) {
+    int rc = graph_for(h, nsteps, &ex);
+    if (rc) return rc;
+  }
+  CK(cudaEventRecord(h->ev[0], h->st));
+  if (use_graph) {
+    CK(cudaGraphLaunch(ex, h->st));
+  } else {
+    int rc = h->fp32 ? do_steps<float>(h, nsteps) : do_steps<double>(h, nsteps);
+    if (rc) return rc;
+  }
+  CK(cudaEventRecord(h->ev[1], h->st));
+  int rc = wait_stream(h);
+  if (rc) return rc;
+  CK(cudaEventElapsedTime(ms, h->ev[0], h->ev[1]));
+  return MHD_OK;
+}
+
+int mhd_set_tau(void* handle, double tau) {
+  Handle* h = (Handle*)handle;
+  if (!h || !(tau > 0.0)) return fail(MHD_E_ARG, "bad handle or tau");
+  int rc = wait_stream(h);
+  if (rc) return rc;
+  CK(cudaMemcpy(h->sc_h, h->sc, sizeof(Scal), cudaMemcpyDeviceToHost));
+  h->sc_h->tau = tau;
+  h->sc_h->tau0 = tau;
+  CK(cudaMemcpy(h->sc, h->sc_h, sizeof(Scal), cudaMemcpyHostToDevice));
+  h->prm.tau = tau;
+  return MHD_OK;
+}
+
+int mhd_set_profiling(void* handle, int32_t on) {
+  Handle* h = (Handle*)handle;
+  if (!h) return fail(MHD_E_ARG, "null handle");
+  h->profile = on != 0;
+  return MHD_OK;
+}
+
+int mhd_last_timings(void* handle, float out_ms[5]) {
+  Handle* h = (Handle*)handle;
+  if (!h || !out_ms) return fail(MHD_E_ARG, "null argument");
+  for (int i = 0; i < 5; ++i) out_ms[i] = h->tms[i];
+  return MHD_OK;
+}
+
+template <typename T>
+static int fetch_t(Handle* h, double* const* outs) {
+  const Geom& g = h->g;
+  Dev<T>& d = dev<T>(h);
+  const T* srcs[11] = {d.rho, d.vx, d.vy, d.vz, d.p, d.bx, d.by, d.bz, d.bi, d.bj, d.bk};
+  int ext[11][3];
+  for (int a = 0; a < 8; ++a) { ext[a][0] = g.nx; ext[a][1] = g.ny; ext[a][2] = g.nz; }
+  ext[8][0] = g.nx + 1; ext[8][1] = g.ny; ext[8][2] = g.nz;
+  ext[9][0] = g.nx; ext[9][1] = g.ny + 1; ext[9][2] = g.nz;
+  ext[10][0] = g.nx; ext[10][1] = g.ny; ext[10][2] = g.nz + 1;
+  T* stage = nullptr;
+  CK(cudaMallocHost(&stage, (size_t)g.vol * sizeof(T)));
+  for (int a = 0; a < 11; ++a) {
+    if (!outs[a]) continue;
+    cudaError_t e = cudaMemcpyAsync(stage, srcs[a], (size_t)g.vol * sizeof(T), cudaMemcpyDeviceToHost, h->st);
+    if (e != cudaSuccess) { cudaFreeHost(stage); return fail(MHD_E_CUDA, cudaGetErrorString(e)); }
+    int rc = wait_stream(h);
+    if (rc) { cudaFreeHost(stage); return rc; }
+    unpack<T>(g, stage, ext[a][0], ext[a][1], ext[a][2], outs[a]);
+  }
+  cudaFreeHost(stage);
+  return MHD_OK;
+}
+
+int mhd_fetch(void* handle, double* rho, double* vx, double* vy, double* vz, double* p, double* bx,
+              double* by, double* bz, double* bi, double* bj, double* bk) {
+  Handle* h = (Handle*)handle;
+  if (!h) return fail(MHD_E_ARG, "null handle");
+  double* outs[11] = {rho, vx, vy, vz, p, bx, by, bz, bi, bj, bk};
+  return h->fp32 ? fetch_t<float>(h, outs) : fetch_t<double>(h, outs);
+}
+
+template <typename T>
+static int diag_t(Handle* h, double out[5]) {
+  Dev<T>& d = dev<T>(h);
+  Launch<T>::diagnostics(d, h->diag, h->st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(h->diag_h, h->diag, sizeof(double) * 4, cudaMemcpyDeviceToHost, h->st));
+  int rc = wait_stream(h);
+  if (rc) return rc;
+  for (int i = 0; i < 4; ++i) out[i] = h->diag_h[i];
+  // CFL dt of the current state: the dt kernel in "peek" mode (status kept)
+  Launch<T>::cfl(d, 3, h->st);
+  CK(cudaMemcpyAsync(h->sc_h, h->sc, sizeof(Scal), cudaMemcpyDeviceToHost, h->st));
+  rc = wait_stream(h);
+  if (rc) return rc;
+  out[4] = h->sc_h->dt_cfl;
+  return MHD_OK;
+}
+
+int mhd_diagnostics(void* handle, double out[5]) {
+  Handle* h = (Handle*)handle;
+  if (!h || !out) return fail(MHD_E_ARG, "null argument");
+  return h->fp32 ? diag_t<float>(h, out) : diag_t<double>(h, out);
+}
+
+template <typename T>
+static int dbg_flux_t(Handle* h, double* out) {
+  const Geom& g = h->g;
+  Dev<T>& d = dev<T>(h);
+  Launch<T>::fluxes(d, state_inp(d), h->st);
+  CK(cudaGetLastError());
+  std::vector<T> host((size_t)g.vol);
+  size_t off = 0;
+  for (int ax = 0; ax < 3; ++ax) {
+    int ex = g.nx0 + (ax == 0), ey = g.ny0 + (ax == 1), ez = g.nz0 + (ax == 2);
+    for (int q = 0; q < 8; ++q) {
+      CK(cudaMemcpyAsync(host.data(), d.F[ax][q], (size_t)g.vol * sizeof(T), cudaMemcpyDeviceToHost, h->st));
+      int rc = wait_stream(h);
+      if (rc) return rc;
+      for (int k = 0; k < ez; ++k)
+        for (int j = 0; j < ey; ++j)
+          for (int i = 0; i < ex; ++i)
+            out[off + i + (size_t)ex * (j + (size_t)ey * k)] =
+                (double)host[(size_t)(i + g.ng) + (size_t)g.px * ((j + g.ng) + (size_t)g.py * (k + g.ng))];
+      off += (size_t)ex * ey * ez;
+    }
+  }
+  return MHD_OK;
+}
+
+int mhd_debug_fluxes(void* handle, double* out) {
+  Handle* h = (Handle*)handle;
+  if (!h || !out) return fail(MHD_E_ARG, "null argument");
+  return h->fp32 ? dbg_flux_t<float>(h, out) : dbg_flux_t<double>(h, out);
+}
+
+template <typename T>
+static int dbg_emf_t(Handle* h, double* const* outs) {
+  const Geom& g = h->g;
+  Dev<T>& d = dev<T>(h);
+  Launch<T>::bxyz_vf(d, true, h->st);
+  Launch<T>::emf(d, state_inp(d), h->st);
+  CK(cudaGetLastError());
+  std::vector<T> host((size_t)g.vol);
+  for (int e = 0; e < 3; ++e) {
+    if (!outs[e]) continue;
+    int ex = g.nx0 + (e != 0), ey = g.ny0 + (e != 1), ez = g.nz0 + (e != 2);
+    CK(cudaMemcpyAsync(host.data(), d.E[e], (size_t)g.vol * sizeof(T), cudaMemcpyDeviceToHost, h->st));
+    int rc = wait_stream(h);
+    if (rc) return rc;
+    for (int k = 0; k < ez; ++k)
+      for (int j = 0; j < ey; ++j)
+        for (int i = 0; i < ex; ++i)
+          outs[e][i + (size_t)ex * (j + (size_t)ey * k)] =
+              (double)host[(size_t)(i + g.ng) + (size_t)g.px * ((j + g.ng) + (size_t)g.py * (k + g.ng))];
+  }
+  return MHD_OK;
+}
+
+int mhd_debug_emf(void* handle, double* ei, double* ej, double* ek) {
+  Handle* h = (Handle*)handle;
+  if (!h) return fail(MHD_E_ARG, "null handle");
+  double* outs[3] = {ei, ej, ek};
+  return h->fp32 ? dbg_emf_t<float>(h, outs) : dbg_emf_t<double>(h, outs);
+}
+
+// Ensemble: one CUDA graph with one branch per grid (grids run concurrently),
+// nsteps steps per grid; cached per (handle list, nsteps).
+int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* status) {
+  if (!handles || ngrids <= 0 || nsteps <= 0) return fail(MHD_E_ARG, "bad ensemble arguments");
+  Handle* h0 = (Handle*)handles[0];
+  for (int i = 0; i < ngrids; ++i) {
+    Handle* h = (Handle*)handles[i];
+    if (!h) return fail(MHD_E_ARG, "null handle in ensemble");
+    if (h->fp32 != h0->fp32) return fail(MHD_E_ARG, "ensemble grids must share the precision");
+  }
+  static thread_local std::map<std::vector<void*>, std::pair<int, cudaGraphExec_t>> cache;
+  std::vector<void*> key(handles, handles + ngrids);
+  key.push_back((void*)(intptr_t)nsteps);
+  cudaGraphExec_t ex = nullptr;
+  auto it = cache.find(key);
+  if (it == cache.end()) {
+    cudaEvent_t fork;
+    CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    CK(cudaStreamBeginCapture(h0->st, cudaStreamCaptureModeThreadLocal));
+    CK(cudaEventRecord(fork, h0->st));
+    std::vector<cudaEvent_t> joins(ngrids);
+    for (int i = 1; i < ngrids; ++i) {
+      Handle* h = (Handle*)handles[i];
+      CK(cudaStreamWaitEvent(h->st, fork, 0));
+    }
+    for (int i = 0; i < ngrids; ++i) {
+      Handle* h = (Handle*)handles[i];
+      for (int s = 0; s < nsteps; ++s) {
+        if (h->fp32) enqueue_step<float>(h, h->df, h->st);
+        else enqueue_step<double>(h, h->dd, h->st);
+      }
+      if (i > 0) {
+        CK(cudaEventCreateWithFlags(&joins[i], cudaEventDisableTiming));
+        CK(cudaEventRecord(joins[i], h->st));
+        CK(cudaStreamWaitEvent(h0->st, joins[i], 0));
+      }
+    }
+    cudaGraph_t gr;
+    CK(cudaStreamEndCapture(h0->st, &gr));
+    CK(cudaGraphInstantiate(&ex, gr, 0));
+    cudaGraphDestroy(gr);
+    for (int i = 1; i < ngrids; ++i) cudaEventDestroy(joins[i]);
+    cudaEventDestroy(fork);
+    cache[key] = {nsteps, ex};
+  } else {
+    ex = it->second.second;
+  }
+  CK(cudaGraphLaunch(ex, h0->st));
+  uint32_t acc = 0;
+  for (int i = 0; i < ngrids; ++i) {
+    Handle* h = (Handle*)handles[i];
+    uint32_t st = 0;
+    int rc = finish(h, nullptr, &st);
+    if (rc) return rc;
+    acc |= st;
+  }
+  if (status) *status = acc;
+  return MHD_OK;
+}
+
+int mhd_free(void* handle) {
+  Handle* h = (Handle*)handle;
+  if (!h) return MHD_OK;
+  if (h->st) cudaStreamSynchronize(h->st);
+  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+  for (int i = 0; i < 16; ++i)
+    if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+  for (cudaEvent_t e : h->pool) cudaEventDestroy(e);
+  if (h->buf) cudaFree(h->buf);
+  if (h->geo) cudaFree(h->geo);
+  if (h->sc) cudaFree(h->sc);
+  if (h->diag) cudaFree(h->diag);
+  if (h->sc_h) cudaFreeHost(h->sc_h);
+  if (h->diag_h) cudaFreeHost(h->diag_h);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return MHD_OK;
+}

@@ -1,0 +1,897 @@
+// Device kernels of the per-timestep MHD update.  Included by exactly one
+// translation unit per precision: mhd_fp64.cu (built with -fmad=false so that
+// every FP64 expression is rounded exactly as the reference writes it) and
+// mhd_fp32.cu (FMA contraction on, the performance path).
+//
+// Kernel map (reference routine -> kernel):
+//   get_bxyz (mhd3d3.f90:2118-2128) + vf of get_eijk_LFM (1766)  -> k_bxyz_vf
+//   get_dt   (1608-1639) + diag_rho_neg/diag_overflow (3143-3160) -> k_cfl, k_cfl_final
+//   advance_previous (3794-3819)                                  -> k_save_prev
+//   advance_predictor_ab (3821-3840)                              -> k_predictor_ab
+//   get_flux_stress + get_v_face + reconstruct_3d (2385-2615, 833-1596) -> k_flux
+//   get_eijk_LFM + get_vav_center2corner + interp2_* (1754-2116, 926-1067) -> k_emf
+//   get_conserve + advance_corrector1/2 + RK combines (1641-1650, 3842-3907,
+//     3670-3697, 3741-3783)                                       -> k_update_hydro
+//   advance_bijk + B combines (3909-3933, 3698-3702, 3784-3788)   -> k_update_b
+//   fill_hydro_mpi / fill_mag_mpi (781-819, 346-616)              -> k_fill
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include "mhd_state.h"
+
+namespace mhd {
+
+enum { R_PDM = 1, R_TVD = 2, R_WENO = 3, R_MPWENO = 4, R_TVDMC = 5 };
+enum { BC_PERIODIC = 0, BC_EVEN = 1, BC_REFLECT = 2, BC_OUTFLOW = 3 };
+enum { ST_NAN = 1u, ST_NEG_RHO = 2u, ST_NEG_P = 4u, ST_CFL = 8u };
+
+// ---------------------------------------------------------------- scalar ops
+// Fortran sign(1,x) with ifort's default: +1 for x >= 0, including -0.0.
+template <typename T> __device__ __forceinline__ T sgn1(T x) { return x >= T(0) ? T(1) : T(-1); }
+template <typename T> __device__ __forceinline__ T mx(T a, T b) { return a > b ? a : b; }
+template <typename T> __device__ __forceinline__ T mn(T a, T b) { return a < b ? a : b; }
+__device__ __forceinline__ double fab(double x) { return fabs(x); }
+__device__ __forceinline__ float fab(float x) { return fabsf(x); }
+__device__ __forceinline__ double sq(double x) { return sqrt(x); }
+__device__ __forceinline__ float sq(float x) { return sqrtf(x); }
+__device__ __forceinline__ double ex(double x) { return exp(x); }
+__device__ __forceinline__ float ex(float x) { return expf(x); }
+__device__ __forceinline__ double erc(double x) { return erfc(x); }
+__device__ __forceinline__ float erc(float x) { return erfcf(x); }
+
+// Division by a constant: exact in FP64 (reference rounding), reciprocal
+// multiply in FP32.
+template <typename T> struct Div;
+template <> struct Div<double> {
+  static __device__ __forceinline__ double by(double a, double b) { return a / b; }
+};
+template <> struct Div<float> {
+  static __device__ __forceinline__ float by(float a, float b) { return a * (1.0f / b); }
+};
+
+// 8-point centred interpolant (interp_pdm, mhd3d3.f90:866-872), operand order kept.
+template <typename T>
+__device__ __forceinline__ T tap8(T a0, T a1, T a2, T a3, T a4, T a5, T a6, T a7) {
+  T s = T(-3) * a0;
+  s = s + T(29) * a1;
+  s = s - T(139) * a2;
+  s = s + T(533) * a3;
+  s = s + T(533) * a4;
+  s = s - T(139) * a5;
+  s = s + T(29) * a6;
+  s = s - T(3) * a7;
+  return Div<T>::by(s, T(840));
+}
+
+// PDM2 (mhd3d3.f90:1069-1172): clamp of the interpolant and partial-donor limiter.
+template <typename T>
+__device__ __forceinline__ void pdm2(T fm2, T fm1, T f0, T fp1, T fi, T pdmb, T& fl, T& fr) {
+  T maxf = mx(fm1, f0), minf = mn(fm1, f0);
+  T fii = mx(minf, mn(fi, maxf));
+  T dfm = pdmb * (fm1 - fm2);
+  T df0 = pdmb * (f0 - fm1);
+  T dfp = pdmb * (fp1 - f0);
+  T sm = sgn1(dfm), s0 = sgn1(df0), sp = sgn1(dfp);
+  dfm = fab(dfm);
+  dfp = fab(dfp);
+  T qm = fab(sm + s0), qp = fab(s0 + sp);
+  T dfl = fii - fm1, dfr = f0 - fii;
+  fl = fii - s0 * mx(T(0), fab(dfl) - qm * dfm);
+  fr = fii + s0 * mx(T(0), fab(dfr) - qp * dfp);
+}
+
+// TVD (mhd3d3.f90:1238-1248): van Leer b = (a+|a|)/(1+|a|); MC variant
+// b = max(0, min(2a, (1+a)/2, 2)) (fi is the centred value, so b is phi(a)).
+template <typename T, bool MC>
+__device__ __forceinline__ T tvdb(T a) {
+  if (MC) return mx(T(0), mn(mn(T(2) * a, T(0.5) * (T(1) + a)), T(2)));
+  return (a + fab(a)) / (T(1) + fab(a));
+}
+template <typename T, bool MC>
+__device__ __forceinline__ void tvd(T fm2, T fm1, T f0, T fp1, T fi, T eps, T& fl, T& fr) {
+  T a = (fm1 - fm2) / (f0 - fm1 + eps);
+  T b = tvdb<T, MC>(a);
+  fl = fm1 - b * (fm1 - fi);
+  a = (f0 - fp1) / (fm1 - f0 + eps);
+  b = tvdb<T, MC>(a);
+  fr = f0 - b * (f0 - fi);
+}
+
+// WENO5 (mhd3d3.f90:1329-1375), one face.
+template <typename T>
+__device__ __forceinline__ void weno5(T fm3, T fm2, T fm1, T f0, T fp1, T fp2, T eps, T& fl, T& fr) {
+  const T c13 = T(13.0) / T(12.0);
+  T h0 = Div<T>::by(T(2) * fm3 - T(7) * fm2 + T(11) * fm1, T(6));
+  T h1 = Div<T>::by(-fm2 + T(5) * fm1 + T(2) * f0, T(6));
+  T h2 = Div<T>::by(T(2) * fm1 + T(5) * f0 - fp1, T(6));
+  T t = fm3 - T(2) * fm2 + fm1, u = fm3 - T(4) * fm2 + T(3) * fm1;
+  T s0 = c13 * (t * t) + T(0.25) * (u * u);
+  t = fm2 - T(2) * fm1 + f0; u = fm2 - f0;
+  T s1 = c13 * (t * t) + T(0.25) * (u * u);
+  t = fm1 - T(2) * f0 + fp1; u = T(3) * fm1 - T(4) * f0 + fp1;
+  T s2 = c13 * (t * t) + T(0.25) * (u * u);
+  s0 = T(0.1) / ((eps + s0) * (eps + s0));
+  s1 = T(0.6) / ((eps + s1) * (eps + s1));
+  s2 = T(0.3) / ((eps + s2) * (eps + s2));
+  T sum = s0 + s1 + s2;
+  fl = (s0 / sum) * h0 + (s1 / sum) * h1 + (s2 / sum) * h2;
+  h0 = Div<T>::by(T(2) * fp2 - T(7) * fp1 + T(11) * f0, T(6));
+  h1 = Div<T>::by(-fp1 + T(5) * f0 + T(2) * fm1, T(6));
+  h2 = Div<T>::by(T(2) * f0 + T(5) * fm1 - fm2, T(6));
+  t = fp2 - T(2) * fp1 + f0; u = fp2 - T(4) * fp1 + T(3) * f0;
+  s0 = c13 * (t * t) + T(0.25) * (u * u);
+  t = fp1 - T(2) * f0 + fm1; u = fp1 - fm1;
+  s1 = c13 * (t * t) + T(0.25) * (u * u);
+  t = f0 - T(2) * fm1 + fm2; u = T(3) * f0 - T(4) * fm1 + fm2;
+  s2 = c13 * (t * t) + T(0.25) * (u * u);
+  s0 = T(0.1) / ((eps + s0) * (eps + s0));
+  s1 = T(0.6) / ((eps + s1) * (eps + s1));
+  s2 = T(0.3) / ((eps + s2) * (eps + s2));
+  sum = s0 + s1 + s2;
+  fr = (s0 / sum) * h0 + (s1 / sum) * h1 + (s2 / sum) * h2;
+}
+
+// minmod / median (mhd3d3.f90:1380-1403)
+template <typename T> __device__ __forceinline__ T minmod(T a, T b) {
+  return T(0.5) * (sgn1(a) + sgn1(b)) * mn(fab(a), fab(b));
+}
+// Monotonicity-preserving bound of MPWENO5 (mhd3d3.f90:1530-1591) for one
+// side; left state: (a3,a2,a1,b0,b1) = (fm3,fm2,fm1,f0,fp1), right state:
+// (fp2,fp1,f0,fm1,fm2).
+template <typename T>
+__device__ __forceinline__ T mp_side(T w, T a3, T a2, T a1, T b0, T b1, T alpha, T beta) {
+  T h0 = a3 - T(2) * a2 + a1;
+  T h1 = a2 - T(2) * a1 + b0;
+  T h2 = a1 - T(2) * b0 + b1;
+  T s1 = minmod(T(4) * h1 - h2, T(4) * h2 - h1);
+  T s2 = minmod(h1, h2);
+  T s0 = minmod(s1, s2);
+  T w1 = minmod(T(4) * h0 - h1, T(4) * h1 - h0);
+  T w2 = minmod(h0, h1);
+  T w0 = minmod(w1, w2);
+  s1 = a1 + alpha * (a1 - a2);
+  s2 = T(0.5) * (a1 + b0 - s0);
+  s0 = T(0.5) * (T(3) * a1 - a2) + Div<T>::by(beta * w0, T(3));
+  T lo = mx(mn(mn(a1, b0), s2), mn(mn(a1, s1), s0));
+  T hi = mn(mx(mx(a1, b0), s2), mx(mx(a1, s1), s0));
+  return w + minmod(lo - w, hi - w);
+}
+
+template <typename T>
+struct Prm {
+  T pdmb, eps, alpha, beta;
+  int tvd_shift;
+};
+
+// One-sided face states of f at the low face of element c along stride s
+// (reconstruct_3d for dirs 1-3, mhd3d3.f90:833-860).
+template <typename T, int RECON>
+__device__ __forceinline__ void recon_face(const T* __restrict__ f, long long c, long long s,
+                                           const Prm<T>& P, T& fl, T& fr) {
+  if (RECON == R_PDM) {
+    T a0 = f[c - 4 * s], a1 = f[c - 3 * s], a2 = f[c - 2 * s], a3 = f[c - s];
+    T a4 = f[c], a5 = f[c + s], a6 = f[c + 2 * s], a7 = f[c + 3 * s];
+    T fi = tap8(a0, a1, a2, a3, a4, a5, a6, a7);
+    pdm2(a2, a3, a4, a5, fi, P.pdmb, fl, fr);
+  } else if (RECON == R_TVD || RECON == R_TVDMC) {
+    T fm2 = f[c - 2 * s], fm1 = f[c - s], f0 = f[c], fp1 = f[c + s];
+    T fi = (fm1 + f0) / T(2);
+    tvd<T, RECON == R_TVDMC>(fm2, fm1, f0, fp1, fi, P.eps, fl, fr);
+  } else {
+    T fm3 = f[c - 3 * s], fm2 = f[c - 2 * s], fm1 = f[c - s], f0 = f[c], fp1 = f[c + s], fp2 = f[c + 2 * s];
+    weno5(fm3, fm2, fm1, f0, fp1, fp2, P.eps, fl, fr);
+    if (RECON == R_MPWENO) {
+      fl = mp_side(fl, fm3, fm2, fm1, f0, fp1, P.alpha, P.beta);
+      fr = mp_side(fr, fp2, fp1, f0, fm1, fm2, P.alpha, P.beta);
+    }
+  }
+}
+
+// WENO5/MPWENO5 pair on six values held in registers.
+template <typename T, int RECON>
+__device__ __forceinline__ void weno_vals(const T* a, const Prm<T>& P, T& fl, T& fr) {
+  weno5(a[0], a[1], a[2], a[3], a[4], a[5], P.eps, fl, fr);
+  if (RECON == R_MPWENO) {
+    fl = mp_side(fl, a[0], a[1], a[2], a[3], a[4], P.alpha, P.beta);
+    fr = mp_side(fr, a[5], a[4], a[3], a[2], a[1], P.alpha, P.beta);
+  }
+}
+
+// Limited corner value of v at the edge whose two transverse axes have
+// strides s1 (d1) and s2 (d2) and whose upper cell is c
+// (get_vav_center2corner, mhd3d3.f90:1858-2116).  Quadrant cell q_ab =
+// c - (1-a) s1 - (1-b) s2; v_ab_0 / v_ab_1 are the two one-sided estimates.
+template <typename T, int RECON>
+__device__ __forceinline__ T corner_vel(const T* __restrict__ v, long long c, long long s1, long long s2,
+                                        const Prm<T>& P) {
+  T v00_0, v00_1, v10_0, v10_1, v01_0, v01_1, v11_0, v11_1;
+  if (RECON == R_PDM) {
+    // interp2_pdm (926-989): 8-tap along d1 at the 8 d2-rows, then along d2
+    T g[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const T* r = v + c + (long long)(m - 4) * s2;
+      g[m] = tap8(r[-4 * s1], r[-3 * s1], r[-2 * s1], r[-s1], r[0], r[s1], r[2 * s1], r[3 * s1]);
+    }
+    T vi = tap8(g[0], g[1], g[2], g[3], g[4], g[5], g[6], g[7]);
+    T pd = P.pdmb;
+    pdm2(v[c - s2 - 2 * s1], v[c - s2 - s1], v[c - s2], v[c - s2 + s1], vi, pd, v00_0, v10_0);
+    pdm2(v[c - s1 - 2 * s2], v[c - s1 - s2], v[c - s1], v[c - s1 + s2], vi, pd, v00_1, v01_1);
+    pdm2(v[c - 2 * s2], v[c - s2], v[c], v[c + s2], vi, pd, v10_1, v11_1);
+    pdm2(v[c - 2 * s1], v[c - s1], v[c], v[c + s1], vi, pd, v01_0, v11_0);
+  } else if (RECON == R_TVD || RECON == R_TVDMC) {
+    // interp2_tvd (1037-1067) and TVD with (mhd3d2) or without (mhd3d3) shifts
+    constexpr bool MC = (RECON == R_TVDMC);
+    T vi = (v[c - s1 - s2] + v[c - s2] + v[c] + v[c - s1]) / T(4);
+    long long a = P.tvd_shift ? c - s2 : c;
+    long long b = P.tvd_shift ? c - s1 : c;
+    tvd<T, MC>(v[a - 2 * s1], v[a - s1], v[a], v[a + s1], vi, P.eps, v00_0, v10_0);
+    tvd<T, MC>(v[b - 2 * s2], v[b - s2], v[b], v[b + s2], vi, P.eps, v00_1, v01_1);
+    tvd<T, MC>(v[c - 2 * s2], v[c - s2], v[c], v[c + s2], vi, P.eps, v10_1, v11_1);
+    tvd<T, MC>(v[c - 2 * s1], v[c - s1], v[c], v[c + s1], vi, P.eps, v01_0, v11_0);
+  } else {
+    // WENO5 / MPWENO5 two-level reconstruction (1925-2049): "_1" = along d1
+    // then d2, "_0" = along d2 then d1, with the reference's output naming.
+    T L[6], R[6], a[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const T* r = v + c + (long long)(m - 3) * s2;
+#pragma unroll
+      for (int t = 0; t < 6; ++t) a[t] = r[(long long)(t - 3) * s1];
+      weno_vals<T, RECON>(a, P, L[m], R[m]);
+    }
+    weno_vals<T, RECON>(L, P, v00_1, v01_1);
+    weno_vals<T, RECON>(R, P, v10_1, v11_1);
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const T* r = v + c + (long long)(m - 3) * s1;
+#pragma unroll
+      for (int t = 0; t < 6; ++t) a[t] = r[(long long)(t - 3) * s2];
+      weno_vals<T, RECON>(a, P, L[m], R[m]);
+    }
+    weno_vals<T, RECON>(L, P, v00_0, v01_0);
+    weno_vals<T, RECON>(R, P, v10_0, v11_0);
+  }
+  // dif signs pick the smoother one-sided estimate per quadrant (2056-2106)
+  const long long q00 = c - s1 - s2, q10 = c - s2, q01 = c - s1, q11 = c;
+  T d00 = fab(v[q00 - s1] - v[q00]) - fab(v[q00 - s2] - v[q00]);
+  T d10 = fab(v[q10 + s1] - v[q10]) - fab(v[q10 - s2] - v[q10]);
+  T d01 = fab(v[q01 - s1] - v[q01]) - fab(v[q01 + s2] - v[q01]);
+  T d11 = fab(v[q11 + s1] - v[q11]) - fab(v[q11 + s2] - v[q11]);
+  T v00 = d00 >= T(0) ? v00_0 : v00_1;
+  T v10 = d10 >= T(0) ? v10_0 : v10_1;
+  T v01 = d01 >= T(0) ? v01_0 : v01_1;
+  T v11 = d11 >= T(0) ? v11_0 : v11_1;
+  return T(0.25) * (v00 + v01 + v10 + v11);
+}
+
+// ------------------------------------------------------------- small kernels
+template <typename T>
+__device__ __forceinline__ long long idx3(const Geom& g, int i, int j, int k) {
+  return (long long)i + (long long)g.px * ((long long)j + (long long)g.py * (long long)k);
+}
+
+// get_bxyz over all cells (incl. ghosts) and vf = |v| + |B|/sqrt(rho).
+template <typename T>
+__global__ void k_bxyz_vf(Dev<T> d, int want_vf) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int j = blockIdx.y * blockDim.y + threadIdx.y;
+  int k = blockIdx.z;
+  const Geom& g = d.g;
+  if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+  long long c = idx3<T>(g, i, j, k);
+  T bx = T(0.5) * (d.bi[c + 1] + d.bi[c]);
+  T by = T(0.5) * (d.bj[c + g.px] + d.bj[c]);
+  T bz = T(0.5) * (d.bk[c + g.plane] + d.bk[c]);
+  d.bx[c] = bx;
+  d.by[c] = by;
+  d.bz[c] = bz;
+  if (want_vf) {
+    T u = d.vx[c], v = d.vy[c], w = d.vz[c];
+    d.vf[c] = sq(u * u + v * v + w * w) + sq((bx * bx + by * by + bz * bz) / d.rho[c]);
+  }
+}
+
+// get_dt over all cells incl. ghosts: per-block min, then atomicMin on the
+// bit pattern (positive doubles order like their bits).  Status bits mirror
+// diag_rho_neg / diag_overflow.
+template <typename T>
+__global__ void k_cfl(Dev<T> d) {
+  const Geom& g = d.g;
+  long long n = (long long)g.nx * g.ny * g.nz;
+  double m = INFINITY;
+  unsigned st = 0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    int i = (int)(t % g.nx);
+    long long r = t / g.nx;
+    int j = (int)(r % g.ny);
+    int k = (int)(r / g.ny);
+    long long c = idx3<T>(g, i, j, k);
+    T r0 = d.rho[c], p0 = d.p[c], u = d.vx[c], v = d.vy[c], w = d.vz[c];
+    T a = d.bx[c], b = d.by[c], cc = d.bz[c];
+    T vv = sq(u * u + v * v + w * w);
+    T btot = sq(a * a + b * b + cc * cc);
+    T valf = btot / sq(r0);
+    T vs = sq(d.gam * p0 / r0);
+    T vcfl = vv + sq(valf * valf + vs * vs);
+    T dt = d.cfl / (vcfl / T(d.dx[i]) + vcfl / T(d.dy[j]) + vcfl / T(d.dz[k]));
+    double dtd = (double)dt;
+    m = (dtd < m) ? dtd : m;
+    if (isnan(r0) || isnan(p0) || isnan(u) || isnan(v) || isnan(w)) st |= ST_NAN;
+    if (r0 < T(0)) st |= ST_NEG_RHO;
+    if (p0 < T(0)) st |= ST_NEG_P;
+    if (isnan(dt)) st |= ST_NAN;
+  }
+  // warp then block reduction
+  for (int o = 16; o > 0; o >>= 1) {
+    double y = __shfl_xor_sync(0xffffffffu, m, o);
+    m = (y < m) ? y : m;
+    st |= __shfl_xor_sync(0xffffffffu, st, o);
+  }
+  __shared__ double sm[32];
+  __shared__ unsigned ss[32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { sm[wid] = m; ss[wid] = st; }
+  __syncthreads();
+  if (wid == 0) {
+    int nw = blockDim.x >> 5;
+    m = (lane < nw) ? sm[lane] : INFINITY;
+    st = (lane < nw) ? ss[lane] : 0u;
+    for (int o = 16; o > 0; o >>= 1) {
+      double y = __shfl_xor_sync(0xffffffffu, m, o);
+      m = (y < m) ? y : m;
+      st |= __shfl_xor_sync(0xffffffffu, st, o);
+    }
+    if (lane == 0) {
+      if (m >= 0.0) atomicMin(&d.sc->dtmin_bits, (unsigned long long)__double_as_longlong(m));
+      if (st) atomicOr(&d.sc->status, st);
+    }
+  }
+}
+
+// tau selection of step_ab (3609) / step_rk2,3 (3656-3661, 3723-3728).
+// mode 0: RK with fixed deck dt; 1: CFL dt every step; 2: AB (CFL dt and the
+// predictor coefficient tau/tau0/2, then tau0=tau).
+template <typename T>
+__global__ void k_cfl_final(Dev<T> d, int mode) {
+  Scal* s = d.sc;
+  double dt = __longlong_as_double((long long)s->dtmin_bits);
+  s->dtmin_bits = (unsigned long long)__double_as_longlong(INFINITY);
+  s->dt_cfl = dt;
+  if (mode == 0) {
+    if (dt < s->tau0) s->status |= ST_CFL;
+    s->tau = s->tau0;
+  } else if (mode == 1) {
+    s->tau = dt;
+    s->tau0 = dt;
+  } else if (mode == 2) {
+    s->tau = dt;
+    s->ab_coef = dt / s->tau0 / 2.0;
+    s->tau0 = dt;
+  }
+  // mode 3: read-only (diagnostics); tau untouched
+}
+
+// advance_previous for RK (3794-3819): U^n of the stage combines.
+template <typename T>
+__global__ void k_save_prev(Dev<T> d) {
+  long long n = d.g.vol;
+  T gm1 = d.gam - T(1);
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+       c += (long long)gridDim.x * blockDim.x) {
+    T r = d.rho[c], u = d.vx[c], v = d.vy[c], w = d.vz[c];
+    d.q[0][c] = r;
+    d.q[1][c] = r * u;
+    d.q[2][c] = r * v;
+    d.q[3][c] = r * w;
+    d.q[4][c] = T(0.5) * r * (u * u + v * v + w * w) + d.p[c] / gm1;
+    d.q[5][c] = d.bi[c];
+    d.q[6][c] = d.bj[c];
+    d.q[7][c] = d.bk[c];
+  }
+}
+
+// advance_predictor_ab (3821-3840): Xh = X + tau/tau0/2*(X-Xp), then Xp = X;
+// also vf of the predicted state.
+template <typename T>
+__global__ void k_predictor_ab(Dev<T> d) {
+  long long n = d.g.vol;
+  T cf = (T)d.sc->ab_coef;
+  T* x[11] = {d.rho, d.vx, d.vy, d.vz, d.p, d.bi, d.bj, d.bk, d.bx, d.by, d.bz};
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+       c += (long long)gridDim.x * blockDim.x) {
+    T hv[11];
+#pragma unroll
+    for (int a = 0; a < 11; ++a) {
+      T xv = x[a][c], xp = d.q[a][c];
+      hv[a] = xv + cf * (xv - xp);
+      d.h[a][c] = hv[a];
+      d.q[a][c] = xv;
+    }
+    T rr = hv[0];
+    d.vf[c] = (rr > T(0)) ? sq(hv[1] * hv[1] + hv[2] * hv[2] + hv[3] * hv[3]) +
+                                sq((hv[8] * hv[8] + hv[9] * hv[9] + hv[10] * hv[10]) / rr)
+                          : T(0);
+  }
+}
+
+// ------------------------------------------------------------------ fluxes
+// Gaussian-split fluxes and magnetic stress through the low face of cell c
+// along axis D (get_flux_stress, 2385-2560; get_v_face, 2594-2615).  Left
+// state uses the + moments, right state the - moments.
+template <typename T, int RECON, int D>
+__global__ void k_flux(Dev<T> d, Inp<T> in, Prm<T> P) {
+  const Geom& g = d.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x + g.ng;
+  int j = blockIdx.y * blockDim.y + threadIdx.y + g.ng;
+  int k = blockIdx.z + g.ng;
+  int ni = g.nx0 + (D == 0), nj = g.ny0 + (D == 1), nk = g.nz0 + (D == 2);
+  if (i >= g.ng + ni || j >= g.ng + nj || k >= g.ng + nk) return;
+  long long c = idx3<T>(g, i, j, k);
+  long long s = (D == 0) ? 1 : (D == 1) ? (long long)g.px : g.plane;
+  T rl, rr, ul, ur, vl, vr, wl, wr, pl, pr, xl, xr, yl, yr, zl, zr;
+  recon_face<T, RECON>(in.rho, c, s, P, rl, rr);
+  recon_face<T, RECON>(in.vx, c, s, P, ul, ur);
+  recon_face<T, RECON>(in.vy, c, s, P, vl, vr);
+  recon_face<T, RECON>(in.vz, c, s, P, wl, wr);
+  recon_face<T, RECON>(in.p, c, s, P, pl, pr);
+  recon_face<T, RECON>(in.bx, c, s, P, xl, xr);
+  recon_face<T, RECON>(in.by, c, s, P, yl, yr);
+  recon_face<T, RECON>(in.bz, c, s, P, zl, zr);
+  const T gm1 = d.gam - T(1);
+  const T rspi = sq(T(3.14159265358979323846));  // sqrt(pi)
+  T out[8];
+  // ---- left state, + moments
+  {
+    T vn = (D == 0) ? ul : (D == 1) ? vl : wl;
+    T bn = (D == 0) ? xl : (D == 1) ? yl : zl;
+    T leng = T(0.5) * rl * (ul * ul + vl * vl + wl * wl) + pl / gm1;
+    T lam = rl / (T(2) * pl);
+    T a = sq(lam);
+    T bb = T(0.5) * ex(-lam * (vn * vn)) / a / rspi;
+    T v0 = T(0.5) * erc(-a * vn);
+    T v1 = vn * v0 + bb;
+    out[0] = rl * v1;
+    out[1] = rl * ul * v1;
+    out[2] = rl * vl * v1;
+    out[3] = rl * wl * v1;
+    out[4] = (leng + T(0.5) * pl) * v1;
+    out[1 + D] = out[1 + D] + pl * v0;
+    out[4] = out[4] + T(0.5) * pl * vn * v0;
+    T lbsq = xl * xl + yl * yl + zl * zl;
+    lam = rl / (T(2) * pl + lbsq);
+    a = sq(lam);
+    v0 = T(0.5) * erc(-a * vn);
+    out[5] = ((D == 0) ? (T(0.5) * lbsq - xl * xl) : (-xl * bn)) * v0;
+    out[6] = ((D == 1) ? (T(0.5) * lbsq - yl * yl) : (-yl * bn)) * v0;
+    out[7] = ((D == 2) ? (T(0.5) * lbsq - zl * zl) : (-zl * bn)) * v0;
+  }
+  // ---- right state, - moments
+  {
+    T vn = (D == 0) ? ur : (D == 1) ? vr : wr;
+    T bn = (D == 0) ? xr : (D == 1) ? yr : zr;
+    T leng = T(0.5) * rr * (ur * ur + vr * vr + wr * wr) + pr / gm1;
+    T lam = rr / (T(2) * pr);
+    T a = sq(lam);
+    T bb = T(0.5) * ex(-lam * (vn * vn)) / a / rspi;
+    T v0 = T(0.5) * erc(a * vn);
+    T v1 = vn * v0 - bb;
+    T f0 = rr * v1;
+    T f1 = rr * ur * v1;
+    T f2 = rr * vr * v1;
+    T f3 = rr * wr * v1;
+    T f4 = (leng + T(0.5) * pr) * v1;
+    if (D == 0) f1 = f1 + pr * v0;
+    if (D == 1) f2 = f2 + pr * v0;
+    if (D == 2) f3 = f3 + pr * v0;
+    f4 = f4 + T(0.5) * pr * vn * v0;
+    T lbsq = xr * xr + yr * yr + zr * zr;
+    lam = rr / (T(2) * pr + lbsq);
+    a = sq(lam);
+    v0 = T(0.5) * erc(a * vn);
+    T s5 = ((D == 0) ? (T(0.5) * lbsq - xr * xr) : (-xr * bn)) * v0;
+    T s6 = ((D == 1) ? (T(0.5) * lbsq - yr * yr) : (-yr * bn)) * v0;
+    T s7 = ((D == 2) ? (T(0.5) * lbsq - zr * zr) : (-zr * bn)) * v0;
+    out[0] = out[0] + f0;
+    out[1] = out[1] + f1;
+    out[2] = out[2] + f2;
+    out[3] = out[3] + f3;
+    out[4] = out[4] + f4;
+    out[5] = out[5] + s5;
+    out[6] = out[6] + s6;
+    out[7] = out[7] + s7;
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) d.F[D][q][c] = out[q];
+}
+
+// -------------------------------------------------------------------- EMF
+// Edge EMF of family E (0: ei along x, 1: ej along y, 2: ek along z) at the
+// edge whose upper cell is c (get_eijk_LFM, 1754-1856).  a1 = E+1, a2 = E+2
+// (cyclic): v1 = v_a1, v2 = v_a2; b1 = B_a1 reconstructed along a2 and
+// upwinded by sign(v2); b2 = B_a2 reconstructed along a1, upwinded by sign(v1).
+template <typename T, int RECON, int E>
+__global__ void k_emf(Dev<T> d, Inp<T> in, Prm<T> P) {
+  const Geom& g = d.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x + g.ng;
+  int j = blockIdx.y * blockDim.y + threadIdx.y + g.ng;
+  int k = blockIdx.z + g.ng;
+  int ni = g.nx0 + (E != 0), nj = g.ny0 + (E != 1), nk = g.nz0 + (E != 2);
+  if (i >= g.ng + ni || j >= g.ng + nj || k >= g.ng + nk) return;
+  long long c = idx3<T>(g, i, j, k);
+  const long long st[3] = {1, (long long)g.px, g.plane};
+  constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
+  const long long s1 = st[A1], s2 = st[A2];
+  const T* vel[3] = {in.vx, in.vy, in.vz};
+  const T* fb[3] = {in.bi, in.bj, in.bk};
+  T v1av = corner_vel<T, RECON>(vel[A1], c, s1, s2, P);
+  T v2av = corner_vel<T, RECON>(vel[A2], c, s1, s2, P);
+  T b1l, b1r, b2l, b2r;
+  recon_face<T, RECON>(fb[A1], c, s2, P, b1l, b1r);
+  recon_face<T, RECON>(fb[A2], c, s1, P, b2l, b2r);
+  T b1u = (v2av >= T(0)) ? b1l : b1r;
+  T b2u = (v1av >= T(0)) ? b2l : b2r;
+  T e = -v1av * b2u + v2av * b1u;
+  const T* vf = d.vf;
+  T eta = T(0.25) * (vf[c - s1 - s2] + vf[c - s2] + vf[c] + vf[c - s1]);
+  e = e + eta * (b1l + b2r - b1r - b2l);
+  d.E[E][c] = e;
+}
+
+// ------------------------------------------------------------------ update
+// get_conserve + advance_corrector1 + stage combine + p + advance_corrector2 +
+// combine + v (RK: 3666-3697 / 3736-3783; AB: 3616, 3626-3627), interior cells.
+template <typename T>
+__device__ __forceinline__ T comb(int form, T c, T xp, T x, T den) {
+  if (form == 0) return (xp + x) / den;
+  if (form == 1) return (c * xp + x) / den;
+  return (xp + c * x) / den;
+}
+
+template <typename T>
+__global__ void k_update_hydro(Dev<T> d, int form, T cw, T den) {
+  const Geom& g = d.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x + g.ng;
+  int j = blockIdx.y * blockDim.y + threadIdx.y + g.ng;
+  int k = blockIdx.z + g.ng;
+  if (i >= g.ng + g.nx0 || j >= g.ng + g.ny0 || k >= g.ng + g.nz0) return;
+  long long c = idx3<T>(g, i, j, k);
+  const long long sy = g.px, sz = g.plane;
+  const T tau = (T)d.sc->tau;
+  const T dx = (T)d.dx[i], dy = (T)d.dy[j], dz = (T)d.dz[k];
+  const T gm1 = d.gam - T(1);
+  T r = d.rho[c], u = d.vx[c], v = d.vy[c], w = d.vz[c], pr = d.p[c];
+  // get_conserve (1641-1650)
+  T rho0 = r, rvx0 = r * u, rvy0 = r * v, rvz0 = r * w;
+  T eng0 = T(0.5) * r * (u * u + v * v + w * w) + pr / gm1;
+  T dv[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+    dv[q] = (d.F[0][q][c + 1] - d.F[0][q][c]) / dx + (d.F[1][q][c + sy] - d.F[1][q][c]) / dy +
+            (d.F[2][q][c + sz] - d.F[2][q][c]) / dz;
+  // advance_corrector1 (3842-3878)
+  T rho1 = rho0 - tau * dv[0];
+  T eng1 = eng0 - tau * dv[4];
+  T rx = rvx0 - tau * dv[1], ry = rvy0 - tau * dv[2], rz = rvz0 - tau * dv[3];
+  T hx = rx, hy = ry, hz = rz;
+  if (form >= 0) {
+    rho1 = comb(form, cw, d.q[0][c], rho1, den);
+    hx = comb(form, cw, d.q[1][c], rx, den);
+    hy = comb(form, cw, d.q[2][c], ry, den);
+    hz = comb(form, cw, d.q[3][c], rz, den);
+    eng1 = comb(form, cw, d.q[4][c], eng1, den);
+  }
+  T pn = gm1 * (eng1 - T(0.5) * (hx * hx + hy * hy + hz * hz) / rho1);
+  // advance_corrector2 (3880-3907): magnetic stress on the pre-combine momentum
+  rx = rx - tau * dv[5];
+  ry = ry - tau * dv[6];
+  rz = rz - tau * dv[7];
+  if (form >= 0) {
+    rx = comb(form, cw, d.q[1][c], rx, den);
+    ry = comb(form, cw, d.q[2][c], ry, den);
+    rz = comb(form, cw, d.q[3][c], rz, den);
+  }
+  d.rho[c] = rho1;
+  d.p[c] = pn;
+  d.vx[c] = rx / rho1;
+  d.vy[c] = ry / rho1;
+  d.vz[c] = rz / rho1;
+}
+
+// advance_bijk (3909-3933) + B combine, interior faces of all three arrays.
+template <typename T>
+__global__ void k_update_b(Dev<T> d, int form, T cw, T den) {
+  const Geom& g = d.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x + g.ng;
+  int j = blockIdx.y * blockDim.y + threadIdx.y + g.ng;
+  int k = blockIdx.z + g.ng;
+  if (i > g.ng + g.nx0 || j > g.ng + g.ny0 || k > g.ng + g.nz0) return;
+  bool in_x = i < g.ng + g.nx0, in_y = j < g.ng + g.ny0, in_z = k < g.ng + g.nz0;
+  long long c = idx3<T>(g, i, j, k);
+  const long long sy = g.px, sz = g.plane;
+  const T tau = (T)d.sc->tau;
+  const T dx = (T)d.dx[i], dy = (T)d.dy[j], dz = (T)d.dz[k];
+  const T *ei = d.E[0], *ej = d.E[1], *ek = d.E[2];
+  if (in_y && in_z) {
+    T b = d.bi[c] - tau * ((ek[c + sy] - ek[c]) / dy - (ej[c + sz] - ej[c]) / dz);
+    if (form >= 0) b = comb(form, cw, d.q[5][c], b, den);
+    d.bi[c] = b;
+  }
+  if (in_x && in_z) {
+    T b = d.bj[c] - tau * ((ei[c + sz] - ei[c]) / dz - (ek[c + 1] - ek[c]) / dx);
+    if (form >= 0) b = comb(form, cw, d.q[6][c], b, den);
+    d.bj[c] = b;
+  }
+  if (in_x && in_y) {
+    T b = d.bk[c] - tau * ((ej[c + 1] - ej[c]) / dx - (ei[c + sy] - ei[c]) / dy);
+    if (form >= 0) b = comb(form, cw, d.q[7][c], b, den);
+    d.bk[c] = b;
+  }
+}
+
+// ------------------------------------------------------------------- fill
+// Single-device replacement of fill_hydro_mpi / fill_mag_mpi (781-819): every
+// ghost element takes the value of its per-axis image (the x, y, z passes of
+// the reference compose to exactly this, since each pass reads only interior
+// values along its own axis).  Cell axes: interior [ng, ng+n0); the face
+// array's own axis: interior [ng, ng+n0].
+__device__ __forceinline__ int ghost_src(int x, int ng, int n0, bool face, int kind, bool& flip) {
+  flip = false;
+  int hi = face ? ng + n0 : ng + n0 - 1;  // last interior index
+  if (x >= ng && x <= hi) return x;
+  bool lo = x < ng;
+  if (kind == BC_PERIODIC) return lo ? x + n0 : x - n0;
+  if (kind == BC_OUTFLOW) return lo ? ng : hi;
+  flip = true;  // mirror: even (flip ignored) or odd
+  if (!face) return lo ? 2 * ng - 1 - x : 2 * n0 + 2 * ng - 1 - x;
+  return lo ? 2 * ng - x : 2 * n0 + 2 * ng - x;
+}
+
+template <typename T>
+__global__ void k_fill(Dev<T> d) {
+  const Geom& g = d.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int j = blockIdx.y * blockDim.y + threadIdx.y;
+  int k = blockIdx.z;
+  if (i > g.nx || j > g.ny || k > g.nz) return;
+  T* arr[8] = {d.rho, d.vx, d.vy, d.vz, d.p, d.bi, d.bj, d.bk};
+  const int n0[3] = {g.nx0, g.ny0, g.nz0};
+  const int x3[3] = {i, j, k};
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    int fa = a - 5;  // own staggering axis of bi/bj/bk
+    bool ghost = false, inside = true;
+    int s3[3];
+    T sgn = T(1);
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      bool face = (fa == ax);
+      int ext = (ax == 0 ? g.nx : ax == 1 ? g.ny : g.nz) + (face ? 1 : 0);
+      if (x3[ax] >= ext) inside = false;
+      bool flip;
+      s3[ax] = ghost_src(x3[ax], g.ng, n0[ax], face, d.bc[ax], flip);
+      if (s3[ax] != x3[ax]) ghost = true;
+      // reflecting wall: the normal velocity is odd (a = 1,2,3 -> vx,vy,vz)
+      if (flip && d.bc[ax] == BC_REFLECT && a == 1 + ax) sgn = -sgn;
+    }
+    if (!inside || !ghost) continue;
+    long long c = idx3<T>(g, i, j, k);
+    long long s = idx3<T>(g, s3[0], s3[1], s3[2]);
+    T val = arr[a][s];
+    arr[a][c] = (sgn > T(0)) ? val : -val;
+  }
+}
+
+// ------------------------------------------------------------ diagnostics
+// Double-double (Neumaier/TwoSum) accumulation of mass and energy, max |div B|
+// (FP64), min rho incl. ghosts.  Deterministic: fixed per-thread order,
+// fixed tree; partial results per block reduced by one block in order.
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
+  s = a + b;
+  double bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+struct DD { double s, c; };
+__device__ __forceinline__ DD dd_add(DD x, DD y) {
+  double s, e;
+  two_sum(x.s, y.s, s, e);
+  e += x.c + y.c;
+  double s2, e2;
+  two_sum(s, e, s2, e2);
+  return DD{s2, e2};
+}
+
+template <typename T>
+__global__ void k_diag_partial(Dev<T> d, double* part) {
+  const Geom& g = d.g;
+  long long n = (long long)g.nx0 * g.ny0 * g.nz0;
+  DD ms{0, 0}, es{0, 0};
+  double dmax = 0.0;
+  const double gm1 = (double)d.gam - 1.0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    int i = (int)(t % g.nx0) + g.ng;
+    long long r = t / g.nx0;
+    int j = (int)(r % g.ny0) + g.ng;
+    int k = (int)(r / g.ny0) + g.ng;
+    long long c = idx3<T>(g, i, j, k);
+    double dv = d.dx[i] * d.dy[j] * d.dz[k];
+    double rr = d.rho[c], u = d.vx[c], v = d.vy[c], w = d.vz[c], pp = d.p[c];
+    double a = d.bx[c], b = d.by[c], cc = d.bz[c];
+    ms = dd_add(ms, DD{rr * dv, 0.0});
+    double e = 0.5 * rr * (u * u + v * v + w * w) + pp / gm1 + 0.5 * (a * a + b * b + cc * cc);
+    es = dd_add(es, DD{e * dv, 0.0});
+    double db = ((double)d.bi[c + 1] - (double)d.bi[c]) / d.dx[i] +
+                ((double)d.bj[c + g.px] - (double)d.bj[c]) / d.dy[j] +
+                ((double)d.bk[c + g.plane] - (double)d.bk[c]) / d.dz[k];
+    db = fabs(db);
+    dmax = db > dmax ? db : dmax;
+  }
+  __shared__ double sh[5][256];
+  int tid = threadIdx.x;
+  sh[0][tid] = ms.s; sh[1][tid] = ms.c; sh[2][tid] = es.s; sh[3][tid] = es.c; sh[4][tid] = dmax;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (tid < w) {
+      DD a = dd_add(DD{sh[0][tid], sh[1][tid]}, DD{sh[0][tid + w], sh[1][tid + w]});
+      DD b = dd_add(DD{sh[2][tid], sh[3][tid]}, DD{sh[2][tid + w], sh[3][tid + w]});
+      sh[0][tid] = a.s; sh[1][tid] = a.c; sh[2][tid] = b.s; sh[3][tid] = b.c;
+      sh[4][tid] = sh[4][tid] > sh[4][tid + w] ? sh[4][tid] : sh[4][tid + w];
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    double* o = part + 5 * blockIdx.x;
+    o[0] = sh[0][0]; o[1] = sh[1][0]; o[2] = sh[2][0]; o[3] = sh[3][0]; o[4] = sh[4][0];
+  }
+}
+
+template <typename T>
+__global__ void k_diag_final(Dev<T> d, const double* part, int nb, double* out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  DD m{0, 0}, e{0, 0};
+  double dm = 0;
+  for (int b = 0; b < nb; ++b) {
+    const double* o = part + 5 * b;
+    m = dd_add(m, DD{o[0], o[1]});
+    e = dd_add(e, DD{o[2], o[3]});
+    dm = o[4] > dm ? o[4] : dm;
+  }
+  out[0] = m.s + m.c;
+  out[1] = e.s + e.c;
+  out[2] = dm;
+}
+
+template <typename T>
+__global__ void k_min_rho(Dev<T> d, double* out) {
+  const Geom& g = d.g;
+  long long n = (long long)g.nx * g.ny * g.nz;
+  double m = INFINITY;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    int i = (int)(t % g.nx);
+    long long r = t / g.nx;
+    int j = (int)(r % g.ny);
+    int k = (int)(r / g.ny);
+    double v = d.rho[idx3<T>(g, i, j, k)];
+    m = v < m ? v : m;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    double y = __shfl_xor_sync(0xffffffffu, m, o);
+    m = y < m ? y : m;
+  }
+  __shared__ double sm[32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sm[wid] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = sm[w] < m ? sm[w] : m;
+    m = sm[0] < m ? sm[0] : m;
+    // single block launch: plain store
+    out[3] = m;
+  }
+}
+
+// ---------------------------------------------------------------- launchers
+inline dim3 grid3(int ni, int nj, int nk, dim3 b) {
+  return dim3((ni + b.x - 1) / b.x, (nj + b.y - 1) / b.y, nk);
+}
+
+template <typename T>
+Prm<T> prm_of(const Dev<T>& d) {
+  Prm<T> P;
+  P.pdmb = d.pdmb; P.eps = d.eps; P.alpha = d.alpha; P.beta = d.beta; P.tvd_shift = d.tvd_shift;
+  return P;
+}
+
+template <typename T>
+void Launch<T>::bxyz_vf(const Dev<T>& d, bool want_vf, cudaStream_t st) {
+  dim3 b(64, 4, 1);
+  k_bxyz_vf<T><<<grid3(d.g.nx, d.g.ny, d.g.nz, b), b, 0, st>>>(d, want_vf ? 1 : 0);
+}
+
+template <typename T>
+void Launch<T>::cfl(const Dev<T>& d, int mode, cudaStream_t st) {
+  k_cfl<T><<<152 * 4, 256, 0, st>>>(d);
+  k_cfl_final<T><<<1, 1, 0, st>>>(d, mode);
+}
+
+template <typename T>
+void Launch<T>::save_prev(const Dev<T>& d, cudaStream_t st) {
+  k_save_prev<T><<<152 * 8, 256, 0, st>>>(d);
+}
+
+template <typename T>
+void Launch<T>::predictor_ab(const Dev<T>& d, cudaStream_t st) {
+  k_predictor_ab<T><<<152 * 8, 256, 0, st>>>(d);
+}
+
+template <typename T, int RECON>
+void flux_r(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
+  Prm<T> P = prm_of(d);
+  dim3 b(32, 4, 1);
+  const Geom& g = d.g;
+  k_flux<T, RECON, 0><<<grid3(g.nx0 + 1, g.ny0, g.nz0, b), b, 0, st>>>(d, in, P);
+  k_flux<T, RECON, 1><<<grid3(g.nx0, g.ny0 + 1, g.nz0, b), b, 0, st>>>(d, in, P);
+  k_flux<T, RECON, 2><<<grid3(g.nx0, g.ny0, g.nz0 + 1, b), b, 0, st>>>(d, in, P);
+}
+
+template <typename T>
+void Launch<T>::fluxes(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
+  switch (d.recon) {
+    case R_PDM: flux_r<T, R_PDM>(d, in, st); break;
+    case R_TVD: flux_r<T, R_TVD>(d, in, st); break;
+    case R_WENO: flux_r<T, R_WENO>(d, in, st); break;
+    case R_MPWENO: flux_r<T, R_MPWENO>(d, in, st); break;
+    default: flux_r<T, R_TVDMC>(d, in, st); break;
+  }
+}
+
+template <typename T, int RECON>
+void emf_r(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
+  Prm<T> P = prm_of(d);
+  dim3 b(32, 4, 1);
+  const Geom& g = d.g;
+  k_emf<T, RECON, 0><<<grid3(g.nx0, g.ny0 + 1, g.nz0 + 1, b), b, 0, st>>>(d, in, P);
+  k_emf<T, RECON, 1><<<grid3(g.nx0 + 1, g.ny0, g.nz0 + 1, b), b, 0, st>>>(d, in, P);
+  k_emf<T, RECON, 2><<<grid3(g.nx0 + 1, g.ny0 + 1, g.nz0, b), b, 0, st>>>(d, in, P);
+}
+
+template <typename T>
+void Launch<T>::emf(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
+  switch (d.recon) {
+    case R_PDM: emf_r<T, R_PDM>(d, in, st); break;
+    case R_TVD: emf_r<T, R_TVD>(d, in, st); break;
+    case R_WENO: emf_r<T, R_WENO>(d, in, st); break;
+    case R_MPWENO: emf_r<T, R_MPWENO>(d, in, st); break;
+    default: emf_r<T, R_TVDMC>(d, in, st); break;
+  }
+}
+
+template <typename T>
+void Launch<T>::update(const Dev<T>& d, int form, double c, double den, cudaStream_t st) {
+  dim3 b(32, 4, 1);
+  const Geom& g = d.g;
+  k_update_hydro<T><<<grid3(g.nx0, g.ny0, g.nz0, b), b, 0, st>>>(d, form, (T)c, (T)den);
+  k_update_b<T><<<grid3(g.nx0 + 1, g.ny0 + 1, g.nz0 + 1, b), b, 0, st>>>(d, form, (T)c, (T)den);
+}
+
+template <typename T>
+void Launch<T>::fill(const Dev<T>& d, cudaStream_t st) {
+  dim3 b(64, 4, 1);
+  k_fill<T><<<grid3(d.g.nx + 1, d.g.ny + 1, d.g.nz + 1, b), b, 0, st>>>(d);
+}
+
+template <typename T>
+void Launch<T>::diagnostics(const Dev<T>& d, double* out, cudaStream_t st) {
+  // out: device buffer of 5 + 5*nb doubles; out[4] (CFL dt) is filled by the caller
+  const int nb = 152 * 2;
+  double* part = out + 8;
+  k_diag_partial<T><<<nb, 256, 0, st>>>(d, part);
+  k_diag_final<T><<<1, 1, 0, st>>>(d, part, nb, out);
+  k_min_rho<T><<<1, 1024, 0, st>>>(d, out);
+}
+
+}  // namespace mhd

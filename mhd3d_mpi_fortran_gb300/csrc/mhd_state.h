@@ -1,0 +1,78 @@
+// Device-side state of one solver handle and the launcher interface shared by
+// the precision-specific translation units (mhd_fp32.cu, mhd_fp64.cu) and the
+// C-ABI layer (mhd_api.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mhd {
+
+// Ghost-inclusive grid.  Cell arrays have (nx,ny,nz) elements, face arrays one
+// more along their own axis; every array of a handle uses the same padded
+// strides, element (i,j,k) (0-based, ghost-inclusive) at i + px*(j + py*k).
+// The face at the low side of cell c along an axis is stored at index c, as
+// are the flux through it and, for edges, the edge at the low sides of c.
+struct Geom {
+  int nx0, ny0, nz0;   // interior cells
+  int ng, nord;        // ghost layers, nord = 2*ng
+  int nx, ny, nz;      // cells incl. ghosts (nx0 + nord)
+  int px, py, pz;      // strides: px >= nx+1 (multiple of 32), py = ny+1, pz = nz+1
+  long long plane;     // px*py
+  long long vol;       // plane*pz
+};
+
+// Scalars that live on the device so that a step never waits on the host.
+struct Scal {
+  double tau;                    // dt of the current step (module `tau`)
+  double tau0;                   // previous dt (AB) / fixed deck dt (RK)
+  double dt_cfl;                 // last CFL dt (get_dt)
+  double ab_coef;                // tau/tau0/2 of advance_predictor_ab
+  unsigned long long dtmin_bits; // running min of the CFL reduction (+inf between steps)
+  unsigned int status;           // MHD_ST_* bits
+  unsigned int pad;
+};
+
+template <typename T>
+struct Dev {
+  Geom g;
+  int recon, stepop, tvd_shift, dt_mode;
+  int bc[3];
+  T gam, pdmb, eps, alpha, beta, cfl;
+  // state of the current level
+  T *rho, *vx, *vy, *vz, *p, *bi, *bj, *bk, *bx, *by, *bz;
+  // previous level: RK {rho, rvx, rvy, rvz, eng, bi, bj, bk};
+  //                 AB {rho, vx, vy, vz, p, bi, bj, bk, bx, by, bz}
+  T* q[11];
+  // AB predicted half step {rho, vx, vy, vz, p, bi, bj, bk, bx, by, bz}
+  T* h[11];
+  T* F[3][8];  // face fluxes [axis][rho, rvx, rvy, rvz, eng, s_x, s_y, s_z]
+  T* E[3];     // edge EMFs ei, ej, ek
+  T* vf;       // |v| + |B|/sqrt(rho) of the stage input
+  const double *dx, *dy, *dz;  // FP64 cell widths (ghost-inclusive, 1-D)
+  Scal* sc;
+  unsigned int* partial;       // per-block scratch of the CFL reduction
+  unsigned int* counter;
+};
+
+// Stage-input view: which arrays feed the EMF and flux kernels (RK: the
+// state; AB: the predicted half step, mhd3d3.f90:3622-3624).
+template <typename T>
+struct Inp {
+  const T *rho, *vx, *vy, *vz, *p, *bx, *by, *bz, *bi, *bj, *bk;
+};
+
+template <typename T>
+struct Launch {
+  static void bxyz_vf(const Dev<T>& d, bool want_vf, cudaStream_t st);
+  static void cfl(const Dev<T>& d, int mode, cudaStream_t st);  // mode: 0 RK fixed, 1 CFL, 2 AB
+  static void save_prev(const Dev<T>& d, cudaStream_t st);
+  static void predictor_ab(const Dev<T>& d, cudaStream_t st);
+  static void fluxes(const Dev<T>& d, const Inp<T>& in, cudaStream_t st);
+  static void emf(const Dev<T>& d, const Inp<T>& in, cudaStream_t st);
+  // form: -1 none (stage 1 / AB), 0 (Xp+X)/den, 1 (c*Xp+X)/den, 2 (Xp+c*X)/den
+  static void update(const Dev<T>& d, int form, double c, double den, cudaStream_t st);
+  static void fill(const Dev<T>& d, cudaStream_t st);
+  static void diagnostics(const Dev<T>& d, double* out5_dev, cudaStream_t st);
+};
+
+}  // namespace mhd

@@ -1,0 +1,149 @@
+"""Host-side mirror of the reference's step interface over the C ABI.
+
+``MHDSolver`` is what a Python driver (or a test) uses in place of the
+reference's module state + ``call step``:
+
+    s = MHDSolver(params, state)      # end of initialization (mhd3d3.f90:3327-3377)
+    tau, status = s.step()            # call step (mhd3d3.f90:3286)
+    fields = s.fetch()                # arrays read by outputxyz / diag_* (3091-3109, 3143-3160)
+    s.close()                         # termination (3936-3943)
+
+All arrays are FP64, Fortran order, ghost-inclusive, exactly the reference's
+module arrays.  The work runs in ``libmhdgpu.so`` on the current CUDA device;
+there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .abi import Params, check
+from .ics import State
+
+_DP = C.POINTER(C.c_double)
+
+
+def _ptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags["F_CONTIGUOUS"], "FP64 Fortran-order array required"
+    return a.ctypes.data_as(_DP)
+
+
+def _f64(a) -> np.ndarray:
+    return np.asfortranarray(np.asarray(a, dtype=np.float64))
+
+
+class MHDSolver:
+    def __init__(self, params: Params, state: State, dx=None, dy=None, dz=None, lib=None):
+        self.lib = lib or abi.load()
+        self.params = params
+        g = state.grid
+        self._keep = [_f64(a) for a in state.arrays()]
+        self._geo = [_f64(g.dx if dx is None else dx), _f64(g.dy if dy is None else dy),
+                     _f64(g.dz if dz is None else dz)]
+        self._cp = params.to_c()
+        h = C.c_void_p()
+        rc = self.lib.mhd_init(C.byref(self._cp), *[_ptr(a) for a in self._keep],
+                               *[_ptr(a) for a in self._geo], C.byref(h))
+        check(self.lib, rc, "mhd_init")
+        self.h = h
+        self._keep = None
+
+    # -- stepping -------------------------------------------------------
+    def step(self, n: int = 1, graph: bool = False):
+        tau = C.c_double()
+        st = C.c_uint32()
+        fn = self.lib.mhd_step_graph if graph else self.lib.mhd_step_n
+        rc = fn(self.h, int(n), C.byref(tau), C.byref(st))
+        check(self.lib, rc, "mhd_step")
+        return tau.value, st.value
+
+    def step_async(self, n: int = 1):
+        """Enqueue n steps without waiting (no tau/status readback)."""
+        rc = self.lib.mhd_step_n(self.h, int(n), None, None)
+        check(self.lib, rc, "mhd_step_n")
+
+    def time_steps(self, n: int, graph: bool = False) -> float:
+        """Device time (ms) of n steps between CUDA events on the solver's stream."""
+        ms = C.c_float()
+        rc = self.lib.mhd_time_steps(self.h, int(n), 1 if graph else 0, C.byref(ms))
+        check(self.lib, rc, "mhd_time_steps")
+        return ms.value
+
+    def set_tau(self, tau: float):
+        check(self.lib, self.lib.mhd_set_tau(self.h, float(tau)), "mhd_set_tau")
+
+    def set_profiling(self, on: bool):
+        check(self.lib, self.lib.mhd_set_profiling(self.h, 1 if on else 0), "mhd_set_profiling")
+
+    def timings(self):
+        out = (C.c_float * 5)()
+        check(self.lib, self.lib.mhd_last_timings(self.h, out), "mhd_last_timings")
+        return dict(zip(("fluxes", "emf", "update", "fill", "dt"), list(out)))
+
+    # -- readback -------------------------------------------------------
+    def fetch(self) -> dict:
+        nx, ny, nz = self.params.shape
+        cs = (nx, ny, nz)
+        out = {k: np.zeros(cs, order="F") for k in ("rho", "vx", "vy", "vz", "p", "bx", "by", "bz")}
+        out["bi"] = np.zeros((nx + 1, ny, nz), order="F")
+        out["bj"] = np.zeros((nx, ny + 1, nz), order="F")
+        out["bk"] = np.zeros((nx, ny, nz + 1), order="F")
+        names = ("rho", "vx", "vy", "vz", "p", "bx", "by", "bz", "bi", "bj", "bk")
+        rc = self.lib.mhd_fetch(self.h, *[_ptr(out[k]) for k in names])
+        check(self.lib, rc, "mhd_fetch")
+        return out
+
+    def diagnostics(self) -> dict:
+        out = (C.c_double * 5)()
+        check(self.lib, self.lib.mhd_diagnostics(self.h, out), "mhd_diagnostics")
+        return dict(zip(("mass", "energy", "divb_max", "rho_min", "dt_cfl"), list(out)))
+
+    def debug_fluxes(self) -> list:
+        p = self.params
+        sizes = [(p.nx0 + (d == 0), p.ny0 + (d == 1), p.nz0 + (d == 2)) for d in range(3)]
+        n = sum(8 * int(np.prod(s)) for s in sizes)
+        buf = np.zeros(n)
+        check(self.lib, self.lib.mhd_debug_fluxes(self.h, buf.ctypes.data_as(_DP)), "mhd_debug_fluxes")
+        out, off = [], 0
+        for s in sizes:
+            m = int(np.prod(s))
+            out.append([buf[off + q * m: off + (q + 1) * m].reshape(s, order="F") for q in range(8)])
+            off += 8 * m
+        return out
+
+    def debug_emf(self):
+        p = self.params
+        sh = [(p.nx0 + (e != 0), p.ny0 + (e != 1), p.nz0 + (e != 2)) for e in range(3)]
+        es = [np.zeros(s, order="F") for s in sh]
+        check(self.lib, self.lib.mhd_debug_emf(self.h, *[_ptr(a) for a in es]), "mhd_debug_emf")
+        return es
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mhd_free(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def ensemble_step(solvers: list, nsteps: int) -> int:
+    """Advance independent grids together (one CUDA graph, one branch per grid)."""
+    lib = solvers[0].lib
+    arr = (C.c_void_p * len(solvers))(*[s.h.value for s in solvers])
+    st = C.c_uint32()
+    check(lib, lib.mhd_ensemble_step(arr, len(solvers), int(nsteps), C.byref(st)), "mhd_ensemble_step")
+    return st.value

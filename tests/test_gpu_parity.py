@@ -1,0 +1,204 @@
+"""GPU parity: libmhdgpu.so (through the C ABI) against the CPU oracle.
+
+FP64 mode follows the reference's expression order with no FMA, so kernel
+outputs agree with the oracle to a few ulps (only exp/erfc differ: CUDA vs
+glibc).  Tolerances are written per test.  FP32 mode is checked against the
+FP64 solution with an error budget, as the production path.
+"""
+import numpy as np
+import pytest
+
+from mhd3d_mpi_fortran_gb300 import ics, MHDSolver, ensemble_step
+from mhd3d_mpi_fortran_gb300.abi import (Params, BC_PERIODIC, BC_EVEN, BC_REFLECT, BC_OUTFLOW,
+                                         STEP_AB2, STEP_RK2, STEP_RK3, FP32, FP64, ST_NAN, ST_NEG_RHO,
+                                         DT_CFL)
+from oracle.oracle import OracleSolver
+
+pytestmark = pytest.mark.gpu
+
+RECONS = [1, 2, 3, 4, 5]
+FIELDS = ("rho", "vx", "vy", "vz", "p", "bx", "by", "bz", "bi", "bj", "bk")
+
+
+def rand_state(nx0, ny0, nz0, seed=0, nord=8):
+    """Smooth waves plus a density/pressure jump and random face B."""
+    g = ics.grid(nx0, ny0, nz0, nord=nord)
+    s = ics.empty_state(g)
+    rng = np.random.default_rng(seed)
+    xc, yc, zc = [c.reshape(sh) for c, sh in zip(g.centres(), ((-1, 1, 1), (1, -1, 1), (1, 1, -1)))]
+    s.rho[...] = 1.0 + 0.3 * np.sin(2 * np.pi * xc) * np.cos(2 * np.pi * yc) + 0.5 * (zc > 0.5)
+    s.p[...] = 0.8 + 0.2 * np.cos(2 * np.pi * (xc + zc)) + 0.4 * (xc > 0.6)
+    s.vx[...] = 0.4 * np.sin(2 * np.pi * yc) + 0.05 * rng.standard_normal(s.vx.shape)
+    s.vy[...] = -0.3 * np.sin(2 * np.pi * zc) + 0.05 * rng.standard_normal(s.vy.shape)
+    s.vz[...] = 0.2 * np.cos(2 * np.pi * xc) + 0.05 * rng.standard_normal(s.vz.shape)
+    for a in (s.bi, s.bj, s.bk):
+        a[...] = 0.3 * rng.standard_normal(a.shape)
+    return s
+
+
+def relmax(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def rel_l2(a, b):
+    return np.sqrt(np.sum((a - b) ** 2)) / max(np.sqrt(np.sum(b ** 2)), 1e-300)
+
+
+@pytest.mark.parametrize("recon", RECONS)
+def test_fluxes_fp64_match_oracle(recon):
+    s = rand_state(12, 10, 9, seed=recon)
+    prm = Params(12, 10, 9, reconop=recon, tau=1e-3)
+    with MHDSolver(prm, s) as gpu:
+        fg = gpu.debug_fluxes()
+    fo = OracleSolver(prm, s).fluxes()
+    for d in range(3):
+        for q in range(8):
+            assert relmax(fg[d][q], fo[d][q]) <= 1e-13, (d, q)
+
+
+@pytest.mark.parametrize("recon", RECONS)
+@pytest.mark.parametrize("shift", [0, 1])
+def test_emf_fp64_match_oracle(recon, shift):
+    if shift and recon not in (2, 5):
+        pytest.skip("stencil shifts only differ for TVD")
+    s = rand_state(11, 12, 10, seed=10 + recon)
+    prm = Params(11, 12, 10, reconop=recon, tvd_shift=shift, tau=1e-3)
+    with MHDSolver(prm, s) as gpu:
+        eg = gpu.debug_emf()
+    eo = OracleSolver(prm, s).emf()
+    for e in range(3):
+        assert relmax(eg[e], eo[e]) <= 1e-13, e
+
+
+@pytest.mark.parametrize("recon", RECONS)
+@pytest.mark.parametrize("stepop", [STEP_AB2, STEP_RK2, STEP_RK3])
+def test_steps_fp64_match_oracle(recon, stepop):
+    s = ics.orszag_tang_3d(12, seed=recon, ny0=10, nz0=9)
+    prm = Params(12, 10, 9, reconop=recon, stepop=stepop, tau=0.5 * ics.cfl_dt(s),
+                 nord=8)
+    with MHDSolver(prm, s) as gpu:
+        tg, sg = gpu.step(4)
+        fg = gpu.fetch()
+    o = OracleSolver(prm, s)
+    to, so = o.step(4)
+    fo = o.fetch()
+    assert tg == pytest.approx(to, rel=1e-13)
+    assert sg == so
+    for k in FIELDS:
+        assert relmax(fg[k], fo[k]) <= 1e-11, k
+
+
+@pytest.mark.parametrize("kind", [BC_EVEN, BC_REFLECT, BC_OUTFLOW])
+def test_boundary_kinds_fp64(kind):
+    s = ics.blast(12)
+    prm = Params(12, 12, 12, bc=(kind,) * 3, tau=0.5 * ics.cfl_dt(s))
+    with MHDSolver(prm, s) as gpu:
+        gpu.step(5)
+        fg = gpu.fetch()
+    o = OracleSolver(prm, s)
+    o.step(5)
+    fo = o.fetch()
+    for k in FIELDS:
+        assert relmax(fg[k], fo[k]) <= 1e-11, k
+
+
+def test_cfl_dt_mode_and_diagnostics():
+    s = ics.turbulence(16, seed=4)
+    prm = Params(16, 16, 16, dt_mode=DT_CFL, tau=1.0)
+    with MHDSolver(prm, s) as gpu:
+        dg0 = gpu.diagnostics()
+        tg, _ = gpu.step(3)
+        dg = gpu.diagnostics()
+    o = OracleSolver(prm, s)
+    do0 = o.diagnostics()
+    to, _ = o.step(3)
+    do = o.diagnostics()
+    assert dg0["dt_cfl"] == pytest.approx(do0["dt_cfl"], rel=1e-14)
+    assert tg == pytest.approx(to, rel=1e-12)
+    assert dg["mass"] == pytest.approx(do["mass"], rel=1e-13)
+    assert dg["energy"] == pytest.approx(do["energy"], rel=1e-12)
+    assert dg["divb_max"] <= 1e-12 and do["divb_max"] <= 1e-12
+    assert dg["rho_min"] == pytest.approx(do["rho_min"], rel=1e-12)
+
+
+@pytest.mark.slow
+def test_whole_step_parity_64cubed_100_steps():
+    """All-FP64 mode vs the oracle: 64^3 periodic 3-D Orszag-Tang, PDM + RK2,
+    fixed tau = the CFL-0.3 dt of the initial state, 100 steps: relative L2
+    <= 1e-10 per field and div B <= 1e-12."""
+    s = ics.orszag_tang_3d(64, seed=0)
+    prm = Params(64, 64, 64, reconop=1, stepop=STEP_RK2, cfl=0.3, tau=ics.cfl_dt(s, cfl=0.3))
+    with MHDSolver(prm, s) as gpu:
+        gpu.step(100)
+        fg = gpu.fetch()
+        dg = gpu.diagnostics()
+    o = OracleSolver(prm, s)
+    o.step(100)
+    fo = o.fetch()
+    for k in FIELDS:
+        assert rel_l2(fg[k], fo[k]) <= 1e-10, k
+    assert dg["divb_max"] <= 1e-12
+
+
+def test_fp32_error_budget_vs_fp64():
+    s = ics.orszag_tang_3d(32, seed=0)
+    tau = ics.cfl_dt(s)
+    res = {}
+    for prec in (FP64, FP32):
+        with MHDSolver(Params(32, 32, 32, precision=prec, tau=tau), s) as gpu:
+            gpu.step(20)
+            res[prec] = gpu.fetch()
+            if prec == FP32:
+                d32 = gpu.diagnostics()
+    for k in ("rho", "p", "vx", "bi"):
+        a, b = res[FP32][k], res[FP64][k]
+        l1 = np.abs(a - b).sum() / np.abs(b).sum()
+        assert l1 <= 1e-5, (k, l1)
+    # CT keeps div B at FP32 round-off
+    assert d32["divb_max"] <= 1e-4
+
+
+def test_graph_replay_equals_stream_fp64():
+    s = ics.orszag_tang_3d(16, seed=2)
+    prm = Params(16, 16, 16, tau=0.5 * ics.cfl_dt(s))
+    with MHDSolver(prm, s) as a, MHDSolver(prm, s) as b:
+        a.step(6)
+        b.step(3, graph=True)
+        b.step(3, graph=True)
+        fa, fb = a.fetch(), b.fetch()
+    for k in FIELDS:
+        assert np.array_equal(fa[k], fb[k]), k
+
+
+def test_ensemble_equals_sequential_fp64():
+    sizes = (12, 16, 8)
+    states = [ics.orszag_tang_3d(n, seed=i, amp=0.5 + 0.25 * i) for i, n in enumerate(sizes)]
+    prms = [Params(n, n, n, tau=0.5 * ics.cfl_dt(st)) for n, st in zip(sizes, states)]
+    seq = []
+    for prm, st in zip(prms, states):
+        with MHDSolver(prm, st) as g:
+            g.step(3)
+            seq.append(g.fetch())
+    ens = [MHDSolver(p, st) for p, st in zip(prms, states)]
+    ensemble_step(ens, 3)
+    for e, ref in zip(ens, seq):
+        got = e.fetch()
+        for k in FIELDS:
+            assert np.array_equal(got[k], ref[k]), k
+        e.close()
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32])
+def test_status_bits_from_poisoned_input(prec):
+    base = ics.orszag_tang_3d(8)
+    tau = 0.5 * ics.cfl_dt(base)
+    s = ics.orszag_tang_3d(8)
+    s.rho[6, 6, 6] = np.nan
+    with MHDSolver(Params(8, 8, 8, precision=prec, tau=tau), s) as g:
+        _, st = g.step(1)
+    assert st & ST_NAN
+    s = ics.orszag_tang_3d(8)
+    s.rho[6, 6, 6] = -1.0
+    with MHDSolver(Params(8, 8, 8, precision=prec, tau=tau), s) as g:
+        _, st = g.step(1)
+    assert st & ST_NEG_RHO
