@@ -126,9 +126,10 @@ int mhd_set_tau(void* handle, double tau);
 /* Per-launch-family timing: when on, mhd_step_n brackets every launch family
  * with CUDA events on the handle's stream (no extra synchronisation);
  * mhd_last_timings then returns the summed device time of the last
- * mhd_step_n call in ms: [fluxes, emf, update, fill+bxyz, dt(+save/predict)]. */
+ * mhd_step_n call in ms: [x fluxes, y fluxes, z fluxes + conserved update,
+ * emf, face-B update, fill + bxyz, dt (+ save / predictor), unused]. */
 int mhd_set_profiling(void* handle, int32_t on);
-int mhd_last_timings(void* handle, float out_ms[5]);
+int mhd_last_timings(void* handle, float out_ms[8]);
 
 /* Enqueue nsteps (graph-replayed when use_graph != 0) between two CUDA events
  * recorded on the handle's stream; *ms = their elapsed device time. */

@@ -59,11 +59,14 @@ struct Handle {
   Dev<float> df{};
   Dev<double> dd{};
   bool profile = false;
-  float tms[5] = {0, 0, 0, 0, 0};
+  float tms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   cudaEvent_t ev[16] = {};
   std::vector<cudaEvent_t> pool;
   std::vector<int> fam;
-  std::map<int, cudaGraphExec_t> graphs;
+  int par = 0;                 // which half of the double-buffered primitives is current
+  float* geoT = nullptr;       // FP32 copy of the cell widths
+  // graphs keyed by (nsteps, starting parity) -> (exec, parity after replay)
+  std::map<std::pair<int, int>, std::pair<cudaGraphExec_t, int>> graphs;
 };
 
 size_t round_up(size_t a, size_t b) { return (a + b - 1) / b * b; }
@@ -103,7 +106,8 @@ Inp<T> half_inp(const Dev<T>& d) {
 
 // Launch-family recorder: in profile mode every family is bracketed by a pair
 // of CUDA events on the stream (no synchronisation); pairs are resolved after
-// the call.  Families: 0 fluxes, 1 emf, 2 update, 3 fill+bxyz, 4 dt/save/predict.
+// the call.  Families: 0 x fluxes, 1 y fluxes (+x divergence), 2 z fluxes +
+// conserved update, 3 emf, 4 ct (face B), 5 fill+bxyz, 6 dt/save/predict.
 struct Rec {
   Handle* h = nullptr;
   cudaStream_t st = nullptr;
@@ -128,25 +132,54 @@ struct Rec {
 };
 
 template <typename T>
-void enqueue_step(Handle* h, const Dev<T>& d, cudaStream_t st, Rec* r = nullptr) {
+Dev<T>& dev(Handle* h);
+template <>
+Dev<float>& dev<float>(Handle* h) { return h->df; }
+template <>
+Dev<double>& dev<double>(Handle* h) { return h->dd; }
+
+// The handle's Dev with the current half of the primitive buffers in front.
+template <typename T>
+Dev<T> at_par(const Dev<T>& base, int par) {
+  Dev<T> d = base;
+  if (par) {
+    std::swap(d.rho, d.orho);
+    std::swap(d.vx, d.ovx);
+    std::swap(d.vy, d.ovy);
+    std::swap(d.vz, d.ovz);
+    std::swap(d.p, d.op);
+  }
+  return d;
+}
+
+template <typename T>
+void enqueue_step(Handle* h, int& par, cudaStream_t st, Rec* r = nullptr) {
   Rec none;
   Rec& R = r ? *r : none;
+  const Dev<T>& base = dev<T>(h);
   const mhd_params& p = h->prm;
   if (p.stepop == MHD_STEP_AB2) {
-    R.begin(); Launch<T>::cfl(d, 2, st); Launch<T>::predictor_ab(d, st); R.end(4);
+    Dev<T> d = at_par(base, par);
+    R.begin(); Launch<T>::cfl(d, 2, st); Launch<T>::predictor_ab(d, st); R.end(6);
     Inp<T> in = half_inp(d);
-    R.begin(); Launch<T>::emf(d, in, st); R.end(1);
-    R.begin(); Launch<T>::fluxes(d, in, st); R.end(0);
-    R.begin(); Launch<T>::update(d, -1, 0.0, 1.0, st); R.end(2);
-    R.begin(); Launch<T>::fill(d, st); Launch<T>::bxyz_vf(d, false, st); R.end(3);
+    R.begin(); Launch<T>::emf(d, in, st); R.end(3);
+    for (int part = 0; part < 3; ++part) {
+      R.begin(); Launch<T>::hydro(d, in, part, -1, 0.0, 1.0, true, st); R.end(part);
+    }
+    R.begin(); Launch<T>::ct(d, -1, 0.0, 1.0, st); R.end(4);
+    par ^= 1;
+    d = at_par(base, par);
+    R.begin(); Launch<T>::fill(d, st); Launch<T>::bxyz_vf(d, false, st); R.end(5);
     return;
   }
-  R.begin();
-  Launch<T>::cfl(d, p.dt_mode == MHD_DT_CFL ? 1 : 0, st);
-  Launch<T>::save_prev(d, st);
-  R.end(4);
+  {
+    Dev<T> d = at_par(base, par);
+    R.begin();
+    Launch<T>::cfl(d, p.dt_mode == MHD_DT_CFL ? 1 : 0, st);
+    Launch<T>::save_prev(d, st);
+    R.end(6);
+  }
   int nst = (p.stepop == MHD_STEP_RK2) ? 2 : 3;
-  Inp<T> in = state_inp(d);
   for (int s = 1; s <= nst; ++s) {
     int form = -1;
     double c = 0.0, den = 1.0;
@@ -155,11 +188,25 @@ void enqueue_step(Handle* h, const Dev<T>& d, cudaStream_t st, Rec* r = nullptr)
       else if (s == 2) { form = 1; c = 3.0; den = 4.0; }
       else { form = 2; c = 2.0; den = 3.0; }
     }
-    R.begin(); Launch<T>::emf(d, in, st); R.end(1);
-    R.begin(); Launch<T>::fluxes(d, in, st); R.end(0);
-    R.begin(); Launch<T>::update(d, form, c, den, st); R.end(2);
-    R.begin(); Launch<T>::fill(d, st); Launch<T>::bxyz_vf(d, true, st); R.end(3);
+    Dev<T> d = at_par(base, par);
+    Inp<T> in = state_inp(d);
+    R.begin(); Launch<T>::emf(d, in, st); R.end(3);
+    for (int part = 0; part < 3; ++part) {
+      R.begin(); Launch<T>::hydro(d, in, part, form, c, den, false, st); R.end(part);
+    }
+    R.begin(); Launch<T>::ct(d, form, c, den, st); R.end(4);
+    par ^= 1;
+    d = at_par(base, par);
+    R.begin(); Launch<T>::fill(d, st); Launch<T>::bxyz_vf(d, true, st); R.end(5);
   }
+}
+
+inline void set_widths(Handle* h, Dev<double>& d) {
+  d.wx = d.dx; d.wy = d.dy; d.wz = d.dz;
+}
+inline void set_widths(Handle* h, Dev<float>& d) {
+  const Geom& g = h->g;
+  d.wx = h->geoT; d.wy = h->geoT + g.nx; d.wz = h->geoT + g.nx + g.ny;
 }
 
 template <typename T>
@@ -178,6 +225,8 @@ void carve(Handle* h, Dev<T>& d, char* base) {
   d.alpha = (T)h->prm.alpha; d.beta = (T)h->prm.beta; d.cfl = (T)h->prm.cfl;
   d.rho = next(); d.vx = next(); d.vy = next(); d.vz = next(); d.p = next();
   d.bi = next(); d.bj = next(); d.bk = next(); d.bx = next(); d.by = next(); d.bz = next();
+  d.orho = next(); d.ovx = next(); d.ovy = next(); d.ovz = next(); d.op = next();
+  for (int q = 0; q < 8; ++q) d.dU[q] = next();
   int nq = (h->prm.stepop == MHD_STEP_AB2) ? 11 : 8;
   for (int i = 0; i < 11; ++i) d.q[i] = (i < nq) ? next() : nullptr;
   for (int i = 0; i < 11; ++i) d.h[i] = (h->prm.stepop == MHD_STEP_AB2) ? next() : nullptr;
@@ -186,13 +235,14 @@ void carve(Handle* h, Dev<T>& d, char* base) {
   for (int e = 0; e < 3; ++e) d.E[e] = next();
   d.vf = next();
   d.dx = h->geo; d.dy = h->geo + g.nx; d.dz = h->geo + g.nx + g.ny;
+  set_widths(h, d);
   d.sc = h->sc;
   d.partial = nullptr;
   d.counter = nullptr;
 }
 
 size_t n_arrays(const mhd_params& p) {
-  size_t n = 11 + ((p.stepop == MHD_STEP_AB2) ? 22 : 8) + 24 + 3 + 1;
+  size_t n = 11 + 5 + 8 + ((p.stepop == MHD_STEP_AB2) ? 22 : 8) + 24 + 3 + 1;
   return n;
 }
 
@@ -215,13 +265,6 @@ void unpack(const Geom& g, const T* src, int ex, int ey, int ez, double* dst) {
       for (int i = 0; i < ex; ++i) d[i] = (double)s[i];
     }
 }
-
-template <typename T>
-Dev<T>& dev(Handle* h);
-template <>
-Dev<float>& dev<float>(Handle* h) { return h->df; }
-template <>
-Dev<double>& dev<double>(Handle* h) { return h->dd; }
 
 template <typename T>
 int upload(Handle* h, const double* const* arrs) {
@@ -265,13 +308,12 @@ int init_device(Handle* h) {
 
 template <typename T>
 int do_steps(Handle* h, int n) {
-  Dev<T>& d = dev<T>(h);
   if (h->profile) {
-    for (int i = 0; i < 5; ++i) h->tms[i] = 0;
+    for (int i = 0; i < 8; ++i) h->tms[i] = 0;
     Rec r;
     r.h = h; r.st = h->st; r.pool = &h->pool; r.fam = &h->fam;
     h->fam.clear();
-    for (int s = 0; s < n; ++s) enqueue_step<T>(h, d, h->st, &r);
+    for (int s = 0; s < n; ++s) enqueue_step<T>(h, h->par, h->st, &r);
     CK(cudaGetLastError());
     int rc = wait_stream(h);
     if (rc) return rc;
@@ -282,7 +324,7 @@ int do_steps(Handle* h, int n) {
     }
     return MHD_OK;
   }
-  for (int s = 0; s < n; ++s) enqueue_step<T>(h, d, h->st);
+  for (int s = 0; s < n; ++s) enqueue_step<T>(h, h->par, h->st);
   CK(cudaGetLastError());
   return MHD_OK;
 }
@@ -375,6 +417,12 @@ int mhd_init(const mhd_params* prm, const double* rho, const double* vx, const d
     if (!(v > 0.0)) return bail(MHD_E_ARG, "cell widths must be positive (diag_geom)");
   if (cudaMemcpy(h->geo, geo.data(), sizeof(double) * geo.size(), cudaMemcpyHostToDevice) != cudaSuccess)
     return bail(MHD_E_CUDA, "geometry upload failed");
+  {
+    std::vector<float> gf(geo.begin(), geo.end());
+    if (cudaMalloc(&h->geoT, sizeof(float) * gf.size()) != cudaSuccess ||
+        cudaMemcpy(h->geoT, gf.data(), sizeof(float) * gf.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+      return bail(MHD_E_NOMEM, "geometry upload failed");
+  }
   Scal s{};
   s.tau = prm->tau;
   s.tau0 = prm->tau;
@@ -426,22 +474,26 @@ int mhd_step_graph(void* handle, int32_t nsteps, double* tau_out, uint32_t* stat
 }
 
 static int graph_for(Handle* h, int nsteps, cudaGraphExec_t* out) {
-  auto it = h->graphs.find(nsteps);
+  auto key = std::make_pair(nsteps, h->par);
+  auto it = h->graphs.find(key);
   if (it != h->graphs.end()) {
-    *out = it->second;
+    *out = it->second.first;
+    h->par = it->second.second;  // the replay leaves this half current
     return MHD_OK;
   }
   cudaGraph_t gr;
   cudaGraphExec_t ex;
+  int par = h->par;
   CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
   for (int s = 0; s < nsteps; ++s) {
-    if (h->fp32) enqueue_step<float>(h, h->df, h->st);
-    else enqueue_step<double>(h, h->dd, h->st);
+    if (h->fp32) enqueue_step<float>(h, par, h->st);
+    else enqueue_step<double>(h, par, h->st);
   }
   CK(cudaStreamEndCapture(h->st, &gr));
   CK(cudaGraphInstantiate(&ex, gr, 0));
   cudaGraphDestroy(gr);
-  h->graphs[nsteps] = ex;
+  h->graphs[key] = std::make_pair(ex, par);
+  h->par = par;
   *out = ex;
   return MHD_OK;
 }
@@ -488,17 +540,17 @@ int mhd_set_profiling(void* handle, int32_t on) {
   return MHD_OK;
 }
 
-int mhd_last_timings(void* handle, float out_ms[5]) {
+int mhd_last_timings(void* handle, float out_ms[8]) {
   Handle* h = (Handle*)handle;
   if (!h || !out_ms) return fail(MHD_E_ARG, "null argument");
-  for (int i = 0; i < 5; ++i) out_ms[i] = h->tms[i];
+  for (int i = 0; i < 8; ++i) out_ms[i] = h->tms[i];
   return MHD_OK;
 }
 
 template <typename T>
 static int fetch_t(Handle* h, double* const* outs) {
   const Geom& g = h->g;
-  Dev<T>& d = dev<T>(h);
+  Dev<T> d = at_par(dev<T>(h), h->par);
   const T* srcs[11] = {d.rho, d.vx, d.vy, d.vz, d.p, d.bx, d.by, d.bz, d.bi, d.bj, d.bk};
   int ext[11][3];
   for (int a = 0; a < 8; ++a) { ext[a][0] = g.nx; ext[a][1] = g.ny; ext[a][2] = g.nz; }
@@ -529,7 +581,7 @@ int mhd_fetch(void* handle, double* rho, double* vx, double* vy, double* vz, dou
 
 template <typename T>
 static int diag_t(Handle* h, double out[5]) {
-  Dev<T>& d = dev<T>(h);
+  Dev<T> d = at_par(dev<T>(h), h->par);
   Launch<T>::diagnostics(d, h->diag, h->st);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(h->diag_h, h->diag, sizeof(double) * 4, cudaMemcpyDeviceToHost, h->st));
@@ -554,7 +606,7 @@ int mhd_diagnostics(void* handle, double out[5]) {
 template <typename T>
 static int dbg_flux_t(Handle* h, double* out) {
   const Geom& g = h->g;
-  Dev<T>& d = dev<T>(h);
+  Dev<T> d = at_par(dev<T>(h), h->par);
   Launch<T>::fluxes(d, state_inp(d), h->st);
   CK(cudaGetLastError());
   std::vector<T> host((size_t)g.vol);
@@ -585,7 +637,7 @@ int mhd_debug_fluxes(void* handle, double* out) {
 template <typename T>
 static int dbg_emf_t(Handle* h, double* const* outs) {
   const Geom& g = h->g;
-  Dev<T>& d = dev<T>(h);
+  Dev<T> d = at_par(dev<T>(h), h->par);
   Launch<T>::bxyz_vf(d, true, h->st);
   Launch<T>::emf(d, state_inp(d), h->st);
   CK(cudaGetLastError());
@@ -622,9 +674,17 @@ int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* 
     if (!h) return fail(MHD_E_ARG, "null handle in ensemble");
     if (h->fp32 != h0->fp32) return fail(MHD_E_ARG, "ensemble grids must share the precision");
   }
-  static thread_local std::map<std::vector<void*>, std::pair<int, cudaGraphExec_t>> cache;
-  std::vector<void*> key(handles, handles + ngrids);
-  key.push_back((void*)(intptr_t)nsteps);
+  struct Entry {
+    cudaGraphExec_t ex;
+    std::vector<int> par_end;
+  };
+  static thread_local std::map<std::vector<intptr_t>, Entry> cache;
+  std::vector<intptr_t> key;
+  for (int i = 0; i < ngrids; ++i) {
+    key.push_back((intptr_t)handles[i]);
+    key.push_back(((Handle*)handles[i])->par);
+  }
+  key.push_back(nsteps);
   cudaGraphExec_t ex = nullptr;
   auto it = cache.find(key);
   if (it == cache.end()) {
@@ -637,12 +697,15 @@ int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* 
       Handle* h = (Handle*)handles[i];
       CK(cudaStreamWaitEvent(h->st, fork, 0));
     }
+    std::vector<int> pars(ngrids);
     for (int i = 0; i < ngrids; ++i) {
       Handle* h = (Handle*)handles[i];
+      int par = h->par;
       for (int s = 0; s < nsteps; ++s) {
-        if (h->fp32) enqueue_step<float>(h, h->df, h->st);
-        else enqueue_step<double>(h, h->dd, h->st);
+        if (h->fp32) enqueue_step<float>(h, par, h->st);
+        else enqueue_step<double>(h, par, h->st);
       }
+      pars[i] = par;
       if (i > 0) {
         CK(cudaEventCreateWithFlags(&joins[i], cudaEventDisableTiming));
         CK(cudaEventRecord(joins[i], h->st));
@@ -655,10 +718,11 @@ int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* 
     cudaGraphDestroy(gr);
     for (int i = 1; i < ngrids; ++i) cudaEventDestroy(joins[i]);
     cudaEventDestroy(fork);
-    cache[key] = {nsteps, ex};
-  } else {
-    ex = it->second.second;
+    cache[key] = Entry{ex, pars};
+    it = cache.find(key);
   }
+  ex = it->second.ex;
+  for (int i = 0; i < ngrids; ++i) ((Handle*)handles[i])->par = it->second.par_end[i];
   CK(cudaGraphLaunch(ex, h0->st));
   uint32_t acc = 0;
   for (int i = 0; i < ngrids; ++i) {
@@ -676,12 +740,13 @@ int mhd_free(void* handle) {
   Handle* h = (Handle*)handle;
   if (!h) return MHD_OK;
   if (h->st) cudaStreamSynchronize(h->st);
-  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second.first);
   for (int i = 0; i < 16; ++i)
     if (h->ev[i]) cudaEventDestroy(h->ev[i]);
   for (cudaEvent_t e : h->pool) cudaEventDestroy(e);
   if (h->buf) cudaFree(h->buf);
   if (h->geo) cudaFree(h->geo);
+  if (h->geoT) cudaFree(h->geoT);
   if (h->sc) cudaFree(h->sc);
   if (h->diag) cudaFree(h->diag);
   if (h->sc_h) cudaFreeHost(h->sc_h);

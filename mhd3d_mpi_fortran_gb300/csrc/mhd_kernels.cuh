@@ -8,10 +8,12 @@
 //   get_dt   (1608-1639) + diag_rho_neg/diag_overflow (3143-3160) -> k_cfl, k_cfl_final
 //   advance_previous (3794-3819)                                  -> k_save_prev
 //   advance_predictor_ab (3821-3840)                              -> k_predictor_ab
-//   get_flux_stress + get_v_face + reconstruct_3d (2385-2615, 833-1596) -> k_flux
+//   get_flux_stress + get_v_face + reconstruct_3d (2385-2615, 833-1596)
+//     -> k_flux (x faces), k_flux_t<D=1> (y faces, x+y divergence),
+//        k_flux_t<D=2> (z faces + the conserved update below)
 //   get_eijk_LFM + get_vav_center2corner + interp2_* (1754-2116, 926-1067) -> k_emf
 //   get_conserve + advance_corrector1/2 + RK combines (1641-1650, 3842-3907,
-//     3670-3697, 3741-3783)                                       -> k_update_hydro
+//     3670-3697, 3741-3783)                                       -> k_flux_t<D=2>
 //   advance_bijk + B combines (3909-3933, 3698-3702, 3784-3788)   -> k_update_b
 //   fill_hydro_mpi / fill_mag_mpi (781-819, 346-616)              -> k_fill
 #pragma once
@@ -198,6 +200,30 @@ __device__ __forceinline__ void weno_vals(const T* a, const Prm<T>& P, T& fl, T&
   }
 }
 
+// PDM part of get_vav_center2corner (mhd3d3.f90:1901-1905, 2056-2108) for
+// an edge with upper cell c and transverse strides s1 (d1), s2 (d2), given
+// the corner interpolant vi: the four shifted PDM2 limiters, the quadrant
+// choice by the sign of dif and the 4-quadrant mean.  v may point to global
+// or shared memory.
+template <typename T, typename I>
+__device__ __forceinline__ T corner_pdm(const T* __restrict__ v, I c, I s1, I s2, T vi, T pd) {
+  T v00_0, v00_1, v10_0, v10_1, v01_0, v01_1, v11_0, v11_1;
+  pdm2(v[c - s2 - 2 * s1], v[c - s2 - s1], v[c - s2], v[c - s2 + s1], vi, pd, v00_0, v10_0);
+  pdm2(v[c - s1 - 2 * s2], v[c - s1 - s2], v[c - s1], v[c - s1 + s2], vi, pd, v00_1, v01_1);
+  pdm2(v[c - 2 * s2], v[c - s2], v[c], v[c + s2], vi, pd, v10_1, v11_1);
+  pdm2(v[c - 2 * s1], v[c - s1], v[c], v[c + s1], vi, pd, v01_0, v11_0);
+  const I q00 = c - s1 - s2, q10 = c - s2, q01 = c - s1, q11 = c;
+  T d00 = fab(v[q00 - s1] - v[q00]) - fab(v[q00 - s2] - v[q00]);
+  T d10 = fab(v[q10 + s1] - v[q10]) - fab(v[q10 - s2] - v[q10]);
+  T d01 = fab(v[q01 - s1] - v[q01]) - fab(v[q01 + s2] - v[q01]);
+  T d11 = fab(v[q11 + s1] - v[q11]) - fab(v[q11 + s2] - v[q11]);
+  T v00 = d00 >= T(0) ? v00_0 : v00_1;
+  T v10 = d10 >= T(0) ? v10_0 : v10_1;
+  T v01 = d01 >= T(0) ? v01_0 : v01_1;
+  T v11 = d11 >= T(0) ? v11_0 : v11_1;
+  return T(0.25) * (v00 + v01 + v10 + v11);
+}
+
 // Limited corner value of v at the edge whose two transverse axes have
 // strides s1 (d1) and s2 (d2) and whose upper cell is c
 // (get_vav_center2corner, mhd3d3.f90:1858-2116).  Quadrant cell q_ab =
@@ -215,11 +241,7 @@ __device__ __forceinline__ T corner_vel(const T* __restrict__ v, long long c, lo
       g[m] = tap8(r[-4 * s1], r[-3 * s1], r[-2 * s1], r[-s1], r[0], r[s1], r[2 * s1], r[3 * s1]);
     }
     T vi = tap8(g[0], g[1], g[2], g[3], g[4], g[5], g[6], g[7]);
-    T pd = P.pdmb;
-    pdm2(v[c - s2 - 2 * s1], v[c - s2 - s1], v[c - s2], v[c - s2 + s1], vi, pd, v00_0, v10_0);
-    pdm2(v[c - s1 - 2 * s2], v[c - s1 - s2], v[c - s1], v[c - s1 + s2], vi, pd, v00_1, v01_1);
-    pdm2(v[c - 2 * s2], v[c - s2], v[c], v[c + s2], vi, pd, v10_1, v11_1);
-    pdm2(v[c - 2 * s1], v[c - s1], v[c], v[c + s1], vi, pd, v01_0, v11_0);
+    return corner_pdm(v, c, s1, s2, vi, P.pdmb);
   } else if (RECON == R_TVD || RECON == R_TVDMC) {
     // interp2_tvd (1037-1067) and TVD with (mhd3d2) or without (mhd3d3) shifts
     constexpr bool MC = (RECON == R_TVDMC);
@@ -316,7 +338,7 @@ __global__ void k_cfl(Dev<T> d) {
     T valf = btot / sq(r0);
     T vs = sq(d.gam * p0 / r0);
     T vcfl = vv + sq(valf * valf + vs * vs);
-    T dt = d.cfl / (vcfl / T(d.dx[i]) + vcfl / T(d.dy[j]) + vcfl / T(d.dz[k]));
+    T dt = d.cfl / (vcfl / d.wx[i] + vcfl / d.wy[j] + vcfl / d.wz[k]);
     double dtd = (double)dt;
     m = (dtd < m) ? dtd : m;
     if (isnan(r0) || isnan(p0) || isnan(u) || isnan(v) || isnan(w)) st |= ST_NAN;
@@ -418,41 +440,84 @@ __global__ void k_predictor_ab(Dev<T> d) {
 }
 
 // ------------------------------------------------------------------ fluxes
-// Gaussian-split fluxes and magnetic stress through the low face of cell c
-// along axis D (get_flux_stress, 2385-2560; get_v_face, 2594-2615).  Left
-// state uses the + moments, right state the - moments.
-template <typename T, int RECON, int D>
-__global__ void k_flux(Dev<T> d, Inp<T> in, Prm<T> P) {
-  const Geom& g = d.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + g.ng;
-  int j = blockIdx.y * blockDim.y + threadIdx.y + g.ng;
-  int k = blockIdx.z + g.ng;
-  int ni = g.nx0 + (D == 0), nj = g.ny0 + (D == 1), nk = g.nz0 + (D == 2);
-  if (i >= g.ng + ni || j >= g.ng + nj || k >= g.ng + nk) return;
-  long long c = idx3<T>(g, i, j, k);
-  long long s = (D == 0) ? 1 : (D == 1) ? (long long)g.px : g.plane;
-  T rl, rr, ul, ur, vl, vr, wl, wr, pl, pr, xl, xr, yl, yr, zl, zr;
-  recon_face<T, RECON>(in.rho, c, s, P, rl, rr);
-  recon_face<T, RECON>(in.vx, c, s, P, ul, ur);
-  recon_face<T, RECON>(in.vy, c, s, P, vl, vr);
-  recon_face<T, RECON>(in.vz, c, s, P, wl, wr);
-  recon_face<T, RECON>(in.p, c, s, P, pl, pr);
-  recon_face<T, RECON>(in.bx, c, s, P, xl, xr);
-  recon_face<T, RECON>(in.by, c, s, P, yl, yr);
-  recon_face<T, RECON>(in.bz, c, s, P, zl, zr);
-  const T gm1 = d.gam - T(1);
-  const T rspi = sq(T(3.14159265358979323846));  // sqrt(pi)
-  T out[8];
-  // ---- left state, + moments
+// Gaussian velocity moments of get_v_face (mhd3d3.f90:2594-2615):
+//   a = sqrt(lam), b = .5 exp(-lam v^2)/a/sqrt(pi), v0+- = .5 erfc(-+a v),
+//   v1+- = v v0+- +- b.
+// FP64: CUDA's sqrt/exp/erfc in the reference's operand order (parity mode).
+// FP32: erfc from the Chebyshev fit "erfcc" of Numerical Recipes (Press et
+// al., 2nd ed., sec. 6.2; fractional error < 1.2e-7 for all arguments),
+// rsqrt and exp2-based exp (the performance path).
+template <typename T> struct Moments;
+template <> struct Moments<double> {
+  static __device__ __forceinline__ void hydro(double lam, double vn, bool left, double& v0, double& v1) {
+    const double rspi = sqrt(3.14159265358979323846);
+    double a = sqrt(lam);
+    double b = 0.5 * exp(-lam * (vn * vn)) / a / rspi;
+    if (left) {
+      v0 = 0.5 * erfc(-a * vn);
+      v1 = vn * v0 + b;
+    } else {
+      v0 = 0.5 * erfc(a * vn);
+      v1 = vn * v0 - b;
+    }
+  }
+  static __device__ __forceinline__ double mag(double lam, double vn, bool left) {
+    double a = sqrt(lam);
+    return left ? 0.5 * erfc(-a * vn) : 0.5 * erfc(a * vn);
+  }
+  static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+};
+template <> struct Moments<float> {
+  // erfc(z) for z >= 0 (Numerical Recipes erfcc)
+  static __device__ __forceinline__ float erfc_pos(float z) {
+    float t = __fdividef(1.0f, fmaf(0.5f, z, 1.0f));
+    float q = fmaf(t, 0.17087277f, -0.82215223f);
+    q = fmaf(t, q, 1.48851587f);
+    q = fmaf(t, q, -1.13520398f);
+    q = fmaf(t, q, 0.27886807f);
+    q = fmaf(t, q, -0.18628806f);
+    q = fmaf(t, q, 0.09678418f);
+    q = fmaf(t, q, 0.37409196f);
+    q = fmaf(t, q, 1.00002368f);
+    q = fmaf(t, q, -1.26551223f);
+    return t * __expf(fmaf(-z, z, q));
+  }
+  // 0.5 erfc(-s x) for the left (s=+1) or 0.5 erfc(x) for the right state
+  static __device__ __forceinline__ float half_erfc(float x, bool left) {
+    float h = 0.5f * erfc_pos(fabsf(x));
+    bool direct = left ? (x <= 0.0f) : (x >= 0.0f);
+    return direct ? h : 1.0f - h;
+  }
+  static __device__ __forceinline__ void hydro(float lam, float vn, bool left, float& v0, float& v1) {
+    float ra = rsqrtf(lam);
+    float a = lam * ra;
+    v0 = half_erfc(a * vn, left);
+    float b = (0.5f * 0.56418958354775628f) * ra * __expf(-lam * vn * vn);
+    v1 = left ? fmaf(vn, v0, b) : fmaf(vn, v0, -b);
+  }
+  static __device__ __forceinline__ float mag(float lam, float vn, bool left) {
+    float a = lam * rsqrtf(lam);
+    return half_erfc(a * vn, left);
+  }
+  static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+};
+
+// Fluxes and magnetic stress through one face normal to axis D from the
+// reconstructed left (l) and right (r) states {rho, vx, vy, vz, p, bx, by, bz}
+// (get_flux_stress, mhd3d3.f90:2385-2560): out = {rho, rvx, rvy, rvz, eng,
+// s_x, s_y, s_z}.  Left state with the + moments, right with the - moments.
+template <typename T, int D>
+__device__ __forceinline__ void face_flux(const T* l, const T* r, T gam, T* out) {
+  typedef Moments<T> M;
+  const T gm1 = gam - T(1);
   {
-    T vn = (D == 0) ? ul : (D == 1) ? vl : wl;
-    T bn = (D == 0) ? xl : (D == 1) ? yl : zl;
+    T rl = l[0], ul = l[1], vl = l[2], wl = l[3], pl = l[4], xl = l[5], yl = l[6], zl = l[7];
+    T vn = l[1 + D];
+    T bn = l[5 + D];
     T leng = T(0.5) * rl * (ul * ul + vl * vl + wl * wl) + pl / gm1;
-    T lam = rl / (T(2) * pl);
-    T a = sq(lam);
-    T bb = T(0.5) * ex(-lam * (vn * vn)) / a / rspi;
-    T v0 = T(0.5) * erc(-a * vn);
-    T v1 = vn * v0 + bb;
+    T lam = M::div(rl, T(2) * pl);
+    T v0, v1;
+    M::hydro(lam, vn, true, v0, v1);
     out[0] = rl * v1;
     out[1] = rl * ul * v1;
     out[2] = rl * vl * v1;
@@ -461,50 +526,173 @@ __global__ void k_flux(Dev<T> d, Inp<T> in, Prm<T> P) {
     out[1 + D] = out[1 + D] + pl * v0;
     out[4] = out[4] + T(0.5) * pl * vn * v0;
     T lbsq = xl * xl + yl * yl + zl * zl;
-    lam = rl / (T(2) * pl + lbsq);
-    a = sq(lam);
-    v0 = T(0.5) * erc(-a * vn);
+    lam = M::div(rl, T(2) * pl + lbsq);
+    v0 = M::mag(lam, vn, true);
     out[5] = ((D == 0) ? (T(0.5) * lbsq - xl * xl) : (-xl * bn)) * v0;
     out[6] = ((D == 1) ? (T(0.5) * lbsq - yl * yl) : (-yl * bn)) * v0;
     out[7] = ((D == 2) ? (T(0.5) * lbsq - zl * zl) : (-zl * bn)) * v0;
   }
-  // ---- right state, - moments
   {
-    T vn = (D == 0) ? ur : (D == 1) ? vr : wr;
-    T bn = (D == 0) ? xr : (D == 1) ? yr : zr;
+    T rr = r[0], ur = r[1], vr = r[2], wr = r[3], pr = r[4], xr = r[5], yr = r[6], zr = r[7];
+    T vn = r[1 + D];
+    T bn = r[5 + D];
     T leng = T(0.5) * rr * (ur * ur + vr * vr + wr * wr) + pr / gm1;
-    T lam = rr / (T(2) * pr);
-    T a = sq(lam);
-    T bb = T(0.5) * ex(-lam * (vn * vn)) / a / rspi;
-    T v0 = T(0.5) * erc(a * vn);
-    T v1 = vn * v0 - bb;
-    T f0 = rr * v1;
-    T f1 = rr * ur * v1;
-    T f2 = rr * vr * v1;
-    T f3 = rr * wr * v1;
-    T f4 = (leng + T(0.5) * pr) * v1;
-    if (D == 0) f1 = f1 + pr * v0;
-    if (D == 1) f2 = f2 + pr * v0;
-    if (D == 2) f3 = f3 + pr * v0;
-    f4 = f4 + T(0.5) * pr * vn * v0;
+    T lam = M::div(rr, T(2) * pr);
+    T v0, v1;
+    M::hydro(lam, vn, false, v0, v1);
+    T f[8];
+    f[0] = rr * v1;
+    f[1] = rr * ur * v1;
+    f[2] = rr * vr * v1;
+    f[3] = rr * wr * v1;
+    f[4] = (leng + T(0.5) * pr) * v1;
+    f[1 + D] = f[1 + D] + pr * v0;
+    f[4] = f[4] + T(0.5) * pr * vn * v0;
     T lbsq = xr * xr + yr * yr + zr * zr;
-    lam = rr / (T(2) * pr + lbsq);
-    a = sq(lam);
-    v0 = T(0.5) * erc(a * vn);
-    T s5 = ((D == 0) ? (T(0.5) * lbsq - xr * xr) : (-xr * bn)) * v0;
-    T s6 = ((D == 1) ? (T(0.5) * lbsq - yr * yr) : (-yr * bn)) * v0;
-    T s7 = ((D == 2) ? (T(0.5) * lbsq - zr * zr) : (-zr * bn)) * v0;
-    out[0] = out[0] + f0;
-    out[1] = out[1] + f1;
-    out[2] = out[2] + f2;
-    out[3] = out[3] + f3;
-    out[4] = out[4] + f4;
-    out[5] = out[5] + s5;
-    out[6] = out[6] + s6;
-    out[7] = out[7] + s7;
+    lam = M::div(rr, T(2) * pr + lbsq);
+    v0 = M::mag(lam, vn, false);
+    f[5] = ((D == 0) ? (T(0.5) * lbsq - xr * xr) : (-xr * bn)) * v0;
+    f[6] = ((D == 1) ? (T(0.5) * lbsq - yr * yr) : (-yr * bn)) * v0;
+    f[7] = ((D == 2) ? (T(0.5) * lbsq - zr * zr) : (-zr * bn)) * v0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) out[q] = out[q] + f[q];
   }
+}
+
+// One-sided states from an 8-tap register window (tap m = cell c+m-4 for the
+// face at the low side of cell c): slot of tap m is (m + PH) & 7.
+template <typename T, int RECON, int PH>
+__device__ __forceinline__ void recon_win(const T* w, const Prm<T>& P, T& fl, T& fr) {
+#define TAP(m) w[((m) + PH) & 7]
+  if (RECON == R_PDM) {
+    T fi = tap8(TAP(0), TAP(1), TAP(2), TAP(3), TAP(4), TAP(5), TAP(6), TAP(7));
+    pdm2(TAP(2), TAP(3), TAP(4), TAP(5), fi, P.pdmb, fl, fr);
+  } else if (RECON == R_TVD || RECON == R_TVDMC) {
+    T fi = (TAP(3) + TAP(4)) / T(2);
+    tvd<T, RECON == R_TVDMC>(TAP(2), TAP(3), TAP(4), TAP(5), fi, P.eps, fl, fr);
+  } else {
+    weno5(TAP(1), TAP(2), TAP(3), TAP(4), TAP(5), TAP(6), P.eps, fl, fr);
+    if (RECON == R_MPWENO) {
+      fl = mp_side(fl, TAP(1), TAP(2), TAP(3), TAP(4), TAP(5), P.alpha, P.beta);
+      fr = mp_side(fr, TAP(6), TAP(5), TAP(4), TAP(3), TAP(2), P.alpha, P.beta);
+    }
+  }
+#undef TAP
+}
+
+// Face fluxes through the low face of cell c along axis D by direct (cached)
+// loads; one face per thread.  Used for the x faces of every stage and, for
+// all three axes, by the kernel-level debug entry point.
+template <typename T, int RECON, int D>
+__global__ void k_flux(Dev<T> d, Inp<T> in, Prm<T> P) {
+  const Geom& g = d.g;
+  const int ni = g.nx0 + (D == 0), nj = g.ny0 + (D == 1), nk = g.nz0 + (D == 2);
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ni * nj * nk) return;
+  const int i = t % ni + g.ng;
+  const int r = t / ni;
+  const int j = r % nj + g.ng;
+  const int k = r / nj + g.ng;
+  const int c = i + g.px * (j + g.py * k);
+  const int s = (D == 0) ? 1 : (D == 1) ? g.px : (int)g.plane;
+  const T* src[8] = {in.rho, in.vx, in.vy, in.vz, in.p, in.bx, in.by, in.bz};
+  T L[8], R[8], out[8];
+#pragma unroll
+  for (int v = 0; v < 8; ++v) recon_face<T, RECON>(src[v], c, s, P, L[v], R[v]);
+  face_flux<T, D>(L, R, d.gam, out);
 #pragma unroll
   for (int q = 0; q < 8; ++q) d.F[D][q][c] = out[q];
+}
+
+// Stage combine of the RK steps (mhd3d3.f90:3674-3702, 3745-3788):
+// form 0: (Xp+X)/den, 1: (c*Xp+X)/den, 2: (Xp+c*X)/den.
+template <typename T>
+__device__ __forceinline__ T comb(int form, T c, T xp, T x, T den) {
+  if (form == 0) return (xp + x) / den;
+  if (form == 1) return (c * xp + x) / den;
+  return (xp + c * x) / den;
+}
+
+// y / z faces with the flux divergence fused through shared memory.  A block
+// covers 32 cells along x and TD = 8 cells along the sweep axis D (1: y,
+// 2: z); its TD+1 thread rows compute the TD+1 faces bounding those cells
+// (one face per thread, direct cached loads), then the first TD rows combine
+// the face pair of their cell:
+//   D == 1: dU_q = (Fx_q(i+1)-Fx_q(i))/dx + (Fy_q(j+1)-Fy_q(j))/dy, the first
+//     two terms of advance_corrector1/2 (mhd3d3.f90:3850-3906) in their order;
+//   D == 2: the z term completes advance_corrector1 + stage combine + p +
+//     advance_corrector2 + combine + v (RK: 3666-3697 / 3736-3783; AB:
+//     3626-3627, 3876, 3901-3905), written to the other half of the
+//     double-buffered primitives.
+constexpr int TD = 8;
+
+template <typename T, int RECON, int D>
+__global__ void __launch_bounds__(32 * (TD + 1)) k_flux_t(Dev<T> d, Inp<T> in, Prm<T> P, int form, T cw, T den,
+                                                          int ab) {
+  __shared__ T sF[8][TD + 1][32];
+  const Geom& g = d.g;
+  const int tx = threadIdx.x, r = threadIdx.y;
+  const int i = blockIdx.x * 32 + tx + g.ng;
+  const int n0 = (D == 1) ? g.ny0 : g.nz0;
+  const int cd = blockIdx.y * TD + r + g.ng;  // cell whose low face this thread computes
+  const int o = blockIdx.z + g.ng;             // remaining transverse index
+  const int s = (D == 1) ? g.px : (int)g.plane;
+  const int c = (D == 1) ? i + g.px * (cd + g.py * o) : i + g.px * (o + g.py * cd);
+  const bool xin = i < g.ng + g.nx0;
+  if (xin && cd <= g.ng + n0) {
+    const T* src[8] = {in.rho, in.vx, in.vy, in.vz, in.p, in.bx, in.by, in.bz};
+    T L[8], R[8], F[8];
+#pragma unroll
+    for (int v = 0; v < 8; ++v) recon_face<T, RECON>(src[v], c, s, P, L[v], R[v]);
+    face_flux<T, D>(L, R, d.gam, F);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) sF[q][r][tx] = F[q];
+  }
+  __syncthreads();
+  if (r >= TD || !xin || cd >= g.ng + n0) return;
+  if (D == 1) {
+    const T dx = d.wx[i], dy = d.wy[cd];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      d.dU[q][c] = (d.F[0][q][c + 1] - d.F[0][q][c]) / dx + (sF[q][r + 1][tx] - sF[q][r][tx]) / dy;
+    return;
+  }
+  const T dz = d.wz[cd];
+  const T tau = (T)d.sc->tau;
+  const T gm1 = d.gam - T(1);
+  T dv[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) dv[q] = d.dU[q][c] + (sF[q][r + 1][tx] - sF[q][r][tx]) / dz;
+  // get_conserve of the current state (AB: the state, not the prediction)
+  T rr = d.rho[c], u = d.vx[c], v = d.vy[c], ww = d.vz[c], pr = d.p[c];
+  T rvx0 = rr * u, rvy0 = rr * v, rvz0 = rr * ww;
+  T eng0 = T(0.5) * rr * (u * u + v * v + ww * ww) + pr / gm1;
+  T rho1 = rr - tau * dv[0];
+  T eng1 = eng0 - tau * dv[4];
+  T rx = rvx0 - tau * dv[1], ry = rvy0 - tau * dv[2], rz = rvz0 - tau * dv[3];
+  T hx = rx, hy = ry, hz = rz;
+  if (form >= 0) {
+    rho1 = comb(form, cw, d.q[0][c], rho1, den);
+    hx = comb(form, cw, d.q[1][c], rx, den);
+    hy = comb(form, cw, d.q[2][c], ry, den);
+    hz = comb(form, cw, d.q[3][c], rz, den);
+    eng1 = comb(form, cw, d.q[4][c], eng1, den);
+  }
+  T pn = gm1 * (eng1 - T(0.5) * (hx * hx + hy * hy + hz * hz) / rho1);
+  rx = rx - tau * dv[5];
+  ry = ry - tau * dv[6];
+  rz = rz - tau * dv[7];
+  if (form >= 0) {
+    rx = comb(form, cw, d.q[1][c], rx, den);
+    ry = comb(form, cw, d.q[2][c], ry, den);
+    rz = comb(form, cw, d.q[3][c], rz, den);
+  }
+  d.orho[c] = rho1;
+  d.op[c] = pn;
+  d.ovx[c] = rx / rho1;
+  d.ovy[c] = ry / rho1;
+  d.ovz[c] = rz / rho1;
+  (void)ab;
 }
 
 // -------------------------------------------------------------------- EMF
@@ -540,66 +728,115 @@ __global__ void k_emf(Dev<T> d, Inp<T> in, Prm<T> P) {
   d.E[E][c] = e;
 }
 
-// ------------------------------------------------------------------ update
-// get_conserve + advance_corrector1 + stage combine + p + advance_corrector2 +
-// combine + v (RK: 3666-3697 / 3736-3783; AB: 3616, 3626-3627), interior cells.
-template <typename T>
-__device__ __forceinline__ T comb(int form, T c, T xp, T x, T den) {
-  if (form == 0) return (xp + x) / den;
-  if (form == 1) return (c * xp + x) / den;
-  return (xp + c * x) / den;
-}
-
-template <typename T>
-__global__ void k_update_hydro(Dev<T> d, int form, T cw, T den) {
+// Shared-memory tiled EMF of family E for PDM (the default deck's
+// reconstruction).  A block stages v_a1 and v_a2 of its tile of edges plus a
+// 4-cell halo in the transverse (a1, a2) plane, computes the first pass of
+// interp2_pdm (8-tap along a1, mhd3d3.f90:926-989) once per (a1 face, a2 row)
+// into shared memory, and each edge then takes the second pass along a2, the
+// limiters (corner_pdm), the upwinded face-B reconstructions and the Alfven
+// resistivity term exactly as k_emf does.  Tile (TX, TY, TZ) in edges.
+template <typename T, int E, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(256) k_emf_pdm(Dev<T> d, Inp<T> in, Prm<T> P) {
+  constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
+  constexpr int HX = (E == 0) ? 0 : 4, HY = (E == 1) ? 0 : 4, HZ = (E == 2) ? 0 : 4;
+  constexpr int SX = TX + 2 * HX, SY = TY + 2 * HY, SZ = TZ + 2 * HZ;
+  constexpr int NV = SX * SY * SZ;
+  constexpr int SE = (E == 0) ? 1 : (E == 1) ? SX : SX * SY;
+  constexpr int S1 = (A1 == 0) ? 1 : (A1 == 1) ? SX : SX * SY;
+  constexpr int S2 = (A2 == 0) ? 1 : (A2 == 1) ? SX : SX * SY;
+  constexpr int TE = (E == 0) ? TX : (E == 1) ? TY : TZ;
+  constexpr int T1 = (A1 == 0) ? TX : (A1 == 1) ? TY : TZ;
+  constexpr int T2 = (A2 == 0) ? TX : (A2 == 1) ? TY : TZ;
+  constexpr int NG = TE * T1 * (T2 + 8);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sv = reinterpret_cast<T*>(smem_raw);  // [2][NV]: v_a1, v_a2
+  T* sg = sv + 2 * NV;                     // [2][NG]: first-pass interpolants
   const Geom& g = d.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + g.ng;
-  int j = blockIdx.y * blockDim.y + threadIdx.y + g.ng;
-  int k = blockIdx.z + g.ng;
-  if (i >= g.ng + g.nx0 || j >= g.ng + g.ny0 || k >= g.ng + g.nz0) return;
-  long long c = idx3<T>(g, i, j, k);
-  const long long sy = g.px, sz = g.plane;
-  const T tau = (T)d.sc->tau;
-  const T dx = (T)d.dx[i], dy = (T)d.dy[j], dz = (T)d.dz[k];
-  const T gm1 = d.gam - T(1);
-  T r = d.rho[c], u = d.vx[c], v = d.vy[c], w = d.vz[c], pr = d.p[c];
-  // get_conserve (1641-1650)
-  T rho0 = r, rvx0 = r * u, rvy0 = r * v, rvz0 = r * w;
-  T eng0 = T(0.5) * r * (u * u + v * v + w * w) + pr / gm1;
-  T dv[8];
+  const int ox = g.ng + blockIdx.x * TX, oy = g.ng + blockIdx.y * TY, oz = g.ng + blockIdx.z * TZ;
+  const T* vel[3] = {in.vx, in.vy, in.vz};
+  const T* v1 = vel[A1];
+  const T* v2 = vel[A2];
+  for (int t = threadIdx.x; t < NV; t += blockDim.x) {
+    const int lx = t % SX, r = t / SX, ly = r % SY, lz = r / SY;
+    const int gx = ox - HX + lx, gy = oy - HY + ly, gz = oz - HZ + lz;
+    T a = T(0), b = T(0);
+    if (gx < g.nx && gy < g.ny && gz < g.nz) {
+      const int c = gx + g.px * (gy + g.py * gz);
+      a = v1[c];
+      b = v2[c];
+    }
+    sv[t] = a;
+    sv[NV + t] = b;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < NG; t += blockDim.x) {
+    const int e = t % TE, r = t / TE, f1 = r % T1, r2 = r / T1;
+    const int b0 = e * SE + f1 * S1 + r2 * S2;
 #pragma unroll
-  for (int q = 0; q < 8; ++q)
-    dv[q] = (d.F[0][q][c + 1] - d.F[0][q][c]) / dx + (d.F[1][q][c + sy] - d.F[1][q][c]) / dy +
-            (d.F[2][q][c + sz] - d.F[2][q][c]) / dz;
-  // advance_corrector1 (3842-3878)
-  T rho1 = rho0 - tau * dv[0];
-  T eng1 = eng0 - tau * dv[4];
-  T rx = rvx0 - tau * dv[1], ry = rvy0 - tau * dv[2], rz = rvz0 - tau * dv[3];
-  T hx = rx, hy = ry, hz = rz;
-  if (form >= 0) {
-    rho1 = comb(form, cw, d.q[0][c], rho1, den);
-    hx = comb(form, cw, d.q[1][c], rx, den);
-    hy = comb(form, cw, d.q[2][c], ry, den);
-    hz = comb(form, cw, d.q[3][c], rz, den);
-    eng1 = comb(form, cw, d.q[4][c], eng1, den);
+    for (int w = 0; w < 2; ++w) {
+      const T* a = sv + w * NV + b0;
+      sg[w * NG + t] = tap8(a[0], a[S1], a[2 * S1], a[3 * S1], a[4 * S1], a[5 * S1], a[6 * S1], a[7 * S1]);
+    }
   }
-  T pn = gm1 * (eng1 - T(0.5) * (hx * hx + hy * hy + hz * hz) / rho1);
-  // advance_corrector2 (3880-3907): magnetic stress on the pre-combine momentum
-  rx = rx - tau * dv[5];
-  ry = ry - tau * dv[6];
-  rz = rz - tau * dv[7];
-  if (form >= 0) {
-    rx = comb(form, cw, d.q[1][c], rx, den);
-    ry = comb(form, cw, d.q[2][c], ry, den);
-    rz = comb(form, cw, d.q[3][c], rz, den);
+  __syncthreads();
+  const int n0[3] = {g.nx0, g.ny0, g.nz0};
+  const int lim[3] = {g.ng + n0[0] + (E != 0), g.ng + n0[1] + (E != 1), g.ng + n0[2] + (E != 2)};
+  const int st[3] = {1, g.px, (int)g.plane};
+  const T* fb[3] = {in.bi, in.bj, in.bk};
+  for (int t = threadIdx.x; t < TX * TY * TZ; t += blockDim.x) {
+    const int lx = t % TX, r = t / TX, ly = r % TY, lz = r / TY;
+    const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
+    if (gx >= lim[0] || gy >= lim[1] || gz >= lim[2]) continue;
+    const int e = (E == 0) ? lx : (E == 1) ? ly : lz;
+    const int f1 = (A1 == 0) ? lx : (A1 == 1) ? ly : lz;
+    const int f2 = (A2 == 0) ? lx : (A2 == 1) ? ly : lz;
+    const int cv = e * SE + (f1 + 4) * S1 + (f2 + 4) * S2;
+    T vav[2];
+#pragma unroll
+    for (int w = 0; w < 2; ++w) {
+      const T* gg = sg + w * NG + e + TE * f1 + TE * T1 * f2;
+      constexpr int GS = TE * T1;
+      T vi = tap8(gg[0], gg[GS], gg[2 * GS], gg[3 * GS], gg[4 * GS], gg[5 * GS], gg[6 * GS], gg[7 * GS]);
+      vav[w] = corner_pdm<T, int>(sv + w * NV, cv, S1, S2, vi, P.pdmb);
+    }
+    const int c = gx + g.px * (gy + g.py * gz);
+    const int s1 = st[A1], s2 = st[A2];
+    T b1l, b1r, b2l, b2r;
+    recon_face<T, R_PDM>(fb[A1], c, s2, P, b1l, b1r);
+    recon_face<T, R_PDM>(fb[A2], c, s1, P, b2l, b2r);
+    const T v1av = vav[0], v2av = vav[1];
+    T b1u = (v2av >= T(0)) ? b1l : b1r;
+    T b2u = (v1av >= T(0)) ? b2l : b2r;
+    T ee = -v1av * b2u + v2av * b1u;
+    const T* vf = d.vf;
+    T eta = T(0.25) * (vf[c - s1 - s2] + vf[c - s2] + vf[c] + vf[c - s1]);
+    ee = ee + eta * (b1l + b2r - b1r - b2l);
+    d.E[E][c] = ee;
   }
-  d.rho[c] = rho1;
-  d.p[c] = pn;
-  d.vx[c] = rx / rho1;
-  d.vy[c] = ry / rho1;
-  d.vz[c] = rz / rho1;
 }
 
+template <typename T, int E, int TX, int TY, int TZ>
+void launch_emf_pdm(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStream_t st) {
+  constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
+  constexpr int HX = (E == 0) ? 0 : 4, HY = (E == 1) ? 0 : 4, HZ = (E == 2) ? 0 : 4;
+  constexpr int NV = (TX + 2 * HX) * (TY + 2 * HY) * (TZ + 2 * HZ);
+  constexpr int TE = (E == 0) ? TX : (E == 1) ? TY : TZ;
+  constexpr int T1 = (A1 == 0) ? TX : (A1 == 1) ? TY : TZ;
+  constexpr int T2 = (A2 == 0) ? TX : (A2 == 1) ? TY : TZ;
+  constexpr int NG = TE * T1 * (T2 + 8);
+  constexpr size_t bytes = sizeof(T) * (2 * NV + 2 * NG);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_emf_pdm<T, E, TX, TY, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    attr = true;
+  }
+  const Geom& g = d.g;
+  const int ex = g.nx0 + (E != 0), ey = g.ny0 + (E != 1), ez = g.nz0 + (E != 2);
+  dim3 grid((ex + TX - 1) / TX, (ey + TY - 1) / TY, (ez + TZ - 1) / TZ);
+  k_emf_pdm<T, E, TX, TY, TZ><<<grid, 256, bytes, st>>>(d, in, P);
+}
+
+// ------------------------------------------------------------------ update
 // advance_bijk (3909-3933) + B combine, interior faces of all three arrays.
 template <typename T>
 __global__ void k_update_b(Dev<T> d, int form, T cw, T den) {
@@ -612,7 +849,7 @@ __global__ void k_update_b(Dev<T> d, int form, T cw, T den) {
   long long c = idx3<T>(g, i, j, k);
   const long long sy = g.px, sz = g.plane;
   const T tau = (T)d.sc->tau;
-  const T dx = (T)d.dx[i], dy = (T)d.dy[j], dz = (T)d.dz[k];
+  const T dx = d.wx[i], dy = d.wy[j], dz = d.wz[k];
   const T *ei = d.E[0], *ej = d.E[1], *ek = d.E[2];
   if (in_y && in_z) {
     T b = d.bi[c] - tau * ((ek[c + sy] - ek[c]) / dy - (ej[c + sz] - ej[c]) / dz);
@@ -831,11 +1068,11 @@ void Launch<T>::predictor_ab(const Dev<T>& d, cudaStream_t st) {
 template <typename T, int RECON>
 void flux_r(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
   Prm<T> P = prm_of(d);
-  dim3 b(32, 4, 1);
   const Geom& g = d.g;
-  k_flux<T, RECON, 0><<<grid3(g.nx0 + 1, g.ny0, g.nz0, b), b, 0, st>>>(d, in, P);
-  k_flux<T, RECON, 1><<<grid3(g.nx0, g.ny0 + 1, g.nz0, b), b, 0, st>>>(d, in, P);
-  k_flux<T, RECON, 2><<<grid3(g.nx0, g.ny0, g.nz0 + 1, b), b, 0, st>>>(d, in, P);
+  const int n0 = (g.nx0 + 1) * g.ny0 * g.nz0, n1 = g.nx0 * (g.ny0 + 1) * g.nz0, n2 = g.nx0 * g.ny0 * (g.nz0 + 1);
+  k_flux<T, RECON, 0><<<(n0 + 127) / 128, 128, 0, st>>>(d, in, P);
+  k_flux<T, RECON, 1><<<(n1 + 127) / 128, 128, 0, st>>>(d, in, P);
+  k_flux<T, RECON, 2><<<(n2 + 127) / 128, 128, 0, st>>>(d, in, P);
 }
 
 template <typename T>
@@ -850,6 +1087,35 @@ void Launch<T>::fluxes(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
 }
 
 template <typename T, int RECON>
+void hydro_r(const Dev<T>& d, const Inp<T>& in, int part, int form, double c, double den, bool ab,
+             cudaStream_t st) {
+  Prm<T> P = prm_of(d);
+  const Geom& g = d.g;
+  if (part == 0) {
+    const int n0 = (g.nx0 + 1) * g.ny0 * g.nz0;
+    k_flux<T, RECON, 0><<<(n0 + 127) / 128, 128, 0, st>>>(d, in, P);
+  } else if (part == 1) {
+    dim3 grid((g.nx0 + 31) / 32, (g.ny0 + TD - 1) / TD, g.nz0);
+    k_flux_t<T, RECON, 1><<<grid, dim3(32, TD + 1), 0, st>>>(d, in, P, -1, T(0), T(1), 0);
+  } else {
+    dim3 grid((g.nx0 + 31) / 32, (g.nz0 + TD - 1) / TD, g.ny0);
+    k_flux_t<T, RECON, 2><<<grid, dim3(32, TD + 1), 0, st>>>(d, in, P, form, (T)c, (T)den, ab ? 1 : 0);
+  }
+}
+
+template <typename T>
+void Launch<T>::hydro(const Dev<T>& d, const Inp<T>& in, int part, int form, double c, double den, bool ab,
+                      cudaStream_t st) {
+  switch (d.recon) {
+    case R_PDM: hydro_r<T, R_PDM>(d, in, part, form, c, den, ab, st); break;
+    case R_TVD: hydro_r<T, R_TVD>(d, in, part, form, c, den, ab, st); break;
+    case R_WENO: hydro_r<T, R_WENO>(d, in, part, form, c, den, ab, st); break;
+    case R_MPWENO: hydro_r<T, R_MPWENO>(d, in, part, form, c, den, ab, st); break;
+    default: hydro_r<T, R_TVDMC>(d, in, part, form, c, den, ab, st); break;
+  }
+}
+
+template <typename T, int RECON>
 void emf_r(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
   Prm<T> P = prm_of(d);
   dim3 b(32, 4, 1);
@@ -859,8 +1125,19 @@ void emf_r(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
   k_emf<T, RECON, 2><<<grid3(g.nx0 + 1, g.ny0 + 1, g.nz0, b), b, 0, st>>>(d, in, P);
 }
 
+// ei tile: 32 x 8 x 8 edges in FP32, 32 x 4 x 4 in FP64 (96 KB of shared memory each)
+template <typename T> struct EiTile { static constexpr int Y = 8; };
+template <> struct EiTile<double> { static constexpr int Y = 4; };
+
 template <typename T>
 void Launch<T>::emf(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
+  if (d.recon == R_PDM) {
+    Prm<T> P = prm_of(d);
+    launch_emf_pdm<T, 0, 32, EiTile<T>::Y, EiTile<T>::Y>(d, in, P, st);
+    launch_emf_pdm<T, 1, 32, 1, 8>(d, in, P, st);
+    launch_emf_pdm<T, 2, 32, 8, 1>(d, in, P, st);
+    return;
+  }
   switch (d.recon) {
     case R_PDM: emf_r<T, R_PDM>(d, in, st); break;
     case R_TVD: emf_r<T, R_TVD>(d, in, st); break;
@@ -871,10 +1148,9 @@ void Launch<T>::emf(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
 }
 
 template <typename T>
-void Launch<T>::update(const Dev<T>& d, int form, double c, double den, cudaStream_t st) {
+void Launch<T>::ct(const Dev<T>& d, int form, double c, double den, cudaStream_t st) {
   dim3 b(32, 4, 1);
   const Geom& g = d.g;
-  k_update_hydro<T><<<grid3(g.nx0, g.ny0, g.nz0, b), b, 0, st>>>(d, form, (T)c, (T)den);
   k_update_b<T><<<grid3(g.nx0 + 1, g.ny0 + 1, g.nz0 + 1, b), b, 0, st>>>(d, form, (T)c, (T)den);
 }
 

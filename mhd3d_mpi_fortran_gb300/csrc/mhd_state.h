@@ -38,8 +38,11 @@ struct Dev {
   int recon, stepop, tvd_shift, dt_mode;
   int bc[3];
   T gam, pdmb, eps, alpha, beta, cfl;
-  // state of the current level
+  // state of the current level; the cell primitives are double-buffered:
+  // the z-flux kernel writes the new level into o* (swapped after each stage)
   T *rho, *vx, *vy, *vz, *p, *bi, *bj, *bk, *bx, *by, *bz;
+  T *orho, *ovx, *ovy, *ovz, *op;
+  T* dU[8];    // x+y flux divergence per cell {rho, rvx, rvy, rvz, eng, s_x, s_y, s_z}
   // previous level: RK {rho, rvx, rvy, rvz, eng, bi, bj, bk};
   //                 AB {rho, vx, vy, vz, p, bi, bj, bk, bx, by, bz}
   T* q[11];
@@ -49,6 +52,7 @@ struct Dev {
   T* E[3];     // edge EMFs ei, ej, ek
   T* vf;       // |v| + |B|/sqrt(rho) of the stage input
   const double *dx, *dy, *dz;  // FP64 cell widths (ghost-inclusive, 1-D)
+  const T *wx, *wy, *wz;       // the same widths in T (FP32 path: converted once)
   Scal* sc;
   unsigned int* partial;       // per-block scratch of the CFL reduction
   unsigned int* counter;
@@ -67,10 +71,16 @@ struct Launch {
   static void cfl(const Dev<T>& d, int mode, cudaStream_t st);  // mode: 0 RK fixed, 1 CFL, 2 AB
   static void save_prev(const Dev<T>& d, cudaStream_t st);
   static void predictor_ab(const Dev<T>& d, cudaStream_t st);
+  // face fluxes of all three axes into F (kernel-level debug entry point)
   static void fluxes(const Dev<T>& d, const Inp<T>& in, cudaStream_t st);
   static void emf(const Dev<T>& d, const Inp<T>& in, cudaStream_t st);
+  // hydro part of a stage, part 0: x faces; 1: y march (x+y divergence);
+  // 2: z march with the conserved update and combine, new primitives into d.o*.
   // form: -1 none (stage 1 / AB), 0 (Xp+X)/den, 1 (c*Xp+X)/den, 2 (Xp+c*X)/den
-  static void update(const Dev<T>& d, int form, double c, double den, cudaStream_t st);
+  static void hydro(const Dev<T>& d, const Inp<T>& in, int part, int form, double c, double den, bool ab,
+                    cudaStream_t st);
+  // constrained-transport face-B update + combine
+  static void ct(const Dev<T>& d, int form, double c, double den, cudaStream_t st);
   static void fill(const Dev<T>& d, cudaStream_t st);
   static void diagnostics(const Dev<T>& d, double* out5_dev, cudaStream_t st);
 };

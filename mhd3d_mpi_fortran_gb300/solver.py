@@ -80,9 +80,9 @@ class MHDSolver:
         check(self.lib, self.lib.mhd_set_profiling(self.h, 1 if on else 0), "mhd_set_profiling")
 
     def timings(self):
-        out = (C.c_float * 5)()
+        out = (C.c_float * 8)()
         check(self.lib, self.lib.mhd_last_timings(self.h, out), "mhd_last_timings")
-        return dict(zip(("fluxes", "emf", "update", "fill", "dt"), list(out)))
+        return dict(zip(("flux_x", "flux_y", "flux_z_update", "emf", "ct", "fill", "dt"), list(out)))
 
     # -- readback -------------------------------------------------------
     def fetch(self) -> dict:
