@@ -4,13 +4,14 @@
 //
 // Step sequence (reference routine -> launches):
 //   step_rk2/rk3 (mhd3d3.f90:3648-3792):
-//     get_dt -> Launch::cfl; advance_previous -> save_prev;
-//     per stage: get_eijk_LFM -> emf; get_flux_stress -> fluxes;
-//     advance_corrector1/2 + advance_bijk + combines -> update;
-//     fill_hydro_mpi/fill_mag_mpi -> fill; get_bxyz -> bxyz_vf.
+//     get_dt + advance_previous -> Launch::cfl(save);
+//     per stage: get_eijk_LFM -> emf; get_flux_stress + advance_corrector1/2
+//     + combines -> hydro (x faces, y faces, z faces + update);
+//     advance_bijk + combine -> ct; fill_hydro_mpi/fill_mag_mpi + get_bxyz
+//     -> fill_bxyz.
 //   step_ab (mhd3d3.f90:3602-3644):
 //     get_dt -> cfl(AB); advance_predictor_ab -> predictor_ab; emf(h);
-//     fluxes(h); update; fill; bxyz.
+//     hydro(h); ct; fill_bxyz.
 #include <cuda_runtime.h>
 #include <chrono>
 #include <cmath>
@@ -169,14 +170,13 @@ void enqueue_step(Handle* h, int& par, cudaStream_t st, Rec* r = nullptr) {
     R.begin(); Launch<T>::ct(d, -1, 0.0, 1.0, st); R.end(4);
     par ^= 1;
     d = at_par(base, par);
-    R.begin(); Launch<T>::fill(d, st); Launch<T>::bxyz_vf(d, false, st); R.end(5);
+    R.begin(); Launch<T>::fill_bxyz(d, false, st); R.end(5);
     return;
   }
   {
     Dev<T> d = at_par(base, par);
     R.begin();
-    Launch<T>::cfl(d, p.dt_mode == MHD_DT_CFL ? 1 : 0, st);
-    Launch<T>::save_prev(d, st);
+    Launch<T>::cfl(d, p.dt_mode == MHD_DT_CFL ? 1 : 0, st, true);
     R.end(6);
   }
   int nst = (p.stepop == MHD_STEP_RK2) ? 2 : 3;
@@ -197,7 +197,7 @@ void enqueue_step(Handle* h, int& par, cudaStream_t st, Rec* r = nullptr) {
     R.begin(); Launch<T>::ct(d, form, c, den, st); R.end(4);
     par ^= 1;
     d = at_par(base, par);
-    R.begin(); Launch<T>::fill(d, st); Launch<T>::bxyz_vf(d, true, st); R.end(5);
+    R.begin(); Launch<T>::fill_bxyz(d, true, st); R.end(5);
   }
 }
 

@@ -318,12 +318,15 @@ __global__ void k_bxyz_vf(Dev<T> d, int want_vf) {
 // get_dt over all cells incl. ghosts: per-block min, then atomicMin on the
 // bit pattern (positive doubles order like their bits).  Status bits mirror
 // diag_rho_neg / diag_overflow.
+// save != 0 also stores U^n of the RK stage combines (advance_previous,
+// 3794-3819) at interior cells and faces, the only places they are read.
 template <typename T>
-__global__ void k_cfl(Dev<T> d) {
+__global__ void k_cfl(Dev<T> d, int save) {
   const Geom& g = d.g;
   long long n = (long long)g.nx * g.ny * g.nz;
   double m = INFINITY;
   unsigned st = 0;
+  const T gm1 = d.gam - T(1);
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
        t += (long long)gridDim.x * blockDim.x) {
     int i = (int)(t % g.nx);
@@ -332,6 +335,22 @@ __global__ void k_cfl(Dev<T> d) {
     int k = (int)(r / g.ny);
     long long c = idx3<T>(g, i, j, k);
     T r0 = d.rho[c], p0 = d.p[c], u = d.vx[c], v = d.vy[c], w = d.vz[c];
+    if (save) {
+      const bool ix = i >= g.ng && i < g.ng + g.nx0, iy = j >= g.ng && j < g.ng + g.ny0,
+                 iz = k >= g.ng && k < g.ng + g.nz0;
+      if (ix && iy && iz) {
+        d.q[0][c] = r0;
+        d.q[1][c] = r0 * u;
+        d.q[2][c] = r0 * v;
+        d.q[3][c] = r0 * w;
+        d.q[4][c] = T(0.5) * r0 * (u * u + v * v + w * w) + p0 / gm1;
+      }
+      const bool fx = i >= g.ng && i <= g.ng + g.nx0, fy = j >= g.ng && j <= g.ng + g.ny0,
+                 fz = k >= g.ng && k <= g.ng + g.nz0;
+      if (fx && iy && iz) d.q[5][c] = d.bi[c];
+      if (ix && fy && iz) d.q[6][c] = d.bj[c];
+      if (ix && iy && fz) d.q[7][c] = d.bk[c];
+    }
     T a = d.bx[c], b = d.by[c], cc = d.bz[c];
     T vv = sq(u * u + v * v + w * w);
     T btot = sq(a * a + b * b + cc * cc);
@@ -613,48 +632,96 @@ __device__ __forceinline__ T comb(int form, T c, T xp, T x, T den) {
   return (xp + c * x) / den;
 }
 
+// One-sided states from a column of taps in shared memory: tap m (cell
+// c+m-4 for the face at the low side of cell c) at col[m * RS].
+template <typename T, int RECON, int RS>
+__device__ __forceinline__ void recon_col(const T* col, const Prm<T>& P, T& fl, T& fr) {
+  if (RECON == R_PDM) {
+    T fi = tap8(col[0], col[RS], col[2 * RS], col[3 * RS], col[4 * RS], col[5 * RS], col[6 * RS], col[7 * RS]);
+    pdm2(col[2 * RS], col[3 * RS], col[4 * RS], col[5 * RS], fi, P.pdmb, fl, fr);
+  } else if (RECON == R_TVD || RECON == R_TVDMC) {
+    T fi = (col[3 * RS] + col[4 * RS]) / T(2);
+    tvd<T, RECON == R_TVDMC>(col[2 * RS], col[3 * RS], col[4 * RS], col[5 * RS], fi, P.eps, fl, fr);
+  } else {
+    T a1 = col[RS], a2 = col[2 * RS], a3 = col[3 * RS], a4 = col[4 * RS], a5 = col[5 * RS], a6 = col[6 * RS];
+    weno5(a1, a2, a3, a4, a5, a6, P.eps, fl, fr);
+    if (RECON == R_MPWENO) {
+      fl = mp_side(fl, a1, a2, a3, a4, a5, P.alpha, P.beta);
+      fr = mp_side(fr, a6, a5, a4, a3, a2, P.alpha, P.beta);
+    }
+  }
+}
+
 // y / z faces with the flux divergence fused through shared memory.  A block
-// covers 32 cells along x and TD = 8 cells along the sweep axis D (1: y,
-// 2: z); its TD+1 thread rows compute the TD+1 faces bounding those cells
-// (one face per thread, direct cached loads), then the first TD rows combine
-// the face pair of their cell:
+// covers 32 cells along x and TD cells along the sweep axis D (1: y, 2: z) at
+// one value of the remaining axis.  It stages the 8 reconstructed cell fields
+// of TD+8 rows (4-cell halo each side) with independent coalesced loads, its
+// TD+1 thread rows compute the TD+1 faces bounding those cells from shared
+// memory, and the first TD rows combine the face pair of their cell:
 //   D == 1: dU_q = (Fx_q(i+1)-Fx_q(i))/dx + (Fy_q(j+1)-Fy_q(j))/dy, the first
 //     two terms of advance_corrector1/2 (mhd3d3.f90:3850-3906) in their order;
 //   D == 2: the z term completes advance_corrector1 + stage combine + p +
 //     advance_corrector2 + combine + v (RK: 3666-3697 / 3736-3783; AB:
 //     3626-3627, 3876, 3901-3905), written to the other half of the
 //     double-buffered primitives.
-constexpr int TD = 8;
+constexpr int TD = 16;
+constexpr int TROWS = TD + 8;
+
+template <typename T>
+__host__ __device__ constexpr size_t flux_t_smem() {
+  return sizeof(T) * (8 * TROWS * 32 + 8 * (TD + 1) * 32);
+}
 
 template <typename T, int RECON, int D>
 __global__ void __launch_bounds__(32 * (TD + 1)) k_flux_t(Dev<T> d, Inp<T> in, Prm<T> P, int form, T cw, T den,
                                                           int ab) {
-  __shared__ T sF[8][TD + 1][32];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sv = reinterpret_cast<T*>(smem_raw);  // [8][TROWS][32] cell fields
+  T* sF = sv + 8 * TROWS * 32;             // [8][TD+1][32] face fluxes
   const Geom& g = d.g;
   const int tx = threadIdx.x, r = threadIdx.y;
-  const int i = blockIdx.x * 32 + tx + g.ng;
+  const int i0 = blockIdx.x * 32 + g.ng;
+  const int i = i0 + tx;
   const int n0 = (D == 1) ? g.ny0 : g.nz0;
-  const int cd = blockIdx.y * TD + r + g.ng;  // cell whose low face this thread computes
-  const int o = blockIdx.z + g.ng;             // remaining transverse index
+  const int nD = (D == 1) ? g.ny : g.nz;
+  const int cd0 = blockIdx.y * TD + g.ng;  // first cell of the tile along D
+  const int o = blockIdx.z + g.ng;         // remaining transverse index
   const int s = (D == 1) ? g.px : (int)g.plane;
-  const int c = (D == 1) ? i + g.px * (cd + g.py * o) : i + g.px * (o + g.py * cd);
+  const int rowbase = (D == 1) ? i0 + g.px * g.py * o : i0 + g.px * o;  // + cd * s
+  {
+    const T* src[8] = {in.rho, in.vx, in.vy, in.vz, in.p, in.bx, in.by, in.bz};
+    const int nthr = 32 * (TD + 1);
+    const bool xok = i0 + tx < g.nx;
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+      const T* sp = src[v] + rowbase + tx;
+      for (int t = r * 32 + tx; t < TROWS * 32; t += nthr) {
+        const int cd = cd0 - 4 + (t >> 5);
+        sv[v * TROWS * 32 + t] = (xok && cd < nD) ? sp[cd * s] : T(0);
+      }
+    }
+  }
+  __syncthreads();
+  const int cd = cd0 + r;  // cell whose low face this thread computes
   const bool xin = i < g.ng + g.nx0;
   if (xin && cd <= g.ng + n0) {
-    const T* src[8] = {in.rho, in.vx, in.vy, in.vz, in.p, in.bx, in.by, in.bz};
     T L[8], R[8], F[8];
 #pragma unroll
-    for (int v = 0; v < 8; ++v) recon_face<T, RECON>(src[v], c, s, P, L[v], R[v]);
+    for (int v = 0; v < 8; ++v) recon_col<T, RECON, 32>(sv + (v * TROWS + r) * 32 + tx, P, L[v], R[v]);
     face_flux<T, D>(L, R, d.gam, F);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) sF[q][r][tx] = F[q];
+    for (int q = 0; q < 8; ++q) sF[(q * (TD + 1) + r) * 32 + tx] = F[q];
   }
   __syncthreads();
   if (r >= TD || !xin || cd >= g.ng + n0) return;
+  const int c = rowbase + tx + cd * s;
+  T dF[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) dF[q] = sF[(q * (TD + 1) + r + 1) * 32 + tx] - sF[(q * (TD + 1) + r) * 32 + tx];
   if (D == 1) {
     const T dx = d.wx[i], dy = d.wy[cd];
 #pragma unroll
-    for (int q = 0; q < 8; ++q)
-      d.dU[q][c] = (d.F[0][q][c + 1] - d.F[0][q][c]) / dx + (sF[q][r + 1][tx] - sF[q][r][tx]) / dy;
+    for (int q = 0; q < 8; ++q) d.dU[q][c] = (d.F[0][q][c + 1] - d.F[0][q][c]) / dx + dF[q] / dy;
     return;
   }
   const T dz = d.wz[cd];
@@ -662,7 +729,7 @@ __global__ void __launch_bounds__(32 * (TD + 1)) k_flux_t(Dev<T> d, Inp<T> in, P
   const T gm1 = d.gam - T(1);
   T dv[8];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) dv[q] = d.dU[q][c] + (sF[q][r + 1][tx] - sF[q][r][tx]) / dz;
+  for (int q = 0; q < 8; ++q) dv[q] = d.dU[q][c] + dF[q] / dz;
   // get_conserve of the current state (AB: the state, not the prediction)
   T rr = d.rho[c], u = d.vx[c], v = d.vy[c], ww = d.vz[c], pr = d.p[c];
   T rvx0 = rr * u, rvy0 = rr * v, rvz0 = rr * ww;
@@ -921,6 +988,66 @@ __global__ void k_fill(Dev<T> d) {
   }
 }
 
+// Ghost fill fused with get_bxyz (mhd3d3.f90:2118-2128) and vf: every thread
+// fills the ghost elements it owns (as k_fill) and computes the cell-centred
+// B and vf of its cell from the ghost images of the faces and cells it needs,
+// so no thread reads an element another thread is filling.  Face B is even
+// under every boundary kind and vf uses only squares, so the images give
+// exactly the values the separate fill followed by get_bxyz produces.
+template <typename T>
+__global__ void k_fill_bxyz(Dev<T> d, int want_vf) {
+  const Geom& g = d.g;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int j = blockIdx.y * blockDim.y + threadIdx.y;
+  int k = blockIdx.z;
+  if (i > g.nx || j > g.ny || k > g.nz) return;
+  T* arr[8] = {d.rho, d.vx, d.vy, d.vz, d.p, d.bi, d.bj, d.bk};
+  const int n0[3] = {g.nx0, g.ny0, g.nz0};
+  const int x3[3] = {i, j, k};
+  bool fl;
+  int sc[3], sf[3], sf1[3];
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    sc[ax] = ghost_src(x3[ax], g.ng, n0[ax], false, d.bc[ax], fl);
+    sf[ax] = ghost_src(x3[ax], g.ng, n0[ax], true, d.bc[ax], fl);
+    sf1[ax] = ghost_src(x3[ax] + 1, g.ng, n0[ax], true, d.bc[ax], fl);
+  }
+  const long long c = idx3<T>(g, i, j, k);
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    const int fa = a - 5;
+    bool ghost = false, inside = true;
+    int s3[3];
+    T sgn = T(1);
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      const bool face = (fa == ax);
+      const int ext = (ax == 0 ? g.nx : ax == 1 ? g.ny : g.nz) + (face ? 1 : 0);
+      if (x3[ax] >= ext) inside = false;
+      s3[ax] = face ? sf[ax] : sc[ax];
+      if (s3[ax] != x3[ax]) {
+        ghost = true;
+        if (d.bc[ax] == BC_REFLECT && a == 1 + ax) sgn = -sgn;
+      }
+    }
+    if (!inside || !ghost) continue;
+    const T val = arr[a][idx3<T>(g, s3[0], s3[1], s3[2])];
+    arr[a][c] = (sgn > T(0)) ? val : -val;
+  }
+  if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+  const T bx = T(0.5) * (d.bi[idx3<T>(g, sf1[0], sc[1], sc[2])] + d.bi[idx3<T>(g, sf[0], sc[1], sc[2])]);
+  const T by = T(0.5) * (d.bj[idx3<T>(g, sc[0], sf1[1], sc[2])] + d.bj[idx3<T>(g, sc[0], sf[1], sc[2])]);
+  const T bz = T(0.5) * (d.bk[idx3<T>(g, sc[0], sc[1], sf1[2])] + d.bk[idx3<T>(g, sc[0], sc[1], sf[2])]);
+  d.bx[c] = bx;
+  d.by[c] = by;
+  d.bz[c] = bz;
+  if (want_vf) {
+    const long long s = idx3<T>(g, sc[0], sc[1], sc[2]);
+    const T u = d.vx[s], v = d.vy[s], w = d.vz[s];
+    d.vf[c] = sq(u * u + v * v + w * w) + sq((bx * bx + by * by + bz * bz) / d.rho[s]);
+  }
+}
+
 // ------------------------------------------------------------ diagnostics
 // Double-double (Neumaier/TwoSum) accumulation of mass and energy, max |div B|
 // (FP64), min rho incl. ghosts.  Deterministic: fixed per-thread order,
@@ -1050,8 +1177,14 @@ void Launch<T>::bxyz_vf(const Dev<T>& d, bool want_vf, cudaStream_t st) {
 }
 
 template <typename T>
-void Launch<T>::cfl(const Dev<T>& d, int mode, cudaStream_t st) {
-  k_cfl<T><<<152 * 4, 256, 0, st>>>(d);
+void Launch<T>::fill_bxyz(const Dev<T>& d, bool want_vf, cudaStream_t st) {
+  dim3 b(64, 4, 1);
+  k_fill_bxyz<T><<<grid3(d.g.nx + 1, d.g.ny + 1, d.g.nz + 1, b), b, 0, st>>>(d, want_vf ? 1 : 0);
+}
+
+template <typename T>
+void Launch<T>::cfl(const Dev<T>& d, int mode, cudaStream_t st, bool save) {
+  k_cfl<T><<<152 * 8, 256, 0, st>>>(d, save ? 1 : 0);
   k_cfl_final<T><<<1, 1, 0, st>>>(d, mode);
 }
 
@@ -1095,11 +1228,23 @@ void hydro_r(const Dev<T>& d, const Inp<T>& in, int part, int form, double c, do
     const int n0 = (g.nx0 + 1) * g.ny0 * g.nz0;
     k_flux<T, RECON, 0><<<(n0 + 127) / 128, 128, 0, st>>>(d, in, P);
   } else if (part == 1) {
+    constexpr size_t sm = flux_t_smem<T>();
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_flux_t<T, RECON, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      attr = true;
+    }
     dim3 grid((g.nx0 + 31) / 32, (g.ny0 + TD - 1) / TD, g.nz0);
-    k_flux_t<T, RECON, 1><<<grid, dim3(32, TD + 1), 0, st>>>(d, in, P, -1, T(0), T(1), 0);
+    k_flux_t<T, RECON, 1><<<grid, dim3(32, TD + 1), sm, st>>>(d, in, P, -1, T(0), T(1), 0);
   } else {
+    constexpr size_t sm = flux_t_smem<T>();
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_flux_t<T, RECON, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      attr = true;
+    }
     dim3 grid((g.nx0 + 31) / 32, (g.nz0 + TD - 1) / TD, g.ny0);
-    k_flux_t<T, RECON, 2><<<grid, dim3(32, TD + 1), 0, st>>>(d, in, P, form, (T)c, (T)den, ab ? 1 : 0);
+    k_flux_t<T, RECON, 2><<<grid, dim3(32, TD + 1), sm, st>>>(d, in, P, form, (T)c, (T)den, ab ? 1 : 0);
   }
 }
 

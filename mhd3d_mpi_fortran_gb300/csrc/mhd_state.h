@@ -68,7 +68,10 @@ struct Inp {
 template <typename T>
 struct Launch {
   static void bxyz_vf(const Dev<T>& d, bool want_vf, cudaStream_t st);
-  static void cfl(const Dev<T>& d, int mode, cudaStream_t st);  // mode: 0 RK fixed, 1 CFL, 2 AB
+  // ghost fill + get_bxyz + vf in one pass
+  static void fill_bxyz(const Dev<T>& d, bool want_vf, cudaStream_t st);
+  // mode: 0 RK fixed, 1 CFL, 2 AB, 3 read only; save: also store RK U^n
+  static void cfl(const Dev<T>& d, int mode, cudaStream_t st, bool save = false);
   static void save_prev(const Dev<T>& d, cudaStream_t st);
   static void predictor_ab(const Dev<T>& d, cudaStream_t st);
   // face fluxes of all three axes into F (kernel-level debug entry point)
