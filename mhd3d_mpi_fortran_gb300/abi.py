@@ -89,11 +89,13 @@ _LIB = None
 
 
 def load(path: str | os.PathLike | None = None) -> C.CDLL:
-    """Open libmhdgpu.so (building it first if absent) and declare signatures."""
+    """Open libmhdgpu.so (building it first if absent) and declare signatures.
+    The environment variable MHD_LIB selects another build of the library."""
     global _LIB
     if _LIB is not None and path is None:
         return _LIB
-    p = Path(path) if path else LIBPATH
+    env = os.environ.get("MHD_LIB")
+    p = Path(path) if path else (Path(env) if env else LIBPATH)
     if not p.exists():
         from . import build as _b
         _b.build()

@@ -664,20 +664,33 @@ __device__ __forceinline__ void recon_col(const T* col, const Prm<T>& P, T& fl, 
 //     advance_corrector2 + combine + v (RK: 3666-3697 / 3736-3783; AB:
 //     3626-3627, 3876, 3901-3905), written to the other half of the
 //     double-buffered primitives.
-constexpr int TD = 16;
+// Tuning knobs (compile time): cells per block along the sweep axis, whether
+// the cell tile is staged in shared memory (1) or read through L1 (0), and
+// the minimum resident blocks per SM requested from the register allocator.
+#ifndef MHD_FLUX_TD
+#define MHD_FLUX_TD 8
+#endif
+#ifndef MHD_FLUX_STAGED
+#define MHD_FLUX_STAGED 0
+#endif
+#ifndef MHD_FLUX_MINB
+#define MHD_FLUX_MINB 1
+#endif
+constexpr int TD = MHD_FLUX_TD;
 constexpr int TROWS = TD + 8;
+constexpr bool FLUX_STAGED = MHD_FLUX_STAGED != 0;
 
 template <typename T>
 __host__ __device__ constexpr size_t flux_t_smem() {
-  return sizeof(T) * (8 * TROWS * 32 + 8 * (TD + 1) * 32);
+  return sizeof(T) * ((FLUX_STAGED ? 8 * TROWS * 32 : 0) + 8 * (TD + 1) * 32);
 }
 
 template <typename T, int RECON, int D>
-__global__ void __launch_bounds__(32 * (TD + 1)) k_flux_t(Dev<T> d, Inp<T> in, Prm<T> P, int form, T cw, T den,
-                                                          int ab) {
+__global__ void __launch_bounds__(32 * (TD + 1), MHD_FLUX_MINB)
+    k_flux_t(Dev<T> d, Inp<T> in, Prm<T> P, int form, T cw, T den, int ab) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* sv = reinterpret_cast<T*>(smem_raw);  // [8][TROWS][32] cell fields
-  T* sF = sv + 8 * TROWS * 32;             // [8][TD+1][32] face fluxes
+  T* sv = reinterpret_cast<T*>(smem_raw);                      // [8][TROWS][32] cell fields
+  T* sF = sv + (FLUX_STAGED ? 8 * TROWS * 32 : 0);             // [8][TD+1][32] face fluxes
   const Geom& g = d.g;
   const int tx = threadIdx.x, r = threadIdx.y;
   const int i0 = blockIdx.x * 32 + g.ng;
@@ -688,8 +701,8 @@ __global__ void __launch_bounds__(32 * (TD + 1)) k_flux_t(Dev<T> d, Inp<T> in, P
   const int o = blockIdx.z + g.ng;         // remaining transverse index
   const int s = (D == 1) ? g.px : (int)g.plane;
   const int rowbase = (D == 1) ? i0 + g.px * g.py * o : i0 + g.px * o;  // + cd * s
-  {
-    const T* src[8] = {in.rho, in.vx, in.vy, in.vz, in.p, in.bx, in.by, in.bz};
+  const T* src[8] = {in.rho, in.vx, in.vy, in.vz, in.p, in.bx, in.by, in.bz};
+  if (FLUX_STAGED) {
     const int nthr = 32 * (TD + 1);
     const bool xok = i0 + tx < g.nx;
 #pragma unroll
@@ -700,14 +713,20 @@ __global__ void __launch_bounds__(32 * (TD + 1)) k_flux_t(Dev<T> d, Inp<T> in, P
         sv[v * TROWS * 32 + t] = (xok && cd < nD) ? sp[cd * s] : T(0);
       }
     }
+    __syncthreads();
   }
-  __syncthreads();
   const int cd = cd0 + r;  // cell whose low face this thread computes
   const bool xin = i < g.ng + g.nx0;
   if (xin && cd <= g.ng + n0) {
     T L[8], R[8], F[8];
+    if (FLUX_STAGED) {
 #pragma unroll
-    for (int v = 0; v < 8; ++v) recon_col<T, RECON, 32>(sv + (v * TROWS + r) * 32 + tx, P, L[v], R[v]);
+      for (int v = 0; v < 8; ++v) recon_col<T, RECON, 32>(sv + (v * TROWS + r) * 32 + tx, P, L[v], R[v]);
+    } else {
+      const int cf = rowbase + tx + cd * s;
+#pragma unroll
+      for (int v = 0; v < 8; ++v) recon_face<T, RECON>(src[v], cf, s, P, L[v], R[v]);
+    }
     face_flux<T, D>(L, R, d.gam, F);
 #pragma unroll
     for (int q = 0; q < 8; ++q) sF[(q * (TD + 1) + r) * 32 + tx] = F[q];
