@@ -168,9 +168,8 @@ struct Prm {
 
 // One-sided face states of f at the low face of element c along stride s
 // (reconstruct_3d for dirs 1-3, mhd3d3.f90:833-860).
-template <typename T, int RECON>
-__device__ __forceinline__ void recon_face(const T* __restrict__ f, long long c, long long s,
-                                           const Prm<T>& P, T& fl, T& fr) {
+template <typename T, int RECON, typename I>
+__device__ __forceinline__ void recon_face(const T* __restrict__ f, I c, I s, const Prm<T>& P, T& fl, T& fr) {
   if (RECON == R_PDM) {
     T a0 = f[c - 4 * s], a1 = f[c - 3 * s], a2 = f[c - 2 * s], a3 = f[c - s];
     T a4 = f[c], a5 = f[c + s], a6 = f[c + 2 * s], a7 = f[c + 3 * s];
@@ -327,13 +326,13 @@ __global__ void k_cfl(Dev<T> d, int save) {
   double m = INFINITY;
   unsigned st = 0;
   const T gm1 = d.gam - T(1);
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
-       t += (long long)gridDim.x * blockDim.x) {
-    int i = (int)(t % g.nx);
-    long long r = t / g.nx;
-    int j = (int)(r % g.ny);
-    int k = (int)(r / g.ny);
-    long long c = idx3<T>(g, i, j, k);
+  (void)n;
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  const int k1 = min(g.nz, (int)(blockIdx.z + 1) * 8);
+  for (int k = blockIdx.z * 8; k < k1; ++k) {
+    if (i >= g.nx || j >= g.ny) break;
+    const int c = i + g.px * (j + g.py * k);
     T r0 = d.rho[c], p0 = d.p[c], u = d.vx[c], v = d.vy[c], w = d.vz[c];
     if (save) {
       const bool ix = i >= g.ng && i < g.ng + g.nx0, iy = j >= g.ng && j < g.ng + g.ny0,
@@ -674,7 +673,7 @@ __device__ __forceinline__ void recon_col(const T* col, const Prm<T>& P, T& fl, 
 #define MHD_FLUX_STAGED 0
 #endif
 #ifndef MHD_FLUX_MINB
-#define MHD_FLUX_MINB 1
+#define MHD_FLUX_MINB 5
 #endif
 constexpr int TD = MHD_FLUX_TD;
 constexpr int TROWS = TD + 8;
@@ -834,6 +833,11 @@ __global__ void __launch_bounds__(256) k_emf_pdm(Dev<T> d, Inp<T> in, Prm<T> P) 
   constexpr int T1 = (A1 == 0) ? TX : (A1 == 1) ? TY : TZ;
   constexpr int T2 = (A2 == 0) ? TX : (A2 == 1) ? TY : TZ;
   constexpr int NG = TE * T1 * (T2 + 8);
+  // first-pass layout with the x-mapped index contiguous (conflict-free banks)
+  constexpr int R2 = T2 + 8;
+  constexpr int GE = (E == 0) ? 1 : (A1 == 0) ? T1 : R2;
+  constexpr int G1 = (E == 0) ? TE : (A1 == 0) ? 1 : R2 * TE;
+  constexpr int G2 = (E == 0) ? TE * T1 : (A1 == 0) ? T1 * TE : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sv = reinterpret_cast<T*>(smem_raw);  // [2][NV]: v_a1, v_a2
   T* sg = sv + 2 * NV;                     // [2][NG]: first-pass interpolants
@@ -856,12 +860,20 @@ __global__ void __launch_bounds__(256) k_emf_pdm(Dev<T> d, Inp<T> in, Prm<T> P) 
   }
   __syncthreads();
   for (int t = threadIdx.x; t < NG; t += blockDim.x) {
-    const int e = t % TE, r = t / TE, f1 = r % T1, r2 = r / T1;
+    int e, f1, r2;  // decomposed with the x-mapped index fastest
+    if (E == 0) {
+      e = t % TE; const int r = t / TE; f1 = r % T1; r2 = r / T1;
+    } else if (A1 == 0) {
+      f1 = t % T1; const int r = t / T1; e = r % TE; r2 = r / TE;
+    } else {
+      r2 = t % R2; const int r = t / R2; e = r % TE; f1 = r / TE;
+    }
     const int b0 = e * SE + f1 * S1 + r2 * S2;
+    const int gi = e * GE + f1 * G1 + r2 * G2;
 #pragma unroll
     for (int w = 0; w < 2; ++w) {
       const T* a = sv + w * NV + b0;
-      sg[w * NG + t] = tap8(a[0], a[S1], a[2 * S1], a[3 * S1], a[4 * S1], a[5 * S1], a[6 * S1], a[7 * S1]);
+      sg[w * NG + gi] = tap8(a[0], a[S1], a[2 * S1], a[3 * S1], a[4 * S1], a[5 * S1], a[6 * S1], a[7 * S1]);
     }
   }
   __syncthreads();
@@ -880,8 +892,8 @@ __global__ void __launch_bounds__(256) k_emf_pdm(Dev<T> d, Inp<T> in, Prm<T> P) 
     T vav[2];
 #pragma unroll
     for (int w = 0; w < 2; ++w) {
-      const T* gg = sg + w * NG + e + TE * f1 + TE * T1 * f2;
-      constexpr int GS = TE * T1;
+      const T* gg = sg + w * NG + e * GE + f1 * G1 + f2 * G2;
+      constexpr int GS = G2;
       T vi = tap8(gg[0], gg[GS], gg[2 * GS], gg[3 * GS], gg[4 * GS], gg[5 * GS], gg[6 * GS], gg[7 * GS]);
       vav[w] = corner_pdm<T, int>(sv + w * NV, cv, S1, S2, vi, P.pdmb);
     }
@@ -1203,7 +1215,8 @@ void Launch<T>::fill_bxyz(const Dev<T>& d, bool want_vf, cudaStream_t st) {
 
 template <typename T>
 void Launch<T>::cfl(const Dev<T>& d, int mode, cudaStream_t st, bool save) {
-  k_cfl<T><<<152 * 8, 256, 0, st>>>(d, save ? 1 : 0);
+  dim3 grid((d.g.nx + 31) / 32, (d.g.ny + 7) / 8, (d.g.nz + 7) / 8);
+  k_cfl<T><<<grid, 256, 0, st>>>(d, save ? 1 : 0);
   k_cfl_final<T><<<1, 1, 0, st>>>(d, mode);
 }
 
@@ -1289,8 +1302,11 @@ void emf_r(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
   k_emf<T, RECON, 2><<<grid3(g.nx0 + 1, g.ny0 + 1, g.nz0, b), b, 0, st>>>(d, in, P);
 }
 
-// ei tile: 32 x 8 x 8 edges in FP32, 32 x 4 x 4 in FP64 (96 KB of shared memory each)
-template <typename T> struct EiTile { static constexpr int Y = 8; };
+// ei tile: 32 x 4 x 4 edges (48 KB of shared memory in FP32, 96 KB in FP64)
+#ifndef MHD_EI_TILE
+#define MHD_EI_TILE 4
+#endif
+template <typename T> struct EiTile { static constexpr int Y = MHD_EI_TILE; };
 template <> struct EiTile<double> { static constexpr int Y = 4; };
 
 template <typename T>
