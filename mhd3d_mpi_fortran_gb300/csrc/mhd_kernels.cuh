@@ -673,7 +673,7 @@ __device__ __forceinline__ void recon_col(const T* col, const Prm<T>& P, T& fl, 
 #define MHD_FLUX_STAGED 0
 #endif
 #ifndef MHD_FLUX_MINB
-#define MHD_FLUX_MINB 5
+#define MHD_FLUX_MINB 6
 #endif
 constexpr int TD = MHD_FLUX_TD;
 constexpr int TROWS = TD + 8;
@@ -1302,9 +1302,9 @@ void emf_r(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
   k_emf<T, RECON, 2><<<grid3(g.nx0 + 1, g.ny0 + 1, g.nz0, b), b, 0, st>>>(d, in, P);
 }
 
-// ei tile: 32 x 4 x 4 edges (48 KB of shared memory in FP32, 96 KB in FP64)
+// ei tile: 32 x 8 x 8 edges in FP32, 32 x 4 x 4 in FP64 (96 KB of shared memory each)
 #ifndef MHD_EI_TILE
-#define MHD_EI_TILE 4
+#define MHD_EI_TILE 8
 #endif
 template <typename T> struct EiTile { static constexpr int Y = MHD_EI_TILE; };
 template <> struct EiTile<double> { static constexpr int Y = 4; };
