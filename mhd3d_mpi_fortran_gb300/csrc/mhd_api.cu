@@ -203,10 +203,13 @@ void enqueue_step(Handle* h, int& par, cudaStream_t st, Rec* r = nullptr) {
 
 inline void set_widths(Handle* h, Dev<double>& d) {
   d.wx = d.dx; d.wy = d.dy; d.wz = d.dz;
+  d.rwx = d.dx; d.rwy = d.dy; d.rwz = d.dz;
 }
 inline void set_widths(Handle* h, Dev<float>& d) {
   const Geom& g = h->g;
+  const int n = g.nx + g.ny + g.nz;
   d.wx = h->geoT; d.wy = h->geoT + g.nx; d.wz = h->geoT + g.nx + g.ny;
+  d.rwx = h->geoT + n; d.rwy = h->geoT + n + g.nx; d.rwz = h->geoT + n + g.nx + g.ny;
 }
 
 template <typename T>
@@ -418,7 +421,9 @@ int mhd_init(const mhd_params* prm, const double* rho, const double* vx, const d
   if (cudaMemcpy(h->geo, geo.data(), sizeof(double) * geo.size(), cudaMemcpyHostToDevice) != cudaSuccess)
     return bail(MHD_E_CUDA, "geometry upload failed");
   {
+    // FP32 widths and their reciprocals (1/dx computed in FP64, rounded once)
     std::vector<float> gf(geo.begin(), geo.end());
+    for (double v : geo) gf.push_back((float)(1.0 / v));
     if (cudaMalloc(&h->geoT, sizeof(float) * gf.size()) != cudaSuccess ||
         cudaMemcpy(h->geoT, gf.data(), sizeof(float) * gf.size(), cudaMemcpyHostToDevice) != cudaSuccess)
       return bail(MHD_E_NOMEM, "geometry upload failed");

@@ -52,6 +52,22 @@ template <> struct Div<float> {
   static __device__ __forceinline__ float by(float a, float b) { return a * (1.0f / b); }
 };
 
+// Divisions on the hot path: FP64 divides exactly as the reference writes
+// it; FP32 multiplies by a reciprocal (precomputed for the cell widths).
+template <typename T> struct Ops;
+template <> struct Ops<double> {
+  static __device__ __forceinline__ double dw(double a, double w, double) { return a / w; }  // a / width
+  static __device__ __forceinline__ double dv(double a, double b) { return a / b; }
+  static __device__ __forceinline__ double rcp(double b) { return b; }  // used with dvr below
+  static __device__ __forceinline__ double dvr(double a, double b, double) { return a / b; }
+};
+template <> struct Ops<float> {
+  static __device__ __forceinline__ float dw(float a, float, float rw) { return a * rw; }
+  static __device__ __forceinline__ float dv(float a, float b) { return __fdividef(a, b); }
+  static __device__ __forceinline__ float rcp(float b) { return __frcp_rn(b); }
+  static __device__ __forceinline__ float dvr(float a, float, float rb) { return a * rb; }
+};
+
 // 8-point centred interpolant (interp_pdm, mhd3d3.f90:866-872), operand order kept.
 template <typename T>
 __device__ __forceinline__ T tap8(T a0, T a1, T a2, T a3, T a4, T a5, T a6, T a7) {
@@ -532,7 +548,7 @@ __device__ __forceinline__ void face_flux(const T* l, const T* r, T gam, T* out)
     T rl = l[0], ul = l[1], vl = l[2], wl = l[3], pl = l[4], xl = l[5], yl = l[6], zl = l[7];
     T vn = l[1 + D];
     T bn = l[5 + D];
-    T leng = T(0.5) * rl * (ul * ul + vl * vl + wl * wl) + pl / gm1;
+    T leng = T(0.5) * rl * (ul * ul + vl * vl + wl * wl) + Ops<T>::dv(pl, gm1);
     T lam = M::div(rl, T(2) * pl);
     T v0, v1;
     M::hydro(lam, vn, true, v0, v1);
@@ -554,7 +570,7 @@ __device__ __forceinline__ void face_flux(const T* l, const T* r, T gam, T* out)
     T rr = r[0], ur = r[1], vr = r[2], wr = r[3], pr = r[4], xr = r[5], yr = r[6], zr = r[7];
     T vn = r[1 + D];
     T bn = r[5 + D];
-    T leng = T(0.5) * rr * (ur * ur + vr * vr + wr * wr) + pr / gm1;
+    T leng = T(0.5) * rr * (ur * ur + vr * vr + wr * wr) + Ops<T>::dv(pr, gm1);
     T lam = M::div(rr, T(2) * pr);
     T v0, v1;
     M::hydro(lam, vn, false, v0, v1);
@@ -626,9 +642,9 @@ __global__ void k_flux(Dev<T> d, Inp<T> in, Prm<T> P) {
 // form 0: (Xp+X)/den, 1: (c*Xp+X)/den, 2: (Xp+c*X)/den.
 template <typename T>
 __device__ __forceinline__ T comb(int form, T c, T xp, T x, T den) {
-  if (form == 0) return (xp + x) / den;
-  if (form == 1) return (c * xp + x) / den;
-  return (xp + c * x) / den;
+  if (form == 0) return Ops<T>::dv(xp + x, den);
+  if (form == 1) return Ops<T>::dv(c * xp + x, den);
+  return Ops<T>::dv(xp + c * x, den);
 }
 
 // One-sided states from a column of taps in shared memory: tap m (cell
@@ -737,21 +753,22 @@ __global__ void __launch_bounds__(32 * (TD + 1), MHD_FLUX_MINB)
 #pragma unroll
   for (int q = 0; q < 8; ++q) dF[q] = sF[(q * (TD + 1) + r + 1) * 32 + tx] - sF[(q * (TD + 1) + r) * 32 + tx];
   if (D == 1) {
-    const T dx = d.wx[i], dy = d.wy[cd];
+    const T dx = d.wx[i], dy = d.wy[cd], rdx = d.rwx[i], rdy = d.rwy[cd];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) d.dU[q][c] = (d.F[0][q][c + 1] - d.F[0][q][c]) / dx + dF[q] / dy;
+    for (int q = 0; q < 8; ++q)
+      d.dU[q][c] = Ops<T>::dw(d.F[0][q][c + 1] - d.F[0][q][c], dx, rdx) + Ops<T>::dw(dF[q], dy, rdy);
     return;
   }
-  const T dz = d.wz[cd];
+  const T dz = d.wz[cd], rdz = d.rwz[cd];
   const T tau = (T)d.sc->tau;
   const T gm1 = d.gam - T(1);
   T dv[8];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) dv[q] = d.dU[q][c] + dF[q] / dz;
+  for (int q = 0; q < 8; ++q) dv[q] = d.dU[q][c] + Ops<T>::dw(dF[q], dz, rdz);
   // get_conserve of the current state (AB: the state, not the prediction)
   T rr = d.rho[c], u = d.vx[c], v = d.vy[c], ww = d.vz[c], pr = d.p[c];
   T rvx0 = rr * u, rvy0 = rr * v, rvz0 = rr * ww;
-  T eng0 = T(0.5) * rr * (u * u + v * v + ww * ww) + pr / gm1;
+  T eng0 = T(0.5) * rr * (u * u + v * v + ww * ww) + Ops<T>::dv(pr, gm1);
   T rho1 = rr - tau * dv[0];
   T eng1 = eng0 - tau * dv[4];
   T rx = rvx0 - tau * dv[1], ry = rvy0 - tau * dv[2], rz = rvz0 - tau * dv[3];
@@ -763,7 +780,8 @@ __global__ void __launch_bounds__(32 * (TD + 1), MHD_FLUX_MINB)
     hz = comb(form, cw, d.q[3][c], rz, den);
     eng1 = comb(form, cw, d.q[4][c], eng1, den);
   }
-  T pn = gm1 * (eng1 - T(0.5) * (hx * hx + hy * hy + hz * hz) / rho1);
+  const T rrho = Ops<T>::rcp(rho1);
+  T pn = gm1 * (eng1 - Ops<T>::dvr(T(0.5) * (hx * hx + hy * hy + hz * hz), rho1, rrho));
   rx = rx - tau * dv[5];
   ry = ry - tau * dv[6];
   rz = rz - tau * dv[7];
@@ -774,9 +792,9 @@ __global__ void __launch_bounds__(32 * (TD + 1), MHD_FLUX_MINB)
   }
   d.orho[c] = rho1;
   d.op[c] = pn;
-  d.ovx[c] = rx / rho1;
-  d.ovy[c] = ry / rho1;
-  d.ovz[c] = rz / rho1;
+  d.ovx[c] = Ops<T>::dvr(rx, rho1, rrho);
+  d.ovy[c] = Ops<T>::dvr(ry, rho1, rrho);
+  d.ovz[c] = Ops<T>::dvr(rz, rho1, rrho);
   (void)ab;
 }
 
@@ -846,34 +864,52 @@ __global__ void __launch_bounds__(256) k_emf_pdm(Dev<T> d, Inp<T> in, Prm<T> P) 
   const T* vel[3] = {in.vx, in.vy, in.vz};
   const T* v1 = vel[A1];
   const T* v2 = vel[A2];
-  for (int t = threadIdx.x; t < NV; t += blockDim.x) {
-    const int lx = t % SX, r = t / SX, ly = r % SY, lz = r / SY;
-    const int gx = ox - HX + lx, gy = oy - HY + ly, gz = oz - HZ + lz;
-    T a = T(0), b = T(0);
-    if (gx < g.nx && gy < g.ny && gz < g.nz) {
-      const int c = gx + g.px * (gy + g.py * gz);
-      a = v1[c];
-      b = v2[c];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  // stage v_a1, v_a2: warps over (y, z) rows, lanes over x
+  for (int row = warp; row < SY * SZ; row += nwarp) {
+    const int ly = row % SY, lz = row / SY;
+    const int gy = oy - HY + ly, gz = oz - HZ + lz;
+    const bool rowok = gy < g.ny && gz < g.nz;
+    const int gb = g.px * (gy + g.py * gz) + ox - HX;
+#pragma unroll
+    for (int xx = 0; xx < SX; xx += 32) {
+      const int lx = xx + lane;
+      if (lx < SX) {
+        T a = T(0), b = T(0);
+        if (rowok && ox - HX + lx < g.nx) {
+          a = v1[gb + lx];
+          b = v2[gb + lx];
+        }
+        sv[row * SX + lx] = a;
+        sv[NV + row * SX + lx] = b;
+      }
     }
-    sv[t] = a;
-    sv[NV + t] = b;
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < NG; t += blockDim.x) {
-    int e, f1, r2;  // decomposed with the x-mapped index fastest
-    if (E == 0) {
-      e = t % TE; const int r = t / TE; f1 = r % T1; r2 = r / T1;
-    } else if (A1 == 0) {
-      f1 = t % T1; const int r = t / T1; e = r % TE; r2 = r / TE;
-    } else {
-      r2 = t % R2; const int r = t / R2; e = r % TE; f1 = r / TE;
-    }
-    const int b0 = e * SE + f1 * S1 + r2 * S2;
-    const int gi = e * GE + f1 * G1 + r2 * G2;
+  // first pass of interp2_pdm: lanes over the x-mapped index of (e, f1, r2)
+  constexpr int NX = (E == 0) ? TE : (A1 == 0) ? T1 : R2;   // x-mapped extent
+  constexpr int NR = NG / NX;                                // remaining (row) extent
+  for (int row = warp; row < NR; row += nwarp) {
 #pragma unroll
-    for (int w = 0; w < 2; ++w) {
-      const T* a = sv + w * NV + b0;
-      sg[w * NG + gi] = tap8(a[0], a[S1], a[2 * S1], a[3 * S1], a[4 * S1], a[5 * S1], a[6 * S1], a[7 * S1]);
+    for (int xx = 0; xx < NX; xx += 32) {
+      const int ix = xx + lane;
+      if (ix < NX) {
+        int e, f1, r2;
+        if (E == 0) {
+          e = ix; f1 = row % T1; r2 = row / T1;
+        } else if (A1 == 0) {
+          f1 = ix; e = row % TE; r2 = row / TE;
+        } else {
+          r2 = ix; e = row % TE; f1 = row / TE;
+        }
+        const int b0 = e * SE + f1 * S1 + r2 * S2;
+        const int gi = e * GE + f1 * G1 + r2 * G2;
+#pragma unroll
+        for (int w = 0; w < 2; ++w) {
+          const T* a = sv + w * NV + b0;
+          sg[w * NG + gi] = tap8(a[0], a[S1], a[2 * S1], a[3 * S1], a[4 * S1], a[5 * S1], a[6 * S1], a[7 * S1]);
+        }
+      }
     }
   }
   __syncthreads();
@@ -948,19 +984,21 @@ __global__ void k_update_b(Dev<T> d, int form, T cw, T den) {
   const long long sy = g.px, sz = g.plane;
   const T tau = (T)d.sc->tau;
   const T dx = d.wx[i], dy = d.wy[j], dz = d.wz[k];
+  const T rx = d.rwx[i], ry = d.rwy[j], rz = d.rwz[k];
   const T *ei = d.E[0], *ej = d.E[1], *ek = d.E[2];
+  typedef Ops<T> O;
   if (in_y && in_z) {
-    T b = d.bi[c] - tau * ((ek[c + sy] - ek[c]) / dy - (ej[c + sz] - ej[c]) / dz);
+    T b = d.bi[c] - tau * (O::dw(ek[c + sy] - ek[c], dy, ry) - O::dw(ej[c + sz] - ej[c], dz, rz));
     if (form >= 0) b = comb(form, cw, d.q[5][c], b, den);
     d.bi[c] = b;
   }
   if (in_x && in_z) {
-    T b = d.bj[c] - tau * ((ei[c + sz] - ei[c]) / dz - (ek[c + 1] - ek[c]) / dx);
+    T b = d.bj[c] - tau * (O::dw(ei[c + sz] - ei[c], dz, rz) - O::dw(ek[c + 1] - ek[c], dx, rx));
     if (form >= 0) b = comb(form, cw, d.q[6][c], b, den);
     d.bj[c] = b;
   }
   if (in_x && in_y) {
-    T b = d.bk[c] - tau * ((ej[c + 1] - ej[c]) / dx - (ei[c + sy] - ei[c]) / dy);
+    T b = d.bk[c] - tau * (O::dw(ej[c + 1] - ej[c], dx, rx) - O::dw(ei[c + sy] - ei[c], dy, ry));
     if (form >= 0) b = comb(form, cw, d.q[7][c], b, den);
     d.bk[c] = b;
   }

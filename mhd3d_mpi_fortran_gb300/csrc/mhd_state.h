@@ -53,6 +53,7 @@ struct Dev {
   T* vf;       // |v| + |B|/sqrt(rho) of the stage input
   const double *dx, *dy, *dz;  // FP64 cell widths (ghost-inclusive, 1-D)
   const T *wx, *wy, *wz;       // the same widths in T (FP32 path: converted once)
+  const T *rwx, *rwy, *rwz;    // reciprocal widths (FP32 path; unused in FP64)
   Scal* sc;
   unsigned int* partial;       // per-block scratch of the CFL reduction
   unsigned int* counter;
