@@ -152,6 +152,35 @@ int mhd_debug_fluxes(void* handle, double* out);
  * ei (nx0,ny0+1,nz0+1), ej (nx0+1,ny0,nz0+1), ek (nx0+1,ny0+1,nz0). */
 int mhd_debug_emf(void* handle, double* ei, double* ej, double* ek);
 
+/* ---- allocation-free diagnostics (no counterpart in the reference) ----
+ *
+ * For callers that cannot allocate device memory when they need the
+ * diagnostics: a driver whose device memory is all owned by its own pool, a
+ * latency-critical loop that must not take the implicit device
+ * synchronisation of cudaMalloc/cudaFree, or a process capped by MPS/MIG
+ * limits.  Same five outputs as mhd_diagnostics, computed from arrays the
+ * caller already holds on the device; the call allocates nothing.
+ *
+ * All array arguments are DEVICE pointers to FP64, ghost-inclusive, Fortran-
+ * ordered arrays of the layout mhd_init takes from the host (cell arrays
+ * (nx,ny,nz), bi (nx+1,ny,nz), bj (nx,ny+1,nz), bk (nx,ny,nz+1); dx/dy/dz of
+ * length nx/ny/nz).  Only nx0, ny0, nz0, nord, gam and cfl of *prm are read.
+ * out is a DEVICE pointer to 5 doubles, written on `stream` (a cudaStream_t,
+ * NULL for the legacy default stream); the call returns without waiting.
+ *
+ * Scratch: a file-scope device array of 2048 x 7 doubles (112 KB) that every
+ * GPU loading this library keeps until the process exits; grids with more
+ * than 2048 z planes (nz0 + nord) are rejected with MHD_E_ARG.  All calls share
+ * that array, so calls whose kernels overlap on the GPU (different streams,
+ * or other host threads, on the same device) race: order them on one stream.
+ * The first call on each device looks up the array's device address with
+ * that device current; make that first call before any stream capture. */
+int mhd_diagnostics_noalloc(const mhd_params* prm, const double* rho, const double* vx,
+                            const double* vy, const double* vz, const double* p,
+                            const double* bi, const double* bj, const double* bk,
+                            const double* dx, const double* dy, const double* dz,
+                            double* out, void* stream);
+
 /* ---- batched ensemble of independent grids -------------------------- */
 
 /* Advance `ngrids` independent solvers (created by mhd_init, same precision,

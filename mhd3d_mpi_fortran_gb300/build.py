@@ -1,11 +1,12 @@
 """In-tree build of the GB300 shared library ``_lib/libmhdgpu.so``.
 
-Three translation units are compiled in parallel with nvcc for sm_103a and
+The translation units are compiled in parallel with nvcc for sm_103a and
 linked into one C-ABI library (declared in ``include/mhd_gpu.h``):
 
 * ``csrc/mhd_fp64.cu`` -- FP64 kernels, ``-fmad=false`` (reference rounding),
 * ``csrc/mhd_fp32.cu`` -- FP32 kernels (FMA contraction on),
-* ``csrc/mhd_api.cu``  -- host sequencing and the ``extern "C"`` entry points.
+* ``csrc/mhd_api.cu``  -- host sequencing and the ``extern "C"`` entry points,
+* ``csrc/mhd_noalloc.cu`` -- the allocation-free diagnostics entry point.
 
 Usage: ``python -m mhd3d_mpi_fortran_gb300.build`` (or ``build()``).
 """
@@ -33,6 +34,7 @@ UNITS = {
     "mhd_fp64": ["-fmad=false"],
     "mhd_fp32": ["-fmad=true"],
     "mhd_api": [],
+    "mhd_noalloc": ["-fmad=false"],
 }
 
 

@@ -369,6 +369,8 @@ int validate(const mhd_params* p) {
 
 }  // namespace
 
+void mhd::set_last_error(const std::string& msg) { g_err = msg; }
+
 // Entry points: C linkage comes from their declarations in mhd_gpu.h.
 
 const char* mhd_last_error(void) { return g_err.c_str(); }

@@ -4,8 +4,12 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string>
 
 namespace mhd {
+
+// Text returned by mhd_last_error() on this thread (library-internal).
+__attribute__((visibility("hidden"))) void set_last_error(const std::string& msg);
 
 // Ghost-inclusive grid.  Cell arrays have (nx,ny,nz) elements, face arrays one
 // more along their own axis; every array of a handle uses the same padded
