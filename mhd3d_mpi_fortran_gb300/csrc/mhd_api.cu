@@ -66,6 +66,7 @@ struct Handle {
   std::vector<int> fam;
   int par = 0;                 // which half of the double-buffered primitives is current
   float* geoT = nullptr;       // FP32 copy of the cell widths
+  int* gmap = nullptr;         // ghost-image tables
   // graphs keyed by (nsteps, starting parity) -> (exec, parity after replay)
   std::map<std::pair<int, int>, std::pair<cudaGraphExec_t, int>> graphs;
 };
@@ -240,6 +241,7 @@ void carve(Handle* h, Dev<T>& d, char* base) {
   d.dx = h->geo; d.dy = h->geo + g.nx; d.dz = h->geo + g.nx + g.ny;
   set_widths(h, d);
   d.sc = h->sc;
+  d.gmap = h->gmap;
   d.partial = nullptr;
   d.counter = nullptr;
 }
@@ -371,6 +373,32 @@ int validate(const mhd_params* p) {
 
 void mhd::set_last_error(const std::string& msg) { g_err = msg; }
 
+// Host twin of the device ghost_src: image of index x on an axis with n0
+// interior cells (cell axis) or n0+1 interior faces (face axis).
+static int host_ghost_src(int x, int ng, int n0, bool face, int kind) {
+  const int hi = face ? ng + n0 : ng + n0 - 1;
+  if (x >= ng && x <= hi) return x;
+  const bool lo = x < ng;
+  if (kind == MHD_BC_PERIODIC) return lo ? x + n0 : x - n0;
+  if (kind == MHD_BC_OUTFLOW) return lo ? ng : hi;
+  if (!face) return lo ? 2 * ng - 1 - x : 2 * n0 + 2 * ng - 1 - x;
+  return lo ? 2 * ng - x : 2 * n0 + 2 * ng - x;
+}
+
+std::vector<int> mhd::ghost_maps(int nx0, int ny0, int nz0, int ng, const int bc[3]) {
+  const int n0[3] = {nx0, ny0, nz0};
+  std::vector<int> m;
+  for (int face = 0; face < 2; ++face)
+    for (int a = 0; a < 3; ++a) {
+      const int n = n0[a] + 2 * ng;  // cells incl. ghosts; faces are n+1
+      for (int x = 0; x < n + 2; ++x) {
+        const bool valid = face ? x <= n : x < n;
+        m.push_back(valid ? host_ghost_src(x, ng, n0[a], face != 0, bc[a]) : 0);
+      }
+    }
+  return m;
+}
+
 // Entry points: C linkage comes from their declarations in mhd_gpu.h.
 
 const char* mhd_last_error(void) { return g_err.c_str(); }
@@ -429,6 +457,12 @@ int mhd_init(const mhd_params* prm, const double* rho, const double* vx, const d
     if (cudaMalloc(&h->geoT, sizeof(float) * gf.size()) != cudaSuccess ||
         cudaMemcpy(h->geoT, gf.data(), sizeof(float) * gf.size(), cudaMemcpyHostToDevice) != cudaSuccess)
       return bail(MHD_E_NOMEM, "geometry upload failed");
+  }
+  {
+    std::vector<int> gm = mhd::ghost_maps(g.nx0, g.ny0, g.nz0, g.ng, prm->bc);
+    if (cudaMalloc(&h->gmap, sizeof(int) * gm.size()) != cudaSuccess ||
+        cudaMemcpy(h->gmap, gm.data(), sizeof(int) * gm.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+      return bail(MHD_E_NOMEM, "ghost map upload failed");
   }
   Scal s{};
   s.tau = prm->tau;
@@ -754,6 +788,7 @@ int mhd_free(void* handle) {
   if (h->buf) cudaFree(h->buf);
   if (h->geo) cudaFree(h->geo);
   if (h->geoT) cudaFree(h->geoT);
+  if (h->gmap) cudaFree(h->gmap);
   if (h->sc) cudaFree(h->sc);
   if (h->diag) cudaFree(h->diag);
   if (h->sc_h) cudaFreeHost(h->sc_h);

@@ -333,16 +333,20 @@ __global__ void k_bxyz_vf(Dev<T> d, int want_vf) {
 // get_dt over all cells incl. ghosts: per-block min, then atomicMin on the
 // bit pattern (positive doubles order like their bits).  Status bits mirror
 // diag_rho_neg / diag_overflow.
+// Fast square root for the FP32 CFL estimate; exact in FP64.
+__device__ __forceinline__ double cfl_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float cfl_sqrt(float x) { return x > 0.0f ? x * rsqrtf(x) : 0.0f; }
+
 // save != 0 also stores U^n of the RK stage combines (advance_previous,
 // 3794-3819) at interior cells and faces, the only places they are read.
+// The minimum is reduced in T and converted to FP64 once per block.
 template <typename T>
-__global__ void k_cfl(Dev<T> d, int save) {
+__global__ void __launch_bounds__(256) k_cfl(Dev<T> d, int save) {
   const Geom& g = d.g;
-  long long n = (long long)g.nx * g.ny * g.nz;
-  double m = INFINITY;
+  T m = T(INFINITY);
   unsigned st = 0;
   const T gm1 = d.gam - T(1);
-  (void)n;
+  typedef Ops<T> O;
   const int i = blockIdx.x * 32 + (threadIdx.x & 31);
   const int j = blockIdx.y * 8 + (threadIdx.x >> 5);
   const int k1 = min(g.nz, (int)(blockIdx.z + 1) * 8);
@@ -358,7 +362,7 @@ __global__ void k_cfl(Dev<T> d, int save) {
         d.q[1][c] = r0 * u;
         d.q[2][c] = r0 * v;
         d.q[3][c] = r0 * w;
-        d.q[4][c] = T(0.5) * r0 * (u * u + v * v + w * w) + p0 / gm1;
+        d.q[4][c] = T(0.5) * r0 * (u * u + v * v + w * w) + O::dv(p0, gm1);
       }
       const bool fx = i >= g.ng && i <= g.ng + g.nx0, fy = j >= g.ng && j <= g.ng + g.ny0,
                  fz = k >= g.ng && k <= g.ng + g.nz0;
@@ -366,44 +370,39 @@ __global__ void k_cfl(Dev<T> d, int save) {
       if (ix && fy && iz) d.q[6][c] = d.bj[c];
       if (ix && iy && fz) d.q[7][c] = d.bk[c];
     }
+    // get_dt (mhd3d3.f90:1608-1639)
     T a = d.bx[c], b = d.by[c], cc = d.bz[c];
-    T vv = sq(u * u + v * v + w * w);
-    T btot = sq(a * a + b * b + cc * cc);
-    T valf = btot / sq(r0);
-    T vs = sq(d.gam * p0 / r0);
-    T vcfl = vv + sq(valf * valf + vs * vs);
-    T dt = d.cfl / (vcfl / d.wx[i] + vcfl / d.wy[j] + vcfl / d.wz[k]);
-    double dtd = (double)dt;
-    m = (dtd < m) ? dtd : m;
+    T vv = cfl_sqrt(u * u + v * v + w * w);
+    T btot = cfl_sqrt(a * a + b * b + cc * cc);
+    T valf = O::dv(btot, cfl_sqrt(r0));
+    T vs = cfl_sqrt(O::dv(d.gam * p0, r0));
+    T vcfl = vv + cfl_sqrt(valf * valf + vs * vs);
+    T dt = O::dv(d.cfl, O::dw(vcfl, d.wx[i], d.rwx[i]) + O::dw(vcfl, d.wy[j], d.rwy[j]) +
+                            O::dw(vcfl, d.wz[k], d.rwz[k]));
+    m = (dt < m) ? dt : m;
     if (isnan(r0) || isnan(p0) || isnan(u) || isnan(v) || isnan(w)) st |= ST_NAN;
     if (r0 < T(0)) st |= ST_NEG_RHO;
     if (p0 < T(0)) st |= ST_NEG_P;
     if (isnan(dt)) st |= ST_NAN;
   }
-  // warp then block reduction
   for (int o = 16; o > 0; o >>= 1) {
-    double y = __shfl_xor_sync(0xffffffffu, m, o);
+    T y = __shfl_xor_sync(0xffffffffu, m, o);
     m = (y < m) ? y : m;
     st |= __shfl_xor_sync(0xffffffffu, st, o);
   }
-  __shared__ double sm[32];
-  __shared__ unsigned ss[32];
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __shared__ T sm[8];
+  __shared__ unsigned ss[8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0) { sm[wid] = m; ss[wid] = st; }
   __syncthreads();
-  if (wid == 0) {
-    int nw = blockDim.x >> 5;
-    m = (lane < nw) ? sm[lane] : INFINITY;
-    st = (lane < nw) ? ss[lane] : 0u;
-    for (int o = 16; o > 0; o >>= 1) {
-      double y = __shfl_xor_sync(0xffffffffu, m, o);
-      m = (y < m) ? y : m;
-      st |= __shfl_xor_sync(0xffffffffu, st, o);
+  if (threadIdx.x == 0) {
+    for (int w2 = 1; w2 < 8; ++w2) {
+      m = (sm[w2] < m) ? sm[w2] : m;
+      st |= ss[w2];
     }
-    if (lane == 0) {
-      if (m >= 0.0) atomicMin(&d.sc->dtmin_bits, (unsigned long long)__double_as_longlong(m));
-      if (st) atomicOr(&d.sc->status, st);
-    }
+    const double md = (double)m;
+    if (md >= 0.0) atomicMin(&d.sc->dtmin_bits, (unsigned long long)__double_as_longlong(md));
+    if (st) atomicOr(&d.sc->status, st);
   }
 }
 
@@ -838,8 +837,8 @@ __global__ void k_emf(Dev<T> d, Inp<T> in, Prm<T> P) {
 // into shared memory, and each edge then takes the second pass along a2, the
 // limiters (corner_pdm), the upwinded face-B reconstructions and the Alfven
 // resistivity term exactly as k_emf does.  Tile (TX, TY, TZ) in edges.
-template <typename T, int E, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(256) k_emf_pdm(Dev<T> d, Inp<T> in, Prm<T> P) {
+template <typename T, int E, int TX, int TY, int TZ, int NT>
+__global__ void __launch_bounds__(NT) k_emf_pdm(Dev<T> d, Inp<T> in, Prm<T> P) {
   constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
   constexpr int HX = (E == 0) ? 0 : 4, HY = (E == 1) ? 0 : 4, HZ = (E == 2) ? 0 : 4;
   constexpr int SX = TX + 2 * HX, SY = TY + 2 * HY, SZ = TZ + 2 * HZ;
@@ -949,7 +948,7 @@ __global__ void __launch_bounds__(256) k_emf_pdm(Dev<T> d, Inp<T> in, Prm<T> P) 
   }
 }
 
-template <typename T, int E, int TX, int TY, int TZ>
+template <typename T, int E, int TX, int TY, int TZ, int NT>
 void launch_emf_pdm(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStream_t st) {
   constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
   constexpr int HX = (E == 0) ? 0 : 4, HY = (E == 1) ? 0 : 4, HZ = (E == 2) ? 0 : 4;
@@ -961,13 +960,13 @@ void launch_emf_pdm(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStre
   constexpr size_t bytes = sizeof(T) * (2 * NV + 2 * NG);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_emf_pdm<T, E, TX, TY, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaFuncSetAttribute(k_emf_pdm<T, E, TX, TY, TZ, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     attr = true;
   }
   const Geom& g = d.g;
   const int ex = g.nx0 + (E != 0), ey = g.ny0 + (E != 1), ez = g.nz0 + (E != 2);
   dim3 grid((ex + TX - 1) / TX, (ey + TY - 1) / TY, (ez + TZ - 1) / TZ);
-  k_emf_pdm<T, E, TX, TY, TZ><<<grid, 256, bytes, st>>>(d, in, P);
+  k_emf_pdm<T, E, TX, TY, TZ, NT><<<grid, NT, bytes, st>>>(d, in, P);
 }
 
 // ------------------------------------------------------------------ update
@@ -1062,56 +1061,51 @@ __global__ void k_fill(Dev<T> d) {
 // B and vf of its cell from the ghost images of the faces and cells it needs,
 // so no thread reads an element another thread is filling.  Face B is even
 // under every boundary kind and vf uses only squares, so the images give
-// exactly the values the separate fill followed by get_bxyz produces.
+// exactly the values the separate fill followed by get_bxyz produces.  The
+// per-axis image of every index comes from d.gmap (ghost_src tabulated at
+// set-up): cell maps of x, y, z then face maps of x, y, z, each padded to n+2.
 template <typename T>
-__global__ void k_fill_bxyz(Dev<T> d, int want_vf) {
+__global__ void __launch_bounds__(256) k_fill_bxyz(Dev<T> d, int want_vf) {
   const Geom& g = d.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  int j = blockIdx.y * blockDim.y + threadIdx.y;
-  int k = blockIdx.z;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
   if (i > g.nx || j > g.ny || k > g.nz) return;
-  T* arr[8] = {d.rho, d.vx, d.vy, d.vz, d.p, d.bi, d.bj, d.bk};
-  const int n0[3] = {g.nx0, g.ny0, g.nz0};
-  const int x3[3] = {i, j, k};
-  bool fl;
-  int sc[3], sf[3], sf1[3];
-#pragma unroll
-  for (int ax = 0; ax < 3; ++ax) {
-    sc[ax] = ghost_src(x3[ax], g.ng, n0[ax], false, d.bc[ax], fl);
-    sf[ax] = ghost_src(x3[ax], g.ng, n0[ax], true, d.bc[ax], fl);
-    sf1[ax] = ghost_src(x3[ax] + 1, g.ng, n0[ax], true, d.bc[ax], fl);
+  const int* cx = d.gmap;
+  const int* cy = cx + g.nx + 2;
+  const int* cz = cy + g.ny + 2;
+  const int* fx = cz + g.nz + 2;
+  const int* fy = fx + g.nx + 2;
+  const int* fz = fy + g.ny + 2;
+  const int sci = cx[i], scj = cy[j], sck = cz[k];  // cell images (entries n, n+1 unused)
+  const int sfi = fx[i], sfj = fy[j], sfk = fz[k];  // face images
+  const int px = g.px, pl = (int)g.plane;
+  const int c = i + px * j + pl * k;
+  const bool cin = i < g.nx && j < g.ny && k < g.nz;
+  // ghost copies: cell arrays (rho, vx, vy, vz, p), then bi, bj, bk
+  const bool gx = sci != i, gy = scj != j, gz = sck != k;
+  if (cin && (gx || gy || gz)) {
+    const int sc = sci + px * scj + pl * sck;
+    d.rho[c] = d.rho[sc];
+    d.p[c] = d.p[sc];
+    const T ux = d.vx[sc], uy = d.vy[sc], uz = d.vz[sc];
+    d.vx[c] = (gx && d.bc[0] == BC_REFLECT) ? -ux : ux;
+    d.vy[c] = (gy && d.bc[1] == BC_REFLECT) ? -uy : uy;
+    d.vz[c] = (gz && d.bc[2] == BC_REFLECT) ? -uz : uz;
   }
-  const long long c = idx3<T>(g, i, j, k);
-#pragma unroll
-  for (int a = 0; a < 8; ++a) {
-    const int fa = a - 5;
-    bool ghost = false, inside = true;
-    int s3[3];
-    T sgn = T(1);
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-      const bool face = (fa == ax);
-      const int ext = (ax == 0 ? g.nx : ax == 1 ? g.ny : g.nz) + (face ? 1 : 0);
-      if (x3[ax] >= ext) inside = false;
-      s3[ax] = face ? sf[ax] : sc[ax];
-      if (s3[ax] != x3[ax]) {
-        ghost = true;
-        if (d.bc[ax] == BC_REFLECT && a == 1 + ax) sgn = -sgn;
-      }
-    }
-    if (!inside || !ghost) continue;
-    const T val = arr[a][idx3<T>(g, s3[0], s3[1], s3[2])];
-    arr[a][c] = (sgn > T(0)) ? val : -val;
-  }
-  if (i >= g.nx || j >= g.ny || k >= g.nz) return;
-  const T bx = T(0.5) * (d.bi[idx3<T>(g, sf1[0], sc[1], sc[2])] + d.bi[idx3<T>(g, sf[0], sc[1], sc[2])]);
-  const T by = T(0.5) * (d.bj[idx3<T>(g, sc[0], sf1[1], sc[2])] + d.bj[idx3<T>(g, sc[0], sf[1], sc[2])]);
-  const T bz = T(0.5) * (d.bk[idx3<T>(g, sc[0], sc[1], sf1[2])] + d.bk[idx3<T>(g, sc[0], sc[1], sf[2])]);
+  if (j < g.ny && k < g.nz && (sfi != i || gy || gz)) d.bi[c] = d.bi[sfi + px * scj + pl * sck];
+  if (i < g.nx && k < g.nz && (gx || sfj != j || gz)) d.bj[c] = d.bj[sci + px * sfj + pl * sck];
+  if (i < g.nx && j < g.ny && (gx || gy || sfk != k)) d.bk[c] = d.bk[sci + px * scj + pl * sfk];
+  if (!cin) return;
+  const int cyz = px * scj + pl * sck;
+  const T bx = T(0.5) * (d.bi[fx[i + 1] + cyz] + d.bi[sfi + cyz]);
+  const T by = T(0.5) * (d.bj[sci + px * fy[j + 1] + pl * sck] + d.bj[sci + px * sfj + pl * sck]);
+  const T bz = T(0.5) * (d.bk[sci + px * scj + pl * fz[k + 1]] + d.bk[sci + px * scj + pl * sfk]);
   d.bx[c] = bx;
   d.by[c] = by;
   d.bz[c] = bz;
   if (want_vf) {
-    const long long s = idx3<T>(g, sc[0], sc[1], sc[2]);
+    const int s = sci + cyz;
     const T u = d.vx[s], v = d.vy[s], w = d.vz[s];
     d.vf[c] = sq(u * u + v * v + w * w) + sq((bx * bx + by * by + bz * bz) / d.rho[s]);
   }
@@ -1351,9 +1345,9 @@ template <typename T>
 void Launch<T>::emf(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
   if (d.recon == R_PDM) {
     Prm<T> P = prm_of(d);
-    launch_emf_pdm<T, 0, 32, EiTile<T>::Y, EiTile<T>::Y>(d, in, P, st);
-    launch_emf_pdm<T, 1, 32, 1, 8>(d, in, P, st);
-    launch_emf_pdm<T, 2, 32, 8, 1>(d, in, P, st);
+    launch_emf_pdm<T, 0, 32, EiTile<T>::Y, EiTile<T>::Y, 512>(d, in, P, st);
+    launch_emf_pdm<T, 1, 32, 1, 8, 256>(d, in, P, st);
+    launch_emf_pdm<T, 2, 32, 8, 1, 256>(d, in, P, st);
     return;
   }
   switch (d.recon) {

@@ -5,8 +5,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <vector>
 
 namespace mhd {
+
+// Per-axis ghost-image tables for the fused fill (host side of ghost_src).
+std::vector<int> ghost_maps(int nx0, int ny0, int nz0, int ng, const int bc[3]);
 
 // Text returned by mhd_last_error() on this thread (library-internal).
 __attribute__((visibility("hidden"))) void set_last_error(const std::string& msg);
@@ -59,6 +63,7 @@ struct Dev {
   const T *wx, *wy, *wz;       // the same widths in T (FP32 path: converted once)
   const T *rwx, *rwy, *rwz;    // reciprocal widths (FP32 path; unused in FP64)
   Scal* sc;
+  const int* gmap;             // per-axis ghost-image tables (cell x,y,z; face x,y,z), each n+2
   unsigned int* partial;       // per-block scratch of the CFL reduction
   unsigned int* counter;
 };
