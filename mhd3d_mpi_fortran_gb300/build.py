@@ -33,7 +33,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "mhd_fp64": ["-fmad=false"],
     "mhd_fp32": ["-fmad=true"],
-    "mhd_api": [],
+    "mhd_api": ["-Xcompiler", "-fopenmp"],
     "mhd_noalloc": ["-fmad=false"],
 }
 
@@ -78,7 +78,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose), UNITS.items()))
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-Xcompiler", "-fopenmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

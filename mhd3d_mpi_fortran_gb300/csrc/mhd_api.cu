@@ -251,9 +251,10 @@ size_t n_arrays(const mhd_params& p) {
   return n;
 }
 
-// host FP64 Fortran array (ex,ey,ez) <-> device padded T
+// host FP64 Fortran array (ex,ey,ez) <-> device padded T; rows in parallel
 template <typename T>
 void pack(const Geom& g, const double* src, int ex, int ey, int ez, T* dst) {
+#pragma omp parallel for schedule(static)
   for (int k = 0; k < ez; ++k)
     for (int j = 0; j < ey; ++j) {
       const double* s = src + (size_t)ex * ((size_t)j + (size_t)ey * k);
@@ -263,6 +264,7 @@ void pack(const Geom& g, const double* src, int ex, int ey, int ez, T* dst) {
 }
 template <typename T>
 void unpack(const Geom& g, const T* src, int ex, int ey, int ez, double* dst) {
+#pragma omp parallel for schedule(static)
   for (int k = 0; k < ez; ++k)
     for (int j = 0; j < ey; ++j) {
       const T* s = src + (size_t)g.px * ((size_t)j + (size_t)g.py * k);
@@ -271,6 +273,9 @@ void unpack(const Geom& g, const T* src, int ex, int ey, int ez, double* dst) {
     }
 }
 
+// Two pinned staging buffers: packing array a+1 overlaps the copy of array a.
+// Padding elements are never read by the kernels, so the device buffer
+// (zeroed at allocation) supplies them and only the extents are copied.
 template <typename T>
 int upload(Handle* h, const double* const* arrs) {
   const Geom& g = h->g;
@@ -279,20 +284,38 @@ int upload(Handle* h, const double* const* arrs) {
   int ext[8][3] = {{g.nx, g.ny, g.nz}, {g.nx, g.ny, g.nz}, {g.nx, g.ny, g.nz}, {g.nx, g.ny, g.nz},
                    {g.nx, g.ny, g.nz}, {g.nx + 1, g.ny, g.nz}, {g.nx, g.ny + 1, g.nz},
                    {g.nx, g.ny, g.nz + 1}};
-  T* stage = nullptr;
-  CK(cudaMallocHost(&stage, (size_t)g.vol * sizeof(T)));
-  for (int a = 0; a < 8; ++a) {
-    std::memset(stage, 0, (size_t)g.vol * sizeof(T));
-    pack<T>(g, arrs[a], ext[a][0], ext[a][1], ext[a][2], stage);
-    cudaError_t e = cudaMemcpyAsync(dsts[a], stage, (size_t)g.vol * sizeof(T), cudaMemcpyHostToDevice, h->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
-    if (e != cudaSuccess) {
-      cudaFreeHost(stage);
-      return fail(MHD_E_CUDA, std::string("upload: ") + cudaGetErrorString(e));
-    }
+  T* stage[2] = {nullptr, nullptr};
+  cudaEvent_t done[2];
+  CK(cudaMallocHost(&stage[0], (size_t)g.vol * sizeof(T)));
+  if (cudaMallocHost(&stage[1], (size_t)g.vol * sizeof(T)) != cudaSuccess) {
+    cudaFreeHost(stage[0]);
+    return fail(MHD_E_NOMEM, "pinned staging allocation failed");
   }
-  cudaFreeHost(stage);
-  return MHD_OK;
+  std::memset(stage[0], 0, (size_t)g.vol * sizeof(T));
+  std::memset(stage[1], 0, (size_t)g.vol * sizeof(T));
+  cudaEventCreateWithFlags(&done[0], cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&done[1], cudaEventDisableTiming);
+  int rc = MHD_OK;
+  for (int a = 0; a < 8 && rc == MHD_OK; ++a) {
+    const int b = a & 1;
+    if (a >= 2) {
+      cudaError_t e = cudaEventSynchronize(done[b]);
+      if (e != cudaSuccess) rc = fail(MHD_E_CUDA, std::string("upload: ") + cudaGetErrorString(e));
+    }
+    if (rc) break;
+    pack<T>(g, arrs[a], ext[a][0], ext[a][1], ext[a][2], stage[b]);
+    const size_t bytes = ((size_t)ext[a][2] - 1) * g.plane * sizeof(T) +
+                         ((size_t)(ext[a][1] - 1) * g.px + ext[a][0]) * sizeof(T);
+    cudaError_t e = cudaMemcpyAsync(dsts[a], stage[b], bytes, cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) e = cudaEventRecord(done[b], h->st);
+    if (e != cudaSuccess) rc = fail(MHD_E_CUDA, std::string("upload: ") + cudaGetErrorString(e));
+  }
+  if (rc == MHD_OK) rc = wait_stream(h);
+  cudaEventDestroy(done[0]);
+  cudaEventDestroy(done[1]);
+  cudaFreeHost(stage[0]);
+  cudaFreeHost(stage[1]);
+  return rc;
 }
 
 template <typename T>
@@ -588,6 +611,7 @@ int mhd_last_timings(void* handle, float out_ms[8]) {
   return MHD_OK;
 }
 
+// Two pinned staging buffers: unpacking array a overlaps the copy of array a+1.
 template <typename T>
 static int fetch_t(Handle* h, double* const* outs) {
   const Geom& g = h->g;
@@ -598,18 +622,45 @@ static int fetch_t(Handle* h, double* const* outs) {
   ext[8][0] = g.nx + 1; ext[8][1] = g.ny; ext[8][2] = g.nz;
   ext[9][0] = g.nx; ext[9][1] = g.ny + 1; ext[9][2] = g.nz;
   ext[10][0] = g.nx; ext[10][1] = g.ny; ext[10][2] = g.nz + 1;
-  T* stage = nullptr;
-  CK(cudaMallocHost(&stage, (size_t)g.vol * sizeof(T)));
-  for (int a = 0; a < 11; ++a) {
-    if (!outs[a]) continue;
-    cudaError_t e = cudaMemcpyAsync(stage, srcs[a], (size_t)g.vol * sizeof(T), cudaMemcpyDeviceToHost, h->st);
-    if (e != cudaSuccess) { cudaFreeHost(stage); return fail(MHD_E_CUDA, cudaGetErrorString(e)); }
-    int rc = wait_stream(h);
-    if (rc) { cudaFreeHost(stage); return rc; }
-    unpack<T>(g, stage, ext[a][0], ext[a][1], ext[a][2], outs[a]);
+  std::vector<int> todo;
+  for (int a = 0; a < 11; ++a)
+    if (outs[a]) todo.push_back(a);
+  if (todo.empty()) return MHD_OK;
+  T* stage[2] = {nullptr, nullptr};
+  cudaEvent_t done[2];
+  CK(cudaMallocHost(&stage[0], (size_t)g.vol * sizeof(T)));
+  if (cudaMallocHost(&stage[1], (size_t)g.vol * sizeof(T)) != cudaSuccess) {
+    cudaFreeHost(stage[0]);
+    return fail(MHD_E_NOMEM, "pinned staging allocation failed");
   }
-  cudaFreeHost(stage);
-  return MHD_OK;
+  cudaEventCreateWithFlags(&done[0], cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&done[1], cudaEventDisableTiming);
+  auto issue = [&](int n) -> cudaError_t {
+    const int a = todo[n];
+    const size_t bytes = ((size_t)ext[a][2] - 1) * g.plane * sizeof(T) +
+                         ((size_t)(ext[a][1] - 1) * g.px + ext[a][0]) * sizeof(T);
+    cudaError_t e = cudaMemcpyAsync(stage[n & 1], srcs[a], bytes, cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaEventRecord(done[n & 1], h->st);
+    return e;
+  };
+  int rc = MHD_OK;
+  cudaError_t e = issue(0);
+  for (size_t n = 0; n < todo.size() && rc == MHD_OK; ++n) {
+    if (e == cudaSuccess && n + 1 < todo.size()) e = issue((int)n + 1);
+    if (e == cudaSuccess) e = cudaEventSynchronize(done[n & 1]);
+    if (e != cudaSuccess) {
+      rc = fail(MHD_E_CUDA, std::string("fetch: ") + cudaGetErrorString(e));
+      break;
+    }
+    const int a = todo[n];
+    unpack<T>(g, stage[n & 1], ext[a][0], ext[a][1], ext[a][2], outs[a]);
+  }
+  if (rc == MHD_OK) rc = wait_stream(h);
+  cudaEventDestroy(done[0]);
+  cudaEventDestroy(done[1]);
+  cudaFreeHost(stage[0]);
+  cudaFreeHost(stage[1]);
+  return rc;
 }
 
 int mhd_fetch(void* handle, double* rho, double* vx, double* vy, double* vz, double* p, double* bx,

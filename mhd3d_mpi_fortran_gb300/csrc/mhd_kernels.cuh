@@ -1071,6 +1071,22 @@ __global__ void __launch_bounds__(256) k_fill_bxyz(Dev<T> d, int want_vf) {
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i > g.nx || j > g.ny || k > g.nz) return;
+  const int px = g.px, pl = (int)g.plane;
+  const int c = i + px * j + pl * k;
+  // interior fast path (no ghost element owned, all images are the identity)
+  if (i >= g.ng && i < g.ng + g.nx0 && j >= g.ng && j < g.ng + g.ny0 && k >= g.ng && k < g.ng + g.nz0) {
+    const T bx = T(0.5) * (d.bi[c + 1] + d.bi[c]);
+    const T by = T(0.5) * (d.bj[c + px] + d.bj[c]);
+    const T bz = T(0.5) * (d.bk[c + pl] + d.bk[c]);
+    d.bx[c] = bx;
+    d.by[c] = by;
+    d.bz[c] = bz;
+    if (want_vf) {
+      const T u = d.vx[c], v = d.vy[c], w = d.vz[c];
+      d.vf[c] = sq(u * u + v * v + w * w) + sq((bx * bx + by * by + bz * bz) / d.rho[c]);
+    }
+    return;
+  }
   const int* cx = d.gmap;
   const int* cy = cx + g.nx + 2;
   const int* cz = cy + g.ny + 2;
@@ -1079,8 +1095,6 @@ __global__ void __launch_bounds__(256) k_fill_bxyz(Dev<T> d, int want_vf) {
   const int* fz = fy + g.ny + 2;
   const int sci = cx[i], scj = cy[j], sck = cz[k];  // cell images (entries n, n+1 unused)
   const int sfi = fx[i], sfj = fy[j], sfk = fz[k];  // face images
-  const int px = g.px, pl = (int)g.plane;
-  const int c = i + px * j + pl * k;
   const bool cin = i < g.nx && j < g.ny && k < g.nz;
   // ghost copies: cell arrays (rho, vx, vy, vz, p), then bi, bj, bk
   const bool gx = sci != i, gy = scj != j, gz = sck != k;
