@@ -140,6 +140,21 @@ int mhd_free(void* handle);
 /* Human-readable text of the last error on this thread. */
 const char* mhd_last_error(void);
 
+/* ---- checkpoint / restart (no counterpart in the reference, which only
+ * plans one: mhd3d3.f90:16, 63, 88) ------------------------------------
+ * mhd_checkpoint_save writes everything a step depends on: the parameter
+ * block, the device scalars (tau, tau0), the cell primitives, the face B
+ * (bi, bj, bk; the reference's HDF5 frames keep only cell B) and, for AB,
+ * the previous level; in the handle's own precision, so a run resumed with
+ * mhd_checkpoint_load continues bit for bit.  Format: 16-byte magic
+ * "MHDGB300CKPT0001", uint32 version, uint32 sizeof(mhd_params), the
+ * mhd_params, 4 doubles (tau, tau0, dt_cfl, ab_coef), uint32 element size,
+ * uint32 array count, then per array uint32 id + uint64 bytes + the raw
+ * padded device array (ids 0-10 state, 100-110 AB previous level), and last
+ * id 999 with the FP64 cell widths dx|dy|dz.  Little-endian. */
+int mhd_checkpoint_save(void* handle, const char* path);
+int mhd_checkpoint_load(const char* path, void** handle);
+
 /* ---- kernel-level entry points used by the parity tests --------------- */
 
 /* Face fluxes of the current state, as get_flux_stress (mhd3d3.f90:2385-2560)

@@ -426,15 +426,11 @@ std::vector<int> mhd::ghost_maps(int nx0, int ny0, int nz0, int ng, const int bc
 
 const char* mhd_last_error(void) { return g_err.c_str(); }
 
-int mhd_init(const mhd_params* prm, const double* rho, const double* vx, const double* vy,
-             const double* vz, const double* p, const double* bi, const double* bj, const double* bk,
-             const double* dx, const double* dy, const double* dz, void** handle) {
-  if (!handle) return fail(MHD_E_ARG, "null handle pointer");
-  *handle = nullptr;
-  int rc = validate(prm);
-  if (rc) return rc;
-  if (!rho || !vx || !vy || !vz || !p || !bi || !bj || !bk || !dx || !dy || !dz)
-    return fail(MHD_E_ARG, "null field pointer");
+// Handle with its device buffers allocated and cleared, scalars set from prm,
+// but no fields uploaded yet.
+static int create_handle(const mhd_params* prm, const double* dx, const double* dy, const double* dz,
+                         Handle** out) {
+  *out = nullptr;
   Handle* h = new Handle();
   h->prm = *prm;
   h->fp32 = (prm->precision == MHD_FP32);
@@ -447,6 +443,10 @@ int mhd_init(const mhd_params* prm, const double* rho, const double* vx, const d
   g.pz = g.nz + 1;
   g.plane = (long long)g.px * g.py;
   g.vol = g.plane * g.pz;
+  if (g.vol >= (1LL << 31)) {
+    delete h;
+    return fail(MHD_E_ARG, "grid too large for 32-bit indexing");
+  }
   size_t es = h->fp32 ? sizeof(float) : sizeof(double);
   h->bytes = n_arrays(*prm) * (size_t)g.vol * es;
   auto bail = [&](int code, const std::string& m) {
@@ -499,11 +499,149 @@ int mhd_init(const mhd_params* prm, const double* rho, const double* vx, const d
     return bail(MHD_E_CUDA, "scalar upload failed");
   if (h->fp32) carve<float>(h, h->df, (char*)h->buf);
   else carve<double>(h, h->dd, (char*)h->buf);
+  *out = h;
+  return MHD_OK;
+}
+
+int mhd_init(const mhd_params* prm, const double* rho, const double* vx, const double* vy,
+             const double* vz, const double* p, const double* bi, const double* bj, const double* bk,
+             const double* dx, const double* dy, const double* dz, void** handle) {
+  if (!handle) return fail(MHD_E_ARG, "null handle pointer");
+  *handle = nullptr;
+  int rc = validate(prm);
+  if (rc) return rc;
+  if (!rho || !vx || !vy || !vz || !p || !bi || !bj || !bk || !dx || !dy || !dz)
+    return fail(MHD_E_ARG, "null field pointer");
+  Handle* h = nullptr;
+  rc = create_handle(prm, dx, dy, dz, &h);
+  if (rc) return rc;
   const double* arrs[8] = {rho, vx, vy, vz, p, bi, bj, bk};
   rc = h->fp32 ? upload<float>(h, arrs) : upload<double>(h, arrs);
   if (rc) { std::string m = g_err; mhd_free(h); return fail(rc, m); }
   rc = h->fp32 ? init_device<float>(h) : init_device<double>(h);
   if (rc) { std::string m = g_err; mhd_free(h); return fail(rc, m); }
+  *handle = h;
+  return MHD_OK;
+}
+
+// ---- checkpoint / restart
+static const char kMagic[17] = "MHDGB300CKPT0001";
+
+template <typename T>
+static void ckpt_arrays(Handle* h, std::vector<std::pair<uint32_t, void*>>& out) {
+  Dev<T> d = at_par(dev<T>(h), h->par);
+  T* st[11] = {d.rho, d.vx, d.vy, d.vz, d.p, d.bi, d.bj, d.bk, d.bx, d.by, d.bz};
+  for (uint32_t a = 0; a < 11; ++a) out.push_back({a, (void*)st[a]});
+  if (h->prm.stepop == MHD_STEP_AB2)
+    for (uint32_t a = 0; a < 11; ++a) out.push_back({100 + a, (void*)d.q[a]});
+}
+
+int mhd_checkpoint_save(void* handle, const char* path) {
+  Handle* h = (Handle*)handle;
+  if (!h || !path) return fail(MHD_E_ARG, "null argument");
+  int rc = wait_stream(h);
+  if (rc) return rc;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(MHD_E_ARG, std::string("cannot open ") + path);
+  std::vector<std::pair<uint32_t, void*>> arrs;
+  if (h->fp32) ckpt_arrays<float>(h, arrs);
+  else ckpt_arrays<double>(h, arrs);
+  CK(cudaMemcpy(h->sc_h, h->sc, sizeof(Scal), cudaMemcpyDeviceToHost));
+  const uint32_t ver = 1, psz = (uint32_t)sizeof(mhd_params);
+  const uint32_t es = h->fp32 ? 4 : 8, na = (uint32_t)arrs.size() + 1;
+  const double sc4[4] = {h->sc_h->tau, h->sc_h->tau0, h->sc_h->dt_cfl, h->sc_h->ab_coef};
+  bool ok = std::fwrite(kMagic, 1, 16, f) == 16 && std::fwrite(&ver, 4, 1, f) == 1 &&
+            std::fwrite(&psz, 4, 1, f) == 1 && std::fwrite(&h->prm, sizeof(mhd_params), 1, f) == 1 &&
+            std::fwrite(sc4, 8, 4, f) == 4 && std::fwrite(&es, 4, 1, f) == 1 && std::fwrite(&na, 4, 1, f) == 1;
+  const size_t bytes = (size_t)h->g.vol * es;
+  std::vector<char> buf(ok ? bytes : 0);
+  for (auto& a : arrs) {
+    if (!ok) break;
+    if (cudaMemcpy(buf.data(), a.second, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) { ok = false; break; }
+    const uint64_t nb = bytes;
+    ok = std::fwrite(&a.first, 4, 1, f) == 1 && std::fwrite(&nb, 8, 1, f) == 1 &&
+         std::fwrite(buf.data(), 1, bytes, f) == bytes;
+  }
+  if (ok) {  // FP64 cell widths, id 999
+    const size_t ng = (size_t)h->g.nx + h->g.ny + h->g.nz;
+    std::vector<double> w(ng);
+    ok = cudaMemcpy(w.data(), h->geo, ng * 8, cudaMemcpyDeviceToHost) == cudaSuccess;
+    const uint32_t id = 999;
+    const uint64_t nb = ng * 8;
+    ok = ok && std::fwrite(&id, 4, 1, f) == 1 && std::fwrite(&nb, 8, 1, f) == 1 &&
+         std::fwrite(w.data(), 8, ng, f) == ng;
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) return fail(MHD_E_ARG, std::string("checkpoint write failed: ") + path);
+  return MHD_OK;
+}
+
+int mhd_checkpoint_load(const char* path, void** handle) {
+  if (!path || !handle) return fail(MHD_E_ARG, "null argument");
+  *handle = nullptr;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(MHD_E_ARG, std::string("cannot open ") + path);
+  char magic[16];
+  uint32_t ver = 0, psz = 0, es = 0, na = 0;
+  mhd_params prm{};
+  double sc4[4];
+  bool ok = std::fread(magic, 1, 16, f) == 16 && std::memcmp(magic, kMagic, 16) == 0 &&
+            std::fread(&ver, 4, 1, f) == 1 && ver == 1 && std::fread(&psz, 4, 1, f) == 1 &&
+            psz == sizeof(mhd_params) && std::fread(&prm, sizeof(mhd_params), 1, f) == 1 &&
+            std::fread(sc4, 8, 4, f) == 4 && std::fread(&es, 4, 1, f) == 1 && std::fread(&na, 4, 1, f) == 1;
+  if (!ok || validate(&prm) != MHD_OK || es != (prm.precision == MHD_FP32 ? 4u : 8u)) {
+    std::fclose(f);
+    return fail(MHD_E_ARG, std::string("not a compatible checkpoint: ") + path);
+  }
+  // geometry is not stored: widths come back from the widths array below
+  const int nx = prm.nx0 + prm.nord, ny = prm.ny0 + prm.nord, nz = prm.nz0 + prm.nord;
+  std::vector<double> ones((size_t)nx + ny + nz, 1.0);
+  Handle* h = nullptr;
+  int rc = create_handle(&prm, ones.data(), ones.data() + nx, ones.data() + nx + ny, &h);
+  if (rc) { std::fclose(f); return rc; }
+  std::vector<std::pair<uint32_t, void*>> arrs;
+  if (h->fp32) ckpt_arrays<float>(h, arrs);
+  else ckpt_arrays<double>(h, arrs);
+  const size_t bytes = (size_t)h->g.vol * es;
+  std::vector<char> buf(bytes);
+  size_t loaded = 0;
+  for (uint32_t n = 0; n < na && ok; ++n) {
+    uint32_t id = 0;
+    uint64_t nb = 0;
+    ok = std::fread(&id, 4, 1, f) == 1 && std::fread(&nb, 8, 1, f) == 1 &&
+         (nb == bytes || (id == 999 && nb == ((size_t)nx + ny + nz) * 8)) &&
+         std::fread(buf.data(), 1, nb, f) == nb;
+    if (!ok) break;
+    void* dst = nullptr;
+    if (id == 999) {  // cell widths (FP64)
+      const size_t ng = (size_t)nx + ny + nz;
+      ok = cudaMemcpy(h->geo, buf.data(), ng * 8, cudaMemcpyHostToDevice) == cudaSuccess;
+      std::vector<float> gf(ng * 2);
+      const double* w = (const double*)buf.data();
+      for (size_t i = 0; i < ng; ++i) { gf[i] = (float)w[i]; gf[ng + i] = (float)(1.0 / w[i]); }
+      ok = ok && cudaMemcpy(h->geoT, gf.data(), gf.size() * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+      ++loaded;
+      continue;
+    }
+    for (auto& a : arrs)
+      if (a.first == id) dst = a.second;
+    if (!dst) { ok = false; break; }
+    ok = cudaMemcpy(dst, buf.data(), bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+    ++loaded;
+  }
+  std::fclose(f);
+  if (!ok || loaded != arrs.size() + 1) {
+    mhd_free(h);
+    return fail(MHD_E_ARG, std::string("checkpoint is truncated or inconsistent: ") + path);
+  }
+  Scal s{};
+  s.tau = sc4[0]; s.tau0 = sc4[1]; s.dt_cfl = sc4[2]; s.ab_coef = sc4[3];
+  double inf = INFINITY;
+  std::memcpy(&s.dtmin_bits, &inf, sizeof(double));
+  if (cudaMemcpy(h->sc, &s, sizeof(Scal), cudaMemcpyHostToDevice) != cudaSuccess) {
+    mhd_free(h);
+    return fail(MHD_E_CUDA, "scalar upload failed");
+  }
   *handle = h;
   return MHD_OK;
 }

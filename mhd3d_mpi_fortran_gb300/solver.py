@@ -37,9 +37,13 @@ def _f64(a) -> np.ndarray:
 
 
 class MHDSolver:
-    def __init__(self, params: Params, state: State, dx=None, dy=None, dz=None, lib=None):
+    def __init__(self, params: Params, state: State | None, dx=None, dy=None, dz=None, lib=None,
+                 _handle=None):
         self.lib = lib or abi.load()
         self.params = params
+        if _handle is not None:  # from a checkpoint
+            self.h = _handle
+            return
         g = state.grid
         self._keep = [_f64(a) for a in state.arrays()]
         self._geo = [_f64(g.dx if dx is None else dx), _f64(g.dy if dy is None else dy),
@@ -72,6 +76,18 @@ class MHDSolver:
         rc = self.lib.mhd_time_steps(self.h, int(n), 1 if graph else 0, C.byref(ms))
         check(self.lib, rc, "mhd_time_steps")
         return ms.value
+
+    def save(self, path: str):
+        """Checkpoint everything a step depends on (mhd_checkpoint_save)."""
+        check(self.lib, self.lib.mhd_checkpoint_save(self.h, str(path).encode()), "mhd_checkpoint_save")
+
+    @classmethod
+    def load(cls, path: str, params: Params):
+        """Resume from a checkpoint written by save(); params must describe the same run."""
+        lib = abi.load()
+        h = C.c_void_p()
+        check(lib, lib.mhd_checkpoint_load(str(path).encode(), C.byref(h)), "mhd_checkpoint_load")
+        return cls(params, None, lib=lib, _handle=h)
 
     def set_tau(self, tau: float):
         check(self.lib, self.lib.mhd_set_tau(self.h, float(tau)), "mhd_set_tau")

@@ -202,3 +202,23 @@ def test_status_bits_from_poisoned_input(prec):
     with MHDSolver(Params(8, 8, 8, precision=prec, tau=tau), s) as g:
         _, st = g.step(1)
     assert st & ST_NEG_RHO
+
+
+@pytest.mark.parametrize("prec,stepop", [(FP64, STEP_RK2), (FP32, STEP_RK2), (FP64, STEP_AB2), (FP32, STEP_RK3)])
+def test_checkpoint_restart_is_bit_exact(tmp_path, prec, stepop):
+    """Save after 3 steps, continue 4 more; a run resumed from the file
+    reproduces the continued run bit for bit (state, face B, AB history)."""
+    s = ics.orszag_tang_3d(12, seed=2)
+    prm = Params(12, 12, 12, precision=prec, stepop=stepop, tau=0.5 * ics.cfl_dt(s))
+    path = tmp_path / "run.ckpt"
+    with MHDSolver(prm, s) as a:
+        a.step(3)
+        a.save(path)
+        ta, _ = a.step(4)
+        fa = a.fetch()
+    with MHDSolver.load(path, prm) as b:
+        tb, _ = b.step(4)
+        fb = b.fetch()
+    assert ta == tb
+    for k in FIELDS:
+        assert np.array_equal(fa[k], fb[k]), k
