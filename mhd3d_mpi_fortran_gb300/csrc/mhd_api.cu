@@ -642,6 +642,17 @@ int mhd_checkpoint_load(const char* path, void** handle) {
     mhd_free(h);
     return fail(MHD_E_CUDA, "scalar upload failed");
   }
+  // vf (and cell B) as the end of the saved step left them: the same fused
+  // kernel the step runs, on the restored fields
+  const bool want_vf = prm.stepop != MHD_STEP_AB2;
+  if (h->fp32) Launch<float>::fill_bxyz(h->df, want_vf, h->st);
+  else Launch<double>::fill_bxyz(h->dd, want_vf, h->st);
+  rc = wait_stream(h);
+  if (rc) {
+    std::string m = g_err;
+    mhd_free(h);
+    return fail(rc, m);
+  }
   *handle = h;
   return MHD_OK;
 }
