@@ -15,6 +15,16 @@ Generators:
 * ``implosion``       -- diagonal-interface implosion (``init_ic_imp``, mhd3d2.f90:3440-3471).
 * ``turbulence``      -- solenoidal Gaussian-random v and B, E(k) ~ k^-2 on
                          kmin <= |k| <= kmax, B from a vector potential.
+
+Curvilinear (metric-mode) states carry ``nodes`` (ghost-inclusive node
+coordinates X, Y, Z of shape (nx+1, ny+1, nz+1)) and hold in bi/bj/bk the
+magnetic flux Phi = B.A through each face instead of B:
+* ``mapped_grid``      -- logical grid plus nodes of x = xi + a sin 2 pi eta,
+                          y = eta + a sin 2 pi zeta, z = zeta (or the identity).
+* ``mapped_blast``     -- magnetised blast on a mapped grid, Phi = B.A.
+* ``mapped_orszag_tang`` -- 3-D Orszag-Tang on a mapped grid, Phi = loop
+                          integral of the vector potential (div-free exactly).
+* ``uniform_flow``     -- uniform rho, p, v and B on a mapped grid.
 """
 from __future__ import annotations
 
@@ -100,16 +110,17 @@ class State:
     bj: np.ndarray
     bk: np.ndarray
     grid: Grid
+    nodes: tuple | None = None  # metric mode: (X, Y, Z) node coordinates
 
     def arrays(self):
         return [self.rho, self.vx, self.vy, self.vz, self.p, self.bi, self.bj, self.bk]
 
 
-def empty_state(g: Grid) -> State:
+def empty_state(g: Grid, nodes=None) -> State:
     cs = (g.nx, g.ny, g.nz)
     z = lambda s: np.zeros(s, dtype=np.float64, order="F")
     return State(z(cs), z(cs), z(cs), z(cs), z(cs), z((g.nx + 1, g.ny, g.nz)),
-                 z((g.nx, g.ny + 1, g.nz)), z((g.nx, g.ny, g.nz + 1)), g)
+                 z((g.nx, g.ny + 1, g.nz)), z((g.nx, g.ny, g.nz + 1)), g, nodes)
 
 
 def _bcast(g: Grid):
@@ -330,3 +341,192 @@ def cfl_dt(s: State, gam: float = 5.0 / 3.0, cfl: float = 0.3) -> float:
     dy = g.dy[sl[1]][None, :, None]
     dz = g.dz[sl[2]][None, None, :]
     return float(np.min(cfl / (vc / dx + vc / dy + vc / dz)))
+
+
+# ---------------------------------------------------------------- mapped grids
+def mapped_grid(nx0, ny0, nz0, nord=8, amp=0.05, kind="sine"):
+    """Logical grid on [0,1]^3 (nodes extended into the ghosts as in init_geom)
+    and the ghost-inclusive physical node coordinates of the mapping
+    x = xi + amp sin(2 pi eta), y = eta + amp sin(2 pi zeta), z = zeta
+    (kind "sine") or of the identity (kind "cartesian").  The sine mapping
+    is periodic in shape: x(xi + 1) = x(xi) + 1 and so on."""
+    g = grid(nx0, ny0, nz0, nord=nord)
+    XI, ETA, ZETA = np.meshgrid(g.xn, g.yn, g.zn, indexing="ij")
+    if kind == "sine":
+        X = XI + amp * np.sin(2.0 * PI * ETA)
+        Y = ETA + amp * np.sin(2.0 * PI * ZETA)
+        Z = ZETA.copy()
+    elif kind == "cartesian":
+        X, Y, Z = XI.copy(), ETA.copy(), ZETA.copy()
+    else:
+        raise ValueError(kind)
+    f = lambda a: np.asfortranarray(a, dtype=np.float64)
+    return g, (f(X), f(Y), f(Z))
+
+
+def face_areas(nodes):
+    """Low-face area vectors 0.5 (d1 x d2) from the face diagonals, for the
+    x, y and z face families: list of 3 arrays of shape (..., 3)."""
+    P = np.stack(nodes, axis=-1)
+    out = []
+    for ax in range(3):
+        t1, t2 = (ax + 1) % 3, (ax + 2) % 3
+        n = P.shape[:3]
+        ext = [n[0] - 1, n[1] - 1, n[2] - 1]
+        ext[ax] = n[ax]
+
+        def at(o1, o2):
+            sl = [slice(0, e) for e in ext]
+            if o1:
+                sl[t1] = slice(1, ext[t1] + 1)
+            if o2:
+                sl[t2] = slice(1, ext[t2] + 1)
+            return P[tuple(sl)]
+        d1 = at(1, 1) - at(0, 0)
+        d2 = at(0, 1) - at(1, 0)
+        out.append(0.5 * np.cross(d1, d2))
+    return out
+
+
+def cell_centres_mapped(nodes):
+    """Physical cell centres: mean of the 8 corner nodes."""
+    out = []
+    for a in nodes:
+        out.append(0.125 * (a[:-1, :-1, :-1] + a[1:, :-1, :-1] + a[:-1, 1:, :-1] + a[1:, 1:, :-1] +
+                            a[:-1, :-1, 1:] + a[1:, :-1, 1:] + a[:-1, 1:, 1:] + a[1:, 1:, 1:]))
+    return out
+
+
+def _phi_uniform(s: State, B):
+    for arr, A in zip((s.bi, s.bj, s.bk), face_areas(s.nodes)):
+        arr[...] = A[..., 0] * B[0] + A[..., 1] * B[1] + A[..., 2] * B[2]
+
+
+def mapped_blast(n: int, nord: int = 8, amp: float = 0.05, p_in: float = 10.0, p_out: float = 0.1,
+                 r0: float = 0.1, kind: str = "sine", ny0=None, nz0=None) -> State:
+    """Magnetised blast on a mapped grid: rho = 1, v = 0, p = p_out and p_in
+    where the physical cell centre lies within r0 of (0.5, 0.5, 0.5), uniform
+    B = (1, 1, 0)/sqrt(2) stored as face fluxes Phi = B.A."""
+    g, nodes = mapped_grid(n, n if ny0 is None else ny0, n if nz0 is None else nz0, nord=nord, amp=amp,
+                           kind=kind)
+    s = empty_state(g, nodes)
+    xc, yc, zc = cell_centres_mapped(nodes)
+    r2 = (xc - 0.5) ** 2 + (yc - 0.5) ** 2 + (zc - 0.5) ** 2
+    s.rho[...] = 1.0
+    s.p[...] = np.where(r2 < r0 * r0, p_in, p_out)
+    _phi_uniform(s, (1.0 / np.sqrt(2.0), 1.0 / np.sqrt(2.0), 0.0))
+    return s
+
+
+def uniform_flow(n: int, v=(0.3, -0.2, 0.1), B=(0.0, 0.0, 0.0), rho: float = 1.0, p: float = 0.6,
+                 nord: int = 8, amp: float = 0.05, kind: str = "sine") -> State:
+    """Uniform rho, p, v and B (Phi = B.A) on a mapped grid."""
+    g, nodes = mapped_grid(n, n, n, nord=nord, amp=amp, kind=kind)
+    s = empty_state(g, nodes)
+    s.rho[...] = rho
+    s.p[...] = p
+    s.vx[...], s.vy[...], s.vz[...] = v
+    _phi_uniform(s, B)
+    return s
+
+
+def _edge_circulation(nodes, afun):
+    """Line integrals of the vector potential along every cell edge, midpoint
+    rule: afun(x, y, z) -> (Ax, Ay, Az) at the edge midpoint, dotted with the
+    edge vector.  Returns [x-edges, y-edges, z-edges]."""
+    out = []
+    for e in range(3):
+        sl0 = [slice(None)] * 3
+        sl1 = [slice(None)] * 3
+        sl0[e] = slice(0, -1)
+        sl1[e] = slice(1, None)
+        p0 = [a[tuple(sl0)] for a in nodes]
+        p1 = [a[tuple(sl1)] for a in nodes]
+        mid = [0.5 * (a + b) for a, b in zip(p0, p1)]
+        A = afun(*mid)
+        out.append(sum(A[c] * (p1[c] - p0[c]) for c in range(3)))
+    return out
+
+
+def mapped_orszag_tang(n: int, nord: int = 8, amp: float = 0.05, seed: int = 0, noise: float = 1e-3,
+                       kind: str = "sine", ny0=None, nz0=None) -> State:
+    """3-D Orszag-Tang on a periodic mapped grid: the Cartesian generator's
+    rho, p and v at the physical cell centres, and face fluxes Phi from the
+    loop integrals of A_z = [cos(2 pi y)/(2 pi) + cos(4 pi x)/(4 pi)]/sqrt(4 pi)
+    around each face (so the discrete div B is zero to round-off)."""
+    ny0 = n if ny0 is None else ny0
+    nz0 = n if nz0 is None else nz0
+    g, nodes = mapped_grid(n, ny0, nz0, nord=nord, amp=amp, kind=kind)
+    s = empty_state(g, nodes)
+    xc, yc, zc = cell_centres_mapped(nodes)
+    rng = np.random.default_rng(seed)
+    s.rho[...] = 25.0 / (36.0 * PI) + rng.uniform(-noise, noise, size=s.rho.shape[::-1]).transpose(2, 1, 0)
+    s.p[...] = 5.0 / (12.0 * PI)
+    s.vx[...] = -np.sin(2.0 * PI * yc)
+    s.vy[...] = np.sin(2.0 * PI * xc)
+    s.vz[...] = 0.1 * np.sin(2.0 * PI * zc)
+
+    def afun(x, y, z):
+        az = (np.cos(2.0 * PI * y) / (2.0 * PI) + np.cos(4.0 * PI * x) / (4.0 * PI)) / np.sqrt(4.0 * PI)
+        return (0.0 * x, 0.0 * x, az)
+    ex, ey, ez = _edge_circulation(nodes, afun)
+    # Phi through the low face = circulation around its loop (right-handed
+    # about the +axis normal), the same orientation as the CT update
+    s.bi[...] = (ez[:, 1:, :] - ez[:, :-1, :]) - (ey[:, :, 1:] - ey[:, :, :-1])
+    s.bj[...] = (ex[:, :, 1:] - ex[:, :, :-1]) - (ez[1:, :, :] - ez[:-1, :, :])
+    s.bk[...] = (ey[1:, :, :] - ey[:-1, :, :]) - (ex[:, 1:, :] - ex[:, :-1, :])
+    return s
+
+
+def cfl_dt_mapped(s: State, gam: float = 5.0 / 3.0, cfl: float = 0.3) -> float:
+    """CFL dt of a mapped state on its interior: cfl V / (vcfl sum_a |Abar_a|),
+    cell B from the face fluxes (B = sum_a Phibar_a / V * e_a)."""
+    g = s.grid
+    ng = g.ng
+    A = face_areas(s.nodes)
+    # volumes by the divergence theorem over face centroids
+    P = np.stack(s.nodes, axis=-1)
+    cen = []
+    for ax in range(3):
+        t1, t2 = (ax + 1) % 3, (ax + 2) % 3
+        n = P.shape[:3]
+        ext = [n[0] - 1, n[1] - 1, n[2] - 1]
+        ext[ax] = n[ax]
+        acc = 0
+        for o1 in (0, 1):
+            for o2 in (0, 1):
+                sl = [slice(0, e) for e in ext]
+                if o1:
+                    sl[t1] = slice(1, ext[t1] + 1)
+                if o2:
+                    sl[t2] = slice(1, ext[t2] + 1)
+                acc = acc + P[tuple(sl)]
+        cen.append(0.25 * acc)
+    V = 0
+    eb = []
+    for ax in range(3):
+        lo = [slice(None)] * 3
+        hi = [slice(None)] * 3
+        lo[ax] = slice(0, -1)
+        hi[ax] = slice(1, None)
+        V = V + (np.sum(cen[ax][tuple(hi)] * A[ax][tuple(hi)], -1) - np.sum(cen[ax][tuple(lo)] * A[ax][tuple(lo)], -1))
+        eb.append(cen[ax][tuple(hi)] - cen[ax][tuple(lo)])
+    V = V / 3.0
+    phis = (s.bi, s.bj, s.bk)
+    Bc = 0
+    ssum = 0
+    for ax in range(3):
+        lo = [slice(None)] * 3
+        hi = [slice(None)] * 3
+        lo[ax] = slice(0, -1)
+        hi[ax] = slice(1, None)
+        ph = 0.5 * (phis[ax][tuple(hi)] + phis[ax][tuple(lo)]) / V
+        Bc = Bc + ph[..., None] * eb[ax]
+        Ab = 0.5 * (A[ax][tuple(lo)] + A[ax][tuple(hi)])
+        ssum = ssum + np.sqrt(np.sum(Ab * Ab, -1))
+    sl = (slice(ng, ng + g.nx0), slice(ng, ng + g.ny0), slice(ng, ng + g.nz0))
+    r, p = s.rho[sl], s.p[sl]
+    v = np.sqrt(s.vx[sl] ** 2 + s.vy[sl] ** 2 + s.vz[sl] ** 2)
+    b2 = np.sum(Bc[sl] ** 2, -1)
+    vc = v + np.sqrt(b2 / r + gam * p / r)
+    return float(np.min(cfl * V[sl] / (vc * ssum[sl])))

@@ -73,6 +73,18 @@ struct Oracle {
   A3 flux[3][8];  // [dir][rho, rvx, rvy, rvz, eng, stress_x, stress_y, stress_z]
   uint32_t status = 0;
 
+  // ---- curvilinear (metric) mode: no reference counterpart; this oracle is
+  // its specification.  Face fields bi/bj/bk hold the magnetic flux
+  // Phi = B.A through each face; fluxes are multiplied by face areas and the
+  // update divided by cell volumes; CT is the circulation of E.dl.  On a
+  // Cartesian mesh every term reduces to the reference's formula.
+  bool metric = false;
+  A3 X[3];               // node coordinates (nx+1, ny+1, nz+1)
+  A3 Af[3][3];           // [face axis][component] low-face area vectors (face extents)
+  A3 vol;                // cell volumes (nx, ny, nz)
+  A3 eb[3][3];           // [axis][component] cell edge vectors (face-centroid differences)
+  A3 w[3];               // v . (mean unit normal of the a-faces), per stage
+
   double dxb(int i, int, int) const { return dxv[i - 1]; }
   double dyb(int, int j, int) const { return dyv[j - 1]; }
   double dzb(int, int, int k) const { return dzv[k - 1]; }
@@ -417,6 +429,7 @@ struct Oracle {
   // --------------------------------------------------------------- get_*
   // get_dt (mhd3d3.f90:1608-1639): CFL dt, minval over all cells incl. ghosts
   double get_dt() {
+    if (metric) return get_dt_metric();
     double m = INFINITY;
 #pragma omp parallel for reduction(min : m) schedule(static)
     for (int k = 1; k <= nz; ++k)
@@ -568,6 +581,10 @@ struct Oracle {
                     const A3& lbx, const A3& lby, const A3& lbz, const A3& lbi, const A3& lbj,
                     const A3& lbk) {
     (void)lp;
+    if (metric) {
+      get_eijk_metric(lrho, lvx, lvy, lvz, lbx, lby, lbz, lbi, lbj, lbk);
+      return;
+    }
     A3 vf(nx, ny, nz);
     FOR3(nx, ny, nz) {
       double u = lvx(i, j, k), v = lvy(i, j, k), w = lvz(i, j, k);
@@ -611,6 +628,10 @@ struct Oracle {
 
   // get_bxyz (mhd3d3.f90:2118-2128)
   void get_bxyz() {
+    if (metric) {
+      get_bxyz_metric();
+      return;
+    }
     FOR3(nx, ny, nz) {
       bx(i, j, k) = 0.5 * (bi(i + 1, j, k) + bi(i, j, k));
       by(i, j, k) = 0.5 * (bj(i, j + 1, k) + bj(i, j, k));
@@ -631,6 +652,10 @@ struct Oracle {
   // get_flux_stress (mhd3d3.f90:2385-2560)
   void get_flux_stress(const A3& lrho, const A3& lvx, const A3& lvy, const A3& lvz, const A3& lp,
                        const A3& lbx, const A3& lby, const A3& lbz) {
+    if (metric) {
+      get_flux_stress_metric(lrho, lvx, lvy, lvz, lp, lbx, lby, lbz);
+      return;
+    }
     for (int kkk = 1; kkk <= 3; ++kkk) {
       int ii = nx0, jj = ny0, kk = nz0;
       if (kkk == 1) ii = nx0 + 1;
@@ -738,7 +763,8 @@ struct Oracle {
   void advance_corrector1() {
     A3* F = flux[0]; A3* Gf = flux[1]; A3* H = flux[2];
     const int G = ng;
-    FOR3(nx0, ny0, nz0) {
+    if (metric) advance_corrector_metric(1);
+    else FOR3(nx0, ny0, nz0) {
       double dx = dxb(G + i, G + j, G + k), dy = dyb(G + i, G + j, G + k), dz = dzb(G + i, G + j, G + k);
       auto d = [&](int q) {
         return (F[q](i + 1, j, k) - F[q](i, j, k)) / dx + (Gf[q](i, j + 1, k) - Gf[q](i, j, k)) / dy +
@@ -762,7 +788,8 @@ struct Oracle {
   void advance_corrector2() {
     A3* F = flux[0]; A3* Gf = flux[1]; A3* H = flux[2];
     const int G = ng;
-    FOR3(nx0, ny0, nz0) {
+    if (metric) advance_corrector_metric(2);
+    else FOR3(nx0, ny0, nz0) {
       double dx = dxb(G + i, G + j, G + k), dy = dyb(G + i, G + j, G + k), dz = dzb(G + i, G + j, G + k);
       auto d = [&](int q) {
         return (F[q](i + 1, j, k) - F[q](i, j, k)) / dx + (Gf[q](i, j + 1, k) - Gf[q](i, j, k)) / dy +
@@ -784,6 +811,10 @@ struct Oracle {
 
   // advance_bijk (mhd3d3.f90:3909-3933)
   void advance_bijk() {
+    if (metric) {
+      advance_bijk_metric();
+      return;
+    }
     const int G = ng;
     FOR3(nx0 + 1, ny0, nz0) {
       bi(G + i, G + j, G + k) = bi(G + i, G + j, G + k) -
@@ -860,6 +891,305 @@ struct Oracle {
     get_bxyz();
   }
 
+
+  // ------------------------------------------------------------ metric mode
+  static inline void cross(const double* a, const double* b, double* c) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+  }
+  // node (i,j,k) coordinate vector
+  inline void node(int i, int j, int k, double* x) const {
+    x[0] = X[0](i, j, k); x[1] = X[1](i, j, k); x[2] = X[2](i, j, k);
+  }
+  // Face area vector 0.5*(d1 x d2) of the low face normal to `ax` of cell
+  // (i,j,k) (face-array index), from its four nodes (diagonals d1, d2).
+  void face_area(int ax, int i, int j, int k, double* A) const {
+    double p0[3], p1[3], q0[3], q1[3], d1[3], d2[3];
+    if (ax == 0) { node(i, j, k, p0); node(i, j + 1, k + 1, p1); node(i, j + 1, k, q0); node(i, j, k + 1, q1); }
+    else if (ax == 1) { node(i, j, k, p0); node(i + 1, j, k + 1, p1); node(i, j, k + 1, q0); node(i + 1, j, k, q1); }
+    else { node(i, j, k, p0); node(i + 1, j + 1, k, p1); node(i + 1, j, k, q0); node(i, j + 1, k, q1); }
+    for (int c = 0; c < 3; ++c) { d1[c] = p1[c] - p0[c]; d2[c] = q1[c] - q0[c]; }
+    cross(d1, d2, A);
+    for (int c = 0; c < 3; ++c) A[c] = 0.5 * A[c];
+  }
+  // centroid (mean of the 4 nodes) of the low face normal to `ax`
+  void face_centroid(int ax, int i, int j, int k, double* C) const {
+    int o1[3] = {0, 0, 0}, o2[3] = {0, 0, 0};
+    o1[(ax + 1) % 3] = 1;
+    o2[(ax + 2) % 3] = 1;
+    double a[3], b[3], c[3], d[3];
+    node(i, j, k, a);
+    node(i + o1[0], j + o1[1], k + o1[2], b);
+    node(i + o1[0] + o2[0], j + o1[1] + o2[1], k + o1[2] + o2[2], c);
+    node(i + o2[0], j + o2[1], k + o2[2], d);
+    for (int q = 0; q < 3; ++q) C[q] = 0.25 * (a[q] + b[q] + c[q] + d[q]);
+  }
+  void metric_geometry() {
+    int fe[3][3] = {{nx + 1, ny, nz}, {nx, ny + 1, nz}, {nx, ny, nz + 1}};
+    for (int ax = 0; ax < 3; ++ax)
+      for (int c = 0; c < 3; ++c) Af[ax][c].alloc(fe[ax][0], fe[ax][1], fe[ax][2]);
+    for (int ax = 0; ax < 3; ++ax) {
+      for (int k = 1; k <= fe[ax][2]; ++k)
+        for (int j = 1; j <= fe[ax][1]; ++j)
+          for (int i = 1; i <= fe[ax][0]; ++i) {
+            double A[3];
+            face_area(ax, i, j, k, A);
+            for (int c = 0; c < 3; ++c) Af[ax][c](i, j, k) = A[c];
+          }
+    }
+    vol.alloc(nx, ny, nz);
+    for (int a = 0; a < 3; ++a)
+      for (int c = 0; c < 3; ++c) eb[a][c].alloc(nx, ny, nz);
+    for (int k = 1; k <= nz; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          // V = (1/3) sum over faces of centroid . outward area
+          double v = 0.0;
+          for (int ax = 0; ax < 3; ++ax) {
+            int hi[3] = {i, j, k};
+            hi[ax] += 1;
+            double Clo[3], Chi[3];
+            face_centroid(ax, i, j, k, Clo);
+            face_centroid(ax, hi[0], hi[1], hi[2], Chi);
+            double slo = Clo[0] * Af[ax][0](i, j, k) + Clo[1] * Af[ax][1](i, j, k) + Clo[2] * Af[ax][2](i, j, k);
+            double shi = Chi[0] * Af[ax][0](hi[0], hi[1], hi[2]) + Chi[1] * Af[ax][1](hi[0], hi[1], hi[2]) +
+                         Chi[2] * Af[ax][2](hi[0], hi[1], hi[2]);
+            v = v + (shi - slo);
+            for (int c = 0; c < 3; ++c) eb[ax][c](i, j, k) = Chi[c] - Clo[c];
+          }
+          vol(i, j, k) = v / 3.0;
+        }
+  }
+  double amag(int ax, int i, int j, int k) const {
+    double a = Af[ax][0](i, j, k), b = Af[ax][1](i, j, k), c = Af[ax][2](i, j, k);
+    return std::sqrt(a * a + b * b + c * c);
+  }
+  // cell-averaged area vector of the a-faces of cell (i,j,k)
+  void abar(int ax, int i, int j, int k, double* A) const {
+    int hi[3] = {i, j, k};
+    hi[ax] += 1;
+    for (int c = 0; c < 3; ++c) A[c] = 0.5 * (Af[ax][c](i, j, k) + Af[ax][c](hi[0], hi[1], hi[2]));
+  }
+
+  // B = sum_a (Phi_a averaged over the two a-faces / V) * (cell edge vector along a)
+  void get_bxyz_metric() {
+    A3* F[3] = {&bi, &bj, &bk};
+    A3* B[3] = {&bx, &by, &bz};
+    FOR3(nx, ny, nz) {
+      double ph[3];
+      for (int a = 0; a < 3; ++a) {
+        int hi[3] = {i, j, k};
+        hi[a] += 1;
+        ph[a] = 0.5 * ((*F[a])(hi[0], hi[1], hi[2]) + (*F[a])(i, j, k)) / vol(i, j, k);
+      }
+      for (int c = 0; c < 3; ++c)
+        (*B[c])(i, j, k) = ph[0] * eb[0][c](i, j, k) + ph[1] * eb[1][c](i, j, k) + ph[2] * eb[2][c](i, j, k);
+    }
+  }
+
+  // CFL dt with 1/dx_a -> |abar_a| / V
+  double get_dt_metric() {
+    double m = INFINITY;
+#pragma omp parallel for reduction(min : m) schedule(static)
+    for (int k = 1; k <= nz; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          double v = std::sqrt(vx(i, j, k) * vx(i, j, k) + vy(i, j, k) * vy(i, j, k) + vz(i, j, k) * vz(i, j, k));
+          double btot = std::sqrt(bx(i, j, k) * bx(i, j, k) + by(i, j, k) * by(i, j, k) + bz(i, j, k) * bz(i, j, k));
+          double valf = btot / std::sqrt(rho(i, j, k));
+          double vs = std::sqrt(gam * p(i, j, k) / rho(i, j, k));
+          double vcfl = v + std::sqrt(valf * valf + vs * vs);
+          double s = 0.0;
+          for (int a = 0; a < 3; ++a) {
+            double A[3];
+            abar(a, i, j, k, A);
+            s = s + std::sqrt(A[0] * A[0] + A[1] * A[1] + A[2] * A[2]);
+          }
+          double dt = cfl / (vcfl * s / vol(i, j, k));
+          m = (dt < m) ? dt : m;
+        }
+    return m;
+  }
+
+  // Face fluxes in metric form: the reference's Gaussian-split formulas with the
+  // face normal n = A/|A| in place of the axis, vector momentum and stress, and
+  // every flux multiplied by |A| (stored in `flux`, interior extents).
+  void get_flux_stress_metric(const A3& lrho, const A3& lvx, const A3& lvy, const A3& lvz, const A3& lp,
+                              const A3& lbx, const A3& lby, const A3& lbz) {
+    for (int kkk = 1; kkk <= 3; ++kkk) {
+      int ii = nx0, jj = ny0, kk = nz0;
+      if (kkk == 1) ii = nx0 + 1;
+      if (kkk == 2) jj = ny0 + 1;
+      if (kkk == 3) kk = nz0 + 1;
+      A3 L[8], R[8];
+      const A3* src[8] = {&lrho, &lvx, &lvy, &lvz, &lp, &lbx, &lby, &lbz};
+      for (int v = 0; v < 8; ++v) reconstruct_3d(L[v], R[v], *src[v], ii, jj, kk, kkk);
+      A3* out = flux[kkk - 1];
+      for (int q = 0; q < 8; ++q) out[q].alloc(ii, jj, kk);
+      const int ax = kkk - 1;
+      FOR3(ii, jj, kk) {
+        const int fi = ng + i, fj = ng + j, fk = ng + k;  // face-array index of this face
+        double A[3] = {Af[ax][0](fi, fj, fk), Af[ax][1](fi, fj, fk), Af[ax][2](fi, fj, fk)};
+        double am = std::sqrt(A[0] * A[0] + A[1] * A[1] + A[2] * A[2]);
+        double n[3] = {A[0] / am, A[1] / am, A[2] / am};
+        double tot[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int side = 0; side < 2; ++side) {
+          const A3* S = side == 0 ? L : R;
+          double r = S[0](i, j, k), u[3] = {S[1](i, j, k), S[2](i, j, k), S[3](i, j, k)}, pr = S[4](i, j, k);
+          double b[3] = {S[5](i, j, k), S[6](i, j, k), S[7](i, j, k)};
+          double vn = u[0] * n[0] + u[1] * n[1] + u[2] * n[2];
+          double bn = b[0] * n[0] + b[1] * n[1] + b[2] * n[2];
+          double leng = 0.5 * r * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]) + pr / (gam - 1.0);
+          double v0p, v0n, v1p, v1n;
+          v_face(r / (2.0 * pr), vn, v0p, v0n, v1p, v1n);
+          double v0 = side == 0 ? v0p : v0n, v1 = side == 0 ? v1p : v1n;
+          double f[8];
+          f[0] = r * v1;
+          for (int c = 0; c < 3; ++c) f[1 + c] = r * u[c] * v1 + pr * n[c] * v0;
+          f[4] = (leng + 0.5 * pr) * v1 + 0.5 * pr * vn * v0;
+          double lbsq = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+          v_face(r / (2.0 * pr + lbsq), vn, v0p, v0n, v1p, v1n);
+          v0 = side == 0 ? v0p : v0n;
+          for (int c = 0; c < 3; ++c) f[5 + c] = (0.5 * lbsq * n[c] - b[c] * bn) * v0;
+          for (int q = 0; q < 8; ++q) tot[q] = tot[q] + f[q];
+        }
+        for (int q = 0; q < 8; ++q) out[q](i, j, k) = tot[q] * am;
+      }
+    }
+  }
+
+  // w^a = v . nbar_a per cell, nbar_a = abar_a / |abar_a| the mean unit
+  // normal of the a-faces (the velocity normal to those faces)
+  void get_w(const A3& lvx, const A3& lvy, const A3& lvz) {
+    for (int a = 0; a < 3; ++a) w[a].alloc(nx, ny, nz);
+    for (int a = 0; a < 3; ++a) {
+      FOR3(nx, ny, nz) {
+        double A[3];
+        abar(a, i, j, k, A);
+        double m = std::sqrt(A[0] * A[0] + A[1] * A[1] + A[2] * A[2]);
+        w[a](i, j, k) = lvx(i, j, k) * (A[0] / m) + lvy(i, j, k) * (A[1] / m) + lvz(i, j, k) * (A[2] / m);
+      }
+    }
+  }
+
+  // Edge circulation E.dl in metric form.  The reference's procedure runs on
+  // normal components: w^a (corner-limited like v) and the face-normal field
+  // b_a = Phi_a / |A_a| (reconstructed to the edge and upwinded like bi/bj/bk):
+  //   E.dl = g_e (-w1 b2u + w2 b1u) + eta |dl_e| (b1l + b2r - b1r - b2l),
+  //   g_e = |A1|_e |A2|_e / Vbar_e,
+  // |A1|_e, |A2|_e the mean magnitudes of the two a1 (a2) faces that share
+  // the edge and Vbar_e the mean volume of its 4 cells.  On a Cartesian mesh
+  // g_e = |dl_e| = the edge length and E.dl = E dl of get_eijk_LFM.
+  void get_eijk_metric(const A3& lrho, const A3& lvx, const A3& lvy, const A3& lvz, const A3& lbx,
+                       const A3& lby, const A3& lbz, const A3& lbi, const A3& lbj, const A3& lbk) {
+    A3 vf(nx, ny, nz);
+    FOR3(nx, ny, nz) {
+      double u = lvx(i, j, k), v = lvy(i, j, k), ww = lvz(i, j, k);
+      double a = lbx(i, j, k), b = lby(i, j, k), c = lbz(i, j, k);
+      vf(i, j, k) = std::sqrt(u * u + v * v + ww * ww) + std::sqrt((a * a + b * b + c * c) / lrho(i, j, k));
+    }
+    get_w(lvx, lvy, lvz);
+    const A3* fb[3] = {&lbi, &lbj, &lbk};
+    A3 bn[3];
+    for (int a = 0; a < 3; ++a) {
+      const A3& F = *fb[a];
+      bn[a].alloc(F.n1, F.n2, F.n3);
+      FOR3(F.n1, F.n2, F.n3) { bn[a](i, j, k) = F(i, j, k) / amag(a, i, j, k); }
+    }
+    for (int kkk = 1; kkk <= 3; ++kkk) {
+      const int e = kkk - 1, a1 = (e + 1) % 3, a2 = (e + 2) % 3;
+      int ii = nx0 + 1, jj = ny0 + 1, kk = nz0 + 1;
+      if (e == 0) ii = nx0;
+      else if (e == 1) jj = ny0;
+      else kk = nz0;
+      // b1 = normal field of the a1 faces reconstructed along a2, b2 = that
+      // of the a2 faces along a1 (the reference's d1 / d2)
+      A3 w1av, w2av, b1l, b1r, b2l, b2r;
+      get_vav_center2corner(w[a1], w1av, kkk);
+      get_vav_center2corner(w[a2], w2av, kkk);
+      reconstruct_3d(b1l, b1r, bn[a1], ii, jj, kk, a2 + 1);
+      reconstruct_3d(b2l, b2r, bn[a2], ii, jj, kk, a1 + 1);
+      A3& E = (e == 0) ? ei : (e == 1) ? ej : ek;
+      E.alloc(ii, jj, kk);
+      FOR3(ii, jj, kk) {
+        double ga, dl;
+        edge_metric(e, ng + i, ng + j, ng + k, ga, dl);
+        int c[3] = {ng + i, ng + j, ng + k};  // upper cell of the edge
+        int m1[3] = {c[0], c[1], c[2]}, m2[3] = {c[0], c[1], c[2]}, m12[3] = {c[0], c[1], c[2]};
+        m1[a1] -= 1; m2[a2] -= 1; m12[a1] -= 1; m12[a2] -= 1;
+        double sig1 = fsign1(w1av(i, j, k)), sig2 = fsign1(w2av(i, j, k));
+        double b1u = (1.0 + sig2) / 2.0 * b1l(i, j, k) + (1.0 - sig2) / 2.0 * b1r(i, j, k);
+        double b2u = (1.0 + sig1) / 2.0 * b2l(i, j, k) + (1.0 - sig1) / 2.0 * b2r(i, j, k);
+        double dum = -w1av(i, j, k) * b2u + w2av(i, j, k) * b1u;
+        double eta = 0.25 * (vf(m12[0], m12[1], m12[2]) + vf(m2[0], m2[1], m2[2]) + vf(c[0], c[1], c[2]) +
+                             vf(m1[0], m1[1], m1[2]));
+        E(i, j, k) = ga * dum + eta * dl * (b1l(i, j, k) + b2r(i, j, k) - b1r(i, j, k) - b2l(i, j, k));
+      }
+    }
+  }
+
+  // g_e and |dl_e| of the e-directed edge whose upper cell is c = (ci,cj,ck)
+  void edge_metric(int e, int ci, int cj, int ck, double& ga, double& dl) const {
+    const int a1 = (e + 1) % 3, a2 = (e + 2) % 3;
+    int c[3] = {ci, cj, ck};
+    int m1[3] = {ci, cj, ck}, m2[3] = {ci, cj, ck}, m12[3] = {ci, cj, ck};
+    m1[a1] -= 1; m2[a2] -= 1; m12[a1] -= 1; m12[a2] -= 1;
+    double vb = 0.25 * (vol(m12[0], m12[1], m12[2]) + vol(m2[0], m2[1], m2[2]) + vol(c[0], c[1], c[2]) +
+                        vol(m1[0], m1[1], m1[2]));
+    double a1b = 0.5 * (amag(a1, m2[0], m2[1], m2[2]) + amag(a1, c[0], c[1], c[2]));
+    double a2b = 0.5 * (amag(a2, m1[0], m1[1], m1[2]) + amag(a2, c[0], c[1], c[2]));
+    ga = a1b * a2b / vb;
+    int ce[3] = {ci, cj, ck};
+    ce[e] += 1;
+    double p0[3], p1[3];
+    node(ci, cj, ck, p0);
+    node(ce[0], ce[1], ce[2], p1);
+    dl = std::sqrt((p1[0] - p0[0]) * (p1[0] - p0[0]) + (p1[1] - p0[1]) * (p1[1] - p0[1]) +
+                   (p1[2] - p0[2]) * (p1[2] - p0[2]));
+  }
+
+  // conserved update with fluxes already multiplied by areas: / V
+  void advance_corrector_metric(int which) {
+    A3* F = flux[0]; A3* Gf = flux[1]; A3* H = flux[2];
+    const int G = ng;
+    FOR3(nx0, ny0, nz0) {
+      double V = vol(G + i, G + j, G + k);
+      auto d = [&](int q) {
+        return ((F[q](i + 1, j, k) - F[q](i, j, k)) + (Gf[q](i, j + 1, k) - Gf[q](i, j, k)) +
+                (H[q](i, j, k + 1) - H[q](i, j, k))) / V;
+      };
+      if (which == 1) {
+        rho(G + i, G + j, G + k) = rho0(G + i, G + j, G + k) - tau * d(0);
+        eng(G + i, G + j, G + k) = eng0(G + i, G + j, G + k) - tau * d(4);
+        rhovx(G + i, G + j, G + k) = rhovx0(G + i, G + j, G + k) - tau * d(1);
+        rhovy(G + i, G + j, G + k) = rhovy0(G + i, G + j, G + k) - tau * d(2);
+        rhovz(G + i, G + j, G + k) = rhovz0(G + i, G + j, G + k) - tau * d(3);
+      } else {
+        rhovx(G + i, G + j, G + k) = rhovx(G + i, G + j, G + k) - tau * d(5);
+        rhovy(G + i, G + j, G + k) = rhovy(G + i, G + j, G + k) - tau * d(6);
+        rhovz(G + i, G + j, G + k) = rhovz(G + i, G + j, G + k) - tau * d(7);
+      }
+    }
+  }
+
+  // face fluxes: Phi -= tau * circulation of E.dl
+  void advance_bijk_metric() {
+    const int G = ng;
+    FOR3(nx0 + 1, ny0, nz0) {
+      bi(G + i, G + j, G + k) = bi(G + i, G + j, G + k) -
+          tau * ((ek(i, j + 1, k) - ek(i, j, k)) - (ej(i, j, k + 1) - ej(i, j, k)));
+    }
+    FOR3(nx0, ny0 + 1, nz0) {
+      bj(G + i, G + j, G + k) = bj(G + i, G + j, G + k) -
+          tau * ((ei(i, j, k + 1) - ei(i, j, k)) - (ek(i + 1, j, k) - ek(i, j, k)));
+    }
+    FOR3(nx0, ny0, nz0 + 1) {
+      bk(G + i, G + j, G + k) = bk(G + i, G + j, G + k) -
+          tau * ((ej(i + 1, j, k) - ej(i, j, k)) - (ei(i, j + 1, k) - ei(i, j, k)));
+    }
+  }
+
   void check_status(double dtc) {
     // diag_rho_neg / diag_overflow (mhd3d3.f90:3143-3160) as status bits
     bool nan = false, negr = false, negp = false;
@@ -920,14 +1250,16 @@ struct Oracle {
       for (int j = 1; j <= ny0; ++j)
         for (int i = 1; i <= nx0; ++i) {
           int I = G + i, J = G + j, K = G + k;
-          double dv = dxv[I - 1] * dyv[J - 1] * dzv[K - 1];
+          double dv = metric ? vol(I, J, K) : dxv[I - 1] * dyv[J - 1] * dzv[K - 1];
           double r = rho(I, J, K), u = vx(I, J, K), v = vy(I, J, K), w = vz(I, J, K);
           double a = bx(I, J, K), b = by(I, J, K), c = bz(I, J, K);
           add(ms, mc, r * dv);
           double e = 0.5 * r * (u * u + v * v + w * w) + p(I, J, K) / (gam - 1.0) + 0.5 * (a * a + b * b + c * c);
           add(es, ec, e * dv);
-          double db = (bi(I + 1, J, K) - bi(I, J, K)) / dxv[I - 1] + (bj(I, J + 1, K) - bj(I, J, K)) / dyv[J - 1] +
-                      (bk(I, J, K + 1) - bk(I, J, K)) / dzv[K - 1];
+          double db = metric ? ((bi(I + 1, J, K) - bi(I, J, K)) + (bj(I, J + 1, K) - bj(I, J, K)) +
+                                (bk(I, J, K + 1) - bk(I, J, K))) / vol(I, J, K)
+                             : (bi(I + 1, J, K) - bi(I, J, K)) / dxv[I - 1] + (bj(I, J + 1, K) - bj(I, J, K)) / dyv[J - 1] +
+                                   (bk(I, J, K + 1) - bk(I, J, K)) / dzv[K - 1];
           dmax = std::max(dmax, std::fabs(db));
         }
     for (double r : rho.v) rmin = std::min(rmin, r);
@@ -948,9 +1280,12 @@ void copy_out(const A3& a, double* dst) {
 
 extern "C" {
 
-void* oracle_init(const mhd_params* prm, const double* rho, const double* vx, const double* vy,
-                  const double* vz, const double* p, const double* bi, const double* bj,
-                  const double* bk, const double* dx, const double* dy, const double* dz) {
+// Shared by oracle_init and oracle_init_mapped: dx/dy/dz are null in
+// metric mode, xn/yn/zn null in Cartesian mode.
+static void* init_common(const mhd_params* prm, const double* rho, const double* vx, const double* vy,
+                         const double* vz, const double* p, const double* bi, const double* bj,
+                         const double* bk, const double* dx, const double* dy, const double* dz,
+                         const double* xn, const double* yn, const double* zn) {
   Oracle* o = new Oracle();
   o->nx0 = prm->nx0; o->ny0 = prm->ny0; o->nz0 = prm->nz0;
   o->nord = prm->nord; o->ng = prm->nord / 2;
@@ -963,7 +1298,15 @@ void* oracle_init(const mhd_params* prm, const double* rho, const double* vx, co
   o->pi = 4.0 * std::atan(1.0);
   o->tau = prm->tau; o->tau0 = prm->tau;  // read_input: tau0=tau (mhd3d3.f90:196)
   int nx = o->nx, ny = o->ny, nz = o->nz;
-  o->dxv.assign(dx, dx + nx); o->dyv.assign(dy, dy + ny); o->dzv.assign(dz, dz + nz);
+  if (xn) {
+    o->metric = true;
+    o->dxv.assign(nx, 1.0); o->dyv.assign(ny, 1.0); o->dzv.assign(nz, 1.0);
+    for (int c = 0; c < 3; ++c) o->X[c].alloc(nx + 1, ny + 1, nz + 1);
+    copy_in(o->X[0], xn); copy_in(o->X[1], yn); copy_in(o->X[2], zn);
+    o->metric_geometry();
+  } else {
+    o->dxv.assign(dx, dx + nx); o->dyv.assign(dy, dy + ny); o->dzv.assign(dz, dz + nz);
+  }
   A3* cells[] = {&o->rho, &o->vx, &o->vy, &o->vz, &o->p, &o->bx, &o->by, &o->bz, &o->rhovx, &o->rhovy,
                  &o->rhovz, &o->eng, &o->rho0, &o->rhovx0, &o->rhovy0, &o->rhovz0, &o->eng0, &o->rhop,
                  &o->vxp, &o->vyp, &o->vzp, &o->pp, &o->bxp, &o->byp, &o->bzp, &o->rhovxp, &o->rhovyp,
@@ -984,6 +1327,28 @@ void* oracle_init(const mhd_params* prm, const double* rho, const double* vx, co
     o->bxp = o->bx; o->byp = o->by; o->bzp = o->bz; o->bip = o->bi; o->bjp = o->bj; o->bkp = o->bk;
   }
   return o;
+}
+
+void* oracle_init(const mhd_params* prm, const double* rho, const double* vx, const double* vy,
+                  const double* vz, const double* p, const double* bi, const double* bj,
+                  const double* bk, const double* dx, const double* dy, const double* dz) {
+  return init_common(prm, rho, vx, vy, vz, p, bi, bj, bk, dx, dy, dz, nullptr, nullptr, nullptr);
+}
+
+// Metric mode: bi/bj/bk are face fluxes Phi = B.A; xn/yn/zn are the
+// ghost-inclusive node coordinates, (nx+1)(ny+1)(nz+1) each, Fortran order.
+void* oracle_init_mapped(const mhd_params* prm, const double* rho, const double* vx, const double* vy,
+                         const double* vz, const double* p, const double* phi_i, const double* phi_j,
+                         const double* phi_k, const double* xn, const double* yn, const double* zn) {
+  return init_common(prm, rho, vx, vy, vz, p, phi_i, phi_j, phi_k, nullptr, nullptr, nullptr, xn, yn, zn);
+}
+
+// Cell volumes (nx, ny, nz) of a metric-mode oracle.
+int oracle_volumes(void* h, double* out) {
+  Oracle* o = (Oracle*)h;
+  if (!o->metric) return -1;
+  copy_out(o->vol, out);
+  return 0;
 }
 
 int oracle_step(void* h, int nsteps, double* tau_out, uint32_t* status) {

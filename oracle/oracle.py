@@ -38,6 +38,9 @@ def load():
         from mhd3d_mpi_fortran_gb300.abi import CParams
         lib.oracle_init.restype = C.c_void_p
         lib.oracle_init.argtypes = [C.POINTER(CParams)] + [_DP] * 11
+        lib.oracle_init_mapped.restype = C.c_void_p
+        lib.oracle_init_mapped.argtypes = [C.POINTER(CParams)] + [_DP] * 11
+        lib.oracle_volumes.argtypes = [C.c_void_p, _DP]
         lib.oracle_step.argtypes = [C.c_void_p, C.c_int, _DP, C.POINTER(C.c_uint32)]
         lib.oracle_fetch.argtypes = [C.c_void_p] + [_DP] * 11
         lib.oracle_fluxes.argtypes = [C.c_void_p, _DP]
@@ -63,10 +66,16 @@ class OracleSolver:
         self.params = params
         g = state.grid
         arrs = [np.asfortranarray(a, dtype=np.float64) for a in state.arrays()]
+        self._cp = params.to_c()
+        self.metric = getattr(state, "nodes", None) is not None
+        if self.metric:
+            nodes = [np.asfortranarray(a, dtype=np.float64) for a in state.nodes]
+            self.h = self.lib.oracle_init_mapped(C.byref(self._cp), *[_ptr(a) for a in arrs],
+                                                 *[_ptr(a) for a in nodes])
+            return
         geo = [np.ascontiguousarray(g.dx if dx is None else dx, dtype=np.float64),
                np.ascontiguousarray(g.dy if dy is None else dy, dtype=np.float64),
                np.ascontiguousarray(g.dz if dz is None else dz, dtype=np.float64)]
-        self._cp = params.to_c()
         self.h = self.lib.oracle_init(C.byref(self._cp), *[_ptr(a) for a in arrs], *[_ptr(a) for a in geo])
 
     def step(self, n: int = 1):
@@ -90,6 +99,13 @@ class OracleSolver:
         out = np.zeros(5)
         self.lib.oracle_diagnostics(self.h, _ptr(out))
         return dict(zip(("mass", "energy", "divb_max", "rho_min", "dt_cfl"), out.tolist()))
+
+    def volumes(self) -> np.ndarray:
+        """Cell volumes of a metric-mode oracle (ghost-inclusive)."""
+        nx, ny, nz = self.params.shape
+        out = np.zeros((nx, ny, nz), order="F")
+        assert self.lib.oracle_volumes(self.h, _ptr(out)) == 0
+        return out
 
     def fluxes(self) -> list:
         p = self.params
