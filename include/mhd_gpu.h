@@ -90,6 +90,23 @@ int mhd_init(const mhd_params* prm,
              const double* p, const double* bi, const double* bj, const double* bk,
              const double* dx, const double* dy, const double* dz, void** handle);
 
+/* Curvilinear metric mode (no reference counterpart: the reference mesh is
+ * Cartesian, init_geom mhd3d3.f90:3473-3486).  xn, yn, zn are the physical
+ * coordinates of the ghost-inclusive mesh nodes, each (nx+1, ny+1, nz+1) in
+ * Fortran order; phi_i/j/k are the magnetic fluxes B.A through the faces
+ * (same extents as bi/bj/bk).  The library computes the FP64 metric (face
+ * area vectors and normals, cell volumes, edge lengths) on the device.
+ * Fluxes go through the face area vectors, the conserved update divides by
+ * the cell volume and CT advances the face fluxes by the circulation of E.dl,
+ * so every term reduces to the Cartesian scheme on a rectilinear mesh.
+ * mhd_fetch then returns the face fluxes in bi/bj/bk and the cell-centred B
+ * in bx/by/bz; mhd_diagnostics uses the cell volumes.  Returns MHD_E_ARG for a
+ * mesh with a non-positive interior cell volume. */
+int mhd_init_mapped(const mhd_params* prm,
+                    const double* rho, const double* vx, const double* vy, const double* vz,
+                    const double* p, const double* phi_i, const double* phi_j, const double* phi_k,
+                    const double* xn, const double* yn, const double* zn, void** handle);
+
 /* One time step (replaces `call step`, mhd3d3.f90:3286).  On return *tau_out
  * (if non-NULL) holds the dt the step used (the module `tau` after the step)
  * and *status (if non-NULL) the MHD_ST_* bits of the checks made during it.

@@ -23,7 +23,7 @@ ST_NAN, ST_NEG_RHO, ST_NEG_P, ST_CFL, ST_TIMEOUT, ST_CUDA_ERROR = 1, 2, 4, 8, 16
 E_OK, E_ARG, E_CUDA, E_NOMEM, E_TIMEOUT, E_STATE = 0, -1, -2, -3, -4, -5
 
 EXPORTS = (
-    "mhd_init", "mhd_step", "mhd_step_n", "mhd_fetch", "mhd_diagnostics", "mhd_step_graph",
+    "mhd_init", "mhd_init_mapped", "mhd_step", "mhd_step_n", "mhd_fetch", "mhd_diagnostics", "mhd_step_graph",
     "mhd_set_tau", "mhd_set_profiling", "mhd_last_timings", "mhd_free", "mhd_last_error",
     "mhd_debug_fluxes", "mhd_debug_emf", "mhd_ensemble_step", "mhd_time_steps",
     "mhd_diagnostics_noalloc", "mhd_checkpoint_save", "mhd_checkpoint_load",
@@ -106,6 +106,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     dp = C.POINTER(C.c_double)
     vp = C.c_void_p
     lib.mhd_init.argtypes = [C.POINTER(CParams)] + [dp] * 11 + [C.POINTER(vp)]
+    lib.mhd_init_mapped.argtypes = [C.POINTER(CParams)] + [dp] * 11 + [C.POINTER(vp)]
     lib.mhd_step.argtypes = [vp, dp, C.POINTER(C.c_uint32)]
     lib.mhd_step_n.argtypes = [vp, C.c_int32, dp, C.POINTER(C.c_uint32)]
     lib.mhd_step_graph.argtypes = [vp, C.c_int32, dp, C.POINTER(C.c_uint32)]
@@ -132,10 +133,14 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
 
 
 class MHDError(RuntimeError):
-    pass
+    """A C-ABI call returned a negative MHD_E_* code (kept in ``code``)."""
+
+    def __init__(self, msg: str, code: int = 0):
+        super().__init__(msg)
+        self.code = code
 
 
 def check(lib, rc: int, what: str) -> None:
     if rc != 0:
         msg = lib.mhd_last_error()
-        raise MHDError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
+        raise MHDError(f"{what} failed ({rc}): {msg.decode() if msg else ''}", rc)

@@ -5,6 +5,9 @@ linked into one C-ABI library (declared in ``include/mhd_gpu.h``):
 
 * ``csrc/mhd_fp64.cu`` -- FP64 kernels, ``-fmad=false`` (reference rounding),
 * ``csrc/mhd_fp32.cu`` -- FP32 kernels (FMA contraction on),
+* ``csrc/mhd_metric_fp64.cu`` / ``mhd_metric_fp32.cu`` -- the same kernels in
+  curvilinear metric mode,
+* ``csrc/mhd_geom.cu`` -- FP64 metric terms from node coordinates (``-fmad=false``),
 * ``csrc/mhd_api.cu``  -- host sequencing and the ``extern "C"`` entry points,
 * ``csrc/mhd_noalloc.cu`` -- the allocation-free diagnostics entry point.
 
@@ -33,6 +36,9 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "mhd_fp64": ["-fmad=false"],
     "mhd_fp32": ["-fmad=true"],
+    "mhd_metric_fp64": ["-fmad=false"],
+    "mhd_metric_fp32": ["-fmad=true"],
+    "mhd_geom": ["-fmad=false"],
     "mhd_api": ["-Xcompiler", "-fopenmp"],
     "mhd_noalloc": ["-fmad=false"],
 }

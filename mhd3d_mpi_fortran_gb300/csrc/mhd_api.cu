@@ -1,6 +1,8 @@
 // C ABI of the GB300 MHD step (declared in include/mhd_gpu.h).  Host-side
 // sequencing of one time step on one CUDA stream; every kernel is in
-// mhd_kernels.cuh, instantiated per precision in mhd_fp32.cu / mhd_fp64.cu.
+// mhd_kernels.cuh, instantiated per precision in mhd_fp32.cu / mhd_fp64.cu
+// (Cartesian) and mhd_metric_fp32.cu / mhd_metric_fp64.cu (curvilinear
+// metric mode, handles made by mhd_init_mapped).
 //
 // Step sequence (reference routine -> launches):
 //   step_rk2/rk3 (mhd3d3.f90:3648-3792):
@@ -13,6 +15,7 @@
 //     get_dt -> cfl(AB); advance_predictor_ab -> predictor_ab; emf(h);
 //     hydro(h); ct; fill_bxyz.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -67,6 +70,9 @@ struct Handle {
   int par = 0;                 // which half of the double-buffered primitives is current
   float* geoT = nullptr;       // FP32 copy of the cell widths
   int* gmap = nullptr;         // ghost-image tables
+  bool metric = false;         // curvilinear metric mode (mhd_init_mapped)
+  double* met = nullptr;       // FP64 metric arrays (kMetricArrays x vol)
+  std::vector<double> nodes;   // host copy of the node coordinates (checkpoints)
   // graphs keyed by (nsteps, starting parity) -> (exec, parity after replay)
   std::map<std::pair<int, int>, std::pair<cudaGraphExec_t, int>> graphs;
 };
@@ -154,30 +160,31 @@ Dev<T> at_par(const Dev<T>& base, int par) {
   return d;
 }
 
-template <typename T>
+template <typename T, bool M>
 void enqueue_step(Handle* h, int& par, cudaStream_t st, Rec* r = nullptr) {
+  typedef Launch<T, M> L;
   Rec none;
   Rec& R = r ? *r : none;
   const Dev<T>& base = dev<T>(h);
   const mhd_params& p = h->prm;
   if (p.stepop == MHD_STEP_AB2) {
     Dev<T> d = at_par(base, par);
-    R.begin(); Launch<T>::cfl(d, 2, st); Launch<T>::predictor_ab(d, st); R.end(6);
+    R.begin(); L::cfl(d, 2, st); L::predictor_ab(d, st); R.end(6);
     Inp<T> in = half_inp(d);
-    R.begin(); Launch<T>::emf(d, in, st); R.end(3);
+    R.begin(); L::emf(d, in, st); R.end(3);
     for (int part = 0; part < 3; ++part) {
-      R.begin(); Launch<T>::hydro(d, in, part, -1, 0.0, 1.0, true, st); R.end(part);
+      R.begin(); L::hydro(d, in, part, -1, 0.0, 1.0, true, st); R.end(part);
     }
-    R.begin(); Launch<T>::ct(d, -1, 0.0, 1.0, st); R.end(4);
+    R.begin(); L::ct(d, -1, 0.0, 1.0, st); R.end(4);
     par ^= 1;
     d = at_par(base, par);
-    R.begin(); Launch<T>::fill_bxyz(d, false, st); R.end(5);
+    R.begin(); L::fill_bxyz(d, false, st); R.end(5);
     return;
   }
   {
     Dev<T> d = at_par(base, par);
     R.begin();
-    Launch<T>::cfl(d, p.dt_mode == MHD_DT_CFL ? 1 : 0, st, true);
+    L::cfl(d, p.dt_mode == MHD_DT_CFL ? 1 : 0, st, true);
     R.end(6);
   }
   int nst = (p.stepop == MHD_STEP_RK2) ? 2 : 3;
@@ -191,15 +198,22 @@ void enqueue_step(Handle* h, int& par, cudaStream_t st, Rec* r = nullptr) {
     }
     Dev<T> d = at_par(base, par);
     Inp<T> in = state_inp(d);
-    R.begin(); Launch<T>::emf(d, in, st); R.end(3);
+    R.begin(); L::emf(d, in, st); R.end(3);
     for (int part = 0; part < 3; ++part) {
-      R.begin(); Launch<T>::hydro(d, in, part, form, c, den, false, st); R.end(part);
+      R.begin(); L::hydro(d, in, part, form, c, den, false, st); R.end(part);
     }
-    R.begin(); Launch<T>::ct(d, form, c, den, st); R.end(4);
+    R.begin(); L::ct(d, form, c, den, st); R.end(4);
     par ^= 1;
     d = at_par(base, par);
-    R.begin(); Launch<T>::fill_bxyz(d, true, st); R.end(5);
+    R.begin(); L::fill_bxyz(d, true, st); R.end(5);
   }
+}
+
+// Cartesian or metric step of a handle.
+template <typename T>
+void enqueue_any(Handle* h, int& par, cudaStream_t st, Rec* r = nullptr) {
+  if (h->metric) enqueue_step<T, true>(h, par, st, r);
+  else enqueue_step<T, false>(h, par, st, r);
 }
 
 inline void set_widths(Handle* h, Dev<double>& d) {
@@ -244,10 +258,53 @@ void carve(Handle* h, Dev<T>& d, char* base) {
   d.gmap = h->gmap;
   d.partial = nullptr;
   d.counter = nullptr;
+  d.m = Metric{};
+  for (int a = 0; a < 3; ++a) {
+    d.mw[a] = h->metric ? next() : nullptr;
+    d.mbn[a] = h->metric ? next() : nullptr;
+  }
+  if (h->metric) {
+    const double* mb = h->met;
+    auto nm = [&]() { const double* r = mb; mb += n; return r; };
+    Metric& m = d.m;
+    for (int a = 0; a < 3; ++a)
+      for (int q = 0; q < 3; ++q) m.nrm[a][q] = nm();
+    for (int a = 0; a < 3; ++a) m.am[a] = nm();
+    m.vol = nm();
+    m.rvol = nm();
+    for (int a = 0; a < 3; ++a)
+      for (int q = 0; q < 3; ++q) m.eb[a][q] = nm();
+    for (int a = 0; a < 3; ++a)
+      for (int q = 0; q < 3; ++q) m.nb[a][q] = nm();
+    m.sa = nm();
+    for (int e = 0; e < 3; ++e) m.ge[e] = nm();
+    for (int e = 0; e < 3; ++e) m.dl[e] = nm();
+  }
 }
 
-size_t n_arrays(const mhd_params& p) {
-  size_t n = 11 + 5 + 8 + ((p.stepop == MHD_STEP_AB2) ? 22 : 8) + 24 + 3 + 1;
+// The writable view of the metric block carved as carve() lays it out.
+MetricOut metric_out(Handle* h) {
+  const size_t n = (size_t)h->g.vol;
+  double* mb = h->met;
+  auto nm = [&]() { double* r = mb; mb += n; return r; };
+  MetricOut m;
+  for (int a = 0; a < 3; ++a)
+    for (int q = 0; q < 3; ++q) m.nrm[a][q] = nm();
+  for (int a = 0; a < 3; ++a) m.am[a] = nm();
+  m.vol = nm();
+  m.rvol = nm();
+  for (int a = 0; a < 3; ++a)
+    for (int q = 0; q < 3; ++q) m.eb[a][q] = nm();
+  for (int a = 0; a < 3; ++a)
+    for (int q = 0; q < 3; ++q) m.nb[a][q] = nm();
+  m.sa = nm();
+  for (int e = 0; e < 3; ++e) m.ge[e] = nm();
+  for (int e = 0; e < 3; ++e) m.dl[e] = nm();
+  return m;
+}
+
+size_t n_arrays(const mhd_params& p, bool metric) {
+  size_t n = 11 + 5 + 8 + ((p.stepop == MHD_STEP_AB2) ? 22 : 8) + 24 + 3 + 1 + (metric ? 6 : 0);
   return n;
 }
 
@@ -318,14 +375,14 @@ int upload(Handle* h, const double* const* arrs) {
   return rc;
 }
 
-template <typename T>
+template <typename T, bool M>
 int init_device(Handle* h) {
   Dev<T>& d = dev<T>(h);
   cudaStream_t st = h->st;
-  Launch<T>::fill(d, st);
-  Launch<T>::bxyz_vf(d, h->prm.stepop != MHD_STEP_AB2, st);
+  Launch<T, M>::fill(d, st);
+  Launch<T, M>::bxyz_vf(d, h->prm.stepop != MHD_STEP_AB2, st);
   if (h->prm.stepop == MHD_STEP_AB2) {
-    if (!(h->prm.tau > 0.0)) Launch<T>::cfl(d, 1, st);  // prime with the CFL dt (mhd3d2)
+    if (!(h->prm.tau > 0.0)) Launch<T, M>::cfl(d, 1, st);  // prime with the CFL dt (mhd3d2)
     T* x[11] = {d.rho, d.vx, d.vy, d.vz, d.p, d.bi, d.bj, d.bk, d.bx, d.by, d.bz};
     for (int a = 0; a < 11; ++a)
       CK(cudaMemcpyAsync(d.q[a], x[a], (size_t)h->g.vol * sizeof(T), cudaMemcpyDeviceToDevice, st));
@@ -341,7 +398,7 @@ int do_steps(Handle* h, int n) {
     Rec r;
     r.h = h; r.st = h->st; r.pool = &h->pool; r.fam = &h->fam;
     h->fam.clear();
-    for (int s = 0; s < n; ++s) enqueue_step<T>(h, h->par, h->st, &r);
+    for (int s = 0; s < n; ++s) enqueue_any<T>(h, h->par, h->st, &r);
     CK(cudaGetLastError());
     int rc = wait_stream(h);
     if (rc) return rc;
@@ -352,7 +409,7 @@ int do_steps(Handle* h, int n) {
     }
     return MHD_OK;
   }
-  for (int s = 0; s < n; ++s) enqueue_step<T>(h, h->par, h->st);
+  for (int s = 0; s < n; ++s) enqueue_any<T>(h, h->par, h->st);
   CK(cudaGetLastError());
   return MHD_OK;
 }
@@ -429,11 +486,12 @@ const char* mhd_last_error(void) { return g_err.c_str(); }
 // Handle with its device buffers allocated and cleared, scalars set from prm,
 // but no fields uploaded yet.
 static int create_handle(const mhd_params* prm, const double* dx, const double* dy, const double* dz,
-                         Handle** out) {
+                         Handle** out, bool metric = false) {
   *out = nullptr;
   Handle* h = new Handle();
   h->prm = *prm;
   h->fp32 = (prm->precision == MHD_FP32);
+  h->metric = metric;
   Geom& g = h->g;
   g.nx0 = prm->nx0; g.ny0 = prm->ny0; g.nz0 = prm->nz0;
   g.nord = prm->nord; g.ng = prm->nord / 2;
@@ -448,7 +506,7 @@ static int create_handle(const mhd_params* prm, const double* dx, const double* 
     return fail(MHD_E_ARG, "grid too large for 32-bit indexing");
   }
   size_t es = h->fp32 ? sizeof(float) : sizeof(double);
-  h->bytes = n_arrays(*prm) * (size_t)g.vol * es;
+  h->bytes = n_arrays(*prm, metric) * (size_t)g.vol * es;
   auto bail = [&](int code, const std::string& m) {
     mhd_free(h);
     return fail(code, m);
@@ -456,6 +514,8 @@ static int create_handle(const mhd_params* prm, const double* dx, const double* 
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess)
     return bail(MHD_E_CUDA, "stream create failed");
   if (cudaMalloc(&h->buf, h->bytes) != cudaSuccess) return bail(MHD_E_NOMEM, "device allocation failed");
+  if (metric && cudaMalloc(&h->met, sizeof(double) * kMetricArrays * (size_t)g.vol) != cudaSuccess)
+    return bail(MHD_E_NOMEM, "device allocation of the metric failed");
   if (cudaMalloc(&h->geo, sizeof(double) * (g.nx + g.ny + g.nz)) != cudaSuccess ||
       cudaMalloc(&h->sc, sizeof(Scal)) != cudaSuccess ||
       cudaMalloc(&h->diag, sizeof(double) * (8 + 5 * 152 * 2)) != cudaSuccess)
@@ -518,7 +578,76 @@ int mhd_init(const mhd_params* prm, const double* rho, const double* vx, const d
   const double* arrs[8] = {rho, vx, vy, vz, p, bi, bj, bk};
   rc = h->fp32 ? upload<float>(h, arrs) : upload<double>(h, arrs);
   if (rc) { std::string m = g_err; mhd_free(h); return fail(rc, m); }
-  rc = h->fp32 ? init_device<float>(h) : init_device<double>(h);
+  rc = h->fp32 ? init_device<float, false>(h) : init_device<double, false>(h);
+  if (rc) { std::string m = g_err; mhd_free(h); return fail(rc, m); }
+  *handle = h;
+  return MHD_OK;
+}
+
+// Metric mode: upload the node coordinates, compute the FP64 metric on the
+// device, reject meshes with a non-positive interior cell volume.
+static int setup_metric(Handle* h, const double* const xyz[3]) {
+  const Geom& g = h->g;
+  const size_t nn = (size_t)(g.nx + 1) * (g.ny + 1) * (g.nz + 1);
+  h->nodes.resize(3 * nn);
+  for (int a = 0; a < 3; ++a) std::memcpy(h->nodes.data() + a * nn, xyz[a], nn * sizeof(double));
+  for (double v : h->nodes)
+    if (!std::isfinite(v)) return fail(MHD_E_ARG, "node coordinates must be finite");
+  double* dn = nullptr;
+  double* mv = nullptr;
+  CK(cudaMalloc(&dn, sizeof(double) * 3 * (size_t)g.vol + sizeof(double)));
+  mv = dn + 3 * (size_t)g.vol;
+  int rc = MHD_OK;
+  if (cudaMemsetAsync(dn, 0, sizeof(double) * 3 * (size_t)g.vol, h->st) != cudaSuccess)
+    rc = fail(MHD_E_CUDA, "metric set-up memset failed");
+  std::vector<double> stage(rc ? 0 : (size_t)g.vol);
+  for (int a = 0; a < 3 && rc == MHD_OK; ++a) {
+    pack<double>(g, h->nodes.data() + a * nn, g.nx + 1, g.ny + 1, g.nz + 1, stage.data());
+    if (cudaMemcpyAsync(dn + a * (size_t)g.vol, stage.data(), sizeof(double) * (size_t)g.vol,
+                        cudaMemcpyHostToDevice, h->st) != cudaSuccess ||
+        cudaStreamSynchronize(h->st) != cudaSuccess)
+      rc = fail(MHD_E_CUDA, "node coordinate upload failed");
+  }
+  double vmin = 0.0;
+  if (rc == MHD_OK) {
+    metric_geometry(g, dn, dn + (size_t)g.vol, dn + 2 * (size_t)g.vol, metric_out(h), mv, h->st);
+    if (cudaGetLastError() != cudaSuccess) rc = fail(MHD_E_CUDA, "metric kernels failed to launch");
+  }
+  if (rc == MHD_OK) {
+    if (cudaMemcpyAsync(&vmin, mv, sizeof(double), cudaMemcpyDeviceToHost, h->st) != cudaSuccess)
+      rc = fail(MHD_E_CUDA, "metric read-back failed");
+    else rc = wait_stream(h);
+  }
+  cudaFree(dn);
+  if (rc) return rc;
+  if (!(vmin > 0.0)) return fail(MHD_E_ARG, "mapped grid has a non-positive cell volume");
+  // the Dev views were carved before the metric existed: refresh them
+  if (h->fp32) carve<float>(h, h->df, (char*)h->buf);
+  else carve<double>(h, h->dd, (char*)h->buf);
+  return MHD_OK;
+}
+
+int mhd_init_mapped(const mhd_params* prm, const double* rho, const double* vx, const double* vy,
+                    const double* vz, const double* p, const double* phi_i, const double* phi_j,
+                    const double* phi_k, const double* xn, const double* yn, const double* zn, void** handle) {
+  if (!handle) return fail(MHD_E_ARG, "null handle pointer");
+  *handle = nullptr;
+  int rc = validate(prm);
+  if (rc) return rc;
+  if (!rho || !vx || !vy || !vz || !p || !phi_i || !phi_j || !phi_k || !xn || !yn || !zn)
+    return fail(MHD_E_ARG, "null field pointer");
+  const int nx = prm->nx0 + prm->nord, ny = prm->ny0 + prm->nord, nz = prm->nz0 + prm->nord;
+  std::vector<double> ones((size_t)nx + ny + nz, 1.0);
+  Handle* h = nullptr;
+  rc = create_handle(prm, ones.data(), ones.data() + nx, ones.data() + nx + ny, &h, true);
+  if (rc) return rc;
+  const double* xyz[3] = {xn, yn, zn};
+  rc = setup_metric(h, xyz);
+  if (rc) { std::string m = g_err; mhd_free(h); return fail(rc, m); }
+  const double* arrs[8] = {rho, vx, vy, vz, p, phi_i, phi_j, phi_k};
+  rc = h->fp32 ? upload<float>(h, arrs) : upload<double>(h, arrs);
+  if (rc) { std::string m = g_err; mhd_free(h); return fail(rc, m); }
+  rc = h->fp32 ? init_device<float, true>(h) : init_device<double, true>(h);
   if (rc) { std::string m = g_err; mhd_free(h); return fail(rc, m); }
   *handle = h;
   return MHD_OK;
@@ -547,8 +676,9 @@ int mhd_checkpoint_save(void* handle, const char* path) {
   if (h->fp32) ckpt_arrays<float>(h, arrs);
   else ckpt_arrays<double>(h, arrs);
   CK(cudaMemcpy(h->sc_h, h->sc, sizeof(Scal), cudaMemcpyDeviceToHost));
-  const uint32_t ver = 1, psz = (uint32_t)sizeof(mhd_params);
-  const uint32_t es = h->fp32 ? 4 : 8, na = (uint32_t)arrs.size() + 1;
+  // version 2: metric mode, with the node coordinates as record 200
+  const uint32_t ver = h->metric ? 2 : 1, psz = (uint32_t)sizeof(mhd_params);
+  const uint32_t es = h->fp32 ? 4 : 8, na = (uint32_t)arrs.size() + 1 + (h->metric ? 1 : 0);
   const double sc4[4] = {h->sc_h->tau, h->sc_h->tau0, h->sc_h->dt_cfl, h->sc_h->ab_coef};
   bool ok = std::fwrite(kMagic, 1, 16, f) == 16 && std::fwrite(&ver, 4, 1, f) == 1 &&
             std::fwrite(&psz, 4, 1, f) == 1 && std::fwrite(&h->prm, sizeof(mhd_params), 1, f) == 1 &&
@@ -571,6 +701,12 @@ int mhd_checkpoint_save(void* handle, const char* path) {
     ok = ok && std::fwrite(&id, 4, 1, f) == 1 && std::fwrite(&nb, 8, 1, f) == 1 &&
          std::fwrite(w.data(), 8, ng, f) == ng;
   }
+  if (ok && h->metric) {  // node coordinates X | Y | Z (FP64, ghost-inclusive, Fortran order)
+    const uint32_t id = 200;
+    const uint64_t nb = h->nodes.size() * 8;
+    ok = std::fwrite(&id, 4, 1, f) == 1 && std::fwrite(&nb, 8, 1, f) == 1 &&
+         std::fwrite(h->nodes.data(), 8, h->nodes.size(), f) == h->nodes.size();
+  }
   ok = (std::fclose(f) == 0) && ok;
   if (!ok) return fail(MHD_E_ARG, std::string("checkpoint write failed: ") + path);
   return MHD_OK;
@@ -586,7 +722,7 @@ int mhd_checkpoint_load(const char* path, void** handle) {
   mhd_params prm{};
   double sc4[4];
   bool ok = std::fread(magic, 1, 16, f) == 16 && std::memcmp(magic, kMagic, 16) == 0 &&
-            std::fread(&ver, 4, 1, f) == 1 && ver == 1 && std::fread(&psz, 4, 1, f) == 1 &&
+            std::fread(&ver, 4, 1, f) == 1 && (ver == 1 || ver == 2) && std::fread(&psz, 4, 1, f) == 1 &&
             psz == sizeof(mhd_params) && std::fread(&prm, sizeof(mhd_params), 1, f) == 1 &&
             std::fread(sc4, 8, 4, f) == 4 && std::fread(&es, 4, 1, f) == 1 && std::fread(&na, 4, 1, f) == 1;
   if (!ok || validate(&prm) != MHD_OK || es != (prm.precision == MHD_FP32 ? 4u : 8u)) {
@@ -597,22 +733,32 @@ int mhd_checkpoint_load(const char* path, void** handle) {
   const int nx = prm.nx0 + prm.nord, ny = prm.ny0 + prm.nord, nz = prm.nz0 + prm.nord;
   std::vector<double> ones((size_t)nx + ny + nz, 1.0);
   Handle* h = nullptr;
-  int rc = create_handle(&prm, ones.data(), ones.data() + nx, ones.data() + nx + ny, &h);
+  const bool metric = (ver == 2);
+  const size_t nnodes = (size_t)(nx + 1) * (ny + 1) * (nz + 1);
+  int rc = create_handle(&prm, ones.data(), ones.data() + nx, ones.data() + nx + ny, &h, metric);
   if (rc) { std::fclose(f); return rc; }
   std::vector<std::pair<uint32_t, void*>> arrs;
   if (h->fp32) ckpt_arrays<float>(h, arrs);
   else ckpt_arrays<double>(h, arrs);
   const size_t bytes = (size_t)h->g.vol * es;
-  std::vector<char> buf(bytes);
+  std::vector<char> buf(std::max(bytes, metric ? 3 * nnodes * 8 : (size_t)0));
   size_t loaded = 0;
   for (uint32_t n = 0; n < na && ok; ++n) {
     uint32_t id = 0;
     uint64_t nb = 0;
     ok = std::fread(&id, 4, 1, f) == 1 && std::fread(&nb, 8, 1, f) == 1 &&
-         (nb == bytes || (id == 999 && nb == ((size_t)nx + ny + nz) * 8)) &&
+         (nb == bytes || (id == 999 && nb == ((size_t)nx + ny + nz) * 8) ||
+          (metric && id == 200 && nb == 3 * nnodes * 8)) &&
          std::fread(buf.data(), 1, nb, f) == nb;
     if (!ok) break;
     void* dst = nullptr;
+    if (id == 200) {  // node coordinates: rebuild the metric
+      const double* nd = (const double*)buf.data();
+      const double* xyz[3] = {nd, nd + nnodes, nd + 2 * nnodes};
+      ok = setup_metric(h, xyz) == MHD_OK;
+      ++loaded;
+      continue;
+    }
     if (id == 999) {  // cell widths (FP64)
       const size_t ng = (size_t)nx + ny + nz;
       ok = cudaMemcpy(h->geo, buf.data(), ng * 8, cudaMemcpyHostToDevice) == cudaSuccess;
@@ -630,7 +776,7 @@ int mhd_checkpoint_load(const char* path, void** handle) {
     ++loaded;
   }
   std::fclose(f);
-  if (!ok || loaded != arrs.size() + 1) {
+  if (!ok || loaded != arrs.size() + 1 + (metric ? 1 : 0)) {
     mhd_free(h);
     return fail(MHD_E_ARG, std::string("checkpoint is truncated or inconsistent: ") + path);
   }
@@ -645,8 +791,13 @@ int mhd_checkpoint_load(const char* path, void** handle) {
   // vf (and cell B) as the end of the saved step left them: the same fused
   // kernel the step runs, on the restored fields
   const bool want_vf = prm.stepop != MHD_STEP_AB2;
-  if (h->fp32) Launch<float>::fill_bxyz(h->df, want_vf, h->st);
-  else Launch<double>::fill_bxyz(h->dd, want_vf, h->st);
+  if (h->fp32) {
+    if (metric) Launch<float, true>::fill_bxyz(h->df, want_vf, h->st);
+    else Launch<float>::fill_bxyz(h->df, want_vf, h->st);
+  } else {
+    if (metric) Launch<double, true>::fill_bxyz(h->dd, want_vf, h->st);
+    else Launch<double>::fill_bxyz(h->dd, want_vf, h->st);
+  }
   rc = wait_stream(h);
   if (rc) {
     std::string m = g_err;
@@ -699,8 +850,8 @@ static int graph_for(Handle* h, int nsteps, cudaGraphExec_t* out) {
   int par = h->par;
   CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
   for (int s = 0; s < nsteps; ++s) {
-    if (h->fp32) enqueue_step<float>(h, par, h->st);
-    else enqueue_step<double>(h, par, h->st);
+    if (h->fp32) enqueue_any<float>(h, par, h->st);
+    else enqueue_any<double>(h, par, h->st);
   }
   CK(cudaStreamEndCapture(h->st, &gr));
   CK(cudaGraphInstantiate(&ex, gr, 0));
@@ -820,17 +971,17 @@ int mhd_fetch(void* handle, double* rho, double* vx, double* vy, double* vz, dou
   return h->fp32 ? fetch_t<float>(h, outs) : fetch_t<double>(h, outs);
 }
 
-template <typename T>
+template <typename T, bool M>
 static int diag_t(Handle* h, double out[5]) {
   Dev<T> d = at_par(dev<T>(h), h->par);
-  Launch<T>::diagnostics(d, h->diag, h->st);
+  Launch<T, M>::diagnostics(d, h->diag, h->st);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(h->diag_h, h->diag, sizeof(double) * 4, cudaMemcpyDeviceToHost, h->st));
   int rc = wait_stream(h);
   if (rc) return rc;
   for (int i = 0; i < 4; ++i) out[i] = h->diag_h[i];
   // CFL dt of the current state: the dt kernel in "peek" mode (status kept)
-  Launch<T>::cfl(d, 3, h->st);
+  Launch<T, M>::cfl(d, 3, h->st);
   CK(cudaMemcpyAsync(h->sc_h, h->sc, sizeof(Scal), cudaMemcpyDeviceToHost, h->st));
   rc = wait_stream(h);
   if (rc) return rc;
@@ -841,14 +992,15 @@ static int diag_t(Handle* h, double out[5]) {
 int mhd_diagnostics(void* handle, double out[5]) {
   Handle* h = (Handle*)handle;
   if (!h || !out) return fail(MHD_E_ARG, "null argument");
-  return h->fp32 ? diag_t<float>(h, out) : diag_t<double>(h, out);
+  if (h->metric) return h->fp32 ? diag_t<float, true>(h, out) : diag_t<double, true>(h, out);
+  return h->fp32 ? diag_t<float, false>(h, out) : diag_t<double, false>(h, out);
 }
 
-template <typename T>
+template <typename T, bool M>
 static int dbg_flux_t(Handle* h, double* out) {
   const Geom& g = h->g;
   Dev<T> d = at_par(dev<T>(h), h->par);
-  Launch<T>::fluxes(d, state_inp(d), h->st);
+  Launch<T, M>::fluxes(d, state_inp(d), h->st);
   CK(cudaGetLastError());
   std::vector<T> host((size_t)g.vol);
   size_t off = 0;
@@ -872,15 +1024,16 @@ static int dbg_flux_t(Handle* h, double* out) {
 int mhd_debug_fluxes(void* handle, double* out) {
   Handle* h = (Handle*)handle;
   if (!h || !out) return fail(MHD_E_ARG, "null argument");
-  return h->fp32 ? dbg_flux_t<float>(h, out) : dbg_flux_t<double>(h, out);
+  if (h->metric) return h->fp32 ? dbg_flux_t<float, true>(h, out) : dbg_flux_t<double, true>(h, out);
+  return h->fp32 ? dbg_flux_t<float, false>(h, out) : dbg_flux_t<double, false>(h, out);
 }
 
-template <typename T>
+template <typename T, bool M>
 static int dbg_emf_t(Handle* h, double* const* outs) {
   const Geom& g = h->g;
   Dev<T> d = at_par(dev<T>(h), h->par);
-  Launch<T>::bxyz_vf(d, true, h->st);
-  Launch<T>::emf(d, state_inp(d), h->st);
+  Launch<T, M>::bxyz_vf(d, true, h->st);
+  Launch<T, M>::emf(d, state_inp(d), h->st);
   CK(cudaGetLastError());
   std::vector<T> host((size_t)g.vol);
   for (int e = 0; e < 3; ++e) {
@@ -902,7 +1055,8 @@ int mhd_debug_emf(void* handle, double* ei, double* ej, double* ek) {
   Handle* h = (Handle*)handle;
   if (!h) return fail(MHD_E_ARG, "null handle");
   double* outs[3] = {ei, ej, ek};
-  return h->fp32 ? dbg_emf_t<float>(h, outs) : dbg_emf_t<double>(h, outs);
+  if (h->metric) return h->fp32 ? dbg_emf_t<float, true>(h, outs) : dbg_emf_t<double, true>(h, outs);
+  return h->fp32 ? dbg_emf_t<float, false>(h, outs) : dbg_emf_t<double, false>(h, outs);
 }
 
 // Ensemble: one CUDA graph with one branch per grid (grids run concurrently),
@@ -943,8 +1097,8 @@ int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* 
       Handle* h = (Handle*)handles[i];
       int par = h->par;
       for (int s = 0; s < nsteps; ++s) {
-        if (h->fp32) enqueue_step<float>(h, par, h->st);
-        else enqueue_step<double>(h, par, h->st);
+        if (h->fp32) enqueue_any<float>(h, par, h->st);
+        else enqueue_any<double>(h, par, h->st);
       }
       pars[i] = par;
       if (i > 0) {
@@ -989,6 +1143,7 @@ int mhd_free(void* handle) {
   if (h->geo) cudaFree(h->geo);
   if (h->geoT) cudaFree(h->geoT);
   if (h->gmap) cudaFree(h->gmap);
+  if (h->met) cudaFree(h->met);
   if (h->sc) cudaFree(h->sc);
   if (h->diag) cudaFree(h->diag);
   if (h->sc_h) cudaFreeHost(h->sc_h);

@@ -309,8 +309,23 @@ __device__ __forceinline__ long long idx3(const Geom& g, int i, int j, int k) {
   return (long long)i + (long long)g.px * ((long long)j + (long long)g.py * (long long)k);
 }
 
-// get_bxyz over all cells (incl. ghosts) and vf = |v| + |B|/sqrt(rho).
+// Metric-mode cell B from the face fluxes of cell c (low / high faces):
+// B = sum_a (Phi_a averaged over the two a-faces / V) e_a, e_a the cell's
+// edge vector along a (the oracle's get_bxyz_metric, in its operand order).
 template <typename T>
+__device__ __forceinline__ void cell_b_metric(const Metric& m, long long c, T lo0, T hi0, T lo1, T hi1, T lo2,
+                                              T hi2, T& bx, T& by, T& bz) {
+  const T V = (T)m.vol[c], rV = (T)m.rvol[c];
+  const T p0 = Ops<T>::dw(T(0.5) * (hi0 + lo0), V, rV);
+  const T p1 = Ops<T>::dw(T(0.5) * (hi1 + lo1), V, rV);
+  const T p2 = Ops<T>::dw(T(0.5) * (hi2 + lo2), V, rV);
+  bx = p0 * (T)m.eb[0][0][c] + p1 * (T)m.eb[1][0][c] + p2 * (T)m.eb[2][0][c];
+  by = p0 * (T)m.eb[0][1][c] + p1 * (T)m.eb[1][1][c] + p2 * (T)m.eb[2][1][c];
+  bz = p0 * (T)m.eb[0][2][c] + p1 * (T)m.eb[1][2][c] + p2 * (T)m.eb[2][2][c];
+}
+
+// get_bxyz over all cells (incl. ghosts) and vf = |v| + |B|/sqrt(rho).
+template <typename T, bool M>
 __global__ void k_bxyz_vf(Dev<T> d, int want_vf) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -318,9 +333,14 @@ __global__ void k_bxyz_vf(Dev<T> d, int want_vf) {
   const Geom& g = d.g;
   if (i >= g.nx || j >= g.ny || k >= g.nz) return;
   long long c = idx3<T>(g, i, j, k);
-  T bx = T(0.5) * (d.bi[c + 1] + d.bi[c]);
-  T by = T(0.5) * (d.bj[c + g.px] + d.bj[c]);
-  T bz = T(0.5) * (d.bk[c + g.plane] + d.bk[c]);
+  T bx, by, bz;
+  if (M) {
+    cell_b_metric<T>(d.m, c, d.bi[c], d.bi[c + 1], d.bj[c], d.bj[c + g.px], d.bk[c], d.bk[c + g.plane], bx, by, bz);
+  } else {
+    bx = T(0.5) * (d.bi[c + 1] + d.bi[c]);
+    by = T(0.5) * (d.bj[c + g.px] + d.bj[c]);
+    bz = T(0.5) * (d.bk[c + g.plane] + d.bk[c]);
+  }
   d.bx[c] = bx;
   d.by[c] = by;
   d.bz[c] = bz;
@@ -340,7 +360,7 @@ __device__ __forceinline__ float cfl_sqrt(float x) { return x > 0.0f ? x * rsqrt
 // save != 0 also stores U^n of the RK stage combines (advance_previous,
 // 3794-3819) at interior cells and faces, the only places they are read.
 // The minimum is reduced in T and converted to FP64 once per block.
-template <typename T>
+template <typename T, bool M>
 __global__ void __launch_bounds__(256) k_cfl(Dev<T> d, int save) {
   const Geom& g = d.g;
   T m = T(INFINITY);
@@ -377,7 +397,11 @@ __global__ void __launch_bounds__(256) k_cfl(Dev<T> d, int save) {
     T valf = O::dv(btot, cfl_sqrt(r0));
     T vs = cfl_sqrt(O::dv(d.gam * p0, r0));
     T vcfl = vv + cfl_sqrt(valf * valf + vs * vs);
-    T dt = O::dv(d.cfl, O::dw(vcfl, d.wx[i], d.rwx[i]) + O::dw(vcfl, d.wy[j], d.rwy[j]) +
+    T dt;
+    if (M)  // metric mode: 1/dx_a -> |mean area vector of the a-faces| / V
+      dt = O::dv(d.cfl, O::dw(vcfl * (T)d.m.sa[c], (T)d.m.vol[c], (T)d.m.rvol[c]));
+    else
+      dt = O::dv(d.cfl, O::dw(vcfl, d.wx[i], d.rwx[i]) + O::dw(vcfl, d.wy[j], d.rwy[j]) +
                             O::dw(vcfl, d.wz[k], d.rwz[k]));
     m = (dt < m) ? dt : m;
     if (isnan(r0) || isnan(p0) || isnan(u) || isnan(v) || isnan(w)) st |= ST_NAN;
@@ -592,6 +616,55 @@ __device__ __forceinline__ void face_flux(const T* l, const T* r, T gam, T* out)
   }
 }
 
+// Metric-mode flux through a face of unit normal n and area am: the
+// Gaussian-split formulas of face_flux with n in place of the axis (vector
+// momentum and magnetic stress), left with the + moments and right with the
+// - moments, the sum multiplied by am (the oracle's get_flux_stress_metric).
+template <typename T>
+__device__ __forceinline__ void face_flux_n(const T* l, const T* r, T gam, const T* n, T am, T* out) {
+  typedef Moments<T> Mo;
+  const T gm1 = gam - T(1);
+  T tot[8];
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const T* s = side ? r : l;
+    const T rr = s[0], u0 = s[1], u1 = s[2], u2 = s[3], pr = s[4], b0 = s[5], b1 = s[6], b2 = s[7];
+    const T vn = u0 * n[0] + u1 * n[1] + u2 * n[2];
+    const T bn = b0 * n[0] + b1 * n[1] + b2 * n[2];
+    const T leng = T(0.5) * rr * (u0 * u0 + u1 * u1 + u2 * u2) + Ops<T>::dv(pr, gm1);
+    T lam = Mo::div(rr, T(2) * pr);
+    T v0, v1;
+    Mo::hydro(lam, vn, side == 0, v0, v1);
+    T f[8];
+    f[0] = rr * v1;
+    f[1] = rr * u0 * v1 + pr * n[0] * v0;
+    f[2] = rr * u1 * v1 + pr * n[1] * v0;
+    f[3] = rr * u2 * v1 + pr * n[2] * v0;
+    f[4] = (leng + T(0.5) * pr) * v1 + T(0.5) * pr * vn * v0;
+    const T lbsq = b0 * b0 + b1 * b1 + b2 * b2;
+    lam = Mo::div(rr, T(2) * pr + lbsq);
+    v0 = Mo::mag(lam, vn, side == 0);
+    f[5] = (T(0.5) * lbsq * n[0] - b0 * bn) * v0;
+    f[6] = (T(0.5) * lbsq * n[1] - b1 * bn) * v0;
+    f[7] = (T(0.5) * lbsq * n[2] - b2 * bn) * v0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) tot[q] = side ? tot[q] + f[q] : f[q];
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) out[q] = tot[q] * am;
+}
+
+// Face flux of axis D at face c, Cartesian or metric.
+template <typename T, int D, bool M>
+__device__ __forceinline__ void any_face_flux(const Dev<T>& d, long long c, const T* L, const T* R, T* out) {
+  if (M) {
+    const T n[3] = {(T)d.m.nrm[D][0][c], (T)d.m.nrm[D][1][c], (T)d.m.nrm[D][2][c]};
+    face_flux_n<T>(L, R, d.gam, n, (T)d.m.am[D][c], out);
+  } else {
+    face_flux<T, D>(L, R, d.gam, out);
+  }
+}
+
 // One-sided states from an 8-tap register window (tap m = cell c+m-4 for the
 // face at the low side of cell c): slot of tap m is (m + PH) & 7.
 template <typename T, int RECON, int PH>
@@ -616,7 +689,7 @@ __device__ __forceinline__ void recon_win(const T* w, const Prm<T>& P, T& fl, T&
 // Face fluxes through the low face of cell c along axis D by direct (cached)
 // loads; one face per thread.  Used for the x faces of every stage and, for
 // all three axes, by the kernel-level debug entry point.
-template <typename T, int RECON, int D>
+template <typename T, int RECON, int D, bool M>
 __global__ void k_flux(Dev<T> d, Inp<T> in, Prm<T> P) {
   const Geom& g = d.g;
   const int ni = g.nx0 + (D == 0), nj = g.ny0 + (D == 1), nk = g.nz0 + (D == 2);
@@ -632,7 +705,7 @@ __global__ void k_flux(Dev<T> d, Inp<T> in, Prm<T> P) {
   T L[8], R[8], out[8];
 #pragma unroll
   for (int v = 0; v < 8; ++v) recon_face<T, RECON>(src[v], c, s, P, L[v], R[v]);
-  face_flux<T, D>(L, R, d.gam, out);
+  any_face_flux<T, D, M>(d, c, L, R, out);
 #pragma unroll
   for (int q = 0; q < 8; ++q) d.F[D][q][c] = out[q];
 }
@@ -699,7 +772,7 @@ __host__ __device__ constexpr size_t flux_t_smem() {
   return sizeof(T) * ((FLUX_STAGED ? 8 * TROWS * 32 : 0) + 8 * (TD + 1) * 32);
 }
 
-template <typename T, int RECON, int D>
+template <typename T, int RECON, int D, bool M>
 __global__ void __launch_bounds__(32 * (TD + 1), MHD_FLUX_MINB)
     k_flux_t(Dev<T> d, Inp<T> in, Prm<T> P, int form, T cw, T den, int ab) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -741,7 +814,7 @@ __global__ void __launch_bounds__(32 * (TD + 1), MHD_FLUX_MINB)
 #pragma unroll
       for (int v = 0; v < 8; ++v) recon_face<T, RECON>(src[v], cf, s, P, L[v], R[v]);
     }
-    face_flux<T, D>(L, R, d.gam, F);
+    any_face_flux<T, D, M>(d, rowbase + tx + cd * s, L, R, F);
 #pragma unroll
     for (int q = 0; q < 8; ++q) sF[(q * (TD + 1) + r) * 32 + tx] = F[q];
   }
@@ -752,18 +825,29 @@ __global__ void __launch_bounds__(32 * (TD + 1), MHD_FLUX_MINB)
 #pragma unroll
   for (int q = 0; q < 8; ++q) dF[q] = sF[(q * (TD + 1) + r + 1) * 32 + tx] - sF[(q * (TD + 1) + r) * 32 + tx];
   if (D == 1) {
+    if (M) {  // area-weighted fluxes: the sum is divided by V after the z term
+#pragma unroll
+      for (int q = 0; q < 8; ++q) d.dU[q][c] = (d.F[0][q][c + 1] - d.F[0][q][c]) + dF[q];
+      return;
+    }
     const T dx = d.wx[i], dy = d.wy[cd], rdx = d.rwx[i], rdy = d.rwy[cd];
 #pragma unroll
     for (int q = 0; q < 8; ++q)
       d.dU[q][c] = Ops<T>::dw(d.F[0][q][c + 1] - d.F[0][q][c], dx, rdx) + Ops<T>::dw(dF[q], dy, rdy);
     return;
   }
-  const T dz = d.wz[cd], rdz = d.rwz[cd];
   const T tau = (T)d.sc->tau;
   const T gm1 = d.gam - T(1);
   T dv[8];
+  if (M) {
+    const T V = (T)d.m.vol[c], rV = (T)d.m.rvol[c];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) dv[q] = d.dU[q][c] + Ops<T>::dw(dF[q], dz, rdz);
+    for (int q = 0; q < 8; ++q) dv[q] = Ops<T>::dw(d.dU[q][c] + dF[q], V, rV);
+  } else {
+    const T dz = d.wz[cd], rdz = d.rwz[cd];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) dv[q] = d.dU[q][c] + Ops<T>::dw(dF[q], dz, rdz);
+  }
   // get_conserve of the current state (AB: the state, not the prediction)
   T rr = d.rho[c], u = d.vx[c], v = d.vy[c], ww = d.vz[c], pr = d.p[c];
   T rvx0 = rr * u, rvy0 = rr * v, rvz0 = rr * ww;
@@ -802,7 +886,7 @@ __global__ void __launch_bounds__(32 * (TD + 1), MHD_FLUX_MINB)
 // edge whose upper cell is c (get_eijk_LFM, 1754-1856).  a1 = E+1, a2 = E+2
 // (cyclic): v1 = v_a1, v2 = v_a2; b1 = B_a1 reconstructed along a2 and
 // upwinded by sign(v2); b2 = B_a2 reconstructed along a1, upwinded by sign(v1).
-template <typename T, int RECON, int E>
+template <typename T, int RECON, int E, bool M>
 __global__ void k_emf(Dev<T> d, Inp<T> in, Prm<T> P) {
   const Geom& g = d.g;
   int i = blockIdx.x * blockDim.x + threadIdx.x + g.ng;
@@ -826,7 +910,10 @@ __global__ void k_emf(Dev<T> d, Inp<T> in, Prm<T> P) {
   T e = -v1av * b2u + v2av * b1u;
   const T* vf = d.vf;
   T eta = T(0.25) * (vf[c - s1 - s2] + vf[c - s2] + vf[c] + vf[c - s1]);
-  e = e + eta * (b1l + b2r - b1r - b2l);
+  if (M)  // E.dl: g_e * (convective term) + eta |dl_e| * (resistive term)
+    e = (T)d.m.ge[E][c] * e + eta * (T)d.m.dl[E][c] * (b1l + b2r - b1r - b2l);
+  else
+    e = e + eta * (b1l + b2r - b1r - b2l);
   d.E[E][c] = e;
 }
 
@@ -837,7 +924,7 @@ __global__ void k_emf(Dev<T> d, Inp<T> in, Prm<T> P) {
 // into shared memory, and each edge then takes the second pass along a2, the
 // limiters (corner_pdm), the upwinded face-B reconstructions and the Alfven
 // resistivity term exactly as k_emf does.  Tile (TX, TY, TZ) in edges.
-template <typename T, int E, int TX, int TY, int TZ, int NT>
+template <typename T, int E, int TX, int TY, int TZ, int NT, bool M>
 __global__ void __launch_bounds__(NT) k_emf_pdm(Dev<T> d, Inp<T> in, Prm<T> P) {
   constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
   constexpr int HX = (E == 0) ? 0 : 4, HY = (E == 1) ? 0 : 4, HZ = (E == 2) ? 0 : 4;
@@ -943,12 +1030,15 @@ __global__ void __launch_bounds__(NT) k_emf_pdm(Dev<T> d, Inp<T> in, Prm<T> P) {
     T ee = -v1av * b2u + v2av * b1u;
     const T* vf = d.vf;
     T eta = T(0.25) * (vf[c - s1 - s2] + vf[c - s2] + vf[c] + vf[c - s1]);
-    ee = ee + eta * (b1l + b2r - b1r - b2l);
+    if (M)
+      ee = (T)d.m.ge[E][c] * ee + eta * (T)d.m.dl[E][c] * (b1l + b2r - b1r - b2l);
+    else
+      ee = ee + eta * (b1l + b2r - b1r - b2l);
     d.E[E][c] = ee;
   }
 }
 
-template <typename T, int E, int TX, int TY, int TZ, int NT>
+template <typename T, int E, int TX, int TY, int TZ, int NT, bool M>
 void launch_emf_pdm(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStream_t st) {
   constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
   constexpr int HX = (E == 0) ? 0 : 4, HY = (E == 1) ? 0 : 4, HZ = (E == 2) ? 0 : 4;
@@ -960,18 +1050,40 @@ void launch_emf_pdm(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStre
   constexpr size_t bytes = sizeof(T) * (2 * NV + 2 * NG);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_emf_pdm<T, E, TX, TY, TZ, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaFuncSetAttribute(k_emf_pdm<T, E, TX, TY, TZ, NT, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     attr = true;
   }
   const Geom& g = d.g;
   const int ex = g.nx0 + (E != 0), ey = g.ny0 + (E != 1), ez = g.nz0 + (E != 2);
   dim3 grid((ex + TX - 1) / TX, (ey + TY - 1) / TY, (ez + TZ - 1) / TZ);
-  k_emf_pdm<T, E, TX, TY, TZ, NT><<<grid, NT, bytes, st>>>(d, in, P);
+  k_emf_pdm<T, E, TX, TY, TZ, NT, M><<<grid, NT, bytes, st>>>(d, in, P);
+}
+
+// Metric-mode EMF inputs of a stage: w^a = v . nbar_a at every cell and the
+// face-normal field b_a = Phi_a / |A_a| at every face (ghosts included),
+// which the EMF kernels then treat as the reference treats v and bi/bj/bk.
+template <typename T>
+__global__ void k_metric_prep(Dev<T> d, Inp<T> in) {
+  const Geom& g = d.g;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i > g.nx || j > g.ny || k > g.nz) return;
+  const long long c = idx3<T>(g, i, j, k);
+  const Metric& m = d.m;
+  if (i < g.nx && j < g.ny && k < g.nz) {
+    const T u = in.vx[c], v = in.vy[c], w = in.vz[c];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) d.mw[a][c] = u * (T)m.nb[a][0][c] + v * (T)m.nb[a][1][c] + w * (T)m.nb[a][2][c];
+  }
+  if (j < g.ny && k < g.nz) d.mbn[0][c] = Ops<T>::dv(in.bi[c], (T)m.am[0][c]);
+  if (i < g.nx && k < g.nz) d.mbn[1][c] = Ops<T>::dv(in.bj[c], (T)m.am[1][c]);
+  if (i < g.nx && j < g.ny) d.mbn[2][c] = Ops<T>::dv(in.bk[c], (T)m.am[2][c]);
 }
 
 // ------------------------------------------------------------------ update
 // advance_bijk (3909-3933) + B combine, interior faces of all three arrays.
-template <typename T>
+template <typename T, bool M>
 __global__ void k_update_b(Dev<T> d, int form, T cw, T den) {
   const Geom& g = d.g;
   int i = blockIdx.x * blockDim.x + threadIdx.x + g.ng;
@@ -986,6 +1098,24 @@ __global__ void k_update_b(Dev<T> d, int form, T cw, T den) {
   const T rx = d.rwx[i], ry = d.rwy[j], rz = d.rwz[k];
   const T *ei = d.E[0], *ej = d.E[1], *ek = d.E[2];
   typedef Ops<T> O;
+  if (M) {  // face fluxes minus tau times the circulation of E.dl
+    if (in_y && in_z) {
+      T b = d.bi[c] - tau * ((ek[c + sy] - ek[c]) - (ej[c + sz] - ej[c]));
+      if (form >= 0) b = comb(form, cw, d.q[5][c], b, den);
+      d.bi[c] = b;
+    }
+    if (in_x && in_z) {
+      T b = d.bj[c] - tau * ((ei[c + sz] - ei[c]) - (ek[c + 1] - ek[c]));
+      if (form >= 0) b = comb(form, cw, d.q[6][c], b, den);
+      d.bj[c] = b;
+    }
+    if (in_x && in_y) {
+      T b = d.bk[c] - tau * ((ej[c + 1] - ej[c]) - (ei[c + sy] - ei[c]));
+      if (form >= 0) b = comb(form, cw, d.q[7][c], b, den);
+      d.bk[c] = b;
+    }
+    return;
+  }
   if (in_y && in_z) {
     T b = d.bi[c] - tau * (O::dw(ek[c + sy] - ek[c], dy, ry) - O::dw(ej[c + sz] - ej[c], dz, rz));
     if (form >= 0) b = comb(form, cw, d.q[5][c], b, den);
@@ -1064,7 +1194,7 @@ __global__ void k_fill(Dev<T> d) {
 // exactly the values the separate fill followed by get_bxyz produces.  The
 // per-axis image of every index comes from d.gmap (ghost_src tabulated at
 // set-up): cell maps of x, y, z then face maps of x, y, z, each padded to n+2.
-template <typename T>
+template <typename T, bool M>
 __global__ void __launch_bounds__(256) k_fill_bxyz(Dev<T> d, int want_vf) {
   const Geom& g = d.g;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1075,9 +1205,14 @@ __global__ void __launch_bounds__(256) k_fill_bxyz(Dev<T> d, int want_vf) {
   const int c = i + px * j + pl * k;
   // interior fast path (no ghost element owned, all images are the identity)
   if (i >= g.ng && i < g.ng + g.nx0 && j >= g.ng && j < g.ng + g.ny0 && k >= g.ng && k < g.ng + g.nz0) {
-    const T bx = T(0.5) * (d.bi[c + 1] + d.bi[c]);
-    const T by = T(0.5) * (d.bj[c + px] + d.bj[c]);
-    const T bz = T(0.5) * (d.bk[c + pl] + d.bk[c]);
+    T bx, by, bz;
+    if (M) {
+      cell_b_metric<T>(d.m, c, d.bi[c], d.bi[c + 1], d.bj[c], d.bj[c + px], d.bk[c], d.bk[c + pl], bx, by, bz);
+    } else {
+      bx = T(0.5) * (d.bi[c + 1] + d.bi[c]);
+      by = T(0.5) * (d.bj[c + px] + d.bj[c]);
+      bz = T(0.5) * (d.bk[c + pl] + d.bk[c]);
+    }
     d.bx[c] = bx;
     d.by[c] = by;
     d.bz[c] = bz;
@@ -1112,9 +1247,16 @@ __global__ void __launch_bounds__(256) k_fill_bxyz(Dev<T> d, int want_vf) {
   if (i < g.nx && j < g.ny && (gx || gy || sfk != k)) d.bk[c] = d.bk[sci + px * scj + pl * sfk];
   if (!cin) return;
   const int cyz = px * scj + pl * sck;
-  const T bx = T(0.5) * (d.bi[fx[i + 1] + cyz] + d.bi[sfi + cyz]);
-  const T by = T(0.5) * (d.bj[sci + px * fy[j + 1] + pl * sck] + d.bj[sci + px * sfj + pl * sck]);
-  const T bz = T(0.5) * (d.bk[sci + px * scj + pl * fz[k + 1]] + d.bk[sci + px * scj + pl * sfk]);
+  T bx, by, bz;
+  if (M) {  // face fluxes of the images, geometry of this cell (as fill then get_bxyz)
+    cell_b_metric<T>(d.m, c, d.bi[sfi + cyz], d.bi[fx[i + 1] + cyz], d.bj[sci + px * sfj + pl * sck],
+                     d.bj[sci + px * fy[j + 1] + pl * sck], d.bk[sci + px * scj + pl * sfk],
+                     d.bk[sci + px * scj + pl * fz[k + 1]], bx, by, bz);
+  } else {
+    bx = T(0.5) * (d.bi[fx[i + 1] + cyz] + d.bi[sfi + cyz]);
+    by = T(0.5) * (d.bj[sci + px * fy[j + 1] + pl * sck] + d.bj[sci + px * sfj + pl * sck]);
+    bz = T(0.5) * (d.bk[sci + px * scj + pl * fz[k + 1]] + d.bk[sci + px * scj + pl * sfk]);
+  }
   d.bx[c] = bx;
   d.by[c] = by;
   d.bz[c] = bz;
@@ -1144,7 +1286,7 @@ __device__ __forceinline__ DD dd_add(DD x, DD y) {
   return DD{s2, e2};
 }
 
-template <typename T>
+template <typename T, bool M>
 __global__ void k_diag_partial(Dev<T> d, double* part) {
   const Geom& g = d.g;
   long long n = (long long)g.nx0 * g.ny0 * g.nz0;
@@ -1158,15 +1300,20 @@ __global__ void k_diag_partial(Dev<T> d, double* part) {
     int j = (int)(r % g.ny0) + g.ng;
     int k = (int)(r / g.ny0) + g.ng;
     long long c = idx3<T>(g, i, j, k);
-    double dv = d.dx[i] * d.dy[j] * d.dz[k];
+    double dv = M ? d.m.vol[c] : d.dx[i] * d.dy[j] * d.dz[k];
     double rr = d.rho[c], u = d.vx[c], v = d.vy[c], w = d.vz[c], pp = d.p[c];
     double a = d.bx[c], b = d.by[c], cc = d.bz[c];
     ms = dd_add(ms, DD{rr * dv, 0.0});
     double e = 0.5 * rr * (u * u + v * v + w * w) + pp / gm1 + 0.5 * (a * a + b * b + cc * cc);
     es = dd_add(es, DD{e * dv, 0.0});
-    double db = ((double)d.bi[c + 1] - (double)d.bi[c]) / d.dx[i] +
-                ((double)d.bj[c + g.px] - (double)d.bj[c]) / d.dy[j] +
-                ((double)d.bk[c + g.plane] - (double)d.bk[c]) / d.dz[k];
+    double db;
+    if (M)  // net face flux out of the cell / V
+      db = (((double)d.bi[c + 1] - (double)d.bi[c]) + ((double)d.bj[c + g.px] - (double)d.bj[c]) +
+            ((double)d.bk[c + g.plane] - (double)d.bk[c])) / dv;
+    else
+      db = ((double)d.bi[c + 1] - (double)d.bi[c]) / d.dx[i] +
+           ((double)d.bj[c + g.px] - (double)d.bj[c]) / d.dy[j] +
+           ((double)d.bk[c + g.plane] - (double)d.bk[c]) / d.dz[k];
     db = fabs(db);
     dmax = db > dmax ? db : dmax;
   }
@@ -1247,105 +1394,105 @@ Prm<T> prm_of(const Dev<T>& d) {
   return P;
 }
 
-template <typename T>
-void Launch<T>::bxyz_vf(const Dev<T>& d, bool want_vf, cudaStream_t st) {
+template <typename T, bool M>
+void Launch<T, M>::bxyz_vf(const Dev<T>& d, bool want_vf, cudaStream_t st) {
   dim3 b(64, 4, 1);
-  k_bxyz_vf<T><<<grid3(d.g.nx, d.g.ny, d.g.nz, b), b, 0, st>>>(d, want_vf ? 1 : 0);
+  k_bxyz_vf<T, M><<<grid3(d.g.nx, d.g.ny, d.g.nz, b), b, 0, st>>>(d, want_vf ? 1 : 0);
 }
 
-template <typename T>
-void Launch<T>::fill_bxyz(const Dev<T>& d, bool want_vf, cudaStream_t st) {
+template <typename T, bool M>
+void Launch<T, M>::fill_bxyz(const Dev<T>& d, bool want_vf, cudaStream_t st) {
   dim3 b(64, 4, 1);
-  k_fill_bxyz<T><<<grid3(d.g.nx + 1, d.g.ny + 1, d.g.nz + 1, b), b, 0, st>>>(d, want_vf ? 1 : 0);
+  k_fill_bxyz<T, M><<<grid3(d.g.nx + 1, d.g.ny + 1, d.g.nz + 1, b), b, 0, st>>>(d, want_vf ? 1 : 0);
 }
 
-template <typename T>
-void Launch<T>::cfl(const Dev<T>& d, int mode, cudaStream_t st, bool save) {
+template <typename T, bool M>
+void Launch<T, M>::cfl(const Dev<T>& d, int mode, cudaStream_t st, bool save) {
   dim3 grid((d.g.nx + 31) / 32, (d.g.ny + 7) / 8, (d.g.nz + 7) / 8);
-  k_cfl<T><<<grid, 256, 0, st>>>(d, save ? 1 : 0);
+  k_cfl<T, M><<<grid, 256, 0, st>>>(d, save ? 1 : 0);
   k_cfl_final<T><<<1, 1, 0, st>>>(d, mode);
 }
 
-template <typename T>
-void Launch<T>::save_prev(const Dev<T>& d, cudaStream_t st) {
+template <typename T, bool M>
+void Launch<T, M>::save_prev(const Dev<T>& d, cudaStream_t st) {
   k_save_prev<T><<<152 * 8, 256, 0, st>>>(d);
 }
 
-template <typename T>
-void Launch<T>::predictor_ab(const Dev<T>& d, cudaStream_t st) {
+template <typename T, bool M>
+void Launch<T, M>::predictor_ab(const Dev<T>& d, cudaStream_t st) {
   k_predictor_ab<T><<<152 * 8, 256, 0, st>>>(d);
 }
 
-template <typename T, int RECON>
+template <typename T, int RECON, bool M>
 void flux_r(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
   Prm<T> P = prm_of(d);
   const Geom& g = d.g;
   const int n0 = (g.nx0 + 1) * g.ny0 * g.nz0, n1 = g.nx0 * (g.ny0 + 1) * g.nz0, n2 = g.nx0 * g.ny0 * (g.nz0 + 1);
-  k_flux<T, RECON, 0><<<(n0 + 127) / 128, 128, 0, st>>>(d, in, P);
-  k_flux<T, RECON, 1><<<(n1 + 127) / 128, 128, 0, st>>>(d, in, P);
-  k_flux<T, RECON, 2><<<(n2 + 127) / 128, 128, 0, st>>>(d, in, P);
+  k_flux<T, RECON, 0, M><<<(n0 + 127) / 128, 128, 0, st>>>(d, in, P);
+  k_flux<T, RECON, 1, M><<<(n1 + 127) / 128, 128, 0, st>>>(d, in, P);
+  k_flux<T, RECON, 2, M><<<(n2 + 127) / 128, 128, 0, st>>>(d, in, P);
 }
 
-template <typename T>
-void Launch<T>::fluxes(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
+template <typename T, bool M>
+void Launch<T, M>::fluxes(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
   switch (d.recon) {
-    case R_PDM: flux_r<T, R_PDM>(d, in, st); break;
-    case R_TVD: flux_r<T, R_TVD>(d, in, st); break;
-    case R_WENO: flux_r<T, R_WENO>(d, in, st); break;
-    case R_MPWENO: flux_r<T, R_MPWENO>(d, in, st); break;
-    default: flux_r<T, R_TVDMC>(d, in, st); break;
+    case R_PDM: flux_r<T, R_PDM, M>(d, in, st); break;
+    case R_TVD: flux_r<T, R_TVD, M>(d, in, st); break;
+    case R_WENO: flux_r<T, R_WENO, M>(d, in, st); break;
+    case R_MPWENO: flux_r<T, R_MPWENO, M>(d, in, st); break;
+    default: flux_r<T, R_TVDMC, M>(d, in, st); break;
   }
 }
 
-template <typename T, int RECON>
+template <typename T, int RECON, bool M>
 void hydro_r(const Dev<T>& d, const Inp<T>& in, int part, int form, double c, double den, bool ab,
              cudaStream_t st) {
   Prm<T> P = prm_of(d);
   const Geom& g = d.g;
   if (part == 0) {
     const int n0 = (g.nx0 + 1) * g.ny0 * g.nz0;
-    k_flux<T, RECON, 0><<<(n0 + 127) / 128, 128, 0, st>>>(d, in, P);
+    k_flux<T, RECON, 0, M><<<(n0 + 127) / 128, 128, 0, st>>>(d, in, P);
   } else if (part == 1) {
     constexpr size_t sm = flux_t_smem<T>();
     static bool attr = false;
     if (!attr) {
-      cudaFuncSetAttribute(k_flux_t<T, RECON, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      cudaFuncSetAttribute(k_flux_t<T, RECON, 1, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
       attr = true;
     }
     dim3 grid((g.nx0 + 31) / 32, (g.ny0 + TD - 1) / TD, g.nz0);
-    k_flux_t<T, RECON, 1><<<grid, dim3(32, TD + 1), sm, st>>>(d, in, P, -1, T(0), T(1), 0);
+    k_flux_t<T, RECON, 1, M><<<grid, dim3(32, TD + 1), sm, st>>>(d, in, P, -1, T(0), T(1), 0);
   } else {
     constexpr size_t sm = flux_t_smem<T>();
     static bool attr = false;
     if (!attr) {
-      cudaFuncSetAttribute(k_flux_t<T, RECON, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      cudaFuncSetAttribute(k_flux_t<T, RECON, 2, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
       attr = true;
     }
     dim3 grid((g.nx0 + 31) / 32, (g.nz0 + TD - 1) / TD, g.ny0);
-    k_flux_t<T, RECON, 2><<<grid, dim3(32, TD + 1), sm, st>>>(d, in, P, form, (T)c, (T)den, ab ? 1 : 0);
+    k_flux_t<T, RECON, 2, M><<<grid, dim3(32, TD + 1), sm, st>>>(d, in, P, form, (T)c, (T)den, ab ? 1 : 0);
   }
 }
 
-template <typename T>
-void Launch<T>::hydro(const Dev<T>& d, const Inp<T>& in, int part, int form, double c, double den, bool ab,
-                      cudaStream_t st) {
+template <typename T, bool M>
+void Launch<T, M>::hydro(const Dev<T>& d, const Inp<T>& in, int part, int form, double c, double den, bool ab,
+                         cudaStream_t st) {
   switch (d.recon) {
-    case R_PDM: hydro_r<T, R_PDM>(d, in, part, form, c, den, ab, st); break;
-    case R_TVD: hydro_r<T, R_TVD>(d, in, part, form, c, den, ab, st); break;
-    case R_WENO: hydro_r<T, R_WENO>(d, in, part, form, c, den, ab, st); break;
-    case R_MPWENO: hydro_r<T, R_MPWENO>(d, in, part, form, c, den, ab, st); break;
-    default: hydro_r<T, R_TVDMC>(d, in, part, form, c, den, ab, st); break;
+    case R_PDM: hydro_r<T, R_PDM, M>(d, in, part, form, c, den, ab, st); break;
+    case R_TVD: hydro_r<T, R_TVD, M>(d, in, part, form, c, den, ab, st); break;
+    case R_WENO: hydro_r<T, R_WENO, M>(d, in, part, form, c, den, ab, st); break;
+    case R_MPWENO: hydro_r<T, R_MPWENO, M>(d, in, part, form, c, den, ab, st); break;
+    default: hydro_r<T, R_TVDMC, M>(d, in, part, form, c, den, ab, st); break;
   }
 }
 
-template <typename T, int RECON>
+template <typename T, int RECON, bool M>
 void emf_r(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
   Prm<T> P = prm_of(d);
   dim3 b(32, 4, 1);
   const Geom& g = d.g;
-  k_emf<T, RECON, 0><<<grid3(g.nx0, g.ny0 + 1, g.nz0 + 1, b), b, 0, st>>>(d, in, P);
-  k_emf<T, RECON, 1><<<grid3(g.nx0 + 1, g.ny0, g.nz0 + 1, b), b, 0, st>>>(d, in, P);
-  k_emf<T, RECON, 2><<<grid3(g.nx0 + 1, g.ny0 + 1, g.nz0, b), b, 0, st>>>(d, in, P);
+  k_emf<T, RECON, 0, M><<<grid3(g.nx0, g.ny0 + 1, g.nz0 + 1, b), b, 0, st>>>(d, in, P);
+  k_emf<T, RECON, 1, M><<<grid3(g.nx0 + 1, g.ny0, g.nz0 + 1, b), b, 0, st>>>(d, in, P);
+  k_emf<T, RECON, 2, M><<<grid3(g.nx0 + 1, g.ny0 + 1, g.nz0, b), b, 0, st>>>(d, in, P);
 }
 
 // ei tile: 32 x 8 x 8 edges in FP32, 32 x 4 x 4 in FP64 (96 KB of shared memory each)
@@ -1355,43 +1502,51 @@ void emf_r(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
 template <typename T> struct EiTile { static constexpr int Y = MHD_EI_TILE; };
 template <> struct EiTile<double> { static constexpr int Y = 4; };
 
-template <typename T>
-void Launch<T>::emf(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
+template <typename T, bool M>
+void Launch<T, M>::emf(const Dev<T>& d, const Inp<T>& in0, cudaStream_t st) {
+  Inp<T> in = in0;
+  if (M) {
+    // normal velocities and face-normal field of the stage input, in the
+    // places of v and bi/bj/bk
+    dim3 b(64, 4, 1);
+    k_metric_prep<T><<<grid3(d.g.nx + 1, d.g.ny + 1, d.g.nz + 1, b), b, 0, st>>>(d, in0);
+    in.vx = d.mw[0]; in.vy = d.mw[1]; in.vz = d.mw[2];
+    in.bi = d.mbn[0]; in.bj = d.mbn[1]; in.bk = d.mbn[2];
+  }
   if (d.recon == R_PDM) {
     Prm<T> P = prm_of(d);
-    launch_emf_pdm<T, 0, 32, EiTile<T>::Y, EiTile<T>::Y, 512>(d, in, P, st);
-    launch_emf_pdm<T, 1, 32, 1, 8, 256>(d, in, P, st);
-    launch_emf_pdm<T, 2, 32, 8, 1, 256>(d, in, P, st);
+    launch_emf_pdm<T, 0, 32, EiTile<T>::Y, EiTile<T>::Y, 512, M>(d, in, P, st);
+    launch_emf_pdm<T, 1, 32, 1, 8, 256, M>(d, in, P, st);
+    launch_emf_pdm<T, 2, 32, 8, 1, 256, M>(d, in, P, st);
     return;
   }
   switch (d.recon) {
-    case R_PDM: emf_r<T, R_PDM>(d, in, st); break;
-    case R_TVD: emf_r<T, R_TVD>(d, in, st); break;
-    case R_WENO: emf_r<T, R_WENO>(d, in, st); break;
-    case R_MPWENO: emf_r<T, R_MPWENO>(d, in, st); break;
-    default: emf_r<T, R_TVDMC>(d, in, st); break;
+    case R_TVD: emf_r<T, R_TVD, M>(d, in, st); break;
+    case R_WENO: emf_r<T, R_WENO, M>(d, in, st); break;
+    case R_MPWENO: emf_r<T, R_MPWENO, M>(d, in, st); break;
+    default: emf_r<T, R_TVDMC, M>(d, in, st); break;
   }
 }
 
-template <typename T>
-void Launch<T>::ct(const Dev<T>& d, int form, double c, double den, cudaStream_t st) {
+template <typename T, bool M>
+void Launch<T, M>::ct(const Dev<T>& d, int form, double c, double den, cudaStream_t st) {
   dim3 b(32, 4, 1);
   const Geom& g = d.g;
-  k_update_b<T><<<grid3(g.nx0 + 1, g.ny0 + 1, g.nz0 + 1, b), b, 0, st>>>(d, form, (T)c, (T)den);
+  k_update_b<T, M><<<grid3(g.nx0 + 1, g.ny0 + 1, g.nz0 + 1, b), b, 0, st>>>(d, form, (T)c, (T)den);
 }
 
-template <typename T>
-void Launch<T>::fill(const Dev<T>& d, cudaStream_t st) {
+template <typename T, bool M>
+void Launch<T, M>::fill(const Dev<T>& d, cudaStream_t st) {
   dim3 b(64, 4, 1);
   k_fill<T><<<grid3(d.g.nx + 1, d.g.ny + 1, d.g.nz + 1, b), b, 0, st>>>(d);
 }
 
-template <typename T>
-void Launch<T>::diagnostics(const Dev<T>& d, double* out, cudaStream_t st) {
+template <typename T, bool M>
+void Launch<T, M>::diagnostics(const Dev<T>& d, double* out, cudaStream_t st) {
   // out: device buffer of 5 + 5*nb doubles; out[4] (CFL dt) is filled by the caller
   const int nb = 152 * 2;
   double* part = out + 8;
-  k_diag_partial<T><<<nb, 256, 0, st>>>(d, part);
+  k_diag_partial<T, M><<<nb, 256, 0, st>>>(d, part);
   k_diag_final<T><<<1, 1, 0, st>>>(d, part, nb, out);
   k_min_rho<T><<<1, 1024, 0, st>>>(d, out);
 }

@@ -40,6 +40,34 @@ struct Scal {
   unsigned int pad;
 };
 
+// Curvilinear metric (metric mode only; FP64 in both precisions), computed
+// once on the device from the node coordinates.  Same padded layout as the
+// fields: a face at the index of the cell on its high side (the cell whose
+// low face it is), an edge at the index of its upper cell.
+struct Metric {
+  const double* nrm[3][3];  // unit normals of the low faces [face axis][component]
+  const double* am[3];      // face area magnitudes |A|
+  const double* vol;        // cell volumes V
+  const double* rvol;       // 1/V
+  const double* eb[3][3];   // cell edge vectors (face-centroid differences) [axis][component]
+  const double* nb[3][3];   // mean unit normal of the two a-faces of a cell [axis][component]
+  const double* sa;         // sum over a of |mean area vector of the a-faces| (CFL)
+  const double* ge[3];      // per edge family: g_e = |A1|_e |A2|_e / Vbar_e
+  const double* dl[3];      // per edge family: edge length
+};
+
+// Raw device arrays the geometry kernels write (the const views above alias them).
+struct MetricOut {
+  double *nrm[3][3], *am[3], *vol, *rvol, *eb[3][3], *nb[3][3], *sa, *ge[3], *dl[3];
+};
+constexpr int kMetricArrays = 9 + 3 + 2 + 9 + 9 + 1 + 3 + 3;
+
+// Geometry of a mapped grid from ghost-inclusive node coordinates stored in
+// the padded layout (node (i,j,k) at i + px*(j + py*k)); FP64, no FMA.
+// Writes the minimum interior cell volume to *min_vol (device).
+void metric_geometry(const Geom& g, const double* X, const double* Y, const double* Z, const MetricOut& m,
+                     double* min_vol, cudaStream_t st);
+
 template <typename T>
 struct Dev {
   Geom g;
@@ -66,6 +94,11 @@ struct Dev {
   const int* gmap;             // per-axis ghost-image tables (cell x,y,z; face x,y,z), each n+2
   unsigned int* partial;       // per-block scratch of the CFL reduction
   unsigned int* counter;
+  // metric mode: geometry, and the per-stage normal velocities w^a (cells)
+  // and face-normal field b_a = Phi_a/|A_a| (faces) of the EMF
+  Metric m;
+  T* mw[3];
+  T* mbn[3];
 };
 
 // Stage-input view: which arrays feed the EMF and flux kernels (RK: the
@@ -75,7 +108,10 @@ struct Inp {
   const T *rho, *vx, *vy, *vz, *p, *bx, *by, *bz, *bi, *bj, *bk;
 };
 
-template <typename T>
+// M: curvilinear metric mode (face fluxes Phi in bi/bj/bk, area-weighted
+// fluxes, E.dl circulation); instantiated in mhd_metric_fp32.cu /
+// mhd_metric_fp64.cu.  M = false is the reference's Cartesian scheme.
+template <typename T, bool M = false>
 struct Launch {
   static void bxyz_vf(const Dev<T>& d, bool want_vf, cudaStream_t st);
   // ghost fill + get_bxyz + vf in one pass

@@ -46,13 +46,20 @@ class MHDSolver:
             return
         g = state.grid
         self._keep = [_f64(a) for a in state.arrays()]
-        self._geo = [_f64(g.dx if dx is None else dx), _f64(g.dy if dy is None else dy),
-                     _f64(g.dz if dz is None else dz)]
         self._cp = params.to_c()
         h = C.c_void_p()
-        rc = self.lib.mhd_init(C.byref(self._cp), *[_ptr(a) for a in self._keep],
-                               *[_ptr(a) for a in self._geo], C.byref(h))
-        check(self.lib, rc, "mhd_init")
+        if getattr(state, "nodes", None) is not None:
+            # curvilinear metric mode: bi/bj/bk hold face fluxes Phi = B.A
+            self._geo = [_f64(a) for a in state.nodes]
+            rc = self.lib.mhd_init_mapped(C.byref(self._cp), *[_ptr(a) for a in self._keep],
+                                          *[_ptr(a) for a in self._geo], C.byref(h))
+            check(self.lib, rc, "mhd_init_mapped")
+        else:
+            self._geo = [_f64(g.dx if dx is None else dx), _f64(g.dy if dy is None else dy),
+                         _f64(g.dz if dz is None else dz)]
+            rc = self.lib.mhd_init(C.byref(self._cp), *[_ptr(a) for a in self._keep],
+                                   *[_ptr(a) for a in self._geo], C.byref(h))
+            check(self.lib, rc, "mhd_init")
         self.h = h
         self._keep = None
 
