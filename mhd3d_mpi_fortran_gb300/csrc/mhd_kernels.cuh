@@ -767,13 +767,19 @@ constexpr int TD = MHD_FLUX_TD;
 constexpr int TROWS = TD + 8;
 constexpr bool FLUX_STAGED = MHD_FLUX_STAGED != 0;
 
+// Resident blocks per SM requested for the flux tiles: FP32 trades registers
+// for occupancy (latency-bound); FP64 needs about twice the registers and
+// would spill at the FP32 setting.
+template <typename T> struct FluxMinB { static constexpr int value = MHD_FLUX_MINB; };
+template <> struct FluxMinB<double> { static constexpr int value = 2; };
+
 template <typename T>
 __host__ __device__ constexpr size_t flux_t_smem() {
   return sizeof(T) * ((FLUX_STAGED ? 8 * TROWS * 32 : 0) + 8 * (TD + 1) * 32);
 }
 
 template <typename T, int RECON, int D, bool M>
-__global__ void __launch_bounds__(32 * (TD + 1), MHD_FLUX_MINB)
+__global__ void __launch_bounds__(32 * (TD + 1), FluxMinB<T>::value)
     k_flux_t(Dev<T> d, Inp<T> in, Prm<T> P, int form, T cw, T den, int ab) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sv = reinterpret_cast<T*>(smem_raw);                      // [8][TROWS][32] cell fields

@@ -1,0 +1,149 @@
+"""Accuracy studies of the FP32 production path against the all-FP64 mode.
+
+The all-FP64 mode reproduces the oracle (the CPU restatement of the
+reference's step) to round-off on identical inputs, so it is the reference
+solution here at sizes the oracle cannot reach in reasonable time.
+
+* ``curvilinear`` -- magnetised blast on the mapped grid
+  x = xi + 0.05 sin 2 pi eta, y = eta + 0.05 sin 2 pi zeta, z = zeta; outflow
+  walls, PDM, AB2 (CFL dt); FP32 and FP64 side by side: L1/L2 error of FP32,
+  div B of both, GPU time and zone-updates/s of both.
+* ``precision``   -- decaying turbulence on the periodic box (rho = 1,
+  p = 1/(gam Ms^2), Ms = 0.5, solenoidal k^-2 v and B); PDM, TVD-MC and WENO5
+  with RK2; L1/L2 and shell-averaged energy-spectrum error of FP32 against
+  FP64, GPU time of both.
+
+``python -m mhd3d_mpi_fortran_gb300.studies curvilinear|precision [--n N] [--steps K]``
+prints one JSON line per case.
+"""
+from __future__ import annotations
+
+import json
+import sys
+
+import numpy as np
+
+from . import ics
+from .abi import Params, FP32, FP64, STEP_AB2, STEP_RK2, BC_OUTFLOW
+from .solver import MHDSolver
+
+FIELDS = ("rho", "vx", "vy", "vz", "p", "bx", "by", "bz")
+
+
+def _interior(a: np.ndarray, ng: int) -> np.ndarray:
+    return a[ng:-ng, ng:-ng, ng:-ng]
+
+
+def errors(a: dict, b: dict, ng: int) -> dict:
+    """Relative L1 and L2 errors of a against b over the interior cells;
+    vector fields as groups (v, B) so that a near-zero component does not
+    blow up its relative error."""
+    out = {}
+    groups = {"rho": ("rho",), "p": ("p",), "v": ("vx", "vy", "vz"), "B": ("bx", "by", "bz")}
+    for name, ks in groups.items():
+        d1 = sum(np.abs(_interior(a[k], ng) - _interior(b[k], ng)).sum() for k in ks)
+        n1 = sum(np.abs(_interior(b[k], ng)).sum() for k in ks)
+        d2 = sum(((_interior(a[k], ng) - _interior(b[k], ng)) ** 2).sum() for k in ks)
+        n2 = sum((_interior(b[k], ng) ** 2).sum() for k in ks)
+        out[name] = {"l1": float(d1 / n1), "l2": float(np.sqrt(d2 / n2))}
+    return out
+
+
+def spectrum(f: dict, ng: int) -> np.ndarray:
+    """Shell-averaged kinetic + magnetic energy spectrum E(k), k = 1..N/2, of a
+    periodic cubic state (sqrt(rho) v and B)."""
+    r = _interior(f["rho"], ng)
+    n = r.shape[0]
+    comps = [np.sqrt(r) * _interior(f[k], ng) for k in ("vx", "vy", "vz")]
+    comps += [_interior(f[k], ng) for k in ("bx", "by", "bz")]
+    k1 = np.fft.fftfreq(n, d=1.0 / n)
+    kk = np.sqrt(k1[:, None, None] ** 2 + k1[None, :, None] ** 2 + k1[None, None, :] ** 2)
+    shell = np.rint(kk).astype(np.int64)
+    e = np.zeros(n // 2 + 1)
+    for c in comps:
+        p = np.abs(np.fft.fftn(c)) ** 2 * 0.5 / n ** 6
+        e += np.bincount(shell.ravel(), weights=p.ravel(), minlength=shell.max() + 1)[: n // 2 + 1]
+    return e[1:]
+
+
+def _run(prm: Params, state, steps: int):
+    # FP64 runs ~30x slower than FP32 on this part: time it in chunks so that
+    # every host wait stays short (each chunk is one graph replay)
+    chunk = 10 if prm.precision == FP64 else 100
+    with MHDSolver(prm, state) as s:
+        ms, done = 0.0, 0
+        while done < steps:
+            k = min(chunk, steps - done)
+            ms += s.time_steps(k, graph=True)
+            done += k
+        f = s.fetch()
+        d = s.diagnostics()
+    return ms, f, d
+
+
+def curvilinear(n: int = 192, steps: int = 200, amp: float = 0.05) -> dict:
+    s = ics.mapped_blast(n, amp=amp)
+    base = dict(stepop=STEP_AB2, bc=(BC_OUTFLOW,) * 3, reconop=1, tau=0.0)
+    res = {}
+    for prec in (FP64, FP32):
+        res[prec] = _run(Params(n, n, n, precision=prec, **base), s, steps)
+    ms64, f64, d64 = res[FP64]
+    ms32, f32, d32 = res[FP32]
+    zones = n ** 3 * steps
+    return {
+        "study": "curvilinear", "workload": f"{n}^3 magnetised blast on x=xi+{amp} sin 2pi eta, "
+                                            f"y=eta+{amp} sin 2pi zeta, z=zeta; outflow, PDM, AB2, {steps} steps",
+        "fp32_error_vs_fp64": errors(f32, f64, 4),
+        "divb_max": {"fp32": d32["divb_max"], "fp64": d64["divb_max"]},
+        "mass": {"fp32": d32["mass"], "fp64": d64["mass"]},
+        "gpu_ms": {"fp32": ms32, "fp64": ms64},
+        "zone_updates_per_s": {"fp32": zones / (ms32 * 1e-3), "fp64": zones / (ms64 * 1e-3)},
+        "timing": "CUDA events around graph replays of all steps, state resident in HBM",
+    }
+
+
+def precision(n: int = 256, steps: int = 500, recons=(1, 5, 3)) -> list:
+    s = ics.turbulence(n, seed=0)
+    tau = 0.8 * ics.cfl_dt(s, cfl=0.3)
+    out = []
+    names = {1: "PDM", 2: "TVD", 3: "WENO5", 4: "MPWENO5", 5: "TVD-MC"}
+    for recon in recons:
+        res = {}
+        for prec in (FP64, FP32):
+            res[prec] = _run(Params(n, n, n, reconop=recon, stepop=STEP_RK2, precision=prec, tau=tau), s, steps)
+        ms64, f64, d64 = res[FP64]
+        ms32, f32, d32 = res[FP32]
+        e64, e32 = spectrum(f64, 4), spectrum(f32, 4)
+        kmax = n // 3  # shells well resolved by the scheme
+        spec_err = float(np.abs(e32[:kmax] - e64[:kmax]).sum() / e64[:kmax].sum())
+        zones = n ** 3 * steps
+        out.append({
+            "study": "precision", "recon": names[recon],
+            "workload": f"{n}^3 periodic decaying turbulence (Ms 0.5, k^-2, rms v 1, B 0.5), RK2, {steps} steps",
+            "fp32_error_vs_fp64": errors(f32, f64, 4),
+            "spectrum_error_k_le_n_over_3": spec_err,
+            "energy": {"fp32": d32["energy"], "fp64": d64["energy"]},
+            "divb_max": {"fp32": d32["divb_max"], "fp64": d64["divb_max"]},
+            "gpu_ms": {"fp32": ms32, "fp64": ms64},
+            "zone_updates_per_s": {"fp32": zones / (ms32 * 1e-3), "fp64": zones / (ms64 * 1e-3)},
+        })
+    return out
+
+
+def main(argv=None) -> None:
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("study", choices=["curvilinear", "precision"])
+    ap.add_argument("--n", type=int, default=None)
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--recons", default="1,5,3", help="precision study: reconop values (1 PDM, 5 TVD-MC, 3 WENO5)")
+    a = ap.parse_args(argv)
+    if a.study == "curvilinear":
+        print(json.dumps(curvilinear(a.n or 192, a.steps or 200)), flush=True)
+    else:
+        for line in precision(a.n or 256, a.steps or 500, tuple(int(r) for r in a.recons.split(","))):
+            print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
