@@ -215,10 +215,27 @@ int mhd_diagnostics_noalloc(const mhd_params* prm, const double* rho, const doub
 
 /* ---- batched ensemble of independent grids -------------------------- */
 
-/* Advance `ngrids` independent solvers (created by mhd_init, same precision,
- * reconop and stepop, any sizes) by nsteps each, all grids of a stage in one
- * launch per kernel family, replayed as one CUDA graph. */
+/* Advance `ngrids` independent solvers (same precision, any sizes) by nsteps
+ * each in one CUDA graph (no reference counterpart: the reference runs one
+ * grid per job).  Cartesian PDM grids that share an RK stepper, dt mode and
+ * limiter constants run every stage as one launch per kernel family over all
+ * grids (with the launch shapes of the first grid); other ensembles get one
+ * graph branch per grid.  Each grid's result is bit-for-bit what stepping it
+ * alone gives.  Graphs are cached per (grids, nsteps). */
 int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* status);
+
+/* Tile autotuner (no reference counterpart).  Times the launch-shape variants
+ * compiled for the FP32 Cartesian PDM path -- y/z face-tile length 4, 8 or 16
+ * and ei EMF tile 4x4 or 8x8 edges -- on the handle's own grid, `reps` timed
+ * runs each, keeps the fastest and writes it to out[0] (tile length) and
+ * out[1] (EMF tile).  The timed launches touch only scratch arrays, so the
+ * state is unchanged, and every choice gives bit-identical steps.  Other
+ * handles keep their fixed shapes (returned in out). */
+int mhd_autotune(void* handle, int32_t reps, int32_t out[2]);
+
+/* The same for a batched ensemble: times the batched launches over all grids
+ * and gives every grid the fastest shapes. */
+int mhd_ensemble_autotune(void** handles, int32_t ngrids, int32_t reps, int32_t out[2]);
 
 #ifdef __cplusplus
 }

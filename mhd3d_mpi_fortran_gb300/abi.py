@@ -27,6 +27,7 @@ EXPORTS = (
     "mhd_set_tau", "mhd_set_profiling", "mhd_last_timings", "mhd_free", "mhd_last_error",
     "mhd_debug_fluxes", "mhd_debug_emf", "mhd_ensemble_step", "mhd_time_steps",
     "mhd_diagnostics_noalloc", "mhd_checkpoint_save", "mhd_checkpoint_load",
+    "mhd_autotune", "mhd_ensemble_autotune",
 )
 
 
@@ -122,6 +123,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.mhd_time_steps.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_float)]
     lib.mhd_ensemble_step.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.POINTER(C.c_uint32)]
     lib.mhd_checkpoint_save.argtypes = [vp, C.c_char_p]
+    lib.mhd_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
+    lib.mhd_ensemble_autotune.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.POINTER(C.c_int32)]
     lib.mhd_checkpoint_load.argtypes = [C.c_char_p, C.POINTER(vp)]
     lib.mhd_diagnostics_noalloc.argtypes = [C.POINTER(CParams)] + [vp] * 12 + [vp]
     for name in EXPORTS:

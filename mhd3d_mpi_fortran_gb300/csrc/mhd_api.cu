@@ -23,6 +23,7 @@
 #include <string>
 #include <thread>
 #include <vector>
+#include <atomic>
 #include <map>
 
 #include "../../include/mhd_gpu.h"
@@ -48,7 +49,10 @@ int fail(int code, const std::string& msg) {
 
 constexpr double kWaitSeconds = 600.0;  // bound on any host wait for the device
 
+std::atomic<unsigned long long> g_next_uid{1};
+
 struct Handle {
+  unsigned long long uid = 0;  // never reused: keys the ensemble graph cache
   mhd_params prm{};
   Geom g{};
   int fp32 = 0;
@@ -68,6 +72,7 @@ struct Handle {
   std::vector<cudaEvent_t> pool;
   std::vector<int> fam;
   int par = 0;                 // which half of the double-buffered primitives is current
+  int tile_td = 8, tile_ey = 8;  // launch shapes (autotuned for FP32 Cartesian PDM)
   float* geoT = nullptr;       // FP32 copy of the cell widths
   int* gmap = nullptr;         // ghost-image tables
   bool metric = false;         // curvilinear metric mode (mhd_init_mapped)
@@ -259,6 +264,8 @@ void carve(Handle* h, Dev<T>& d, char* base) {
   d.partial = nullptr;
   d.counter = nullptr;
   d.m = Metric{};
+  d.tile_td = h->tile_td;
+  d.tile_ey = h->tile_ey;
   for (int a = 0; a < 3; ++a) {
     d.mw[a] = h->metric ? next() : nullptr;
     d.mbn[a] = h->metric ? next() : nullptr;
@@ -489,9 +496,11 @@ static int create_handle(const mhd_params* prm, const double* dx, const double* 
                          Handle** out, bool metric = false) {
   *out = nullptr;
   Handle* h = new Handle();
+  h->uid = g_next_uid++;
   h->prm = *prm;
   h->fp32 = (prm->precision == MHD_FP32);
   h->metric = metric;
+  h->tile_ey = h->fp32 ? 8 : 4;
   Geom& g = h->g;
   g.nx0 = prm->nx0; g.ny0 = prm->ny0; g.nz0 = prm->nz0;
   g.nord = prm->nord; g.ng = prm->nord / 2;
@@ -1059,42 +1068,114 @@ int mhd_debug_emf(void* handle, double* ei, double* ej, double* ek) {
   return h->fp32 ? dbg_emf_t<float, false>(h, outs) : dbg_emf_t<double, false>(h, outs);
 }
 
-// Ensemble: one CUDA graph with one branch per grid (grids run concurrently),
-// nsteps steps per grid; cached per (handle list, nsteps).
-int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* status) {
-  if (!handles || ngrids <= 0 || nsteps <= 0) return fail(MHD_E_ARG, "bad ensemble arguments");
-  Handle* h0 = (Handle*)handles[0];
-  for (int i = 0; i < ngrids; ++i) {
-    Handle* h = (Handle*)handles[i];
-    if (!h) return fail(MHD_E_ARG, "null handle in ensemble");
-    if (h->fp32 != h0->fp32) return fail(MHD_E_ARG, "ensemble grids must share the precision");
+// ---- ensembles
+// Device tables of a batched ensemble (see Batch in mhd_state.h).
+struct BatchBufs {
+  void* tabs = nullptr;
+  int4* maps = nullptr;
+  BatchView view{};
+};
+
+// Grids that can share one batched launch per kernel family: same precision,
+// Cartesian, PDM, the same RK stepper, dt mode and limiter constants.
+static bool batchable(Handle* const* hs, int n) {
+  const mhd_params& a = hs[0]->prm;
+  if (hs[0]->metric || a.reconop != MHD_RECON_PDM || (a.stepop != MHD_STEP_RK2 && a.stepop != MHD_STEP_RK3))
+    return false;
+  for (int i = 1; i < n; ++i) {
+    const mhd_params& b = hs[i]->prm;
+    if (hs[i]->metric || hs[i]->fp32 != hs[0]->fp32 || b.reconop != a.reconop || b.stepop != a.stepop ||
+        b.dt_mode != a.dt_mode || b.pdmb != a.pdmb || b.eps != a.eps || b.alpha != a.alpha || b.beta != a.beta ||
+        b.tvd_shift != a.tvd_shift)
+      return false;
   }
-  struct Entry {
-    cudaGraphExec_t ex;
-    std::vector<int> par_end;
-  };
-  static thread_local std::map<std::vector<intptr_t>, Entry> cache;
-  std::vector<intptr_t> key;
-  for (int i = 0; i < ngrids; ++i) {
-    key.push_back((intptr_t)handles[i]);
-    key.push_back(((Handle*)handles[i])->par);
+  return true;
+}
+
+template <typename T>
+static int build_batch(Handle* const* hs, int n, BatchBufs& b) {
+  std::vector<Dev<T>> tab(2 * (size_t)n);
+  for (int i = 0; i < n; ++i) {
+    tab[i] = at_par(dev<T>(hs[i]), hs[i]->par);
+    tab[n + i] = at_par(dev<T>(hs[i]), hs[i]->par ^ 1);
   }
-  key.push_back(nsteps);
-  cudaGraphExec_t ex = nullptr;
-  auto it = cache.find(key);
-  if (it == cache.end()) {
+  std::vector<int4> map;
+  size_t off[BF_COUNT];
+  for (int f = 0; f < BF_COUNT; ++f) {
+    off[f] = map.size();
+    for (int i = 0; i < n; ++i) {
+      const dim3 dd = Batch<T>::dims(f, hs[i]->g, hs[0]->tile_td, hs[0]->tile_ey);
+      for (unsigned z = 0; z < dd.z; ++z)
+        for (unsigned y = 0; y < dd.y; ++y)
+          for (unsigned x = 0; x < dd.x; ++x) map.push_back(make_int4(i, (int)x, (int)y, (int)z));
+    }
+    const size_t nb = map.size() - off[f];
+    if (nb >= (size_t)INT32_MAX) return fail(MHD_E_ARG, "ensemble too large for one launch per kernel family");
+    b.view.nblk[f] = (int)nb;
+  }
+  CK(cudaMalloc(&b.tabs, sizeof(Dev<T>) * tab.size()));
+  CK(cudaMalloc(&b.maps, sizeof(int4) * map.size()));
+  CK(cudaMemcpy(b.tabs, tab.data(), sizeof(Dev<T>) * tab.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b.maps, map.data(), sizeof(int4) * map.size(), cudaMemcpyHostToDevice));
+  b.view.tab[0] = b.tabs;
+  b.view.tab[1] = (const Dev<T>*)b.tabs + n;
+  for (int f = 0; f < BF_COUNT; ++f) b.view.map[f] = b.maps + off[f];
+  b.view.ngrids = n;
+  const mhd_params& p = hs[0]->prm;
+  b.view.pdmb = p.pdmb; b.view.eps = p.eps; b.view.alpha = p.alpha; b.view.beta = p.beta;
+  b.view.tvd_shift = p.tvd_shift;
+  b.view.tile_td = hs[0]->tile_td;
+  b.view.tile_ey = hs[0]->tile_ey;
+  return MHD_OK;
+}
+
+// nsteps RK steps of every grid of a batch; returns the number of half swaps.
+template <typename T>
+static int enqueue_batch(const BatchView& v, int stepop, int dt_mode, int nsteps, cudaStream_t st) {
+  int flips = 0;
+  const int nst = (stepop == MHD_STEP_RK2) ? 2 : 3;
+  for (int s = 0; s < nsteps; ++s) {
+    Batch<T>::cfl(v, flips & 1, dt_mode == MHD_DT_CFL ? 1 : 0, st);
+    for (int k = 1; k <= nst; ++k) {
+      int form = -1;
+      double c = 0.0, den = 1.0;
+      if (k > 1) {
+        if (nst == 2) { form = 0; den = 2.0; }
+        else if (k == 2) { form = 1; c = 3.0; den = 4.0; }
+        else { form = 2; c = 2.0; den = 3.0; }
+      }
+      Batch<T>::stage(v, flips & 1, form, c, den, st);
+      ++flips;
+    }
+  }
+  return flips;
+}
+
+// Graph of nsteps steps of every grid: batched (one launch per kernel family
+// over all grids) when the grids allow it, else one branch per grid.
+static int capture_ensemble(const std::vector<Handle*>& hs, int nsteps, cudaGraphExec_t* ex,
+                            std::vector<int>& pars, BatchBufs& bufs) {
+  Handle* h0 = hs[0];
+  const int n = (int)hs.size();
+  pars.resize(n);
+  cudaGraph_t gr = nullptr;
+  if (batchable(hs.data(), n)) {
+    int rc = h0->fp32 ? build_batch<float>(hs.data(), n, bufs) : build_batch<double>(hs.data(), n, bufs);
+    if (rc) return rc;
+    CK(cudaStreamBeginCapture(h0->st, cudaStreamCaptureModeThreadLocal));
+    const int flips = h0->fp32 ? enqueue_batch<float>(bufs.view, h0->prm.stepop, h0->prm.dt_mode, nsteps, h0->st)
+                               : enqueue_batch<double>(bufs.view, h0->prm.stepop, h0->prm.dt_mode, nsteps, h0->st);
+    CK(cudaStreamEndCapture(h0->st, &gr));
+    for (int i = 0; i < n; ++i) pars[i] = hs[i]->par ^ (flips & 1);
+  } else {
     cudaEvent_t fork;
     CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    std::vector<cudaEvent_t> joins(n, nullptr);
     CK(cudaStreamBeginCapture(h0->st, cudaStreamCaptureModeThreadLocal));
-    CK(cudaEventRecord(fork, h0->st));
-    std::vector<cudaEvent_t> joins(ngrids);
-    for (int i = 1; i < ngrids; ++i) {
-      Handle* h = (Handle*)handles[i];
-      CK(cudaStreamWaitEvent(h->st, fork, 0));
-    }
-    std::vector<int> pars(ngrids);
-    for (int i = 0; i < ngrids; ++i) {
-      Handle* h = (Handle*)handles[i];
+    cudaEventRecord(fork, h0->st);
+    for (int i = 1; i < n; ++i) cudaStreamWaitEvent(hs[i]->st, fork, 0);
+    for (int i = 0; i < n; ++i) {
+      Handle* h = hs[i];
       int par = h->par;
       for (int s = 0; s < nsteps; ++s) {
         if (h->fp32) enqueue_any<float>(h, par, h->st);
@@ -1102,32 +1183,206 @@ int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* 
       }
       pars[i] = par;
       if (i > 0) {
-        CK(cudaEventCreateWithFlags(&joins[i], cudaEventDisableTiming));
-        CK(cudaEventRecord(joins[i], h->st));
-        CK(cudaStreamWaitEvent(h0->st, joins[i], 0));
+        cudaEventCreateWithFlags(&joins[i], cudaEventDisableTiming);
+        cudaEventRecord(joins[i], h->st);
+        cudaStreamWaitEvent(h0->st, joins[i], 0);
       }
     }
-    cudaGraph_t gr;
-    CK(cudaStreamEndCapture(h0->st, &gr));
-    CK(cudaGraphInstantiate(&ex, gr, 0));
-    cudaGraphDestroy(gr);
-    for (int i = 1; i < ngrids; ++i) cudaEventDestroy(joins[i]);
+    cudaError_t e = cudaStreamEndCapture(h0->st, &gr);
+    for (int i = 1; i < n; ++i)
+      if (joins[i]) cudaEventDestroy(joins[i]);
     cudaEventDestroy(fork);
-    cache[key] = Entry{ex, pars};
-    it = cache.find(key);
+    if (e != cudaSuccess) return fail(MHD_E_CUDA, std::string("ensemble capture: ") + cudaGetErrorString(e));
   }
-  ex = it->second.ex;
-  for (int i = 0; i < ngrids; ++i) ((Handle*)handles[i])->par = it->second.par_end[i];
-  CK(cudaGraphLaunch(ex, h0->st));
-  uint32_t acc = 0;
+  cudaError_t e = cudaGraphInstantiate(ex, gr, 0);
+  cudaGraphDestroy(gr);
+  if (e != cudaSuccess) return fail(MHD_E_CUDA, std::string("ensemble graph: ") + cudaGetErrorString(e));
+  return MHD_OK;
+}
+
+// Ensemble: nsteps steps of every grid in one CUDA graph on the first grid's
+// stream; graphs cached per (grids, their current halves, nsteps, shapes).
+int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* status) {
+  if (!handles || ngrids <= 0 || nsteps <= 0) return fail(MHD_E_ARG, "bad ensemble arguments");
+  std::vector<Handle*> hs(ngrids);
   for (int i = 0; i < ngrids; ++i) {
     Handle* h = (Handle*)handles[i];
+    if (!h) return fail(MHD_E_ARG, "null handle in ensemble");
+    if (h->fp32 != ((Handle*)handles[0])->fp32) return fail(MHD_E_ARG, "ensemble grids must share the precision");
+    for (int j = 0; j < i; ++j)
+      if (hs[j] == h) return fail(MHD_E_ARG, "a grid appears twice in the ensemble");
+    hs[i] = h;
+  }
+  Handle* h0 = hs[0];
+  struct Entry {
+    cudaGraphExec_t ex = nullptr;
+    std::vector<int> par_end;
+    BatchBufs bufs;
+  };
+  static thread_local std::map<std::vector<unsigned long long>, Entry> cache;
+  std::vector<unsigned long long> key;
+  for (Handle* h : hs) {
+    key.push_back(h->uid);
+    key.push_back((unsigned long long)h->par);
+  }
+  key.push_back((unsigned long long)nsteps);
+  key.push_back((unsigned long long)(h0->tile_td * 64 + h0->tile_ey));  // the batch's launch shapes
+  auto it = cache.find(key);
+  if (it == cache.end()) {
+    Entry en;
+    int rc = capture_ensemble(hs, nsteps, &en.ex, en.par_end, en.bufs);
+    if (rc) {
+      if (en.bufs.tabs) cudaFree(en.bufs.tabs);
+      if (en.bufs.maps) cudaFree(en.bufs.maps);
+      return rc;
+    }
+    it = cache.emplace(key, en).first;
+  }
+  // order the graph after work already queued on every grid's own stream
+  for (int i = 1; i < ngrids; ++i) {
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    CK(cudaEventRecord(e, hs[i]->st));
+    CK(cudaStreamWaitEvent(h0->st, e, 0));
+    cudaEventDestroy(e);
+  }
+  for (int i = 0; i < ngrids; ++i) hs[i]->par = it->second.par_end[i];
+  CK(cudaGraphLaunch(it->second.ex, h0->st));
+  // h0's stream carries the whole graph: waiting on it first covers every grid
+  uint32_t acc = 0;
+  for (int i = 0; i < ngrids; ++i) {
     uint32_t st = 0;
-    int rc = finish(h, nullptr, &st);
+    int rc = finish(hs[i], nullptr, &st);
     if (rc) return rc;
     acc |= st;
   }
   if (status) *status = acc;
+  return MHD_OK;
+}
+
+// ---- tile autotuner
+// Device time (ms) of `reps` runs of fn on stream st, the minimum over runs.
+template <typename Fn>
+static float time_min(cudaStream_t st, int reps, Fn fn) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best = INFINITY;
+  fn();  // warm-up (and first-launch attributes)
+  for (int r = 0; r < reps; ++r) {
+    cudaEventRecord(a, st);
+    fn();
+    cudaEventRecord(b, st);
+    if (cudaEventSynchronize(b) != cudaSuccess) break;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    best = ms < best ? ms : best;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return best;
+}
+
+static void drop_graphs(Handle* h) {
+  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second.first);
+  h->graphs.clear();
+}
+
+static bool tunable(const Handle* h) {
+  return h->fp32 && !h->metric && h->prm.reconop == MHD_RECON_PDM;
+}
+
+int mhd_autotune(void* handle, int32_t reps, int32_t out[2]) {
+  Handle* h = (Handle*)handle;
+  if (!h || reps <= 0) return fail(MHD_E_ARG, "bad autotune arguments");
+  if (tunable(h)) {
+    int rc = wait_stream(h);
+    if (rc) return rc;
+    // The timed launches (EMF, face fluxes + update) write only scratch (E,
+    // F, dU) and the other half of the double buffer, so the state a step
+    // starts from is untouched; every tile choice gives the same bits.
+    float best = INFINITY;
+    int pick = h->tile_td;
+    for (int td : kTileTD) {
+      h->tile_td = td;
+      carve<float>(h, h->df, (char*)h->buf);
+      Dev<float> d = at_par(h->df, h->par);
+      const Inp<float> in = state_inp(d);
+      Launch<float>::hydro(d, in, 0, -1, 0.0, 1.0, false, h->st);
+      const float ms = time_min(h->st, reps, [&] {
+        Launch<float>::hydro(d, in, 1, -1, 0.0, 1.0, false, h->st);
+        Launch<float>::hydro(d, in, 2, -1, 0.0, 1.0, false, h->st);
+      });
+      if (ms < best) { best = ms; pick = td; }
+    }
+    h->tile_td = pick;
+    best = INFINITY;
+    pick = h->tile_ey;
+    for (int ey : kTileEY) {
+      h->tile_ey = ey;
+      carve<float>(h, h->df, (char*)h->buf);
+      Dev<float> d = at_par(h->df, h->par);
+      const float ms = time_min(h->st, reps, [&] { Launch<float>::emf(d, state_inp(d), h->st); });
+      if (ms < best) { best = ms; pick = ey; }
+    }
+    h->tile_ey = pick;
+    carve<float>(h, h->df, (char*)h->buf);
+    drop_graphs(h);
+    CK(cudaGetLastError());
+  }
+  if (out) { out[0] = h->tile_td; out[1] = h->tile_ey; }
+  return MHD_OK;
+}
+
+int mhd_ensemble_autotune(void** handles, int32_t ngrids, int32_t reps, int32_t out[2]) {
+  if (!handles || ngrids <= 0 || reps <= 0) return fail(MHD_E_ARG, "bad autotune arguments");
+  std::vector<Handle*> hs(ngrids);
+  for (int i = 0; i < ngrids; ++i) {
+    hs[i] = (Handle*)handles[i];
+    if (!hs[i]) return fail(MHD_E_ARG, "null handle in ensemble");
+  }
+  Handle* h0 = hs[0];
+  if (tunable(h0) && batchable(hs.data(), ngrids)) {
+    for (Handle* h : hs) {
+      int rc = wait_stream(h);
+      if (rc) return rc;
+    }
+    int best_td = h0->tile_td, best_ey = h0->tile_ey;
+    float best = INFINITY;
+    for (int td : kTileTD) {
+      for (Handle* h : hs) h->tile_td = td;
+      BatchBufs b;
+      int rc = build_batch<float>(hs.data(), ngrids, b);
+      if (rc == MHD_OK) {
+        const float ms = time_min(h0->st, reps, [&] { Batch<float>::parts(b.view, 0, 2, -1, 0.0, 1.0, h0->st); });
+        if (ms < best) { best = ms; best_td = td; }
+      }
+      cudaFree(b.tabs);
+      cudaFree(b.maps);
+      if (rc) return rc;
+    }
+    best = INFINITY;
+    for (int ey : kTileEY) {
+      for (Handle* h : hs) { h->tile_td = best_td; h->tile_ey = ey; }
+      BatchBufs b;
+      int rc = build_batch<float>(hs.data(), ngrids, b);
+      if (rc == MHD_OK) {
+        const float ms = time_min(h0->st, reps, [&] { Batch<float>::parts(b.view, 0, 1, -1, 0.0, 1.0, h0->st); });
+        if (ms < best) { best = ms; best_ey = ey; }
+      }
+      cudaFree(b.tabs);
+      cudaFree(b.maps);
+      if (rc) return rc;
+    }
+    for (Handle* h : hs) {
+      h->tile_td = best_td;
+      h->tile_ey = best_ey;
+      carve<float>(h, h->df, (char*)h->buf);
+      drop_graphs(h);
+    }
+    CK(cudaGetLastError());
+  }
+  if (out) { out[0] = h0->tile_td; out[1] = h0->tile_ey; }
   return MHD_OK;
 }
 

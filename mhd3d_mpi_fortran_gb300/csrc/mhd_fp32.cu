@@ -5,4 +5,5 @@
 
 namespace mhd {
 template struct Launch<float>;
+template struct Batch<float>;
 }

@@ -5,4 +5,5 @@
 
 namespace mhd {
 template struct Launch<double>;
+template struct Batch<double>;
 }

@@ -18,6 +18,7 @@
 //   fill_hydro_mpi / fill_mag_mpi (781-819, 346-616)              -> k_fill
 #pragma once
 #include <cuda_runtime.h>
+#include <type_traits>
 #include <math.h>
 #include <stdint.h>
 #include "mhd_state.h"
@@ -303,6 +304,35 @@ __device__ __forceinline__ T corner_vel(const T* __restrict__ v, long long c, lo
   return T(0.25) * (v00 + v01 + v10 + v11);
 }
 
+// The current state as a stage input (RK stages of a batch read their own grid's state).
+template <typename T>
+__device__ __forceinline__ Inp<T> state_view(const Dev<T>& d) {
+  return Inp<T>{d.rho, d.vx, d.vy, d.vz, d.p, d.bx, d.by, d.bz, d.bi, d.bj, d.bk};
+}
+
+// ------------------------------------------------------------ kernel args
+// Argument of the step kernels that also run batched over an ensemble.
+// B = false: one grid, its Dev by value, block index from blockIdx.
+// B = true: many grids in one flattened 1-D launch; block b takes its grid
+// and block coordinates from map[b] = {grid, bx, by, bz} and its Dev from
+// tab[grid] (by value: a snapshot the compiler keeps in registers).
+template <typename T, bool B> struct KArg;
+template <typename T> struct KArg<T, false> {
+  Dev<T> d;
+  __device__ __forceinline__ int4 blk() const {
+    return make_int4(0, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z);
+  }
+  __device__ __forceinline__ const Dev<T>& dev(const int4&) const { return d; }
+};
+template <typename T> struct KArg<T, true> {
+  const Dev<T>* __restrict__ tab;
+  const int4* __restrict__ map;
+  __device__ __forceinline__ int4 blk() const { return map[blockIdx.x]; }
+  __device__ __forceinline__ Dev<T> dev(const int4& b) const { return tab[b.x]; }
+};
+template <typename T>
+inline KArg<T, false> one(const Dev<T>& d) { return KArg<T, false>{d}; }
+
 // ------------------------------------------------------------- small kernels
 template <typename T>
 __device__ __forceinline__ long long idx3(const Geom& g, int i, int j, int k) {
@@ -360,17 +390,19 @@ __device__ __forceinline__ float cfl_sqrt(float x) { return x > 0.0f ? x * rsqrt
 // save != 0 also stores U^n of the RK stage combines (advance_previous,
 // 3794-3819) at interior cells and faces, the only places they are read.
 // The minimum is reduced in T and converted to FP64 once per block.
-template <typename T, bool M>
-__global__ void __launch_bounds__(256) k_cfl(Dev<T> d, int save) {
+template <typename T, bool M, bool B>
+__global__ void __launch_bounds__(256) k_cfl(KArg<T, B> ka, int save) {
+  const int4 bb = ka.blk();
+  const auto& d = ka.dev(bb);
   const Geom& g = d.g;
   T m = T(INFINITY);
   unsigned st = 0;
   const T gm1 = d.gam - T(1);
   typedef Ops<T> O;
-  const int i = blockIdx.x * 32 + (threadIdx.x & 31);
-  const int j = blockIdx.y * 8 + (threadIdx.x >> 5);
-  const int k1 = min(g.nz, (int)(blockIdx.z + 1) * 8);
-  for (int k = blockIdx.z * 8; k < k1; ++k) {
+  const int i = bb.y * 32 + (threadIdx.x & 31);
+  const int j = bb.z * 8 + (threadIdx.x >> 5);
+  const int k1 = min(g.nz, (bb.w + 1) * 8);
+  for (int k = bb.w * 8; k < k1; ++k) {
     if (i >= g.nx || j >= g.ny) break;
     const int c = i + g.px * (j + g.py * k);
     T r0 = d.rho[c], p0 = d.p[c], u = d.vx[c], v = d.vy[c], w = d.vz[c];
@@ -451,6 +483,24 @@ __global__ void k_cfl_final(Dev<T> d, int mode) {
     s->tau0 = dt;
   }
   // mode 3: read-only (diagnostics); tau untouched
+}
+
+// k_cfl_final of every grid of a batch (one thread per grid; RK modes 0, 1).
+template <typename T>
+__global__ void k_cfl_final_batch(const Dev<T>* __restrict__ tab, int ngrids, int mode) {
+  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= ngrids) return;
+  Scal* s = tab[gi].sc;
+  double dt = __longlong_as_double((long long)s->dtmin_bits);
+  s->dtmin_bits = (unsigned long long)__double_as_longlong(INFINITY);
+  s->dt_cfl = dt;
+  if (mode == 0) {
+    if (dt < s->tau0) s->status |= ST_CFL;
+    s->tau = s->tau0;
+  } else if (mode == 1) {
+    s->tau = dt;
+    s->tau0 = dt;
+  }
 }
 
 // advance_previous for RK (3794-3819): U^n of the stage combines.
@@ -689,11 +739,14 @@ __device__ __forceinline__ void recon_win(const T* w, const Prm<T>& P, T& fl, T&
 // Face fluxes through the low face of cell c along axis D by direct (cached)
 // loads; one face per thread.  Used for the x faces of every stage and, for
 // all three axes, by the kernel-level debug entry point.
-template <typename T, int RECON, int D, bool M>
-__global__ void k_flux(Dev<T> d, Inp<T> in, Prm<T> P) {
+template <typename T, int RECON, int D, bool M, bool B>
+__global__ void k_flux(KArg<T, B> ka, Inp<T> in0, Prm<T> P) {
+  const int4 bb = ka.blk();
+  const auto& d = ka.dev(bb);
+  const Inp<T> in = B ? state_view(d) : in0;
   const Geom& g = d.g;
   const int ni = g.nx0 + (D == 0), nj = g.ny0 + (D == 1), nk = g.nz0 + (D == 2);
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = bb.y * blockDim.x + threadIdx.x;
   if (t >= ni * nj * nk) return;
   const int i = t % ni + g.ng;
   const int r = t / ni;
@@ -763,8 +816,7 @@ __device__ __forceinline__ void recon_col(const T* col, const Prm<T>& P, T& fl, 
 #ifndef MHD_FLUX_MINB
 #define MHD_FLUX_MINB 6
 #endif
-constexpr int TD = MHD_FLUX_TD;
-constexpr int TROWS = TD + 8;
+constexpr int TD = MHD_FLUX_TD;  // default tile length; FP32 PDM also has 4 and 16 (autotuner)
 constexpr bool FLUX_STAGED = MHD_FLUX_STAGED != 0;
 
 // Resident blocks per SM requested for the flux tiles: FP32 trades registers
@@ -773,25 +825,30 @@ constexpr bool FLUX_STAGED = MHD_FLUX_STAGED != 0;
 template <typename T> struct FluxMinB { static constexpr int value = MHD_FLUX_MINB; };
 template <> struct FluxMinB<double> { static constexpr int value = 2; };
 
-template <typename T>
+template <typename T, int TDV = TD>
 __host__ __device__ constexpr size_t flux_t_smem() {
-  return sizeof(T) * ((FLUX_STAGED ? 8 * TROWS * 32 : 0) + 8 * (TD + 1) * 32);
+  return sizeof(T) * ((FLUX_STAGED ? 8 * (TDV + 8) * 32 : 0) + 8 * (TDV + 1) * 32);
 }
 
-template <typename T, int RECON, int D, bool M>
-__global__ void __launch_bounds__(32 * (TD + 1), FluxMinB<T>::value)
-    k_flux_t(Dev<T> d, Inp<T> in, Prm<T> P, int form, T cw, T den, int ab) {
+template <typename T, int RECON, int D, bool M, bool B, int TDV = TD>
+__global__ void __launch_bounds__(32 * (TDV + 1), FluxMinB<T>::value)
+    k_flux_t(KArg<T, B> ka, Inp<T> in0, Prm<T> P, int form, T cw, T den, int ab) {
+  constexpr int TD = TDV;
+  constexpr int TROWS = TDV + 8;
+  const int4 bb = ka.blk();
+  const auto& d = ka.dev(bb);
+  const Inp<T> in = B ? state_view(d) : in0;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sv = reinterpret_cast<T*>(smem_raw);                      // [8][TROWS][32] cell fields
   T* sF = sv + (FLUX_STAGED ? 8 * TROWS * 32 : 0);             // [8][TD+1][32] face fluxes
   const Geom& g = d.g;
   const int tx = threadIdx.x, r = threadIdx.y;
-  const int i0 = blockIdx.x * 32 + g.ng;
+  const int i0 = bb.y * 32 + g.ng;
   const int i = i0 + tx;
   const int n0 = (D == 1) ? g.ny0 : g.nz0;
   const int nD = (D == 1) ? g.ny : g.nz;
-  const int cd0 = blockIdx.y * TD + g.ng;  // first cell of the tile along D
-  const int o = blockIdx.z + g.ng;         // remaining transverse index
+  const int cd0 = bb.z * TD + g.ng;  // first cell of the tile along D
+  const int o = bb.w + g.ng;         // remaining transverse index
   const int s = (D == 1) ? g.px : (int)g.plane;
   const int rowbase = (D == 1) ? i0 + g.px * g.py * o : i0 + g.px * o;  // + cd * s
   const T* src[8] = {in.rho, in.vx, in.vy, in.vz, in.p, in.bx, in.by, in.bz};
@@ -930,8 +987,11 @@ __global__ void k_emf(Dev<T> d, Inp<T> in, Prm<T> P) {
 // into shared memory, and each edge then takes the second pass along a2, the
 // limiters (corner_pdm), the upwinded face-B reconstructions and the Alfven
 // resistivity term exactly as k_emf does.  Tile (TX, TY, TZ) in edges.
-template <typename T, int E, int TX, int TY, int TZ, int NT, bool M>
-__global__ void __launch_bounds__(NT) k_emf_pdm(Dev<T> d, Inp<T> in, Prm<T> P) {
+template <typename T, int E, int TX, int TY, int TZ, int NT, bool M, bool B>
+__global__ void __launch_bounds__(NT) k_emf_pdm(KArg<T, B> ka, Inp<T> in0, Prm<T> P) {
+  const int4 bb = ka.blk();
+  const auto& d = ka.dev(bb);
+  const Inp<T> in = B ? state_view(d) : in0;
   constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
   constexpr int HX = (E == 0) ? 0 : 4, HY = (E == 1) ? 0 : 4, HZ = (E == 2) ? 0 : 4;
   constexpr int SX = TX + 2 * HX, SY = TY + 2 * HY, SZ = TZ + 2 * HZ;
@@ -952,7 +1012,7 @@ __global__ void __launch_bounds__(NT) k_emf_pdm(Dev<T> d, Inp<T> in, Prm<T> P) {
   T* sv = reinterpret_cast<T*>(smem_raw);  // [2][NV]: v_a1, v_a2
   T* sg = sv + 2 * NV;                     // [2][NG]: first-pass interpolants
   const Geom& g = d.g;
-  const int ox = g.ng + blockIdx.x * TX, oy = g.ng + blockIdx.y * TY, oz = g.ng + blockIdx.z * TZ;
+  const int ox = g.ng + bb.y * TX, oy = g.ng + bb.z * TY, oz = g.ng + bb.w * TZ;
   const T* vel[3] = {in.vx, in.vy, in.vz};
   const T* v1 = vel[A1];
   const T* v2 = vel[A2];
@@ -1056,13 +1116,14 @@ void launch_emf_pdm(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStre
   constexpr size_t bytes = sizeof(T) * (2 * NV + 2 * NG);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_emf_pdm<T, E, TX, TY, TZ, NT, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaFuncSetAttribute(k_emf_pdm<T, E, TX, TY, TZ, NT, M, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)bytes);
     attr = true;
   }
   const Geom& g = d.g;
   const int ex = g.nx0 + (E != 0), ey = g.ny0 + (E != 1), ez = g.nz0 + (E != 2);
   dim3 grid((ex + TX - 1) / TX, (ey + TY - 1) / TY, (ez + TZ - 1) / TZ);
-  k_emf_pdm<T, E, TX, TY, TZ, NT, M><<<grid, NT, bytes, st>>>(d, in, P);
+  k_emf_pdm<T, E, TX, TY, TZ, NT, M, false><<<grid, NT, bytes, st>>>(one(d), in, P);
 }
 
 // Metric-mode EMF inputs of a stage: w^a = v . nbar_a at every cell and the
@@ -1089,12 +1150,14 @@ __global__ void k_metric_prep(Dev<T> d, Inp<T> in) {
 
 // ------------------------------------------------------------------ update
 // advance_bijk (3909-3933) + B combine, interior faces of all three arrays.
-template <typename T, bool M>
-__global__ void k_update_b(Dev<T> d, int form, T cw, T den) {
+template <typename T, bool M, bool B>
+__global__ void k_update_b(KArg<T, B> ka, int form, T cw, T den) {
+  const int4 bb = ka.blk();
+  const auto& d = ka.dev(bb);
   const Geom& g = d.g;
-  int i = blockIdx.x * blockDim.x + threadIdx.x + g.ng;
-  int j = blockIdx.y * blockDim.y + threadIdx.y + g.ng;
-  int k = blockIdx.z + g.ng;
+  int i = bb.y * blockDim.x + threadIdx.x + g.ng;
+  int j = bb.z * blockDim.y + threadIdx.y + g.ng;
+  int k = bb.w + g.ng;
   if (i > g.ng + g.nx0 || j > g.ng + g.ny0 || k > g.ng + g.nz0) return;
   bool in_x = i < g.ng + g.nx0, in_y = j < g.ng + g.ny0, in_z = k < g.ng + g.nz0;
   long long c = idx3<T>(g, i, j, k);
@@ -1200,12 +1263,14 @@ __global__ void k_fill(Dev<T> d) {
 // exactly the values the separate fill followed by get_bxyz produces.  The
 // per-axis image of every index comes from d.gmap (ghost_src tabulated at
 // set-up): cell maps of x, y, z then face maps of x, y, z, each padded to n+2.
-template <typename T, bool M>
-__global__ void __launch_bounds__(256) k_fill_bxyz(Dev<T> d, int want_vf) {
+template <typename T, bool M, bool B>
+__global__ void __launch_bounds__(256) k_fill_bxyz(KArg<T, B> ka, int want_vf) {
+  const int4 bb = ka.blk();
+  const auto& d = ka.dev(bb);
   const Geom& g = d.g;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
+  const int i = bb.y * blockDim.x + threadIdx.x;
+  const int j = bb.z * blockDim.y + threadIdx.y;
+  const int k = bb.w;
   if (i > g.nx || j > g.ny || k > g.nz) return;
   const int px = g.px, pl = (int)g.plane;
   const int c = i + px * j + pl * k;
@@ -1409,13 +1474,13 @@ void Launch<T, M>::bxyz_vf(const Dev<T>& d, bool want_vf, cudaStream_t st) {
 template <typename T, bool M>
 void Launch<T, M>::fill_bxyz(const Dev<T>& d, bool want_vf, cudaStream_t st) {
   dim3 b(64, 4, 1);
-  k_fill_bxyz<T, M><<<grid3(d.g.nx + 1, d.g.ny + 1, d.g.nz + 1, b), b, 0, st>>>(d, want_vf ? 1 : 0);
+  k_fill_bxyz<T, M, false><<<grid3(d.g.nx + 1, d.g.ny + 1, d.g.nz + 1, b), b, 0, st>>>(one(d), want_vf ? 1 : 0);
 }
 
 template <typename T, bool M>
 void Launch<T, M>::cfl(const Dev<T>& d, int mode, cudaStream_t st, bool save) {
   dim3 grid((d.g.nx + 31) / 32, (d.g.ny + 7) / 8, (d.g.nz + 7) / 8);
-  k_cfl<T, M><<<grid, 256, 0, st>>>(d, save ? 1 : 0);
+  k_cfl<T, M, false><<<grid, 256, 0, st>>>(one(d), save ? 1 : 0);
   k_cfl_final<T><<<1, 1, 0, st>>>(d, mode);
 }
 
@@ -1434,9 +1499,9 @@ void flux_r(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
   Prm<T> P = prm_of(d);
   const Geom& g = d.g;
   const int n0 = (g.nx0 + 1) * g.ny0 * g.nz0, n1 = g.nx0 * (g.ny0 + 1) * g.nz0, n2 = g.nx0 * g.ny0 * (g.nz0 + 1);
-  k_flux<T, RECON, 0, M><<<(n0 + 127) / 128, 128, 0, st>>>(d, in, P);
-  k_flux<T, RECON, 1, M><<<(n1 + 127) / 128, 128, 0, st>>>(d, in, P);
-  k_flux<T, RECON, 2, M><<<(n2 + 127) / 128, 128, 0, st>>>(d, in, P);
+  k_flux<T, RECON, 0, M, false><<<(n0 + 127) / 128, 128, 0, st>>>(one(d), in, P);
+  k_flux<T, RECON, 1, M, false><<<(n1 + 127) / 128, 128, 0, st>>>(one(d), in, P);
+  k_flux<T, RECON, 2, M, false><<<(n2 + 127) / 128, 128, 0, st>>>(one(d), in, P);
 }
 
 template <typename T, bool M>
@@ -1450,6 +1515,38 @@ void Launch<T, M>::fluxes(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
   }
 }
 
+// Face tiles of axis D (1: y, 2: z) with tile length TDV along the sweep.
+template <typename T, int RECON, int D, bool M, int TDV>
+void launch_flux_t(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, int form, T c, T den, int ab,
+                   cudaStream_t st) {
+  constexpr size_t sm = flux_t_smem<T, TDV>();
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_flux_t<T, RECON, D, M, false, TDV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    attr = true;
+  }
+  const Geom& g = d.g;
+  const dim3 grid = (D == 1) ? dim3((g.nx0 + 31) / 32, (g.ny0 + TDV - 1) / TDV, g.nz0)
+                             : dim3((g.nx0 + 31) / 32, (g.nz0 + TDV - 1) / TDV, g.ny0);
+  k_flux_t<T, RECON, D, M, false, TDV><<<grid, dim3(32, TDV + 1), sm, st>>>(one(d), in, P, form, c, den, ab);
+}
+
+// Tile lengths compiled for a (precision, reconstruction, mode): 4, 8 and 16
+// for the FP32 Cartesian PDM path (chosen by the autotuner), 8 elsewhere.
+template <typename T, int RECON, bool M>
+constexpr bool tunable() {
+  return std::is_same<T, float>::value && RECON == R_PDM && !M;
+}
+
+template <typename T, int RECON, int D, bool M>
+void flux_t_any(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, int form, T c, T den, int ab, cudaStream_t st) {
+  if constexpr (tunable<T, RECON, M>()) {
+    if (d.tile_td == 4) return launch_flux_t<T, RECON, D, M, 4>(d, in, P, form, c, den, ab, st);
+    if (d.tile_td == 16) return launch_flux_t<T, RECON, D, M, 16>(d, in, P, form, c, den, ab, st);
+  }
+  launch_flux_t<T, RECON, D, M, TD>(d, in, P, form, c, den, ab, st);
+}
+
 template <typename T, int RECON, bool M>
 void hydro_r(const Dev<T>& d, const Inp<T>& in, int part, int form, double c, double den, bool ab,
              cudaStream_t st) {
@@ -1457,25 +1554,11 @@ void hydro_r(const Dev<T>& d, const Inp<T>& in, int part, int form, double c, do
   const Geom& g = d.g;
   if (part == 0) {
     const int n0 = (g.nx0 + 1) * g.ny0 * g.nz0;
-    k_flux<T, RECON, 0, M><<<(n0 + 127) / 128, 128, 0, st>>>(d, in, P);
+    k_flux<T, RECON, 0, M, false><<<(n0 + 127) / 128, 128, 0, st>>>(one(d), in, P);
   } else if (part == 1) {
-    constexpr size_t sm = flux_t_smem<T>();
-    static bool attr = false;
-    if (!attr) {
-      cudaFuncSetAttribute(k_flux_t<T, RECON, 1, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      attr = true;
-    }
-    dim3 grid((g.nx0 + 31) / 32, (g.ny0 + TD - 1) / TD, g.nz0);
-    k_flux_t<T, RECON, 1, M><<<grid, dim3(32, TD + 1), sm, st>>>(d, in, P, -1, T(0), T(1), 0);
+    flux_t_any<T, RECON, 1, M>(d, in, P, -1, T(0), T(1), 0, st);
   } else {
-    constexpr size_t sm = flux_t_smem<T>();
-    static bool attr = false;
-    if (!attr) {
-      cudaFuncSetAttribute(k_flux_t<T, RECON, 2, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      attr = true;
-    }
-    dim3 grid((g.nx0 + 31) / 32, (g.nz0 + TD - 1) / TD, g.ny0);
-    k_flux_t<T, RECON, 2, M><<<grid, dim3(32, TD + 1), sm, st>>>(d, in, P, form, (T)c, (T)den, ab ? 1 : 0);
+    flux_t_any<T, RECON, 2, M>(d, in, P, form, (T)c, (T)den, ab ? 1 : 0, st);
   }
 }
 
@@ -1521,7 +1604,10 @@ void Launch<T, M>::emf(const Dev<T>& d, const Inp<T>& in0, cudaStream_t st) {
   }
   if (d.recon == R_PDM) {
     Prm<T> P = prm_of(d);
-    launch_emf_pdm<T, 0, 32, EiTile<T>::Y, EiTile<T>::Y, 512, M>(d, in, P, st);
+    if (std::is_same<T, float>::value && !M && d.tile_ey == 4)
+      launch_emf_pdm<T, 0, 32, 4, 4, 512, M>(d, in, P, st);
+    else
+      launch_emf_pdm<T, 0, 32, EiTile<T>::Y, EiTile<T>::Y, 512, M>(d, in, P, st);
     launch_emf_pdm<T, 1, 32, 1, 8, 256, M>(d, in, P, st);
     launch_emf_pdm<T, 2, 32, 8, 1, 256, M>(d, in, P, st);
     return;
@@ -1538,13 +1624,129 @@ template <typename T, bool M>
 void Launch<T, M>::ct(const Dev<T>& d, int form, double c, double den, cudaStream_t st) {
   dim3 b(32, 4, 1);
   const Geom& g = d.g;
-  k_update_b<T, M><<<grid3(g.nx0 + 1, g.ny0 + 1, g.nz0 + 1, b), b, 0, st>>>(d, form, (T)c, (T)den);
+  k_update_b<T, M, false><<<grid3(g.nx0 + 1, g.ny0 + 1, g.nz0 + 1, b), b, 0, st>>>(one(d), form, (T)c, (T)den);
 }
 
 template <typename T, bool M>
 void Launch<T, M>::fill(const Dev<T>& d, cudaStream_t st) {
   dim3 b(64, 4, 1);
   k_fill<T><<<grid3(d.g.nx + 1, d.g.ny + 1, d.g.nz + 1, b), b, 0, st>>>(d);
+}
+
+// ------------------------------------------------------------ batched ensemble
+template <typename T, int E, int TX, int TY, int TZ>
+constexpr size_t emf_pdm_smem() {
+  constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
+  constexpr int HX = (E == 0) ? 0 : 4, HY = (E == 1) ? 0 : 4, HZ = (E == 2) ? 0 : 4;
+  constexpr int NV = (TX + 2 * HX) * (TY + 2 * HY) * (TZ + 2 * HZ);
+  constexpr int TE = (E == 0) ? TX : (E == 1) ? TY : TZ;
+  constexpr int T1 = (A1 == 0) ? TX : (A1 == 1) ? TY : TZ;
+  constexpr int T2 = (A2 == 0) ? TX : (A2 == 1) ? TY : TZ;
+  return sizeof(T) * (2 * NV + 2 * TE * T1 * (T2 + 8));
+}
+
+inline dim3 tiles(int ex, int ey, int ez, int tx, int ty, int tz) {
+  return dim3((ex + tx - 1) / tx, (ey + ty - 1) / ty, (ez + tz - 1) / tz);
+}
+
+template <typename T>
+dim3 Batch<T>::dims(int fam, const Geom& g, int td, int ey) {
+  const int Y = std::is_same<T, float>::value ? ey : EiTile<T>::Y;
+  if (!std::is_same<T, float>::value) td = TD;
+  switch (fam) {
+    case BF_CFL: return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + 7) / 8);
+    case BF_FLUX_X: return dim3(((g.nx0 + 1) * g.ny0 * g.nz0 + 127) / 128, 1, 1);
+    case BF_FLUX_Y: return dim3((g.nx0 + 31) / 32, (g.ny0 + td - 1) / td, g.nz0);
+    case BF_FLUX_Z: return dim3((g.nx0 + 31) / 32, (g.nz0 + td - 1) / td, g.ny0);
+    case BF_EMF_I: return tiles(g.nx0, g.ny0 + 1, g.nz0 + 1, 32, Y, Y);
+    case BF_EMF_J: return tiles(g.nx0 + 1, g.ny0, g.nz0 + 1, 32, 1, 8);
+    case BF_EMF_K: return tiles(g.nx0 + 1, g.ny0 + 1, g.nz0, 32, 8, 1);
+    case BF_CT: return grid3(g.nx0 + 1, g.ny0 + 1, g.nz0 + 1, dim3(32, 4, 1));
+    default: return grid3(g.nx + 1, g.ny + 1, g.nz + 1, dim3(64, 4, 1));  // BF_FILL
+  }
+}
+
+template <typename T>
+void Batch<T>::cfl(const BatchView& v, int sel, int mode, cudaStream_t st) {
+  KArg<T, true> a{(const Dev<T>*)v.tab[sel], v.map[BF_CFL]};
+  k_cfl<T, false, true><<<v.nblk[BF_CFL], 256, 0, st>>>(a, 1);
+  k_cfl_final_batch<T><<<(v.ngrids + 127) / 128, 128, 0, st>>>((const Dev<T>*)v.tab[sel], v.ngrids, mode);
+}
+
+template <typename K>
+void set_smem(K kernel, size_t bytes) {
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+// Batched EMF families with ei tile Y (edges along y and z per block).
+template <typename T, int Y>
+void batch_emf(const BatchView& v, const Dev<T>* tab, const Prm<T>& P, cudaStream_t st) {
+  constexpr size_t si = emf_pdm_smem<T, 0, 32, Y, Y>();
+  constexpr size_t sj = emf_pdm_smem<T, 1, 32, 1, 8>();
+  constexpr size_t sk = emf_pdm_smem<T, 2, 32, 8, 1>();
+  static bool attr = false;
+  if (!attr) {
+    set_smem(k_emf_pdm<T, 0, 32, Y, Y, 512, false, true>, si);
+    set_smem(k_emf_pdm<T, 1, 32, 1, 8, 256, false, true>, sj);
+    set_smem(k_emf_pdm<T, 2, 32, 8, 1, 256, false, true>, sk);
+    attr = true;
+  }
+  const Inp<T> none{};
+  k_emf_pdm<T, 0, 32, Y, Y, 512, false, true><<<v.nblk[BF_EMF_I], 512, si, st>>>(
+      KArg<T, true>{tab, v.map[BF_EMF_I]}, none, P);
+  k_emf_pdm<T, 1, 32, 1, 8, 256, false, true><<<v.nblk[BF_EMF_J], 256, sj, st>>>(
+      KArg<T, true>{tab, v.map[BF_EMF_J]}, none, P);
+  k_emf_pdm<T, 2, 32, 8, 1, 256, false, true><<<v.nblk[BF_EMF_K], 256, sk, st>>>(
+      KArg<T, true>{tab, v.map[BF_EMF_K]}, none, P);
+}
+
+// Batched y / z face tiles of length TDV.
+template <typename T, int TDV>
+void batch_flux_t(const BatchView& v, const Dev<T>* tab, const Prm<T>& P, int form, T c, T den, cudaStream_t st) {
+  constexpr size_t sf = flux_t_smem<T, TDV>();
+  static bool attr = false;
+  if (!attr) {
+    set_smem(k_flux_t<T, R_PDM, 1, false, true, TDV>, sf);
+    set_smem(k_flux_t<T, R_PDM, 2, false, true, TDV>, sf);
+    attr = true;
+  }
+  const Inp<T> none{};
+  k_flux_t<T, R_PDM, 1, false, true, TDV><<<v.nblk[BF_FLUX_Y], dim3(32, TDV + 1), sf, st>>>(
+      KArg<T, true>{tab, v.map[BF_FLUX_Y]}, none, P, -1, T(0), T(1), 0);
+  k_flux_t<T, R_PDM, 2, false, true, TDV><<<v.nblk[BF_FLUX_Z], dim3(32, TDV + 1), sf, st>>>(
+      KArg<T, true>{tab, v.map[BF_FLUX_Z]}, none, P, form, c, den, 0);
+}
+
+template <typename T>
+void Batch<T>::parts(const BatchView& v, int sel, int which, int form, double c, double den, cudaStream_t st) {
+  const Dev<T>* tab = (const Dev<T>*)v.tab[sel];
+  // the batch shares the deck's limiter constants (checked when it is built)
+  Prm<T> P;
+  P.pdmb = (T)v.pdmb; P.eps = (T)v.eps; P.alpha = (T)v.alpha; P.beta = (T)v.beta; P.tvd_shift = v.tvd_shift;
+  constexpr bool F32 = std::is_same<T, float>::value;
+  if (which & 1) {  // EMF families
+    if (F32 && v.tile_ey == 4) batch_emf<T, 4>(v, tab, P, st);
+    else batch_emf<T, EiTile<T>::Y>(v, tab, P, st);
+  }
+  if (which & 2) {  // face fluxes and the conserved update
+    const Inp<T> none{};
+    k_flux<T, R_PDM, 0, false, true><<<v.nblk[BF_FLUX_X], 128, 0, st>>>(KArg<T, true>{tab, v.map[BF_FLUX_X]}, none,
+                                                                       P);
+    if (F32 && v.tile_td == 4) batch_flux_t<T, F32 ? 4 : TD>(v, tab, P, form, (T)c, (T)den, st);
+    else if (F32 && v.tile_td == 16) batch_flux_t<T, F32 ? 16 : TD>(v, tab, P, form, (T)c, (T)den, st);
+    else batch_flux_t<T, TD>(v, tab, P, form, (T)c, (T)den, st);
+  }
+  if (which & 4) {  // face-B update, then fill + bxyz + vf of the half the stage wrote
+    k_update_b<T, false, true><<<v.nblk[BF_CT], dim3(32, 4), 0, st>>>(KArg<T, true>{tab, v.map[BF_CT]}, form, (T)c,
+                                                                       (T)den);
+    KArg<T, true> fa{(const Dev<T>*)v.tab[sel ^ 1], v.map[BF_FILL]};
+    k_fill_bxyz<T, false, true><<<v.nblk[BF_FILL], dim3(64, 4), 0, st>>>(fa, 1);
+  }
+}
+
+template <typename T>
+void Batch<T>::stage(const BatchView& v, int sel, int form, double c, double den, cudaStream_t st) {
+  parts(v, sel, 7, form, c, den, st);
 }
 
 template <typename T, bool M>

@@ -99,6 +99,9 @@ struct Dev {
   Metric m;
   T* mw[3];
   T* mbn[3];
+  // launch shapes (host side only): y/z face-tile length and ei EMF tile,
+  // chosen by the autotuner for the FP32 Cartesian PDM path
+  int tile_td, tile_ey;
 };
 
 // Stage-input view: which arrays feed the EMF and flux kernels (RK: the
@@ -133,5 +136,39 @@ struct Launch {
   static void fill(const Dev<T>& d, cudaStream_t st);
   static void diagnostics(const Dev<T>& d, double* out5_dev, cudaStream_t st);
 };
+
+// Batched ensemble (Cartesian, PDM, RK2/RK3): each launch family covers every
+// grid of the batch in one flattened 1-D launch.  A family's per-grid block
+// grid is exactly the one its single-grid launcher uses; map[f] lists
+// {grid, bx, by, bz} for every block of the launch, grid after grid.
+enum BatchFam { BF_CFL, BF_FLUX_X, BF_FLUX_Y, BF_FLUX_Z, BF_EMF_I, BF_EMF_J, BF_EMF_K, BF_CT, BF_FILL, BF_COUNT };
+
+struct BatchView {
+  const void* tab[2];       // device Dev<T>[ngrids] for the two halves of the primitive buffers
+  const int4* map[BF_COUNT];
+  int nblk[BF_COUNT];
+  int ngrids;
+  double pdmb, eps, alpha, beta;  // limiter constants shared by the batch
+  int tvd_shift;
+  int tile_td, tile_ey;           // launch shapes shared by the batch
+};
+
+template <typename T>
+struct Batch {
+  // blocks (x, y, z) of family f for one grid with the given tiles
+  static dim3 dims(int fam, const Geom& g, int td, int ey);
+  // get_dt + advance_previous of every grid (RK); mode as Launch::cfl
+  static void cfl(const BatchView& v, int sel, int mode, cudaStream_t st);
+  // one RK stage of every grid: emf, fluxes + update, ct (on tab[sel]), then
+  // fill + bxyz + vf on tab[sel ^ 1], the half the stage wrote
+  static void stage(const BatchView& v, int sel, int form, double c, double den, cudaStream_t st);
+  // parts of a stage, bit mask: 1 EMF, 2 fluxes + conserved update (writes
+  // only scratch and the other half), 4 face-B update + fill (state)
+  static void parts(const BatchView& v, int sel, int which, int form, double c, double den, cudaStream_t st);
+};
+
+// Tile lengths the autotuner tries (FP32 Cartesian PDM).
+constexpr int kTileTD[3] = {4, 8, 16};
+constexpr int kTileEY[2] = {4, 8};
 
 }  // namespace mhd

@@ -84,6 +84,13 @@ class MHDSolver:
         check(self.lib, rc, "mhd_time_steps")
         return ms.value
 
+    def autotune(self, reps: int = 5) -> tuple:
+        """Pick the fastest compiled launch shapes for this grid (mhd_autotune);
+        returns (face-tile length, EMF tile)."""
+        out = (C.c_int32 * 2)()
+        check(self.lib, self.lib.mhd_autotune(self.h, int(reps), out), "mhd_autotune")
+        return out[0], out[1]
+
     def save(self, path: str):
         """Checkpoint everything a step depends on (mhd_checkpoint_save)."""
         check(self.lib, self.lib.mhd_checkpoint_save(self.h, str(path).encode()), "mhd_checkpoint_save")
@@ -164,9 +171,20 @@ class MHDSolver:
 
 
 def ensemble_step(solvers: list, nsteps: int) -> int:
-    """Advance independent grids together (one CUDA graph, one branch per grid)."""
+    """Advance independent grids together in one CUDA graph (mhd_ensemble_step):
+    Cartesian PDM grids with the same RK stepper share one launch per kernel
+    family; other ensembles get one graph branch per grid."""
     lib = solvers[0].lib
     arr = (C.c_void_p * len(solvers))(*[s.h.value for s in solvers])
     st = C.c_uint32()
     check(lib, lib.mhd_ensemble_step(arr, len(solvers), int(nsteps), C.byref(st)), "mhd_ensemble_step")
     return st.value
+
+
+def ensemble_autotune(solvers: list, reps: int = 5) -> tuple:
+    """Pick the fastest launch shapes for a batched ensemble (mhd_ensemble_autotune)."""
+    lib = solvers[0].lib
+    arr = (C.c_void_p * len(solvers))(*[s.h.value for s in solvers])
+    out = (C.c_int32 * 2)()
+    check(lib, lib.mhd_ensemble_autotune(arr, len(solvers), int(reps), out), "mhd_ensemble_autotune")
+    return out[0], out[1]

@@ -222,3 +222,86 @@ def test_checkpoint_restart_is_bit_exact(tmp_path, prec, stepop):
     assert ta == tb
     for k in FIELDS:
         assert np.array_equal(fa[k], fb[k]), k
+
+
+@pytest.mark.parametrize("prec,stepop", [(FP32, STEP_RK2), (FP64, STEP_RK3)])
+def test_batched_ensemble_equals_sequential(prec, stepop):
+    """Uneven Cartesian PDM grids share one launch per kernel family; each
+    grid's result is bit-identical to stepping it alone, over two calls (the
+    second replays the cached graph) and with grids starting on different
+    halves of their double-buffered state."""
+    sizes = (16, 24, 8, 12)
+    states = [ics.orszag_tang_3d(n, seed=i, amp=0.5 + 0.3 * i, ny0=n + 2 * (i % 2)) for i, n in enumerate(sizes)]
+    prms = [Params(n, n + 2 * (i % 2), n, precision=prec, stepop=stepop, tau=0.4 * ics.cfl_dt(st))
+            for i, (n, st) in enumerate(zip(sizes, states))]
+    seq = []
+    for i, (prm, st) in enumerate(zip(prms, states)):
+        with MHDSolver(prm, st) as g:
+            g.step(1 + (i % 2) + 4)
+            seq.append(g.fetch())
+    ens = [MHDSolver(p, st) for p, st in zip(prms, states)]
+    for i, e in enumerate(ens):  # odd grids one step ahead (the other buffer half for RK3)
+        e.step(1 + (i % 2))
+    ensemble_step(ens, 2)
+    ensemble_step(ens, 2)
+    for e, ref in zip(ens, seq):
+        got = e.fetch()
+        for k in FIELDS:
+            assert np.array_equal(got[k], ref[k]), k
+        e.close()
+
+
+def test_mixed_ensemble_uses_branches_and_matches():
+    """A non-batchable ensemble (AB2 next to RK2) still equals sequential stepping."""
+    s1, s2 = ics.orszag_tang_3d(12, seed=1), ics.orszag_tang_3d(10, seed=2)
+    p1 = Params(12, 12, 12, stepop=STEP_AB2, tau=0.0)
+    p2 = Params(10, 10, 10, stepop=STEP_RK2, tau=0.5 * ics.cfl_dt(s2))
+    ref = []
+    for p, s in ((p1, s1), (p2, s2)):
+        with MHDSolver(p, s) as g:
+            g.step(3)
+            ref.append(g.fetch())
+    ens = [MHDSolver(p1, s1), MHDSolver(p2, s2)]
+    ensemble_step(ens, 3)
+    for e, r in zip(ens, ref):
+        got = e.fetch()
+        for k in FIELDS:
+            assert np.array_equal(got[k], r[k]), k
+        e.close()
+
+
+def test_autotuned_shapes_give_identical_steps():
+    """Every launch shape the autotuner can pick computes the same bits."""
+    s = ics.turbulence(32, seed=3)
+    prm = Params(32, 32, 32, precision=FP32, tau=0.5 * ics.cfl_dt(s))
+    with MHDSolver(prm, s) as a, MHDSolver(prm, s) as b:
+        a.step(2)
+        b.step(2)
+        td, ey = b.autotune(reps=2)
+        assert td in (4, 8, 16) and ey in (4, 8)
+        a.step(3, graph=True)
+        b.step(3, graph=True)
+        fa, fb = a.fetch(), b.fetch()
+    for k in FIELDS:
+        assert np.array_equal(fa[k], fb[k]), k
+
+
+def test_ensemble_autotune_then_step_equals_sequential():
+    from mhd3d_mpi_fortran_gb300 import ensemble_autotune
+    sizes = (16, 20, 12)
+    states = [ics.orszag_tang_3d(n, seed=i) for i, n in enumerate(sizes)]
+    prms = [Params(n, n, n, precision=FP32, tau=0.5 * ics.cfl_dt(st)) for n, st in zip(sizes, states)]
+    seq = []
+    for prm, st in zip(prms, states):
+        with MHDSolver(prm, st) as g:
+            g.step(3)
+            seq.append(g.fetch())
+    ens = [MHDSolver(p, st) for p, st in zip(prms, states)]
+    td, ey = ensemble_autotune(ens, reps=2)
+    assert td in (4, 8, 16) and ey in (4, 8)
+    ensemble_step(ens, 3)
+    for e, ref in zip(ens, seq):
+        got = e.fetch()
+        for k in FIELDS:
+            assert np.array_equal(got[k], ref[k]), k
+        e.close()
