@@ -237,6 +237,47 @@ int mhd_autotune(void* handle, int32_t reps, int32_t out[2]);
  * and gives every grid the fastest shapes. */
 int mhd_ensemble_autotune(void** handles, int32_t ngrids, int32_t reps, int32_t out[2]);
 
+/* ---- learned coarse-grid correction (BF16 tcgen05) ---------------------- */
+
+/* Kernel-level check of the tensor-core GEMM primitive the MLP kernels are
+ * built from: C[M x N] = A[M x K] B[N x K]^T with BF16 A and B (host arrays,
+ * row-major, K contiguous, raw bf16 bits) and FP32 C; N and K multiples of 16
+ * up to 256.  No reference counterpart. */
+int mhd_tc_gemm_test(const uint16_t* a, const uint16_t* b, float* c, int32_t M, int32_t N, int32_t K);
+
+/* Learned coarse-grid correction (no reference counterpart).  A per-cell MLP,
+ * 216 inputs (3x3x3 stencil of the 8 conserved variables rho, rho v, hydro
+ * energy, cell B, normalised) -> 64 -> 64 (GELU) -> 8 outputs (5 conserved
+ * hydro increments and a cell-centred vector-potential increment, times a
+ * per-output scale).  Weights are FP32 masters with BF16 copies; every GEMM of
+ * training and inference runs on the tcgen05 tensor cores with FP32
+ * accumulation.  Parameters are one flat FP32 vector: W1[64][256] b1[64]
+ * W2[64][64] b2[64] W3[16][64] b3[16] (21648 floats; inputs 216..255 and
+ * outputs 8..15 are padding). */
+int mhd_mlp_create(const float* params, void** mlp);
+/* Read (params_out) and/or replace (params_in) the parameters; either may be NULL. */
+int mhd_mlp_params(void* mlp, float* params_out, const float* params_in);
+/* Feature normalisation (mean, std per variable) and output scales. */
+int mhd_mlp_set_norm(void* mlp, const float* mean8, const float* std8, const float* scale8);
+/* Training set: n rows of 256 BF16 features (raw bits) and 8 FP32 targets. */
+int mhd_mlp_set_data(void* mlp, const uint16_t* x, const float* t, int64_t n);
+/* Gradient of the mean squared error over rows [offset, offset+count) of the
+ * training set (no update): grad_out[21648], *loss_out the mean loss. */
+int mhd_mlp_grad(void* mlp, int64_t offset, int32_t count, float* grad_out, float* loss_out);
+/* iters Adam steps on random minibatches of `batch` rows; *loss_out is the
+ * mean minibatch loss of the last iterations. */
+int mhd_mlp_train(void* mlp, int32_t iters, int32_t batch, float lr, uint64_t seed, float* loss_out);
+/* Raw network outputs y[n][8] for feature rows x[n][256] (BF16 bits). */
+int mhd_mlp_forward(void* mlp, const uint16_t* x, int64_t n, float* y);
+/* Apply the correction once to an FP32 Cartesian periodic RK grid (the state
+ * after a step): hydro increments per cell (a cell whose corrected density or
+ * pressure would not be positive keeps its state) and face B += curl of the
+ * edge-averaged vector potential, so div B stays at round-off. */
+int mhd_mlp_apply(void* handle, void* mlp);
+/* nsteps x (mhd_step + mhd_mlp_apply), one host synchronisation at the end. */
+int mhd_step_corrected(void* handle, void* mlp, int32_t nsteps, double* tau_out, uint32_t* status);
+int mhd_mlp_free(void* mlp);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,7 +27,9 @@ EXPORTS = (
     "mhd_set_tau", "mhd_set_profiling", "mhd_last_timings", "mhd_free", "mhd_last_error",
     "mhd_debug_fluxes", "mhd_debug_emf", "mhd_ensemble_step", "mhd_time_steps",
     "mhd_diagnostics_noalloc", "mhd_checkpoint_save", "mhd_checkpoint_load",
-    "mhd_autotune", "mhd_ensemble_autotune",
+    "mhd_autotune", "mhd_ensemble_autotune", "mhd_tc_gemm_test",
+    "mhd_mlp_create", "mhd_mlp_params", "mhd_mlp_set_norm", "mhd_mlp_set_data", "mhd_mlp_grad", "mhd_mlp_train",
+    "mhd_mlp_forward", "mhd_mlp_apply", "mhd_step_corrected", "mhd_mlp_free",
 )
 
 
@@ -124,6 +126,18 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.mhd_ensemble_step.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.POINTER(C.c_uint32)]
     lib.mhd_checkpoint_save.argtypes = [vp, C.c_char_p]
     lib.mhd_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
+    lib.mhd_tc_gemm_test.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
+    fp = C.POINTER(C.c_float)
+    lib.mhd_mlp_create.argtypes = [C.c_void_p, C.POINTER(vp)]
+    lib.mhd_mlp_params.argtypes = [vp, C.c_void_p, C.c_void_p]
+    lib.mhd_mlp_set_norm.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.mhd_mlp_set_data.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_int64]
+    lib.mhd_mlp_grad.argtypes = [vp, C.c_int64, C.c_int32, C.c_void_p, fp]
+    lib.mhd_mlp_train.argtypes = [vp, C.c_int32, C.c_int32, C.c_float, C.c_uint64, fp]
+    lib.mhd_mlp_forward.argtypes = [vp, C.c_void_p, C.c_int64, C.c_void_p]
+    lib.mhd_mlp_apply.argtypes = [vp, vp]
+    lib.mhd_step_corrected.argtypes = [vp, vp, C.c_int32, dp, C.POINTER(C.c_uint32)]
+    lib.mhd_mlp_free.argtypes = [vp]
     lib.mhd_ensemble_autotune.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.POINTER(C.c_int32)]
     lib.mhd_checkpoint_load.argtypes = [C.c_char_p, C.POINTER(vp)]
     lib.mhd_diagnostics_noalloc.argtypes = [C.POINTER(CParams)] + [vp] * 12 + [vp]

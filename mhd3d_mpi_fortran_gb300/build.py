@@ -8,6 +8,7 @@ linked into one C-ABI library (declared in ``include/mhd_gpu.h``):
 * ``csrc/mhd_metric_fp64.cu`` / ``mhd_metric_fp32.cu`` -- the same kernels in
   curvilinear metric mode,
 * ``csrc/mhd_geom.cu`` -- FP64 metric terms from node coordinates (``-fmad=false``),
+* ``csrc/mhd_mlp.cu`` -- BF16 tcgen05 kernels of the learned coarse-grid correction,
 * ``csrc/mhd_api.cu``  -- host sequencing and the ``extern "C"`` entry points,
 * ``csrc/mhd_noalloc.cu`` -- the allocation-free diagnostics entry point.
 
@@ -39,6 +40,7 @@ UNITS = {
     "mhd_metric_fp64": ["-fmad=false"],
     "mhd_metric_fp32": ["-fmad=true"],
     "mhd_geom": ["-fmad=false"],
+    "mhd_mlp": [],
     "mhd_api": ["-Xcompiler", "-fopenmp"],
     "mhd_noalloc": ["-fmad=false"],
 }

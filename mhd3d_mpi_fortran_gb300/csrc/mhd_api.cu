@@ -1386,6 +1386,38 @@ int mhd_ensemble_autotune(void** handles, int32_t ngrids, int32_t reps, int32_t 
   return MHD_OK;
 }
 
+// ---- learned coarse-grid correction
+int mhd_mlp_apply(void* handle, void* mlp) {
+  Handle* h = (Handle*)handle;
+  if (!h || !mlp) return fail(MHD_E_ARG, "null argument");
+  if (!h->fp32 || h->metric || h->prm.stepop == MHD_STEP_AB2)
+    return fail(MHD_E_ARG, "the learned correction runs on FP32 Cartesian grids with an RK stepper");
+  for (int a = 0; a < 3; ++a)
+    if (h->prm.bc[a] != MHD_BC_PERIODIC) return fail(MHD_E_ARG, "the learned correction needs periodic axes");
+  Dev<float> d = at_par(h->df, h->par);
+  int rc = mlp_correct(mlp, d, h->st);
+  if (rc) return rc;
+  Launch<float>::fill_bxyz(d, true, h->st);
+  CK(cudaGetLastError());
+  return MHD_OK;
+}
+
+int mhd_step_corrected(void* handle, void* mlp, int32_t nsteps, double* tau_out, uint32_t* status) {
+  Handle* h = (Handle*)handle;
+  if (!h || !mlp || nsteps < 0) return fail(MHD_E_ARG, "bad arguments");
+  for (int s = 0; s < nsteps; ++s) {
+    int rc = do_steps<float>(h, 1);
+    if (!rc) rc = mhd_mlp_apply(handle, mlp);
+    if (rc) {
+      if (status) *status = MHD_ST_CUDA_ERROR;
+      return rc;
+    }
+  }
+  int rc = finish(h, tau_out, status);
+  if (rc) return rc;
+  return mlp_status(mlp);
+}
+
 int mhd_free(void* handle) {
   Handle* h = (Handle*)handle;
   if (!h) return MHD_OK;

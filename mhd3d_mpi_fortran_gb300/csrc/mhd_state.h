@@ -167,6 +167,17 @@ struct Batch {
   static void parts(const BatchView& v, int sel, int which, int form, double c, double den, cudaStream_t st);
 };
 
+// Normalisation of the learned correction: features (U - mean) / std per
+// conserved variable, outputs times scale.
+struct MlpNorm {
+  float mean[8], std[8], scale[8];
+};
+// Apply the learned correction of MLP handle h to the interior of an FP32
+// Cartesian periodic grid (mhd_mlp.cu); the caller refills the ghosts.
+int mlp_correct(void* h, Dev<float>& d, cudaStream_t st);
+// MHD_E_TIMEOUT if an MLP kernel recorded a wait that gave up, else MHD_OK.
+int mlp_status(void* h);
+
 // Tile lengths the autotuner tries (FP32 Cartesian PDM).
 constexpr int kTileTD[3] = {4, 8, 16};
 constexpr int kTileEY[2] = {4, 8};

@@ -1,0 +1,113 @@
+"""Tensor-core (tcgen05) kernels of the learned coarse-grid correction,
+checked through the C ABI against the numpy oracle (oracle/mlp_oracle.py),
+and the correction coupled to the solver."""
+import numpy as np
+import pytest
+
+from mhd3d_mpi_fortran_gb300 import abi, ics, learned, MHDSolver
+from mhd3d_mpi_fortran_gb300.abi import Params, FP32
+from oracle import mlp_oracle as mo
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 64, 256), (300, 16, 64), (256, 64, 128), (128, 256, 16)])
+def test_tc_gemm_matches_fp32_product_of_bf16_operands(M, N, K):
+    lib = abi.load()
+    rng = np.random.default_rng(M + N + K)
+    a = mo.bf16_bits(rng.standard_normal((M, K)))
+    b = mo.bf16_bits(rng.standard_normal((N, K)))
+    c = np.zeros((M, N), dtype=np.float32)
+    rc = lib.mhd_tc_gemm_test(a.ctypes.data, b.ctypes.data, c.ctypes.data, M, N, K)
+    assert rc == 0, lib.mhd_last_error()
+    ref = mo.bf16_val(a) @ mo.bf16_val(b).T
+    # exact BF16 products, FP32 accumulation
+    assert np.abs(c - ref).max() <= 1e-5 * np.abs(ref).max() + 1e-5
+
+
+def _features(n, seed):
+    rng = np.random.default_rng(seed)
+    x = np.zeros((n, mo.FIN), dtype=np.float32)
+    x[:, :216] = rng.standard_normal((n, 216))
+    return mo.bf16_bits(x)
+
+
+def test_forward_matches_oracle():
+    p = mo.init_params(1)
+    xb = _features(300, 2)
+    mlp = learned.MLP(p)
+    y = mlp.forward(xb)
+    ref = mo.forward(p, mo.bf16_val(xb), bf16=True)
+    # only FP32 accumulation order (and the BF16 roundings it can flip) differ
+    assert np.abs(y - ref).max() <= 1e-2 * np.abs(ref).max()
+    assert np.sqrt(np.mean((y - ref) ** 2)) <= 2e-3 * np.sqrt(np.mean(ref ** 2))
+    mlp.close()
+
+
+def test_gradient_matches_oracle():
+    """Gradients of the tensor-core backward pass (all weight gradients are
+    tcgen05 GEMMs) against the oracle with the same BF16 rounding points."""
+    p = mo.init_params(4)
+    n = 384
+    xb = _features(n, 5)
+    t = (np.random.default_rng(6).standard_normal((n, mo.NOUT)) * 0.5).astype(np.float32)
+    mlp = learned.MLP(p)
+    mlp.set_data(xb, t)
+    loss, g = mlp.grad(0, n)
+    lref, gref = mo.loss_and_grad(p, mo.bf16_val(xb), t, bf16=True)
+    assert loss == pytest.approx(lref, rel=1e-3)
+    gw, gr = mo.unpack(g), mo.unpack(gref)
+    for name, _ in mo.SHAPES:
+        a, b = gw[name], gr[name]
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+        assert rel <= 2e-2, (name, rel)
+    mlp.close()
+
+
+def test_training_reduces_the_loss():
+    rng = np.random.default_rng(7)
+    n = 8192
+    x = np.zeros((n, mo.FIN), dtype=np.float32)
+    x[:, :216] = rng.standard_normal((n, 216))
+    wt = rng.standard_normal((216, mo.NOUT)) / np.sqrt(216)
+    t = np.tanh(x[:, :216] @ wt).astype(np.float32)
+    mlp = learned.MLP(mo.init_params(8))
+    xb = mo.bf16_bits(x)
+    mlp.set_data(xb, t)
+    l0, _ = mlp.grad(0, 1024)
+    loss = mlp.train(300, batch=1024, lr=2e-3, seed=1)
+    l1, _ = mlp.grad(0, 1024)
+    assert l1 < 0.25 * l0, (l0, l1, loss)
+    mlp.close()
+
+
+def test_correction_keeps_div_b_and_a_zero_network_is_the_identity():
+    s = ics.turbulence(16, seed=2)
+    prm = Params(16, 16, 16, precision=FP32, tau=0.5 * ics.cfl_dt(s))
+    zero = learned.MLP(np.zeros(learned.NPARAM, dtype=np.float32))
+    small = learned.MLP(learned.init_params(3) * 0.1)
+    small.set_norm(np.zeros(8), np.ones(8), np.full(8, 1e-3))
+    with MHDSolver(prm, s) as a, MHDSolver(prm, s) as b, MHDSolver(prm, s) as c:
+        a.step(4)
+        zero.step_corrected(b, 4)
+        _, st = small.step_corrected(c, 4)
+        fa, fb = a.fetch(), b.fetch()
+        dc = c.diagnostics()
+    for k in ("rho", "vx", "p", "bi"):
+        assert np.abs(fa[k] - fb[k]).max() <= 1e-5 * np.abs(fa[k]).max(), k
+    assert st == 0
+    assert dc["divb_max"] <= 1e-4
+    zero.close()
+    small.close()
+
+
+def test_trained_correction_reduces_coarse_error():
+    """Tiny version of the learned-correction study: pairs from two fine 32^3
+    runs, a held-out seed, 8 coarse 16^3 steps.  The corrected coarse run is
+    closer to the restricted fine run than the plain coarse run."""
+    mlp, loss, npairs = learned.train_correction([11, 12], 16, steps=40, every=4, iters=600, batch=4096, lr=2e-3)
+    ev = learned.evaluate(mlp, 21, 16, 8)
+    assert npairs > 0 and np.isfinite(loss)
+    assert ev["corrected_status"] == 0 and ev["corrected_divb"] <= 1e-4
+    assert ev["corrected_l1"] < ev["coarse_l1"], ev
+    mlp.close()
