@@ -486,10 +486,24 @@ __global__ void k_mlp_features(Dev<float> d, MlpNorm nm, __nv_bfloat16* __restri
   for (; f < FIN; ++f) row[f] = __float2bfloat16_rn(0.0f);
 }
 
-// Hydro part of the correction: U += y[0..4] * scale (rho, rho v, energy);
-// a cell whose corrected rho or p would not be positive keeps its state.  The
-// vector-potential part y[5..7] * scale goes to d.dU[5..7] for the face update.
-__global__ void k_mlp_apply_hydro(Dev<float> d, MlpNorm nm, const float* __restrict__ Y) {
+// Domain sums of the hydro increments y[0..4] (for a conservative correction).
+__global__ void k_mlp_sums(const float* __restrict__ Y, long long n, double* sums) {
+  double a[5] = {0, 0, 0, 0, 0};
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+#pragma unroll
+    for (int q = 0; q < 5; ++q) a[q] += (double)Y[t * NOUT + q];
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+    for (int m = 16; m > 0; m >>= 1) a[q] += __shfl_xor_sync(0xffffffffu, a[q], m);
+    if ((threadIdx.x & 31) == 0) atomicAdd(sums + q, a[q]);
+  }
+}
+
+// Hydro part of the correction: U += (y[0..4] - domain mean) * scale (rho,
+// rho v, energy), so mass, momentum and energy are conserved; a cell whose
+// corrected rho or p would not be positive keeps its state.  The vector-
+// potential part y[5..7] * scale goes to d.dU[5..7] for the face update.
+__global__ void k_mlp_apply_hydro(Dev<float> d, MlpNorm nm, const float* __restrict__ Y, const double* sums) {
   const Geom& g = d.g;
   const long long n = (long long)g.nx0 * g.ny0 * g.nz0;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -503,7 +517,7 @@ __global__ void k_mlp_apply_hydro(Dev<float> d, MlpNorm nm, const float* __restr
   const float rho = d.rho[c], u = d.vx[c], v = d.vy[c], w = d.vz[c];
   float U[5] = {rho, rho * u, rho * v, rho * w, 0.5f * rho * (u * u + v * v + w * w) + d.p[c] / gm1};
 #pragma unroll
-  for (int a = 0; a < 5; ++a) U[a] += y[a] * nm.scale[a];
+  for (int a = 0; a < 5; ++a) U[a] += (y[a] - (float)(sums[a] / (double)n)) * nm.scale[a];
   const float rn = U[0];
   const float pn = gm1 * (U[4] - 0.5f * (U[1] * U[1] + U[2] * U[2] + U[3] * U[3]) / rn);
   if (rn > 0.0f && pn > 0.0f) {
@@ -519,19 +533,21 @@ __global__ void k_mlp_apply_hydro(Dev<float> d, MlpNorm nm, const float* __restr
 
 // Magnetic part: face B += curl of the edge vector potential, each edge value
 // the mean of the cell-centred potentials of its 4 cells (periodic wrap), so
-// the face update is divergence-free and div B stays at round-off.
+// the face update is divergence-free and div B stays at round-off.  Covers all
+// n0+1 faces per axis (the top face is the periodic image of the bottom one
+// and gets the same increment).
 __global__ void k_mlp_apply_b(Dev<float> d) {
   const Geom& g = d.g;
-  const long long n = (long long)g.nx0 * g.ny0 * g.nz0;
+  const long long n = (long long)(g.nx0 + 1) * (g.ny0 + 1) * (g.nz0 + 1);
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
-  const int i0 = (int)(t % g.nx0);
-  const long long r = t / g.nx0;
-  const int j0 = (int)(r % g.ny0), k0 = (int)(r / g.ny0);
+  const int i0 = (int)(t % (g.nx0 + 1));
+  const long long r = t / (g.nx0 + 1);
+  const int j0 = (int)(r % (g.ny0 + 1)), k0 = (int)(r / (g.ny0 + 1));
   auto at = [&](int a, int i, int j, int k) -> float {  // interior-periodic cell value of d.dU[5+a]
-    i = (i + g.nx0) % g.nx0;
-    j = (j + g.ny0) % g.ny0;
-    k = (k + g.nz0) % g.nz0;
+    i = (i + 2 * g.nx0) % g.nx0;
+    j = (j + 2 * g.ny0) % g.ny0;
+    k = (k + 2 * g.nz0) % g.nz0;
     return d.dU[5 + a][(long long)(i + g.ng) + (long long)g.px * ((long long)(j + g.ng) + (long long)g.py * (k + g.ng))];
   };
   auto ex = [&](int i, int j, int k) {
@@ -545,10 +561,15 @@ __global__ void k_mlp_apply_b(Dev<float> d) {
   };
   const int i = i0 + g.ng, j = j0 + g.ng, k = k0 + g.ng;
   const long long c = (long long)i + (long long)g.px * ((long long)j + (long long)g.py * k);
-  const float rdx = d.rwx[i], rdy = d.rwy[j], rdz = d.rwz[k];
-  d.bi[c] += (ez(i0, j0 + 1, k0) - ez(i0, j0, k0)) * rdy - (ey(i0, j0, k0 + 1) - ey(i0, j0, k0)) * rdz;
-  d.bj[c] += (ex(i0, j0, k0 + 1) - ex(i0, j0, k0)) * rdz - (ez(i0 + 1, j0, k0) - ez(i0, j0, k0)) * rdx;
-  d.bk[c] += (ey(i0 + 1, j0, k0) - ey(i0, j0, k0)) * rdx - (ex(i0, j0 + 1, k0) - ex(i0, j0, k0)) * rdy;
+  const int iw = i0 % g.nx0, jw = j0 % g.ny0, kw = k0 % g.nz0;  // the periodic face this one images
+  const float rdx = d.rwx[g.ng + iw], rdy = d.rwy[g.ng + jw], rdz = d.rwz[g.ng + kw];
+  const bool in_x = i0 < g.nx0, in_y = j0 < g.ny0, in_z = k0 < g.nz0;
+  if (in_y && in_z)
+    d.bi[c] += (ez(iw, jw + 1, kw) - ez(iw, jw, kw)) * rdy - (ey(iw, jw, kw + 1) - ey(iw, jw, kw)) * rdz;
+  if (in_x && in_z)
+    d.bj[c] += (ex(iw, jw, kw + 1) - ex(iw, jw, kw)) * rdz - (ez(iw + 1, jw, kw) - ez(iw, jw, kw)) * rdx;
+  if (in_x && in_y)
+    d.bk[c] += (ey(iw + 1, jw, kw) - ey(iw, jw, kw)) * rdx - (ex(iw, jw + 1, kw) - ex(iw, jw, kw)) * rdy;
 }
 
 int mfail(int code, const std::string& m) {
@@ -572,6 +593,7 @@ struct Mlp {
   MlpNorm norm{};
   __nv_bfloat16* xs = nullptr;  // correction of a grid: its features
   float* ys = nullptr;          // and the network outputs
+  double* sums = nullptr;       // domain sums of the hydro increments
   size_t cap = 0;
   int sms = 148;
 };
@@ -831,7 +853,7 @@ int mhd_mlp_free(void* h) {
   if (!m) return MHD_OK;
   cudaDeviceSynchronize();
   void* ptrs[] = {m->p, m->g, m->m, m->v, m->w1, m->w2, m->w2t, m->w3, m->w3t, m->X, m->T, m->idx, m->loss, m->err,
-                  m->xs, m->ys};
+                  m->xs, m->ys, m->sums};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete m;
@@ -858,8 +880,12 @@ int mhd::mlp_correct(void* h, Dev<float>& d, cudaStream_t st) {
   k_mlp_features<<<nb, 256, 0, st>>>(d, m->norm, m->xs);
   const int tiles = (int)((n + 127) / 128);
   k_mlp_forward<<<tiles < m->sms ? tiles : m->sms, 128, S_TOTAL, st>>>(m->xs, (int)n, wview(m), m->ys, m->err);
-  k_mlp_apply_hydro<<<nb, 256, 0, st>>>(d, m->norm, m->ys);
-  k_mlp_apply_b<<<nb, 256, 0, st>>>(d);
+  if (!m->sums) MCK(cudaMalloc(&m->sums, 8 * sizeof(double)));
+  MCK(cudaMemsetAsync(m->sums, 0, 8 * sizeof(double), st));
+  k_mlp_sums<<<m->sms * 4, 256, 0, st>>>(m->ys, (long long)n, m->sums);
+  k_mlp_apply_hydro<<<nb, 256, 0, st>>>(d, m->norm, m->ys, m->sums);
+  const long long nf = (long long)(d.g.nx0 + 1) * (d.g.ny0 + 1) * (d.g.nz0 + 1);
+  k_mlp_apply_b<<<(int)((nf + 255) / 256), 256, 0, st>>>(d);
   MCK(cudaGetLastError());
   return MHD_OK;
 }

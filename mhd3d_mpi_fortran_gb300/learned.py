@@ -338,10 +338,30 @@ def init_params(seed: int = 0) -> np.ndarray:
                            np.zeros(16)]).astype(np.float32)
 
 
+def calibrate(mlp: MLP, Us, Ts, mean, std, scale) -> np.ndarray:
+    """Per-output least-squares shrinkage of the trained network on held-out
+    pairs: alpha_q = <y_q, t_q> / <y_q, y_q>, clipped to [0, 1].  An output
+    without skill on unseen data (alpha near 0) is switched off rather than
+    allowed to add error.  Returns alpha; the network's output scales become
+    scale * alpha."""
+    num = np.zeros(8)
+    den = np.zeros(8)
+    for U, T in zip(Us, Ts):
+        y = mlp.forward(features(U, mean, std)).astype(np.float64)
+        t = T.reshape(8, -1, order="F").T / scale
+        num += (y * t).sum(0)
+        den += (y * y).sum(0)
+    alpha = np.clip(num / np.maximum(den, 1e-30), 0.0, 1.0)
+    mlp.set_norm(mean, std, (scale * alpha).astype(np.float32))
+    return alpha
+
+
 def train_correction(train_seeds, n_coarse: int, steps: int, every: int = 10, iters: int = 2000,
-                     batch: int = 16384, lr: float = 1e-3, init_seed: int = 0, nord: int = 8):
-    """Generate pairs from the fine runs of train_seeds, normalise, and train
-    a fresh network; returns (mlp, final minibatch loss, number of pairs)."""
+                     batch: int = 16384, lr: float = 1e-3, init_seed: int = 0, nord: int = 8,
+                     val_seeds=None):
+    """Generate pairs from the fine runs of train_seeds, normalise, train a
+    fresh network and, with val_seeds, calibrate its outputs on their pairs.
+    Returns (mlp, final minibatch loss, number of training pairs, alpha)."""
     Us, Ts = generate(train_seeds, n_coarse, steps, every=every, nord=nord)
     mean, std, scale = normalisation(Us, Ts)
     pairs = build(Us, Ts, mean, std, scale)
@@ -349,4 +369,8 @@ def train_correction(train_seeds, n_coarse: int, steps: int, every: int = 10, it
     mlp.set_norm(mean, std, scale)
     mlp.set_data(pairs.x, pairs.t)
     loss = mlp.train(iters, batch=min(batch, (pairs.x.shape[0] // 128) * 128), lr=lr, seed=init_seed)
-    return mlp, loss, pairs.x.shape[0]
+    alpha = np.ones(8)
+    if val_seeds:
+        Uv, Tv = generate(val_seeds, n_coarse, steps, every=every, nord=nord)
+        alpha = calibrate(mlp, Uv, Tv, mean, std, scale)
+    return mlp, loss, pairs.x.shape[0], alpha

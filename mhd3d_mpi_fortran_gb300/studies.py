@@ -12,6 +12,10 @@ solution here at sizes the oracle cannot reach in reasonable time.
   p = 1/(gam Ms^2), Ms = 0.5, solenoidal k^-2 v and B); PDM, TVD-MC and WENO5
   with RK2; L1/L2 and shell-averaged energy-spectrum error of FP32 against
   FP64, GPU time of both.
+* ``learned``     -- the learned coarse-grid correction: training pairs from
+  fine (2N)^3 turbulence runs, outputs calibrated on a validation seed, then
+  held-out seeds: relative L1 error of the plain and the corrected N^3 runs
+  against the restricted fine run, and the wall time of all three.
 
 ``python -m mhd3d_mpi_fortran_gb300.studies curvilinear|precision [--n N] [--steps K]``
 prints one JSON line per case.
@@ -130,16 +134,44 @@ def precision(n: int = 256, steps: int = 500, recons=(1, 5, 3)) -> list:
     return out
 
 
+def learned_study(n: int = 64, train_seeds=tuple(range(100, 108)), val_seed: int = 108,
+                  test_seeds=(200, 201, 202, 203), steps: int = 100, every: int = 10, iters: int = 4000) -> dict:
+    from . import learned
+    import time
+    t0 = time.perf_counter()
+    mlp, loss, npairs, alpha = learned.train_correction(list(train_seeds), n, steps=2 * steps, every=every,
+                                                        iters=iters, batch=16384, lr=1e-3, val_seeds=[val_seed])
+    t_train = time.perf_counter() - t0
+    rows = []
+    for seed in test_seeds:
+        ev = learned.evaluate(mlp, seed, n, steps)
+        rows.append(ev)
+    mlp.close()
+    agg = {k: float(np.mean([r[k] for r in rows])) for k in ("coarse_l1", "corrected_l1", "fine_s", "coarse_s",
+                                                            "corrected_s")}
+    return {
+        "study": "learned", "workload": f"coarse {n}^3 vs fine {2 * n}^3 decaying turbulence (FP32 RK2 PDM), "
+                                        f"{steps} coarse steps, {len(test_seeds)} held-out seeds",
+        "train": {"seeds": len(train_seeds), "pairs": npairs, "iters": iters, "final_loss": loss,
+                  "alpha": [float(a) for a in alpha], "seconds_incl_data": t_train},
+        "mean": agg, "per_seed": rows,
+        "note": "errors are relative L1 of the conserved variables against the restricted fine run; "
+                "times are host wall clock with the device synchronised",
+    }
+
+
 def main(argv=None) -> None:
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["curvilinear", "precision"])
+    ap.add_argument("study", choices=["curvilinear", "precision", "learned"])
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--recons", default="1,5,3", help="precision study: reconop values (1 PDM, 5 TVD-MC, 3 WENO5)")
     a = ap.parse_args(argv)
     if a.study == "curvilinear":
         print(json.dumps(curvilinear(a.n or 192, a.steps or 200)), flush=True)
+    elif a.study == "learned":
+        print(json.dumps(learned_study(a.n or 64, steps=a.steps or 100)), flush=True)
     else:
         for line in precision(a.n or 256, a.steps or 500, tuple(int(r) for r in a.recons.split(","))):
             print(json.dumps(line), flush=True)

@@ -86,8 +86,9 @@ def test_correction_keeps_div_b_and_a_zero_network_is_the_identity():
     prm = Params(16, 16, 16, precision=FP32, tau=0.5 * ics.cfl_dt(s))
     zero = learned.MLP(np.zeros(learned.NPARAM, dtype=np.float32))
     small = learned.MLP(learned.init_params(3) * 0.1)
-    small.set_norm(np.zeros(8), np.ones(8), np.full(8, 1e-3))
+    small.set_norm(np.zeros(8), np.ones(8), np.full(8, 1e-2))
     with MHDSolver(prm, s) as a, MHDSolver(prm, s) as b, MHDSolver(prm, s) as c:
+        d0 = c.diagnostics()
         a.step(4)
         zero.step_corrected(b, 4)
         _, st = small.step_corrected(c, 4)
@@ -96,16 +97,20 @@ def test_correction_keeps_div_b_and_a_zero_network_is_the_identity():
     for k in ("rho", "vx", "p", "bi"):
         assert np.abs(fa[k] - fb[k]).max() <= 1e-5 * np.abs(fa[k]).max(), k
     assert st == 0
+    # the magnetic correction is a curl (div-free), the hydro one has zero mean
     assert dc["divb_max"] <= 1e-4
+    assert dc["mass"] == pytest.approx(d0["mass"], rel=1e-6)
     zero.close()
     small.close()
 
 
 def test_trained_correction_reduces_coarse_error():
-    """Tiny version of the learned-correction study: pairs from two fine 32^3
-    runs, a held-out seed, 8 coarse 16^3 steps.  The corrected coarse run is
-    closer to the restricted fine run than the plain coarse run."""
-    mlp, loss, npairs = learned.train_correction([11, 12], 16, steps=40, every=4, iters=600, batch=4096, lr=2e-3)
+    """Small version of the learned-correction study: pairs from four fine
+    32^3 runs, outputs calibrated on a fifth, evaluated on a held-out sixth
+    seed over 8 coarse 16^3 steps.  The corrected coarse run is closer to the
+    restricted fine run than the plain coarse run."""
+    mlp, loss, npairs, alpha = learned.train_correction([11, 12, 13, 14], 16, steps=40, every=4, iters=2000,
+                                                        batch=8192, lr=1e-3, val_seeds=[15])
     ev = learned.evaluate(mlp, 21, 16, 8)
     assert npairs > 0 and np.isfinite(loss)
     assert ev["corrected_status"] == 0 and ev["corrected_divb"] <= 1e-4
