@@ -216,27 +216,55 @@ __device__ __forceinline__ void weno_vals(const T* a, const Prm<T>& P, T& fl, T&
   }
 }
 
+// The two halves of pdm2: the left-face value (needs fm2, fm1, f0) and the
+// right-face value (needs fm1, f0, fp1), each with pdm2's exact arithmetic.
+template <typename T>
+__device__ __forceinline__ T pdm_left(T fm2, T fm1, T f0, T fi, T pdmb) {
+  const T fii = mx(mn(fm1, f0), mn(fi, mx(fm1, f0)));
+  const T dfm = pdmb * (fm1 - fm2);
+  const T df0 = pdmb * (f0 - fm1);
+  const T s0 = sgn1(df0);
+  const T qm = fab(sgn1(dfm) + s0);
+  return fii - s0 * mx(T(0), fab(fii - fm1) - qm * fab(dfm));
+}
+template <typename T>
+__device__ __forceinline__ T pdm_right(T fm1, T f0, T fp1, T fi, T pdmb) {
+  const T fii = mx(mn(fm1, f0), mn(fi, mx(fm1, f0)));
+  const T df0 = pdmb * (f0 - fm1);
+  const T dfp = pdmb * (fp1 - f0);
+  const T s0 = sgn1(df0);
+  const T qp = fab(s0 + sgn1(dfp));
+  return fii + s0 * mx(T(0), fab(f0 - fii) - qp * fab(dfp));
+}
+
 // PDM part of get_vav_center2corner (mhd3d3.f90:1901-1905, 2056-2108) for
 // an edge with upper cell c and transverse strides s1 (d1), s2 (d2), given
 // the corner interpolant vi: the four shifted PDM2 limiters, the quadrant
-// choice by the sign of dif and the 4-quadrant mean.  v may point to global
-// or shared memory.
+// choice by the sign of dif and the 4-quadrant mean.  Each quadrant keeps one
+// of its two one-sided estimates, so the dif signs pick the stencil first and
+// only that half-limiter is evaluated (same arithmetic, same bits as
+// evaluating all four pdm2 and selecting).  v may point to global or shared
+// memory.
 template <typename T, typename I>
 __device__ __forceinline__ T corner_pdm(const T* __restrict__ v, I c, I s1, I s2, T vi, T pd) {
-  T v00_0, v00_1, v10_0, v10_1, v01_0, v01_1, v11_0, v11_1;
-  pdm2(v[c - s2 - 2 * s1], v[c - s2 - s1], v[c - s2], v[c - s2 + s1], vi, pd, v00_0, v10_0);
-  pdm2(v[c - s1 - 2 * s2], v[c - s1 - s2], v[c - s1], v[c - s1 + s2], vi, pd, v00_1, v01_1);
-  pdm2(v[c - 2 * s2], v[c - s2], v[c], v[c + s2], vi, pd, v10_1, v11_1);
-  pdm2(v[c - 2 * s1], v[c - s1], v[c], v[c + s1], vi, pd, v01_0, v11_0);
   const I q00 = c - s1 - s2, q10 = c - s2, q01 = c - s1, q11 = c;
-  T d00 = fab(v[q00 - s1] - v[q00]) - fab(v[q00 - s2] - v[q00]);
-  T d10 = fab(v[q10 + s1] - v[q10]) - fab(v[q10 - s2] - v[q10]);
-  T d01 = fab(v[q01 - s1] - v[q01]) - fab(v[q01 + s2] - v[q01]);
-  T d11 = fab(v[q11 + s1] - v[q11]) - fab(v[q11 + s2] - v[q11]);
-  T v00 = d00 >= T(0) ? v00_0 : v00_1;
-  T v10 = d10 >= T(0) ? v10_0 : v10_1;
-  T v01 = d01 >= T(0) ? v01_0 : v01_1;
-  T v11 = d11 >= T(0) ? v11_0 : v11_1;
+  const T d00 = fab(v[q00 - s1] - v[q00]) - fab(v[q00 - s2] - v[q00]);
+  const T d10 = fab(v[q10 + s1] - v[q10]) - fab(v[q10 - s2] - v[q10]);
+  const T d01 = fab(v[q01 - s1] - v[q01]) - fab(v[q01 + s2] - v[q01]);
+  const T d11 = fab(v[q11 + s1] - v[q11]) - fab(v[q11 + s2] - v[q11]);
+  // v00: left value of the s1 line through c-s2 (pdm2 #1) or of the s2 line through c-s1 (#2)
+  const bool b00 = d00 >= T(0);
+  const T v00 = pdm_left(b00 ? v[c - s2 - 2 * s1] : v[c - s1 - 2 * s2], v[c - s1 - s2],
+                         b00 ? v[c - s2] : v[c - s1], vi, pd);
+  // v10: right value of #1 or left value of the s2 line through c (#3)
+  const T v10 = (d10 >= T(0)) ? pdm_right(v[c - s2 - s1], v[c - s2], v[c - s2 + s1], vi, pd)
+                              : pdm_left(v[c - 2 * s2], v[c - s2], v[c], vi, pd);
+  // v01: left value of the s1 line through c (#4) or right value of #2
+  const T v01 = (d01 >= T(0)) ? pdm_left(v[c - 2 * s1], v[c - s1], v[c], vi, pd)
+                              : pdm_right(v[c - s1 - s2], v[c - s1], v[c - s1 + s2], vi, pd);
+  // v11: right value of #4 or of #3
+  const bool b11 = d11 >= T(0);
+  const T v11 = pdm_right(b11 ? v[c - s1] : v[c - s2], v[c], b11 ? v[c + s1] : v[c + s2], vi, pd);
   return T(0.25) * (v00 + v01 + v10 + v11);
 }
 
