@@ -333,21 +333,57 @@ __global__ void __launch_bounds__(128, 1)
   if (q == 0) tc::tmem_free(tb, T_COLS);
 }
 
-// Inference on a row-major BF16 feature matrix: Y[n][8] (raw network outputs).
-__global__ void __launch_bounds__(128, 1)
-    k_mlp_forward(const __nv_bfloat16* __restrict__ X, int n, MlpW w, float* __restrict__ Y, int* err) {
+// shared-memory map of the inference kernel: weights, then one 128 x 256 input
+// tile that the hidden activations reuse once the MMA reading it has finished,
+// so two CTAs fit on an SM and hide each other's MMA / TMEM latency
+constexpr int I_W1 = 0, I_W2 = I_W1 + NH * FIN * 2, I_W3 = I_W2 + NH * NH * 2, I_X = 43008,
+              I_TOTAL = I_X + 128 * FIN * 2;
+static_assert(I_W3 + NO * NH * 2 <= I_X && I_X % 1024 == 0, "inference smem map");
+
+// Features of interior cell t of an FP32 Cartesian grid into row r of an
+// input tile: the 3x3x3 stencil of (rho, rho v, hydro energy, cell B),
+// normalised, feature ((dz+1)*9 + (dy+1)*3 + (dx+1))*8 + var; 216..255 zero.
+__device__ __forceinline__ void gather_row(const Dev<float>& d, const MlpNorm& nm, long long t, unsigned char* tile,
+                                           int r) {
+  const Geom& g = d.g;
+  const int i = (int)(t % g.nx0) + g.ng;
+  const long long q = t / g.nx0;
+  const int j = (int)(q % g.ny0) + g.ng, k = (int)(q / g.ny0) + g.ng;
+  const float gm1 = d.gam - 1.0f;
+  int f = 0;
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const long long c = (long long)(i + dx) + (long long)g.px * ((long long)(j + dy) + (long long)g.py * (k + dz));
+        const float rho = d.rho[c], u = d.vx[c], v = d.vy[c], w = d.vz[c];
+        const float U[8] = {rho, rho * u, rho * v, rho * w, 0.5f * rho * (u * u + v * v + w * w) + d.p[c] / gm1,
+                            d.bx[c], d.by[c], d.bz[c]};
+#pragma unroll
+        for (int a = 0; a < 8; ++a) tc::st_bf16(tile, tc::kmaj(r, f + a, FIN), (U[a] - nm.mean[a]) / nm.std[a]);
+        f += 8;
+      }
+  for (; f < FIN; f += 8) *reinterpret_cast<uint4*>(tile + tc::kmaj(r, f, FIN)) = make_uint4(0, 0, 0, 0);
+}
+
+// Inference: Y[n][8] = raw network outputs.  GRID = false: rows of the BF16
+// feature matrix X; GRID = true: the features of the n interior cells of the
+// grid d, gathered straight into the input tile.
+template <bool GRID>
+__global__ void __launch_bounds__(128, 2)
+    k_mlp_infer(const __nv_bfloat16* __restrict__ X, Dev<float> d, MlpNorm nm, int n, MlpW w, float* __restrict__ Y,
+                int* err) {
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tslot;
   const int tid = threadIdx.x, q = tid >> 5;
   if (q == 0) tc::tmem_alloc(&tslot, 256);
   if (tid == 0) tc::bar_init(&bar, 1);
-  stage_w(sm + S_W1, w.w1, NH, FIN);
-  stage_w(sm + S_W2, w.w2, NH, NH);
-  stage_w(sm + S_W3, w.w3, NO, NH);
+  stage_w(sm + I_W1, w.w1, NH, FIN);
+  stage_w(sm + I_W2, w.w2, NH, NH);
+  stage_w(sm + I_W3, w.w3, NO, NH);
   publish();
   const uint32_t tb = tslot, s0 = tc::smem_u32(sm);
-  unsigned char* R1 = sm + S_R1;
+  unsigned char* XS = sm + I_X;
   uint32_t ph = 0;
   bool ok = true;
   auto sync_mma = [&]() {  // every thread calls it; `ok` ends up the same in all of them
@@ -360,46 +396,53 @@ __global__ void __launch_bounds__(128, 1)
   };
   const int ntiles = (n + 127) / 128;
   for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-    for (int t = tid; t < 128 * (FIN / 8); t += 128) {
-      const int r = t >> 5, c8 = (t & 31) * 8;
-      const int g = tile * 128 + r;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (g < n) v = *reinterpret_cast<const uint4*>(X + (size_t)g * FIN + c8);
-      *reinterpret_cast<uint4*>(R1 + tc::kmaj(r, c8, FIN)) = v;
+    if (GRID) {
+      const long long g = (long long)tile * 128 + tid;
+      if (g < n) gather_row(d, nm, g, XS, tid);
+      else
+        for (int f = 0; f < FIN; f += 8) *reinterpret_cast<uint4*>(XS + tc::kmaj(tid, f, FIN)) = make_uint4(0, 0, 0, 0);
+    } else {
+      for (int t = tid; t < 128 * (FIN / 8); t += 128) {
+        const int r = t >> 5, c8 = (t & 31) * 8;
+        const int g = tile * 128 + r;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (g < n) v = *reinterpret_cast<const uint4*>(X + (size_t)g * FIN + c8);
+        *reinterpret_cast<uint4*>(XS + tc::kmaj(r, c8, FIN)) = v;
+      }
     }
     publish();
-    if (tid == 0) gemm(tb + T_D1, s0 + S_R1, s0 + S_W1, NH, FIN, false);
+    if (tid == 0) gemm(tb + T_D1, s0 + I_X, s0 + I_W1, NH, FIN, false);
     sync_mma();
     if (!ok) break;
-    for (int c0 = 0; c0 < NH; c0 += 16) {
+    for (int c0 = 0; c0 < NH; c0 += 16) {  // H1 over the consumed input tile
       float z[16];
       tc::tmem_ld16(tc::tmem_at(tb + T_D1, q, c0), z);
       for (int i = 0; i < 16; ++i) {
         float dg;
-        tc::st_bf16(sm + S_H1, tc::kmaj(tid, c0 + i, NH), gelu_t(z[i] + w.p[OB1 + c0 + i], dg));
+        tc::st_bf16(XS, tc::kmaj(tid, c0 + i, NH), gelu_t(z[i] + w.p[OB1 + c0 + i], dg));
       }
     }
     publish();
-    if (tid == 0) gemm(tb + T_D2, s0 + S_H1, s0 + S_W2, NH, NH, false);
+    if (tid == 0) gemm(tb + T_D2, s0 + I_X, s0 + I_W2, NH, NH, false);
     sync_mma();
     if (!ok) break;
-    for (int c0 = 0; c0 < NH; c0 += 16) {
+    for (int c0 = 0; c0 < NH; c0 += 16) {  // H2 over H1 (consumed)
       float z[16];
       tc::tmem_ld16(tc::tmem_at(tb + T_D2, q, c0), z);
       for (int i = 0; i < 16; ++i) {
         float dg;
-        tc::st_bf16(sm + S_H2, tc::kmaj(tid, c0 + i, NH), gelu_t(z[i] + w.p[OB2 + c0 + i], dg));
+        tc::st_bf16(XS, tc::kmaj(tid, c0 + i, NH), gelu_t(z[i] + w.p[OB2 + c0 + i], dg));
       }
     }
     publish();
-    if (tid == 0) gemm(tb + T_D3, s0 + S_H2, s0 + S_W3, NO, NH, false);
+    if (tid == 0) gemm(tb + T_D3, s0 + I_X, s0 + I_W3, NO, NH, false);
     sync_mma();
     if (!ok) break;
     float y[16];
     tc::tmem_ld16(tc::tmem_at(tb + T_D3, q, 0), y);
-    const int g = tile * 128 + tid;
+    const long long g = (long long)tile * 128 + tid;
     if (g < n)
-      for (int o = 0; o < NOUT; ++o) Y[(size_t)g * NOUT + o] = y[o] + w.p[OB3 + o];
+      for (int o = 0; o < NOUT; ++o) Y[g * NOUT + o] = y[o] + w.p[OB3 + o];
     __syncthreads();
   }
   if (!ok) {
@@ -458,34 +501,6 @@ __global__ void k_iota(int* idx, int count, long long off) {
 }
 
 // ------------------------------------------------------- solver coupling
-// Features of every interior cell of an FP32 Cartesian grid: the 3x3x3
-// stencil of (rho, rho v, hydro energy, cell B), normalised by (mean, std)
-// per variable, feature ((dz+1)*9 + (dy+1)*3 + (dx+1))*8 + var; 216..255 zero.
-__global__ void k_mlp_features(Dev<float> d, MlpNorm nm, __nv_bfloat16* __restrict__ X) {
-  const Geom& g = d.g;
-  const long long n = (long long)g.nx0 * g.ny0 * g.nz0;
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int i = (int)(t % g.nx0) + g.ng;
-  const long long r = t / g.nx0;
-  const int j = (int)(r % g.ny0) + g.ng, k = (int)(r / g.ny0) + g.ng;
-  const float gm1 = d.gam - 1.0f;
-  __nv_bfloat16* row = X + t * FIN;
-  int f = 0;
-  for (int dz = -1; dz <= 1; ++dz)
-    for (int dy = -1; dy <= 1; ++dy)
-      for (int dx = -1; dx <= 1; ++dx) {
-        const long long c = (long long)(i + dx) + (long long)g.px * ((long long)(j + dy) + (long long)g.py * (k + dz));
-        const float rho = d.rho[c], u = d.vx[c], v = d.vy[c], w = d.vz[c];
-        const float U[8] = {rho, rho * u, rho * v, rho * w, 0.5f * rho * (u * u + v * v + w * w) + d.p[c] / gm1,
-                            d.bx[c], d.by[c], d.bz[c]};
-#pragma unroll
-        for (int a = 0; a < 8; ++a) row[f + a] = __float2bfloat16_rn((U[a] - nm.mean[a]) / nm.std[a]);
-        f += 8;
-      }
-  for (; f < FIN; ++f) row[f] = __float2bfloat16_rn(0.0f);
-}
-
 // Domain sums of the hydro increments y[0..4] (for a conservative correction).
 __global__ void k_mlp_sums(const float* __restrict__ Y, long long n, double* sums) {
   double a[5] = {0, 0, 0, 0, 0};
@@ -591,8 +606,7 @@ struct Mlp {
   int* err = nullptr;
   int step = 0;
   MlpNorm norm{};
-  __nv_bfloat16* xs = nullptr;  // correction of a grid: its features
-  float* ys = nullptr;          // and the network outputs
+  float* ys = nullptr;          // correction of a grid: the network outputs
   double* sums = nullptr;       // domain sums of the hydro increments
   size_t cap = 0;
   int sms = 148;
@@ -631,7 +645,8 @@ int set_smem_once() {
   static bool done = false;
   if (done) return MHD_OK;
   MCK(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, S_TOTAL));
-  MCK(cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, S_TOTAL));
+  MCK(cudaFuncSetAttribute(k_mlp_infer<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, I_TOTAL));
+  MCK(cudaFuncSetAttribute(k_mlp_infer<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, I_TOTAL));
   done = true;
   return MHD_OK;
 }
@@ -839,7 +854,8 @@ int mhd_mlp_forward(void* h, const uint16_t* x, int64_t n, float* y) {
   }
   cudaMemcpy(dx, x, (size_t)n * FIN * 2, cudaMemcpyHostToDevice);
   const int tiles = (int)((n + 127) / 128);
-  k_mlp_forward<<<tiles < m->sms ? tiles : m->sms, 128, S_TOTAL>>>(dx, (int)n, wview(m), dy, m->err);
+  k_mlp_infer<false><<<tiles < 2 * m->sms ? tiles : 2 * m->sms, 128, I_TOTAL>>>(dx, Dev<float>{}, m->norm, (int)n,
+                                                                                 wview(m), dy, m->err);
   cudaError_t e = cudaDeviceSynchronize();
   if (e == cudaSuccess) e = cudaMemcpy(y, dy, (size_t)n * NOUT * 4, cudaMemcpyDeviceToHost);
   cudaFree(dx);
@@ -853,7 +869,7 @@ int mhd_mlp_free(void* h) {
   if (!m) return MHD_OK;
   cudaDeviceSynchronize();
   void* ptrs[] = {m->p, m->g, m->m, m->v, m->w1, m->w2, m->w2t, m->w3, m->w3t, m->X, m->T, m->idx, m->loss, m->err,
-                  m->xs, m->ys, m->sums};
+                  m->ys, m->sums};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete m;
@@ -865,21 +881,18 @@ int mhd::mlp_correct(void* h, Dev<float>& d, cudaStream_t st) {
   Mlp* m = (Mlp*)h;
   const size_t n = (size_t)d.g.nx0 * d.g.ny0 * d.g.nz0;
   if (n > m->cap) {
-    cudaFree(m->xs);
     cudaFree(m->ys);
-    m->xs = nullptr;
     m->ys = nullptr;
     m->cap = 0;
-    MCK(cudaMalloc(&m->xs, n * FIN * 2));
     MCK(cudaMalloc(&m->ys, n * NOUT * 4));
     m->cap = n;
   }
   int rc = set_smem_once();
   if (rc) return rc;
   const int nb = (int)((n + 255) / 256);
-  k_mlp_features<<<nb, 256, 0, st>>>(d, m->norm, m->xs);
   const int tiles = (int)((n + 127) / 128);
-  k_mlp_forward<<<tiles < m->sms ? tiles : m->sms, 128, S_TOTAL, st>>>(m->xs, (int)n, wview(m), m->ys, m->err);
+  k_mlp_infer<true><<<tiles < 2 * m->sms ? tiles : 2 * m->sms, 128, I_TOTAL, st>>>(nullptr, d, m->norm, (int)n, wview(m),
+                                                                                   m->ys, m->err);
   if (!m->sums) MCK(cudaMalloc(&m->sums, 8 * sizeof(double)));
   MCK(cudaMemsetAsync(m->sums, 0, 8 * sizeof(double), st));
   k_mlp_sums<<<m->sms * 4, 256, 0, st>>>(m->ys, (long long)n, m->sums);
