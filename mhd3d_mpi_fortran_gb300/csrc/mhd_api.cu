@@ -25,6 +25,7 @@
 #include <vector>
 #include <atomic>
 #include <map>
+#include <mutex>
 
 #include "../../include/mhd_gpu.h"
 #include "mhd_state.h"
@@ -1200,6 +1201,39 @@ static int capture_ensemble(const std::vector<Handle*>& hs, int nsteps, cudaGrap
   return MHD_OK;
 }
 
+// Cached ensemble graphs, keyed by (grid uid, half) pairs, nsteps and the
+// launch shapes; entries holding a grid are dropped when it is freed.
+struct EnsEntry {
+  cudaGraphExec_t ex = nullptr;
+  std::vector<int> par_end;
+  BatchBufs bufs;
+};
+static std::mutex g_ens_mu;
+static std::map<std::vector<unsigned long long>, EnsEntry> g_ens_cache;
+
+static void ens_release(EnsEntry& en) {
+  if (en.ex) cudaGraphExecDestroy(en.ex);
+  if (en.bufs.tabs) cudaFree(en.bufs.tabs);
+  if (en.bufs.maps) cudaFree(en.bufs.maps);
+  en = EnsEntry{};
+}
+
+// Drop every cached ensemble graph that steps grid `uid`.
+static void ens_forget(unsigned long long uid) {
+  std::lock_guard<std::mutex> lk(g_ens_mu);
+  for (auto it = g_ens_cache.begin(); it != g_ens_cache.end();) {
+    bool has = false;
+    const auto& k = it->first;
+    for (size_t i = 0; i + 2 < k.size(); i += 2) has = has || k[i] == uid;
+    if (has) {
+      ens_release(it->second);
+      it = g_ens_cache.erase(it);
+    } else {
+      ++it;
+    }
+  }
+}
+
 // Ensemble: nsteps steps of every grid in one CUDA graph on the first grid's
 // stream; graphs cached per (grids, their current halves, nsteps, shapes).
 int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* status) {
@@ -1214,12 +1248,7 @@ int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* 
     hs[i] = h;
   }
   Handle* h0 = hs[0];
-  struct Entry {
-    cudaGraphExec_t ex = nullptr;
-    std::vector<int> par_end;
-    BatchBufs bufs;
-  };
-  static thread_local std::map<std::vector<unsigned long long>, Entry> cache;
+  std::lock_guard<std::mutex> lk(g_ens_mu);
   std::vector<unsigned long long> key;
   for (Handle* h : hs) {
     key.push_back(h->uid);
@@ -1227,16 +1256,15 @@ int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* 
   }
   key.push_back((unsigned long long)nsteps);
   key.push_back((unsigned long long)(h0->tile_td * 64 + h0->tile_ey));  // the batch's launch shapes
-  auto it = cache.find(key);
-  if (it == cache.end()) {
-    Entry en;
+  auto it = g_ens_cache.find(key);
+  if (it == g_ens_cache.end()) {
+    EnsEntry en;
     int rc = capture_ensemble(hs, nsteps, &en.ex, en.par_end, en.bufs);
     if (rc) {
-      if (en.bufs.tabs) cudaFree(en.bufs.tabs);
-      if (en.bufs.maps) cudaFree(en.bufs.maps);
+      ens_release(en);
       return rc;
     }
-    it = cache.emplace(key, en).first;
+    it = g_ens_cache.emplace(key, en).first;
   }
   // order the graph after work already queued on every grid's own stream
   for (int i = 1; i < ngrids; ++i) {
@@ -1422,6 +1450,7 @@ int mhd_free(void* handle) {
   Handle* h = (Handle*)handle;
   if (!h) return MHD_OK;
   if (h->st) cudaStreamSynchronize(h->st);
+  ens_forget(h->uid);
   for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second.first);
   for (int i = 0; i < 16; ++i)
     if (h->ev[i]) cudaEventDestroy(h->ev[i]);
