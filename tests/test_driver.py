@@ -1,0 +1,67 @@
+"""Driver loop output formats (CPU) and a short deck run on the GPU."""
+import numpy as np
+import pytest
+
+from mhd3d_mpi_fortran_gb300 import driver, ics
+
+DECK = """
+ &dom
+ xmin=-1., xmax=1., ymin=-1., ymax=1., zmin=-1., zmax=1.
+/
+ &grid
+ nx0G=8, ny0G=8, nz0G=16, xprocs=1, yprocs=1, zprocs=1
+/
+ &comset
+ nord=8, reconop=4, stepop=3, outop=2
+/
+ &list
+ nts=3, tau=0.002, nframes=2, nrst=0, nfdump=10
+/
+ &free
+ cfl=.3, pdmb=4., eps=1.e-8, alpha=2., beta=4.
+/
+"""
+
+
+def test_stime_records_are_fortran_unformatted(tmp_path):
+    path = tmp_path / "stime.out"
+    path.write_bytes(b"".join(driver.fortran_record(np.float64(t).tobytes()) for t in (0.0, 0.25, 0.5)))
+    raw = path.read_bytes()
+    assert len(raw) == 3 * 16 and raw[:4] == (8).to_bytes(4, "little") and raw[12:16] == (8).to_bytes(4, "little")
+    assert np.array_equal(driver.read_stime(path), [0.0, 0.25, 0.5])
+
+
+def test_frames_use_the_hdf5_dataset_layout(tmp_path):
+    s = ics.shock_tube(16, axis=2, ntrans=8)
+    f = {k: getattr(s, k) for k in ("rho", "vx", "vy", "vz", "p")}
+    f.update(bx=s.rho * 2, by=s.rho * 3, bz=s.p * 5)
+    w = driver.FrameWriter(tmp_path, (8, 8, 16), 1, 4)
+    w.write(f, 0.0)
+    w.write(f, 0.1)
+    w.close(2)
+    fr = driver.read_frames(tmp_path)
+    assert fr["rho"].shape == (2, 16, 8, 8)
+    x, y, z = 3, 5, 11
+    assert fr["p"][1, z, y, x] == s.p[4 + x, 4 + y, 4 + z]
+    assert np.array_equal(fr["time"], [0.0, 0.1])
+    assert np.array_equal(driver.read_stime(tmp_path / "stime.out"), [0.0, 0.1])
+
+
+def test_initial_state_is_the_reference_tube():
+    deck = driver.read_deck(DECK)
+    s = driver.initial_state(deck, 8)
+    assert s.rho.shape == (16, 16, 24)
+    assert s.rho[8, 8, 5] == 1.0 and s.rho[8, 8, 20] == 0.125
+
+
+@pytest.mark.gpu
+def test_deck_run_writes_every_frame(tmp_path):
+    out = driver.run(DECK, tmp_path)
+    assert out["frames"] == 3 and out["stopped"] is None
+    fr = driver.read_frames(tmp_path)
+    assert fr["rho"].shape == (3, 16, 8, 8)
+    assert np.allclose(fr["time"], [0.0, 3 * 0.002, 6 * 0.002])
+    assert np.array_equal(driver.read_stime(tmp_path / "stime.out"), fr["time"])
+    s0 = driver.initial_state(driver.read_deck(DECK), 8)
+    assert np.array_equal(fr["rho"][0], s0.rho[4:-4, 4:-4, 4:-4].transpose(2, 1, 0))
+    assert not np.array_equal(fr["rho"][2], fr["rho"][0])
