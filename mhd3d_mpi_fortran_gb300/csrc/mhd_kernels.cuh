@@ -216,33 +216,29 @@ __device__ __forceinline__ void weno_vals(const T* a, const Prm<T>& P, T& fl, T&
   }
 }
 
-// The two halves of pdm2: the left-face value (needs fm2, fm1, f0) and the
-// right-face value (needs fm1, f0, fp1), each with pdm2's exact arithmetic.
+// One half of pdm2 in a single form: the clamp pair (lo, hi) = (fm1, f0), the
+// cell `outer` beyond the near end and the side (left: near = fm1, outer =
+// fm2, result fii - s0*X; right: near = f0, outer = fp1, result fii + s0*X).
+// The difference is formed in pdm2's own operand order for each side, so the
+// result has pdm2's bits; the side is data, not control flow, so lanes that
+// pick different sides do not diverge.
 template <typename T>
-__device__ __forceinline__ T pdm_left(T fm2, T fm1, T f0, T fi, T pdmb) {
-  const T fii = mx(mn(fm1, f0), mn(fi, mx(fm1, f0)));
-  const T dfm = pdmb * (fm1 - fm2);
-  const T df0 = pdmb * (f0 - fm1);
-  const T s0 = sgn1(df0);
-  const T qm = fab(sgn1(dfm) + s0);
-  return fii - s0 * mx(T(0), fab(fii - fm1) - qm * fab(dfm));
-}
-template <typename T>
-__device__ __forceinline__ T pdm_right(T fm1, T f0, T fp1, T fi, T pdmb) {
-  const T fii = mx(mn(fm1, f0), mn(fi, mx(fm1, f0)));
-  const T df0 = pdmb * (f0 - fm1);
-  const T dfp = pdmb * (fp1 - f0);
-  const T s0 = sgn1(df0);
-  const T qp = fab(s0 + sgn1(dfp));
-  return fii + s0 * mx(T(0), fab(f0 - fii) - qp * fab(dfp));
+__device__ __forceinline__ T pdm_half(T lo, T hi, T outer, bool left, T fi, T pdmb) {
+  const T fii = mx(mn(lo, hi), mn(fi, mx(lo, hi)));
+  const T near = left ? lo : hi;
+  const T dn = pdmb * (left ? (lo - outer) : (outer - hi));  // pdm2's dfm / dfp
+  const T s0 = sgn1(pdmb * (hi - lo));
+  const T q = fab(sgn1(dn) + s0);
+  const T x = s0 * mx(T(0), fab(near - fii) - q * fab(dn));
+  return left ? fii - x : fii + x;
 }
 
 // PDM part of get_vav_center2corner (mhd3d3.f90:1901-1905, 2056-2108) for
 // an edge with upper cell c and transverse strides s1 (d1), s2 (d2), given
 // the corner interpolant vi: the four shifted PDM2 limiters, the quadrant
 // choice by the sign of dif and the 4-quadrant mean.  Each quadrant keeps one
-// of its two one-sided estimates, so the dif signs pick the stencil first and
-// only that half-limiter is evaluated (same arithmetic, same bits as
+// of its two one-sided estimates, so the dif signs pick the stencil and the
+// side first and only that half-limiter is evaluated (pdm_half: same bits as
 // evaluating all four pdm2 and selecting).  v may point to global or shared
 // memory.
 template <typename T, typename I>
@@ -252,19 +248,18 @@ __device__ __forceinline__ T corner_pdm(const T* __restrict__ v, I c, I s1, I s2
   const T d10 = fab(v[q10 + s1] - v[q10]) - fab(v[q10 - s2] - v[q10]);
   const T d01 = fab(v[q01 - s1] - v[q01]) - fab(v[q01 + s2] - v[q01]);
   const T d11 = fab(v[q11 + s1] - v[q11]) - fab(v[q11 + s2] - v[q11]);
-  // v00: left value of the s1 line through c-s2 (pdm2 #1) or of the s2 line through c-s1 (#2)
-  const bool b00 = d00 >= T(0);
-  const T v00 = pdm_left(b00 ? v[c - s2 - 2 * s1] : v[c - s1 - 2 * s2], v[c - s1 - s2],
-                         b00 ? v[c - s2] : v[c - s1], vi, pd);
-  // v10: right value of #1 or left value of the s2 line through c (#3)
-  const T v10 = (d10 >= T(0)) ? pdm_right(v[c - s2 - s1], v[c - s2], v[c - s2 + s1], vi, pd)
-                              : pdm_left(v[c - 2 * s2], v[c - s2], v[c], vi, pd);
-  // v01: left value of the s1 line through c (#4) or right value of #2
-  const T v01 = (d01 >= T(0)) ? pdm_left(v[c - 2 * s1], v[c - s1], v[c], vi, pd)
-                              : pdm_right(v[c - s1 - s2], v[c - s1], v[c - s1 + s2], vi, pd);
-  // v11: right value of #4 or of #3
-  const bool b11 = d11 >= T(0);
-  const T v11 = pdm_right(b11 ? v[c - s1] : v[c - s2], v[c], b11 ? v[c + s1] : v[c + s2], vi, pd);
+  // pdm2 #1 on (c-s2-2s1, c-s2-s1, c-s2, c-s2+s1) -> (v00_0, v10_0)
+  // pdm2 #2 on (c-s1-2s2, c-s1-s2, c-s1, c-s1+s2) -> (v00_1, v01_1)
+  // pdm2 #3 on (c-2s2, c-s2, c, c+s2)             -> (v10_1, v11_1)
+  // pdm2 #4 on (c-2s1, c-s1, c, c+s1)             -> (v01_0, v11_0)
+  const bool b00 = d00 >= T(0), b10 = d10 >= T(0), b01 = d01 >= T(0), b11 = d11 >= T(0);
+  const T v00 = pdm_half(v[c - s1 - s2], b00 ? v[c - s2] : v[c - s1], b00 ? v[c - s2 - 2 * s1] : v[c - s1 - 2 * s2],
+                         true, vi, pd);
+  const T v10 = pdm_half(b10 ? v[c - s2 - s1] : v[c - s2], b10 ? v[c - s2] : v[c],
+                         b10 ? v[c - s2 + s1] : v[c - 2 * s2], !b10, vi, pd);
+  const T v01 = pdm_half(b01 ? v[c - s1] : v[c - s1 - s2], b01 ? v[c] : v[c - s1],
+                         b01 ? v[c - 2 * s1] : v[c - s1 + s2], b01, vi, pd);
+  const T v11 = pdm_half(b11 ? v[c - s1] : v[c - s2], v[c], b11 ? v[c + s1] : v[c + s2], false, vi, pd);
   return T(0.25) * (v00 + v01 + v10 + v11);
 }
 
