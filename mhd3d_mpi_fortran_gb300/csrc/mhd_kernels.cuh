@@ -850,7 +850,8 @@ template <> struct FluxMinB<double> { static constexpr int value = 2; };
 
 template <typename T, int TDV = TD>
 __host__ __device__ constexpr size_t flux_t_smem() {
-  return sizeof(T) * ((FLUX_STAGED ? 8 * (TDV + 8) * 32 : 0) + 8 * (TDV + 1) * 32);
+  // [+ staged cells] + face fluxes of the sweep + the x-face fluxes the y kernel reads (8 x TD x 33)
+  return sizeof(T) * ((FLUX_STAGED ? 8 * (TDV + 8) * 32 : 0) + 8 * (TDV + 1) * 32 + 8 * TDV * 33);
 }
 
 template <typename T, int RECON, int D, bool M, bool B, int TDV = TD>
@@ -864,6 +865,7 @@ __global__ void __launch_bounds__(32 * (TDV + 1), FluxMinB<T>::value)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sv = reinterpret_cast<T*>(smem_raw);                      // [8][TROWS][32] cell fields
   T* sF = sv + (FLUX_STAGED ? 8 * TROWS * 32 : 0);             // [8][TD+1][32] face fluxes
+  T* sX = sF + 8 * (TD + 1) * 32;                              // [8][TD][33] x-face fluxes (D == 1)
   const Geom& g = d.g;
   const int tx = threadIdx.x, r = threadIdx.y;
   const int i0 = bb.y * 32 + g.ng;
@@ -875,6 +877,28 @@ __global__ void __launch_bounds__(32 * (TDV + 1), FluxMinB<T>::value)
   const int s = (D == 1) ? g.px : (int)g.plane;
   const int rowbase = (D == 1) ? i0 + g.px * g.py * o : i0 + g.px * o;  // + cd * s
   const T* src[8] = {in.rho, in.vx, in.vy, in.vz, in.p, in.bx, in.by, in.bz};
+  if (D == 1) {
+    // The x-face fluxes of the tile's cells (faces i0 .. i0+32 of rows cd0 ..
+    // cd0+TD-1) are only needed in the epilogue: copy them asynchronously now
+    // so their latency hides behind the reconstructions.
+    const int nthr = 32 * (TD + 1);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {  // static q: the flux pointers stay in registers
+      const T* fq = d.F[0][q];
+      for (int t = r * 32 + tx; t < TD * 33; t += nthr) {
+        const int rr = t / 33, col = t - rr * 33;
+        if (cd0 + rr < g.ng + n0 && i0 + col <= g.ng + g.nx0) {
+          const T* gp = fq + rowbase + col + (cd0 + rr) * s;
+          const uint32_t sp = (uint32_t)__cvta_generic_to_shared(sX + q * TD * 33 + t);
+          if (sizeof(T) == 4)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sp), "l"(gp) : "memory");
+          else
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sp), "l"(gp) : "memory");
+        }
+      }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
   if (FLUX_STAGED) {
     const int nthr = 32 * (TD + 1);
     const bool xok = i0 + tx < g.nx;
@@ -904,6 +928,7 @@ __global__ void __launch_bounds__(32 * (TDV + 1), FluxMinB<T>::value)
 #pragma unroll
     for (int q = 0; q < 8; ++q) sF[(q * (TD + 1) + r) * 32 + tx] = F[q];
   }
+  if (D == 1) asm volatile("cp.async.wait_all;" ::: "memory");
   __syncthreads();
   if (r >= TD || !xin || cd >= g.ng + n0) return;
   const int c = rowbase + tx + cd * s;
@@ -913,13 +938,18 @@ __global__ void __launch_bounds__(32 * (TDV + 1), FluxMinB<T>::value)
   if (D == 1) {
     if (M) {  // area-weighted fluxes: the sum is divided by V after the z term
 #pragma unroll
-      for (int q = 0; q < 8; ++q) d.dU[q][c] = (d.F[0][q][c + 1] - d.F[0][q][c]) + dF[q];
+      for (int q = 0; q < 8; ++q) {
+        const T* x = sX + (q * TD + r) * 33 + tx;
+        d.dU[q][c] = (x[1] - x[0]) + dF[q];
+      }
       return;
     }
     const T dx = d.wx[i], dy = d.wy[cd], rdx = d.rwx[i], rdy = d.rwy[cd];
 #pragma unroll
-    for (int q = 0; q < 8; ++q)
-      d.dU[q][c] = Ops<T>::dw(d.F[0][q][c + 1] - d.F[0][q][c], dx, rdx) + Ops<T>::dw(dF[q], dy, rdy);
+    for (int q = 0; q < 8; ++q) {
+      const T* x = sX + (q * TD + r) * 33 + tx;
+      d.dU[q][c] = Ops<T>::dw(x[1] - x[0], dx, rdx) + Ops<T>::dw(dF[q], dy, rdy);
+    }
     return;
   }
   const T tau = (T)d.sc->tau;
