@@ -850,10 +850,8 @@ template <> struct FluxMinB<double> { static constexpr int value = 2; };
 
 template <typename T, int TDV = TD>
 __host__ __device__ constexpr size_t flux_t_smem() {
-  // [+ staged cells] + face fluxes of the sweep + the epilogue operands copied
-  // ahead: the y kernel's x-face fluxes (8 x TD x 33) or the z kernel's x+y
-  // divergence and RK level U^n (13 x TD x 32)
-  return sizeof(T) * ((FLUX_STAGED ? 8 * (TDV + 8) * 32 : 0) + 8 * (TDV + 1) * 32 + 13 * TDV * 32);
+  // [+ staged cells] + face fluxes of the sweep + the x-face fluxes the y kernel reads (8 x TD x 33)
+  return sizeof(T) * ((FLUX_STAGED ? 8 * (TDV + 8) * 32 : 0) + 8 * (TDV + 1) * 32 + 8 * TDV * 33);
 }
 
 template <typename T, int RECON, int D, bool M, bool B, int TDV = TD>
@@ -867,7 +865,7 @@ __global__ void __launch_bounds__(32 * (TDV + 1), FluxMinB<T>::value)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sv = reinterpret_cast<T*>(smem_raw);                      // [8][TROWS][32] cell fields
   T* sF = sv + (FLUX_STAGED ? 8 * TROWS * 32 : 0);             // [8][TD+1][32] face fluxes
-  T* sX = sF + 8 * (TD + 1) * 32;  // D == 1: [8][TD][33] x-face fluxes; D == 2: [13][TD][32] dU, U^n
+  T* sX = sF + 8 * (TD + 1) * 32;                              // [8][TD][33] x-face fluxes (D == 1)
   const Geom& g = d.g;
   const int tx = threadIdx.x, r = threadIdx.y;
   const int i0 = bb.y * 32 + g.ng;
@@ -892,29 +890,6 @@ __global__ void __launch_bounds__(32 * (TDV + 1), FluxMinB<T>::value)
         if (cd0 + rr < g.ng + n0 && i0 + col <= g.ng + g.nx0) {
           const T* gp = fq + rowbase + col + (cd0 + rr) * s;
           const uint32_t sp = (uint32_t)__cvta_generic_to_shared(sX + q * TD * 33 + t);
-          if (sizeof(T) == 4)
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sp), "l"(gp) : "memory");
-          else
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sp), "l"(gp) : "memory");
-        }
-      }
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
-  }
-  if (D == 2) {
-    // the x+y divergence of the tile's cells and, for a stage combine, the RK
-    // level U^n: copied ahead like the y kernel's x fluxes
-    const int nthr = 32 * (TD + 1);
-    const int nq = (form >= 0) ? 13 : 8;
-#pragma unroll
-    for (int q = 0; q < 13; ++q) {
-      if (q >= nq) break;
-      const T* fq = (q < 8) ? d.dU[q] : d.q[q - 8];
-      for (int t = r * 32 + tx; t < TD * 32; t += nthr) {
-        const int rr = t >> 5, col = t & 31;
-        if (cd0 + rr < g.ng + n0 && i0 + col < g.ng + g.nx0) {
-          const T* gp = fq + rowbase + col + (cd0 + rr) * s;
-          const uint32_t sp = (uint32_t)__cvta_generic_to_shared(sX + q * TD * 32 + t);
           if (sizeof(T) == 4)
             asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sp), "l"(gp) : "memory");
           else
@@ -953,7 +928,7 @@ __global__ void __launch_bounds__(32 * (TDV + 1), FluxMinB<T>::value)
 #pragma unroll
     for (int q = 0; q < 8; ++q) sF[(q * (TD + 1) + r) * 32 + tx] = F[q];
   }
-  asm volatile("cp.async.wait_all;" ::: "memory");
+  if (D == 1) asm volatile("cp.async.wait_all;" ::: "memory");
   __syncthreads();
   if (r >= TD || !xin || cd >= g.ng + n0) return;
   const int c = rowbase + tx + cd * s;
@@ -980,15 +955,14 @@ __global__ void __launch_bounds__(32 * (TDV + 1), FluxMinB<T>::value)
   const T tau = (T)d.sc->tau;
   const T gm1 = d.gam - T(1);
   T dv[8];
-  const T* sz = sX + r * 32 + tx;  // this cell's staged operands, stride TD*32
   if (M) {
     const T V = (T)d.m.vol[c], rV = (T)d.m.rvol[c];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) dv[q] = Ops<T>::dw(sz[q * TD * 32] + dF[q], V, rV);
+    for (int q = 0; q < 8; ++q) dv[q] = Ops<T>::dw(d.dU[q][c] + dF[q], V, rV);
   } else {
     const T dz = d.wz[cd], rdz = d.rwz[cd];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) dv[q] = sz[q * TD * 32] + Ops<T>::dw(dF[q], dz, rdz);
+    for (int q = 0; q < 8; ++q) dv[q] = d.dU[q][c] + Ops<T>::dw(dF[q], dz, rdz);
   }
   // get_conserve of the current state (AB: the state, not the prediction)
   T rr = d.rho[c], u = d.vx[c], v = d.vy[c], ww = d.vz[c], pr = d.p[c];
@@ -998,13 +972,12 @@ __global__ void __launch_bounds__(32 * (TDV + 1), FluxMinB<T>::value)
   T eng1 = eng0 - tau * dv[4];
   T rx = rvx0 - tau * dv[1], ry = rvy0 - tau * dv[2], rz = rvz0 - tau * dv[3];
   T hx = rx, hy = ry, hz = rz;
-  const T* sq = sz + 8 * TD * 32;  // staged U^n {rho, rvx, rvy, rvz, eng}
   if (form >= 0) {
-    rho1 = comb(form, cw, sq[0], rho1, den);
-    hx = comb(form, cw, sq[TD * 32], rx, den);
-    hy = comb(form, cw, sq[2 * TD * 32], ry, den);
-    hz = comb(form, cw, sq[3 * TD * 32], rz, den);
-    eng1 = comb(form, cw, sq[4 * TD * 32], eng1, den);
+    rho1 = comb(form, cw, d.q[0][c], rho1, den);
+    hx = comb(form, cw, d.q[1][c], rx, den);
+    hy = comb(form, cw, d.q[2][c], ry, den);
+    hz = comb(form, cw, d.q[3][c], rz, den);
+    eng1 = comb(form, cw, d.q[4][c], eng1, den);
   }
   const T rrho = Ops<T>::rcp(rho1);
   T pn = gm1 * (eng1 - Ops<T>::dvr(T(0.5) * (hx * hx + hy * hy + hz * hz), rho1, rrho));
@@ -1012,9 +985,9 @@ __global__ void __launch_bounds__(32 * (TDV + 1), FluxMinB<T>::value)
   ry = ry - tau * dv[6];
   rz = rz - tau * dv[7];
   if (form >= 0) {
-    rx = comb(form, cw, sq[TD * 32], rx, den);
-    ry = comb(form, cw, sq[2 * TD * 32], ry, den);
-    rz = comb(form, cw, sq[3 * TD * 32], rz, den);
+    rx = comb(form, cw, d.q[1][c], rx, den);
+    ry = comb(form, cw, d.q[2][c], ry, den);
+    rz = comb(form, cw, d.q[3][c], rz, den);
   }
   d.orho[c] = rho1;
   d.op[c] = pn;
