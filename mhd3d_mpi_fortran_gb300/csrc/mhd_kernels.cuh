@@ -1069,52 +1069,40 @@ __global__ void __launch_bounds__(NT) k_emf_pdm(KArg<T, B> ka, Inp<T> in0, Prm<T
   const T* vel[3] = {in.vx, in.vy, in.vz};
   const T* v1 = vel[A1];
   const T* v2 = vel[A2];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  // stage v_a1, v_a2: warps over (y, z) rows, lanes over x
-  for (int row = warp; row < SY * SZ; row += nwarp) {
+  // stage v_a1, v_a2: one flat pass over the (x, y, z) tile, x fastest, so
+  // every lane has an element even when a row is not a multiple of 32 wide
+  for (int t = threadIdx.x; t < NV; t += blockDim.x) {
+    const int lx = t % SX, row = t / SX;
     const int ly = row % SY, lz = row / SY;
-    const int gy = oy - HY + ly, gz = oz - HZ + lz;
-    const bool rowok = gy < g.ny && gz < g.nz;
-    const int gb = g.px * (gy + g.py * gz) + ox - HX;
-#pragma unroll
-    for (int xx = 0; xx < SX; xx += 32) {
-      const int lx = xx + lane;
-      if (lx < SX) {
-        T a = T(0), b = T(0);
-        if (rowok && ox - HX + lx < g.nx) {
-          a = v1[gb + lx];
-          b = v2[gb + lx];
-        }
-        sv[row * SX + lx] = a;
-        sv[NV + row * SX + lx] = b;
-      }
+    const int gx = ox - HX + lx, gy = oy - HY + ly, gz = oz - HZ + lz;
+    T a = T(0), b = T(0);
+    if (gx < g.nx && gy < g.ny && gz < g.nz) {
+      const int gi = gx + g.px * (gy + g.py * gz);
+      a = v1[gi];
+      b = v2[gi];
     }
+    sv[t] = a;
+    sv[NV + t] = b;
   }
   __syncthreads();
-  // first pass of interp2_pdm: lanes over the x-mapped index of (e, f1, r2)
+  // first pass of interp2_pdm over (e, f1, r2), flat with the x-mapped index fastest
   constexpr int NX = (E == 0) ? TE : (A1 == 0) ? T1 : R2;   // x-mapped extent
-  constexpr int NR = NG / NX;                                // remaining (row) extent
-  for (int row = warp; row < NR; row += nwarp) {
+  for (int t = threadIdx.x; t < NG; t += blockDim.x) {
+    const int ix = t % NX, row = t / NX;
+    int e, f1, r2;
+    if (E == 0) {
+      e = ix; f1 = row % T1; r2 = row / T1;
+    } else if (A1 == 0) {
+      f1 = ix; e = row % TE; r2 = row / TE;
+    } else {
+      r2 = ix; e = row % TE; f1 = row / TE;
+    }
+    const int b0 = e * SE + f1 * S1 + r2 * S2;
+    const int gi = e * GE + f1 * G1 + r2 * G2;
 #pragma unroll
-    for (int xx = 0; xx < NX; xx += 32) {
-      const int ix = xx + lane;
-      if (ix < NX) {
-        int e, f1, r2;
-        if (E == 0) {
-          e = ix; f1 = row % T1; r2 = row / T1;
-        } else if (A1 == 0) {
-          f1 = ix; e = row % TE; r2 = row / TE;
-        } else {
-          r2 = ix; e = row % TE; f1 = row / TE;
-        }
-        const int b0 = e * SE + f1 * S1 + r2 * S2;
-        const int gi = e * GE + f1 * G1 + r2 * G2;
-#pragma unroll
-        for (int w = 0; w < 2; ++w) {
-          const T* a = sv + w * NV + b0;
-          sg[w * NG + gi] = tap8(a[0], a[S1], a[2 * S1], a[3 * S1], a[4 * S1], a[5 * S1], a[6 * S1], a[7 * S1]);
-        }
-      }
+    for (int w = 0; w < 2; ++w) {
+      const T* a = sv + w * NV + b0;
+      sg[w * NG + gi] = tap8(a[0], a[S1], a[2 * S1], a[3 * S1], a[4 * S1], a[5 * S1], a[6 * S1], a[7 * S1]);
     }
   }
   __syncthreads();
