@@ -1040,11 +1040,43 @@ __global__ void k_emf(Dev<T> d, Inp<T> in, Prm<T> P) {
 // into shared memory, and each edge then takes the second pass along a2, the
 // limiters (corner_pdm), the upwinded face-B reconstructions and the Alfven
 // resistivity term exactly as k_emf does.  Tile (TX, TY, TZ) in edges.
-template <typename T, int E, int TX, int TY, int TZ, int NT, bool M, bool B>
-__global__ void __launch_bounds__(NT) k_emf_pdm(KArg<T, B> ka, Inp<T> in0, Prm<T> P) {
-  const int4 bb = ka.blk();
-  const auto& d = ka.dev(bb);
-  const Inp<T> in = B ? state_view(d) : in0;
+//
+// A transverse axis of an edge family holds n0 + 1 edges.  For ej and ek,
+// when that count is one more than a multiple of the tile (n0 a multiple of
+// 32 along x, of 8 along the other transverse axis), the last tile of the
+// axis is one edge wider instead of a block of its own holding a single edge
+// row: emf_edge_tiles() counts the tiles, and k_emf_pdm runs the widened
+// variant of emf_pdm_tile in those blocks.  ei keeps the plain count (its
+// halo-padded tile is large, so a wider variant would cost shared memory and
+// occupancy in every block).
+constexpr bool emf_merges(int E, int axis) { return E != 0 && axis != E; }
+
+__host__ __device__ constexpr int emf_edge_tiles(int ext, int t, bool merge) {
+  return (merge && t > 1 && ext > t && ext % t == 1) ? ext / t : (ext + t - 1) / t;
+}
+
+// dynamic shared memory of k_emf_pdm: enough for the widest tile it runs
+template <typename T, int E, int TX, int TY, int TZ>
+constexpr size_t emf_pdm_smem() {
+  constexpr int WX = TX + emf_merges(E, 0), WY = TY + emf_merges(E, 1), WZ = TZ + emf_merges(E, 2);
+  constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
+  constexpr int HX = (E == 0) ? 0 : 4, HY = (E == 1) ? 0 : 4, HZ = (E == 2) ? 0 : 4;
+  constexpr int NV = (WX + 2 * HX) * (WY + 2 * HY) * (WZ + 2 * HZ);
+  constexpr int TE = (E == 0) ? WX : (E == 1) ? WY : WZ;
+  constexpr int T1 = (A1 == 0) ? WX : (A1 == 1) ? WY : WZ;
+  constexpr int T2 = (A2 == 0) ? WX : (A2 == 1) ? WY : WZ;
+  return sizeof(T) * (2 * NV + 2 * TE * T1 * (T2 + 8));
+}
+
+inline dim3 emf_grid(int E, const Geom& g, int tx, int ty, int tz) {
+  const int ex = g.nx0 + (E != 0), ey = g.ny0 + (E != 1), ez = g.nz0 + (E != 2);
+  return dim3(emf_edge_tiles(ex, tx, emf_merges(E, 0)), emf_edge_tiles(ey, ty, emf_merges(E, 1)),
+              emf_edge_tiles(ez, tz, emf_merges(E, 2)));
+}
+
+template <typename T, int E, int TX, int TY, int TZ, bool M>
+__device__ __forceinline__ void emf_pdm_tile(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, int ox, int oy,
+                                             int oz) {
   constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
   constexpr int HX = (E == 0) ? 0 : 4, HY = (E == 1) ? 0 : 4, HZ = (E == 2) ? 0 : 4;
   constexpr int SX = TX + 2 * HX, SY = TY + 2 * HY, SZ = TZ + 2 * HZ;
@@ -1065,7 +1097,6 @@ __global__ void __launch_bounds__(NT) k_emf_pdm(KArg<T, B> ka, Inp<T> in0, Prm<T
   T* sv = reinterpret_cast<T*>(smem_raw);  // [2][NV]: v_a1, v_a2
   T* sg = sv + 2 * NV;                     // [2][NG]: first-pass interpolants
   const Geom& g = d.g;
-  const int ox = g.ng + bb.y * TX, oy = g.ng + bb.z * TY, oz = g.ng + bb.w * TZ;
   const T* vel[3] = {in.vx, in.vy, in.vz};
   const T* v1 = vel[A1];
   const T* v2 = vel[A2];
@@ -1145,26 +1176,45 @@ __global__ void __launch_bounds__(NT) k_emf_pdm(KArg<T, B> ka, Inp<T> in0, Prm<T
   }
 }
 
+template <typename T, int E, int TX, int TY, int TZ, int NT, bool M, bool B>
+__global__ void __launch_bounds__(NT) k_emf_pdm(KArg<T, B> ka, Inp<T> in0, Prm<T> P) {
+  const int4 bb = ka.blk();
+  const auto& d = ka.dev(bb);
+  const Inp<T> in = B ? state_view(d) : in0;
+  const Geom& g = d.g;
+  const int ox = g.ng + bb.y * TX, oy = g.ng + bb.z * TY, oz = g.ng + bb.w * TZ;
+  if constexpr (E == 0) {
+    emf_pdm_tile<T, E, TX, TY, TZ, M>(d, in, P, ox, oy, oz);
+  } else {
+    // transverse axes a1, a2: is this block the widened last tile of the axis?
+    constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
+    const int n0[3] = {g.nx0, g.ny0, g.nz0};
+    const int org[3] = {ox - g.ng, oy - g.ng, oz - g.ng};
+    constexpr int tl[3] = {TX, TY, TZ};
+    const bool w1 = tl[A1] > 1 && n0[A1] - org[A1] == tl[A1];
+    const bool w2 = tl[A2] > 1 && n0[A2] - org[A2] == tl[A2];
+    constexpr int X1 = A1 == 0, Y1 = A1 == 1, Z1 = A1 == 2, X2 = A2 == 0, Y2 = A2 == 1, Z2 = A2 == 2;
+    if (w1 && w2)
+      emf_pdm_tile<T, E, TX + X1 + X2, TY + Y1 + Y2, TZ + Z1 + Z2, M>(d, in, P, ox, oy, oz);
+    else if (w1)
+      emf_pdm_tile<T, E, TX + X1, TY + Y1, TZ + Z1, M>(d, in, P, ox, oy, oz);
+    else if (w2)
+      emf_pdm_tile<T, E, TX + X2, TY + Y2, TZ + Z2, M>(d, in, P, ox, oy, oz);
+    else
+      emf_pdm_tile<T, E, TX, TY, TZ, M>(d, in, P, ox, oy, oz);
+  }
+}
+
 template <typename T, int E, int TX, int TY, int TZ, int NT, bool M>
 void launch_emf_pdm(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStream_t st) {
-  constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
-  constexpr int HX = (E == 0) ? 0 : 4, HY = (E == 1) ? 0 : 4, HZ = (E == 2) ? 0 : 4;
-  constexpr int NV = (TX + 2 * HX) * (TY + 2 * HY) * (TZ + 2 * HZ);
-  constexpr int TE = (E == 0) ? TX : (E == 1) ? TY : TZ;
-  constexpr int T1 = (A1 == 0) ? TX : (A1 == 1) ? TY : TZ;
-  constexpr int T2 = (A2 == 0) ? TX : (A2 == 1) ? TY : TZ;
-  constexpr int NG = TE * T1 * (T2 + 8);
-  constexpr size_t bytes = sizeof(T) * (2 * NV + 2 * NG);
+  constexpr size_t bytes = emf_pdm_smem<T, E, TX, TY, TZ>();
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_emf_pdm<T, E, TX, TY, TZ, NT, M, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)bytes);
     attr = true;
   }
-  const Geom& g = d.g;
-  const int ex = g.nx0 + (E != 0), ey = g.ny0 + (E != 1), ez = g.nz0 + (E != 2);
-  dim3 grid((ex + TX - 1) / TX, (ey + TY - 1) / TY, (ez + TZ - 1) / TZ);
-  k_emf_pdm<T, E, TX, TY, TZ, NT, M, false><<<grid, NT, bytes, st>>>(one(d), in, P);
+  k_emf_pdm<T, E, TX, TY, TZ, NT, M, false><<<emf_grid(E, d.g, TX, TY, TZ), NT, bytes, st>>>(one(d), in, P);
 }
 
 // Metric-mode EMF inputs of a stage: w^a = v . nbar_a at every cell and the
@@ -1675,21 +1725,6 @@ void Launch<T, M>::fill(const Dev<T>& d, cudaStream_t st) {
 }
 
 // ------------------------------------------------------------ batched ensemble
-template <typename T, int E, int TX, int TY, int TZ>
-constexpr size_t emf_pdm_smem() {
-  constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
-  constexpr int HX = (E == 0) ? 0 : 4, HY = (E == 1) ? 0 : 4, HZ = (E == 2) ? 0 : 4;
-  constexpr int NV = (TX + 2 * HX) * (TY + 2 * HY) * (TZ + 2 * HZ);
-  constexpr int TE = (E == 0) ? TX : (E == 1) ? TY : TZ;
-  constexpr int T1 = (A1 == 0) ? TX : (A1 == 1) ? TY : TZ;
-  constexpr int T2 = (A2 == 0) ? TX : (A2 == 1) ? TY : TZ;
-  return sizeof(T) * (2 * NV + 2 * TE * T1 * (T2 + 8));
-}
-
-inline dim3 tiles(int ex, int ey, int ez, int tx, int ty, int tz) {
-  return dim3((ex + tx - 1) / tx, (ey + ty - 1) / ty, (ez + tz - 1) / tz);
-}
-
 template <typename T>
 dim3 Batch<T>::dims(int fam, const Geom& g, int td, int ey) {
   const int Y = std::is_same<T, float>::value ? ey : EiTile<T>::Y;
@@ -1699,9 +1734,9 @@ dim3 Batch<T>::dims(int fam, const Geom& g, int td, int ey) {
     case BF_FLUX_X: return dim3(((g.nx0 + 1) * g.ny0 * g.nz0 + 127) / 128, 1, 1);
     case BF_FLUX_Y: return dim3((g.nx0 + 31) / 32, (g.ny0 + td - 1) / td, g.nz0);
     case BF_FLUX_Z: return dim3((g.nx0 + 31) / 32, (g.nz0 + td - 1) / td, g.ny0);
-    case BF_EMF_I: return tiles(g.nx0, g.ny0 + 1, g.nz0 + 1, 32, Y, Y);
-    case BF_EMF_J: return tiles(g.nx0 + 1, g.ny0, g.nz0 + 1, 32, 1, 8);
-    case BF_EMF_K: return tiles(g.nx0 + 1, g.ny0 + 1, g.nz0, 32, 8, 1);
+    case BF_EMF_I: return emf_grid(0, g, 32, Y, Y);
+    case BF_EMF_J: return emf_grid(1, g, 32, 1, 8);
+    case BF_EMF_K: return emf_grid(2, g, 32, 8, 1);
     case BF_CT: return grid3(g.nx0 + 1, g.ny0 + 1, g.nz0 + 1, dim3(32, 4, 1));
     default: return grid3(g.nx + 1, g.ny + 1, g.nz + 1, dim3(64, 4, 1));  // BF_FILL
   }

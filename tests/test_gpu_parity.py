@@ -70,6 +70,20 @@ def test_emf_fp64_match_oracle(recon, shift):
         assert relmax(eg[e], eo[e]) <= 1e-13, e
 
 
+@pytest.mark.parametrize("shape", [(32, 8, 16), (64, 17, 9), (33, 16, 8)])
+def test_emf_widened_last_tiles_fp64(shape):
+    """PDM ej / ek tiles: a transverse axis with n0 + 1 = 32 q + 1 (x) or
+    8 q + 1 (the other transverse axis) edges ends in a tile one edge wider
+    instead of a block holding one edge row; every edge still matches."""
+    s = rand_state(*shape, seed=sum(shape))
+    prm = Params(*shape, reconop=1, tau=1e-3)
+    with MHDSolver(prm, s) as gpu:
+        eg = gpu.debug_emf()
+    eo = OracleSolver(prm, s).emf()
+    for e in range(3):
+        assert relmax(eg[e], eo[e]) <= 1e-13, e
+
+
 @pytest.mark.parametrize("recon", RECONS)
 @pytest.mark.parametrize("stepop", [STEP_AB2, STEP_RK2, STEP_RK3])
 def test_steps_fp64_match_oracle(recon, stepop):
@@ -230,7 +244,7 @@ def test_batched_ensemble_equals_sequential(prec, stepop):
     grid's result is bit-identical to stepping it alone, over two calls (the
     second replays the cached graph) and with grids starting on different
     halves of their double-buffered state."""
-    sizes = (16, 24, 8, 12)
+    sizes = (16, 24, 8, 12, 32)
     states = [ics.orszag_tang_3d(n, seed=i, amp=0.5 + 0.3 * i, ny0=n + 2 * (i % 2)) for i, n in enumerate(sizes)]
     prms = [Params(n, n + 2 * (i % 2), n, precision=prec, stepop=stepop, tau=0.4 * ics.cfl_dt(st))
             for i, (n, st) in enumerate(zip(sizes, states))]
