@@ -102,17 +102,19 @@ __device__ __forceinline__ void pdm2(T fm2, T fm1, T f0, T fp1, T fi, T pdmb, T&
 
 // TVD (mhd3d3.f90:1238-1248): van Leer b = (a+|a|)/(1+|a|); MC variant
 // b = max(0, min(2a, (1+a)/2, 2)) (fi is the centred value, so b is phi(a)).
+// Quotients: Ops<T>::dv divides exactly in FP64 (the reference's rounding)
+// and multiplies by the hardware reciprocal in FP32.
 template <typename T, bool MC>
 __device__ __forceinline__ T tvdb(T a) {
   if (MC) return mx(T(0), mn(mn(T(2) * a, T(0.5) * (T(1) + a)), T(2)));
-  return (a + fab(a)) / (T(1) + fab(a));
+  return Ops<T>::dv(a + fab(a), T(1) + fab(a));
 }
 template <typename T, bool MC>
 __device__ __forceinline__ void tvd(T fm2, T fm1, T f0, T fp1, T fi, T eps, T& fl, T& fr) {
-  T a = (fm1 - fm2) / (f0 - fm1 + eps);
+  T a = Ops<T>::dv(fm1 - fm2, f0 - fm1 + eps);
   T b = tvdb<T, MC>(a);
   fl = fm1 - b * (fm1 - fi);
-  a = (f0 - fp1) / (fm1 - f0 + eps);
+  a = Ops<T>::dv(f0 - fp1, fm1 - f0 + eps);
   b = tvdb<T, MC>(a);
   fr = f0 - b * (f0 - fi);
 }
@@ -130,11 +132,11 @@ __device__ __forceinline__ void weno5(T fm3, T fm2, T fm1, T f0, T fp1, T fp2, T
   T s1 = c13 * (t * t) + T(0.25) * (u * u);
   t = fm1 - T(2) * f0 + fp1; u = T(3) * fm1 - T(4) * f0 + fp1;
   T s2 = c13 * (t * t) + T(0.25) * (u * u);
-  s0 = T(0.1) / ((eps + s0) * (eps + s0));
-  s1 = T(0.6) / ((eps + s1) * (eps + s1));
-  s2 = T(0.3) / ((eps + s2) * (eps + s2));
+  s0 = Ops<T>::dv(T(0.1), (eps + s0) * (eps + s0));
+  s1 = Ops<T>::dv(T(0.6), (eps + s1) * (eps + s1));
+  s2 = Ops<T>::dv(T(0.3), (eps + s2) * (eps + s2));
   T sum = s0 + s1 + s2;
-  fl = (s0 / sum) * h0 + (s1 / sum) * h1 + (s2 / sum) * h2;
+  fl = Ops<T>::dv(s0, sum) * h0 + Ops<T>::dv(s1, sum) * h1 + Ops<T>::dv(s2, sum) * h2;
   h0 = Div<T>::by(T(2) * fp2 - T(7) * fp1 + T(11) * f0, T(6));
   h1 = Div<T>::by(-fp1 + T(5) * f0 + T(2) * fm1, T(6));
   h2 = Div<T>::by(T(2) * f0 + T(5) * fm1 - fm2, T(6));
@@ -144,11 +146,11 @@ __device__ __forceinline__ void weno5(T fm3, T fm2, T fm1, T f0, T fp1, T fp2, T
   s1 = c13 * (t * t) + T(0.25) * (u * u);
   t = f0 - T(2) * fm1 + fm2; u = T(3) * f0 - T(4) * fm1 + fm2;
   s2 = c13 * (t * t) + T(0.25) * (u * u);
-  s0 = T(0.1) / ((eps + s0) * (eps + s0));
-  s1 = T(0.6) / ((eps + s1) * (eps + s1));
-  s2 = T(0.3) / ((eps + s2) * (eps + s2));
+  s0 = Ops<T>::dv(T(0.1), (eps + s0) * (eps + s0));
+  s1 = Ops<T>::dv(T(0.6), (eps + s1) * (eps + s1));
+  s2 = Ops<T>::dv(T(0.3), (eps + s2) * (eps + s2));
   sum = s0 + s1 + s2;
-  fr = (s0 / sum) * h0 + (s1 / sum) * h1 + (s2 / sum) * h2;
+  fr = Ops<T>::dv(s0, sum) * h0 + Ops<T>::dv(s1, sum) * h1 + Ops<T>::dv(s2, sum) * h2;
 }
 
 // minmod / median (mhd3d3.f90:1380-1403)
@@ -1217,6 +1219,202 @@ void launch_emf_pdm(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStre
   k_emf_pdm<T, E, TX, TY, TZ, NT, M, false><<<emf_grid(E, d.g, TX, TY, TZ), NT, bytes, st>>>(one(d), in, P);
 }
 
+// ------------------------------------------------------------- WENO EMF
+// Shared-memory tiled EMF of family E for WENO5 / MP-WENO5.  The corner
+// velocity of get_vav_center2corner (mhd3d3.f90:1925-2049) reconstructs six
+// rows of cells along d1 and then the six row results along d2 ("_1"), and
+// six columns along d2 and then along d1 ("_0").  Neighbouring edges share
+// five of the six rows, so a block stages v_a1 and v_a2 of its tile of edges
+// with the stencil halo (3 cells below and 2 above on each transverse axis),
+// computes every row and column reconstruction of the tile once into shared
+// memory (first pass), and each edge then takes its four second-pass
+// reconstructions, the dif-sign quadrant choice and the 4-quadrant mean of
+// corner_vel, the upwinded face-B reconstructions and the resistivity term
+// of k_emf, with the same operands in the same order.
+
+// An (e, a1, a2) array of edge family E with the x-mapped index fastest, so
+// that lanes of a warp touch consecutive words.
+template <int E, int DE, int D1, int D2>
+struct EdgeLay {
+  static constexpr int A1 = (E + 1) % 3;
+  static constexpr int N = DE * D1 * D2;
+  static constexpr int NX = (E == 0) ? DE : (A1 == 0) ? D1 : D2;
+  static constexpr int GE = (E == 0) ? 1 : (A1 == 0) ? D1 : D2;
+  static constexpr int G1 = (E == 0) ? DE : (A1 == 0) ? 1 : D2 * DE;
+  static constexpr int G2 = (E == 0) ? DE * D1 : (A1 == 0) ? D1 * DE : 1;
+  // coordinates of flat index t (t == e * GE + f1 * G1 + f2 * G2)
+  __device__ static __forceinline__ void coords(int t, int& e, int& f1, int& f2) {
+    const int ix = t % NX, row = t / NX;
+    if (E == 0) {
+      e = ix; f1 = row % D1; f2 = row / D1;
+    } else if (A1 == 0) {
+      f1 = ix; e = row % DE; f2 = row / DE;
+    } else {
+      f2 = ix; e = row % DE; f1 = row / DE;
+    }
+  }
+};
+
+template <typename T, int E, int TX, int TY, int TZ>
+struct EmfWeno {
+  static constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
+  // staged cells: the edge axis without halo, each transverse axis [-3, T+2)
+  static constexpr int LX = (E == 0) ? 0 : 3, LY = (E == 1) ? 0 : 3, LZ = (E == 2) ? 0 : 3;
+  static constexpr int SX = TX + ((E == 0) ? 0 : 5), SY = TY + ((E == 1) ? 0 : 5), SZ = TZ + ((E == 2) ? 0 : 5);
+  static constexpr int NV = SX * SY * SZ;
+  static constexpr int SE = (E == 0) ? 1 : (E == 1) ? SX : SX * SY;
+  static constexpr int S1 = (A1 == 0) ? 1 : (A1 == 1) ? SX : SX * SY;
+  static constexpr int S2 = (A2 == 0) ? 1 : (A2 == 1) ? SX : SX * SY;
+  static constexpr int TE = (E == 0) ? TX : (E == 1) ? TY : TZ;
+  static constexpr int T1 = (A1 == 0) ? TX : (A1 == 1) ? TY : TZ;
+  static constexpr int T2 = (A2 == 0) ? TX : (A2 == 1) ? TY : TZ;
+  typedef EdgeLay<E, TE, T1, T2 + 5> L1;  // "_1": rows [-3, T2+2) reconstructed along a1 at the a1 faces
+  typedef EdgeLay<E, TE, T1 + 5, T2> L0;  // "_0": columns [-3, T1+2) reconstructed along a2 at the a2 faces
+  static constexpr int NP = L1::N + L0::N;
+  // sv[2][NV] (v_a1, v_a2), then per component: L1, R1 [L1::N], L0, R0 [L0::N]
+  static constexpr size_t smem = sizeof(T) * (2 * NV + 4 * NP);
+};
+
+template <typename T, int RECON, int E, int TX, int TY, int TZ, int NT, bool M>
+__global__ void __launch_bounds__(NT) k_emf_weno(Dev<T> d, Inp<T> in, Prm<T> P) {
+  typedef EmfWeno<T, E, TX, TY, TZ> K;
+  typedef typename K::L1 L1;
+  typedef typename K::L0 L0;
+  constexpr int A1 = K::A1, A2 = K::A2, NV = K::NV, NP = K::NP, N1 = L1::N, N0 = L0::N;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sv = reinterpret_cast<T*>(smem_raw);
+  T* sp = sv + 2 * NV;
+  const Geom& g = d.g;
+  const int ox = g.ng + blockIdx.x * TX, oy = g.ng + blockIdx.y * TY, oz = g.ng + blockIdx.z * TZ;
+  const T* vel[3] = {in.vx, in.vy, in.vz};
+  const T* v1 = vel[A1];
+  const T* v2 = vel[A2];
+  for (int t = threadIdx.x; t < NV; t += blockDim.x) {
+    const int lx = t % K::SX, row = t / K::SX;
+    const int ly = row % K::SY, lz = row / K::SY;
+    const int gx = ox - K::LX + lx, gy = oy - K::LY + ly, gz = oz - K::LZ + lz;
+    T a = T(0), b = T(0);
+    if (gx < g.nx && gy < g.ny && gz < g.nz) {
+      const int gi = gx + g.px * (gy + g.py * gz);
+      a = v1[gi];
+      b = v2[gi];
+    }
+    sv[t] = a;
+    sv[NV + t] = b;
+  }
+  __syncthreads();
+  // first pass: every row ("_1") and column ("_0") reconstruction of the
+  // tile for both components; tap q of an entry is the cell at offset q - 3
+  for (int t = threadIdx.x; t < 2 * NP; t += blockDim.x) {
+    const int w = t >= NP;
+    const int u = t - w * NP;
+    const T* src = sv + w * NV;
+    T* dst = sp + w * 2 * NP;
+    int e, f1, f2, base, step, o1, o2;
+    if (u < N1) {  // row f2 - 3 along a2, reconstructed along a1 at the face of cell f1
+      L1::coords(u, e, f1, f2);
+      base = e * K::SE + f1 * K::S1 + f2 * K::S2;
+      step = K::S1;
+      o1 = u;
+      o2 = N1 + u;
+    } else {  // column f1 - 3 along a1, reconstructed along a2 at the face of cell f2
+      L0::coords(u - N1, e, f1, f2);
+      base = e * K::SE + f1 * K::S1 + f2 * K::S2;
+      step = K::S2;
+      o1 = 2 * N1 + (u - N1);
+      o2 = 2 * N1 + N0 + (u - N1);
+    }
+    T a[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) a[q] = src[base + q * step];
+    T fl, fr;
+    weno_vals<T, RECON>(a, P, fl, fr);
+    dst[o1] = fl;
+    dst[o2] = fr;
+  }
+  __syncthreads();
+  const int lim[3] = {g.ng + g.nx0 + (E != 0), g.ng + g.ny0 + (E != 1), g.ng + g.nz0 + (E != 2)};
+  const int st[3] = {1, g.px, (int)g.plane};
+  const T* fb[3] = {in.bi, in.bj, in.bk};
+  for (int t = threadIdx.x; t < TX * TY * TZ; t += blockDim.x) {
+    const int lx = t % TX, r = t / TX, ly = r % TY, lz = r / TY;
+    const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
+    if (gx >= lim[0] || gy >= lim[1] || gz >= lim[2]) continue;
+    const int e = (E == 0) ? lx : (E == 1) ? ly : lz;
+    const int f1 = (A1 == 0) ? lx : (A1 == 1) ? ly : lz;
+    const int f2 = (A2 == 0) ? lx : (A2 == 1) ? ly : lz;
+    T v1av = T(0), v2av = T(0);
+#pragma unroll 1
+    for (int w = 0; w < 2; ++w) {
+      const T* s = sp + w * 2 * NP;
+      T a[6], v00_0, v00_1, v10_0, v10_1, v01_0, v01_1, v11_0, v11_1;
+      const T* l1 = s + e * L1::GE + f1 * L1::G1 + f2 * L1::G2;  // rows f2 - 3 + m at m * G2
+#pragma unroll
+      for (int m = 0; m < 6; ++m) a[m] = l1[m * L1::G2];
+      weno_vals<T, RECON>(a, P, v00_1, v01_1);
+#pragma unroll
+      for (int m = 0; m < 6; ++m) a[m] = l1[N1 + m * L1::G2];
+      weno_vals<T, RECON>(a, P, v10_1, v11_1);
+      const T* l0 = s + 2 * N1 + e * L0::GE + f1 * L0::G1 + f2 * L0::G2;  // columns f1 - 3 + m
+#pragma unroll
+      for (int m = 0; m < 6; ++m) a[m] = l0[m * L0::G1];
+      weno_vals<T, RECON>(a, P, v00_0, v01_0);
+#pragma unroll
+      for (int m = 0; m < 6; ++m) a[m] = l0[N0 + m * L0::G1];
+      weno_vals<T, RECON>(a, P, v10_0, v11_0);
+      // dif signs pick the smoother one-sided estimate per quadrant (2056-2106)
+      const T* v = sv + w * NV;
+      const int c = e * K::SE + (f1 + 3) * K::S1 + (f2 + 3) * K::S2;
+      constexpr int s1 = K::S1, s2 = K::S2;
+      const int q00 = c - s1 - s2, q10 = c - s2, q01 = c - s1, q11 = c;
+      const T d00 = fab(v[q00 - s1] - v[q00]) - fab(v[q00 - s2] - v[q00]);
+      const T d10 = fab(v[q10 + s1] - v[q10]) - fab(v[q10 - s2] - v[q10]);
+      const T d01 = fab(v[q01 - s1] - v[q01]) - fab(v[q01 + s2] - v[q01]);
+      const T d11 = fab(v[q11 + s1] - v[q11]) - fab(v[q11 + s2] - v[q11]);
+      const T v00 = d00 >= T(0) ? v00_0 : v00_1;
+      const T v10 = d10 >= T(0) ? v10_0 : v10_1;
+      const T v01 = d01 >= T(0) ? v01_0 : v01_1;
+      const T v11 = d11 >= T(0) ? v11_0 : v11_1;
+      const T vc = T(0.25) * (v00 + v01 + v10 + v11);
+      if (w == 0)
+        v1av = vc;
+      else
+        v2av = vc;
+    }
+    const int c = gx + g.px * (gy + g.py * gz);
+    const int s1 = st[A1], s2 = st[A2];
+    T b1l, b1r, b2l, b2r;
+    recon_face<T, RECON>(fb[A1], c, s2, P, b1l, b1r);
+    recon_face<T, RECON>(fb[A2], c, s1, P, b2l, b2r);
+    T b1u = (v2av >= T(0)) ? b1l : b1r;
+    T b2u = (v1av >= T(0)) ? b2l : b2r;
+    T ee = -v1av * b2u + v2av * b1u;
+    const T* vf = d.vf;
+    T eta = T(0.25) * (vf[c - s1 - s2] + vf[c - s2] + vf[c] + vf[c - s1]);
+    if (M)
+      ee = (T)d.m.ge[E][c] * ee + eta * (T)d.m.dl[E][c] * (b1l + b2r - b1r - b2l);
+    else
+      ee = ee + eta * (b1l + b2r - b1r - b2l);
+    d.E[E][c] = ee;
+  }
+}
+
+template <typename T, int RECON, int E, int TX, int TY, int TZ, int NT, bool M>
+void launch_emf_weno(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStream_t st) {
+  constexpr size_t bytes = EmfWeno<T, E, TX, TY, TZ>::smem;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_emf_weno<T, RECON, E, TX, TY, TZ, NT, M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)bytes);
+    attr = true;
+  }
+  const Geom& g = d.g;
+  const int ex = g.nx0 + (E != 0), ey = g.ny0 + (E != 1), ez = g.nz0 + (E != 2);
+  const dim3 grid((ex + TX - 1) / TX, (ey + TY - 1) / TY, (ez + TZ - 1) / TZ);
+  k_emf_weno<T, RECON, E, TX, TY, TZ, NT, M><<<grid, NT, bytes, st>>>(d, in, P);
+}
+
+
 // Metric-mode EMF inputs of a stage: w^a = v . nbar_a at every cell and the
 // face-normal field b_a = Phi_a / |A_a| at every face (ghosts included),
 // which the EMF kernels then treat as the reference treats v and bi/bj/bk.
@@ -1665,6 +1863,16 @@ void Launch<T, M>::hydro(const Dev<T>& d, const Inp<T>& in, int part, int form, 
   }
 }
 
+// ei tiles of 32 (FP32) or 16 (FP64) edges x 4 x 4; ej, ek plane tiles of 32 x 8.
+template <typename T, int RECON, bool M>
+void emf_weno(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
+  const Prm<T> P = prm_of(d);
+  constexpr int EX = std::is_same<T, float>::value ? 32 : 16;
+  launch_emf_weno<T, RECON, 0, EX, 4, 4, EX * 16, M>(d, in, P, st);
+  launch_emf_weno<T, RECON, 1, 32, 1, 8, 256, M>(d, in, P, st);
+  launch_emf_weno<T, RECON, 2, 32, 8, 1, 256, M>(d, in, P, st);
+}
+
 template <typename T, int RECON, bool M>
 void emf_r(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
   Prm<T> P = prm_of(d);
@@ -1705,8 +1913,8 @@ void Launch<T, M>::emf(const Dev<T>& d, const Inp<T>& in0, cudaStream_t st) {
   }
   switch (d.recon) {
     case R_TVD: emf_r<T, R_TVD, M>(d, in, st); break;
-    case R_WENO: emf_r<T, R_WENO, M>(d, in, st); break;
-    case R_MPWENO: emf_r<T, R_MPWENO, M>(d, in, st); break;
+    case R_WENO: emf_weno<T, R_WENO, M>(d, in, st); break;
+    case R_MPWENO: emf_weno<T, R_MPWENO, M>(d, in, st); break;
     default: emf_r<T, R_TVDMC, M>(d, in, st); break;
   }
 }

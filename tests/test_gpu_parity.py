@@ -70,13 +70,16 @@ def test_emf_fp64_match_oracle(recon, shift):
         assert relmax(eg[e], eo[e]) <= 1e-13, e
 
 
+@pytest.mark.parametrize("recon", [1, 3, 4])
 @pytest.mark.parametrize("shape", [(32, 8, 16), (64, 17, 9), (33, 16, 8)])
-def test_emf_widened_last_tiles_fp64(shape):
-    """PDM ej / ek tiles: a transverse axis with n0 + 1 = 32 q + 1 (x) or
-    8 q + 1 (the other transverse axis) edges ends in a tile one edge wider
-    instead of a block holding one edge row; every edge still matches."""
+def test_emf_multi_tile_fp64(shape, recon):
+    """Shared-memory EMF tiles over several blocks per axis.  PDM ej / ek: a
+    transverse axis with n0 + 1 = 32 q + 1 (x) or 8 q + 1 (the other
+    transverse axis) edges ends in a tile one edge wider instead of a block
+    holding one edge row.  WENO5 / MP-WENO5: row and column reconstructions
+    shared through shared memory.  Every edge matches the oracle."""
     s = rand_state(*shape, seed=sum(shape))
-    prm = Params(*shape, reconop=1, tau=1e-3)
+    prm = Params(*shape, reconop=recon, tau=1e-3)
     with MHDSolver(prm, s) as gpu:
         eg = gpu.debug_emf()
     eo = OracleSolver(prm, s).emf()
@@ -154,12 +157,15 @@ def test_whole_step_parity_64cubed_100_steps():
     assert dg["divb_max"] <= 1e-12
 
 
-def test_fp32_error_budget_vs_fp64():
+@pytest.mark.parametrize("recon", RECONS)
+def test_fp32_error_budget_vs_fp64(recon):
+    """FP32 production path (fast reciprocal quotients, fitted erfc) against
+    the all-FP64 mode for every reconstruction."""
     s = ics.orszag_tang_3d(32, seed=0)
     tau = ics.cfl_dt(s)
     res = {}
     for prec in (FP64, FP32):
-        with MHDSolver(Params(32, 32, 32, precision=prec, tau=tau), s) as gpu:
+        with MHDSolver(Params(32, 32, 32, reconop=recon, precision=prec, tau=tau), s) as gpu:
             gpu.step(20)
             res[prec] = gpu.fetch()
             if prec == FP32:
