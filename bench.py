@@ -55,9 +55,45 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="short run for ncu (no JSON extras)")
+    ap.add_argument("--tiles", default=None,
+                    help="launch shapes 'face_tile,ei_tile' (e.g. 8,8) instead of the autotuner's choice")
     ap.add_argument("--ensemble", type=int, default=0,
                     help="batched-ensemble mode: this many periodic OT grids of sizes {32,48,64,96}^3")
     return ap.parse_args()
+
+
+def roofs(zu_per_gpu: float, clocks: dict, recon: int, tiles) -> dict:
+    """FP32 and instruction-issue rooflines of the whole step from per
+    zone-update counts that ncu measured on the same kernels (FP32 flops =
+    fadd + fmul + 2 ffma thread instructions; thread instructions issued),
+    profiles/counts_pdm_rk2_fp32.json.  Peaks: SMs x 128 FP32 lanes x 2 flop
+    and SMs x 4 schedulers x 32 lanes per cycle, at the median SM clock seen
+    during the timed region."""
+    cf = ROOT / "profiles" / "counts_pdm_rk2_fp32.json"
+    if recon != 1 or not cf.exists():
+        return {}
+    counts = json.loads(cf.read_text())
+    key = f"td{tiles[0]}_ei{tiles[1]}"
+    if key not in counts["per_zone_update"]:
+        return {}
+    c = counts["per_zone_update"][key]
+    from mhd3d_mpi_fortran_gb300 import abi
+    import ctypes as C
+    info = (C.c_int32 * 4)()
+    if abi.load().mhd_device_info(info) != 0:
+        return {}
+    sms, mhz = info[0], clocks.get("sm_mhz") or info[3]
+    fp32_peak = sms * 128 * 2 * mhz * 1e6
+    issue_peak = sms * 4 * 32 * mhz * 1e6
+    return {
+        "fp32_roof": {"flop_per_zone_update": c["flop"], "achieved_tflops": zu_per_gpu * c["flop"] / 1e12,
+                      "peak_tflops": fp32_peak / 1e12, "frac": zu_per_gpu * c["flop"] / fp32_peak,
+                      "peak_kind": f"nominal: {sms} SMs x 128 lanes x 2 flop x {mhz:.0f} MHz"},
+        "issue_roof": {"inst_per_zone_update": c["inst"], "achieved_tinst_s": zu_per_gpu * c["inst"] / 1e12,
+                       "peak_tinst_s": issue_peak / 1e12, "frac": zu_per_gpu * c["inst"] / issue_peak,
+                       "peak_kind": f"nominal: {sms} SMs x 4 x 32 thread instructions x {mhz:.0f} MHz",
+                       "counts_from": counts["source"]},
+    }
 
 
 def dist_env():
@@ -198,7 +234,11 @@ def run_ours(a):
     solver = MHDSolver(prm, s)
     # launch shapes: the autotuner times its compiled variants on this grid
     # (state untouched, results bit-identical), outside the timed region
-    tiles = solver.autotune(reps=5)
+    if a.tiles:
+        tiles = tuple(int(t) for t in a.tiles.split(","))
+        solver.set_tiles(*tiles)
+    else:
+        tiles = solver.autotune(reps=5)
     # warm-up (>= 3 steps), then the timed region
     solver.time_steps(max(3, a.warmup), graph=graph)
     if a.profile_only:
@@ -259,6 +299,7 @@ def run_ours(a):
                "sample": f"8 RK2 steps of the 160^3 turbulence state (same generator), PDM, FP64 oracle, {dt:.1f} s"}
     if rank != 0:
         return
+    compute_roofs = roofs(zu / ws, clocks, a.recon, tiles)
     launches_per_step = 2 + 2 * (3 + 3 + 1 + 1)
     line = {
         "metric": "zone-updates/s", "value": zu, "unit": "zone-updates/s", "n_gpus": ws,
@@ -275,6 +316,7 @@ def run_ours(a):
         "hbm_roofline_160B": {"achieved_gbs": zu * 160 / 1e9 / ws, "peak": hbm, "frac": zu * 160 / 1e9 / ws / hbm,
                               "note": "compulsory 160 B per FP32 RK2 zone-update"},
         "family_ms_per_stage": fam_ms,
+        **compute_roofs,
         "gpu_launches": launches_per_step * a.steps,
         "clocks": clocks,
         "status": st,

@@ -157,6 +157,10 @@ int mhd_free(void* handle);
 /* Human-readable text of the last error on this thread. */
 const char* mhd_last_error(void);
 
+/* Device 0's SM count, compute capability (major, minor) and maximum SM clock
+ * in MHz, for roofline denominators (no reference counterpart). */
+int mhd_device_info(int32_t out[4]);
+
 /* ---- checkpoint / restart (no counterpart in the reference, which only
  * plans one: mhd3d3.f90:16, 63, 88) ------------------------------------
  * mhd_checkpoint_save writes everything a step depends on: the parameter
@@ -236,6 +240,13 @@ int mhd_autotune(void* handle, int32_t reps, int32_t out[2]);
 /* The same for a batched ensemble: times the batched launches over all grids
  * and gives every grid the fastest shapes. */
 int mhd_ensemble_autotune(void** handles, int32_t ngrids, int32_t reps, int32_t out[2]);
+
+/* Sets the launch shapes directly (no timing): face-tile length 4, 8 or 16
+ * and ei EMF tile 4 or 8, for a reproducible configuration (profiling, or
+ * shapes found by an earlier mhd_autotune).  Handles outside the tunable
+ * path (FP64, metric mode, other reconstructions) accept only their fixed
+ * shapes.  Every choice gives bit-identical steps. */
+int mhd_set_tiles(void* handle, int32_t face_tile, int32_t ei_tile);
 
 /* ---- learned coarse-grid correction (BF16 tcgen05) ---------------------- */
 

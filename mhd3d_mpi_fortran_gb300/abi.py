@@ -24,10 +24,10 @@ E_OK, E_ARG, E_CUDA, E_NOMEM, E_TIMEOUT, E_STATE = 0, -1, -2, -3, -4, -5
 
 EXPORTS = (
     "mhd_init", "mhd_init_mapped", "mhd_step", "mhd_step_n", "mhd_fetch", "mhd_diagnostics", "mhd_step_graph",
-    "mhd_set_tau", "mhd_set_profiling", "mhd_last_timings", "mhd_free", "mhd_last_error",
+    "mhd_set_tau", "mhd_set_profiling", "mhd_last_timings", "mhd_free", "mhd_last_error", "mhd_device_info",
     "mhd_debug_fluxes", "mhd_debug_emf", "mhd_ensemble_step", "mhd_time_steps",
     "mhd_diagnostics_noalloc", "mhd_checkpoint_save", "mhd_checkpoint_load",
-    "mhd_autotune", "mhd_ensemble_autotune", "mhd_tc_gemm_test",
+    "mhd_autotune", "mhd_ensemble_autotune", "mhd_set_tiles", "mhd_tc_gemm_test",
     "mhd_mlp_create", "mhd_mlp_params", "mhd_mlp_set_norm", "mhd_mlp_set_data", "mhd_mlp_grad", "mhd_mlp_train",
     "mhd_mlp_forward", "mhd_mlp_apply", "mhd_step_corrected", "mhd_mlp_free",
 )
@@ -120,12 +120,14 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.mhd_last_timings.argtypes = [vp, C.POINTER(C.c_float)]
     lib.mhd_free.argtypes = [vp]
     lib.mhd_last_error.restype = C.c_char_p
+    lib.mhd_device_info.argtypes = [C.POINTER(C.c_int32)]
     lib.mhd_debug_fluxes.argtypes = [vp, dp]
     lib.mhd_debug_emf.argtypes = [vp, dp, dp, dp]
     lib.mhd_time_steps.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_float)]
     lib.mhd_ensemble_step.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.POINTER(C.c_uint32)]
     lib.mhd_checkpoint_save.argtypes = [vp, C.c_char_p]
     lib.mhd_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
+    lib.mhd_set_tiles.argtypes = [vp, C.c_int32, C.c_int32]
     lib.mhd_tc_gemm_test.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
     fp = C.POINTER(C.c_float)
     lib.mhd_mlp_create.argtypes = [C.c_void_p, C.POINTER(vp)]

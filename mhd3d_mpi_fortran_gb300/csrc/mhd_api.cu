@@ -491,6 +491,17 @@ std::vector<int> mhd::ghost_maps(int nx0, int ny0, int nz0, int ng, const int bc
 
 const char* mhd_last_error(void) { return g_err.c_str(); }
 
+int mhd_device_info(int32_t out[4]) {
+  if (!out) return fail(MHD_E_ARG, "null output");
+  int v[4] = {0, 0, 0, 0};
+  CK(cudaDeviceGetAttribute(&v[0], cudaDevAttrMultiProcessorCount, 0));
+  CK(cudaDeviceGetAttribute(&v[1], cudaDevAttrComputeCapabilityMajor, 0));
+  CK(cudaDeviceGetAttribute(&v[2], cudaDevAttrComputeCapabilityMinor, 0));
+  CK(cudaDeviceGetAttribute(&v[3], cudaDevAttrClockRate, 0));  // kHz
+  out[0] = v[0]; out[1] = v[1]; out[2] = v[2]; out[3] = v[3] / 1000;
+  return MHD_OK;
+}
+
 // Handle with its device buffers allocated and cleared, scalars set from prm,
 // but no fields uploaded yet.
 static int create_handle(const mhd_params* prm, const double* dx, const double* dy, const double* dz,
@@ -1359,6 +1370,27 @@ int mhd_autotune(void* handle, int32_t reps, int32_t out[2]) {
     CK(cudaGetLastError());
   }
   if (out) { out[0] = h->tile_td; out[1] = h->tile_ey; }
+  return MHD_OK;
+}
+
+int mhd_set_tiles(void* handle, int32_t face_tile, int32_t ei_tile) {
+  Handle* h = (Handle*)handle;
+  if (!h) return fail(MHD_E_ARG, "null handle");
+  if (!tunable(h)) {
+    if (face_tile != h->tile_td || ei_tile != h->tile_ey)
+      return fail(MHD_E_ARG, "this handle's launch shapes are fixed");
+    return MHD_OK;
+  }
+  bool ok_td = false, ok_ey = false;
+  for (int td : kTileTD) ok_td |= td == face_tile;
+  for (int ey : kTileEY) ok_ey |= ey == ei_tile;
+  if (!ok_td || !ok_ey) return fail(MHD_E_ARG, "face tile must be 4, 8 or 16 and ei tile 4 or 8");
+  int rc = wait_stream(h);
+  if (rc) return rc;
+  h->tile_td = face_tile;
+  h->tile_ey = ei_tile;
+  carve<float>(h, h->df, (char*)h->buf);
+  drop_graphs(h);
   return MHD_OK;
 }
 

@@ -91,6 +91,10 @@ class MHDSolver:
         check(self.lib, self.lib.mhd_autotune(self.h, int(reps), out), "mhd_autotune")
         return out[0], out[1]
 
+    def set_tiles(self, face_tile: int, ei_tile: int):
+        """Set the launch shapes directly (mhd_set_tiles)."""
+        check(self.lib, self.lib.mhd_set_tiles(self.h, int(face_tile), int(ei_tile)), "mhd_set_tiles")
+
     def save(self, path: str):
         """Checkpoint everything a step depends on (mhd_checkpoint_save)."""
         check(self.lib, self.lib.mhd_checkpoint_save(self.h, str(path).encode()), "mhd_checkpoint_save")

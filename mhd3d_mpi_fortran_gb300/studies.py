@@ -12,12 +12,14 @@ solution here at sizes the oracle cannot reach in reasonable time.
   p = 1/(gam Ms^2), Ms = 0.5, solenoidal k^-2 v and B); PDM, TVD-MC and WENO5
   with RK2; L1/L2 and shell-averaged energy-spectrum error of FP32 against
   FP64, GPU time of both.
+* ``equal_time``  -- error against the FP64 n^3 solve at comparable GPU time:
+  FP32 at n^3 and (n/2)^3, FP64 at (n/2)^3 and (n/4)^3, same physical time.
 * ``learned``     -- the learned coarse-grid correction: training pairs from
   fine (2N)^3 turbulence runs, outputs calibrated on a validation seed, then
   held-out seeds: relative L1 error of the plain and the corrected N^3 runs
   against the restricted fine run, and the wall time of all three.
 
-``python -m mhd3d_mpi_fortran_gb300.studies curvilinear|precision [--n N] [--steps K]``
+``python -m mhd3d_mpi_fortran_gb300.studies curvilinear|precision|equal_time|learned [--n N] [--steps K]``
 prints one JSON line per case.
 """
 from __future__ import annotations
@@ -134,6 +136,49 @@ def precision(n: int = 256, steps: int = 500, recons=(1, 5, 3)) -> list:
     return out
 
 
+def coarsen(f: dict, n: int, times: int, nord: int = 8) -> dict:
+    """The state restricted `times` times by 2 (conservative 2x2x2 cell means,
+    face B as the mean of the covering fine faces), as a field dict."""
+    from .learned import restrict, state_dict
+    for _ in range(times):
+        f = state_dict(restrict(f, n, nord))
+        n //= 2
+    return f
+
+
+def equal_time(n: int = 256, steps: int = 100, recon: int = 1) -> dict:
+    """Relative L1 error against the FP64 n^3 solve, with the GPU time of each
+    run: FP32 at n^3 and (n/2)^3, FP64 at (n/2)^3 and (n/4)^3.  Every run starts
+    from the n^3 initial state restricted to its grid and covers the same
+    physical time (the step doubles with each halving of the resolution), so
+    the error of a coarse run is measured against the reference restricted to
+    its grid.  FP64 runs about 45x slower per zone-update than FP32 on this
+    part, so FP32 n^3 sits between the two FP64 runs in GPU time."""
+    from .learned import l1_error, state_dict
+    s = ics.turbulence(n, seed=0)
+    tau = 0.8 * ics.cfl_dt(s, cfl=0.3)
+    f0 = state_dict(s)
+    ref_ms, ref, _ = _run(Params(n, n, n, reconop=recon, stepop=STEP_RK2, precision=FP64, tau=tau), s, steps)
+    rows = [{"precision": "fp64", "n": n, "steps": steps, "gpu_ms": ref_ms, "l1_vs_fp64_ref": 0.0}]
+    for prec, level in ((FP32, 0), (FP32, 1), (FP64, 1), (FP64, 2)):
+        m = n >> level
+        init = coarsen(f0, n, level)
+        st = ics.empty_state(ics.grid(m, m, m, nord=8))
+        for k in ("rho", "vx", "vy", "vz", "p", "bi", "bj", "bk"):
+            getattr(st, k)[...] = init[k]
+        prm = Params(m, m, m, reconop=recon, stepop=STEP_RK2, precision=prec, tau=tau * (1 << level))
+        ms, f, _ = _run(prm, st, steps >> level)
+        rows.append({"precision": "fp32" if prec == FP32 else "fp64", "n": m, "steps": steps >> level,
+                     "gpu_ms": ms, "l1_vs_fp64_ref": l1_error(f, coarsen(ref, n, level), 4)})
+    names = {1: "PDM", 2: "TVD", 3: "WENO5", 4: "MPWENO5", 5: "TVD-MC"}
+    return {"study": "equal_time", "recon": names[recon],
+            "workload": f"{n}^3 periodic decaying turbulence (Ms 0.5, k^-2, rms v 1, B 0.5), RK2, "
+                        f"{steps} steps at {n}^3 and the same physical time on the coarser grids",
+            "reference": f"FP64 {n}^3", "runs": rows,
+            "note": "errors: relative L1 of the conserved variables against the FP64 reference restricted to "
+                    "the run's grid; gpu_ms: CUDA events around graph replays, state resident in HBM"}
+
+
 def learned_study(n: int = 64, train_seeds=tuple(range(100, 108)), val_seed: int = 108,
                   test_seeds=(200, 201, 202, 203), steps: int = 100, every: int = 10, iters: int = 4000) -> dict:
     from . import learned
@@ -163,13 +208,16 @@ def learned_study(n: int = 64, train_seeds=tuple(range(100, 108)), val_seed: int
 def main(argv=None) -> None:
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["curvilinear", "precision", "learned"])
+    ap.add_argument("study", choices=["curvilinear", "precision", "learned", "equal_time"])
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--recons", default="1,5,3", help="precision study: reconop values (1 PDM, 5 TVD-MC, 3 WENO5)")
     a = ap.parse_args(argv)
     if a.study == "curvilinear":
         print(json.dumps(curvilinear(a.n or 192, a.steps or 200)), flush=True)
+    elif a.study == "equal_time":
+        for r in tuple(int(r) for r in a.recons.split(",")):
+            print(json.dumps(equal_time(a.n or 256, a.steps or 100, r)), flush=True)
     elif a.study == "learned":
         print(json.dumps(learned_study(a.n or 64, steps=a.steps or 100)), flush=True)
     else:

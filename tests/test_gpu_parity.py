@@ -306,6 +306,35 @@ def test_autotuned_shapes_give_identical_steps():
         assert np.array_equal(fa[k], fb[k]), k
 
 
+def test_set_tiles_every_shape_gives_identical_steps():
+    """mhd_set_tiles: all six FP32 PDM launch-shape pairs step to the same
+    bits; fixed-shape handles refuse other shapes; mhd_device_info reports
+    the device."""
+    import ctypes as C
+    from mhd3d_mpi_fortran_gb300 import abi
+    from mhd3d_mpi_fortran_gb300.abi import MHDError
+    s = ics.turbulence(40, seed=5)
+    prm = Params(40, 40, 40, precision=FP32, tau=0.5 * ics.cfl_dt(s))
+    ref = None
+    for td in (4, 8, 16):
+        for ey in (4, 8):
+            with MHDSolver(prm, s) as g:
+                g.set_tiles(td, ey)
+                g.step(2)
+                g.step(2, graph=True)
+                f = g.fetch()
+            if ref is None:
+                ref = f
+            for k in FIELDS:
+                assert np.array_equal(f[k], ref[k]), (td, ey, k)
+    with MHDSolver(Params(16, 16, 16, precision=FP64, tau=1e-3), ics.orszag_tang_3d(16)) as g:
+        with pytest.raises(MHDError):
+            g.set_tiles(16, 8)
+    info = (C.c_int32 * 4)()
+    assert abi.load().mhd_device_info(info) == 0
+    assert info[0] > 0 and info[1] >= 10 and info[3] > 0
+
+
 def test_ensemble_autotune_then_step_equals_sequential():
     from mhd3d_mpi_fortran_gb300 import ensemble_autotune
     sizes = (16, 20, 12)

@@ -31,3 +31,20 @@ def test_errors_are_zero_for_identical_states_and_grouped():
     g["vz"] = g["vz"] + 1e-3
     e = studies.errors(g, f, 4)
     assert 0 < e["v"]["l1"] < 1e-2 and e["rho"]["l1"] == 0.0
+
+
+def test_coarsen_keeps_mass_and_div_free_faces():
+    from mhd3d_mpi_fortran_gb300.learned import state_dict
+    n, ng = 16, 4
+    s = ics.turbulence(n, seed=3)
+    f = state_dict(s)
+    c = studies.coarsen(f, n, 2)
+    m = n // 4
+    inner = (slice(ng, ng + m),) * 3
+    assert c["rho"].shape == (m + 2 * ng,) * 3
+    assert np.isclose(c["rho"][inner].mean(), s.rho[ng:-ng, ng:-ng, ng:-ng].mean(), rtol=1e-13)
+    bi, bj, bk = c["bi"], c["bj"], c["bk"]
+    div = (bi[ng + 1:ng + m + 1, ng:ng + m, ng:ng + m] - bi[ng:ng + m, ng:ng + m, ng:ng + m]
+           + bj[ng:ng + m, ng + 1:ng + m + 1, ng:ng + m] - bj[ng:ng + m, ng:ng + m, ng:ng + m]
+           + bk[ng:ng + m, ng:ng + m, ng + 1:ng + m + 1] - bk[ng:ng + m, ng:ng + m, ng:ng + m])
+    assert np.abs(div).max() <= 1e-12 * np.abs(bi).max()
