@@ -1384,7 +1384,7 @@ int mhd_set_tiles(void* handle, int32_t face_tile, int32_t ei_tile) {
   bool ok_td = false, ok_ey = false;
   for (int td : kTileTD) ok_td |= td == face_tile;
   for (int ey : kTileEY) ok_ey |= ey == ei_tile;
-  if (!ok_td || !ok_ey) return fail(MHD_E_ARG, "face tile must be 4, 8 or 16 and ei tile 4 or 8");
+  if (!ok_td || !ok_ey) return fail(MHD_E_ARG, "face tile must be 4, 8, 16 or 32 and ei tile 4 or 8");
   int rc = wait_stream(h);
   if (rc) return rc;
   h->tile_td = face_tile;

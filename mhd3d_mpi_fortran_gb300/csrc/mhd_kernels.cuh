@@ -856,6 +856,57 @@ __host__ __device__ constexpr size_t flux_t_smem() {
   return sizeof(T) * ((FLUX_STAGED ? 8 * (TDV + 8) * 32 : 0) + 8 * (TDV + 1) * 32 + 8 * TDV * 33);
 }
 
+// The conserved update of one cell from its z-face flux difference dF and the
+// x+y divergence in dU (advance_corrector1 + stage combine + p +
+// advance_corrector2 + combine + v, mhd3d3.f90:3666-3697 / 3736-3783; AB:
+// 3626-3627, 3876, 3901-3905), written to the other half of the
+// double-buffered primitives.  cd is the cell's z index.
+template <typename T, bool M>
+__device__ __forceinline__ void cell_update(const Dev<T>& d, int c, int cd, const T* dF, int form, T cw, T den) {
+  const T tau = (T)d.sc->tau;
+  const T gm1 = d.gam - T(1);
+  T dv[8];
+  if (M) {
+    const T V = (T)d.m.vol[c], rV = (T)d.m.rvol[c];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) dv[q] = Ops<T>::dw(d.dU[q][c] + dF[q], V, rV);
+  } else {
+    const T dz = d.wz[cd], rdz = d.rwz[cd];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) dv[q] = d.dU[q][c] + Ops<T>::dw(dF[q], dz, rdz);
+  }
+  // get_conserve of the current state (AB: the state, not the prediction)
+  T rr = d.rho[c], u = d.vx[c], v = d.vy[c], ww = d.vz[c], pr = d.p[c];
+  T rvx0 = rr * u, rvy0 = rr * v, rvz0 = rr * ww;
+  T eng0 = T(0.5) * rr * (u * u + v * v + ww * ww) + Ops<T>::dv(pr, gm1);
+  T rho1 = rr - tau * dv[0];
+  T eng1 = eng0 - tau * dv[4];
+  T rx = rvx0 - tau * dv[1], ry = rvy0 - tau * dv[2], rz = rvz0 - tau * dv[3];
+  T hx = rx, hy = ry, hz = rz;
+  if (form >= 0) {
+    rho1 = comb(form, cw, d.q[0][c], rho1, den);
+    hx = comb(form, cw, d.q[1][c], rx, den);
+    hy = comb(form, cw, d.q[2][c], ry, den);
+    hz = comb(form, cw, d.q[3][c], rz, den);
+    eng1 = comb(form, cw, d.q[4][c], eng1, den);
+  }
+  const T rrho = Ops<T>::rcp(rho1);
+  T pn = gm1 * (eng1 - Ops<T>::dvr(T(0.5) * (hx * hx + hy * hy + hz * hz), rho1, rrho));
+  rx = rx - tau * dv[5];
+  ry = ry - tau * dv[6];
+  rz = rz - tau * dv[7];
+  if (form >= 0) {
+    rx = comb(form, cw, d.q[1][c], rx, den);
+    ry = comb(form, cw, d.q[2][c], ry, den);
+    rz = comb(form, cw, d.q[3][c], rz, den);
+  }
+  d.orho[c] = rho1;
+  d.op[c] = pn;
+  d.ovx[c] = Ops<T>::dvr(rx, rho1, rrho);
+  d.ovy[c] = Ops<T>::dvr(ry, rho1, rrho);
+  d.ovz[c] = Ops<T>::dvr(rz, rho1, rrho);
+}
+
 template <typename T, int RECON, int D, bool M, bool B, int TDV = TD>
 __global__ void __launch_bounds__(32 * (TDV + 1), FluxMinB<T>::value)
     k_flux_t(KArg<T, B> ka, Inp<T> in0, Prm<T> P, int form, T cw, T den, int ab) {
@@ -954,49 +1005,133 @@ __global__ void __launch_bounds__(32 * (TDV + 1), FluxMinB<T>::value)
     }
     return;
   }
-  const T tau = (T)d.sc->tau;
-  const T gm1 = d.gam - T(1);
-  T dv[8];
-  if (M) {
-    const T V = (T)d.m.vol[c], rV = (T)d.m.rvol[c];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) dv[q] = Ops<T>::dw(d.dU[q][c] + dF[q], V, rV);
-  } else {
-    const T dz = d.wz[cd], rdz = d.rwz[cd];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) dv[q] = d.dU[q][c] + Ops<T>::dw(dF[q], dz, rdz);
-  }
-  // get_conserve of the current state (AB: the state, not the prediction)
-  T rr = d.rho[c], u = d.vx[c], v = d.vy[c], ww = d.vz[c], pr = d.p[c];
-  T rvx0 = rr * u, rvy0 = rr * v, rvz0 = rr * ww;
-  T eng0 = T(0.5) * rr * (u * u + v * v + ww * ww) + Ops<T>::dv(pr, gm1);
-  T rho1 = rr - tau * dv[0];
-  T eng1 = eng0 - tau * dv[4];
-  T rx = rvx0 - tau * dv[1], ry = rvy0 - tau * dv[2], rz = rvz0 - tau * dv[3];
-  T hx = rx, hy = ry, hz = rz;
-  if (form >= 0) {
-    rho1 = comb(form, cw, d.q[0][c], rho1, den);
-    hx = comb(form, cw, d.q[1][c], rx, den);
-    hy = comb(form, cw, d.q[2][c], ry, den);
-    hz = comb(form, cw, d.q[3][c], rz, den);
-    eng1 = comb(form, cw, d.q[4][c], eng1, den);
-  }
-  const T rrho = Ops<T>::rcp(rho1);
-  T pn = gm1 * (eng1 - Ops<T>::dvr(T(0.5) * (hx * hx + hy * hy + hz * hz), rho1, rrho));
-  rx = rx - tau * dv[5];
-  ry = ry - tau * dv[6];
-  rz = rz - tau * dv[7];
-  if (form >= 0) {
-    rx = comb(form, cw, d.q[1][c], rx, den);
-    ry = comb(form, cw, d.q[2][c], ry, den);
-    rz = comb(form, cw, d.q[3][c], rz, den);
-  }
-  d.orho[c] = rho1;
-  d.op[c] = pn;
-  d.ovx[c] = Ops<T>::dvr(rx, rho1, rrho);
-  d.ovy[c] = Ops<T>::dvr(ry, rho1, rrho);
-  d.ovz[c] = Ops<T>::dvr(rz, rho1, rrho);
+  cell_update<T, M>(d, c, cd, dF, form, cw, den);
   (void)ab;
+}
+
+// y / z faces by column sweeps: the FP32 Cartesian PDM alternative to the face
+// tiles, one more launch shape for the autotuner.  A thread owns one column of
+// cells along D (x from the lane, the remaining axis from the warp) over a
+// segment of SWEEP_SEG cells and keeps the 8 reconstructed fields of the 8
+// cells around its current face in registers: one new cell is loaded per face
+// (issued a face ahead, before that face's arithmetic), every face flux is
+// computed once, and a cell's face-pair difference is the current minus the
+// previous face's flux.  Face arithmetic and epilogues are those of k_flux_t,
+// so the two give the same bits.
+constexpr int SWEEP_SEG = 32;
+#ifndef MHD_SWEEP_UNROLL
+#define MHD_SWEEP_UNROLL 1
+#endif
+constexpr int kSweepUnroll = MHD_SWEEP_UNROLL;  // face-loop unroll (compile-time knob)
+
+template <typename T, int D, bool B>
+__global__ void __launch_bounds__(128, 4)
+    k_flux_sweep(KArg<T, B> ka, Inp<T> in0, Prm<T> P, int form, T cw, T den) {
+  const int4 bb = ka.blk();
+  const auto& d = ka.dev(bb);
+  const Inp<T> in = B ? state_view(d) : in0;
+  const Geom& g = d.g;
+  const int n0 = (D == 1) ? g.ny0 : g.nz0;
+  const int no = (D == 1) ? g.nz0 : g.ny0;
+  const int o = bb.w * 4 + threadIdx.y + g.ng;  // remaining axis (one per warp): z for y faces, y for z faces
+  if (o >= g.ng + no) return;
+  const int tx = threadIdx.x;
+  // lanes past the last column work on a copy of it and store nothing, so the
+  // whole warp stays in the loop (warp-synchronous copies below)
+  const int i0 = bb.y * 32 + tx + g.ng;
+  const bool xin = i0 < g.ng + g.nx0;
+  const int i = xin ? i0 : g.ng + g.nx0 - 1;
+  const int c0 = g.ng + bb.z * SWEEP_SEG;
+  const int c1 = min(c0 + SWEEP_SEG, g.ng + n0);
+  const int s = (D == 1) ? g.px : (int)g.plane;
+  const int col = (D == 1) ? i + (int)g.plane * o : i + g.px * o;  // + cd * s
+  const T* src[8] = {in.rho, in.vx, in.vy, in.vz, in.p, in.bx, in.by, in.bz};
+  // y faces: the x-face fluxes of the next cell are copied asynchronously into
+  // a per-warp double buffer one face ahead of the epilogue that reads them
+  __shared__ __align__(16) T sxf[4][2][8][33];
+  T (*xs)[8][33] = sxf[threadIdx.y];
+  T w[8][8], nx[8], Fp[8];
+  // window of the first face (cell c0): cells c0-4 .. c0+3; the loop shifts
+  // one cell in per face, so w[v][1..7] start as cells c0-4 .. c0+2
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+#pragma unroll
+    for (int m = 1; m < 8; ++m) w[v][m] = src[v][col + (c0 - 5 + m) * s];
+    nx[v] = src[v][col + (c0 + 3) * s];
+  }
+  T dx = T(0), rdx = T(0);
+  if (D == 1) {
+    dx = d.wx[i];
+    rdx = d.rwx[i];
+  }
+#pragma unroll kSweepUnroll
+  for (int cd = c0; cd <= c1; ++cd) {  // the face at the low side of cell cd
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+#pragma unroll
+      for (int m = 0; m < 7; ++m) w[v][m] = w[v][m + 1];
+      w[v][7] = nx[v];
+    }
+    if (cd < c1) {
+#pragma unroll
+      for (int v = 0; v < 8; ++v) nx[v] = src[v][col + (cd + 4) * s];
+    }
+    if (D == 1) {
+      __syncwarp();  // every lane is done reading the slot refilled here
+      if (cd < c1) {
+        // x faces i0 (this lane) and, on lane 31, i0 + 32, clamped to the last
+        // face (a lane past the last column supplies its left neighbour's high face)
+        const int fo = ((D == 1) ? (int)g.plane * o : g.px * o) + cd * s;
+        const int fl = fo + min(i0, g.ng + g.nx0), fh = fo + min(i0 + 1, g.ng + g.nx0);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const T* fx = d.F[0][q] + fl;
+          const uint32_t sp = (uint32_t)__cvta_generic_to_shared(&xs[cd & 1][q][tx]);
+          if (sizeof(T) == 4)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sp), "l"(fx) : "memory");
+          else
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sp), "l"(fx) : "memory");
+          if (tx == 31) {
+            const uint32_t sq = (uint32_t)__cvta_generic_to_shared(&xs[cd & 1][q][32]);
+            const T* fy = d.F[0][q] + fh;
+            if (sizeof(T) == 4)
+              asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sq), "l"(fy) : "memory");
+            else
+              asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sq), "l"(fy) : "memory");
+          }
+        }
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");  // one group per face, empty on the last
+    }
+    T L[8], R[8], F[8];
+#pragma unroll
+    for (int v = 0; v < 8; ++v) recon_win<T, R_PDM, 0>(w[v], P, L[v], R[v]);
+    face_flux<T, D>(L, R, d.gam, F);
+    if (cd > c0) {
+      const int cc = cd - 1;
+      const int c = col + cc * s;
+      T dF[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) dF[q] = F[q] - Fp[q];
+      if (D == 1) {
+        asm volatile("cp.async.wait_group 1;" ::: "memory");  // the group of cell cc (one face old)
+        __syncwarp();
+        const T dy = d.wy[cc], rdy = d.rwy[cc];
+        if (xin) {
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const T* x = &xs[cc & 1][q][tx];
+            d.dU[q][c] = Ops<T>::dw(x[1] - x[0], dx, rdx) + Ops<T>::dw(dF[q], dy, rdy);
+          }
+        }
+      } else if (xin) {
+        cell_update<T, false>(d, c, cc, dF, form, cw, den);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) Fp[q] = F[q];
+  }
+  if (D == 1) asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
 // -------------------------------------------------------------------- EMF
@@ -1827,9 +1962,18 @@ constexpr bool tunable() {
   return std::is_same<T, float>::value && RECON == R_PDM && !M;
 }
 
+inline dim3 sweep_grid(int D, const Geom& g) {
+  const int n0 = (D == 1) ? g.ny0 : g.nz0, no = (D == 1) ? g.nz0 : g.ny0;
+  return dim3((g.nx0 + 31) / 32, (n0 + SWEEP_SEG - 1) / SWEEP_SEG, (no + 3) / 4);
+}
+
 template <typename T, int RECON, int D, bool M>
 void flux_t_any(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, int form, T c, T den, int ab, cudaStream_t st) {
   if constexpr (tunable<T, RECON, M>()) {
+    if (d.tile_td == SWEEP_SEG) {
+      k_flux_sweep<T, D, false><<<sweep_grid(D, d.g), dim3(32, 4), 0, st>>>(one(d), in, P, form, c, den);
+      return;
+    }
     if (d.tile_td == 4) return launch_flux_t<T, RECON, D, M, 4>(d, in, P, form, c, den, ab, st);
     if (d.tile_td == 16) return launch_flux_t<T, RECON, D, M, 16>(d, in, P, form, c, den, ab, st);
   }
@@ -1940,8 +2084,8 @@ dim3 Batch<T>::dims(int fam, const Geom& g, int td, int ey) {
   switch (fam) {
     case BF_CFL: return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + 7) / 8);
     case BF_FLUX_X: return dim3(((g.nx0 + 1) * g.ny0 * g.nz0 + 127) / 128, 1, 1);
-    case BF_FLUX_Y: return dim3((g.nx0 + 31) / 32, (g.ny0 + td - 1) / td, g.nz0);
-    case BF_FLUX_Z: return dim3((g.nx0 + 31) / 32, (g.nz0 + td - 1) / td, g.ny0);
+    case BF_FLUX_Y: return td == SWEEP_SEG ? sweep_grid(1, g) : dim3((g.nx0 + 31) / 32, (g.ny0 + td - 1) / td, g.nz0);
+    case BF_FLUX_Z: return td == SWEEP_SEG ? sweep_grid(2, g) : dim3((g.nx0 + 31) / 32, (g.nz0 + td - 1) / td, g.ny0);
     case BF_EMF_I: return emf_grid(0, g, 32, Y, Y);
     case BF_EMF_J: return emf_grid(1, g, 32, 1, 8);
     case BF_EMF_K: return emf_grid(2, g, 32, 8, 1);
@@ -2016,7 +2160,12 @@ void Batch<T>::parts(const BatchView& v, int sel, int which, int form, double c,
     const Inp<T> none{};
     k_flux<T, R_PDM, 0, false, true><<<v.nblk[BF_FLUX_X], 128, 0, st>>>(KArg<T, true>{tab, v.map[BF_FLUX_X]}, none,
                                                                        P);
-    if (F32 && v.tile_td == 4) batch_flux_t<T, F32 ? 4 : TD>(v, tab, P, form, (T)c, (T)den, st);
+    if (F32 && v.tile_td == SWEEP_SEG) {
+      k_flux_sweep<T, 1, true><<<v.nblk[BF_FLUX_Y], dim3(32, 4), 0, st>>>(KArg<T, true>{tab, v.map[BF_FLUX_Y]}, none,
+                                                                           P, -1, T(0), T(1));
+      k_flux_sweep<T, 2, true><<<v.nblk[BF_FLUX_Z], dim3(32, 4), 0, st>>>(KArg<T, true>{tab, v.map[BF_FLUX_Z]}, none,
+                                                                           P, form, (T)c, (T)den);
+    } else if (F32 && v.tile_td == 4) batch_flux_t<T, F32 ? 4 : TD>(v, tab, P, form, (T)c, (T)den, st);
     else if (F32 && v.tile_td == 16) batch_flux_t<T, F32 ? 16 : TD>(v, tab, P, form, (T)c, (T)den, st);
     else batch_flux_t<T, TD>(v, tab, P, form, (T)c, (T)den, st);
   }

@@ -179,7 +179,7 @@ int mlp_correct(void* h, Dev<float>& d, cudaStream_t st);
 int mlp_status(void* h);
 
 // Tile lengths the autotuner tries (FP32 Cartesian PDM).
-constexpr int kTileTD[3] = {4, 8, 16};
+constexpr int kTileTD[4] = {4, 8, 16, 32};  // 32: column sweeps of 32-cell segments
 constexpr int kTileEY[2] = {4, 8};
 
 }  // namespace mhd

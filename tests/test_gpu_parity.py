@@ -298,7 +298,7 @@ def test_autotuned_shapes_give_identical_steps():
         a.step(2)
         b.step(2)
         td, ey = b.autotune(reps=2)
-        assert td in (4, 8, 16) and ey in (4, 8)
+        assert td in (4, 8, 16, 32) and ey in (4, 8)
         a.step(3, graph=True)
         b.step(3, graph=True)
         fa, fb = a.fetch(), b.fetch()
@@ -307,7 +307,8 @@ def test_autotuned_shapes_give_identical_steps():
 
 
 def test_set_tiles_every_shape_gives_identical_steps():
-    """mhd_set_tiles: all six FP32 PDM launch-shape pairs step to the same
+    """mhd_set_tiles: all eight FP32 PDM launch-shape pairs (face tiles 4, 8,
+    16 and the 32-cell column sweeps; ei tiles 4x4, 8x8) step to the same
     bits; fixed-shape handles refuse other shapes; mhd_device_info reports
     the device."""
     import ctypes as C
@@ -316,7 +317,7 @@ def test_set_tiles_every_shape_gives_identical_steps():
     s = ics.turbulence(40, seed=5)
     prm = Params(40, 40, 40, precision=FP32, tau=0.5 * ics.cfl_dt(s))
     ref = None
-    for td in (4, 8, 16):
+    for td in (4, 8, 16, 32):
         for ey in (4, 8):
             with MHDSolver(prm, s) as g:
                 g.set_tiles(td, ey)
@@ -333,6 +334,28 @@ def test_set_tiles_every_shape_gives_identical_steps():
     info = (C.c_int32 * 4)()
     assert abi.load().mhd_device_info(info) == 0
     assert info[0] > 0 and info[1] >= 10 and info[3] > 0
+
+
+def test_batched_column_sweeps_equal_sequential_tiles():
+    """Batched ensemble on the column-sweep face kernels (tile 32) against each
+    grid stepped alone on the default face tiles: bit-identical."""
+    sizes = (16, 40, 24)
+    states = [ics.turbulence(n, seed=10 + i) for i, n in enumerate(sizes)]
+    prms = [Params(n, n, n, precision=FP32, tau=0.4 * ics.cfl_dt(st)) for n, st in zip(sizes, states)]
+    seq = []
+    for prm, st in zip(prms, states):
+        with MHDSolver(prm, st) as g:
+            g.step(4)
+            seq.append(g.fetch())
+    ens = [MHDSolver(p, st) for p, st in zip(prms, states)]
+    for e in ens:
+        e.set_tiles(32, 8)
+    ensemble_step(ens, 4)
+    for e, ref in zip(ens, seq):
+        got = e.fetch()
+        for k in FIELDS:
+            assert np.array_equal(got[k], ref[k]), k
+        e.close()
 
 
 def test_ensemble_autotune_then_step_equals_sequential():
