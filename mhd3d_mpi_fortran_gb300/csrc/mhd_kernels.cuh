@@ -861,22 +861,25 @@ __host__ __device__ constexpr size_t flux_t_smem() {
 // advance_corrector2 + combine + v, mhd3d3.f90:3666-3697 / 3736-3783; AB:
 // 3626-3627, 3876, 3901-3905), written to the other half of the
 // double-buffered primitives.  cd is the cell's z index.
+// du: the x+y divergence dU of the cell; pv: its rho, vx, vy, vz, p; qv: its
+// U^n (q[0..4], read only when form >= 0).
 template <typename T, bool M>
-__device__ __forceinline__ void cell_update(const Dev<T>& d, int c, int cd, const T* dF, int form, T cw, T den) {
+__device__ __forceinline__ void cell_update_vals(const Dev<T>& d, int c, int cd, const T* dF, const T* du,
+                                                 const T* pv, const T* qv, int form, T cw, T den) {
   const T tau = (T)d.sc->tau;
   const T gm1 = d.gam - T(1);
   T dv[8];
   if (M) {
     const T V = (T)d.m.vol[c], rV = (T)d.m.rvol[c];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) dv[q] = Ops<T>::dw(d.dU[q][c] + dF[q], V, rV);
+    for (int q = 0; q < 8; ++q) dv[q] = Ops<T>::dw(du[q] + dF[q], V, rV);
   } else {
     const T dz = d.wz[cd], rdz = d.rwz[cd];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) dv[q] = d.dU[q][c] + Ops<T>::dw(dF[q], dz, rdz);
+    for (int q = 0; q < 8; ++q) dv[q] = du[q] + Ops<T>::dw(dF[q], dz, rdz);
   }
   // get_conserve of the current state (AB: the state, not the prediction)
-  T rr = d.rho[c], u = d.vx[c], v = d.vy[c], ww = d.vz[c], pr = d.p[c];
+  T rr = pv[0], u = pv[1], v = pv[2], ww = pv[3], pr = pv[4];
   T rvx0 = rr * u, rvy0 = rr * v, rvz0 = rr * ww;
   T eng0 = T(0.5) * rr * (u * u + v * v + ww * ww) + Ops<T>::dv(pr, gm1);
   T rho1 = rr - tau * dv[0];
@@ -884,11 +887,11 @@ __device__ __forceinline__ void cell_update(const Dev<T>& d, int c, int cd, cons
   T rx = rvx0 - tau * dv[1], ry = rvy0 - tau * dv[2], rz = rvz0 - tau * dv[3];
   T hx = rx, hy = ry, hz = rz;
   if (form >= 0) {
-    rho1 = comb(form, cw, d.q[0][c], rho1, den);
-    hx = comb(form, cw, d.q[1][c], rx, den);
-    hy = comb(form, cw, d.q[2][c], ry, den);
-    hz = comb(form, cw, d.q[3][c], rz, den);
-    eng1 = comb(form, cw, d.q[4][c], eng1, den);
+    rho1 = comb(form, cw, qv[0], rho1, den);
+    hx = comb(form, cw, qv[1], rx, den);
+    hy = comb(form, cw, qv[2], ry, den);
+    hz = comb(form, cw, qv[3], rz, den);
+    eng1 = comb(form, cw, qv[4], eng1, den);
   }
   const T rrho = Ops<T>::rcp(rho1);
   T pn = gm1 * (eng1 - Ops<T>::dvr(T(0.5) * (hx * hx + hy * hy + hz * hz), rho1, rrho));
@@ -896,15 +899,26 @@ __device__ __forceinline__ void cell_update(const Dev<T>& d, int c, int cd, cons
   ry = ry - tau * dv[6];
   rz = rz - tau * dv[7];
   if (form >= 0) {
-    rx = comb(form, cw, d.q[1][c], rx, den);
-    ry = comb(form, cw, d.q[2][c], ry, den);
-    rz = comb(form, cw, d.q[3][c], rz, den);
+    rx = comb(form, cw, qv[1], rx, den);
+    ry = comb(form, cw, qv[2], ry, den);
+    rz = comb(form, cw, qv[3], rz, den);
   }
   d.orho[c] = rho1;
   d.op[c] = pn;
   d.ovx[c] = Ops<T>::dvr(rx, rho1, rrho);
   d.ovy[c] = Ops<T>::dvr(ry, rho1, rrho);
   d.ovz[c] = Ops<T>::dvr(rz, rho1, rrho);
+}
+
+template <typename T, bool M>
+__device__ __forceinline__ void cell_update(const Dev<T>& d, int c, int cd, const T* dF, int form, T cw, T den) {
+  T du[8], pv[5], qv[5];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) du[q] = d.dU[q][c];
+  pv[0] = d.rho[c]; pv[1] = d.vx[c]; pv[2] = d.vy[c]; pv[3] = d.vz[c]; pv[4] = d.p[c];
+#pragma unroll
+  for (int q = 0; q < 5; ++q) qv[q] = (form >= 0) ? d.q[q][c] : T(0);
+  cell_update_vals<T, M>(d, c, cd, dF, du, pv, qv, form, cw, den);
 }
 
 template <typename T, int RECON, int D, bool M, bool B, int TDV = TD>
@@ -1050,6 +1064,10 @@ __global__ void __launch_bounds__(128, 4)
   // a per-warp double buffer one face ahead of the epilogue that reads them
   __shared__ __align__(16) T sxf[4][2][8][33];
   T (*xs)[8][33] = sxf[threadIdx.y];
+  // z faces: dU, the state (rho, v, p) and U^n of the next cell, likewise
+  // (each lane reads back only what it copied)
+  __shared__ __align__(16) T szf[4][2][18][32];
+  T (*zs)[18][32] = szf[threadIdx.y];
   T w[8][8], nx[8], Fp[8];
   // window of the first face (cell c0): cells c0-4 .. c0+3; the loop shifts
   // one cell in per face, so w[v][1..7] start as cells c0-4 .. c0+2
@@ -1102,6 +1120,25 @@ __global__ void __launch_bounds__(128, 4)
         }
       }
       asm volatile("cp.async.commit_group;" ::: "memory");  // one group per face, empty on the last
+    } else {
+      if (cd < c1) {
+        const int c = col + cd * s;
+        const T* gsrc[18] = {d.dU[0] + c, d.dU[1] + c, d.dU[2] + c, d.dU[3] + c, d.dU[4] + c, d.dU[5] + c,
+                             d.dU[6] + c, d.dU[7] + c, d.rho + c,   d.vx + c,    d.vy + c,    d.vz + c,
+                             d.p + c,     d.q[0] + c, d.q[1] + c, d.q[2] + c, d.q[3] + c, d.q[4] + c};
+        const int nz = (form >= 0) ? 18 : 13;
+#pragma unroll
+        for (int a = 0; a < 18; ++a) {
+          if (a < nz) {
+            const uint32_t sp = (uint32_t)__cvta_generic_to_shared(&zs[cd & 1][a][tx]);
+            if (sizeof(T) == 4)
+              asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sp), "l"(gsrc[a]) : "memory");
+            else
+              asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sp), "l"(gsrc[a]) : "memory");
+          }
+        }
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
     }
     T L[8], R[8], F[8];
 #pragma unroll
@@ -1124,14 +1161,25 @@ __global__ void __launch_bounds__(128, 4)
             d.dU[q][c] = Ops<T>::dw(x[1] - x[0], dx, rdx) + Ops<T>::dw(dF[q], dy, rdy);
           }
         }
-      } else if (xin) {
-        cell_update<T, false>(d, c, cc, dF, form, cw, den);
+      } else {
+        asm volatile("cp.async.wait_group 1;" ::: "memory");  // this lane's copies of cell cc
+        if (xin) {
+          const T* zv = &zs[cc & 1][0][tx];
+          T du[8], pv[5], qv[5];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) du[q] = zv[q * 32];
+#pragma unroll
+          for (int q = 0; q < 5; ++q) pv[q] = zv[(8 + q) * 32];
+#pragma unroll
+          for (int q = 0; q < 5; ++q) qv[q] = (form >= 0) ? zv[(13 + q) * 32] : T(0);
+          cell_update_vals<T, false>(d, c, cc, dF, du, pv, qv, form, cw, den);
+        }
       }
     }
 #pragma unroll
     for (int q = 0; q < 8; ++q) Fp[q] = F[q];
   }
-  if (D == 1) asm volatile("cp.async.wait_all;" ::: "memory");
+  asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
 // -------------------------------------------------------------------- EMF
