@@ -1032,7 +1032,10 @@ __global__ void __launch_bounds__(32 * (TDV + 1), FluxMinB<T>::value)
 // computed once, and a cell's face-pair difference is the current minus the
 // previous face's flux.  Face arithmetic and epilogues are those of k_flux_t,
 // so the two give the same bits.
-constexpr int SWEEP_SEG = 32;
+#ifndef MHD_SWEEP_SEG
+#define MHD_SWEEP_SEG 32
+#endif
+constexpr int SWEEP_SEG = MHD_SWEEP_SEG;  // cells per column segment (compile-time knob)
 #ifndef MHD_SWEEP_UNROLL
 #define MHD_SWEEP_UNROLL 1
 #endif
@@ -2018,7 +2021,7 @@ inline dim3 sweep_grid(int D, const Geom& g) {
 template <typename T, int RECON, int D, bool M>
 void flux_t_any(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, int form, T c, T den, int ab, cudaStream_t st) {
   if constexpr (tunable<T, RECON, M>()) {
-    if (d.tile_td == SWEEP_SEG) {
+    if (d.tile_td == kSweepTile) {
       k_flux_sweep<T, D, false><<<sweep_grid(D, d.g), dim3(32, 4), 0, st>>>(one(d), in, P, form, c, den);
       return;
     }
@@ -2132,8 +2135,8 @@ dim3 Batch<T>::dims(int fam, const Geom& g, int td, int ey) {
   switch (fam) {
     case BF_CFL: return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + 7) / 8);
     case BF_FLUX_X: return dim3(((g.nx0 + 1) * g.ny0 * g.nz0 + 127) / 128, 1, 1);
-    case BF_FLUX_Y: return td == SWEEP_SEG ? sweep_grid(1, g) : dim3((g.nx0 + 31) / 32, (g.ny0 + td - 1) / td, g.nz0);
-    case BF_FLUX_Z: return td == SWEEP_SEG ? sweep_grid(2, g) : dim3((g.nx0 + 31) / 32, (g.nz0 + td - 1) / td, g.ny0);
+    case BF_FLUX_Y: return td == kSweepTile ? sweep_grid(1, g) : dim3((g.nx0 + 31) / 32, (g.ny0 + td - 1) / td, g.nz0);
+    case BF_FLUX_Z: return td == kSweepTile ? sweep_grid(2, g) : dim3((g.nx0 + 31) / 32, (g.nz0 + td - 1) / td, g.ny0);
     case BF_EMF_I: return emf_grid(0, g, 32, Y, Y);
     case BF_EMF_J: return emf_grid(1, g, 32, 1, 8);
     case BF_EMF_K: return emf_grid(2, g, 32, 8, 1);
@@ -2208,7 +2211,7 @@ void Batch<T>::parts(const BatchView& v, int sel, int which, int form, double c,
     const Inp<T> none{};
     k_flux<T, R_PDM, 0, false, true><<<v.nblk[BF_FLUX_X], 128, 0, st>>>(KArg<T, true>{tab, v.map[BF_FLUX_X]}, none,
                                                                        P);
-    if (F32 && v.tile_td == SWEEP_SEG) {
+    if (F32 && v.tile_td == kSweepTile) {
       k_flux_sweep<T, 1, true><<<v.nblk[BF_FLUX_Y], dim3(32, 4), 0, st>>>(KArg<T, true>{tab, v.map[BF_FLUX_Y]}, none,
                                                                            P, -1, T(0), T(1));
       k_flux_sweep<T, 2, true><<<v.nblk[BF_FLUX_Z], dim3(32, 4), 0, st>>>(KArg<T, true>{tab, v.map[BF_FLUX_Z]}, none,

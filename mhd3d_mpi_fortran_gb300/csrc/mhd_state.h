@@ -179,7 +179,8 @@ int mlp_correct(void* h, Dev<float>& d, cudaStream_t st);
 int mlp_status(void* h);
 
 // Tile lengths the autotuner tries (FP32 Cartesian PDM).
-constexpr int kTileTD[4] = {4, 8, 16, 32};  // 32: column sweeps of 32-cell segments
+constexpr int kSweepTile = 32;  // face-shape value of the column sweeps
+constexpr int kTileTD[4] = {4, 8, 16, kSweepTile};
 constexpr int kTileEY[2] = {4, 8};
 
 }  // namespace mhd
