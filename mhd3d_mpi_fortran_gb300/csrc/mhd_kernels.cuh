@@ -243,26 +243,82 @@ __device__ __forceinline__ T pdm_half(T lo, T hi, T outer, bool left, T fi, T pd
 // side first and only that half-limiter is evaluated (pdm_half: same bits as
 // evaluating all four pdm2 and selecting).  v may point to global or shared
 // memory.
-template <typename T, typename I>
-__device__ __forceinline__ T corner_pdm(const T* __restrict__ v, I c, I s1, I s2, T vi, T pd) {
-  const I q00 = c - s1 - s2, q10 = c - s2, q01 = c - s1, q11 = c;
-  const T d00 = fab(v[q00 - s1] - v[q00]) - fab(v[q00 - s2] - v[q00]);
-  const T d10 = fab(v[q10 + s1] - v[q10]) - fab(v[q10 - s2] - v[q10]);
-  const T d01 = fab(v[q01 - s1] - v[q01]) - fab(v[q01 + s2] - v[q01]);
-  const T d11 = fab(v[q11 + s1] - v[q11]) - fab(v[q11 + s2] - v[q11]);
+// The same on the 12 cells it reads, named by (offset along d1, offset along
+// d2) from the upper cell: mAB = (-A, -B), pAB = (+A, -B) etc.
+template <typename T>
+__device__ __forceinline__ T corner_pdm_vals(T m11, T m21, T m12, T m01, T p11, T m02, T m10, T m20, T m1p, T c0,
+                                             T p10, T p01, T vi, T pd) {
+  // quadrant cells q00 = (-1,-1), q10 = (0,-1), q01 = (-1,0), q11 = (0,0)
+  const T d00 = fab(m21 - m11) - fab(m12 - m11);
+  const T d10 = fab(p11 - m01) - fab(m02 - m01);
+  const T d01 = fab(m20 - m10) - fab(m1p - m10);
+  const T d11 = fab(p10 - c0) - fab(p01 - c0);
   // pdm2 #1 on (c-s2-2s1, c-s2-s1, c-s2, c-s2+s1) -> (v00_0, v10_0)
   // pdm2 #2 on (c-s1-2s2, c-s1-s2, c-s1, c-s1+s2) -> (v00_1, v01_1)
   // pdm2 #3 on (c-2s2, c-s2, c, c+s2)             -> (v10_1, v11_1)
   // pdm2 #4 on (c-2s1, c-s1, c, c+s1)             -> (v01_0, v11_0)
   const bool b00 = d00 >= T(0), b10 = d10 >= T(0), b01 = d01 >= T(0), b11 = d11 >= T(0);
-  const T v00 = pdm_half(v[c - s1 - s2], b00 ? v[c - s2] : v[c - s1], b00 ? v[c - s2 - 2 * s1] : v[c - s1 - 2 * s2],
-                         true, vi, pd);
-  const T v10 = pdm_half(b10 ? v[c - s2 - s1] : v[c - s2], b10 ? v[c - s2] : v[c],
-                         b10 ? v[c - s2 + s1] : v[c - 2 * s2], !b10, vi, pd);
-  const T v01 = pdm_half(b01 ? v[c - s1] : v[c - s1 - s2], b01 ? v[c] : v[c - s1],
-                         b01 ? v[c - 2 * s1] : v[c - s1 + s2], b01, vi, pd);
-  const T v11 = pdm_half(b11 ? v[c - s1] : v[c - s2], v[c], b11 ? v[c + s1] : v[c + s2], false, vi, pd);
+  const T v00 = pdm_half(m11, b00 ? m01 : m10, b00 ? m21 : m12, true, vi, pd);
+  const T v10 = pdm_half(b10 ? m11 : m01, b10 ? m01 : c0, b10 ? p11 : m02, !b10, vi, pd);
+  const T v01 = pdm_half(b01 ? m10 : m11, b01 ? c0 : m10, b01 ? m20 : m1p, b01, vi, pd);
+  const T v11 = pdm_half(b11 ? m10 : m01, c0, b11 ? p10 : p01, false, vi, pd);
   return T(0.25) * (v00 + v01 + v10 + v11);
+}
+
+template <typename T, typename I>
+__device__ __forceinline__ T corner_pdm(const T* __restrict__ v, I c, I s1, I s2, T vi, T pd) {
+  return corner_pdm_vals(v[c - s1 - s2], v[c - 2 * s1 - s2], v[c - s1 - 2 * s2], v[c - s2], v[c + s1 - s2],
+                         v[c - 2 * s2], v[c - s1], v[c - 2 * s1], v[c - s1 + s2], v[c], v[c + s1], v[c + s2], vi, pd);
+}
+
+// Two values carried together (the v_a1 and v_a2 components of an edge): one
+// 8-byte (FP32) or 16-byte (FP64) shared-memory access per pair, and FP32
+// pair arithmetic on the packed FMA / MUL pipes (each lane rounds as the
+// scalar fma / mul does); FP64 stays scalar, with separate mul and add as
+// the reference writes them.
+template <typename T> struct Pr;
+template <> struct Pr<float> {
+  typedef float2 V;
+  static __device__ __forceinline__ V mk(float a, float b) { return make_float2(a, b); }
+  static __device__ __forceinline__ V mul(float k, V a) { return __fmul2_rn(make_float2(k, k), a); }
+  static __device__ __forceinline__ V mad(float k, V a, V c) { return __ffma2_rn(make_float2(k, k), a, c); }  // c + k a
+  static __device__ __forceinline__ V by(V a, float b) { return mul(1.0f / b, a); }  // Div<float>::by
+};
+template <> struct Pr<double> {
+  typedef double2 V;
+  static __device__ __forceinline__ V mk(double a, double b) { return make_double2(a, b); }
+  static __device__ __forceinline__ V mul(double k, V a) { return make_double2(k * a.x, k * a.y); }
+  static __device__ __forceinline__ V mad(double k, V a, V c) { return make_double2(c.x + k * a.x, c.y + k * a.y); }
+  static __device__ __forceinline__ V by(V a, double b) { return make_double2(a.x / b, a.y / b); }
+};
+
+// tap8 on pairs (same operand order: s = -3 a0, s + 29 a1, s - 139 a2, ...)
+template <typename T>
+__device__ __forceinline__ typename Pr<T>::V tap8p(typename Pr<T>::V a0, typename Pr<T>::V a1, typename Pr<T>::V a2,
+                                                    typename Pr<T>::V a3, typename Pr<T>::V a4, typename Pr<T>::V a5,
+                                                    typename Pr<T>::V a6, typename Pr<T>::V a7) {
+  typedef Pr<T> Q;
+  typename Q::V s = Q::mul(T(-3), a0);
+  s = Q::mad(T(29), a1, s);
+  s = Q::mad(T(-139), a2, s);
+  s = Q::mad(T(533), a3, s);
+  s = Q::mad(T(533), a4, s);
+  s = Q::mad(T(-139), a5, s);
+  s = Q::mad(T(29), a6, s);
+  s = Q::mad(T(-3), a7, s);
+  return Q::by(s, T(840));
+}
+
+// corner_pdm of both components from pair-interleaved shared memory.
+template <typename T>
+__device__ __forceinline__ void corner_pdm_pair(const typename Pr<T>::V* __restrict__ v, int c, int s1, int s2,
+                                                typename Pr<T>::V vi, T pd, T& r0, T& r1) {
+  typedef typename Pr<T>::V V;
+  const V m11 = v[c - s1 - s2], m21 = v[c - 2 * s1 - s2], m12 = v[c - s1 - 2 * s2], m01 = v[c - s2];
+  const V p11 = v[c + s1 - s2], m02 = v[c - 2 * s2], m10 = v[c - s1], m20 = v[c - 2 * s1];
+  const V m1p = v[c - s1 + s2], c0 = v[c], p10 = v[c + s1], p01 = v[c + s2];
+  r0 = corner_pdm_vals(m11.x, m21.x, m12.x, m01.x, p11.x, m02.x, m10.x, m20.x, m1p.x, c0.x, p10.x, p01.x, vi.x, pd);
+  r1 = corner_pdm_vals(m11.y, m21.y, m12.y, m01.y, p11.y, m02.y, m10.y, m20.y, m1p.y, c0.y, p10.y, p01.y, vi.y, pd);
 }
 
 // Limited corner value of v at the edge whose two transverse axes have
@@ -1281,9 +1337,11 @@ __device__ __forceinline__ void emf_pdm_tile(const Dev<T>& d, const Inp<T>& in, 
   constexpr int GE = (E == 0) ? 1 : (A1 == 0) ? T1 : R2;
   constexpr int G1 = (E == 0) ? TE : (A1 == 0) ? 1 : R2 * TE;
   constexpr int G2 = (E == 0) ? TE * T1 : (A1 == 0) ? T1 * TE : 1;
+  typedef Pr<T> Q;
+  typedef typename Q::V V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* sv = reinterpret_cast<T*>(smem_raw);  // [2][NV]: v_a1, v_a2
-  T* sg = sv + 2 * NV;                     // [2][NG]: first-pass interpolants
+  V* sv = reinterpret_cast<V*>(smem_raw);  // [NV] (v_a1, v_a2) pairs
+  V* sg = sv + NV;                         // [NG] first-pass interpolant pairs
   const Geom& g = d.g;
   const T* vel[3] = {in.vx, in.vy, in.vz};
   const T* v1 = vel[A1];
@@ -1300,8 +1358,7 @@ __device__ __forceinline__ void emf_pdm_tile(const Dev<T>& d, const Inp<T>& in, 
       a = v1[gi];
       b = v2[gi];
     }
-    sv[t] = a;
-    sv[NV + t] = b;
+    sv[t] = Q::mk(a, b);
   }
   __syncthreads();
   // first pass of interp2_pdm over (e, f1, r2), flat with the x-mapped index fastest
@@ -1318,11 +1375,8 @@ __device__ __forceinline__ void emf_pdm_tile(const Dev<T>& d, const Inp<T>& in, 
     }
     const int b0 = e * SE + f1 * S1 + r2 * S2;
     const int gi = e * GE + f1 * G1 + r2 * G2;
-#pragma unroll
-    for (int w = 0; w < 2; ++w) {
-      const T* a = sv + w * NV + b0;
-      sg[w * NG + gi] = tap8(a[0], a[S1], a[2 * S1], a[3 * S1], a[4 * S1], a[5 * S1], a[6 * S1], a[7 * S1]);
-    }
+    const V* a = sv + b0;
+    sg[gi] = tap8p<T>(a[0], a[S1], a[2 * S1], a[3 * S1], a[4 * S1], a[5 * S1], a[6 * S1], a[7 * S1]);
   }
   __syncthreads();
   const int n0[3] = {g.nx0, g.ny0, g.nz0};
@@ -1337,20 +1391,16 @@ __device__ __forceinline__ void emf_pdm_tile(const Dev<T>& d, const Inp<T>& in, 
     const int f1 = (A1 == 0) ? lx : (A1 == 1) ? ly : lz;
     const int f2 = (A2 == 0) ? lx : (A2 == 1) ? ly : lz;
     const int cv = e * SE + (f1 + 4) * S1 + (f2 + 4) * S2;
-    T vav[2];
-#pragma unroll
-    for (int w = 0; w < 2; ++w) {
-      const T* gg = sg + w * NG + e * GE + f1 * G1 + f2 * G2;
-      constexpr int GS = G2;
-      T vi = tap8(gg[0], gg[GS], gg[2 * GS], gg[3 * GS], gg[4 * GS], gg[5 * GS], gg[6 * GS], gg[7 * GS]);
-      vav[w] = corner_pdm<T, int>(sv + w * NV, cv, S1, S2, vi, P.pdmb);
-    }
+    const V* gg = sg + e * GE + f1 * G1 + f2 * G2;
+    constexpr int GS = G2;
+    const V vi = tap8p<T>(gg[0], gg[GS], gg[2 * GS], gg[3 * GS], gg[4 * GS], gg[5 * GS], gg[6 * GS], gg[7 * GS]);
+    T v1av, v2av;
+    corner_pdm_pair<T>(sv, cv, S1, S2, vi, P.pdmb, v1av, v2av);
     const int c = gx + g.px * (gy + g.py * gz);
     const int s1 = st[A1], s2 = st[A2];
     T b1l, b1r, b2l, b2r;
     recon_face<T, R_PDM>(fb[A1], c, s2, P, b1l, b1r);
     recon_face<T, R_PDM>(fb[A2], c, s1, P, b2l, b2r);
-    const T v1av = vav[0], v2av = vav[1];
     T b1u = (v2av >= T(0)) ? b1l : b1r;
     T b2u = (v1av >= T(0)) ? b2l : b2r;
     T ee = -v1av * b2u + v2av * b1u;
@@ -1364,8 +1414,14 @@ __device__ __forceinline__ void emf_pdm_tile(const Dev<T>& d, const Inp<T>& in, 
   }
 }
 
+// Register budget of the single-grid EMF tiles: 1 = full occupancy (2048 / NT
+// resident blocks' worth of registers), 0 = the compiler's choice.
+#ifndef MHD_EMF_FULL_OCC
+#define MHD_EMF_FULL_OCC 1
+#endif
 template <typename T, int E, int TX, int TY, int TZ, int NT, bool M, bool B>
-__global__ void __launch_bounds__(NT) k_emf_pdm(KArg<T, B> ka, Inp<T> in0, Prm<T> P) {
+__global__ void __launch_bounds__(NT, (B || !MHD_EMF_FULL_OCC) ? 1 : 2048 / NT)
+    k_emf_pdm(KArg<T, B> ka, Inp<T> in0, Prm<T> P) {
   const int4 bb = ka.blk();
   const auto& d = ka.dev(bb);
   const Inp<T> in = B ? state_view(d) : in0;
