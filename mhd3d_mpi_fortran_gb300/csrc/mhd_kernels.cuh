@@ -1414,13 +1414,19 @@ __device__ __forceinline__ void emf_pdm_tile(const Dev<T>& d, const Inp<T>& in, 
   }
 }
 
-// Register budget of the single-grid EMF tiles: 1 = full occupancy (2048 / NT
-// resident blocks' worth of registers), 0 = the compiler's choice.
+// Register budgets of the EMF tiles (resident threads per SM the allocator
+// must allow): single grid 2048 (full occupancy); batched 1536 for the plane
+// tiles and 1024 for ei, whose shared memory allows 2 blocks anyway (the
+// batched kernels carry a grid-table lookup and spill at 32 registers).
+// MHD_EMF_FULL_OCC=0 leaves every budget to the compiler.
 #ifndef MHD_EMF_FULL_OCC
 #define MHD_EMF_FULL_OCC 1
 #endif
+constexpr int emf_min_blocks(int E, int NT, bool B) {
+  return !MHD_EMF_FULL_OCC ? 1 : !B ? 2048 / NT : (E == 0 ? 1024 / NT : 1536 / NT);
+}
 template <typename T, int E, int TX, int TY, int TZ, int NT, bool M, bool B>
-__global__ void __launch_bounds__(NT, (B || !MHD_EMF_FULL_OCC) ? 1 : 2048 / NT)
+__global__ void __launch_bounds__(NT, emf_min_blocks(E, NT, B))
     k_emf_pdm(KArg<T, B> ka, Inp<T> in0, Prm<T> P) {
   const int4 bb = ka.blk();
   const auto& d = ka.dev(bb);
