@@ -1096,9 +1096,13 @@ constexpr int SWEEP_SEG = MHD_SWEEP_SEG;  // cells per column segment (compile-t
 #define MHD_SWEEP_UNROLL 1
 #endif
 constexpr int kSweepUnroll = MHD_SWEEP_UNROLL;  // face-loop unroll (compile-time knob)
+#ifndef MHD_SWEEP_MINB
+#define MHD_SWEEP_MINB 4
+#endif
+constexpr int kSweepMinB = MHD_SWEEP_MINB;  // resident 128-thread blocks per SM (register budget)
 
 template <typename T, int D, bool B>
-__global__ void __launch_bounds__(128, 4)
+__global__ void __launch_bounds__(128, kSweepMinB)
     k_flux_sweep(KArg<T, B> ka, Inp<T> in0, Prm<T> P, int form, T cw, T den) {
   const int4 bb = ka.blk();
   const auto& d = ka.dev(bb);
