@@ -185,6 +185,22 @@ def cpu_rate(n, steps, recon=1):
     return n ** 3 * steps / dt, dt, threads()
 
 
+def cpu_detail(recon=1):
+    """The oracle on all host threads and on one, at 64^3 (2 RK2 steps each)
+    and at 256^3 on all threads (1 step): the rates the reference's own CPU
+    path would be compared at."""
+    from oracle.oracle import threads, set_threads
+    allt = threads()
+    rows = []
+    for n, steps, t in ((64, 2, allt), (64, 2, 1), (256, 1, allt)):
+        set_threads(t)
+        v, dt, cores = cpu_rate(n, steps, recon)
+        rows.append({"grid": n, "steps": steps, "cores": cores, "value": v, "unit": "zone-updates/s",
+                     "seconds": dt})
+    set_threads(allt)
+    return rows
+
+
 def run_reference(a):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -296,7 +312,8 @@ def run_ours(a):
     if not a.no_cpu_baseline and rank == 0 and ws == 1:
         v, dt, cores = cpu_rate(160, 8, a.recon)
         cpu = {"value": v, "unit": "zone-updates/s", "cores": cores, "kind": "port",
-               "sample": f"8 RK2 steps of the 160^3 turbulence state (same generator), PDM, FP64 oracle, {dt:.1f} s"}
+               "sample": f"8 RK2 steps of the 160^3 turbulence state (same generator), PDM, FP64 oracle, {dt:.1f} s",
+               "detail": cpu_detail(a.recon)}
     if rank != 0:
         return
     compute_roofs = roofs(zu / ws, clocks, a.recon, tiles)

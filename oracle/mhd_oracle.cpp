@@ -1417,4 +1417,9 @@ void oracle_free(void* h) { delete (Oracle*)h; }
 
 int oracle_threads(void) { return omp_get_max_threads(); }
 
+// Thread count of the following oracle calls (n <= 0: leave it unchanged).
+void oracle_set_threads(int n) {
+  if (n > 0) omp_set_num_threads(n);
+}
+
 }  // extern "C"

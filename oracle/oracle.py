@@ -48,12 +48,18 @@ def load():
         lib.oracle_diagnostics.argtypes = [C.c_void_p, _DP]
         lib.oracle_recon_line.argtypes = [C.POINTER(CParams), C.c_int, _DP, _DP, _DP]
         lib.oracle_free.argtypes = [C.c_void_p]
+        lib.oracle_set_threads.argtypes = [C.c_int]
         _lib = lib
     return _lib
 
 
 def threads() -> int:
     return load().oracle_threads()
+
+
+def set_threads(n: int) -> None:
+    """OpenMP thread count of the following oracle calls."""
+    load().oracle_set_threads(int(n))
 
 
 def _ptr(a):
