@@ -1804,19 +1804,77 @@ __global__ void k_fill(Dev<T> d) {
 // exactly the values the separate fill followed by get_bxyz produces.  The
 // per-axis image of every index comes from d.gmap (ghost_src tabulated at
 // set-up): cell maps of x, y, z then face maps of x, y, z, each padded to n+2.
+//
+// Launch layout (256 threads per block, block index bb.y): first the interior
+// tiles, 32 x 8 cells of one z plane each, which take the fast path with no
+// divergence; then the shell, every (i <= nx, j <= ny, k <= nz) outside the
+// interior box, 256 elements per block in a flattened order (the z slabs,
+// then the y slabs, then the x slabs of the remaining rows).
+struct FillShape {
+  int nbx, nby, nint, nshell;
+  __host__ __device__ FillShape(const Geom& g)
+      : nbx((g.nx0 + 31) / 32), nby((g.ny0 + 7) / 8), nint(nbx * nby * g.nz0),
+        nshell((g.nz + 1 - g.nz0) * (g.ny + 1) * (g.nx + 1) + g.nz0 * (g.ny + 1 - g.ny0) * (g.nx + 1) +
+               g.nz0 * g.ny0 * (g.nx + 1 - g.nx0)) {}
+  __host__ __device__ int blocks() const { return nint + (nshell + 255) / 256; }
+};
+
+// (i, j, k) of shell element u (0 <= u < nshell)
+__device__ __forceinline__ void fill_shell_ijk(const Geom& g, int u, int& i, int& j, int& k) {
+  const int X = g.nx + 1, Y = g.ny + 1, Z = g.nz + 1;
+  const int a = (Z - g.nz0) * Y * X;
+  if (u < a) {  // k outside the interior
+    const int kk = u / (Y * X), r = u - kk * (Y * X);
+    k = kk < g.ng ? kk : kk + g.nz0;
+    j = r / X;
+    i = r - j * X;
+    return;
+  }
+  u -= a;
+  const int yb = (Y - g.ny0) * X, b = g.nz0 * yb;
+  if (u < b) {  // k inside, j outside
+    const int kk = u / yb, r = u - kk * yb;
+    k = g.ng + kk;
+    const int jj = r / X;
+    j = jj < g.ng ? jj : jj + g.ny0;
+    i = r - jj * X;
+    return;
+  }
+  u -= b;  // k, j inside, i outside
+  const int xs = X - g.nx0, xb = g.ny0 * xs;
+  const int kk = u / xb, r = u - kk * xb;
+  k = g.ng + kk;
+  const int jj = r / xs;
+  j = g.ng + jj;
+  const int ii = r - jj * xs;
+  i = ii < g.ng ? ii : ii + g.nx0;
+}
+
 template <typename T, bool M, bool B>
 __global__ void __launch_bounds__(256) k_fill_bxyz(KArg<T, B> ka, int want_vf) {
   const int4 bb = ka.blk();
   const auto& d = ka.dev(bb);
   const Geom& g = d.g;
-  const int i = bb.y * blockDim.x + threadIdx.x;
-  const int j = bb.z * blockDim.y + threadIdx.y;
-  const int k = bb.w;
-  if (i > g.nx || j > g.ny || k > g.nz) return;
+  const FillShape fs(g);
+  int i, j, k;
+  bool inner;
+  if (bb.y < fs.nint) {
+    const int bx = bb.y % fs.nbx, r = bb.y / fs.nbx, by = r % fs.nby, kz = r / fs.nby;
+    i = g.ng + bx * 32 + (threadIdx.x & 31);
+    j = g.ng + by * 8 + (threadIdx.x >> 5);
+    k = g.ng + kz;
+    if (i >= g.ng + g.nx0 || j >= g.ng + g.ny0) return;  // those cells belong to no block here
+    inner = true;
+  } else {
+    const int u = (bb.y - fs.nint) * 256 + threadIdx.x;
+    if (u >= fs.nshell) return;
+    fill_shell_ijk(g, u, i, j, k);
+    inner = false;
+  }
   const int px = g.px, pl = (int)g.plane;
   const int c = i + px * j + pl * k;
   // interior fast path (no ghost element owned, all images are the identity)
-  if (i >= g.ng && i < g.ng + g.nx0 && j >= g.ng && j < g.ng + g.ny0 && k >= g.ng && k < g.ng + g.nz0) {
+  if (inner) {
     T bx, by, bz;
     if (M) {
       cell_b_metric<T>(d.m, c, d.bi[c], d.bi[c + 1], d.bj[c], d.bj[c + px], d.bk[c], d.bk[c + pl], bx, by, bz);
@@ -2014,8 +2072,7 @@ void Launch<T, M>::bxyz_vf(const Dev<T>& d, bool want_vf, cudaStream_t st) {
 
 template <typename T, bool M>
 void Launch<T, M>::fill_bxyz(const Dev<T>& d, bool want_vf, cudaStream_t st) {
-  dim3 b(64, 4, 1);
-  k_fill_bxyz<T, M, false><<<grid3(d.g.nx + 1, d.g.ny + 1, d.g.nz + 1, b), b, 0, st>>>(one(d), want_vf ? 1 : 0);
+  k_fill_bxyz<T, M, false><<<FillShape(d.g).blocks(), 256, 0, st>>>(one(d), want_vf ? 1 : 0);
 }
 
 template <typename T, bool M>
@@ -2207,7 +2264,7 @@ dim3 Batch<T>::dims(int fam, const Geom& g, int td, int ey) {
     case BF_EMF_J: return emf_grid(1, g, 32, 1, 8);
     case BF_EMF_K: return emf_grid(2, g, 32, 8, 1);
     case BF_CT: return grid3(g.nx0 + 1, g.ny0 + 1, g.nz0 + 1, dim3(32, 4, 1));
-    default: return grid3(g.nx + 1, g.ny + 1, g.nz + 1, dim3(64, 4, 1));  // BF_FILL
+    default: return dim3(FillShape(g).blocks(), 1, 1);  // BF_FILL
   }
 }
 
@@ -2290,7 +2347,7 @@ void Batch<T>::parts(const BatchView& v, int sel, int which, int form, double c,
     k_update_b<T, false, true><<<v.nblk[BF_CT], dim3(32, 4), 0, st>>>(KArg<T, true>{tab, v.map[BF_CT]}, form, (T)c,
                                                                        (T)den);
     KArg<T, true> fa{(const Dev<T>*)v.tab[sel ^ 1], v.map[BF_FILL]};
-    k_fill_bxyz<T, false, true><<<v.nblk[BF_FILL], dim3(64, 4), 0, st>>>(fa, 1);
+    k_fill_bxyz<T, false, true><<<v.nblk[BF_FILL], 256, 0, st>>>(fa, 1);
   }
 }
 
