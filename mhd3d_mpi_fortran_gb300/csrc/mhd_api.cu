@@ -58,6 +58,8 @@ struct Handle {
   Geom g{};
   int fp32 = 0;
   cudaStream_t st = nullptr;
+  cudaStream_t st2 = nullptr;  // side stream: the EMF families run on it beside the face fluxes
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   void* buf = nullptr;
   size_t bytes = 0;
   double* geo = nullptr;       // dx | dy | dz (FP64)
@@ -166,6 +168,32 @@ Dev<T> at_par(const Dev<T>& base, int par) {
   return d;
 }
 
+// The EMF families and the face-flux kernels of a stage read the same stage
+// input and write disjoint arrays (E; F, dU and the other half of the
+// primitives), so the EMF runs on the side stream between a fork and a join
+// event while the fluxes run on st; CT, which reads both, follows the join.
+// In graph capture the fork and join become the graph's dependencies.  The
+// family recorder (profile mode) keeps one stream so that its event pairs
+// time one family each.
+template <typename T, bool M>
+void emf_and_fluxes(Handle* h, const Dev<T>& d, const Inp<T>& in, int form, double c, double den, bool ab,
+                    cudaStream_t st, Rec& R) {
+  typedef Launch<T, M> L;
+  if (R.pool || !h->st2) {
+    R.begin(); L::emf(d, in, st); R.end(3);
+    for (int part = 0; part < 3; ++part) {
+      R.begin(); L::hydro(d, in, part, form, c, den, ab, st); R.end(part);
+    }
+    return;
+  }
+  cudaEventRecord(h->ev_fork, st);
+  cudaStreamWaitEvent(h->st2, h->ev_fork, 0);
+  L::emf(d, in, h->st2);
+  for (int part = 0; part < 3; ++part) L::hydro(d, in, part, form, c, den, ab, st);
+  cudaEventRecord(h->ev_join, h->st2);
+  cudaStreamWaitEvent(st, h->ev_join, 0);
+}
+
 template <typename T, bool M>
 void enqueue_step(Handle* h, int& par, cudaStream_t st, Rec* r = nullptr) {
   typedef Launch<T, M> L;
@@ -177,10 +205,7 @@ void enqueue_step(Handle* h, int& par, cudaStream_t st, Rec* r = nullptr) {
     Dev<T> d = at_par(base, par);
     R.begin(); L::cfl(d, 2, st); L::predictor_ab(d, st); R.end(6);
     Inp<T> in = half_inp(d);
-    R.begin(); L::emf(d, in, st); R.end(3);
-    for (int part = 0; part < 3; ++part) {
-      R.begin(); L::hydro(d, in, part, -1, 0.0, 1.0, true, st); R.end(part);
-    }
+    emf_and_fluxes<T, M>(h, d, in, -1, 0.0, 1.0, true, st, R);
     R.begin(); L::ct(d, -1, 0.0, 1.0, st); R.end(4);
     par ^= 1;
     d = at_par(base, par);
@@ -204,10 +229,7 @@ void enqueue_step(Handle* h, int& par, cudaStream_t st, Rec* r = nullptr) {
     }
     Dev<T> d = at_par(base, par);
     Inp<T> in = state_inp(d);
-    R.begin(); L::emf(d, in, st); R.end(3);
-    for (int part = 0; part < 3; ++part) {
-      R.begin(); L::hydro(d, in, part, form, c, den, false, st); R.end(part);
-    }
+    emf_and_fluxes<T, M>(h, d, in, form, c, den, false, st, R);
     R.begin(); L::ct(d, form, c, den, st); R.end(4);
     par ^= 1;
     d = at_par(base, par);
@@ -532,7 +554,10 @@ static int create_handle(const mhd_params* prm, const double* dx, const double* 
     mhd_free(h);
     return fail(code, m);
   };
-  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess)
     return bail(MHD_E_CUDA, "stream create failed");
   if (cudaMalloc(&h->buf, h->bytes) != cudaSuccess) return bail(MHD_E_NOMEM, "device allocation failed");
   if (metric && cudaMalloc(&h->met, sizeof(double) * kMetricArrays * (size_t)g.vol) != cudaSuccess)
@@ -1497,6 +1522,9 @@ int mhd_free(void* handle) {
   if (h->sc_h) cudaFreeHost(h->sc_h);
   if (h->diag_h) cudaFreeHost(h->diag_h);
   if (h->st) cudaStreamDestroy(h->st);
+  if (h->st2) cudaStreamDestroy(h->st2);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
   delete h;
   return MHD_OK;
 }
