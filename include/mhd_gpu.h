@@ -40,6 +40,11 @@ enum { MHD_RECON_PDM = 1, MHD_RECON_TVD = 2, MHD_RECON_WENO5 = 3, MHD_RECON_MPWE
        MHD_RECON_TVD_MC = 5 };
 /* stepop values (mhd3d3.f90:3585-3600) */
 enum { MHD_STEP_AB2 = 1, MHD_STEP_RK2 = 2, MHD_STEP_RK3 = 3 };
+/* Edge EMF: MHD_EMF_LFM is get_eijk_LFM, the one the reference calls
+ * (mhd3d3.f90:1754-1856); MHD_EMF_YEE is get_eijk_Yee (1654-1752, with
+ * get_v_center 2562-2592), whose calls the reference keeps commented out
+ * (3354, 3621).  Yee runs on Cartesian meshes only. */
+enum { MHD_EMF_LFM = 0, MHD_EMF_YEE = 1 };
 /* per-axis boundary kinds */
 enum { MHD_BC_PERIODIC = 0,   /* periodic Cartesian topology (mhd3d2.f90:3063-3064) */
        MHD_BC_EVEN = 1,       /* even mirror of every variable (mhd3d3.f90:781-819, bc=0) */
@@ -78,7 +83,8 @@ typedef struct mhd_params {
   double gam;              /* 5/3 in the reference (mhd3d3.f90:51) */
   double cfl, pdmb, eps, alpha, beta;   /* namelist `free` (mhd3d3.f90:91,156) */
   double tau;              /* deck tau (namelist `list`); AB priming dt if > 0 */
-  int32_t reserved[8];
+  int32_t emf;             /* MHD_EMF_*: edge EMF scheme */
+  int32_t reserved[7];
 } mhd_params;
 
 /* Create a solver on the current CUDA device from the driver's initialised

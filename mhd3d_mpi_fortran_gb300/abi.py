@@ -19,6 +19,7 @@ STEP_AB2, STEP_RK2, STEP_RK3 = 1, 2, 3
 BC_PERIODIC, BC_EVEN, BC_REFLECT, BC_OUTFLOW = 0, 1, 2, 3
 FP64, FP32 = 0, 1
 DT_REFERENCE, DT_CFL = 0, 1
+EMF_LFM, EMF_YEE = 0, 1
 ST_NAN, ST_NEG_RHO, ST_NEG_P, ST_CFL, ST_TIMEOUT, ST_CUDA_ERROR = 1, 2, 4, 8, 16, 32
 E_OK, E_ARG, E_CUDA, E_NOMEM, E_TIMEOUT, E_STATE = 0, -1, -2, -3, -4, -5
 
@@ -41,7 +42,7 @@ class CParams(C.Structure):
         ("tvd_shift", C.c_int32),
         ("gam", C.c_double), ("cfl", C.c_double), ("pdmb", C.c_double), ("eps", C.c_double),
         ("alpha", C.c_double), ("beta", C.c_double), ("tau", C.c_double),
-        ("reserved", C.c_int32 * 8),
+        ("emf", C.c_int32), ("reserved", C.c_int32 * 7),
     ]
 
 
@@ -69,6 +70,7 @@ class Params:
     alpha: float = 2.0
     beta: float = 4.0
     tau: float = 2.0e-4
+    emf: int = EMF_LFM
 
     @property
     def ng(self) -> int:

@@ -293,6 +293,8 @@ void carve(Handle* h, Dev<T>& d, char* base) {
     d.mw[a] = h->metric ? next() : nullptr;
     d.mbn[a] = h->metric ? next() : nullptr;
   }
+  d.emf = h->prm.emf;
+  for (int q = 0; q < 12; ++q) d.ye[q] = (h->prm.emf == MHD_EMF_YEE) ? next() : nullptr;
   if (h->metric) {
     const double* mb = h->met;
     auto nm = [&]() { const double* r = mb; mb += n; return r; };
@@ -334,7 +336,8 @@ MetricOut metric_out(Handle* h) {
 }
 
 size_t n_arrays(const mhd_params& p, bool metric) {
-  size_t n = 11 + 5 + 8 + ((p.stepop == MHD_STEP_AB2) ? 22 : 8) + 24 + 3 + 1 + (metric ? 6 : 0);
+  size_t n = 11 + 5 + 8 + ((p.stepop == MHD_STEP_AB2) ? 22 : 8) + 24 + 3 + 1 + (metric ? 6 : 0) +
+             ((p.emf == MHD_EMF_YEE) ? 12 : 0);
   return n;
 }
 
@@ -464,6 +467,7 @@ int validate(const mhd_params* p) {
   if (p->nord <= 0 || (p->nord & 1)) return fail(MHD_E_ARG, "nord must be even and positive");
   if (p->reconop < 1 || p->reconop > 5) return fail(MHD_E_ARG, "reconop must be 1..5");
   if (p->stepop < 1 || p->stepop > 3) return fail(MHD_E_ARG, "stepop must be 1..3");
+  if (p->emf != MHD_EMF_LFM && p->emf != MHD_EMF_YEE) return fail(MHD_E_ARG, "emf must be 0 (LFM) or 1 (Yee)");
   int need = (p->reconop == 1) ? 8 : (p->reconop == 3 || p->reconop == 4) ? 6 : 4;
   if (p->nord < need) return fail(MHD_E_ARG, "nord too small for the reconstruction stencil");
   int ng = p->nord / 2;
@@ -680,6 +684,7 @@ int mhd_init_mapped(const mhd_params* prm, const double* rho, const double* vx, 
   *handle = nullptr;
   int rc = validate(prm);
   if (rc) return rc;
+  if (prm->emf == MHD_EMF_YEE) return fail(MHD_E_ARG, "the Yee EMF runs on Cartesian meshes only");
   if (!rho || !vx || !vy || !vz || !p || !phi_i || !phi_j || !phi_k || !xn || !yn || !zn)
     return fail(MHD_E_ARG, "null field pointer");
   const int nx = prm->nx0 + prm->nord, ny = prm->ny0 + prm->nord, nz = prm->nz0 + prm->nord;
@@ -1117,13 +1122,14 @@ struct BatchBufs {
 // Cartesian, PDM, the same RK stepper, dt mode and limiter constants.
 static bool batchable(Handle* const* hs, int n) {
   const mhd_params& a = hs[0]->prm;
-  if (hs[0]->metric || a.reconop != MHD_RECON_PDM || (a.stepop != MHD_STEP_RK2 && a.stepop != MHD_STEP_RK3))
+  if (hs[0]->metric || a.reconop != MHD_RECON_PDM || a.emf != MHD_EMF_LFM ||
+      (a.stepop != MHD_STEP_RK2 && a.stepop != MHD_STEP_RK3))
     return false;
   for (int i = 1; i < n; ++i) {
     const mhd_params& b = hs[i]->prm;
     if (hs[i]->metric || hs[i]->fp32 != hs[0]->fp32 || b.reconop != a.reconop || b.stepop != a.stepop ||
         b.dt_mode != a.dt_mode || b.pdmb != a.pdmb || b.eps != a.eps || b.alpha != a.alpha || b.beta != a.beta ||
-        b.tvd_shift != a.tvd_shift)
+        b.tvd_shift != a.tvd_shift || b.emf != a.emf)
       return false;
   }
   return true;

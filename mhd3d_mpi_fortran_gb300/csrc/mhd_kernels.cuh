@@ -27,6 +27,11 @@ namespace mhd {
 
 enum { R_PDM = 1, R_TVD = 2, R_WENO = 3, R_MPWENO = 4, R_TVDMC = 5 };
 enum { BC_PERIODIC = 0, BC_EVEN = 1, BC_REFLECT = 2, BC_OUTFLOW = 3 };
+enum { EMF_LFM = 0, EMF_YEE = 1 };
+
+inline dim3 grid3(int ni, int nj, int nk, dim3 b) {
+  return dim3((ni + b.x - 1) / b.x, (nj + b.y - 1) / b.y, nk);
+}
 enum { ST_NAN = 1u, ST_NEG_RHO = 2u, ST_NEG_P = 4u, ST_CFL = 8u };
 
 // ---------------------------------------------------------------- scalar ops
@@ -2053,9 +2058,6 @@ __global__ void k_min_rho(Dev<T> d, double* out) {
 }
 
 // ---------------------------------------------------------------- launchers
-inline dim3 grid3(int ni, int nj, int nk, dim3 b) {
-  return dim3((ni + b.x - 1) / b.x, (nj + b.y - 1) / b.y, nk);
-}
 
 template <typename T>
 Prm<T> prm_of(const Dev<T>& d) {
@@ -2181,6 +2183,112 @@ void Launch<T, M>::hydro(const Dev<T>& d, const Inp<T>& in, int part, int form, 
   }
 }
 
+// ------------------------------------------------------------- Yee EMF
+// get_eijk_Yee (mhd3d3.f90:1654-1752).  First the 12 split electric fields
+// of every cell, ghosts included, from the Gaussian moments of get_v_center
+// (2562-2592, the get_v_face element formula):
+//   ez_ab = bx vx0a vy1b - by vx1a vy0b, ex_ab = by vy0a vz1b - bz vy1a vz0b,
+//   ey_ab = bz vz0a vx1b - bx vz1a vx0b   (a, b = + / - moments),
+// stored as ye[f * 4 + s], f = x, y, z edges, s = pp, np, pn, nn.
+template <typename T>
+__global__ void k_yee_split(Dev<T> d, Inp<T> in) {
+  const Geom& g = d.g;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+  const int c = i + g.px * (j + g.py * k);
+  const T bxc = in.bx[c], byc = in.by[c], bzc = in.bz[c];
+  const T bsq = bxc * bxc + byc * byc + bzc * bzc;
+  const T lam = Ops<T>::dv(in.rho[c], T(2) * in.p[c] + bsq);
+  T x0p, x0n, x1p, x1n, y0p, y0n, y1p, y1n, z0p, z0n, z1p, z1n;
+  Moments<T>::hydro(lam, in.vx[c], true, x0p, x1p);
+  Moments<T>::hydro(lam, in.vx[c], false, x0n, x1n);
+  Moments<T>::hydro(lam, in.vy[c], true, y0p, y1p);
+  Moments<T>::hydro(lam, in.vy[c], false, y0n, y1n);
+  Moments<T>::hydro(lam, in.vz[c], true, z0p, z1p);
+  Moments<T>::hydro(lam, in.vz[c], false, z0n, z1n);
+  d.ye[0][c] = byc * y0p * z1p - bzc * y1p * z0p;
+  d.ye[1][c] = byc * y0n * z1p - bzc * y1n * z0p;
+  d.ye[2][c] = byc * y0p * z1n - bzc * y1p * z0n;
+  d.ye[3][c] = byc * y0n * z1n - bzc * y1n * z0n;
+  d.ye[4][c] = bzc * z0p * x1p - bxc * z1p * x0p;
+  d.ye[5][c] = bzc * z0n * x1p - bxc * z1n * x0p;
+  d.ye[6][c] = bzc * z0p * x1n - bxc * z1p * x0n;
+  d.ye[7][c] = bzc * z0n * x1n - bxc * z1n * x0n;
+  d.ye[8][c] = bxc * x0p * y1p - byc * x1p * y0p;
+  d.ye[9][c] = bxc * x0n * y1p - byc * x1n * y0p;
+  d.ye[10][c] = bxc * x0p * y1n - byc * x1p * y0n;
+  d.ye[11][c] = bxc * x0n * y1n - byc * x1n * y0n;
+}
+
+// Then, per edge of family E, each split field is reconstructed to the edge
+// in two passes -- along axis DA to the edge's DA face (first index of the
+// field), at the rows of the DB stencil, then along DB to its DB face (second
+// index) -- taking the left state for a + moment and the right one for a -
+// moment; the edge EMF is epp + enp + epn + enn.  ei: y then z, ej: z then x,
+// ek: x then y (reconstruct_3d dirs 5/6, 6/4, 4/5).  Only the rows the
+// second pass reads are reconstructed in the first.
+template <typename T, int RECON, int E>
+__global__ void k_emf_yee(Dev<T> d, Prm<T> P) {
+  const Geom& g = d.g;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + g.ng;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + g.ng;
+  const int k = blockIdx.z + g.ng;
+  const int ni = g.nx0 + (E != 0), nj = g.ny0 + (E != 1), nk = g.nz0 + (E != 2);
+  if (i >= g.ng + ni || j >= g.ng + nj || k >= g.ng + nk) return;
+  const int c = i + g.px * (j + g.py * k);
+  const int st[3] = {1, g.px, (int)g.plane};
+  constexpr int DA = (E == 0) ? 1 : (E == 1) ? 2 : 0;
+  constexpr int DB = (E == 0) ? 2 : (E == 1) ? 0 : 1;
+  const int sA = st[DA], sB = st[DB];
+  constexpr bool TV = (RECON == R_TVD || RECON == R_TVDMC);
+  constexpr int M0 = (RECON == R_PDM) ? 0 : TV ? 2 : 1;
+  constexpr int M1 = (RECON == R_PDM) ? 7 : TV ? 5 : 6;
+  T part[4];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {  // pp, np, pn, nn
+    const T* f = d.ye[E * 4 + s];
+    const bool left1 = (s == 0 || s == 2), left2 = (s < 2);
+    T q[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      q[m] = T(0);
+      if (m >= M0 && m <= M1) {
+        T l, r;
+        recon_face<T, RECON>(f, c + (m - 4) * sB, sA, P, l, r);
+        q[m] = left1 ? l : r;
+      }
+    }
+    T l, r;
+    recon_win<T, RECON, 0>(q, P, l, r);
+    part[s] = left2 ? l : r;
+  }
+  d.E[E][c] = part[0] + part[1] + part[2] + part[3];
+}
+
+template <typename T, int RECON>
+void emf_yee_r(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
+  const Prm<T> P = prm_of(d);
+  const Geom& g = d.g;
+  const dim3 b(32, 4, 1);
+  k_yee_split<T><<<grid3(g.nx, g.ny, g.nz, b), b, 0, st>>>(d, in);
+  k_emf_yee<T, RECON, 0><<<grid3(g.nx0, g.ny0 + 1, g.nz0 + 1, b), b, 0, st>>>(d, P);
+  k_emf_yee<T, RECON, 1><<<grid3(g.nx0 + 1, g.ny0, g.nz0 + 1, b), b, 0, st>>>(d, P);
+  k_emf_yee<T, RECON, 2><<<grid3(g.nx0 + 1, g.ny0 + 1, g.nz0, b), b, 0, st>>>(d, P);
+}
+
+template <typename T>
+void emf_yee(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
+  switch (d.recon) {
+    case R_PDM: emf_yee_r<T, R_PDM>(d, in, st); break;
+    case R_TVD: emf_yee_r<T, R_TVD>(d, in, st); break;
+    case R_WENO: emf_yee_r<T, R_WENO>(d, in, st); break;
+    case R_MPWENO: emf_yee_r<T, R_MPWENO>(d, in, st); break;
+    default: emf_yee_r<T, R_TVDMC>(d, in, st); break;
+  }
+}
+
 // ei tiles of 32 (FP32) or 16 (FP64) edges x 4 x 4; ej, ek plane tiles of 32 x 8.
 template <typename T, int RECON, bool M>
 void emf_weno(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
@@ -2210,6 +2318,10 @@ template <> struct EiTile<double> { static constexpr int Y = 4; };
 
 template <typename T, bool M>
 void Launch<T, M>::emf(const Dev<T>& d, const Inp<T>& in0, cudaStream_t st) {
+  if (!M && d.emf == EMF_YEE) {  // Cartesian only (checked at mhd_init)
+    emf_yee<T>(d, in0, st);
+    return;
+  }
   Inp<T> in = in0;
   if (M) {
     // normal velocities and face-normal field of the stage input, in the

@@ -102,6 +102,8 @@ struct Dev {
   // launch shapes (host side only): y/z face-tile length and ei EMF tile,
   // chosen by the autotuner for the FP32 Cartesian PDM path
   int tile_td, tile_ey;
+  int emf;           // edge EMF scheme: 0 LFM, 1 Yee
+  T* ye[12];         // Yee split electric fields, [x, y, z edges][pp, np, pn, nn] (emf = 1)
 };
 
 // Stage-input view: which arrays feed the EMF and flux kernels (RK: the

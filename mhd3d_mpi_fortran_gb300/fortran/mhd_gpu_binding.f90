@@ -20,7 +20,8 @@ module mhd_gpu_binding
       integer(c_int32_t) :: precision, dt_mode, tvd_shift
       real(c_double)     :: gam, cfl, pdmb, eps, alpha, beta
       real(c_double)     :: tau
-      integer(c_int32_t) :: reserved(8)
+      integer(c_int32_t) :: emf
+      integer(c_int32_t) :: reserved(7)
    end type mhd_params
 
    interface
@@ -79,7 +80,7 @@ contains
       prm%nord = nord; prm%reconop = reconop; prm%stepop = stepop
       prm%bc = bcs; prm%precision = prec; prm%dt_mode = 0; prm%tvd_shift = 0
       prm%gam = gam; prm%cfl = cfl; prm%pdmb = pdmb; prm%eps = eps
-      prm%alpha = alpha; prm%beta = beta; prm%tau = tau; prm%reserved = 0
+      prm%alpha = alpha; prm%beta = beta; prm%tau = tau; prm%emf = 0; prm%reserved = 0
       rc = mhd_init(prm, rho, vx, vy, vz, p, bi, bj, bk, dx, dy, dz, gpu_handle)
       if (rc /= 0) stop 'mhd_init failed'
    end subroutine gpu_init

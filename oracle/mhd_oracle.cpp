@@ -61,7 +61,7 @@ inline double fmin2(double a, double b) { return (a < b) ? a : b; }
 
 struct Oracle {
   // pars (mhd3d3.f90:33-104)
-  int nx0, ny0, nz0, nord, ng, nx, ny, nz, reconop, stepop, bc[3], dt_mode, tvd_shift;
+  int nx0, ny0, nz0, nord, ng, nx, ny, nz, reconop, stepop, bc[3], dt_mode, tvd_shift, emf = 0;
   double gam, cfl, pdmb, eps, alpha, beta, tau, tau0, pi;
   std::vector<double> dxv, dyv, dzv;  // dxblock(i,j,k) = dxv[i-1]
   // fields (mhd3d3.f90:251-283)
@@ -639,6 +639,68 @@ struct Oracle {
     }
   }
 
+  // get_eijk_Yee (mhd3d3.f90:1654-1752) with get_v_center (2562-2592, the
+  // element formula of get_v_face): split electric fields of the Gaussian
+  // velocity moments of every cell, each reconstructed to the edges in two
+  // passes -- the left face state for a + moment, the right one for a -
+  // moment -- and summed.  The reference keeps its calls commented out
+  // (3354, 3621); emf = MHD_EMF_YEE selects it here.
+  void get_eijk_Yee(const A3& lrho, const A3& lvx, const A3& lvy, const A3& lvz, const A3& lp,
+                    const A3& lbx, const A3& lby, const A3& lbz) {
+    A3 e[3][4];  // [x, y, z][pp, np, pn, nn]
+    for (int f = 0; f < 3; ++f)
+      for (int q = 0; q < 4; ++q) e[f][q].alloc(nx, ny, nz);
+    FOR3(nx, ny, nz) {
+      const double bxc = lbx(i, j, k), byc = lby(i, j, k), bzc = lbz(i, j, k);
+      const double bsq = bxc * bxc + byc * byc + bzc * bzc;
+      const double lam = lrho(i, j, k) / (2. * lp(i, j, k) + bsq);
+      double x0p, x0n, x1p, x1n, y0p, y0n, y1p, y1n, z0p, z0n, z1p, z1n;
+      v_face(lam, lvx(i, j, k), x0p, x0n, x1p, x1n);
+      v_face(lam, lvy(i, j, k), y0p, y0n, y1p, y1n);
+      v_face(lam, lvz(i, j, k), z0p, z0n, z1p, z1n);
+      e[2][0](i, j, k) = bxc * x0p * y1p - byc * x1p * y0p;
+      e[2][1](i, j, k) = bxc * x0n * y1p - byc * x1n * y0p;
+      e[2][2](i, j, k) = bxc * x0p * y1n - byc * x1p * y0n;
+      e[2][3](i, j, k) = bxc * x0n * y1n - byc * x1n * y0n;
+      e[0][0](i, j, k) = byc * y0p * z1p - bzc * y1p * z0p;
+      e[0][1](i, j, k) = byc * y0n * z1p - bzc * y1n * z0p;
+      e[0][2](i, j, k) = byc * y0p * z1n - bzc * y1p * z0n;
+      e[0][3](i, j, k) = byc * y0n * z1n - bzc * y1n * z0n;
+      e[1][0](i, j, k) = bzc * z0p * x1p - bxc * z1p * x0p;
+      e[1][1](i, j, k) = bzc * z0n * x1p - bxc * z1n * x0p;
+      e[1][2](i, j, k) = bzc * z0p * x1n - bxc * z1p * x0n;
+      e[1][3](i, j, k) = bzc * z0n * x1n - bxc * z1n * x0n;
+    }
+    // family kkk: first pass along d1 over (l1), second along d2 over (l2)
+    for (int kkk = 1; kkk <= 3; ++kkk) {
+      int d1, d2, l1[3], l2[3], oe[3];
+      if (kkk == 1) {
+        d1 = 5; d2 = 6; l1[0] = nx; l1[1] = ny0 + 1; l1[2] = nz; l2[0] = nx; l2[1] = ny0 + 1; l2[2] = nz0 + 1;
+      } else if (kkk == 2) {
+        d1 = 6; d2 = 4; l1[0] = nx; l1[1] = ny; l1[2] = nz0 + 1; l2[0] = nx0 + 1; l2[1] = ny; l2[2] = nz0 + 1;
+      } else {
+        d1 = 4; d2 = 5; l1[0] = nx0 + 1; l1[1] = ny; l1[2] = nz; l2[0] = nx0 + 1; l2[1] = ny0 + 1; l2[2] = nz;
+      }
+      A3* F = e[kkk - 1];
+      A3 qpp, qpn, qnp, qnn, dum;
+      reconstruct_3d(qpp, dum, F[0], l1[0], l1[1], l1[2], d1);
+      reconstruct_3d(qpn, dum, F[2], l1[0], l1[1], l1[2], d1);
+      reconstruct_3d(dum, qnn, F[3], l1[0], l1[1], l1[2], d1);
+      reconstruct_3d(dum, qnp, F[1], l1[0], l1[1], l1[2], d1);
+      A3 epp, enp, enn, epn, d2m;
+      reconstruct_3d(epp, d2m, qpp, l2[0], l2[1], l2[2], d2);
+      reconstruct_3d(enp, d2m, qnp, l2[0], l2[1], l2[2], d2);
+      reconstruct_3d(d2m, enn, qnn, l2[0], l2[1], l2[2], d2);
+      reconstruct_3d(d2m, epn, qpn, l2[0], l2[1], l2[2], d2);
+      oe[0] = (kkk == 1) ? ng : 0; oe[1] = (kkk == 2) ? ng : 0; oe[2] = (kkk == 3) ? ng : 0;
+      A3& E = (kkk == 1) ? ei : (kkk == 2) ? ej : ek;
+      E.alloc(kkk == 1 ? nx0 : nx0 + 1, kkk == 2 ? ny0 : ny0 + 1, kkk == 3 ? nz0 : nz0 + 1);
+      FOR3(E.n1, E.n2, E.n3) {
+        const int a = i + oe[0], b = j + oe[1], c = k + oe[2];
+        E(i, j, k) = epp(a, b, c) + enp(a, b, c) + epn(a, b, c) + enn(a, b, c);
+      }
+    }
+  }
   // get_v_face (mhd3d3.f90:2594-2615), element form
   inline void v_face(double llam, double lv, double& v0p, double& v0n, double& v1p, double& v1n) const {
     double a = std::sqrt(llam);
@@ -848,9 +910,15 @@ struct Oracle {
     return (xp + c * x) / den;
   }
 
+  void edge_emf(const A3& lrho, const A3& lvx, const A3& lvy, const A3& lvz, const A3& lp, const A3& lbx,
+                const A3& lby, const A3& lbz, const A3& lbi, const A3& lbj, const A3& lbk) {
+    if (emf == MHD_EMF_YEE) get_eijk_Yee(lrho, lvx, lvy, lvz, lp, lbx, lby, lbz);
+    else get_eijk_LFM(lrho, lvx, lvy, lvz, lp, lbx, lby, lbz, lbi, lbj, lbk);
+  }
+
   void rk_stage(int s, int nst) {
     get_conserve();
-    get_eijk_LFM(rho, vx, vy, vz, p, bx, by, bz, bi, bj, bk);
+    edge_emf(rho, vx, vy, vz, p, bx, by, bz, bi, bj, bk);
     get_flux_stress(rho, vx, vy, vz, p, bx, by, bz);
     advance_corrector1();
     int form = -1; double c = 0, den = 1;
@@ -1214,7 +1282,7 @@ struct Oracle {
       get_conserve();
       advance_predictor_ab();
       tau0 = tau;
-      get_eijk_LFM(rhoh, vxh, vyh, vzh, ph, bxh, byh, bzh, bih, bjh, bkh);
+      edge_emf(rhoh, vxh, vyh, vzh, ph, bxh, byh, bzh, bih, bjh, bkh);
       get_flux_stress(rhoh, vxh, vyh, vzh, ph, bxh, byh, bzh);
       advance_corrector1();
       advance_corrector2();
@@ -1292,7 +1360,7 @@ static void* init_common(const mhd_params* prm, const double* rho, const double*
   o->nx = o->nx0 + o->nord; o->ny = o->ny0 + o->nord; o->nz = o->nz0 + o->nord;
   o->reconop = prm->reconop; o->stepop = prm->stepop;
   for (int a = 0; a < 3; ++a) o->bc[a] = prm->bc[a];
-  o->dt_mode = prm->dt_mode; o->tvd_shift = prm->tvd_shift;
+  o->dt_mode = prm->dt_mode; o->tvd_shift = prm->tvd_shift; o->emf = prm->emf;
   o->gam = prm->gam; o->cfl = prm->cfl; o->pdmb = prm->pdmb; o->eps = prm->eps;
   o->alpha = prm->alpha; o->beta = prm->beta;
   o->pi = 4.0 * std::atan(1.0);
@@ -1386,7 +1454,7 @@ int oracle_fluxes(void* h, double* out) {
 
 int oracle_emf(void* h, double* ei, double* ej, double* ek) {
   Oracle* o = (Oracle*)h;
-  o->get_eijk_LFM(o->rho, o->vx, o->vy, o->vz, o->p, o->bx, o->by, o->bz, o->bi, o->bj, o->bk);
+  o->edge_emf(o->rho, o->vx, o->vy, o->vz, o->p, o->bx, o->by, o->bz, o->bi, o->bj, o->bk);
   copy_out(o->ei, ei); copy_out(o->ej, ej); copy_out(o->ek, ek);
   return 0;
 }

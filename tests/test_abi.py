@@ -49,7 +49,7 @@ def test_params_layout_matches_c():
 int main(void){
   printf("%zu %zu %zu %zu %zu %zu\n", sizeof(mhd_params), offsetof(mhd_params,bc),
          offsetof(mhd_params,gam), offsetof(mhd_params,tau), offsetof(mhd_params,tvd_shift),
-         offsetof(mhd_params,reserved));
+         offsetof(mhd_params,emf));
   return 0; }
 '''
     cc = shutil.which("gcc") or shutil.which("cc")
@@ -62,7 +62,7 @@ int main(void){
         subprocess.run([cc, "-I", str(ROOT / "include"), str(c), "-o", str(exe)], check=True)
         vals = list(map(int, subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()))
     assert vals == [C.sizeof(CParams), CParams.bc.offset, CParams.gam.offset, CParams.tau.offset,
-                    CParams.tvd_shift.offset, CParams.reserved.offset]
+                    CParams.tvd_shift.offset, CParams.emf.offset]
 
 
 @pytest.mark.parametrize("bad", [dict(nord=7), dict(reconop=9), dict(stepop=0), dict(nord=6, reconop=1),

@@ -377,3 +377,53 @@ def test_ensemble_autotune_then_step_equals_sequential():
         for k in FIELDS:
             assert np.array_equal(got[k], ref[k]), k
         e.close()
+
+
+# ---- Yee edge EMF (get_eijk_Yee; commented out in the reference) ----------
+@pytest.mark.parametrize("recon", RECONS)
+@pytest.mark.parametrize("shape", [(11, 12, 10), (33, 16, 8)])
+def test_yee_emf_fp64_match_oracle(recon, shape):
+    from mhd3d_mpi_fortran_gb300.abi import EMF_YEE
+    s = rand_state(*shape, seed=20 + recon)
+    prm = Params(*shape, reconop=recon, emf=EMF_YEE, tau=1e-3)
+    with MHDSolver(prm, s) as gpu:
+        eg = gpu.debug_emf()
+    eo = OracleSolver(prm, s).emf()
+    for e in range(3):
+        assert relmax(eg[e], eo[e]) <= 1e-13, e
+
+
+@pytest.mark.parametrize("stepop", [STEP_AB2, STEP_RK2, STEP_RK3])
+@pytest.mark.parametrize("recon", [1, 4])
+def test_yee_steps_fp64_match_oracle(stepop, recon):
+    from mhd3d_mpi_fortran_gb300.abi import EMF_YEE
+    s = ics.orszag_tang_3d(12, seed=7, ny0=10, nz0=9)
+    prm = Params(12, 10, 9, reconop=recon, stepop=stepop, emf=EMF_YEE, tau=0.4 * ics.cfl_dt(s))
+    with MHDSolver(prm, s) as gpu:
+        tg, sg = gpu.step(4)
+        fg = gpu.fetch()
+        dg = gpu.diagnostics()
+    o = OracleSolver(prm, s)
+    to, so = o.step(4)
+    fo = o.fetch()
+    assert tg == pytest.approx(to, rel=1e-13) and sg == so
+    for k in FIELDS:
+        assert relmax(fg[k], fo[k]) <= 1e-11, k
+    assert dg["divb_max"] <= 1e-12
+
+
+def test_yee_fp32_budget_and_cartesian_only():
+    from mhd3d_mpi_fortran_gb300.abi import EMF_YEE, MHDError
+    s = ics.orszag_tang_3d(32, seed=0)
+    tau = ics.cfl_dt(s)
+    res = {}
+    for prec in (FP64, FP32):
+        with MHDSolver(Params(32, 32, 32, precision=prec, emf=EMF_YEE, tau=tau), s) as gpu:
+            gpu.step(20)
+            res[prec] = gpu.fetch()
+    for k in ("rho", "p", "vx", "bi"):
+        a, b = res[FP32][k], res[FP64][k]
+        assert np.abs(a - b).sum() / np.abs(b).sum() <= 1e-5, k
+    m = ics.mapped_blast(8)
+    with pytest.raises(MHDError):
+        MHDSolver(Params(8, 8, 8, emf=EMF_YEE, tau=0.0, stepop=STEP_AB2), m)
