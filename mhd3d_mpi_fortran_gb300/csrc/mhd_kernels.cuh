@@ -2318,9 +2318,11 @@ template <> struct EiTile<double> { static constexpr int Y = 4; };
 
 template <typename T, bool M>
 void Launch<T, M>::emf(const Dev<T>& d, const Inp<T>& in0, cudaStream_t st) {
-  if (!M && d.emf == EMF_YEE) {  // Cartesian only (checked at mhd_init)
-    emf_yee<T>(d, in0, st);
-    return;
+  if constexpr (!M) {  // Yee: Cartesian only (checked at mhd_init)
+    if (d.emf == EMF_YEE) {
+      emf_yee<T>(d, in0, st);
+      return;
+    }
   }
   Inp<T> in = in0;
   if (M) {
