@@ -302,12 +302,15 @@ def run_ours(a):
         out = sv.fetch()
         sv.close()
         el = time.perf_counter() - t0
-        vol = (n + 9) * (n + 9) * (n + 9)
-        h2d = 8 * prm.shape[0] * prm.shape[1] * prm.shape[2] * 4
-        d2h = 11 * prm.shape[0] * prm.shape[1] * prm.shape[2] * 4 + ke * 48
+        # FP64 host arrays copied as they are (the library converts on the device):
+        # 5 cell + 3 face arrays in, 8 cell + 3 face arrays out, + tau/status per step
+        nx, ny, nz = prm.shape
+        cell, faces = nx * ny * nz, (nx + 1) * ny * nz + nx * (ny + 1) * nz + nx * ny * (nz + 1)
+        h2d = 8 * (5 * cell + faces)
+        d2h = 8 * (8 * cell + faces) + ke * 48
         e2e = {"value": n ** 3 * ke / el, "unit": "zone-updates/s", "h2d_bytes_per_step": int(h2d / ke),
                "d2h_bytes_per_step": int(d2h / ke), "steps": ke, "seconds": el}
-        del out, vol
+        del out
     cpu = None
     if not a.no_cpu_baseline and rank == 0 and ws == 1:
         v, dt, cores = cpu_rate(160, 8, a.recon)

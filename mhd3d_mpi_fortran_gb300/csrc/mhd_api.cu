@@ -26,6 +26,7 @@
 #include <atomic>
 #include <map>
 #include <mutex>
+#include <unistd.h>
 
 #include "../../include/mhd_gpu.h"
 #include "mhd_state.h"
@@ -341,7 +342,7 @@ size_t n_arrays(const mhd_params& p, bool metric) {
   return n;
 }
 
-// host FP64 Fortran array (ex,ey,ez) <-> device padded T; rows in parallel
+// host FP64 Fortran array (ex,ey,ez) -> padded T on the host; rows in parallel
 template <typename T>
 void pack(const Geom& g, const double* src, int ex, int ey, int ez, T* dst) {
 #pragma omp parallel for schedule(static)
@@ -352,20 +353,33 @@ void pack(const Geom& g, const double* src, int ex, int ey, int ez, T* dst) {
       for (int i = 0; i < ex; ++i) d[i] = (T)s[i];
     }
 }
+
+// Host FP64 Fortran arrays (ex, ey, ez) <-> the padded device arrays, with the
+// conversion on the device: the FP64 array is copied as it is (pageable
+// copies run at the link rate on Grace-Blackwell, about 190 GB/s measured)
+// into the face-flux scratch, which holds no live data outside a step, and a
+// kernel converts it into (or out of) the padded layout.  Padding elements
+// are never read by the kernels; the device buffer is zeroed at allocation.
 template <typename T>
-void unpack(const Geom& g, const T* src, int ex, int ey, int ez, double* dst) {
-#pragma omp parallel for schedule(static)
-  for (int k = 0; k < ez; ++k)
-    for (int j = 0; j < ey; ++j) {
-      const T* s = src + (size_t)g.px * ((size_t)j + (size_t)g.py * k);
-      double* d = dst + (size_t)ex * ((size_t)j + (size_t)ey * k);
-      for (int i = 0; i < ex; ++i) d[i] = (double)s[i];
-    }
+__global__ void k_from_f64(const double* __restrict__ src, int ex, int ey, int px, long long plane,
+                           T* __restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y, k = blockIdx.z;
+  if (i < ex) dst[i + (long long)px * j + plane * k] = (T)src[i + (long long)ex * (j + (long long)ey * k)];
+}
+template <typename T>
+__global__ void k_to_f64(const T* __restrict__ src, int ex, int ey, int px, long long plane,
+                         double* __restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y, k = blockIdx.z;
+  if (i < ex) dst[i + (long long)ex * (j + (long long)ey * k)] = (double)src[i + (long long)px * j + plane * k];
 }
 
-// Two pinned staging buffers: packing array a+1 overlaps the copy of array a.
-// Padding elements are never read by the kernels, so the device buffer
-// (zeroed at allocation) supplies them and only the extents are copied.
+template <typename T>
+double* f64_scratch(const Dev<T>& d) {
+  return reinterpret_cast<double*>(d.F[0][0]);  // 24 x vol x sizeof(T) bytes, >= one FP64 array
+}
+
 template <typename T>
 int upload(Handle* h, const double* const* arrs) {
   const Geom& g = h->g;
@@ -374,38 +388,14 @@ int upload(Handle* h, const double* const* arrs) {
   int ext[8][3] = {{g.nx, g.ny, g.nz}, {g.nx, g.ny, g.nz}, {g.nx, g.ny, g.nz}, {g.nx, g.ny, g.nz},
                    {g.nx, g.ny, g.nz}, {g.nx + 1, g.ny, g.nz}, {g.nx, g.ny + 1, g.nz},
                    {g.nx, g.ny, g.nz + 1}};
-  T* stage[2] = {nullptr, nullptr};
-  cudaEvent_t done[2];
-  CK(cudaMallocHost(&stage[0], (size_t)g.vol * sizeof(T)));
-  if (cudaMallocHost(&stage[1], (size_t)g.vol * sizeof(T)) != cudaSuccess) {
-    cudaFreeHost(stage[0]);
-    return fail(MHD_E_NOMEM, "pinned staging allocation failed");
+  double* scratch = f64_scratch(d);
+  for (int a = 0; a < 8; ++a) {
+    const int ex = ext[a][0], ey = ext[a][1], ez = ext[a][2];
+    CK(cudaMemcpyAsync(scratch, arrs[a], sizeof(double) * (size_t)ex * ey * ez, cudaMemcpyHostToDevice, h->st));
+    k_from_f64<T><<<dim3((ex + 255) / 256, ey, ez), 256, 0, h->st>>>(scratch, ex, ey, g.px, g.plane, dsts[a]);
   }
-  std::memset(stage[0], 0, (size_t)g.vol * sizeof(T));
-  std::memset(stage[1], 0, (size_t)g.vol * sizeof(T));
-  cudaEventCreateWithFlags(&done[0], cudaEventDisableTiming);
-  cudaEventCreateWithFlags(&done[1], cudaEventDisableTiming);
-  int rc = MHD_OK;
-  for (int a = 0; a < 8 && rc == MHD_OK; ++a) {
-    const int b = a & 1;
-    if (a >= 2) {
-      cudaError_t e = cudaEventSynchronize(done[b]);
-      if (e != cudaSuccess) rc = fail(MHD_E_CUDA, std::string("upload: ") + cudaGetErrorString(e));
-    }
-    if (rc) break;
-    pack<T>(g, arrs[a], ext[a][0], ext[a][1], ext[a][2], stage[b]);
-    const size_t bytes = ((size_t)ext[a][2] - 1) * g.plane * sizeof(T) +
-                         ((size_t)(ext[a][1] - 1) * g.px + ext[a][0]) * sizeof(T);
-    cudaError_t e = cudaMemcpyAsync(dsts[a], stage[b], bytes, cudaMemcpyHostToDevice, h->st);
-    if (e == cudaSuccess) e = cudaEventRecord(done[b], h->st);
-    if (e != cudaSuccess) rc = fail(MHD_E_CUDA, std::string("upload: ") + cudaGetErrorString(e));
-  }
-  if (rc == MHD_OK) rc = wait_stream(h);
-  cudaEventDestroy(done[0]);
-  cudaEventDestroy(done[1]);
-  cudaFreeHost(stage[0]);
-  cudaFreeHost(stage[1]);
-  return rc;
+  CK(cudaGetLastError());
+  return wait_stream(h);
 }
 
 template <typename T, bool M>
@@ -539,6 +529,8 @@ static int create_handle(const mhd_params* prm, const double* dx, const double* 
   h->fp32 = (prm->precision == MHD_FP32);
   h->metric = metric;
   h->tile_ey = h->fp32 ? 8 : 4;
+  // the column sweeps are the fastest face shape at production sizes (the autotuner may still pick a tile)
+  h->tile_td = (h->fp32 && !metric && prm->reconop == MHD_RECON_PDM) ? kSweepTile : 8;
   Geom& g = h->g;
   g.nx0 = prm->nx0; g.ny0 = prm->ny0; g.nz0 = prm->nz0;
   g.nord = prm->nord; g.ng = prm->nord / 2;
@@ -962,7 +954,19 @@ int mhd_last_timings(void* handle, float out_ms[8]) {
   return MHD_OK;
 }
 
-// Two pinned staging buffers: unpacking array a overlaps the copy of array a+1.
+// Writes the first byte of every page of a caller's output array on all host
+// threads.  A copy into pages the process has not touched yet would take
+// their first-touch faults one at a time inside the copy; already-mapped pages
+// cost one store each.  The array is overwritten right after.
+static void prefault(double* p, size_t bytes) {
+  const size_t page = (size_t)sysconf(_SC_PAGESIZE);
+  char* c = reinterpret_cast<char*>(p);
+  const long long npg = (long long)((bytes + page - 1) / page);
+#pragma omp parallel for schedule(static)
+  for (long long k = 0; k < npg; ++k) c[(size_t)k * page] = 0;
+}
+
+// Device-side conversion to FP64, then a copy straight into the caller's arrays.
 template <typename T>
 static int fetch_t(Handle* h, double* const* outs) {
   const Geom& g = h->g;
@@ -973,45 +977,17 @@ static int fetch_t(Handle* h, double* const* outs) {
   ext[8][0] = g.nx + 1; ext[8][1] = g.ny; ext[8][2] = g.nz;
   ext[9][0] = g.nx; ext[9][1] = g.ny + 1; ext[9][2] = g.nz;
   ext[10][0] = g.nx; ext[10][1] = g.ny; ext[10][2] = g.nz + 1;
-  std::vector<int> todo;
+  double* scratch = f64_scratch(d);
   for (int a = 0; a < 11; ++a)
-    if (outs[a]) todo.push_back(a);
-  if (todo.empty()) return MHD_OK;
-  T* stage[2] = {nullptr, nullptr};
-  cudaEvent_t done[2];
-  CK(cudaMallocHost(&stage[0], (size_t)g.vol * sizeof(T)));
-  if (cudaMallocHost(&stage[1], (size_t)g.vol * sizeof(T)) != cudaSuccess) {
-    cudaFreeHost(stage[0]);
-    return fail(MHD_E_NOMEM, "pinned staging allocation failed");
+    if (outs[a]) prefault(outs[a], sizeof(double) * (size_t)ext[a][0] * ext[a][1] * ext[a][2]);
+  for (int a = 0; a < 11; ++a) {
+    if (!outs[a]) continue;
+    const int ex = ext[a][0], ey = ext[a][1], ez = ext[a][2];
+    k_to_f64<T><<<dim3((ex + 255) / 256, ey, ez), 256, 0, h->st>>>(srcs[a], ex, ey, g.px, g.plane, scratch);
+    CK(cudaMemcpyAsync(outs[a], scratch, sizeof(double) * (size_t)ex * ey * ez, cudaMemcpyDeviceToHost, h->st));
   }
-  cudaEventCreateWithFlags(&done[0], cudaEventDisableTiming);
-  cudaEventCreateWithFlags(&done[1], cudaEventDisableTiming);
-  auto issue = [&](int n) -> cudaError_t {
-    const int a = todo[n];
-    const size_t bytes = ((size_t)ext[a][2] - 1) * g.plane * sizeof(T) +
-                         ((size_t)(ext[a][1] - 1) * g.px + ext[a][0]) * sizeof(T);
-    cudaError_t e = cudaMemcpyAsync(stage[n & 1], srcs[a], bytes, cudaMemcpyDeviceToHost, h->st);
-    if (e == cudaSuccess) e = cudaEventRecord(done[n & 1], h->st);
-    return e;
-  };
-  int rc = MHD_OK;
-  cudaError_t e = issue(0);
-  for (size_t n = 0; n < todo.size() && rc == MHD_OK; ++n) {
-    if (e == cudaSuccess && n + 1 < todo.size()) e = issue((int)n + 1);
-    if (e == cudaSuccess) e = cudaEventSynchronize(done[n & 1]);
-    if (e != cudaSuccess) {
-      rc = fail(MHD_E_CUDA, std::string("fetch: ") + cudaGetErrorString(e));
-      break;
-    }
-    const int a = todo[n];
-    unpack<T>(g, stage[n & 1], ext[a][0], ext[a][1], ext[a][2], outs[a]);
-  }
-  if (rc == MHD_OK) rc = wait_stream(h);
-  cudaEventDestroy(done[0]);
-  cudaEventDestroy(done[1]);
-  cudaFreeHost(stage[0]);
-  cudaFreeHost(stage[1]);
-  return rc;
+  CK(cudaGetLastError());
+  return wait_stream(h);
 }
 
 int mhd_fetch(void* handle, double* rho, double* vx, double* vy, double* vz, double* p, double* bx,
