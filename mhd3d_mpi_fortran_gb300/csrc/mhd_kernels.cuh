@@ -158,9 +158,14 @@ __device__ __forceinline__ void weno5(T fm3, T fm2, T fm1, T f0, T fp1, T fp2, T
   fr = Ops<T>::dv(s0, sum) * h0 + Ops<T>::dv(s1, sum) * h1 + Ops<T>::dv(s2, sum) * h2;
 }
 
-// minmod / median (mhd3d3.f90:1380-1403)
+// minmod (mhd3d3.f90:1380-1403): 0.5 (sign(1,a) + sign(1,b)) min(|a|, |b|).
+// The factor is exactly 1, -1 or 0, so one comparison of the two signs and a
+// select give the same value for every finite m = min(|a|, |b|) (NaN operands
+// included: sign(1, NaN) counts as -1 on both forms).
 template <typename T> __device__ __forceinline__ T minmod(T a, T b) {
-  return T(0.5) * (sgn1(a) + sgn1(b)) * mn(fab(a), fab(b));
+  const T m = mn(fab(a), fab(b));
+  const bool pa = a >= T(0), pb = b >= T(0);
+  return (pa == pb) ? (pa ? m : -m) : T(0);
 }
 // Monotonicity-preserving bound of MPWENO5 (mhd3d3.f90:1530-1591) for one
 // side; left state: (a3,a2,a1,b0,b1) = (fm3,fm2,fm1,f0,fp1), right state:
