@@ -124,9 +124,11 @@ __device__ __forceinline__ void tvd(T fm2, T fm1, T f0, T fp1, T fi, T eps, T& f
   fr = f0 - b * (f0 - fi);
 }
 
-// WENO5 (mhd3d3.f90:1329-1375), one face.
+// WENO5 (mhd3d3.f90:1329-1375), one face.  The right state is the left-state
+// formula on the mirrored stencil (fp2, fp1, f0, fm1, fm2), term for term, so
+// both come from weno5_left.
 template <typename T>
-__device__ __forceinline__ void weno5(T fm3, T fm2, T fm1, T f0, T fp1, T fp2, T eps, T& fl, T& fr) {
+__device__ __forceinline__ T weno5_left(T fm3, T fm2, T fm1, T f0, T fp1, T eps) {
   const T c13 = T(13.0) / T(12.0);
   T h0 = Div<T>::by(T(2) * fm3 - T(7) * fm2 + T(11) * fm1, T(6));
   T h1 = Div<T>::by(-fm2 + T(5) * fm1 + T(2) * f0, T(6));
@@ -141,21 +143,12 @@ __device__ __forceinline__ void weno5(T fm3, T fm2, T fm1, T f0, T fp1, T fp2, T
   s1 = Ops<T>::dv(T(0.6), (eps + s1) * (eps + s1));
   s2 = Ops<T>::dv(T(0.3), (eps + s2) * (eps + s2));
   T sum = s0 + s1 + s2;
-  fl = Ops<T>::dv(s0, sum) * h0 + Ops<T>::dv(s1, sum) * h1 + Ops<T>::dv(s2, sum) * h2;
-  h0 = Div<T>::by(T(2) * fp2 - T(7) * fp1 + T(11) * f0, T(6));
-  h1 = Div<T>::by(-fp1 + T(5) * f0 + T(2) * fm1, T(6));
-  h2 = Div<T>::by(T(2) * f0 + T(5) * fm1 - fm2, T(6));
-  t = fp2 - T(2) * fp1 + f0; u = fp2 - T(4) * fp1 + T(3) * f0;
-  s0 = c13 * (t * t) + T(0.25) * (u * u);
-  t = fp1 - T(2) * f0 + fm1; u = fp1 - fm1;
-  s1 = c13 * (t * t) + T(0.25) * (u * u);
-  t = f0 - T(2) * fm1 + fm2; u = T(3) * f0 - T(4) * fm1 + fm2;
-  s2 = c13 * (t * t) + T(0.25) * (u * u);
-  s0 = Ops<T>::dv(T(0.1), (eps + s0) * (eps + s0));
-  s1 = Ops<T>::dv(T(0.6), (eps + s1) * (eps + s1));
-  s2 = Ops<T>::dv(T(0.3), (eps + s2) * (eps + s2));
-  sum = s0 + s1 + s2;
-  fr = Ops<T>::dv(s0, sum) * h0 + Ops<T>::dv(s1, sum) * h1 + Ops<T>::dv(s2, sum) * h2;
+  return Ops<T>::dv(s0, sum) * h0 + Ops<T>::dv(s1, sum) * h1 + Ops<T>::dv(s2, sum) * h2;
+}
+template <typename T>
+__device__ __forceinline__ void weno5(T fm3, T fm2, T fm1, T f0, T fp1, T fp2, T eps, T& fl, T& fr) {
+  fl = weno5_left(fm3, fm2, fm1, f0, fp1, eps);
+  fr = weno5_left(fp2, fp1, f0, fm1, fm2, eps);
 }
 
 // minmod (mhd3d3.f90:1380-1403): 0.5 (sign(1,a) + sign(1,b)) min(|a|, |b|).
@@ -216,6 +209,15 @@ __device__ __forceinline__ void recon_face(const T* __restrict__ f, I c, I s, co
       fr = mp_side(fr, fp2, fp1, f0, fm1, fm2, P.alpha, P.beta);
     }
   }
+}
+
+// One side of weno_vals: the left state of the stencil (x0..x4) = (fm3..fp1);
+// the right state is this on the mirrored stencil (fp2, fp1, f0, fm1, fm2).
+template <typename T, int RECON>
+__device__ __forceinline__ T weno_one(T x0, T x1, T x2, T x3, T x4, const Prm<T>& P) {
+  T f = weno5_left(x0, x1, x2, x3, x4, P.eps);
+  if (RECON == R_MPWENO) f = mp_side(f, x0, x1, x2, x3, x4, P.alpha, P.beta);
+  return f;
 }
 
 // WENO5/MPWENO5 pair on six values held in registers.
@@ -1609,22 +1611,8 @@ __global__ void __launch_bounds__(NT) k_emf_weno(Dev<T> d, Inp<T> in, Prm<T> P) 
 #pragma unroll 1
     for (int w = 0; w < 2; ++w) {
       const T* s = sp + w * 2 * NP;
-      T a[6], v00_0, v00_1, v10_0, v10_1, v01_0, v01_1, v11_0, v11_1;
-      const T* l1 = s + e * L1::GE + f1 * L1::G1 + f2 * L1::G2;  // rows f2 - 3 + m at m * G2
-#pragma unroll
-      for (int m = 0; m < 6; ++m) a[m] = l1[m * L1::G2];
-      weno_vals<T, RECON>(a, P, v00_1, v01_1);
-#pragma unroll
-      for (int m = 0; m < 6; ++m) a[m] = l1[N1 + m * L1::G2];
-      weno_vals<T, RECON>(a, P, v10_1, v11_1);
-      const T* l0 = s + 2 * N1 + e * L0::GE + f1 * L0::G1 + f2 * L0::G2;  // columns f1 - 3 + m
-#pragma unroll
-      for (int m = 0; m < 6; ++m) a[m] = l0[m * L0::G1];
-      weno_vals<T, RECON>(a, P, v00_0, v01_0);
-#pragma unroll
-      for (int m = 0; m < 6; ++m) a[m] = l0[N0 + m * L0::G1];
-      weno_vals<T, RECON>(a, P, v10_0, v11_0);
-      // dif signs pick the smoother one-sided estimate per quadrant (2056-2106)
+      // dif signs pick the smoother one-sided estimate per quadrant (2056-2106):
+      // "_0" (columns, second pass along d1) if d >= 0, else "_1" (rows)
       const T* v = sv + w * NV;
       const int c = e * K::SE + (f1 + 3) * K::S1 + (f2 + 3) * K::S2;
       constexpr int s1 = K::S1, s2 = K::S2;
@@ -1633,10 +1621,23 @@ __global__ void __launch_bounds__(NT) k_emf_weno(Dev<T> d, Inp<T> in, Prm<T> P) 
       const T d10 = fab(v[q10 + s1] - v[q10]) - fab(v[q10 - s2] - v[q10]);
       const T d01 = fab(v[q01 - s1] - v[q01]) - fab(v[q01 + s2] - v[q01]);
       const T d11 = fab(v[q11 + s1] - v[q11]) - fab(v[q11 + s2] - v[q11]);
-      const T v00 = d00 >= T(0) ? v00_0 : v00_1;
-      const T v10 = d10 >= T(0) ? v10_0 : v10_1;
-      const T v01 = d01 >= T(0) ? v01_0 : v01_1;
-      const T v11 = d11 >= T(0) ? v11_0 : v11_1;
+      // left (L) and right (R) first-pass arrays of the rows ("_1") and columns ("_0")
+      const T* l1 = s + e * L1::GE + f1 * L1::G1 + f2 * L1::G2;           // rows f2 - 3 + m at m * G2
+      const T* l0 = s + 2 * N1 + e * L0::GE + f1 * L0::G1 + f2 * L0::G2;  // columns f1 - 3 + m
+      // only the chosen estimate of each quadrant is evaluated: v_00 / v_10 are
+      // the left states of the L / R stencils, v_01 / v_11 the right states
+      // (the left-state formula on the mirrored stencil)
+      auto pick = [&](bool col, int off) -> const T* { return col ? l0 + off : l1 + off; };
+      const T* a00 = pick(d00 >= T(0), 0);
+      const T* a10 = pick(d10 >= T(0), d10 >= T(0) ? N0 : N1);
+      const T* a01 = pick(d01 >= T(0), 0);
+      const T* a11 = pick(d11 >= T(0), d11 >= T(0) ? N0 : N1);
+      const int g00 = d00 >= T(0) ? L0::G1 : L1::G2, g10 = d10 >= T(0) ? L0::G1 : L1::G2;
+      const int g01 = d01 >= T(0) ? L0::G1 : L1::G2, g11 = d11 >= T(0) ? L0::G1 : L1::G2;
+      const T v00 = weno_one<T, RECON>(a00[0], a00[g00], a00[2 * g00], a00[3 * g00], a00[4 * g00], P);
+      const T v10 = weno_one<T, RECON>(a10[0], a10[g10], a10[2 * g10], a10[3 * g10], a10[4 * g10], P);
+      const T v01 = weno_one<T, RECON>(a01[5 * g01], a01[4 * g01], a01[3 * g01], a01[2 * g01], a01[g01], P);
+      const T v11 = weno_one<T, RECON>(a11[5 * g11], a11[4 * g11], a11[3 * g11], a11[2 * g11], a11[g11], P);
       const T vc = T(0.25) * (v00 + v01 + v10 + v11);
       if (w == 0)
         v1av = vc;
