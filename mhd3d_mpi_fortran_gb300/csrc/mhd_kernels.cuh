@@ -1113,7 +1113,7 @@ constexpr int kSweepUnroll = MHD_SWEEP_UNROLL;  // face-loop unroll (compile-tim
 #endif
 constexpr int kSweepMinB = MHD_SWEEP_MINB;  // resident 128-thread blocks per SM (register budget)
 
-template <typename T, int D, bool B>
+template <typename T, int D, bool B, int RECON = R_PDM>
 __global__ void __launch_bounds__(128, kSweepMinB)
     k_flux_sweep(KArg<T, B> ka, Inp<T> in0, Prm<T> P, int form, T cw, T den) {
   const int4 bb = ka.blk();
@@ -1217,7 +1217,7 @@ __global__ void __launch_bounds__(128, kSweepMinB)
     }
     T L[8], R[8], F[8];
 #pragma unroll
-    for (int v = 0; v < 8; ++v) recon_win<T, R_PDM, 0>(w[v], P, L[v], R[v]);
+    for (int v = 0; v < 8; ++v) recon_win<T, RECON, 0>(w[v], P, L[v], R[v]);
     face_flux<T, D>(L, R, d.gam, F);
     if (cd > c0) {
       const int cc = cd - 1;
@@ -2151,11 +2151,13 @@ inline dim3 sweep_grid(int D, const Geom& g) {
 
 template <typename T, int RECON, int D, bool M>
 void flux_t_any(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, int form, T c, T den, int ab, cudaStream_t st) {
-  if constexpr (tunable<T, RECON, M>()) {
-    if (d.tile_td == kSweepTile) {
-      k_flux_sweep<T, D, false><<<sweep_grid(D, d.g), dim3(32, 4), 0, st>>>(one(d), in, P, form, c, den);
+  if constexpr (std::is_same<T, float>::value && !M && (RECON == R_PDM || RECON == R_WENO || RECON == R_MPWENO)) {
+    if (d.tile_td == kSweepTile) {  // column sweeps (every FP32 Cartesian reconstruction with a register window)
+      k_flux_sweep<T, D, false, RECON><<<sweep_grid(D, d.g), dim3(32, 4), 0, st>>>(one(d), in, P, form, c, den);
       return;
     }
+  }
+  if constexpr (tunable<T, RECON, M>()) {
     if (d.tile_td == 4) return launch_flux_t<T, RECON, D, M, 4>(d, in, P, form, c, den, ab, st);
     if (d.tile_td == 16) return launch_flux_t<T, RECON, D, M, 16>(d, in, P, form, c, den, ab, st);
   }

@@ -336,6 +336,22 @@ def test_set_tiles_every_shape_gives_identical_steps():
     assert info[0] > 0 and info[1] >= 10 and info[3] > 0
 
 
+@pytest.mark.parametrize("recon", [3, 4])
+def test_weno_column_sweeps_equal_face_tiles(recon):
+    """FP32 WENO5 / MP-WENO5: the column-sweep face kernels (shape 32, the
+    default) and the 8-cell face tiles step to the same bits."""
+    s = ics.turbulence(40, seed=6)
+    prm = Params(40, 40, 40, reconop=recon, precision=FP32, tau=0.4 * ics.cfl_dt(s))
+    out = {}
+    for td in (8, 32):
+        with MHDSolver(prm, s) as g:
+            g.set_tiles(td, 8)
+            g.step(3)
+            out[td] = g.fetch()
+    for k in FIELDS:
+        assert np.array_equal(out[8][k], out[32][k]), k
+
+
 def test_batched_column_sweeps_equal_sequential_tiles():
     """Batched ensemble on the column-sweep face kernels (tile 32) against each
     grid stepped alone on the default face tiles: bit-identical."""
