@@ -36,6 +36,17 @@ def _f64(a) -> np.ndarray:
     return np.asfortranarray(np.asarray(a, dtype=np.float64))
 
 
+def output_arrays(params) -> dict:
+    """Fortran-ordered FP64 arrays of the shapes mhd_fetch fills for params."""
+    nx, ny, nz = params.shape
+    cs = (nx, ny, nz)
+    out = {k: np.zeros(cs, order="F") for k in ("rho", "vx", "vy", "vz", "p", "bx", "by", "bz")}
+    out["bi"] = np.zeros((nx + 1, ny, nz), order="F")
+    out["bj"] = np.zeros((nx, ny + 1, nz), order="F")
+    out["bk"] = np.zeros((nx, ny, nz + 1), order="F")
+    return out
+
+
 class MHDSolver:
     def __init__(self, params: Params, state: State | None, dx=None, dy=None, dz=None, lib=None,
                  _handle=None):
@@ -119,13 +130,19 @@ class MHDSolver:
         return dict(zip(("flux_x", "flux_y", "flux_z_update", "emf", "ct", "fill", "dt"), list(out)))
 
     # -- readback -------------------------------------------------------
-    def fetch(self) -> dict:
-        nx, ny, nz = self.params.shape
-        cs = (nx, ny, nz)
-        out = {k: np.zeros(cs, order="F") for k in ("rho", "vx", "vy", "vz", "p", "bx", "by", "bz")}
-        out["bi"] = np.zeros((nx + 1, ny, nz), order="F")
-        out["bj"] = np.zeros((nx, ny + 1, nz), order="F")
-        out["bk"] = np.zeros((nx, ny, nz + 1), order="F")
+    def output_arrays(self) -> dict:
+        """Fortran-ordered FP64 arrays of the shapes mhd_fetch fills."""
+        return output_arrays(self.params)
+
+    def fetch(self, out: dict | None = None) -> dict:
+        """The state as FP64 Fortran arrays (mhd_fetch); `out` (from
+        output_arrays, or arrays of the same shapes and layout) is filled in
+        place, as the Fortran driver's own module arrays are."""
+        if out is None:
+            out = self.output_arrays()
+        for k, a in out.items():
+            if a.dtype != np.float64 or not a.flags.f_contiguous:
+                raise ValueError(f"fetch: {k} must be a Fortran-ordered float64 array")
         names = ("rho", "vx", "vy", "vz", "p", "bx", "by", "bz", "bi", "bj", "bk")
         rc = self.lib.mhd_fetch(self.h, *[_ptr(out[k]) for k in names])
         check(self.lib, rc, "mhd_fetch")

@@ -443,3 +443,17 @@ def test_yee_fp32_budget_and_cartesian_only():
     m = ics.mapped_blast(8)
     with pytest.raises(MHDError):
         MHDSolver(Params(8, 8, 8, emf=EMF_YEE, tau=0.0, stepop=STEP_AB2), m)
+
+
+def test_fetch_fills_caller_arrays_in_place():
+    s = ics.orszag_tang_3d(12, seed=1)
+    with MHDSolver(Params(12, 12, 12, tau=0.4 * ics.cfl_dt(s)), s) as g:
+        g.step(2)
+        a = g.fetch()
+        dst = g.output_arrays()
+        for v in dst.values():
+            v.fill(7.0)
+        b = g.fetch(out=dst)
+    assert b is dst
+    for k in FIELDS:
+        assert np.array_equal(a[k], dst[k]), k
