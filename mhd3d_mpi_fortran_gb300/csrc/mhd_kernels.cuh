@@ -1309,6 +1309,12 @@ __global__ void k_emf(Dev<T> d, Inp<T> in, Prm<T> P) {
 // variant of emf_pdm_tile in those blocks.  ei keeps the plain count (its
 // halo-padded tile is large, so a wider variant would cost shared memory and
 // occupancy in every block).
+// Depth of the ej / ek plane tiles along their second transverse axis
+// (32 x kPT edges, 32 kPT threads); compile-time knob.
+#ifndef MHD_EMF_PLANE
+#define MHD_EMF_PLANE 8
+#endif
+constexpr int kPT = MHD_EMF_PLANE;
 constexpr bool emf_merges(int E, int axis) { return E != 0 && axis != E; }
 
 __host__ __device__ constexpr int emf_edge_tiles(int ext, int t, bool merge) {
@@ -2347,8 +2353,8 @@ void Launch<T, M>::emf(const Dev<T>& d, const Inp<T>& in0, cudaStream_t st) {
       launch_emf_pdm<T, 0, 32, 4, 4, 512, M>(d, in, P, st);
     else
       launch_emf_pdm<T, 0, 32, EiTile<T>::Y, EiTile<T>::Y, 512, M>(d, in, P, st);
-    launch_emf_pdm<T, 1, 32, 1, 8, 256, M>(d, in, P, st);
-    launch_emf_pdm<T, 2, 32, 8, 1, 256, M>(d, in, P, st);
+    launch_emf_pdm<T, 1, 32, 1, kPT, 32 * kPT, M>(d, in, P, st);
+    launch_emf_pdm<T, 2, 32, kPT, 1, 32 * kPT, M>(d, in, P, st);
     return;
   }
   switch (d.recon) {
@@ -2383,8 +2389,8 @@ dim3 Batch<T>::dims(int fam, const Geom& g, int td, int ey) {
     case BF_FLUX_Y: return td == kSweepTile ? sweep_grid(1, g) : dim3((g.nx0 + 31) / 32, (g.ny0 + td - 1) / td, g.nz0);
     case BF_FLUX_Z: return td == kSweepTile ? sweep_grid(2, g) : dim3((g.nx0 + 31) / 32, (g.nz0 + td - 1) / td, g.ny0);
     case BF_EMF_I: return emf_grid(0, g, 32, Y, Y);
-    case BF_EMF_J: return emf_grid(1, g, 32, 1, 8);
-    case BF_EMF_K: return emf_grid(2, g, 32, 8, 1);
+    case BF_EMF_J: return emf_grid(1, g, 32, 1, kPT);
+    case BF_EMF_K: return emf_grid(2, g, 32, kPT, 1);
     case BF_CT: return grid3(g.nx0 + 1, g.ny0 + 1, g.nz0 + 1, dim3(32, 4, 1));
     default: return dim3(FillShape(g).blocks(), 1, 1);  // BF_FILL
   }
@@ -2406,21 +2412,21 @@ void set_smem(K kernel, size_t bytes) {
 template <typename T, int Y>
 void batch_emf(const BatchView& v, const Dev<T>* tab, const Prm<T>& P, cudaStream_t st) {
   constexpr size_t si = emf_pdm_smem<T, 0, 32, Y, Y>();
-  constexpr size_t sj = emf_pdm_smem<T, 1, 32, 1, 8>();
-  constexpr size_t sk = emf_pdm_smem<T, 2, 32, 8, 1>();
+  constexpr size_t sj = emf_pdm_smem<T, 1, 32, 1, kPT>();
+  constexpr size_t sk = emf_pdm_smem<T, 2, 32, kPT, 1>();
   static bool attr = false;
   if (!attr) {
     set_smem(k_emf_pdm<T, 0, 32, Y, Y, 512, false, true>, si);
-    set_smem(k_emf_pdm<T, 1, 32, 1, 8, 256, false, true>, sj);
-    set_smem(k_emf_pdm<T, 2, 32, 8, 1, 256, false, true>, sk);
+    set_smem(k_emf_pdm<T, 1, 32, 1, kPT, 32 * kPT, false, true>, sj);
+    set_smem(k_emf_pdm<T, 2, 32, kPT, 1, 32 * kPT, false, true>, sk);
     attr = true;
   }
   const Inp<T> none{};
   k_emf_pdm<T, 0, 32, Y, Y, 512, false, true><<<v.nblk[BF_EMF_I], 512, si, st>>>(
       KArg<T, true>{tab, v.map[BF_EMF_I]}, none, P);
-  k_emf_pdm<T, 1, 32, 1, 8, 256, false, true><<<v.nblk[BF_EMF_J], 256, sj, st>>>(
+  k_emf_pdm<T, 1, 32, 1, kPT, 32 * kPT, false, true><<<v.nblk[BF_EMF_J], 32 * kPT, sj, st>>>(
       KArg<T, true>{tab, v.map[BF_EMF_J]}, none, P);
-  k_emf_pdm<T, 2, 32, 8, 1, 256, false, true><<<v.nblk[BF_EMF_K], 256, sk, st>>>(
+  k_emf_pdm<T, 2, 32, kPT, 1, 32 * kPT, false, true><<<v.nblk[BF_EMF_K], 32 * kPT, sk, st>>>(
       KArg<T, true>{tab, v.map[BF_EMF_K]}, none, P);
 }
 
