@@ -336,6 +336,22 @@ def test_set_tiles_every_shape_gives_identical_steps():
     assert info[0] > 0 and info[1] >= 10 and info[3] > 0
 
 
+@pytest.mark.parametrize("stepop", [STEP_AB2, STEP_RK3])
+def test_column_sweeps_equal_face_tiles_for_ab2_and_rk3(stepop):
+    """The z-sweep epilogue applies every stepper's stage combine exactly as
+    the z-face tiles do: FP32 PDM AB2 and RK3 steps are bit-identical."""
+    s = ics.turbulence(40, seed=8)
+    prm = Params(40, 40, 40, stepop=stepop, precision=FP32, tau=0.4 * ics.cfl_dt(s))
+    out = {}
+    for td in (8, 32):
+        with MHDSolver(prm, s) as g:
+            g.set_tiles(td, 8)
+            g.step(3)
+            out[td] = g.fetch()
+    for k in FIELDS:
+        assert np.array_equal(out[8][k], out[32][k]), k
+
+
 @pytest.mark.parametrize("recon", [3, 4])
 def test_weno_column_sweeps_equal_face_tiles(recon):
     """FP32 WENO5 / MP-WENO5: the column-sweep face kernels (shape 32, the
