@@ -235,8 +235,8 @@ int mhd_diagnostics_noalloc(const mhd_params* prm, const double* rho, const doub
 int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* status);
 
 /* Tile autotuner (no reference counterpart).  Times the launch-shape variants
- * compiled for the FP32 Cartesian PDM, WENO5 and MP-WENO5 paths -- y/z face-tile
- * length 4, 8 or 16 (8 only for WENO)
+ * compiled for the FP32 Cartesian paths -- y/z face-tile length 4, 8 or 16 (8
+ * only outside PDM)
  * or 32 (32: column sweeps of 32-cell segments with a register window) and
  * ei EMF tile 4x4 or 8x8 edges -- on the handle's own grid, `reps` timed
  * runs each, keeps the fastest and writes it to out[0] (tile length) and

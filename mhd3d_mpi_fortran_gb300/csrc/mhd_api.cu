@@ -530,10 +530,7 @@ static int create_handle(const mhd_params* prm, const double* dx, const double* 
   h->metric = metric;
   h->tile_ey = h->fp32 ? 8 : 4;
   // the column sweeps are the fastest face shape at production sizes (the autotuner may still pick a tile)
-  h->tile_td = (h->fp32 && !metric && (prm->reconop == MHD_RECON_PDM || prm->reconop == MHD_RECON_WENO5 ||
-                                        prm->reconop == MHD_RECON_MPWENO5))
-                    ? kSweepTile
-                    : 8;
+  h->tile_td = (h->fp32 && !metric) ? kSweepTile : 8;
   Geom& g = h->g;
   g.nx0 = prm->nx0; g.ny0 = prm->ny0; g.nz0 = prm->nz0;
   g.nord = prm->nord; g.ng = prm->nord / 2;
@@ -1338,12 +1335,9 @@ static void drop_graphs(Handle* h) {
 }
 
 // FP32 Cartesian PDM: face tiles 4/8/16 or the column sweeps, ei tile 4x4/8x8;
-// FP32 Cartesian WENO5/MP-WENO5: face tile 8 (4 and 16 run as 8) or the column
-// sweeps (their EMF tiles are fixed, the ei value is ignored).
-static bool tunable(const Handle* h) {
-  const int r = h->prm.reconop;
-  return h->fp32 && !h->metric && (r == MHD_RECON_PDM || r == MHD_RECON_WENO5 || r == MHD_RECON_MPWENO5);
-}
+// the other FP32 Cartesian reconstructions: face tile 8 (4 and 16 run as 8) or
+// the column sweeps (their EMF launch shapes are fixed, the ei value is ignored).
+static bool tunable(const Handle* h) { return h->fp32 && !h->metric; }
 
 int mhd_autotune(void* handle, int32_t reps, int32_t out[2]) {
   Handle* h = (Handle*)handle;

@@ -2157,7 +2157,7 @@ inline dim3 sweep_grid(int D, const Geom& g) {
 
 template <typename T, int RECON, int D, bool M>
 void flux_t_any(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, int form, T c, T den, int ab, cudaStream_t st) {
-  if constexpr (std::is_same<T, float>::value && !M && (RECON == R_PDM || RECON == R_WENO || RECON == R_MPWENO)) {
+  if constexpr (std::is_same<T, float>::value && !M) {
     if (d.tile_td == kSweepTile) {  // column sweeps (every FP32 Cartesian reconstruction with a register window)
       k_flux_sweep<T, D, false, RECON><<<sweep_grid(D, d.g), dim3(32, 4), 0, st>>>(one(d), in, P, form, c, den);
       return;

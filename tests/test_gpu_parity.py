@@ -352,10 +352,10 @@ def test_column_sweeps_equal_face_tiles_for_ab2_and_rk3(stepop):
         assert np.array_equal(out[8][k], out[32][k]), k
 
 
-@pytest.mark.parametrize("recon", [3, 4])
+@pytest.mark.parametrize("recon", [2, 3, 4, 5])
 def test_weno_column_sweeps_equal_face_tiles(recon):
-    """FP32 WENO5 / MP-WENO5: the column-sweep face kernels (shape 32, the
-    default) and the 8-cell face tiles step to the same bits."""
+    """FP32 TVD, WENO5, MP-WENO5, TVD-MC: the column-sweep face kernels (shape
+    32, the default) and the 8-cell face tiles step to the same bits."""
     s = ics.turbulence(40, seed=6)
     prm = Params(40, 40, 40, reconop=recon, precision=FP32, tau=0.4 * ics.cfl_dt(s))
     out = {}
