@@ -232,6 +232,22 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+def job_time_ms(ms_local: float, pg) -> float:
+    """The job's time for the timed steps: the slowest rank's (max over ranks;
+    every rank passed a barrier right before its timed region)."""
+    if pg is None:
+        return ms_local
+    import torch
+    t = torch.tensor([ms_local], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(n: int, steps: int, ws: int, ms: float) -> float:
+    """Zone-updates/s of the whole job: every rank advances its own n^3 replica."""
+    return n ** 3 * steps * ws / (ms * 1e-3)
+
+
 def run_ours(a):
     ws, rank, local = dist_env()
     if ws > 1:
@@ -266,12 +282,8 @@ def run_ours(a):
     with Clocks(0 if ws == 1 else local) as ck:
         ms = solver.time_steps(a.steps, graph=graph)
     clocks = ck.summary()
-    if pg:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
-    zu = n ** 3 * a.steps * ws / (ms * 1e-3)
+    ms = job_time_ms(ms, pg)
+    zu = whole_job_rate(n, a.steps, ws, ms)
     # per-family device time (events on the solver's stream)
     kprof = min(a.steps, 20)
     solver.set_profiling(True)
