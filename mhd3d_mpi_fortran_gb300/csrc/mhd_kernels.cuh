@@ -19,6 +19,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <type_traits>
+#include <atomic>
 #include <math.h>
 #include <stdint.h>
 #include "mhd_state.h"
@@ -28,6 +29,21 @@ namespace mhd {
 enum { R_PDM = 1, R_TVD = 2, R_WENO = 3, R_MPWENO = 4, R_TVDMC = 5 };
 enum { BC_PERIODIC = 0, BC_EVEN = 1, BC_REFLECT = 2, BC_OUTFLOW = 3 };
 enum { EMF_LFM = 0, EMF_YEE = 1 };
+
+// Kernels with more than 48 KB of dynamic shared memory must be enabled per
+// device: a launcher sets its attributes the first time it runs on the
+// current device (idempotent if two host threads race; the bit is set only
+// after the attributes are).
+struct PerDevice {
+  std::atomic<unsigned long long> done{0};
+  bool need(unsigned long long& bit) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    bit = 1ull << (dev & 63);
+    return !(done.load(std::memory_order_acquire) & bit);
+  }
+  void mark(unsigned long long bit) { done.fetch_or(bit, std::memory_order_release); }
+};
 
 inline dim3 grid3(int ni, int nj, int nk, dim3 b) {
   return dim3((ni + b.x - 1) / b.x, (nj + b.y - 1) / b.y, nk);
@@ -1480,11 +1496,12 @@ __global__ void __launch_bounds__(NT, emf_min_blocks(E, NT, B))
 template <typename T, int E, int TX, int TY, int TZ, int NT, bool M>
 void launch_emf_pdm(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStream_t st) {
   constexpr size_t bytes = emf_pdm_smem<T, E, TX, TY, TZ>();
-  static bool attr = false;
-  if (!attr) {
+  static PerDevice attr;
+  unsigned long long bit = 0;
+  if (attr.need(bit)) {
     cudaFuncSetAttribute(k_emf_pdm<T, E, TX, TY, TZ, NT, M, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)bytes);
-    attr = true;
+    attr.mark(bit);
   }
   k_emf_pdm<T, E, TX, TY, TZ, NT, M, false><<<emf_grid(E, d.g, TX, TY, TZ), NT, bytes, st>>>(one(d), in, P);
 }
@@ -1671,11 +1688,12 @@ __global__ void __launch_bounds__(NT) k_emf_weno(Dev<T> d, Inp<T> in, Prm<T> P) 
 template <typename T, int RECON, int E, int TX, int TY, int TZ, int NT, bool M>
 void launch_emf_weno(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStream_t st) {
   constexpr size_t bytes = EmfWeno<T, E, TX, TY, TZ>::smem;
-  static bool attr = false;
-  if (!attr) {
+  static PerDevice attr;
+  unsigned long long bit = 0;
+  if (attr.need(bit)) {
     cudaFuncSetAttribute(k_emf_weno<T, RECON, E, TX, TY, TZ, NT, M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)bytes);
-    attr = true;
+    attr.mark(bit);
   }
   const Geom& g = d.g;
   const int ex = g.nx0 + (E != 0), ey = g.ny0 + (E != 1), ez = g.nz0 + (E != 2);
@@ -2132,10 +2150,11 @@ template <typename T, int RECON, int D, bool M, int TDV>
 void launch_flux_t(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, int form, T c, T den, int ab,
                    cudaStream_t st) {
   constexpr size_t sm = flux_t_smem<T, TDV>();
-  static bool attr = false;
-  if (!attr) {
+  static PerDevice attr;
+  unsigned long long bit = 0;
+  if (attr.need(bit)) {
     cudaFuncSetAttribute(k_flux_t<T, RECON, D, M, false, TDV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    attr = true;
+    attr.mark(bit);
   }
   const Geom& g = d.g;
   const dim3 grid = (D == 1) ? dim3((g.nx0 + 31) / 32, (g.ny0 + TDV - 1) / TDV, g.nz0)
@@ -2414,12 +2433,13 @@ void batch_emf(const BatchView& v, const Dev<T>* tab, const Prm<T>& P, cudaStrea
   constexpr size_t si = emf_pdm_smem<T, 0, 32, Y, Y>();
   constexpr size_t sj = emf_pdm_smem<T, 1, 32, 1, kPT>();
   constexpr size_t sk = emf_pdm_smem<T, 2, 32, kPT, 1>();
-  static bool attr = false;
-  if (!attr) {
+  static PerDevice attr;
+  unsigned long long bit = 0;
+  if (attr.need(bit)) {
     set_smem(k_emf_pdm<T, 0, 32, Y, Y, 512, false, true>, si);
     set_smem(k_emf_pdm<T, 1, 32, 1, kPT, 32 * kPT, false, true>, sj);
     set_smem(k_emf_pdm<T, 2, 32, kPT, 1, 32 * kPT, false, true>, sk);
-    attr = true;
+    attr.mark(bit);
   }
   const Inp<T> none{};
   k_emf_pdm<T, 0, 32, Y, Y, 512, false, true><<<v.nblk[BF_EMF_I], 512, si, st>>>(
@@ -2434,11 +2454,12 @@ void batch_emf(const BatchView& v, const Dev<T>* tab, const Prm<T>& P, cudaStrea
 template <typename T, int TDV>
 void batch_flux_t(const BatchView& v, const Dev<T>* tab, const Prm<T>& P, int form, T c, T den, cudaStream_t st) {
   constexpr size_t sf = flux_t_smem<T, TDV>();
-  static bool attr = false;
-  if (!attr) {
+  static PerDevice attr;
+  unsigned long long bit = 0;
+  if (attr.need(bit)) {
     set_smem(k_flux_t<T, R_PDM, 1, false, true, TDV>, sf);
     set_smem(k_flux_t<T, R_PDM, 2, false, true, TDV>, sf);
-    attr = true;
+    attr.mark(bit);
   }
   const Inp<T> none{};
   k_flux_t<T, R_PDM, 1, false, true, TDV><<<v.nblk[BF_FLUX_Y], dim3(32, TDV + 1), sf, st>>>(
