@@ -291,7 +291,6 @@ def run_ours(a):
     fam = solver.timings()
     solver.set_profiling(False)
     _, st = solver.step(1)
-    solver.close()
     stages = 2 * kprof
     fam_ms = {k: v / stages for k, v in fam.items()}  # per stage
     dom = max(WORDS, key=lambda k: fam_ms[k])
@@ -333,6 +332,7 @@ def run_ours(a):
                "d2h_bytes_per_step": int(d2h / ke), "steps": ke, "seconds": el,
                "split_s": {"init": t1 - t0, "steps": t2 - t1, "fetch": t3 - t2}}
         del out
+    solver.close()  # after the e2e run, so that its allocation does not follow a free of the same size
     cpu = None
     if not a.no_cpu_baseline and rank == 0 and ws == 1:
         v, dt, cores = cpu_rate(160, 8, a.recon)
