@@ -170,14 +170,22 @@ def workload(n):
     return s, 0.8 * ics.cfl_dt(s, cfl=0.3)
 
 
-def cpu_rate(n, steps, recon=1):
-    """Oracle (FP64 restatement of the reference) zone-updates/s on the host."""
+_CPU_STATES = {}
+
+
+def cpu_rate(n, steps, recon=1, fused=False):
+    """Oracle (FP64 restatement of the reference) zone-updates/s on the host:
+    the reference's array passes, or with fused=True one pass per face / edge
+    family (the same results)."""
     from mhd3d_mpi_fortran_gb300 import ics
     from mhd3d_mpi_fortran_gb300.abi import Params
     from oracle.oracle import OracleSolver, threads
-    s = ics.turbulence(n, seed=0)
+    if n not in _CPU_STATES:
+        _CPU_STATES[n] = ics.turbulence(n, seed=0)
+    s = _CPU_STATES[n]
     prm = Params(n, n, n, reconop=recon, stepop=2, tau=ics.cfl_dt(s, cfl=0.3))
     o = OracleSolver(prm, s)
+    o.set_fused(fused)
     t0 = time.perf_counter()
     o.step(steps)
     dt = time.perf_counter() - t0
@@ -186,18 +194,21 @@ def cpu_rate(n, steps, recon=1):
 
 
 def cpu_detail(recon=1):
-    """The oracle on all host threads and on one, at 64^3 (2 RK2 steps each)
-    and at 256^3 on all threads (1 step): the rates the reference's own CPU
-    path would be compared at."""
+    """The oracle in both modes (the reference's array passes; fused) on all
+    host threads and on one, at 64^3 (2 RK2 steps each) and at 256^3 on all
+    threads (1 step): the rates the reference's own CPU path would be
+    compared at."""
     from oracle.oracle import threads, set_threads
     allt = threads()
     rows = []
-    for n, steps, t in ((64, 2, allt), (64, 2, 1), (256, 1, allt)):
+    for mode, n, steps, t in [(m, n, st, t) for m in ("array", "fused")
+                              for n, st, t in ((64, 2, allt), (64, 2, 1), (256, 1, allt))]:
         set_threads(t)
-        v, dt, cores = cpu_rate(n, steps, recon)
-        rows.append({"grid": n, "steps": steps, "cores": cores, "value": v, "unit": "zone-updates/s",
+        v, dt, cores = cpu_rate(n, steps, recon, fused=(mode == "fused"))
+        rows.append({"mode": mode, "grid": n, "steps": steps, "cores": cores, "value": v, "unit": "zone-updates/s",
                      "seconds": dt})
     set_threads(allt)
+    _CPU_STATES.clear()
     return rows
 
 
@@ -337,7 +348,8 @@ def run_ours(a):
     if not a.no_cpu_baseline and rank == 0 and ws == 1:
         v, dt, cores = cpu_rate(160, 8, a.recon)
         cpu = {"value": v, "unit": "zone-updates/s", "cores": cores, "kind": "port",
-               "sample": f"8 RK2 steps of the 160^3 turbulence state (same generator), PDM, FP64 oracle, {dt:.1f} s",
+               "sample": f"8 RK2 steps of the 160^3 turbulence state (same generator), PDM, FP64 oracle "
+                         f"(array passes), {dt:.1f} s",
                "detail": cpu_detail(a.recon)}
     if rank != 0:
         return

@@ -7,6 +7,11 @@
 // statement or forall) and the reference's expression order, so that FP64
 // results agree with the GPU FP64 mode to the last bit apart from exp/erfc
 // (glibc here, CUDA's libdevice there).  Built with -ffp-contract=off: no FMA.
+// A second, fused mode (oracle_set_fused) evaluates the face and edge passes
+// one x line at a time from the cell arrays, without the array passes'
+// temporaries; it calls the same element functions in the same order and so
+// gives the array passes' results bit for bit -- it is the faster CPU
+// baseline, not a second specification.
 //
 // Parity pinning: the reference ships no tests or golden vectors and its
 // Fortran cannot be compiled here (no gfortran/ifort, MPI or HDF5), so this
@@ -21,6 +26,7 @@
 // mhd3d2.f90:3063-3064, a plain wrap); MPI_REDUCE/BCAST of dt are identities.
 
 #include <cmath>
+#include <cstddef>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -265,29 +271,33 @@ struct Oracle {
     }
   }
 
-  // PDM2 (mhd3d3.f90:1069-1172): partial-donor limiter of the interpolant fi
+  // PDM2 (mhd3d3.f90:1069-1172): partial-donor limiter of the interpolant fi,
+  // one element (the array form below and the fused step share it).
+  inline void pdm2_el(double fm2, double fm1, double f0, double fp1, double fi, double& fl, double& fr) const {
+    double maxf = fmax2(fm1, f0);
+    double minf = fmin2(fm1, f0);
+    double fii = fmax2(minf, fmin2(fi, maxf));
+    double dfm = pdmb * (fm1 - fm2);
+    double df0 = pdmb * (f0 - fm1);
+    double dfp = pdmb * (fp1 - f0);
+    double sm = fsign1(dfm), s0 = fsign1(df0), sp = fsign1(dfp);
+    dfm = std::fabs(dfm);
+    dfp = std::fabs(dfp);
+    double qm = std::fabs(sm + s0);
+    double qp = std::fabs(s0 + sp);
+    double dfl = fii - fm1;
+    double dfr = f0 - fii;
+    fl = fii - s0 * fmax2(0.0, std::fabs(dfl) - qm * dfm);
+    fr = fii + s0 * fmax2(0.0, std::fabs(dfr) - qp * dfp);
+  }
   void PDM2(A3& fleft, A3& fright, const A3& f, const A3& fi, int lnx, int lny, int lnz,
             int snx, int sny, int snz, int dir) {
     FOR3(lnx, lny, lnz) {
-      double fm2 = gat(f, dir, i, j, k, -2, snx, sny, snz);
-      double fm1 = gat(f, dir, i, j, k, -1, snx, sny, snz);
-      double f0 = gat(f, dir, i, j, k, 0, snx, sny, snz);
-      double fp1 = gat(f, dir, i, j, k, 1, snx, sny, snz);
-      double maxf = fmax2(fm1, f0);
-      double minf = fmin2(fm1, f0);
-      double fii = fmax2(minf, fmin2(fi(i, j, k), maxf));
-      double dfm = pdmb * (fm1 - fm2);
-      double df0 = pdmb * (f0 - fm1);
-      double dfp = pdmb * (fp1 - f0);
-      double sm = fsign1(dfm), s0 = fsign1(df0), sp = fsign1(dfp);
-      dfm = std::fabs(dfm);
-      dfp = std::fabs(dfp);
-      double qm = std::fabs(sm + s0);
-      double qp = std::fabs(s0 + sp);
-      double dfl = fii - fm1;
-      double dfr = f0 - fii;
-      fleft(i, j, k) = fii - s0 * fmax2(0.0, std::fabs(dfl) - qm * dfm);
-      fright(i, j, k) = fii + s0 * fmax2(0.0, std::fabs(dfr) - qp * dfp);
+      double fl, fr;
+      pdm2_el(gat(f, dir, i, j, k, -2, snx, sny, snz), gat(f, dir, i, j, k, -1, snx, sny, snz),
+              gat(f, dir, i, j, k, 0, snx, sny, snz), gat(f, dir, i, j, k, 1, snx, sny, snz), fi(i, j, k), fl, fr);
+      fleft(i, j, k) = fl;
+      fright(i, j, k) = fr;
     }
   }
 
@@ -299,17 +309,21 @@ struct Oracle {
            int snx, int sny, int snz, int dir, bool mc) {
     if (!tvd_shift) { snx = 0; sny = 0; snz = 0; }
     FOR3(lnx, lny, lnz) {
-      double fm2 = gat(f, dir, i, j, k, -2, snx, sny, snz);
-      double fm1 = gat(f, dir, i, j, k, -1, snx, sny, snz);
-      double f0 = gat(f, dir, i, j, k, 0, snx, sny, snz);
-      double fp1 = gat(f, dir, i, j, k, 1, snx, sny, snz);
-      double a = (fm1 - fm2) / (f0 - fm1 + eps);
-      double b = mc ? mclim(a) : (a + std::fabs(a)) / (1.0 + std::fabs(a));
-      fleft(i, j, k) = fm1 - b * (fm1 - fi(i, j, k));
-      a = (f0 - fp1) / (fm1 - f0 + eps);
-      b = mc ? mclim(a) : (a + std::fabs(a)) / (1.0 + std::fabs(a));
-      fright(i, j, k) = f0 - b * (f0 - fi(i, j, k));
+      double fl, fr;
+      tvd_el(gat(f, dir, i, j, k, -2, snx, sny, snz), gat(f, dir, i, j, k, -1, snx, sny, snz),
+             gat(f, dir, i, j, k, 0, snx, sny, snz), gat(f, dir, i, j, k, 1, snx, sny, snz), fi(i, j, k), mc, fl, fr);
+      fleft(i, j, k) = fl;
+      fright(i, j, k) = fr;
     }
+  }
+  inline void tvd_el(double fm2, double fm1, double f0, double fp1, double fi, bool mc, double& fl,
+                     double& fr) const {
+    double a = (fm1 - fm2) / (f0 - fm1 + eps);
+    double b = mc ? mclim(a) : (a + std::fabs(a)) / (1.0 + std::fabs(a));
+    fl = fm1 - b * (fm1 - fi);
+    a = (f0 - fp1) / (fm1 - f0 + eps);
+    b = mc ? mclim(a) : (a + std::fabs(a)) / (1.0 + std::fabs(a));
+    fr = f0 - b * (f0 - fi);
   }
   // MC limiter in the same form: with fi the 2-point mean, fleft = fm1 -
   // b*(fm1-fi) = fm1 + b/2*(f0-fm1), so b is the limiter phi(a) itself (van
@@ -458,6 +472,54 @@ struct Oracle {
     }
   }
 
+  // Quadrant selection by the sign of dif and the 4-quadrant mean of
+  // get_vav_center2corner (mhd3d3.f90:2056-2108), one element
+  inline double corner_blend_el(const A3& lv, int dir, int i, int j, int k, double a00_0, double a00_1,
+                                double a10_0, double a10_1, double a01_0, double a01_1, double a11_0,
+                                double a11_1) const {
+    double d00, d10, d01, d11;
+    const int G = ng;
+    if (dir == 1) {
+      d00 = std::fabs(lv(i + G, j + G - 2, k + G - 1) - lv(i + G, j + G - 1, k + G - 1)) -
+            std::fabs(lv(i + G, j + G - 1, k + G - 2) - lv(i + G, j + G - 1, k + G - 1));
+      d10 = std::fabs(lv(i + G, j + G + 1, k + G - 1) - lv(i + G, j + G, k + G - 1)) -
+            std::fabs(lv(i + G, j + G, k + G - 2) - lv(i + G, j + G, k + G - 1));
+      d01 = std::fabs(lv(i + G, j + G - 2, k + G) - lv(i + G, j + G - 1, k + G)) -
+            std::fabs(lv(i + G, j + G - 1, k + G + 1) - lv(i + G, j + G - 1, k + G));
+      d11 = std::fabs(lv(i + G, j + G + 1, k + G) - lv(i + G, j + G, k + G)) -
+            std::fabs(lv(i + G, j + G, k + G + 1) - lv(i + G, j + G, k + G));
+    } else if (dir == 2) {
+      d00 = std::fabs(lv(i + G - 1, j + G, k + G - 2) - lv(i + G - 1, j + G, k + G - 1)) -
+            std::fabs(lv(i + G - 2, j + G, k + G - 1) - lv(i + G - 1, j + G, k + G - 1));
+      d10 = std::fabs(lv(i + G - 1, j + G, k + G + 1) - lv(i + G - 1, j + G, k + G)) -
+            std::fabs(lv(i + G - 2, j + G, k + G) - lv(i + G - 1, j + G, k + G));
+      d01 = std::fabs(lv(i + G, j + G, k + G - 2) - lv(i + G, j + G, k + G - 1)) -
+            std::fabs(lv(i + G + 1, j + G, k + G - 1) - lv(i + G, j + G, k + G - 1));
+      d11 = std::fabs(lv(i + G, j + G, k + G + 1) - lv(i + G, j + G, k + G)) -
+            std::fabs(lv(i + G + 1, j + G, k + G) - lv(i + G, j + G, k + G));
+    } else {
+      d00 = std::fabs(lv(i + G - 2, j + G - 1, k + G) - lv(i + G - 1, j + G - 1, k + G)) -
+            std::fabs(lv(i + G - 1, j + G - 2, k + G) - lv(i + G - 1, j + G - 1, k + G));
+      d10 = std::fabs(lv(i + G + 1, j + G - 1, k + G) - lv(i + G, j + G - 1, k + G)) -
+            std::fabs(lv(i + G, j + G - 2, k + G) - lv(i + G, j + G - 1, k + G));
+      d01 = std::fabs(lv(i + G - 2, j + G, k + G) - lv(i + G - 1, j + G, k + G)) -
+            std::fabs(lv(i + G - 1, j + G + 1, k + G) - lv(i + G - 1, j + G, k + G));
+      d11 = std::fabs(lv(i + G + 1, j + G, k + G) - lv(i + G, j + G, k + G)) -
+            std::fabs(lv(i + G, j + G + 1, k + G) - lv(i + G, j + G, k + G));
+    }
+    return blend4(d00, d10, d01, d11, a00_0, a00_1, a10_0, a10_1, a01_0, a01_1, a11_0, a11_1);
+  }
+  static inline double blend4(double d00, double d10, double d01, double d11, double a00_0, double a00_1,
+                              double a10_0, double a10_1, double a01_0, double a01_1, double a11_0,
+                              double a11_1) {
+    d00 = fsign1(d00); d10 = fsign1(d10); d01 = fsign1(d01); d11 = fsign1(d11);
+    double v00 = (1.0 + d00) / 2.0 * a00_0 + (1.0 - d00) / 2.0 * a00_1;
+    double v10 = (1.0 + d10) / 2.0 * a10_0 + (1.0 - d10) / 2.0 * a10_1;
+    double v01 = (1.0 + d01) / 2.0 * a01_0 + (1.0 - d01) / 2.0 * a01_1;
+    double v11 = (1.0 + d11) / 2.0 * a11_0 + (1.0 - d11) / 2.0 * a11_1;
+    return 0.25 * (v00 + v01 + v10 + v11);
+  }
+
   // get_vav_center2corner (mhd3d3.f90:1858-2116)
   void get_vav_center2corner(const A3& lv, A3& vav, int dir) {
     int ii = nx0 + 1, jj = ny0 + 1, kk = nz0 + 1;
@@ -537,43 +599,36 @@ struct Oracle {
     // quadrant selection by the sign of dif (mhd3d3.f90:2056-2108)
     vav.alloc(ii, jj, kk);
     FOR3(ii, jj, kk) {
-      double d00, d10, d01, d11;
-      const int G = ng;
-      if (dir == 1) {
-        d00 = std::fabs(lv(i + G, j + G - 2, k + G - 1) - lv(i + G, j + G - 1, k + G - 1)) -
-              std::fabs(lv(i + G, j + G - 1, k + G - 2) - lv(i + G, j + G - 1, k + G - 1));
-        d10 = std::fabs(lv(i + G, j + G + 1, k + G - 1) - lv(i + G, j + G, k + G - 1)) -
-              std::fabs(lv(i + G, j + G, k + G - 2) - lv(i + G, j + G, k + G - 1));
-        d01 = std::fabs(lv(i + G, j + G - 2, k + G) - lv(i + G, j + G - 1, k + G)) -
-              std::fabs(lv(i + G, j + G - 1, k + G + 1) - lv(i + G, j + G - 1, k + G));
-        d11 = std::fabs(lv(i + G, j + G + 1, k + G) - lv(i + G, j + G, k + G)) -
-              std::fabs(lv(i + G, j + G, k + G + 1) - lv(i + G, j + G, k + G));
-      } else if (dir == 2) {
-        d00 = std::fabs(lv(i + G - 1, j + G, k + G - 2) - lv(i + G - 1, j + G, k + G - 1)) -
-              std::fabs(lv(i + G - 2, j + G, k + G - 1) - lv(i + G - 1, j + G, k + G - 1));
-        d10 = std::fabs(lv(i + G - 1, j + G, k + G + 1) - lv(i + G - 1, j + G, k + G)) -
-              std::fabs(lv(i + G - 2, j + G, k + G) - lv(i + G - 1, j + G, k + G));
-        d01 = std::fabs(lv(i + G, j + G, k + G - 2) - lv(i + G, j + G, k + G - 1)) -
-              std::fabs(lv(i + G + 1, j + G, k + G - 1) - lv(i + G, j + G, k + G - 1));
-        d11 = std::fabs(lv(i + G, j + G, k + G + 1) - lv(i + G, j + G, k + G)) -
-              std::fabs(lv(i + G + 1, j + G, k + G) - lv(i + G, j + G, k + G));
-      } else {
-        d00 = std::fabs(lv(i + G - 2, j + G - 1, k + G) - lv(i + G - 1, j + G - 1, k + G)) -
-              std::fabs(lv(i + G - 1, j + G - 2, k + G) - lv(i + G - 1, j + G - 1, k + G));
-        d10 = std::fabs(lv(i + G + 1, j + G - 1, k + G) - lv(i + G, j + G - 1, k + G)) -
-              std::fabs(lv(i + G, j + G - 2, k + G) - lv(i + G, j + G - 1, k + G));
-        d01 = std::fabs(lv(i + G - 2, j + G, k + G) - lv(i + G - 1, j + G, k + G)) -
-              std::fabs(lv(i + G - 1, j + G + 1, k + G) - lv(i + G - 1, j + G, k + G));
-        d11 = std::fabs(lv(i + G + 1, j + G, k + G) - lv(i + G, j + G, k + G)) -
-              std::fabs(lv(i + G, j + G + 1, k + G) - lv(i + G, j + G, k + G));
-      }
-      d00 = fsign1(d00); d10 = fsign1(d10); d01 = fsign1(d01); d11 = fsign1(d11);
-      double v00 = (1.0 + d00) / 2.0 * v00_0(i, j, k) + (1.0 - d00) / 2.0 * v00_1(i, j, k);
-      double v10 = (1.0 + d10) / 2.0 * v10_0(i, j, k) + (1.0 - d10) / 2.0 * v10_1(i, j, k);
-      double v01 = (1.0 + d01) / 2.0 * v01_0(i, j, k) + (1.0 - d01) / 2.0 * v01_1(i, j, k);
-      double v11 = (1.0 + d11) / 2.0 * v11_0(i, j, k) + (1.0 - d11) / 2.0 * v11_1(i, j, k);
-      vav(i, j, k) = 0.25 * (v00 + v01 + v10 + v11);
+      vav(i, j, k) = corner_blend_el(lv, dir, i, j, k, v00_0(i, j, k), v00_1(i, j, k), v10_0(i, j, k),
+                                     v10_1(i, j, k), v01_0(i, j, k), v01_1(i, j, k), v11_0(i, j, k),
+                                     v11_1(i, j, k));
     }
+  }
+
+  // The edge EMF of get_eijk_LFM (mhd3d3.f90:1806-1856) from its corner
+  // velocities and face-B states, one element.
+  inline double edge_emf_el(int kkk, int i, int j, int k, double v1av, double v2av, double b1l, double b1r,
+                            double b2l, double b2r, const A3& vf) const {
+    const int G = ng;
+    double eta;
+    if (kkk == 1)
+      eta = 0.25 * (vf(i + G, j + G - 1, k + G - 1) + vf(i + G, j + G, k + G - 1) + vf(i + G, j + G, k + G) +
+                    vf(i + G, j + G - 1, k + G));
+    else if (kkk == 2)
+      eta = 0.25 * (vf(i + G - 1, j + G, k + G - 1) + vf(i + G - 1, j + G, k + G) + vf(i + G, j + G, k + G) +
+                    vf(i + G, j + G, k + G - 1));
+    else
+      eta = 0.25 * (vf(i + G - 1, j + G - 1, k + G) + vf(i + G, j + G - 1, k + G) + vf(i + G, j + G, k + G) +
+                    vf(i + G - 1, j + G, k + G));
+    return edge_combine(v1av, v2av, b1l, b1r, b2l, b2r, eta);
+  }
+  static inline double edge_combine(double v1av, double v2av, double b1l, double b1r, double b2l, double b2r,
+                                    double eta) {
+    double sig1 = fsign1(v1av), sig2 = fsign1(v2av);
+    double b1u = (1.0 + sig2) / 2.0 * b1l + (1.0 - sig2) / 2.0 * b1r;
+    double b2u = (1.0 + sig1) / 2.0 * b2l + (1.0 - sig1) / 2.0 * b2r;
+    double dum = -v1av * b2u + v2av * b1u;
+    return dum + eta * (b1l + b2r - b1r - b2l);
   }
 
   // get_eijk_LFM (mhd3d3.f90:1754-1856)
@@ -583,6 +638,10 @@ struct Oracle {
     (void)lp;
     if (metric) {
       get_eijk_metric(lrho, lvx, lvy, lvz, lbx, lby, lbz, lbi, lbj, lbk);
+      return;
+    }
+    if (fused_edges()) {
+      get_eijk_LFM_fused(lrho, lvx, lvy, lvz, lbx, lby, lbz, lbi, lbj, lbk);
       return;
     }
     A3 vf(nx, ny, nz);
@@ -604,24 +663,9 @@ struct Oracle {
       reconstruct_3d(b2l, b2r, *b2, ii, jj, kk, d2);
       A3& e = (kkk == 1) ? ei : (kkk == 2) ? ej : ek;
       e.alloc(ii, jj, kk);
-      const int G = ng;
       FOR3(ii, jj, kk) {
-        double sig1 = fsign1(v1av(i, j, k)), sig2 = fsign1(v2av(i, j, k));
-        double b1u = (1.0 + sig2) / 2.0 * b1l(i, j, k) + (1.0 - sig2) / 2.0 * b1r(i, j, k);
-        double b2u = (1.0 + sig1) / 2.0 * b2l(i, j, k) + (1.0 - sig1) / 2.0 * b2r(i, j, k);
-        double dum = -v1av(i, j, k) * b2u + v2av(i, j, k) * b1u;
-        double eta;
-        if (kkk == 1)
-          eta = 0.25 * (vf(i + G, j + G - 1, k + G - 1) + vf(i + G, j + G, k + G - 1) +
-                        vf(i + G, j + G, k + G) + vf(i + G, j + G - 1, k + G));
-        else if (kkk == 2)
-          eta = 0.25 * (vf(i + G - 1, j + G, k + G - 1) + vf(i + G - 1, j + G, k + G) +
-                        vf(i + G, j + G, k + G) + vf(i + G, j + G, k + G - 1));
-        else
-          eta = 0.25 * (vf(i + G - 1, j + G - 1, k + G) + vf(i + G, j + G - 1, k + G) +
-                        vf(i + G, j + G, k + G) + vf(i + G - 1, j + G, k + G));
-        dum = dum + eta * (b1l(i, j, k) + b2r(i, j, k) - b1r(i, j, k) - b2l(i, j, k));
-        e(i, j, k) = dum;
+        e(i, j, k) = edge_emf_el(kkk, i, j, k, v1av(i, j, k), v2av(i, j, k), b1l(i, j, k), b1r(i, j, k),
+                                 b2l(i, j, k), b2r(i, j, k), vf);
       }
     }
   }
@@ -711,11 +755,72 @@ struct Oracle {
     v1n = lv * v0n - b;
   }
 
+  // The Gaussian-split flux of one face (get_flux_stress, mhd3d3.f90:2418-2558)
+  // from its left and right states {rho, vx, vy, vz, p, bx, by, bz}: o = {rho,
+  // rho vx, rho vy, rho vz, energy, stress x, y, z} fluxes along axis kkk.
+  inline void flux_el(int kkk, const double* L, const double* R, double* o) const {
+    double v0p, v0n, v1p, v1n;
+    // left flux
+    double r = L[0], u = L[1], v = L[2], w = L[3], pp_ = L[4];
+    double b1 = L[5], b2 = L[6], b3 = L[7];
+    double vn = (kkk == 1) ? u : (kkk == 2) ? v : w;
+    double bn = (kkk == 1) ? b1 : (kkk == 2) ? b2 : b3;
+    double leng = 0.5 * r * (u * u + v * v + w * w) + pp_ / (gam - 1.0);
+    double llam = r / (2.0 * pp_);
+    v_face(llam, vn, v0p, v0n, v1p, v1n);
+    double rp = r * v1p;
+    double rvxp = r * u * v1p, rvyp = r * v * v1p, rvzp = r * w * v1p;
+    double ep = (leng + 0.5 * pp_) * v1p;
+    if (kkk == 1) rvxp = rvxp + pp_ * v0p;
+    else if (kkk == 2) rvyp = rvyp + pp_ * v0p;
+    else rvzp = rvzp + pp_ * v0p;
+    ep = ep + 0.5 * pp_ * vn * v0p;
+    double lbsq = b1 * b1 + b2 * b2 + b3 * b3;
+    llam = r / (2.0 * pp_ + lbsq);
+    v_face(llam, vn, v0p, v0n, v1p, v1n);
+    double sxp = ((kkk == 1) ? (0.5 * lbsq - b1 * b1) : (-b1 * bn)) * v0p;
+    double syp = ((kkk == 2) ? (0.5 * lbsq - b2 * b2) : (-b2 * bn)) * v0p;
+    double szp = ((kkk == 3) ? (0.5 * lbsq - b3 * b3) : (-b3 * bn)) * v0p;
+    // right flux
+    r = R[0]; u = R[1]; v = R[2]; w = R[3]; pp_ = R[4];
+    b1 = R[5]; b2 = R[6]; b3 = R[7];
+    vn = (kkk == 1) ? u : (kkk == 2) ? v : w;
+    bn = (kkk == 1) ? b1 : (kkk == 2) ? b2 : b3;
+    leng = 0.5 * r * (u * u + v * v + w * w) + pp_ / (gam - 1.0);
+    llam = r / (2.0 * pp_);
+    v_face(llam, vn, v0p, v0n, v1p, v1n);
+    double rn = r * v1n;
+    double rvxn = r * u * v1n, rvyn = r * v * v1n, rvzn = r * w * v1n;
+    double en = (leng + 0.5 * pp_) * v1n;
+    if (kkk == 1) rvxn = rvxn + pp_ * v0n;
+    else if (kkk == 2) rvyn = rvyn + pp_ * v0n;
+    else rvzn = rvzn + pp_ * v0n;
+    en = en + 0.5 * pp_ * vn * v0n;
+    lbsq = b1 * b1 + b2 * b2 + b3 * b3;
+    llam = r / (2.0 * pp_ + lbsq);
+    v_face(llam, vn, v0p, v0n, v1p, v1n);
+    double sxn = ((kkk == 1) ? (0.5 * lbsq - b1 * b1) : (-b1 * bn)) * v0n;
+    double syn = ((kkk == 2) ? (0.5 * lbsq - b2 * b2) : (-b2 * bn)) * v0n;
+    double szn = ((kkk == 3) ? (0.5 * lbsq - b3 * b3) : (-b3 * bn)) * v0n;
+    o[0] = rp + rn;
+    o[1] = rvxp + rvxn;
+    o[2] = rvyp + rvyn;
+    o[3] = rvzp + rvzn;
+    o[4] = ep + en;
+    o[5] = sxp + sxn;
+    o[6] = syp + syn;
+    o[7] = szp + szn;
+  }
+
   // get_flux_stress (mhd3d3.f90:2385-2560)
   void get_flux_stress(const A3& lrho, const A3& lvx, const A3& lvy, const A3& lvz, const A3& lp,
                        const A3& lbx, const A3& lby, const A3& lbz) {
     if (metric) {
       get_flux_stress_metric(lrho, lvx, lvy, lvz, lp, lbx, lby, lbz);
+      return;
+    }
+    if (fused) {
+      get_flux_stress_fused(lrho, lvx, lvy, lvz, lp, lbx, lby, lbz);
       return;
     }
     for (int kkk = 1; kkk <= 3; ++kkk) {
@@ -735,58 +840,211 @@ struct Oracle {
       A3* out = flux[kkk - 1];
       for (int q = 0; q < 8; ++q) out[q].alloc(ii, jj, kk);
       FOR3(ii, jj, kk) {
-        double v0p, v0n, v1p, v1n;
-        // left flux
-        double r = rhol(i, j, k), u = vxl(i, j, k), v = vyl(i, j, k), w = vzl(i, j, k), pp_ = pl(i, j, k);
-        double b1 = bxl(i, j, k), b2 = byl(i, j, k), b3 = bzl(i, j, k);
-        double vn = (kkk == 1) ? u : (kkk == 2) ? v : w;
-        double bn = (kkk == 1) ? b1 : (kkk == 2) ? b2 : b3;
-        double leng = 0.5 * r * (u * u + v * v + w * w) + pp_ / (gam - 1.0);
-        double llam = r / (2.0 * pp_);
-        v_face(llam, vn, v0p, v0n, v1p, v1n);
-        double rp = r * v1p;
-        double rvxp = r * u * v1p, rvyp = r * v * v1p, rvzp = r * w * v1p;
-        double ep = (leng + 0.5 * pp_) * v1p;
-        if (kkk == 1) rvxp = rvxp + pp_ * v0p;
-        else if (kkk == 2) rvyp = rvyp + pp_ * v0p;
-        else rvzp = rvzp + pp_ * v0p;
-        ep = ep + 0.5 * pp_ * vn * v0p;
-        double lbsq = b1 * b1 + b2 * b2 + b3 * b3;
-        llam = r / (2.0 * pp_ + lbsq);
-        v_face(llam, vn, v0p, v0n, v1p, v1n);
-        double sxp = ((kkk == 1) ? (0.5 * lbsq - b1 * b1) : (-b1 * bn)) * v0p;
-        double syp = ((kkk == 2) ? (0.5 * lbsq - b2 * b2) : (-b2 * bn)) * v0p;
-        double szp = ((kkk == 3) ? (0.5 * lbsq - b3 * b3) : (-b3 * bn)) * v0p;
-        // right flux
-        r = rhor(i, j, k); u = vxr(i, j, k); v = vyr(i, j, k); w = vzr(i, j, k); pp_ = pr(i, j, k);
-        b1 = bxr(i, j, k); b2 = byr(i, j, k); b3 = bzr(i, j, k);
-        vn = (kkk == 1) ? u : (kkk == 2) ? v : w;
-        bn = (kkk == 1) ? b1 : (kkk == 2) ? b2 : b3;
-        leng = 0.5 * r * (u * u + v * v + w * w) + pp_ / (gam - 1.0);
-        llam = r / (2.0 * pp_);
-        v_face(llam, vn, v0p, v0n, v1p, v1n);
-        double rn = r * v1n;
-        double rvxn = r * u * v1n, rvyn = r * v * v1n, rvzn = r * w * v1n;
-        double en = (leng + 0.5 * pp_) * v1n;
-        if (kkk == 1) rvxn = rvxn + pp_ * v0n;
-        else if (kkk == 2) rvyn = rvyn + pp_ * v0n;
-        else rvzn = rvzn + pp_ * v0n;
-        en = en + 0.5 * pp_ * vn * v0n;
-        lbsq = b1 * b1 + b2 * b2 + b3 * b3;
-        llam = r / (2.0 * pp_ + lbsq);
-        v_face(llam, vn, v0p, v0n, v1p, v1n);
-        double sxn = ((kkk == 1) ? (0.5 * lbsq - b1 * b1) : (-b1 * bn)) * v0n;
-        double syn = ((kkk == 2) ? (0.5 * lbsq - b2 * b2) : (-b2 * bn)) * v0n;
-        double szn = ((kkk == 3) ? (0.5 * lbsq - b3 * b3) : (-b3 * bn)) * v0n;
-        out[0](i, j, k) = rp + rn;
-        out[1](i, j, k) = rvxp + rvxn;
-        out[2](i, j, k) = rvyp + rvyn;
-        out[3](i, j, k) = rvzp + rvzn;
-        out[4](i, j, k) = ep + en;
-        out[5](i, j, k) = sxp + sxn;
-        out[6](i, j, k) = syp + syn;
-        out[7](i, j, k) = szp + szn;
+        const double L[8] = {rhol(i, j, k), vxl(i, j, k), vyl(i, j, k), vzl(i, j, k),
+                             pl(i, j, k),   bxl(i, j, k), byl(i, j, k), bzl(i, j, k)};
+        const double R[8] = {rhor(i, j, k), vxr(i, j, k), vyr(i, j, k), vzr(i, j, k),
+                             pr(i, j, k),   bxr(i, j, k), byr(i, j, k), bzr(i, j, k)};
+        double o[8];
+        flux_el(kkk, L, R, o);
+        for (int q = 0; q < 8; ++q) out[q](i, j, k) = o[q];
       }
+    }
+  }
+
+  // ------------------------------------------------- fused (optimised) mode
+  // One pass per face family and per edge family: every reconstruction is
+  // evaluated where it is used, from the cell arrays, with no face, edge or
+  // interpolant temporaries (the array passes above allocate and stream about
+  // thirty of them per stage).  Each element calls the same element functions
+  // as the array passes in the same order, so the two modes give identical
+  // bits.  Cartesian meshes; the edge pass covers PDM / TVD / TVD-MC (the
+  // two-level WENO corner reconstruction is not separable per edge and keeps
+  // its array form), the face pass every reconstruction.
+  bool fused = false;
+
+  // Address of f(i, j, k) and the element stride along axis dir (1, 2, 3).
+  static inline const double* at(const A3& f, int i, int j, int k) {
+    return f.v.data() + ((size_t)(i - 1) + (size_t)f.n1 * ((size_t)(j - 1) + (size_t)f.n2 * (size_t)(k - 1)));
+  }
+  static inline ptrdiff_t stride(const A3& f, int dir) {
+    return dir == 1 ? 1 : dir == 2 ? (ptrdiff_t)f.n1 : (ptrdiff_t)f.n1 * f.n2;
+  }
+
+  // reconstruct_3d (mhd3d3.f90:833-860) along one line of n elements: element
+  // t reconstructs from c[t + m * s], m = -3..2, s the stride of the recon
+  // axis.  One loop per reconstruction, no branches inside: it vectorises.
+  template <int RECON>
+  void recon_line(const double* c, ptrdiff_t s, int n, double* __restrict L, double* __restrict R) const {
+    for (int t = 0; t < n; ++t) {
+      const double* e = c + t;
+      if constexpr (RECON == 1) {
+        double fi = tap8(e[-4 * s], e[-3 * s], e[-2 * s], e[-s], e[0], e[s], e[2 * s], e[3 * s]);
+        pdm2_el(e[-2 * s], e[-s], e[0], e[s], fi, L[t], R[t]);
+      } else if constexpr (RECON == 2 || RECON == 5) {
+        double fi = (e[-s] + e[0]) / 2.0;
+        tvd_el(e[-2 * s], e[-s], e[0], e[s], fi, RECON == 5, L[t], R[t]);
+      } else {
+        double fm3 = e[-3 * s], fm2 = e[-2 * s], fm1 = e[-s], f0 = e[0], fp1 = e[s], fp2 = e[2 * s], fl, fr;
+        weno5_pt(fm3, fm2, fm1, f0, fp1, fp2, eps, fl, fr);
+        if constexpr (RECON == 4) {
+          fl = mp_side(fl, fm3, fm2, fm1, f0, fp1, alpha, beta);
+          fr = mp_side(fr, fp2, fp1, f0, fm1, fm2, alpha, beta);
+        }
+        L[t] = fl;
+        R[t] = fr;
+      }
+    }
+  }
+  void recon_line_any(const double* c, ptrdiff_t s, int n, double* L, double* R) const {
+    switch (reconop) {
+      case 1: recon_line<1>(c, s, n, L, R); break;
+      case 2: recon_line<2>(c, s, n, L, R); break;
+      case 3: recon_line<3>(c, s, n, L, R); break;
+      case 4: recon_line<4>(c, s, n, L, R); break;
+      default: recon_line<5>(c, s, n, L, R); break;
+    }
+  }
+
+  // get_vav_center2corner (mhd3d3.f90:1858-2116) along one line of n edges
+  // (PDM / TVD).  Element t sits at c + t; sp and sq are the strides of the
+  // edge's two transverse axes in the reference's order (edges along x: y, z;
+  // along y: z, x; along z: x, y) -- interp2's first and second pass, the
+  // limiters' axes and the quadrant differences all follow from them.
+  // w: scratch of 17 lines.
+  template <int RECON>
+  void corner_line(const double* c, ptrdiff_t sp, ptrdiff_t sq, int n, double* __restrict out,
+                   double* __restrict w, int W) const {
+    double* vi = w;
+    if constexpr (RECON == 1) {  // interp2_pdm: 8-tap along p, then along q
+      double* g = w + W;
+      for (int q = 0; q < 8; ++q) {
+        const double* r = c + (q - 4) * sq;
+        double* gq = g + q * W;
+        for (int t = 0; t < n; ++t) {
+          const double* e = r + t;
+          gq[t] = tap8(e[-4 * sp], e[-3 * sp], e[-2 * sp], e[-sp], e[0], e[sp], e[2 * sp], e[3 * sp]);
+        }
+      }
+      for (int t = 0; t < n; ++t)
+        vi[t] = tap8(g[t], g[W + t], g[2 * W + t], g[3 * W + t], g[4 * W + t], g[5 * W + t], g[6 * W + t],
+                     g[7 * W + t]);
+    } else {  // interp2_tvd: 4-cell mean
+      for (int t = 0; t < n; ++t) {
+        const double* e = c + t;
+        vi[t] = (e[-sp - sq] + e[-sq] + e[0] + e[-sp]) / 4.0;
+      }
+    }
+    // the four limited pairs: (base shift, axis) = (-q, p), (-p, q), (0, q), (0, p);
+    // TVD without the stencil-shift option drops the shifts
+    const bool shift = (RECON == 1) || tvd_shift;
+    double *a00_0 = w + 9 * W, *a10_0 = w + 10 * W, *a00_1 = w + 11 * W, *a01_1 = w + 12 * W;
+    double *a10_1 = w + 13 * W, *a11_1 = w + 14 * W, *a01_0 = w + 15 * W, *a11_0 = w + 16 * W;
+    auto lim = [&](const double* b, ptrdiff_t s, double* A, double* B) {
+      for (int t = 0; t < n; ++t) {
+        const double* e = b + t;
+        if constexpr (RECON == 1) pdm2_el(e[-2 * s], e[-s], e[0], e[s], vi[t], A[t], B[t]);
+        else tvd_el(e[-2 * s], e[-s], e[0], e[s], vi[t], RECON == 5, A[t], B[t]);
+      }
+    };
+    lim(shift ? c - sq : c, sp, a00_0, a10_0);
+    lim(shift ? c - sp : c, sq, a00_1, a01_1);
+    lim(c, sq, a10_1, a11_1);
+    lim(c, sp, a01_0, a11_0);
+    // quadrant selection (mhd3d3.f90:2056-2108)
+    for (int t = 0; t < n; ++t) {
+      const double* e = c + t;
+      double d00 = std::fabs(e[-2 * sp - sq] - e[-sp - sq]) - std::fabs(e[-sp - 2 * sq] - e[-sp - sq]);
+      double d10 = std::fabs(e[sp - sq] - e[-sq]) - std::fabs(e[-2 * sq] - e[-sq]);
+      double d01 = std::fabs(e[-2 * sp] - e[-sp]) - std::fabs(e[-sp + sq] - e[-sp]);
+      double d11 = std::fabs(e[sp] - e[0]) - std::fabs(e[sq] - e[0]);
+      out[t] = blend4(d00, d10, d01, d11, a00_0[t], a00_1[t], a10_0[t], a10_1[t], a01_0[t], a01_1[t], a11_0[t],
+                      a11_1[t]);
+    }
+  }
+  void corner_line_any(const double* c, ptrdiff_t sp, ptrdiff_t sq, int n, double* out, double* w, int W) const {
+    if (reconop == 1) corner_line<1>(c, sp, sq, n, out, w, W);
+    else if (reconop == 2) corner_line<2>(c, sp, sq, n, out, w, W);
+    else corner_line<5>(c, sp, sq, n, out, w, W);
+  }
+
+  bool fused_edges() const { return fused && !metric && (reconop == 1 || reconop == 2 || reconop == 5); }
+
+  // Runs body(j, k, buf, W) over the (j, k) lines of a jj x kk family, OpenMP
+  // over k; buf holds nq per-thread line buffers of W = nx + 1 entries.
+  template <class Body> void lines(int jj, int kk, int nq, Body body) {
+    const int W = nx + 1;
+#pragma omp parallel
+    {
+      std::vector<double> buf((size_t)nq * W);
+#pragma omp for schedule(static)
+      for (int k = 1; k <= kk; ++k)
+        for (int j = 1; j <= jj; ++j) body(j, k, buf.data(), W);
+    }
+  }
+
+  // get_eijk_LFM in one pass per edge family.  Per x line of edges: the two
+  // corner velocities and the two face-B states into line buffers (unit-stride
+  // loops over i that the compiler vectorises), then the edge combine.
+  void get_eijk_LFM_fused(const A3& lrho, const A3& lvx, const A3& lvy, const A3& lvz, const A3& lbx,
+                          const A3& lby, const A3& lbz, const A3& lbi, const A3& lbj, const A3& lbk) {
+    A3 vf(nx, ny, nz);
+    FOR3(nx, ny, nz) {
+      double u = lvx(i, j, k), v = lvy(i, j, k), w = lvz(i, j, k);
+      double a = lbx(i, j, k), b = lby(i, j, k), c = lbz(i, j, k);
+      vf(i, j, k) = std::sqrt(u * u + v * v + w * w) + std::sqrt((a * a + b * b + c * c) / lrho(i, j, k));
+    }
+    for (int kkk = 1; kkk <= 3; ++kkk) {
+      int ii = nx0 + 1, jj = ny0 + 1, kk = nz0 + 1, d1, d2;
+      const A3 *v1, *v2, *b1, *b2;
+      if (kkk == 1) { ii = nx0; v1 = &lvy; v2 = &lvz; b1 = &lbj; b2 = &lbk; d1 = 3; d2 = 2; }
+      else if (kkk == 2) { jj = ny0; v1 = &lvz; v2 = &lvx; b1 = &lbk; b2 = &lbi; d1 = 1; d2 = 3; }
+      else { kk = nz0; v1 = &lvx; v2 = &lvy; b1 = &lbi; b2 = &lbj; d1 = 2; d2 = 1; }
+      A3& e = (kkk == 1) ? ei : (kkk == 2) ? ej : ek;
+      e.alloc(ii, jj, kk);
+      const ptrdiff_t sp = stride(vf, kkk == 1 ? 2 : kkk == 2 ? 3 : 1);
+      const ptrdiff_t sq = stride(vf, kkk == 1 ? 3 : kkk == 2 ? 1 : 2);
+      lines(jj, kk, 6 + 17, [&](int j, int k, double* b, int W) {
+        double *v1a = b, *v2a = b + W, *b1l = b + 2 * W, *b1r = b + 3 * W, *b2l = b + 4 * W, *b2r = b + 5 * W;
+        corner_line_any(at(*v1, ng + 1, ng + j, ng + k), sp, sq, ii, v1a, b + 6 * W, W);
+        corner_line_any(at(*v2, ng + 1, ng + j, ng + k), sp, sq, ii, v2a, b + 6 * W, W);
+        recon_line_any(at(*b1, ng + 1, ng + j, ng + k), stride(*b1, d1), ii, b1l, b1r);
+        recon_line_any(at(*b2, ng + 1, ng + j, ng + k), stride(*b2, d2), ii, b2l, b2r);
+        const double* cv = at(vf, ng + 1, ng + j, ng + k);
+        double* eo = &e(1, j, k);
+        for (int t = 0; t < ii; ++t) {
+          const double* v = cv + t;
+          const double eta = 0.25 * (v[-sp - sq] + v[-sq] + v[0] + v[-sp]);
+          eo[t] = edge_combine(v1a[t], v2a[t], b1l[t], b1r[t], b2l[t], b2r[t], eta);
+        }
+      });
+    }
+  }
+
+  // get_flux_stress in one pass per face family: per x line of faces the 16
+  // reconstructed states into line buffers, then the fluxes.
+  void get_flux_stress_fused(const A3& lrho, const A3& lvx, const A3& lvy, const A3& lvz, const A3& lp,
+                             const A3& lbx, const A3& lby, const A3& lbz) {
+    const A3* src[8] = {&lrho, &lvx, &lvy, &lvz, &lp, &lbx, &lby, &lbz};
+    for (int kkk = 1; kkk <= 3; ++kkk) {
+      int ii = nx0, jj = ny0, kk = nz0;
+      if (kkk == 1) ii = nx0 + 1;
+      if (kkk == 2) jj = ny0 + 1;
+      if (kkk == 3) kk = nz0 + 1;
+      A3* out = flux[kkk - 1];
+      for (int q = 0; q < 8; ++q) out[q].alloc(ii, jj, kk);
+      lines(jj, kk, 16, [&](int j, int k, double* b, int W) {
+        for (int q = 0; q < 8; ++q)
+          recon_line_any(at(*src[q], ng + 1, ng + j, ng + k), stride(*src[q], kkk), ii, b + q * W, b + (8 + q) * W);
+        for (int i = 1; i <= ii; ++i) {
+          double L[8], R[8], o[8];
+          for (int q = 0; q < 8; ++q) {
+            L[q] = b[q * W + i - 1];
+            R[q] = b[(8 + q) * W + i - 1];
+          }
+          flux_el(kkk, L, R, o);
+          for (int q = 0; q < 8; ++q) out[q](i, j, k) = o[q];
+        }
+      });
     }
   }
 
@@ -1482,6 +1740,14 @@ int oracle_recon_line(const mhd_params* prm, int n, const double* f, double* fl,
 }
 
 void oracle_free(void* h) { delete (Oracle*)h; }
+
+// Fused mode of the following steps of handle h: one pass per face / edge
+// family with no intermediate arrays; identical results to the array passes.
+int oracle_set_fused(void* h, int on) {
+  if (!h) return MHD_E_ARG;
+  ((Oracle*)h)->fused = (on != 0);
+  return 0;
+}
 
 int oracle_threads(void) { return omp_get_max_threads(); }
 

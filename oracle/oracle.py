@@ -49,6 +49,7 @@ def load():
         lib.oracle_recon_line.argtypes = [C.POINTER(CParams), C.c_int, _DP, _DP, _DP]
         lib.oracle_free.argtypes = [C.c_void_p]
         lib.oracle_set_threads.argtypes = [C.c_int]
+        lib.oracle_set_fused.argtypes = [C.c_void_p, C.c_int]
         _lib = lib
     return _lib
 
@@ -83,6 +84,13 @@ class OracleSolver:
                np.ascontiguousarray(g.dy if dy is None else dy, dtype=np.float64),
                np.ascontiguousarray(g.dz if dz is None else dz, dtype=np.float64)]
         self.h = self.lib.oracle_init(C.byref(self._cp), *[_ptr(a) for a in arrs], *[_ptr(a) for a in geo])
+
+    def set_fused(self, on: bool = True) -> None:
+        """Fused mode of the following steps: one pass per face / edge family,
+        reconstructions evaluated at the point of use, no intermediate arrays;
+        the same results as the array passes, bit for bit."""
+        if self.lib.oracle_set_fused(self.h, 1 if on else 0) != 0:
+            raise RuntimeError("oracle_set_fused failed")
 
     def step(self, n: int = 1):
         tau = C.c_double()
