@@ -1,0 +1,379 @@
+"""ORACLE -- test infrastructure only.  Nothing in the product path imports
+this file; tests use it to cross-check the C++ oracle.
+
+A second, independent restatement of the reference's per-timestep update
+(tiegcm/mhd3d_mpi_fortran, mhd3d3.f90), written in vectorised numpy straight
+from the Fortran: one whole-array expression per Fortran statement or
+``forall``, in the Fortran's own operand order.  It shares no code with
+``oracle/mhd_oracle.cpp`` (a loop-per-element C++ restatement), so a
+transcription slip in either shows up as a disagreement between them.
+
+Scope -- the path the throughput benchmark runs: Cartesian mesh, periodic
+halos on every axis (one rank of mhd3d2.f90's periodic topology:
+the SENDRECVs of fillx_center / fillx_face, mhd3d3.f90:346-390 / 482-525,
+exchange with the rank itself), reconop 1 (PDM) or 2 (TVD, van Leer), LFM
+edge EMF, stepop 2 (RK2) with the deck's fixed tau (step_rk2, 3646-3711).
+
+Arrays are indexed [i, j, k] from 0: numpy index n is Fortran index n + 1.
+``erfc`` is scipy's and ``exp`` numpy's, so agreement with the C++ oracle
+(glibc) is to round-off, not bit for bit.
+"""
+from __future__ import annotations
+
+import numpy as np
+from scipy.special import erfc
+
+
+def _sign1(x):
+    # sign(1., x): +1 for x >= 0 (including -0.0), -1 otherwise
+    return np.where(x >= 0.0, 1.0, -1.0)
+
+
+def _max(a, b):
+    return np.where(a > b, a, b)
+
+
+def _min(a, b):
+    return np.where(a < b, a, b)
+
+
+def _tap8(a0, a1, a2, a3, a4, a5, a6, a7):
+    # the 8-point interpolant of interp_pdm (mhd3d3.f90:862-924)
+    return (-3. * a0 + 29. * a1 - 139. * a2 + 533. * a3 + 533. * a4 - 139. * a5 + 29. * a6 - 3. * a7) / 840.
+
+
+class NumpyMHD:
+    """One grid of the reference's state, advanced by RK2 steps."""
+
+    def __init__(self, params, state):
+        p = params
+        if p.stepop != 2 or p.reconop not in (1, 2) or any(b != 0 for b in p.bc) or p.emf != 0:
+            raise ValueError("NumpyMHD covers periodic PDM/TVD + LFM + RK2 only")
+        self.nx0, self.ny0, self.nz0 = p.nx0, p.ny0, p.nz0
+        self.ng, self.nord = p.nord // 2, p.nord
+        self.nx, self.ny, self.nz = p.nx0 + p.nord, p.ny0 + p.nord, p.nz0 + p.nord
+        self.reconop, self.gam, self.pdmb, self.eps = p.reconop, p.gam, p.pdmb, p.eps
+        self.tau = self.tau0 = p.tau
+        self.pi = 4. * np.arctan(1.0)  # pars: pi=4.*atan(1.0_8)
+        g = state.grid
+        ng = self.ng
+        # dxblock(ng+i, ng+j, ng+k) of the interior cells
+        self.dx = np.asarray(g.dx)[ng:ng + self.nx0][:, None, None]
+        self.dy = np.asarray(g.dy)[ng:ng + self.ny0][None, :, None]
+        self.dz = np.asarray(g.dz)[ng:ng + self.nz0][None, None, :]
+        c = lambda a: np.array(a, dtype=np.float64)
+        self.rho, self.vx, self.vy, self.vz, self.p = (c(a) for a in state.arrays()[:5])
+        self.bi, self.bj, self.bk = (c(a) for a in state.arrays()[5:])
+        # initialisation (mhd3d3.f90:3349-3351)
+        self.fill_hydro()
+        self.fill_mag()
+        self.get_bxyz()
+
+    # ------------------------------------------------------------ indexing
+    def _take(self, f, off, lens, axes=(0, 1, 2)):
+        """f(ng+i+off0, ng+j+off1, ng+k+off2) for i=1..lens0 etc.; an axis not
+        in ``axes`` is taken whole (the ':' of the dir 4..6 forms)."""
+        sl = []
+        for a in range(3):
+            if a in axes:
+                s = self.ng + off[a]
+                sl.append(slice(s, s + lens[a]))
+            else:
+                sl.append(slice(None))
+        return f[tuple(sl)]
+
+    def _stencil(self, f, d, lens, shift=(0, 0, 0), ms=range(-4, 4)):
+        """[f at offset m along axis d] for m in ms, the element grid lens."""
+        out = []
+        for m in ms:
+            off = list(shift)
+            off[d] += m
+            out.append(self._take(f, off, lens))
+        return out
+
+    # ------------------------------------------------------ reconstruction
+    def interp(self, f, lens, d):
+        """interp_pdm / interp_tvd (mhd3d3.f90:862-924, 991-1035), axis d = 0,1,2."""
+        if self.reconop == 1:
+            return _tap8(*self._stencil(f, d, lens))
+        fm1, f0 = self._stencil(f, d, lens, ms=(-1, 0))
+        return (fm1 + f0) / 2.
+
+    def limit(self, f, fi, lens, d, shift=(0, 0, 0)):
+        """PDM2 (mhd3d3.f90:1069-1172) or TVD (1174-1250, which drops the shifts)."""
+        if self.reconop == 2:
+            shift = (0, 0, 0)
+        fm2, fm1, f0, fp1 = self._stencil(f, d, lens, shift, ms=(-2, -1, 0, 1))
+        if self.reconop == 2:
+            eps = self.eps
+            a = (fm1 - fm2) / (f0 - fm1 + eps)
+            b = (a + np.abs(a)) / (1. + np.abs(a))
+            fleft = fm1 - b * (fm1 - fi)
+            a = (f0 - fp1) / (fm1 - f0 + eps)
+            b = (a + np.abs(a)) / (1. + np.abs(a))
+            fright = f0 - b * (f0 - fi)
+            return fleft, fright
+        maxf = _max(fm1, f0)
+        minf = _min(fm1, f0)
+        fii = _max(minf, _min(fi, maxf))
+        dfm = self.pdmb * (fm1 - fm2)
+        df0 = self.pdmb * (f0 - fm1)
+        dfp = self.pdmb * (fp1 - f0)
+        sm, s0, sp = _sign1(dfm), _sign1(df0), _sign1(dfp)
+        dfm, dfp = np.abs(dfm), np.abs(dfp)
+        qm = np.abs(sm + s0)
+        qp = np.abs(s0 + sp)
+        dfl = fii - fm1
+        dfr = f0 - fii
+        fleft = fii - s0 * _max(0., np.abs(dfl) - qm * dfm)
+        fright = fii + s0 * _max(0., np.abs(dfr) - qp * dfp)
+        return fleft, fright
+
+    def reconstruct(self, f, lens, d):
+        """reconstruct_3d (mhd3d3.f90:833-860) for dir = d+1 in 1..3."""
+        return self.limit(f, self.interp(f, lens, d), lens, d)
+
+    def interp2(self, f, dirn, lens):
+        """interp2_pdm / interp2_tvd (mhd3d3.f90:926-989, 1037-1067), edge family dirn = 1..3."""
+        ng = self.ng
+        if self.reconop == 2:
+            o = {1: [(0, -1, -1), (0, 0, -1), (0, 0, 0), (0, -1, 0)],
+                 2: [(-1, 0, -1), (-1, 0, 0), (0, 0, 0), (0, 0, -1)],
+                 3: [(-1, -1, 0), (0, -1, 0), (0, 0, 0), (-1, 0, 0)]}[dirn]
+            a, b, c, e = (self._take(f, off, lens) for off in o)
+            return (a + b + c + e) / 4.
+        ii, jj, kk = lens
+        if dirn == 1:  # along y over (nx0, ny0+1, nz), then along z
+            g = _tap8(*[self._take(f, (0, m, 0), (ii, jj, 0), axes=(0, 1)) for m in range(-4, 4)])
+            return _tap8(*[g[:, :, ng + m:ng + m + kk] for m in range(-4, 4)])
+        if dirn == 2:  # along z over (nx, ny0, nz0+1), then along x
+            g = _tap8(*[self._take(f, (0, 0, m), (0, jj, kk), axes=(1, 2)) for m in range(-4, 4)])
+            return _tap8(*[g[ng + m:ng + m + ii, :, :] for m in range(-4, 4)])
+        # along x over (nx0+1, ny, nz0), then along y
+        g = _tap8(*[self._take(f, (m, 0, 0), (ii, 0, kk), axes=(0, 2)) for m in range(-4, 4)])
+        return _tap8(*[g[:, ng + m:ng + m + jj, :] for m in range(-4, 4)])
+
+    def vav_center2corner(self, lv, dirn, lens):
+        """get_vav_center2corner (mhd3d3.f90:1858-2116) for PDM / TVD."""
+        vi = self.interp2(lv, dirn, lens)
+        # (shift, axis) of the four limited pairs, axis 0-based
+        calls = {1: [((0, 0, -1), 1), ((0, -1, 0), 2), ((0, 0, 0), 2), ((0, 0, 0), 1)],
+                 2: [((-1, 0, 0), 2), ((0, 0, -1), 0), ((0, 0, 0), 0), ((0, 0, 0), 2)],
+                 3: [((0, -1, 0), 0), ((-1, 0, 0), 1), ((0, 0, 0), 1), ((0, 0, 0), 0)]}[dirn]
+        v00_0, v10_0 = self.limit(lv, vi, lens, calls[0][1], calls[0][0])
+        v00_1, v01_1 = self.limit(lv, vi, lens, calls[1][1], calls[1][0])
+        v10_1, v11_1 = self.limit(lv, vi, lens, calls[2][1], calls[2][0])
+        v01_0, v11_0 = self.limit(lv, vi, lens, calls[3][1], calls[3][0])
+        T = lambda off: self._take(lv, off, lens)
+        if dirn == 1:
+            dif00 = np.abs(T((0, -2, -1)) - T((0, -1, -1))) - np.abs(T((0, -1, -2)) - T((0, -1, -1)))
+            dif10 = np.abs(T((0, 1, -1)) - T((0, 0, -1))) - np.abs(T((0, 0, -2)) - T((0, 0, -1)))
+            dif01 = np.abs(T((0, -2, 0)) - T((0, -1, 0))) - np.abs(T((0, -1, 1)) - T((0, -1, 0)))
+            dif11 = np.abs(T((0, 1, 0)) - T((0, 0, 0))) - np.abs(T((0, 0, 1)) - T((0, 0, 0)))
+        elif dirn == 2:
+            dif00 = np.abs(T((-1, 0, -2)) - T((-1, 0, -1))) - np.abs(T((-2, 0, -1)) - T((-1, 0, -1)))
+            dif10 = np.abs(T((-1, 0, 1)) - T((-1, 0, 0))) - np.abs(T((-2, 0, 0)) - T((-1, 0, 0)))
+            dif01 = np.abs(T((0, 0, -2)) - T((0, 0, -1))) - np.abs(T((1, 0, -1)) - T((0, 0, -1)))
+            dif11 = np.abs(T((0, 0, 1)) - T((0, 0, 0))) - np.abs(T((1, 0, 0)) - T((0, 0, 0)))
+        else:
+            dif00 = np.abs(T((-2, -1, 0)) - T((-1, -1, 0))) - np.abs(T((-1, -2, 0)) - T((-1, -1, 0)))
+            dif10 = np.abs(T((1, -1, 0)) - T((0, -1, 0))) - np.abs(T((0, -2, 0)) - T((0, -1, 0)))
+            dif01 = np.abs(T((-2, 0, 0)) - T((-1, 0, 0))) - np.abs(T((-1, 1, 0)) - T((-1, 0, 0)))
+            dif11 = np.abs(T((1, 0, 0)) - T((0, 0, 0))) - np.abs(T((0, 1, 0)) - T((0, 0, 0)))
+        dif00, dif10, dif01, dif11 = (_sign1(x) for x in (dif00, dif10, dif01, dif11))
+        v00 = (1. + dif00) / 2. * v00_0 + (1. - dif00) / 2. * v00_1
+        v10 = (1. + dif10) / 2. * v10_0 + (1. - dif10) / 2. * v10_1
+        v01 = (1. + dif01) / 2. * v01_0 + (1. - dif01) / 2. * v01_1
+        v11 = (1. + dif11) / 2. * v11_0 + (1. - dif11) / 2. * v11_1
+        return .25 * (v00 + v01 + v10 + v11)
+
+    # ------------------------------------------------------------- get_*
+    def get_eijk_LFM(self, rho, vx, vy, vz, bx, by, bz, bi, bj, bk):
+        """get_eijk_LFM (mhd3d3.f90:1754-1856) -> [ei, ej, ek]."""
+        nx0, ny0, nz0 = self.nx0, self.ny0, self.nz0
+        vf = np.sqrt(vx ** 2 + vy ** 2 + vz ** 2) + np.sqrt((bx ** 2 + by ** 2 + bz ** 2) / rho)
+        out = []
+        for kkk in (1, 2, 3):
+            lens = [nx0 + 1, ny0 + 1, nz0 + 1]
+            lens[kkk - 1] -= 1
+            v1, v2, b1, b2, d1, d2 = {1: (vy, vz, bj, bk, 3, 2), 2: (vz, vx, bk, bi, 1, 3),
+                                      3: (vx, vy, bi, bj, 2, 1)}[kkk]
+            v1av = self.vav_center2corner(v1, kkk, lens)
+            v2av = self.vav_center2corner(v2, kkk, lens)
+            sig1, sig2 = _sign1(v1av), _sign1(v2av)
+            b1l, b1r = self.reconstruct(b1, lens, d1 - 1)
+            b2l, b2r = self.reconstruct(b2, lens, d2 - 1)
+            b1u = (1. + sig2) / 2. * b1l + (1. - sig2) / 2. * b1r
+            b2u = (1. + sig1) / 2. * b2l + (1. - sig1) / 2. * b2r
+            dum = -v1av * b2u + v2av * b1u
+            T = lambda off: self._take(vf, off, lens)
+            o = {1: [(0, -1, -1), (0, 0, -1), (0, 0, 0), (0, -1, 0)],
+                 2: [(-1, 0, -1), (-1, 0, 0), (0, 0, 0), (0, 0, -1)],
+                 3: [(-1, -1, 0), (0, -1, 0), (0, 0, 0), (-1, 0, 0)]}[kkk]
+            eta = .25 * (T(o[0]) + T(o[1]) + T(o[2]) + T(o[3]))
+            out.append(dum + eta * (b1l + b2r - b1r - b2l))
+        return out
+
+    def get_v_face(self, llam, lv):
+        """get_v_face (mhd3d3.f90:2594-2615)."""
+        a = np.sqrt(llam)
+        b = .5 * np.exp(-llam * lv ** 2) / a / np.sqrt(self.pi)
+        v0p = .5 * erfc(-a * lv)
+        v0n = .5 * erfc(a * lv)
+        return v0p, v0n, lv * v0p + b, lv * v0n - b
+
+    def get_flux_stress(self, rho, vx, vy, vz, p, bx, by, bz):
+        """get_flux_stress (mhd3d3.f90:2385-2560) -> per axis [rho, rvx, rvy, rvz, eng,
+        stress x, y, z] fluxes."""
+        gam = self.gam
+        out = []
+        for kkk in (1, 2, 3):
+            lens = [self.nx0, self.ny0, self.nz0]
+            lens[kkk - 1] += 1
+            d = kkk - 1
+            (rhol, rhor), (vxl, vxr), (vyl, vyr), (vzl, vzr), (pl, pr), (bxl, bxr), (byl, byr), (bzl, bzr) = (
+                self.reconstruct(f, lens, d) for f in (rho, vx, vy, vz, p, bx, by, bz))
+            # left flux
+            leng = .5 * rhol * (vxl ** 2 + vyl ** 2 + vzl ** 2) + pl / (gam - 1.)
+            llam = rhol / (2. * pl)
+            vn = (vxl, vyl, vzl)[d]
+            v0p, v0n, v1p, v1n = self.get_v_face(llam, vn)
+            rp = rhol * v1p
+            rvp = [rhol * vxl * v1p, rhol * vyl * v1p, rhol * vzl * v1p]
+            ep = (leng + .5 * pl) * v1p
+            rvp[d] = rvp[d] + pl * v0p
+            ep = ep + .5 * pl * vn * v0p
+            lbsq = bxl ** 2 + byl ** 2 + bzl ** 2
+            llam = rhol / (2. * pl + lbsq)
+            v0p, v0n, v1p, v1n = self.get_v_face(llam, vn)
+            bl = (bxl, byl, bzl)
+            sp = [(-(bl[c] * bl[d])) * v0p for c in range(3)]
+            sp[d] = (.5 * lbsq - bl[d] * bl[d]) * v0p
+            # right flux
+            leng = .5 * rhor * (vxr ** 2 + vyr ** 2 + vzr ** 2) + pr / (gam - 1.)
+            llam = rhor / (2. * pr)
+            vn = (vxr, vyr, vzr)[d]
+            v0p, v0n, v1p, v1n = self.get_v_face(llam, vn)
+            rn = rhor * v1n
+            rvn = [rhor * vxr * v1n, rhor * vyr * v1n, rhor * vzr * v1n]
+            en = (leng + .5 * pr) * v1n
+            rvn[d] = rvn[d] + pr * v0n
+            en = en + .5 * pr * vn * v0n
+            lbsq = bxr ** 2 + byr ** 2 + bzr ** 2
+            llam = rhor / (2. * pr + lbsq)
+            v0p, v0n, v1p, v1n = self.get_v_face(llam, vn)
+            br = (bxr, byr, bzr)
+            sn = [(-(br[c] * br[d])) * v0n for c in range(3)]
+            sn[d] = (.5 * lbsq - br[d] * br[d]) * v0n
+            out.append([rp + rn, rvp[0] + rvn[0], rvp[1] + rvn[1], rvp[2] + rvn[2], ep + en,
+                        sp[0] + sn[0], sp[1] + sn[1], sp[2] + sn[2]])
+        return out
+
+    def get_bxyz(self):
+        """get_bxyz (mhd3d3.f90:2118-2128)."""
+        self.bx = .5 * (self.bi[1:] + self.bi[:-1])
+        self.by = .5 * (self.bj[:, 1:] + self.bj[:, :-1])
+        self.bz = .5 * (self.bk[:, :, 1:] + self.bk[:, :, :-1])
+
+    # -------------------------------------------------------------- fills
+    def _fill(self, a, axis, face):
+        """Periodic fillx_center / fillx_face of one rank (mhd3d3.f90:346-390, 482-525)."""
+        a = np.moveaxis(a, axis, 0)  # a view: writes land in the array
+        n, ng, nord = a.shape[0], self.ng, self.nord
+        if face:
+            a[0:ng] = a[n - nord - 1:n - ng - 1]   # aa(1:ng)=aa(lnx-nord:lnx-ng-1)
+            a[n - ng:n] = a[ng + 1:nord + 1]      # aa(lnx-ng+1:lnx)=aa(ng+2:nord+1)
+        else:
+            a[0:ng] = a[n - nord:n - ng]           # aa(1:ng)=aa(lnx-nord+1:lnx-ng)
+            a[n - ng:n] = a[ng:nord]               # aa(lnx-ng+1:lnx)=aa(ng+1:nord)
+
+    def fill_hydro(self):
+        for ax in range(3):
+            for a in (self.rho, self.p, self.vx, self.vy, self.vz):
+                self._fill(a, ax, False)
+
+    def fill_mag(self):
+        for ax in range(3):
+            for c, a in enumerate((self.bi, self.bj, self.bk)):
+                self._fill(a, ax, c == ax)
+
+    # -------------------------------------------------------------- steps
+    def _div(self, fl):
+        """The flux divergence of advance_corrector1/2 over the interior cells."""
+        fx, fy, fz = fl
+        return ((fx[1:] - fx[:-1]) / self.dx + (fy[:, 1:] - fy[:, :-1]) / self.dy
+                + (fz[:, :, 1:] - fz[:, :, :-1]) / self.dz)
+
+    def step(self):
+        """step_rk2 (mhd3d3.f90:3646-3711) with the deck's fixed tau."""
+        gam, ng = self.gam, self.ng
+        I = (slice(ng, ng + self.nx0), slice(ng, ng + self.ny0), slice(ng, ng + self.nz0))
+        self.tau = self.tau0
+        tau = self.tau
+        # advance_previous (3794-3819), stepop = 2
+        rhop, bip, bjp, bkp = self.rho.copy(), self.bi.copy(), self.bj.copy(), self.bk.copy()
+        rho, vx, vy, vz, p = self.rho, self.vx, self.vy, self.vz, self.p
+        rhovxp, rhovyp, rhovzp = rho * vx, rho * vy, rho * vz
+        engp = .5 * rho * (vx ** 2 + vy ** 2 + vz ** 2) + p / (gam - 1.)
+        for rk_step in (1, 2):
+            rho, vx, vy, vz, p = self.rho, self.vx, self.vy, self.vz, self.p
+            # get_conserve (1641-1650)
+            rho0 = rho.copy()
+            rhovx0, rhovy0, rhovz0 = rho * vx, rho * vy, rho * vz
+            eng0 = .5 * rho * (vx ** 2 + vy ** 2 + vz ** 2) + p / (gam - 1.)
+            ei, ej, ek = self.get_eijk_LFM(rho, vx, vy, vz, self.bx, self.by, self.bz, self.bi, self.bj, self.bk)
+            fl = self.get_flux_stress(rho, vx, vy, vz, p, self.bx, self.by, self.bz)
+            # advance_corrector1 (3836-3866)
+            rho, eng = rho0.copy(), eng0.copy()
+            rhovx, rhovy, rhovz = rhovx0.copy(), rhovy0.copy(), rhovz0.copy()
+            rho[I] = rho0[I] - tau * self._div([fl[a][0] for a in range(3)])
+            eng[I] = eng0[I] - tau * self._div([fl[a][4] for a in range(3)])
+            rhovx[I] = rhovx0[I] - tau * self._div([fl[a][1] for a in range(3)])
+            rhovy[I] = rhovy0[I] - tau * self._div([fl[a][2] for a in range(3)])
+            rhovz[I] = rhovz0[I] - tau * self._div([fl[a][3] for a in range(3)])
+            if rk_step == 1:
+                rhovxh, rhovyh, rhovzh = rhovx, rhovy, rhovz
+            else:
+                rho = (rhop + rho) / 2.
+                rhovxh = (rhovxp + rhovx) / 2.
+                rhovyh = (rhovyp + rhovy) / 2.
+                rhovzh = (rhovzp + rhovz) / 2.
+                eng = (engp + eng) / 2.
+            p = (gam - 1.) * (eng - .5 * (rhovxh ** 2 + rhovyh ** 2 + rhovzh ** 2) / rho)
+            # advance_corrector2 (3868-3891)
+            rhovx = rhovx.copy(); rhovy = rhovy.copy(); rhovz = rhovz.copy()
+            rhovx[I] = rhovx[I] - tau * self._div([fl[a][5] for a in range(3)])
+            rhovy[I] = rhovy[I] - tau * self._div([fl[a][6] for a in range(3)])
+            rhovz[I] = rhovz[I] - tau * self._div([fl[a][7] for a in range(3)])
+            if rk_step == 2:
+                rhovx = (rhovxp + rhovx) / 2.
+                rhovy = (rhovyp + rhovy) / 2.
+                rhovz = (rhovzp + rhovz) / 2.
+            self.rho, self.p = rho, p
+            self.vx, self.vy, self.vz = rhovx / rho, rhovy / rho, rhovz / rho
+            # advance_bijk (3893-3912)
+            nx0, ny0, nz0 = self.nx0, self.ny0, self.nz0
+            bi, bj, bk = self.bi.copy(), self.bj.copy(), self.bk.copy()
+            bi[ng:ng + nx0 + 1, I[1], I[2]] -= tau * ((ek[:, 1:] - ek[:, :-1]) / self.dy
+                                                      - (ej[:, :, 1:] - ej[:, :, :-1]) / self.dz)
+            bj[I[0], ng:ng + ny0 + 1, I[2]] -= tau * ((ei[:, :, 1:] - ei[:, :, :-1]) / self.dz
+                                                      - (ek[1:] - ek[:-1]) / self.dx)
+            bk[I[0], I[1], ng:ng + nz0 + 1] -= tau * ((ej[1:] - ej[:-1]) / self.dx
+                                                      - (ei[:, 1:] - ei[:, :-1]) / self.dy)
+            if rk_step == 2:
+                bi, bj, bk = (bip + bi) / 2., (bjp + bj) / 2., (bkp + bk) / 2.
+            self.bi, self.bj, self.bk = bi, bj, bk
+            self.fill_hydro()
+            self.fill_mag()
+            self.get_bxyz()
+
+    def fluxes(self):
+        return self.get_flux_stress(self.rho, self.vx, self.vy, self.vz, self.p, self.bx, self.by, self.bz)
+
+    def emf(self):
+        return self.get_eijk_LFM(self.rho, self.vx, self.vy, self.vz, self.bx, self.by, self.bz,
+                                 self.bi, self.bj, self.bk)
+
+    def state(self) -> dict:
+        return {"rho": self.rho, "vx": self.vx, "vy": self.vy, "vz": self.vz, "p": self.p, "bx": self.bx,
+                "by": self.by, "bz": self.bz, "bi": self.bi, "bj": self.bj, "bk": self.bk}
