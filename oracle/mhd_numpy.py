@@ -11,8 +11,10 @@ transcription slip in either shows up as a disagreement between them.
 Scope -- the path the throughput benchmark runs: Cartesian mesh, periodic
 halos on every axis (one rank of mhd3d2.f90's periodic topology:
 the SENDRECVs of fillx_center / fillx_face, mhd3d3.f90:346-390 / 482-525,
-exchange with the rank itself), reconop 1 (PDM) or 2 (TVD, van Leer), LFM
-edge EMF, stepop 2 (RK2) with the deck's fixed tau (step_rk2, 3646-3711).
+exchange with the rank itself), reconop 1 (PDM), 2 (TVD, van Leer), 3 (WENO5)
+or 4 (MP-WENO5, the reference deck's choice), LFM edge EMF, stepop 2 (RK2) or
+3 (RK3, the deck's) with the deck's fixed tau (step_rk2 / step_rk3,
+3646-3792).
 
 Arrays are indexed [i, j, k] from 0: numpy index n is Fortran index n + 1.
 ``erfc`` is scipy's and ``exp`` numpy's, so agreement with the C++ oracle
@@ -43,12 +45,13 @@ def _tap8(a0, a1, a2, a3, a4, a5, a6, a7):
 
 
 class NumpyMHD:
-    """One grid of the reference's state, advanced by RK2 steps."""
+    """One grid of the reference's state, advanced by RK2 or RK3 steps."""
 
     def __init__(self, params, state):
         p = params
-        if p.stepop != 2 or p.reconop not in (1, 2) or any(b != 0 for b in p.bc) or p.emf != 0:
-            raise ValueError("NumpyMHD covers periodic PDM/TVD + LFM + RK2 only")
+        if p.stepop not in (2, 3) or p.reconop not in (1, 2, 3, 4) or any(b != 0 for b in p.bc) or p.emf != 0:
+            raise ValueError("NumpyMHD covers periodic PDM/TVD/WENO5/MP-WENO5 + LFM + RK2/RK3 only")
+        self.stepop, self.alpha, self.beta = p.stepop, p.alpha, p.beta
         self.nx0, self.ny0, self.nz0 = p.nx0, p.ny0, p.nz0
         self.ng, self.nord = p.nord // 2, p.nord
         self.nx, self.ny, self.nz = p.nx0 + p.nord, p.ny0 + p.nord, p.nz0 + p.nord
@@ -82,13 +85,13 @@ class NumpyMHD:
                 sl.append(slice(None))
         return f[tuple(sl)]
 
-    def _stencil(self, f, d, lens, shift=(0, 0, 0), ms=range(-4, 4)):
+    def _stencil(self, f, d, lens, shift=(0, 0, 0), ms=range(-4, 4), axes=(0, 1, 2)):
         """[f at offset m along axis d] for m in ms, the element grid lens."""
         out = []
         for m in ms:
             off = list(shift)
             off[d] += m
-            out.append(self._take(f, off, lens))
+            out.append(self._take(f, off, lens, axes))
         return out
 
     # ------------------------------------------------------ reconstruction
@@ -129,9 +132,66 @@ class NumpyMHD:
         fright = fii + s0 * _max(0., np.abs(dfr) - qp * dfp)
         return fleft, fright
 
-    def reconstruct(self, f, lens, d):
-        """reconstruct_3d (mhd3d3.f90:833-860) for dir = d+1 in 1..3."""
+    def reconstruct(self, f, lens, d, axes=(0, 1, 2)):
+        """reconstruct_3d (mhd3d3.f90:833-860) for dir = d+1 in 1..3; with
+        axes=(d,) the dir 4..6 form (the other axes whole)."""
+        if self.reconop >= 3:
+            return self.weno(f, lens, d, axes)
         return self.limit(f, self.interp(f, lens, d), lens, d)
+
+    def weno(self, f, lens, d, axes=(0, 1, 2)):
+        """WENO5 (mhd3d3.f90:1252-1378) and MPWENO5 (1405-1596)."""
+        eps = self.eps
+        fm3, fm2, fm1, f0, fp1, fp2 = self._stencil(f, d, lens, ms=range(-3, 3), axes=axes)
+
+        def side(a3, a2, a1, b0, b1, b2):
+            h0 = (2. * a3 - 7. * a2 + 11. * a1) / 6.
+            h1 = (-a2 + 5. * a1 + 2. * b0) / 6.
+            h2 = (2. * a1 + 5. * b0 - b1) / 6.
+            s0 = 13. / 12. * (a3 - 2. * a2 + a1) ** 2 + .25 * (a3 - 4. * a2 + 3. * a1) ** 2
+            s1 = 13. / 12. * (a2 - 2. * a1 + b0) ** 2 + .25 * (a2 - b0) ** 2
+            s2 = 13. / 12. * (a1 - 2. * b0 + b1) ** 2 + .25 * (3. * a1 - 4. * b0 + b1) ** 2
+            s0 = .1 / (eps + s0) ** 2
+            s1 = .6 / (eps + s1) ** 2
+            s2 = .3 / (eps + s2) ** 2
+            t = s0 + s1 + s2
+            return s0 / t * h0 + s1 / t * h1 + s2 / t * h2
+
+        # left: (fm3, fm2, fm1, f0, fp1); right: the mirrored stencil
+        fl = side(fm3, fm2, fm1, f0, fp1, fp2)
+        fr = side(fp2, fp1, f0, fm1, fm2, fm3)
+        if self.reconop == 3:
+            return fl, fr
+        return self._mp(fl, fm3, fm2, fm1, f0, fp1), self._mp(fr, fp2, fp1, f0, fm1, fm2)
+
+    def _mp(self, w, a3, a2, a1, b0, b1):
+        """The MP bound of one side (MPWENO5, mhd3d3.f90:1530-1591)."""
+        def minmod(a, b):  # mhd3d3.f90:1380-1389
+            return .5 * (_sign1(a) + _sign1(b)) * _min(np.abs(a), np.abs(b))
+        alpha, beta = self.alpha, self.beta
+        h0 = a3 - 2. * a2 + a1
+        h1 = a2 - 2. * a1 + b0
+        h2 = a1 - 2. * b0 + b1
+        s2 = 4. * h1 - h2
+        s0 = 4. * h2 - h1
+        s1 = minmod(s2, s0)
+        s2 = minmod(h1, h2)
+        s0 = minmod(s1, s2)
+        w2 = 4. * h0 - h1
+        w0 = 4. * h1 - h0
+        w1 = minmod(w2, w0)
+        w2 = minmod(h0, h1)
+        w0 = minmod(w1, w2)
+        s1 = a1 + alpha * (a1 - a2)
+        s2 = .5 * (a1 + b0 - s0)
+        s0 = .5 * (3. * a1 - a2) + beta * w0 / 3.
+        w1 = _min(_min(a1, b0), s2)
+        w2 = _min(_min(a1, s1), s0)
+        w0 = _max(w1, w2)
+        h1 = _max(_max(a1, b0), s2)
+        h2 = _max(_max(a1, s1), s0)
+        h0 = _min(h1, h2)
+        return w + minmod(w0 - w, h0 - w)  # median (1391-1403)
 
     def interp2(self, f, dirn, lens):
         """interp2_pdm / interp2_tvd (mhd3d3.f90:926-989, 1037-1067), edge family dirn = 1..3."""
@@ -153,17 +213,51 @@ class NumpyMHD:
         g = _tap8(*[self._take(f, (m, 0, 0), (ii, 0, kk), axes=(0, 2)) for m in range(-4, 4)])
         return _tap8(*[g[:, ng + m:ng + m + jj, :] for m in range(-4, 4)])
 
+    def _corner_weno(self, lv, dirn, lens):
+        """The two-level WENO5 / MP-WENO5 corner states of get_vav_center2corner
+        (mhd3d3.f90:1936-2049): reconstruct along the first transverse axis p
+        (the other axes whole) into rows of a scratch array, reconstruct those
+        along q; then the same with p and q exchanged."""
+        p, q = {1: (1, 2), 2: (2, 0), 3: (0, 1)}[dirn]
+        ng = self.ng
+        vi = np.zeros((self.nx, self.ny, self.nz))  # only the rows written below are read
+
+        def rows(axis, a):
+            sl = [slice(None)] * 3
+            sl[axis] = slice(ng, ng + a.shape[axis])
+            vi[tuple(sl)] = a
+
+        def first(axis):
+            ln = [self.nx, self.ny, self.nz]
+            ln[axis] = lens[axis]
+            return self.reconstruct(lv, ln, axis, axes=(axis,))
+
+        lvl, lvr = first(p)
+        rows(p, lvl)
+        v00_1, v01_1 = self.reconstruct(vi, lens, q)
+        rows(p, lvr)
+        v10_1, v11_1 = self.reconstruct(vi, lens, q)
+        lvl, lvr = first(q)
+        rows(q, lvl)
+        v00_0, v01_0 = self.reconstruct(vi, lens, p)
+        rows(q, lvr)
+        v10_0, v11_0 = self.reconstruct(vi, lens, p)
+        return v00_0, v00_1, v10_0, v10_1, v01_0, v01_1, v11_0, v11_1
+
     def vav_center2corner(self, lv, dirn, lens):
-        """get_vav_center2corner (mhd3d3.f90:1858-2116) for PDM / TVD."""
-        vi = self.interp2(lv, dirn, lens)
-        # (shift, axis) of the four limited pairs, axis 0-based
-        calls = {1: [((0, 0, -1), 1), ((0, -1, 0), 2), ((0, 0, 0), 2), ((0, 0, 0), 1)],
-                 2: [((-1, 0, 0), 2), ((0, 0, -1), 0), ((0, 0, 0), 0), ((0, 0, 0), 2)],
-                 3: [((0, -1, 0), 0), ((-1, 0, 0), 1), ((0, 0, 0), 1), ((0, 0, 0), 0)]}[dirn]
-        v00_0, v10_0 = self.limit(lv, vi, lens, calls[0][1], calls[0][0])
-        v00_1, v01_1 = self.limit(lv, vi, lens, calls[1][1], calls[1][0])
-        v10_1, v11_1 = self.limit(lv, vi, lens, calls[2][1], calls[2][0])
-        v01_0, v11_0 = self.limit(lv, vi, lens, calls[3][1], calls[3][0])
+        """get_vav_center2corner (mhd3d3.f90:1858-2116)."""
+        if self.reconop >= 3:
+            v00_0, v00_1, v10_0, v10_1, v01_0, v01_1, v11_0, v11_1 = self._corner_weno(lv, dirn, lens)
+        else:
+            vi = self.interp2(lv, dirn, lens)
+            # (shift, axis) of the four limited pairs, axis 0-based
+            calls = {1: [((0, 0, -1), 1), ((0, -1, 0), 2), ((0, 0, 0), 2), ((0, 0, 0), 1)],
+                     2: [((-1, 0, 0), 2), ((0, 0, -1), 0), ((0, 0, 0), 0), ((0, 0, 0), 2)],
+                     3: [((0, -1, 0), 0), ((-1, 0, 0), 1), ((0, 0, 0), 1), ((0, 0, 0), 0)]}[dirn]
+            v00_0, v10_0 = self.limit(lv, vi, lens, calls[0][1], calls[0][0])
+            v00_1, v01_1 = self.limit(lv, vi, lens, calls[1][1], calls[1][0])
+            v10_1, v11_1 = self.limit(lv, vi, lens, calls[2][1], calls[2][0])
+            v01_0, v11_0 = self.limit(lv, vi, lens, calls[3][1], calls[3][0])
         T = lambda off: self._take(lv, off, lens)
         if dirn == 1:
             dif00 = np.abs(T((0, -2, -1)) - T((0, -1, -1))) - np.abs(T((0, -1, -2)) - T((0, -1, -1)))
@@ -304,8 +398,16 @@ class NumpyMHD:
         return ((fx[1:] - fx[:-1]) / self.dx + (fy[:, 1:] - fy[:, :-1]) / self.dy
                 + (fz[:, :, 1:] - fz[:, :, :-1]) / self.dz)
 
+    def _comb(self, xp, x, stage):
+        """The stage combinations of step_rk2 / step_rk3 (3646-3792)."""
+        if self.stepop == 2:
+            return (xp + x) / 2.
+        if stage == 2:
+            return (3. * xp + x) / 4.
+        return (xp + 2. * x) / 3.
+
     def step(self):
-        """step_rk2 (mhd3d3.f90:3646-3711) with the deck's fixed tau."""
+        """step_rk2 / step_rk3 (mhd3d3.f90:3646-3792) with the deck's fixed tau."""
         gam, ng = self.gam, self.ng
         I = (slice(ng, ng + self.nx0), slice(ng, ng + self.ny0), slice(ng, ng + self.nz0))
         self.tau = self.tau0
@@ -315,7 +417,7 @@ class NumpyMHD:
         rho, vx, vy, vz, p = self.rho, self.vx, self.vy, self.vz, self.p
         rhovxp, rhovyp, rhovzp = rho * vx, rho * vy, rho * vz
         engp = .5 * rho * (vx ** 2 + vy ** 2 + vz ** 2) + p / (gam - 1.)
-        for rk_step in (1, 2):
+        for rk_step in range(1, self.stepop + 1):
             rho, vx, vy, vz, p = self.rho, self.vx, self.vy, self.vz, self.p
             # get_conserve (1641-1650)
             rho0 = rho.copy()
@@ -334,21 +436,21 @@ class NumpyMHD:
             if rk_step == 1:
                 rhovxh, rhovyh, rhovzh = rhovx, rhovy, rhovz
             else:
-                rho = (rhop + rho) / 2.
-                rhovxh = (rhovxp + rhovx) / 2.
-                rhovyh = (rhovyp + rhovy) / 2.
-                rhovzh = (rhovzp + rhovz) / 2.
-                eng = (engp + eng) / 2.
+                rho = self._comb(rhop, rho, rk_step)
+                rhovxh = self._comb(rhovxp, rhovx, rk_step)
+                rhovyh = self._comb(rhovyp, rhovy, rk_step)
+                rhovzh = self._comb(rhovzp, rhovz, rk_step)
+                eng = self._comb(engp, eng, rk_step)
             p = (gam - 1.) * (eng - .5 * (rhovxh ** 2 + rhovyh ** 2 + rhovzh ** 2) / rho)
             # advance_corrector2 (3868-3891)
             rhovx = rhovx.copy(); rhovy = rhovy.copy(); rhovz = rhovz.copy()
             rhovx[I] = rhovx[I] - tau * self._div([fl[a][5] for a in range(3)])
             rhovy[I] = rhovy[I] - tau * self._div([fl[a][6] for a in range(3)])
             rhovz[I] = rhovz[I] - tau * self._div([fl[a][7] for a in range(3)])
-            if rk_step == 2:
-                rhovx = (rhovxp + rhovx) / 2.
-                rhovy = (rhovyp + rhovy) / 2.
-                rhovz = (rhovzp + rhovz) / 2.
+            if rk_step >= 2:
+                rhovx = self._comb(rhovxp, rhovx, rk_step)
+                rhovy = self._comb(rhovyp, rhovy, rk_step)
+                rhovz = self._comb(rhovzp, rhovz, rk_step)
             self.rho, self.p = rho, p
             self.vx, self.vy, self.vz = rhovx / rho, rhovy / rho, rhovz / rho
             # advance_bijk (3893-3912)
@@ -360,8 +462,8 @@ class NumpyMHD:
                                                       - (ek[1:] - ek[:-1]) / self.dx)
             bk[I[0], I[1], ng:ng + nz0 + 1] -= tau * ((ej[1:] - ej[:-1]) / self.dx
                                                       - (ei[:, 1:] - ei[:, :-1]) / self.dy)
-            if rk_step == 2:
-                bi, bj, bk = (bip + bi) / 2., (bjp + bj) / 2., (bkp + bk) / 2.
+            if rk_step >= 2:
+                bi, bj, bk = self._comb(bip, bi, rk_step), self._comb(bjp, bj, rk_step), self._comb(bkp, bk, rk_step)
             self.bi, self.bj, self.bk = bi, bj, bk
             self.fill_hydro()
             self.fill_mag()

@@ -70,24 +70,33 @@ def compare_steps(prm, s, nsteps):
     o.close()
 
 
-@pytest.mark.parametrize("recon", [1, 2])
+@pytest.mark.parametrize("recon", [1, 2, 3, 4])
 def test_fluxes_and_emf_agree_on_a_random_ragged_state(recon):
     s = random_state(12, 10, 8, seed=5)
     compare_instant(Params(12, 10, 8, reconop=recon), s)
 
 
-@pytest.mark.parametrize("recon", [1, 2])
+@pytest.mark.parametrize("recon", [1, 2, 3, 4])
 def test_fluxes_and_emf_agree_on_orszag_tang(recon):
     s = ics.orszag_tang_3d(12, seed=2)
     compare_instant(Params(12, 12, 12, reconop=recon), s)
 
 
-@pytest.mark.parametrize("recon", [1, 2])
-def test_rk2_steps_agree_on_orszag_tang(recon):
+@pytest.mark.parametrize("recon", [1, 2, 3, 4])
+@pytest.mark.parametrize("stepop", [2, 3])
+def test_rk_steps_agree_on_orszag_tang(recon, stepop):
     s = ics.orszag_tang_3d(12, seed=2)
-    compare_steps(Params(12, 12, 12, reconop=recon, tau=0.4 * ics.cfl_dt(s)), s, 3)
+    compare_steps(Params(12, 12, 12, reconop=recon, stepop=stepop, tau=0.4 * ics.cfl_dt(s)), s, 3)
 
 
-def test_rk2_steps_agree_on_a_random_ragged_state():
+def test_the_reference_deck_agrees():
+    """The scheme of mhd3d3.in (MP-WENO5, RK3, tau = 2e-4) at its 16^3 size, on
+    one rank instead of the deck's 2x2x2 and with periodic halos."""
+    s = ics.orszag_tang_3d(16, seed=4)
+    compare_steps(Params(16, 16, 16, reconop=4, stepop=3, tau=2e-4), s, 4)
+
+
+@pytest.mark.parametrize("recon", [1, 4])
+def test_rk_steps_agree_on_a_random_ragged_state(recon):
     s = random_state(12, 10, 8, seed=6)
-    compare_steps(Params(12, 10, 8, reconop=1, tau=0.05 * ics.cfl_dt(s)), s, 2)
+    compare_steps(Params(12, 10, 8, reconop=recon, stepop=3, tau=0.05 * ics.cfl_dt(s)), s, 2)
