@@ -8,13 +8,17 @@ from the Fortran: one whole-array expression per Fortran statement or
 ``oracle/mhd_oracle.cpp`` (a loop-per-element C++ restatement), so a
 transcription slip in either shows up as a disagreement between them.
 
-Scope -- the path the throughput benchmark runs: Cartesian mesh, periodic
-halos on every axis (one rank of mhd3d2.f90's periodic topology:
-the SENDRECVs of fillx_center / fillx_face, mhd3d3.f90:346-390 / 482-525,
-exchange with the rank itself), reconop 1 (PDM), 2 (TVD, van Leer), 3 (WENO5)
-or 4 (MP-WENO5, the reference deck's choice), LFM edge EMF, stepop 2 (RK2) or
-3 (RK3, the deck's) with the deck's fixed tau (step_rk2 / step_rk3,
-3646-3792).
+Scope: Cartesian mesh; per axis periodic halos (one rank of mhd3d2.f90's
+periodic topology: the SENDRECVs of fillx_center / fillx_face,
+mhd3d3.f90:346-390 / 482-525, exchange with the rank itself) or the even wall
+mirror those routines apply at a domain edge (xbc=0, the only value
+fill_hydro_mpi / fill_mag_mpi pass, 781-819); reconop 1 (PDM), 2 (TVD, van
+Leer), 3 (WENO5) or 4 (MP-WENO5, the reference deck's choice); LFM edge EMF;
+stepop 1 (AB2, step_ab 3602-3644, CFL tau), 2 (RK2) or 3 (RK3, the deck's),
+the last two with the deck's fixed tau (step_rk2 / step_rk3, 3646-3792).
+
+The AB2 priming step takes the deck's tau where the reference hard-codes
+tau=3.e-4 after get_dt (3356-3359), as the C++ oracle and the library do.
 
 Arrays are indexed [i, j, k] from 0: numpy index n is Fortran index n + 1.
 ``erfc`` is scipy's and ``exp`` numpy's, so agreement with the C++ oracle
@@ -49,9 +53,10 @@ class NumpyMHD:
 
     def __init__(self, params, state):
         p = params
-        if p.stepop not in (2, 3) or p.reconop not in (1, 2, 3, 4) or any(b != 0 for b in p.bc) or p.emf != 0:
-            raise ValueError("NumpyMHD covers periodic PDM/TVD/WENO5/MP-WENO5 + LFM + RK2/RK3 only")
-        self.stepop, self.alpha, self.beta = p.stepop, p.alpha, p.beta
+        if p.reconop not in (1, 2, 3, 4) or any(b not in (0, 1) for b in p.bc) or p.emf != 0:
+            raise ValueError("NumpyMHD covers periodic / even-wall PDM, TVD, WENO5, MP-WENO5 + LFM only")
+        self.stepop, self.alpha, self.beta, self.cfl = p.stepop, p.alpha, p.beta, p.cfl
+        self.bc = tuple(p.bc)
         self.nx0, self.ny0, self.nz0 = p.nx0, p.ny0, p.nz0
         self.ng, self.nord = p.nord // 2, p.nord
         self.nx, self.ny, self.nz = p.nx0 + p.nord, p.ny0 + p.nord, p.nz0 + p.nord
@@ -60,6 +65,10 @@ class NumpyMHD:
         self.pi = 4. * np.arctan(1.0)  # pars: pi=4.*atan(1.0_8)
         g = state.grid
         ng = self.ng
+        # dxblock over every cell, ghosts included (get_dt)
+        self.dxa = np.asarray(g.dx)[:, None, None]
+        self.dya = np.asarray(g.dy)[None, :, None]
+        self.dza = np.asarray(g.dz)[None, None, :]
         # dxblock(ng+i, ng+j, ng+k) of the interior cells
         self.dx = np.asarray(g.dx)[ng:ng + self.nx0][:, None, None]
         self.dy = np.asarray(g.dy)[ng:ng + self.ny0][None, :, None]
@@ -71,6 +80,13 @@ class NumpyMHD:
         self.fill_hydro()
         self.fill_mag()
         self.get_bxyz()
+        if self.stepop == 1:  # AB priming (mhd3d3.f90:3356-3373)
+            dtc = self.get_dt()
+            self.tau = self.tau0 = p.tau if p.tau > 0 else dtc
+            self.rhop, self.vxp, self.vyp, self.vzp, self.pp = (a.copy() for a in (
+                self.rho, self.vx, self.vy, self.vz, self.p))
+            self.bxp, self.byp, self.bzp = self.bx.copy(), self.by.copy(), self.bz.copy()
+            self.bip, self.bjp, self.bkp = self.bi.copy(), self.bj.copy(), self.bk.copy()
 
     # ------------------------------------------------------------ indexing
     def _take(self, f, off, lens, axes=(0, 1, 2)):
@@ -371,9 +387,19 @@ class NumpyMHD:
 
     # -------------------------------------------------------------- fills
     def _fill(self, a, axis, face):
-        """Periodic fillx_center / fillx_face of one rank (mhd3d3.f90:346-390, 482-525)."""
+        """fillx_center / fillx_face of one rank (mhd3d3.f90:346-390, 482-525):
+        the periodic exchange, or the even mirror at both walls."""
         a = np.moveaxis(a, axis, 0)  # a view: writes land in the array
         n, ng, nord = a.shape[0], self.ng, self.nord
+        i = np.arange(1, ng + 1)  # Fortran i = 1..ng
+        if self.bc[axis] == 1:
+            if face:  # aa(i)=aa(nord+2-i); aa(n+2-i)=aa(n0+i), n = lnx-1, n0 = n-nord
+                a[i - 1] = a[nord + 2 - i - 1]
+                a[n + 1 - i - 1] = a[n - 1 - nord + i - 1]
+            else:  # aa(i)=aa(nord+1-i); aa(lnx+1-i)=aa(lnx-nord+i)
+                a[i - 1] = a[nord + 1 - i - 1]
+                a[n + 1 - i - 1] = a[n - nord + i - 1]
+            return
         if face:
             a[0:ng] = a[n - nord - 1:n - ng - 1]   # aa(1:ng)=aa(lnx-nord:lnx-ng-1)
             a[n - ng:n] = a[ng + 1:nord + 1]      # aa(lnx-ng+1:lnx)=aa(ng+2:nord+1)
@@ -398,6 +424,66 @@ class NumpyMHD:
         return ((fx[1:] - fx[:-1]) / self.dx + (fy[:, 1:] - fy[:, :-1]) / self.dy
                 + (fz[:, :, 1:] - fz[:, :, :-1]) / self.dz)
 
+    def get_dt(self):
+        """get_dt (mhd3d3.f90:1608-1639): the CFL dt, minimum over every cell."""
+        v = np.sqrt(self.vx ** 2 + self.vy ** 2 + self.vz ** 2)
+        btot = np.sqrt(self.bx ** 2 + self.by ** 2 + self.bz ** 2)
+        valf = btot / np.sqrt(self.rho)
+        vs = np.sqrt(self.gam * self.p / self.rho)
+        vcfl = v + np.sqrt(valf ** 2 + vs ** 2)
+        return (self.cfl / (vcfl / self.dxa + vcfl / self.dya + vcfl / self.dza)).min()
+
+    def step_ab(self):
+        """step_ab (mhd3d3.f90:3602-3644) with advance_predictor_ab (3821-3834)."""
+        gam, ng = self.gam, self.ng
+        I = (slice(ng, ng + self.nx0), slice(ng, ng + self.ny0), slice(ng, ng + self.nz0))
+        self.tau = tau = self.get_dt()
+        rho, vx, vy, vz, p = self.rho, self.vx, self.vy, self.vz, self.p
+        rho0 = rho.copy()
+        rhovx0, rhovy0, rhovz0 = rho * vx, rho * vy, rho * vz
+        eng0 = .5 * rho * (vx ** 2 + vy ** 2 + vz ** 2) + p / (gam - 1.)
+        c = tau / self.tau0 / 2.
+        h = {k: getattr(self, k) + c * (getattr(self, k) - getattr(self, k + "p"))
+             for k in ("rho", "vx", "vy", "vz", "p", "bx", "by", "bz", "bi", "bj", "bk")}
+        for k in ("rho", "vx", "vy", "vz", "p", "bx", "by", "bz", "bi", "bj", "bk"):  # advance_previous
+            setattr(self, k + "p", getattr(self, k).copy())
+        self.tau0 = tau
+        ei, ej, ek = self.get_eijk_LFM(h["rho"], h["vx"], h["vy"], h["vz"], h["bx"], h["by"], h["bz"],
+                                       h["bi"], h["bj"], h["bk"])
+        fl = self.get_flux_stress(h["rho"], h["vx"], h["vy"], h["vz"], h["p"], h["bx"], h["by"], h["bz"])
+        # advance_corrector1, stepop = 1
+        rho, eng = rho0.copy(), eng0.copy()
+        rhovx, rhovy, rhovz = rhovx0.copy(), rhovy0.copy(), rhovz0.copy()
+        rho[I] = rho0[I] - tau * self._div([fl[a][0] for a in range(3)])
+        eng[I] = eng0[I] - tau * self._div([fl[a][4] for a in range(3)])
+        rhovx[I] = rhovx0[I] - tau * self._div([fl[a][1] for a in range(3)])
+        rhovy[I] = rhovy0[I] - tau * self._div([fl[a][2] for a in range(3)])
+        rhovz[I] = rhovz0[I] - tau * self._div([fl[a][3] for a in range(3)])
+        self.p = (gam - 1.) * (eng - .5 * (rhovx ** 2 + rhovy ** 2 + rhovz ** 2) / rho)
+        # advance_corrector2, stepop = 1
+        rhovx[I] = rhovx[I] - tau * self._div([fl[a][5] for a in range(3)])
+        rhovy[I] = rhovy[I] - tau * self._div([fl[a][6] for a in range(3)])
+        rhovz[I] = rhovz[I] - tau * self._div([fl[a][7] for a in range(3)])
+        self.rho = rho
+        self.vx, self.vy, self.vz = rhovx / rho, rhovy / rho, rhovz / rho
+        self._advance_bijk(ei, ej, ek, tau)
+        self.fill_hydro()
+        self.fill_mag()
+        self.get_bxyz()
+
+    def _advance_bijk(self, ei, ej, ek, tau):
+        """advance_bijk (mhd3d3.f90:3893-3912) into new arrays."""
+        ng, nx0, ny0, nz0 = self.ng, self.nx0, self.ny0, self.nz0
+        I = (slice(ng, ng + nx0), slice(ng, ng + ny0), slice(ng, ng + nz0))
+        bi, bj, bk = self.bi.copy(), self.bj.copy(), self.bk.copy()
+        bi[ng:ng + nx0 + 1, I[1], I[2]] -= tau * ((ek[:, 1:] - ek[:, :-1]) / self.dy
+                                                  - (ej[:, :, 1:] - ej[:, :, :-1]) / self.dz)
+        bj[I[0], ng:ng + ny0 + 1, I[2]] -= tau * ((ei[:, :, 1:] - ei[:, :, :-1]) / self.dz
+                                                  - (ek[1:] - ek[:-1]) / self.dx)
+        bk[I[0], I[1], ng:ng + nz0 + 1] -= tau * ((ej[1:] - ej[:-1]) / self.dx
+                                                  - (ei[:, 1:] - ei[:, :-1]) / self.dy)
+        self.bi, self.bj, self.bk = bi, bj, bk
+
     def _comb(self, xp, x, stage):
         """The stage combinations of step_rk2 / step_rk3 (3646-3792)."""
         if self.stepop == 2:
@@ -407,7 +493,9 @@ class NumpyMHD:
         return (xp + 2. * x) / 3.
 
     def step(self):
-        """step_rk2 / step_rk3 (mhd3d3.f90:3646-3792) with the deck's fixed tau."""
+        """step_ab, or step_rk2 / step_rk3 (mhd3d3.f90:3646-3792) with the deck's fixed tau."""
+        if self.stepop == 1:
+            return self.step_ab()
         gam, ng = self.gam, self.ng
         I = (slice(ng, ng + self.nx0), slice(ng, ng + self.ny0), slice(ng, ng + self.nz0))
         self.tau = self.tau0
@@ -453,15 +541,8 @@ class NumpyMHD:
                 rhovz = self._comb(rhovzp, rhovz, rk_step)
             self.rho, self.p = rho, p
             self.vx, self.vy, self.vz = rhovx / rho, rhovy / rho, rhovz / rho
-            # advance_bijk (3893-3912)
-            nx0, ny0, nz0 = self.nx0, self.ny0, self.nz0
-            bi, bj, bk = self.bi.copy(), self.bj.copy(), self.bk.copy()
-            bi[ng:ng + nx0 + 1, I[1], I[2]] -= tau * ((ek[:, 1:] - ek[:, :-1]) / self.dy
-                                                      - (ej[:, :, 1:] - ej[:, :, :-1]) / self.dz)
-            bj[I[0], ng:ng + ny0 + 1, I[2]] -= tau * ((ei[:, :, 1:] - ei[:, :, :-1]) / self.dz
-                                                      - (ek[1:] - ek[:-1]) / self.dx)
-            bk[I[0], I[1], ng:ng + nz0 + 1] -= tau * ((ej[1:] - ej[:-1]) / self.dx
-                                                      - (ei[:, 1:] - ei[:, :-1]) / self.dy)
+            self._advance_bijk(ei, ej, ek, tau)
+            bi, bj, bk = self.bi, self.bj, self.bk
             if rk_step >= 2:
                 bi, bj, bk = self._comb(bip, bi, rk_step), self._comb(bjp, bj, rk_step), self._comb(bkp, bk, rk_step)
             self.bi, self.bj, self.bk = bi, bj, bk

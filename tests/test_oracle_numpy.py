@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from mhd3d_mpi_fortran_gb300 import ics
-from mhd3d_mpi_fortran_gb300.abi import Params
+from mhd3d_mpi_fortran_gb300.abi import BC_EVEN, BC_PERIODIC, Params
 from oracle.mhd_numpy import NumpyMHD
 from oracle.oracle import OracleSolver
 
@@ -100,3 +100,28 @@ def test_the_reference_deck_agrees():
 def test_rk_steps_agree_on_a_random_ragged_state(recon):
     s = random_state(12, 10, 8, seed=6)
     compare_steps(Params(12, 10, 8, reconop=recon, stepop=3, tau=0.05 * ics.cfl_dt(s)), s, 2)
+
+
+@pytest.mark.parametrize("recon", [1, 4])
+def test_ab2_steps_agree(recon):
+    """step_ab with the CFL dt; the priming step takes tau = 3e-4 as the reference
+    hard-codes it (mhd3d3.f90:3356-3359)."""
+    s = ics.orszag_tang_3d(12, seed=2)
+    compare_steps(Params(12, 12, 12, reconop=recon, stepop=1, tau=3e-4), s, 3)
+
+
+@pytest.mark.parametrize("recon,stepop", [(1, 2), (4, 3), (2, 1)])
+def test_even_walls_agree(recon, stepop):
+    """The wall mirror of fillx_center / fillx_face (xbc = 0, the value
+    fill_hydro_mpi and fill_mag_mpi pass) on every axis, shock tube along x."""
+    s = ics.shock_tube(12, axis=0, ntrans=6)
+    prm = Params(12, 6, 6, reconop=recon, stepop=stepop, bc=(BC_EVEN, BC_EVEN, BC_EVEN),
+                 tau=0.3 * ics.cfl_dt(s))
+    compare_steps(prm, s, 3)
+
+
+def test_even_walls_on_a_random_ragged_state():
+    s = random_state(12, 10, 8, seed=7)
+    prm = Params(12, 10, 8, reconop=1, stepop=3, bc=(BC_EVEN, BC_PERIODIC, BC_EVEN), tau=0.05 * ics.cfl_dt(s))
+    compare_instant(prm, s)
+    compare_steps(prm, s, 2)
