@@ -2342,7 +2342,8 @@ void emf_r(const Dev<T>& d, const Inp<T>& in, cudaStream_t st) {
   k_emf<T, RECON, 2, M><<<grid3(g.nx0 + 1, g.ny0 + 1, g.nz0, b), b, 0, st>>>(d, in, P);
 }
 
-// ei tile: 32 x 8 x 8 edges in FP32, 32 x 4 x 4 in FP64 (96 KB of shared memory each)
+// ei tile cross-section: 8 x 8 edges in FP32, 4 x 4 in FP64; its length along
+// the edge axis is ei_x() below.
 #ifndef MHD_EI_TILE
 #define MHD_EI_TILE 8
 #endif
