@@ -163,6 +163,12 @@ int mhd_free(void* handle);
 /* Human-readable text of the last error on this thread. */
 const char* mhd_last_error(void);
 
+/* Bound, in seconds, on every host wait for the device in this process
+ * (default 600).  A wait that runs out returns MHD_E_TIMEOUT, sets
+ * MHD_ST_TIMEOUT in *status, and leaves the enqueued work running: the handle
+ * stays usable and the next waiting call picks up where it ended. */
+int mhd_set_wait_bound(double seconds);
+
 /* Device 0's SM count, compute capability (major, minor) and maximum SM clock
  * in MHz, for roofline denominators (no reference counterpart). */
 int mhd_device_info(int32_t out[4]);

@@ -25,7 +25,8 @@ E_OK, E_ARG, E_CUDA, E_NOMEM, E_TIMEOUT, E_STATE = 0, -1, -2, -3, -4, -5
 
 EXPORTS = (
     "mhd_init", "mhd_init_mapped", "mhd_step", "mhd_step_n", "mhd_fetch", "mhd_diagnostics", "mhd_step_graph",
-    "mhd_set_tau", "mhd_set_profiling", "mhd_last_timings", "mhd_free", "mhd_last_error", "mhd_device_info",
+    "mhd_set_tau", "mhd_set_profiling", "mhd_last_timings", "mhd_free", "mhd_last_error", "mhd_set_wait_bound",
+    "mhd_device_info",
     "mhd_debug_fluxes", "mhd_debug_emf", "mhd_ensemble_step", "mhd_time_steps",
     "mhd_diagnostics_noalloc", "mhd_checkpoint_save", "mhd_checkpoint_load",
     "mhd_autotune", "mhd_ensemble_autotune", "mhd_set_tiles", "mhd_tc_gemm_test",
@@ -113,6 +114,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.mhd_init.argtypes = [C.POINTER(CParams)] + [dp] * 11 + [C.POINTER(vp)]
     lib.mhd_init_mapped.argtypes = [C.POINTER(CParams)] + [dp] * 11 + [C.POINTER(vp)]
     lib.mhd_step.argtypes = [vp, dp, C.POINTER(C.c_uint32)]
+    lib.mhd_set_wait_bound.argtypes = [C.c_double]
     lib.mhd_step_n.argtypes = [vp, C.c_int32, dp, C.POINTER(C.c_uint32)]
     lib.mhd_step_graph.argtypes = [vp, C.c_int32, dp, C.POINTER(C.c_uint32)]
     lib.mhd_fetch.argtypes = [vp] + [dp] * 11

@@ -49,7 +49,8 @@ int fail(int code, const std::string& msg) {
       return fail(MHD_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
   } while (0)
 
-constexpr double kWaitSeconds = 600.0;  // bound on any host wait for the device
+// Bound on any host wait for the device (mhd_set_wait_bound), seconds.
+std::atomic<double> g_wait_seconds{600.0};
 
 std::atomic<unsigned long long> g_next_uid{1};
 
@@ -101,7 +102,7 @@ int wait_stream(Handle* h) {
       return fail(MHD_E_CUDA, std::string("device error: ") + cudaGetErrorString(q));
     }
     double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    if (el > kWaitSeconds) {
+    if (el > g_wait_seconds.load(std::memory_order_relaxed)) {
       cudaEventDestroy(e);
       return fail(MHD_E_TIMEOUT, "device did not finish within the wait bound");
     }
@@ -506,6 +507,12 @@ std::vector<int> mhd::ghost_maps(int nx0, int ny0, int nz0, int ng, const int bc
 // Entry points: C linkage comes from their declarations in mhd_gpu.h.
 
 const char* mhd_last_error(void) { return g_err.c_str(); }
+
+int mhd_set_wait_bound(double seconds) {
+  if (!(seconds > 0.0) || !std::isfinite(seconds)) return fail(MHD_E_ARG, "wait bound must be positive and finite");
+  g_wait_seconds.store(seconds, std::memory_order_relaxed);
+  return MHD_OK;
+}
 
 int mhd_device_info(int32_t out[4]) {
   if (!out) return fail(MHD_E_ARG, "null output");

@@ -5,13 +5,15 @@ outputs agree with the oracle to a few ulps (only exp/erfc differ: CUDA vs
 glibc).  Tolerances are written per test.  FP32 mode is checked against the
 FP64 solution with an error budget, as the production path.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
 from mhd3d_mpi_fortran_gb300 import ics, MHDSolver, ensemble_step
 from mhd3d_mpi_fortran_gb300.abi import (Params, BC_PERIODIC, BC_EVEN, BC_REFLECT, BC_OUTFLOW,
                                          STEP_AB2, STEP_RK2, STEP_RK3, FP32, FP64, ST_NAN, ST_NEG_RHO,
-                                         DT_CFL)
+                                         ST_TIMEOUT, E_OK, E_ARG, E_TIMEOUT, DT_CFL)
 from oracle.oracle import OracleSolver
 
 pytestmark = pytest.mark.gpu
@@ -222,6 +224,33 @@ def test_status_bits_from_poisoned_input(prec):
     with MHDSolver(Params(8, 8, 8, precision=prec, tau=tau), s) as g:
         _, st = g.step(1)
     assert st & ST_NEG_RHO
+
+
+def test_wait_bound_timeout_leaves_the_handle_usable():
+    """A host wait that runs out (mhd_set_wait_bound) returns MHD_E_TIMEOUT with
+    MHD_ST_TIMEOUT while the enqueued steps keep running; with the bound
+    restored the next call waits for them, and the state equals an
+    uninterrupted run.  Nothing on the device faults or hangs: the steps are
+    ordinary FP64 steps (about 0.2 s of device time) that finish by themselves."""
+    s = ics.orszag_tang_3d(96, seed=1)
+    prm = Params(96, 96, 96, precision=FP64, tau=0.3 * ics.cfl_dt(s))
+    with MHDSolver(prm, s) as g, MHDSolver(prm, s) as ref:
+        lib = g.lib
+        tau, st = C.c_double(), C.c_uint32()
+        assert lib.mhd_set_wait_bound(1e-4) == E_OK
+        try:
+            rc = lib.mhd_step_n(g.h, 20, C.byref(tau), C.byref(st))
+        finally:
+            assert lib.mhd_set_wait_bound(600.0) == E_OK
+        assert rc == E_TIMEOUT, rc
+        assert st.value & ST_TIMEOUT
+        assert b"wait bound" in lib.mhd_last_error()
+        g.step(1)  # waits for the 20 steps in flight, then one more
+        ref.step(21)
+        got, want = g.fetch(), ref.fetch()
+        for k in FIELDS:
+            assert np.array_equal(got[k], want[k]), k
+    assert lib.mhd_set_wait_bound(0.0) == E_ARG
 
 
 @pytest.mark.parametrize("prec,stepop", [(FP64, STEP_RK2), (FP32, STEP_RK2), (FP64, STEP_AB2), (FP32, STEP_RK3)])
