@@ -13,7 +13,8 @@ periodic topology: the SENDRECVs of fillx_center / fillx_face,
 mhd3d3.f90:346-390 / 482-525, exchange with the rank itself) or the even wall
 mirror those routines apply at a domain edge (xbc=0, the only value
 fill_hydro_mpi / fill_mag_mpi pass, 781-819); reconop 1 (PDM), 2 (TVD, van
-Leer), 3 (WENO5) or 4 (MP-WENO5, the reference deck's choice); LFM edge EMF;
+Leer, with mhd3d2's stencil shifts when tvd_shift = 1), 3 (WENO5) or 4
+(MP-WENO5, the reference deck's choice); LFM or Yee edge EMF;
 stepop 1 (AB2, step_ab 3602-3644, CFL tau), 2 (RK2) or 3 (RK3, the deck's),
 the last two with the deck's fixed tau (step_rk2 / step_rk3, 3646-3792).
 
@@ -53,8 +54,9 @@ class NumpyMHD:
 
     def __init__(self, params, state):
         p = params
-        if p.reconop not in (1, 2, 3, 4) or any(b not in (0, 1) for b in p.bc) or p.emf != 0:
-            raise ValueError("NumpyMHD covers periodic / even-wall PDM, TVD, WENO5, MP-WENO5 + LFM only")
+        if p.reconop not in (1, 2, 3, 4) or any(b not in (0, 1) for b in p.bc) or p.emf not in (0, 1):
+            raise ValueError("NumpyMHD covers periodic / even-wall PDM, TVD, WENO5, MP-WENO5 + LFM / Yee only")
+        self.emf_kind, self.tvd_shift = p.emf, p.tvd_shift
         self.stepop, self.alpha, self.beta, self.cfl = p.stepop, p.alpha, p.beta, p.cfl
         self.bc = tuple(p.bc)
         self.nx0, self.ny0, self.nz0 = p.nx0, p.ny0, p.nz0
@@ -111,18 +113,19 @@ class NumpyMHD:
         return out
 
     # ------------------------------------------------------ reconstruction
-    def interp(self, f, lens, d):
+    def interp(self, f, lens, d, axes=(0, 1, 2)):
         """interp_pdm / interp_tvd (mhd3d3.f90:862-924, 991-1035), axis d = 0,1,2."""
         if self.reconop == 1:
-            return _tap8(*self._stencil(f, d, lens))
-        fm1, f0 = self._stencil(f, d, lens, ms=(-1, 0))
+            return _tap8(*self._stencil(f, d, lens, axes=axes))
+        fm1, f0 = self._stencil(f, d, lens, ms=(-1, 0), axes=axes)
         return (fm1 + f0) / 2.
 
-    def limit(self, f, fi, lens, d, shift=(0, 0, 0)):
-        """PDM2 (mhd3d3.f90:1069-1172) or TVD (1174-1250, which drops the shifts)."""
-        if self.reconop == 2:
+    def limit(self, f, fi, lens, d, shift=(0, 0, 0), axes=(0, 1, 2)):
+        """PDM2 (mhd3d3.f90:1069-1172) or TVD: mhd3d3's (1174-1250) drops the
+        stencil shifts, mhd3d2's (mhd3d2.f90:1137-1199, tvd_shift = 1) honours them."""
+        if self.reconop == 2 and not self.tvd_shift:
             shift = (0, 0, 0)
-        fm2, fm1, f0, fp1 = self._stencil(f, d, lens, shift, ms=(-2, -1, 0, 1))
+        fm2, fm1, f0, fp1 = self._stencil(f, d, lens, shift, ms=(-2, -1, 0, 1), axes=axes)
         if self.reconop == 2:
             eps = self.eps
             a = (fm1 - fm2) / (f0 - fm1 + eps)
@@ -153,7 +156,7 @@ class NumpyMHD:
         axes=(d,) the dir 4..6 form (the other axes whole)."""
         if self.reconop >= 3:
             return self.weno(f, lens, d, axes)
-        return self.limit(f, self.interp(f, lens, d), lens, d)
+        return self.limit(f, self.interp(f, lens, d, axes), lens, d, axes=axes)
 
     def weno(self, f, lens, d, axes=(0, 1, 2)):
         """WENO5 (mhd3d3.f90:1252-1378) and MPWENO5 (1405-1596)."""
@@ -324,6 +327,51 @@ class NumpyMHD:
             out.append(dum + eta * (b1l + b2r - b1r - b2l))
         return out
 
+    def get_eijk_Yee(self, rho, vx, vy, vz, p, bx, by, bz):
+        """get_eijk_Yee (mhd3d3.f90:1654-1752) with get_v_center (2562-2592):
+        split electric fields of the Gaussian velocity moments at the cell
+        centres, reconstructed to the edges in two passes (left states of +
+        moments, right states of - moments) and summed.  -> [ei, ej, ek]."""
+        nx, ny, nz, ng = self.nx, self.ny, self.nz, self.ng
+        nx0, ny0, nz0 = self.nx0, self.ny0, self.nz0
+        bsq = bx ** 2 + by ** 2 + bz ** 2
+        lam = rho / (2. * p + bsq)
+        x0p, x0n, x1p, x1n = self.get_v_face(lam, vx)
+        y0p, y0n, y1p, y1n = self.get_v_face(lam, vy)
+        z0p, z0n, z1p, z1n = self.get_v_face(lam, vz)
+        E = {  # [pp, np, pn, nn] per edge axis
+            "z": [bx * x0p * y1p - by * x1p * y0p, bx * x0n * y1p - by * x1n * y0p,
+                  bx * x0p * y1n - by * x1p * y0n, bx * x0n * y1n - by * x1n * y0n],
+            "x": [by * y0p * z1p - bz * y1p * z0p, by * y0n * z1p - bz * y1n * z0p,
+                  by * y0p * z1n - bz * y1p * z0n, by * y0n * z1n - bz * y1n * z0n],
+            "y": [bz * z0p * x1p - bx * z1p * x0p, bz * z0n * x1p - bx * z1n * x0p,
+                  bz * z0p * x1n - bx * z1p * x0n, bz * z0n * x1n - bx * z1n * x0n]}
+        # (split fields, first axis and its extents, second axis and its extents, edge axis)
+        plan = [("x", 1, (nx, ny0 + 1, nz), 2, (nx, ny0 + 1, nz0 + 1), 0, nx0),
+                ("y", 2, (nx, ny, nz0 + 1), 0, (nx0 + 1, ny, nz0 + 1), 1, ny0),
+                ("z", 0, (nx0 + 1, ny, nz), 1, (nx0 + 1, ny0 + 1, nz), 2, nz0)]
+        out = []
+        for key, d1, l1, d2, l2, ax, n0 in plan:
+            pp, np_, pn, nn = E[key]
+            qepp = self.reconstruct(pp, l1, d1, axes=(d1,))[0]
+            qepn = self.reconstruct(pn, l1, d1, axes=(d1,))[0]
+            qenn = self.reconstruct(nn, l1, d1, axes=(d1,))[1]
+            qenp = self.reconstruct(np_, l1, d1, axes=(d1,))[1]
+            epp = self.reconstruct(qepp, l2, d2, axes=(d2,))[0]
+            enp = self.reconstruct(qenp, l2, d2, axes=(d2,))[0]
+            enn = self.reconstruct(qenn, l2, d2, axes=(d2,))[1]
+            epn = self.reconstruct(qepn, l2, d2, axes=(d2,))[1]
+            sl = [slice(None)] * 3
+            sl[ax] = slice(ng, ng + n0)
+            sl = tuple(sl)
+            out.append(epp[sl] + enp[sl] + epn[sl] + enn[sl])
+        return out
+
+    def get_eijk(self, rho, vx, vy, vz, p, bx, by, bz, bi, bj, bk):
+        if self.emf_kind == 1:
+            return self.get_eijk_Yee(rho, vx, vy, vz, p, bx, by, bz)
+        return self.get_eijk_LFM(rho, vx, vy, vz, bx, by, bz, bi, bj, bk)
+
     def get_v_face(self, llam, lv):
         """get_v_face (mhd3d3.f90:2594-2615)."""
         a = np.sqrt(llam)
@@ -448,8 +496,8 @@ class NumpyMHD:
         for k in ("rho", "vx", "vy", "vz", "p", "bx", "by", "bz", "bi", "bj", "bk"):  # advance_previous
             setattr(self, k + "p", getattr(self, k).copy())
         self.tau0 = tau
-        ei, ej, ek = self.get_eijk_LFM(h["rho"], h["vx"], h["vy"], h["vz"], h["bx"], h["by"], h["bz"],
-                                       h["bi"], h["bj"], h["bk"])
+        ei, ej, ek = self.get_eijk(h["rho"], h["vx"], h["vy"], h["vz"], h["p"], h["bx"], h["by"], h["bz"],
+                                   h["bi"], h["bj"], h["bk"])
         fl = self.get_flux_stress(h["rho"], h["vx"], h["vy"], h["vz"], h["p"], h["bx"], h["by"], h["bz"])
         # advance_corrector1, stepop = 1
         rho, eng = rho0.copy(), eng0.copy()
@@ -511,7 +559,7 @@ class NumpyMHD:
             rho0 = rho.copy()
             rhovx0, rhovy0, rhovz0 = rho * vx, rho * vy, rho * vz
             eng0 = .5 * rho * (vx ** 2 + vy ** 2 + vz ** 2) + p / (gam - 1.)
-            ei, ej, ek = self.get_eijk_LFM(rho, vx, vy, vz, self.bx, self.by, self.bz, self.bi, self.bj, self.bk)
+            ei, ej, ek = self.get_eijk(rho, vx, vy, vz, p, self.bx, self.by, self.bz, self.bi, self.bj, self.bk)
             fl = self.get_flux_stress(rho, vx, vy, vz, p, self.bx, self.by, self.bz)
             # advance_corrector1 (3836-3866)
             rho, eng = rho0.copy(), eng0.copy()
@@ -554,8 +602,8 @@ class NumpyMHD:
         return self.get_flux_stress(self.rho, self.vx, self.vy, self.vz, self.p, self.bx, self.by, self.bz)
 
     def emf(self):
-        return self.get_eijk_LFM(self.rho, self.vx, self.vy, self.vz, self.bx, self.by, self.bz,
-                                 self.bi, self.bj, self.bk)
+        return self.get_eijk(self.rho, self.vx, self.vy, self.vz, self.p, self.bx, self.by, self.bz,
+                             self.bi, self.bj, self.bk)
 
     def state(self) -> dict:
         return {"rho": self.rho, "vx": self.vx, "vy": self.vy, "vz": self.vz, "p": self.p, "bx": self.bx,

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from mhd3d_mpi_fortran_gb300 import ics
-from mhd3d_mpi_fortran_gb300.abi import BC_EVEN, BC_PERIODIC, Params
+from mhd3d_mpi_fortran_gb300.abi import BC_EVEN, BC_PERIODIC, EMF_YEE, Params
 from oracle.mhd_numpy import NumpyMHD
 from oracle.oracle import OracleSolver
 
@@ -123,5 +123,29 @@ def test_even_walls_agree(recon, stepop):
 def test_even_walls_on_a_random_ragged_state():
     s = random_state(12, 10, 8, seed=7)
     prm = Params(12, 10, 8, reconop=1, stepop=3, bc=(BC_EVEN, BC_PERIODIC, BC_EVEN), tau=0.05 * ics.cfl_dt(s))
+    compare_instant(prm, s)
+    compare_steps(prm, s, 2)
+
+
+@pytest.mark.parametrize("recon", [1, 2, 3, 4])
+def test_yee_emf_agrees(recon):
+    """get_eijk_Yee (mhd3d3.f90:1654-1752; dead code in the reference, built
+    here as emf = MHD_EMF_YEE) on a random state on a ragged grid."""
+    s = random_state(12, 10, 8, seed=8)
+    compare_instant(Params(12, 10, 8, reconop=recon, emf=EMF_YEE), s)
+
+
+@pytest.mark.parametrize("stepop", [1, 2, 3])
+def test_yee_steps_agree(stepop):
+    s = ics.orszag_tang_3d(12, seed=3)
+    compare_steps(Params(12, 12, 12, reconop=1, stepop=stepop, emf=EMF_YEE, tau=3e-4 if stepop == 1
+                         else 0.3 * ics.cfl_dt(s)), s, 3)
+
+
+def test_tvd_with_the_stencil_shifts_of_mhd3d2_agrees():
+    """tvd_shift = 1: the corner TVD calls honour their stencil shifts, as
+    mhd3d2.f90:1137-1199 does (mhd3d3's TVD drops them)."""
+    s = random_state(12, 10, 8, seed=9)
+    prm = Params(12, 10, 8, reconop=2, tvd_shift=1, stepop=3, tau=0.05 * ics.cfl_dt(s))
     compare_instant(prm, s)
     compare_steps(prm, s, 2)
