@@ -11,7 +11,8 @@ Generators:
 * ``orszag_tang_2d``  -- point-sampled vortex of ``init_ic_otv`` (mhd3d2.f90:3420-3438).
 * ``orszag_tang_3d``  -- 3-D OT with vz = 0.1 sin 2 pi z, B from an edge vector
                          potential (div B = 0 to round-off), seeded rho noise.
-* ``blast``           -- magnetised blast (``init_ic_bws``, mhd3d2.f90:3358-3418, 3-D sphere).
+* ``blast``           -- magnetised blast (after ``init_ic_bws``, mhd3d2.f90:3358-3418, as a 3-D sphere).
+* ``blast_bws``       -- ``init_ic_bws`` as written: the pressure cylinder about the domain origin.
 * ``implosion``       -- diagonal-interface implosion (``init_ic_imp``, mhd3d2.f90:3440-3471).
 * ``turbulence``      -- solenoidal Gaussian-random v and B, E(k) ~ k^-2 on
                          kmin <= |k| <= kmax, B from a vector potential.
@@ -253,6 +254,23 @@ def blast(n: int, nord: int = 8, p_in: float = 10.0, p_out: float = 0.1, r0: flo
     s.p[...] = np.where(r2 < r0 * r0, p_in, p_out)
     s.bi[...] = 1.0 / np.sqrt(2.0)
     s.bj[...] = 1.0 / np.sqrt(2.0)
+    s.bk[...] = 0.0
+    return s
+
+
+def blast_bws(n: int, nz0: int = 8, nord: int = 8, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0)) -> State:
+    """init_ic_bws (mhd3d2.f90:3358-3418) as written, on the deck's domain
+    (mhd3d2.in: the unit box): rho = 1, v = 0, p = .1, and p = 10 where
+    xc^2 + yc^2 < .01 -- a cylinder of radius .1 along z about the origin of
+    the coordinates -- with bi = bj = .5, bk = 0.  The reference keeps its
+    call commented out (mhd3d2.f90:3186) in favour of init_ic_otv."""
+    g = grid(n, n, nz0, nord=nord, lo=lo, hi=hi)
+    s = empty_state(g)
+    xc, yc, _ = _bcast(g)
+    s.rho[...] = 1.0
+    s.p[...] = np.where(np.broadcast_to(xc ** 2 + yc ** 2 < 0.01, s.p.shape), 10.0, 0.1)
+    s.bi[...] = 0.5
+    s.bj[...] = 0.5
     s.bk[...] = 0.0
     return s
 

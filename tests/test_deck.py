@@ -69,3 +69,32 @@ def test_turbulence_rms_and_divergence():
     div = (np.diff(s.bi, axis=0)[sl, sl, sl] + np.diff(s.bj, axis=1)[sl, sl, sl] +
            np.diff(s.bk, axis=2)[sl, sl, sl]) / g.dx[ng]
     assert np.abs(div).max() < 1e-12
+
+
+def test_blast_bws_is_the_reference_cylinder():
+    """init_ic_bws (mhd3d2.f90:3358-3418): p = 10 inside xc^2 + yc^2 < .01, .1
+    outside, whatever z; rho = 1, v = 0, bi = bj = .5, bk = 0."""
+    s = ics.blast_bws(32, nz0=4, lo=(-0.5, -0.5, 0.0), hi=(0.5, 0.5, 1.0))
+    xc, yc, zc = s.grid.centres()
+    inside = (xc[:, None] ** 2 + yc[None, :] ** 2) < 0.01
+    assert inside.any() and (~inside).any()
+    for k in range(s.p.shape[2]):
+        assert np.array_equal(s.p[:, :, k], np.where(inside, 10.0, 0.1))
+    assert np.all(s.rho == 1.0) and np.all(s.vx == 0) and np.all(s.vy == 0) and np.all(s.vz == 0)
+    assert np.all(s.bi == 0.5) and np.all(s.bj == 0.5) and np.all(s.bk == 0.0)
+
+
+def test_blast_bws_runs_in_the_oracle():
+    """The cylinder centred in a periodic box: clean steps, div B at round-off,
+    mass conserved."""
+    import pytest
+    from mhd3d_mpi_fortran_gb300.abi import Params
+    from oracle.oracle import OracleSolver
+    s = ics.blast_bws(16, nz0=4, lo=(-0.5, -0.5, 0.0), hi=(0.5, 0.5, 1.0))
+    o = OracleSolver(Params(16, 16, 4, tau=0.3 * ics.cfl_dt(s)), s)
+    d0 = o.diagnostics()
+    _, st = o.step(3)
+    d1 = o.diagnostics()
+    assert st == 0
+    assert d1["divb_max"] <= 1e-12
+    assert d1["mass"] == pytest.approx(d0["mass"], rel=1e-13)
