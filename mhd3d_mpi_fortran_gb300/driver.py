@@ -19,7 +19,7 @@ Differences from the Fortran driver, all forced by this environment:
   after the frame that saw them has been written, as the reference stops
   after ``outputxyz``.
 
-Usage: ``python -m mhd3d_mpi_fortran_gb300.driver mhd3d3.in outdir [--fp32] [--periodic]``.
+Usage: ``python -m mhd3d_mpi_fortran_gb300.driver mhd3d3.in outdir [--fp32] [--periodic] [--ic tube|otv|bws|imp]``.
 """
 from __future__ import annotations
 
@@ -31,7 +31,7 @@ from pathlib import Path
 import numpy as np
 
 from . import ics
-from .abi import ST_NAN, ST_NEG_RHO, BC_PERIODIC, FP32, FP64
+from .abi import ST_NAN, ST_NEG_RHO, BC_PERIODIC, BC_OUTFLOW, FP32, FP64
 from .deck import read_deck, params_from_deck, domain_from_deck
 from .solver import MHDSolver
 
@@ -42,18 +42,44 @@ class RunStopped(RuntimeError):
     """diag_rho_neg / diag_overflow would have stopped the reference here."""
 
 
-def initial_state(deck: dict, nord: int) -> ics.State:
-    """init_ic of mhd3d3 (mhd3d3.f90:3517-3583): the shock tube along z on the
-    deck's domain; the deck's x and y sizes must be equal (the tube's
-    transverse extent)."""
+# The initial conditions a deck can start from: mhd3d3's init_ic and the
+# three of mhd3d2 (its program calls init_ic_otv, mhd3d2.f90:3186-3188).
+ICS = ("tube", "otv", "bws", "imp")
+
+
+def ic_grid(deck: dict, nord: int, ic: str = "tube") -> tuple:
+    """(nx0, ny0, nz0, bc) of the run.  mhd3d2's ICs are 2-D: its deck has
+    nz0 = 1 and fills z with copies of the one plane (fillz_even1,
+    mhd3d2.f90:687-697, 731-772).  Here z gets ng planes (the least the ghost
+    fill takes) with the outflow fill, which is the same copy, and x, y keep
+    mhd3d2's periodic topology (mhd3d2.f90:3063-3064)."""
     grid = deck.get("grid", {})
     nx, ny, nz = (int(grid.get(k + "0g", grid.get(k + "0", 1))) for k in ("nx", "ny", "nz"))
+    if ic == "tube":
+        return nx, ny, nz, None
+    if ic not in ICS:
+        raise ValueError(f"ic must be one of {ICS}")
+    return nx, ny, max(nz, nord // 2), (BC_PERIODIC, BC_PERIODIC, BC_OUTFLOW)
+
+
+def initial_state(deck: dict, nord: int, ic: str = "tube") -> ics.State:
+    """The deck's initial state.  tube: init_ic of mhd3d3 (mhd3d3.f90:3517-3583),
+    the shock tube along z on the deck's domain (x and y sizes equal, the
+    tube's transverse extent).  otv / bws / imp: init_ic_otv / init_ic_bws /
+    init_ic_imp of mhd3d2 (mhd3d2.f90:3358-3471) on the deck's x-y grid."""
+    nx, ny, nz, _ = ic_grid(deck, nord, ic)
     lo, hi = domain_from_deck(deck)
     if nx != ny:
-        raise ValueError("init_ic's tube needs nx0G == ny0G")
-    if lo != (-1.0, -1.0, -1.0) or hi != (1.0, 1.0, 1.0):
-        raise ValueError("init_ic's tube is set up on the deck domain [-1, 1]^3")
-    return ics.shock_tube(nz, axis=2, nord=nord, ntrans=nx)
+        raise ValueError(f"the {ic} initial condition needs nx0G == ny0G")
+    if ic == "tube":
+        if lo != (-1.0, -1.0, -1.0) or hi != (1.0, 1.0, 1.0):
+            raise ValueError("init_ic's tube is set up on the deck domain [-1, 1]^3")
+        return ics.shock_tube(nz, axis=2, nord=nord, ntrans=nx)
+    if ic == "bws":
+        return ics.blast_bws(nx, nz0=nz, nord=nord, lo=lo, hi=hi)
+    if lo != (0.0, 0.0, 0.0) or hi != (1.0, 1.0, 1.0):
+        raise ValueError(f"the {ic} initial condition is set up on the unit box (mhd3d2.in dom)")
+    return ics.orszag_tang_2d(nx, nz0=nz, nord=nord) if ic == "otv" else ics.implosion(nx, nz0=nz, nord=nord)
 
 
 class FrameWriter:
@@ -116,7 +142,7 @@ def read_stime(path) -> np.ndarray:
 
 
 def run(deck, outdir, precision: int = FP64, periodic: bool = False, state: ics.State | None = None,
-        nframes: int | None = None, nts: int | None = None) -> dict:
+        nframes: int | None = None, nts: int | None = None, ic: str = "tube") -> dict:
     """Run the deck: frame 0 is the initial state, then nframes frames of nts
     steps each (the deck's values unless given).  Returns a summary dict."""
     deck = read_deck(deck) if not isinstance(deck, dict) else deck
@@ -124,7 +150,10 @@ def run(deck, outdir, precision: int = FP64, periodic: bool = False, state: ics.
     nframes = int(lst.get("nframes", 1)) if nframes is None else nframes
     nts = int(lst.get("nts", 1)) if nts is None else nts
     prm = params_from_deck(deck, precision=precision, bc=BC_PERIODIC if periodic else None)
-    st0 = state if state is not None else initial_state(deck, prm.nord)
+    if ic != "tube" and state is None:
+        _, _, nz0, bc = ic_grid(deck, prm.nord, ic)
+        prm.nz0, prm.bc = nz0, bc
+    st0 = state if state is not None else initial_state(deck, prm.nord, ic)
     ng = prm.nord // 2
     w = FrameWriter(outdir, (prm.nx0, prm.ny0, prm.nz0), nframes, ng)
     time = 0.0
@@ -162,8 +191,10 @@ def main(argv=None):
     ap.add_argument("outdir")
     ap.add_argument("--fp32", action="store_true")
     ap.add_argument("--periodic", action="store_true")
+    ap.add_argument("--ic", choices=ICS, default="tube",
+                    help="tube: mhd3d3's init_ic; otv / bws / imp: mhd3d2's (2-D, periodic x-y)")
     a = ap.parse_args(argv)
-    print(json.dumps(run(a.deck, a.outdir, precision=FP32 if a.fp32 else FP64, periodic=a.periodic)))
+    print(json.dumps(run(a.deck, a.outdir, precision=FP32 if a.fp32 else FP64, periodic=a.periodic, ic=a.ic)))
 
 
 if __name__ == "__main__":

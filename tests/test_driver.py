@@ -54,6 +54,59 @@ def test_initial_state_is_the_reference_tube():
     assert s.rho[8, 8, 5] == 1.0 and s.rho[8, 8, 20] == 0.125
 
 
+# mhd3d2.in's scheme and grid (one rank, a smaller x-y grid): 2-D, nz0 = 1
+DECK2 = """
+ &dom
+ xmin=0., xmax=1., ymin=0., ymax=1., zmin=0., zmax=1.
+/
+ &grid
+ nx0G=16, ny0G=16, nz0=1, xprocs=1, yprocs=1
+/
+ &comset
+ nord=6, reconop=4, stepop=3, outop=2
+/
+ &list
+ nts=100, tau=1.e-4, nframes=2000, nrst=0, nfdump=10
+/
+ &free
+ cfl=.3, pdmb=4., eps=1.e-8, alpha=2., beta=4.
+/
+"""
+
+
+def test_mhd3d2_ics_lift_z_to_ng_planes_with_the_z_constant_fill():
+    from mhd3d_mpi_fortran_gb300.abi import BC_OUTFLOW, BC_PERIODIC
+    deck = driver.read_deck(DECK2)
+    assert driver.ic_grid(deck, 6, "otv") == (16, 16, 3, (BC_PERIODIC, BC_PERIODIC, BC_OUTFLOW))
+    s = driver.initial_state(deck, 6, "otv")
+    ref = ics.orszag_tang_2d(16, nz0=3, nord=6)
+    for a, b in zip(s.arrays(), ref.arrays()):
+        assert np.array_equal(a, b)
+    assert driver.initial_state(deck, 6, "imp").rho.shape == (22, 22, 9)
+    assert driver.initial_state(deck, 6, "bws").bi[0, 0, 0] == 0.5
+    with pytest.raises(ValueError):
+        driver.ic_grid(deck, 6, "nope")
+
+
+def test_mhd3d2_deck_stays_two_dimensional():
+    """init_ic_otv with mhd3d2.in's scheme (MP-WENO5, RK3, nord 6) on the lifted
+    grid: every z plane evolves identically, as in the reference's 2-D run."""
+    from mhd3d_mpi_fortran_gb300.deck import params_from_deck
+    from oracle.oracle import OracleSolver
+    deck = driver.read_deck(DECK2)
+    prm = params_from_deck(deck)
+    _, _, prm.nz0, prm.bc = driver.ic_grid(deck, prm.nord, "otv")
+    o = OracleSolver(prm, driver.initial_state(deck, prm.nord, "otv"))
+    _, st = o.step(5)
+    assert st == 0
+    out = o.fetch()
+    for k in ("rho", "p", "vx", "vy", "bi", "bj"):
+        a = out[k]
+        for z in range(1, a.shape[2]):
+            assert np.array_equal(a[:, :, z], a[:, :, 0]), (k, z)
+    assert np.abs(out["vz"]).max() == 0.0 and np.abs(out["bk"]).max() == 0.0
+
+
 @pytest.mark.gpu
 def test_deck_run_writes_every_frame(tmp_path):
     out = driver.run(DECK, tmp_path)
