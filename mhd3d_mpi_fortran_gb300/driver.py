@@ -45,21 +45,22 @@ class RunStopped(RuntimeError):
 # The initial conditions a deck can start from: mhd3d3's init_ic and the
 # three of mhd3d2 (its program calls init_ic_otv, mhd3d2.f90:3186-3188).
 ICS = ("tube", "otv", "bws", "imp")
+Z2D = 8  # z planes of a 2-D run: the smallest axis the solver's tests run
 
 
 def ic_grid(deck: dict, nord: int, ic: str = "tube") -> tuple:
     """(nx0, ny0, nz0, bc) of the run.  mhd3d2's ICs are 2-D: its deck has
     nz0 = 1 and fills z with copies of the one plane (fillz_even1,
-    mhd3d2.f90:687-697, 731-772).  Here z gets ng planes (the least the ghost
-    fill takes) with the outflow fill, which is the same copy, and x, y keep
-    mhd3d2's periodic topology (mhd3d2.f90:3063-3064)."""
+    mhd3d2.f90:687-697, 731-772).  Here z gets at least Z2D planes with the
+    outflow fill, which is the same copy, so every plane evolves identically;
+    x, y keep mhd3d2's periodic topology (mhd3d2.f90:3063-3064)."""
     grid = deck.get("grid", {})
     nx, ny, nz = (int(grid.get(k + "0g", grid.get(k + "0", 1))) for k in ("nx", "ny", "nz"))
     if ic == "tube":
         return nx, ny, nz, None
     if ic not in ICS:
         raise ValueError(f"ic must be one of {ICS}")
-    return nx, ny, max(nz, nord // 2), (BC_PERIODIC, BC_PERIODIC, BC_OUTFLOW)
+    return nx, ny, max(nz, Z2D, nord // 2), (BC_PERIODIC, BC_PERIODIC, BC_OUTFLOW)
 
 
 def initial_state(deck: dict, nord: int, ic: str = "tube") -> ics.State:

@@ -74,15 +74,15 @@ DECK2 = """
 """
 
 
-def test_mhd3d2_ics_lift_z_to_ng_planes_with_the_z_constant_fill():
+def test_mhd3d2_ics_lift_z_to_eight_planes_with_the_z_constant_fill():
     from mhd3d_mpi_fortran_gb300.abi import BC_OUTFLOW, BC_PERIODIC
     deck = driver.read_deck(DECK2)
-    assert driver.ic_grid(deck, 6, "otv") == (16, 16, 3, (BC_PERIODIC, BC_PERIODIC, BC_OUTFLOW))
+    assert driver.ic_grid(deck, 6, "otv") == (16, 16, 8, (BC_PERIODIC, BC_PERIODIC, BC_OUTFLOW))
     s = driver.initial_state(deck, 6, "otv")
-    ref = ics.orszag_tang_2d(16, nz0=3, nord=6)
+    ref = ics.orszag_tang_2d(16, nz0=8, nord=6)
     for a, b in zip(s.arrays(), ref.arrays()):
         assert np.array_equal(a, b)
-    assert driver.initial_state(deck, 6, "imp").rho.shape == (22, 22, 9)
+    assert driver.initial_state(deck, 6, "imp").rho.shape == (22, 22, 14)
     assert driver.initial_state(deck, 6, "bws").bi[0, 0, 0] == 0.5
     with pytest.raises(ValueError):
         driver.ic_grid(deck, 6, "nope")
