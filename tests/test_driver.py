@@ -118,3 +118,24 @@ def test_deck_run_writes_every_frame(tmp_path):
     s0 = driver.initial_state(driver.read_deck(DECK), 8)
     assert np.array_equal(fr["rho"][0], s0.rho[4:-4, 4:-4, 4:-4].transpose(2, 1, 0))
     assert not np.array_equal(fr["rho"][2], fr["rho"][0])
+
+
+@pytest.mark.parametrize("recon,stepop,bc", [(4, 3, "2d"), (3, 1, "walls"), (5, 2, "2d")])
+def test_nord6_decks_run_bit_identically_at_nord8(recon, stepop, bc):
+    """The driver runs nord = 6 decks with 8 ghost cells: the interior and the
+    time steps are bit-identical (WENO / TVD stencils reach 3 cells; deeper
+    ghosts are exact copies)."""
+    from mhd3d_mpi_fortran_gb300.abi import BC_EVEN, BC_OUTFLOW, BC_PERIODIC, Params
+    from oracle.oracle import OracleSolver
+    bcs = (BC_PERIODIC, BC_PERIODIC, BC_OUTFLOW) if bc == "2d" else (BC_EVEN,) * 3
+    res = {}
+    for nord in (6, 8):
+        ng = nord // 2
+        prm = Params(16, 16, 8, nord=nord, reconop=recon, stepop=stepop, bc=bcs, tau=1e-3 if stepop == 1 else 2e-3)
+        o = OracleSolver(prm, ics.orszag_tang_2d(16, nz0=8, nord=nord))
+        taus = [o.step(1)[0] for _ in range(3)]
+        out = o.fetch()
+        res[nord] = (taus, {k: a[ng:a.shape[0] - ng, ng:a.shape[1] - ng, ng:a.shape[2] - ng] for k, a in out.items()})
+    assert res[6][0] == res[8][0]
+    for k in res[6][1]:
+        assert np.array_equal(res[6][1][k], res[8][1][k]), k
