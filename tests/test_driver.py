@@ -139,3 +139,29 @@ def test_nord6_decks_run_bit_identically_at_nord8(recon, stepop, bc):
     assert res[6][0] == res[8][0]
     for k in res[6][1]:
         assert np.array_equal(res[6][1][k], res[8][1][k]), k
+
+
+@pytest.mark.gpu
+def test_mhd3d2_otv_deck_runs_on_the_gpu(tmp_path):
+    """mhd3d2.in's scheme (MP-WENO5, RK3; its nord 6 run as 8) from init_ic_otv
+    on the lifted 2-D grid, through the driver loop: the last frame matches the
+    oracle's FP64 run, and every z plane of it is the same."""
+    from mhd3d_mpi_fortran_gb300.deck import params_from_deck
+    from oracle.oracle import OracleSolver
+    deck = driver.read_deck(DECK2)
+    out = driver.run(deck, tmp_path, nframes=2, nts=3, ic="otv")
+    assert out["frames"] == 3 and out["stopped"] is None
+    fr = driver.read_frames(tmp_path)
+    assert fr["rho"].shape == (3, 8, 16, 16)
+    prm = params_from_deck(deck)
+    prm.nord = driver.NORD_RUN
+    _, _, prm.nz0, prm.bc = driver.ic_grid(deck, prm.nord, "otv")
+    o = OracleSolver(prm, driver.initial_state(deck, prm.nord, "otv"))
+    o.step(6)
+    ref = o.fetch()
+    for v in ("rho", "vx", "vy", "p", "bx", "by"):
+        want = ref[v][4:-4, 4:-4, 4:-4].transpose(2, 1, 0)
+        got = fr[v][2]
+        assert np.abs(got - want).max() <= 1e-11 * np.abs(want).max(), v
+        for z in range(1, got.shape[0]):
+            assert np.array_equal(got[z], got[0]), (v, z)
