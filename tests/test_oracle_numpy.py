@@ -149,3 +149,24 @@ def test_tvd_with_the_stencil_shifts_of_mhd3d2_agrees():
     prm = Params(12, 10, 8, reconop=2, tvd_shift=1, stepop=3, tau=0.05 * ics.cfl_dt(s))
     compare_instant(prm, s)
     compare_steps(prm, s, 2)
+
+
+def test_randomised_configurations_agree():
+    """Hypothesis draws the grid shape, reconstruction, stepper, halo kinds,
+    EMF scheme and seed; the two restatements agree on the fluxes, the EMFs
+    and two steps of every configuration it draws."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @hyp.settings(max_examples=20, deadline=None, derandomize=True)
+    @hyp.given(shape=st.tuples(*[st.integers(8, 12)] * 3), recon=st.sampled_from([1, 2, 3, 4]),
+               stepop=st.sampled_from([1, 2, 3]), bc=st.tuples(*[st.sampled_from([BC_PERIODIC, BC_EVEN])] * 3),
+               emf=st.sampled_from([0, EMF_YEE]), seed=st.integers(0, 2 ** 16))
+    def check(shape, recon, stepop, bc, emf, seed):
+        s = random_state(*shape, seed=seed)
+        tau = 3e-4 if stepop == 1 else 0.05 * ics.cfl_dt(s)
+        prm = Params(*shape, reconop=recon, stepop=stepop, bc=bc, emf=emf, tau=tau)
+        compare_instant(prm, s)
+        compare_steps(prm, s, 2)
+
+    check()
