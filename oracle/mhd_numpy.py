@@ -10,11 +10,14 @@ transcription slip in either shows up as a disagreement between them.
 
 Scope: Cartesian mesh; per axis periodic halos (one rank of mhd3d2.f90's
 periodic topology: the SENDRECVs of fillx_center / fillx_face,
-mhd3d3.f90:346-390 / 482-525, exchange with the rank itself) or the even wall
-mirror those routines apply at a domain edge (xbc=0, the only value
-fill_hydro_mpi / fill_mag_mpi pass, 781-819); reconop 1 (PDM), 2 (TVD, van
-Leer, with mhd3d2's stencil shifts when tvd_shift = 1), 3 (WENO5) or 4
-(MP-WENO5, the reference deck's choice); LFM or Yee edge EMF;
+mhd3d3.f90:346-390 / 482-525, exchange with the rank itself), the even wall
+mirror those routines apply at a domain edge (xbc=0, the only value mhd3d3's
+fill_hydro_mpi / fill_mag_mpi pass, 781-819), the reflecting mirror (odd
+normal velocity, the xbc=1 of mhd3d2.f90:713, 720) or the zero-gradient
+outflow copy (no reference counterpart); reconop 1 (PDM), 2 (TVD, van
+Leer, with mhd3d2's stencil shifts when tvd_shift = 1), 3 (WENO5), 4
+(MP-WENO5, the reference deck's choice) or 5 (TVD with the MC limiter, no
+reference counterpart); LFM or Yee edge EMF;
 stepop 1 (AB2, step_ab 3602-3644, CFL tau), 2 (RK2) or 3 (RK3, the deck's),
 the last two with the deck's fixed tau (step_rk2 / step_rk3, 3646-3792).
 
@@ -54,8 +57,8 @@ class NumpyMHD:
 
     def __init__(self, params, state):
         p = params
-        if p.reconop not in (1, 2, 3, 4) or any(b not in (0, 1) for b in p.bc) or p.emf not in (0, 1):
-            raise ValueError("NumpyMHD covers periodic / even-wall PDM, TVD, WENO5, MP-WENO5 + LFM / Yee only")
+        if p.reconop not in (1, 2, 3, 4, 5) or any(b not in (0, 1, 2, 3) for b in p.bc) or p.emf not in (0, 1):
+            raise ValueError("NumpyMHD covers reconop 1-5, halo kinds 0-3 and the LFM / Yee EMFs")
         self.emf_kind, self.tvd_shift = p.emf, p.tvd_shift
         self.stepop, self.alpha, self.beta, self.cfl = p.stepop, p.alpha, p.beta, p.cfl
         self.bc = tuple(p.bc)
@@ -117,23 +120,28 @@ class NumpyMHD:
         """interp_pdm / interp_tvd (mhd3d3.f90:862-924, 991-1035), axis d = 0,1,2."""
         if self.reconop == 1:
             return _tap8(*self._stencil(f, d, lens, axes=axes))
-        fm1, f0 = self._stencil(f, d, lens, ms=(-1, 0), axes=axes)
+        fm1, f0 = self._stencil(f, d, lens, ms=(-1, 0), axes=axes)  # TVD, TVD-MC
         return (fm1 + f0) / 2.
 
     def limit(self, f, fi, lens, d, shift=(0, 0, 0), axes=(0, 1, 2)):
         """PDM2 (mhd3d3.f90:1069-1172) or TVD: mhd3d3's (1174-1250) drops the
         stencil shifts, mhd3d2's (mhd3d2.f90:1137-1199, tvd_shift = 1) honours them."""
-        if self.reconop == 2 and not self.tvd_shift:
+        tvd = self.reconop in (2, 5)
+        if tvd and not self.tvd_shift:
             shift = (0, 0, 0)
         fm2, fm1, f0, fp1 = self._stencil(f, d, lens, shift, ms=(-2, -1, 0, 1), axes=axes)
-        if self.reconop == 2:
+        if tvd:
+            # van Leer b = (a+|a|)/(1+|a|); TVD-MC (reconop 5, no reference
+            # counterpart) b = max(0, min(2a, (1+a)/2, 2)), the MC limiter phi(a)
+            def lim(a):
+                if self.reconop == 5:
+                    return _max(0., _min(_min(2. * a, .5 * (1. + a)), 2.))
+                return (a + np.abs(a)) / (1. + np.abs(a))
             eps = self.eps
             a = (fm1 - fm2) / (f0 - fm1 + eps)
-            b = (a + np.abs(a)) / (1. + np.abs(a))
-            fleft = fm1 - b * (fm1 - fi)
+            fleft = fm1 - lim(a) * (fm1 - fi)
             a = (f0 - fp1) / (fm1 - f0 + eps)
-            b = (a + np.abs(a)) / (1. + np.abs(a))
-            fright = f0 - b * (f0 - fi)
+            fright = f0 - lim(a) * (f0 - fi)
             return fleft, fright
         maxf = _max(fm1, f0)
         minf = _min(fm1, f0)
@@ -154,7 +162,7 @@ class NumpyMHD:
     def reconstruct(self, f, lens, d, axes=(0, 1, 2)):
         """reconstruct_3d (mhd3d3.f90:833-860) for dir = d+1 in 1..3; with
         axes=(d,) the dir 4..6 form (the other axes whole)."""
-        if self.reconop >= 3:
+        if self.reconop in (3, 4):
             return self.weno(f, lens, d, axes)
         return self.limit(f, self.interp(f, lens, d, axes), lens, d, axes=axes)
 
@@ -215,7 +223,7 @@ class NumpyMHD:
     def interp2(self, f, dirn, lens):
         """interp2_pdm / interp2_tvd (mhd3d3.f90:926-989, 1037-1067), edge family dirn = 1..3."""
         ng = self.ng
-        if self.reconop == 2:
+        if self.reconop in (2, 5):
             o = {1: [(0, -1, -1), (0, 0, -1), (0, 0, 0), (0, -1, 0)],
                  2: [(-1, 0, -1), (-1, 0, 0), (0, 0, 0), (0, 0, -1)],
                  3: [(-1, -1, 0), (0, -1, 0), (0, 0, 0), (-1, 0, 0)]}[dirn]
@@ -265,7 +273,7 @@ class NumpyMHD:
 
     def vav_center2corner(self, lv, dirn, lens):
         """get_vav_center2corner (mhd3d3.f90:1858-2116)."""
-        if self.reconop >= 3:
+        if self.reconop in (3, 4):
             v00_0, v00_1, v10_0, v10_1, v01_0, v01_1, v11_0, v11_1 = self._corner_weno(lv, dirn, lens)
         else:
             vi = self.interp2(lv, dirn, lens)
@@ -434,19 +442,30 @@ class NumpyMHD:
         self.bz = .5 * (self.bk[:, :, 1:] + self.bk[:, :, :-1])
 
     # -------------------------------------------------------------- fills
-    def _fill(self, a, axis, face):
+    def _fill(self, a, axis, face, sgn=1.0):
         """fillx_center / fillx_face of one rank (mhd3d3.f90:346-390, 482-525):
-        the periodic exchange, or the even mirror at both walls."""
+        the periodic exchange (kind 0), or the mirror at both walls (kind 1,
+        even; kind 2, with sgn = -1 for the normal velocity, the xbc = 1 that
+        mhd3d2's fill_hydro_mpi passes for vx in x and vy in y,
+        mhd3d2.f90:713, 720), or the zero-gradient copy of the boundary cell or
+        face (kind 3, outflow; no reference counterpart)."""
         a = np.moveaxis(a, axis, 0)  # a view: writes land in the array
         n, ng, nord = a.shape[0], self.ng, self.nord
+        n0 = n - nord - (1 if face else 0)
         i = np.arange(1, ng + 1)  # Fortran i = 1..ng
-        if self.bc[axis] == 1:
+        kind = self.bc[axis]
+        if kind == 3:
+            last = ng + n0 if face else ng + n0 - 1  # the last interior face / cell
+            a[0:ng] = a[ng]
+            a[n - ng:n] = a[last]
+            return
+        if kind in (1, 2):
             if face:  # aa(i)=aa(nord+2-i); aa(n+2-i)=aa(n0+i), n = lnx-1, n0 = n-nord
-                a[i - 1] = a[nord + 2 - i - 1]
-                a[n + 1 - i - 1] = a[n - 1 - nord + i - 1]
+                a[i - 1] = sgn * a[nord + 2 - i - 1]
+                a[n + 1 - i - 1] = sgn * a[n - 1 - nord + i - 1]
             else:  # aa(i)=aa(nord+1-i); aa(lnx+1-i)=aa(lnx-nord+i)
-                a[i - 1] = a[nord + 1 - i - 1]
-                a[n + 1 - i - 1] = a[n - nord + i - 1]
+                a[i - 1] = sgn * a[nord + 1 - i - 1]
+                a[n + 1 - i - 1] = sgn * a[n - nord + i - 1]
             return
         if face:
             a[0:ng] = a[n - nord - 1:n - ng - 1]   # aa(1:ng)=aa(lnx-nord:lnx-ng-1)
@@ -457,8 +476,9 @@ class NumpyMHD:
 
     def fill_hydro(self):
         for ax in range(3):
-            for a in (self.rho, self.p, self.vx, self.vy, self.vz):
-                self._fill(a, ax, False)
+            for a, normal in ((self.rho, None), (self.p, None), (self.vx, 0), (self.vy, 1), (self.vz, 2)):
+                sgn = -1.0 if (self.bc[ax] == 2 and normal == ax) else 1.0
+                self._fill(a, ax, False, sgn)
 
     def fill_mag(self):
         for ax in range(3):

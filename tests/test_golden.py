@@ -44,10 +44,7 @@ def _numpy_run(kind, kw, steps):
                     ng:ng + g.nz0 + ext.get(k, (0, 0, 0))[2]] for k in make_golden.FIELDS}
 
 
-# The fixtures inside the numpy restatement's scope: the reference's own
-# schemes and halos (TVD-MC and the reflecting / outflow halos have no
-# reference counterpart, so the C++ oracle alone specifies them).
-NUMPY_CASES = [c for c in CASES if c[2].get("reconop") != 5 and all(b in (0, 1) for b in c[2].get("bc", (0,)))]
+NUMPY_CASES = CASES
 
 
 @pytest.mark.parametrize("case", NUMPY_CASES, ids=[c[0] for c in NUMPY_CASES])

@@ -159,8 +159,8 @@ def test_randomised_configurations_agree():
     st = hyp.strategies
 
     @hyp.settings(max_examples=20, deadline=None, derandomize=True)
-    @hyp.given(shape=st.tuples(*[st.integers(8, 12)] * 3), recon=st.sampled_from([1, 2, 3, 4]),
-               stepop=st.sampled_from([1, 2, 3]), bc=st.tuples(*[st.sampled_from([BC_PERIODIC, BC_EVEN])] * 3),
+    @hyp.given(shape=st.tuples(*[st.integers(8, 12)] * 3), recon=st.sampled_from([1, 2, 3, 4, 5]),
+               stepop=st.sampled_from([1, 2, 3]), bc=st.tuples(*[st.sampled_from([0, 1, 2, 3])] * 3),
                emf=st.sampled_from([0, EMF_YEE]), seed=st.integers(0, 2 ** 16))
     def check(shape, recon, stepop, bc, emf, seed):
         s = random_state(*shape, seed=seed)
