@@ -30,6 +30,8 @@ Arrays are indexed [i, j, k] from 0: numpy index n is Fortran index n + 1.
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 from scipy.special import erfc
 
@@ -61,6 +63,7 @@ class NumpyMHD:
             raise ValueError("NumpyMHD covers reconop 1-5, halo kinds 0-3 and the LFM / Yee EMFs")
         self.emf_kind, self.tvd_shift = p.emf, p.tvd_shift
         self.stepop, self.alpha, self.beta, self.cfl = p.stepop, p.alpha, p.beta, p.cfl
+        self.dt_mode = p.dt_mode  # 1: RK steps take the CFL dt (no reference counterpart)
         self.bc = tuple(p.bc)
         self.nx0, self.ny0, self.nz0 = p.nx0, p.ny0, p.nz0
         self.ng, self.nord = p.nord // 2, p.nord
@@ -566,6 +569,8 @@ class NumpyMHD:
             return self.step_ab()
         gam, ng = self.gam, self.ng
         I = (slice(ng, ng + self.nx0), slice(ng, ng + self.ny0), slice(ng, ng + self.nz0))
+        if self.dt_mode == 1:
+            self.tau0 = self.get_dt()
         self.tau = self.tau0
         tau = self.tau
         # advance_previous (3794-3819), stepop = 2
@@ -617,6 +622,24 @@ class NumpyMHD:
             self.fill_hydro()
             self.fill_mag()
             self.get_bxyz()
+
+    def diagnostics(self) -> dict:
+        """Total mass and energy (plasma + magnetic) of the interior cells as
+        exactly rounded sums (math.fsum), max |div B| of the face fields, min
+        rho over every cell and the CFL dt (N4; no reference counterpart)."""
+        ng, gam = self.ng, self.gam
+        nx0, ny0, nz0 = self.nx0, self.ny0, self.nz0
+        I = (slice(ng, ng + nx0), slice(ng, ng + ny0), slice(ng, ng + nz0))
+        dv = self.dx * self.dy * self.dz
+        r, u, v, w, p = self.rho[I], self.vx[I], self.vy[I], self.vz[I], self.p[I]
+        a, b, c = self.bx[I], self.by[I], self.bz[I]
+        e = .5 * r * (u * u + v * v + w * w) + p / (gam - 1.) + .5 * (a * a + b * b + c * c)
+        bi = self.bi[ng:ng + nx0 + 1, I[1], I[2]]
+        bj = self.bj[I[0], ng:ng + ny0 + 1, I[2]]
+        bk = self.bk[I[0], I[1], ng:ng + nz0 + 1]
+        divb = (bi[1:] - bi[:-1]) / self.dx + (bj[:, 1:] - bj[:, :-1]) / self.dy + (bk[:, :, 1:] - bk[:, :, :-1]) / self.dz
+        return {"mass": math.fsum((r * dv).ravel()), "energy": math.fsum((e * dv).ravel()),
+                "divb_max": float(np.abs(divb).max()), "rho_min": float(self.rho.min()), "dt_cfl": self.get_dt()}
 
     def fluxes(self):
         return self.get_flux_stress(self.rho, self.vx, self.vy, self.vz, self.p, self.bx, self.by, self.bz)

@@ -170,3 +170,29 @@ def test_randomised_configurations_agree():
         compare_steps(prm, s, 2)
 
     check()
+
+
+@pytest.mark.parametrize("bc", [(0, 0, 0), (1, 2, 3)])
+def test_diagnostics_agree(bc):
+    """N4: the oracle's compensated (Neumaier) mass and energy sums against
+    exactly rounded ones; max |div B|, min rho and the CFL dt."""
+    s = ics.orszag_tang_3d(12, seed=5)
+    prm = Params(12, 12, 12, bc=bc, tau=0.4 * ics.cfl_dt(s))
+    o, n = OracleSolver(prm, s), NumpyMHD(prm, s)
+    for _ in range(2):
+        o.step(1)
+        n.step()
+    do, dn = o.diagnostics(), n.diagnostics()
+    assert do["mass"] == pytest.approx(dn["mass"], rel=1e-15, abs=0)
+    assert do["energy"] == pytest.approx(dn["energy"], rel=1e-14, abs=0)
+    assert abs(do["divb_max"] - dn["divb_max"]) <= 1e-13
+    assert do["rho_min"] == pytest.approx(dn["rho_min"], rel=1e-14)
+    assert do["dt_cfl"] == pytest.approx(dn["dt_cfl"], rel=1e-14)
+    o.close()
+
+
+@pytest.mark.parametrize("stepop", [2, 3])
+def test_cfl_dt_mode_agrees(stepop):
+    """dt_mode = CFL (no reference counterpart): RK steps take get_dt's dt."""
+    s = ics.orszag_tang_3d(12, seed=6)
+    compare_steps(Params(12, 12, 12, stepop=stepop, dt_mode=1, tau=1.0), s, 3)
