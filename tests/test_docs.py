@@ -1,0 +1,47 @@
+"""Every repository file and test the documents cite exists: a path in
+backticks (``csrc/mhd_api.cu``, ``tests/test_driver.py::test_name``) must
+resolve in the tree, and a cited test function must be defined there.
+Reference sources and decks, run outputs and ``a_fp32/64`` shorthands are the
+only names allowed not to resolve."""
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+PKG = ROOT / "mhd3d_mpi_fortran_gb300"
+DOCS = ["README.md", "DESIGN.md", "INTEGRATION.md", "profiles/README.md"]
+# files of the reference project and files a run writes
+NOT_IN_TREE = {"mhd3d3.f90", "mhd3d2.f90", "mhd3d3.in", "mhd3d2.in", "process_mhd_2d.m", "frames.json"}
+PAT = re.compile(r"`([A-Za-z0-9_./-]+\.(?:py|cu|cuh|h|cpp|md|json|f90|npz|in))(?:::(\w+))?`")
+
+
+def _tree_files():
+    return [p for p in ROOT.rglob("*") if p.is_file() and not {".git", "_work", "gpurun_out"} & set(p.parts)]
+
+
+def _resolve(path, files):
+    for base in (ROOT, PKG, ROOT / "profiles", ROOT / "oracle", ROOT / "tests"):
+        if (base / path).is_file():
+            return base / path
+    if "/" not in path:
+        hits = [p for p in files if p.name == path]
+        if hits:
+            return hits[0]
+    return None
+
+
+@pytest.mark.parametrize("doc", DOCS)
+def test_cited_files_and_tests_exist(doc):
+    files = _tree_files()
+    missing = []
+    for m in PAT.finditer((ROOT / doc).read_text()):
+        path, fn = m.group(1), m.group(2)
+        if Path(path).name in NOT_IN_TREE or re.search(r"fp32/64", path):
+            continue
+        hit = _resolve(path, files)
+        if hit is None:
+            missing.append(path)
+        elif fn and not re.search(rf"def {fn}\(", hit.read_text()):
+            missing.append(f"{path}::{fn}")
+    assert not missing, missing
