@@ -45,3 +45,16 @@ def test_cited_files_and_tests_exist(doc):
         elif fn and not re.search(rf"def {fn}\(", hit.read_text()):
             missing.append(f"{path}::{fn}")
     assert not missing, missing
+
+
+@pytest.mark.parametrize("doc", DOCS)
+def test_cited_kernels_and_entry_points_exist(doc):
+    """Every `k_*` kernel, `mhd_*` entry point and `oracle_*` function the
+    document names is defined in the sources."""
+    exts = {".cu", ".cuh", ".h", ".py", ".cpp", ".f90"}
+    roots = [PKG, ROOT / "include", ROOT / "oracle"]
+    src = "".join(p.read_text(errors="ignore") for r in roots for p in r.rglob("*")
+                  if p.is_file() and p.suffix in exts)
+    names = set(re.findall(r"`((?:k|mhd|oracle)_\w+)", (ROOT / doc).read_text()))
+    missing = sorted(n for n in names if not re.search(r"\b" + re.escape(n) + r"\b", src))
+    assert not missing, missing
