@@ -48,13 +48,14 @@ def test_single_precision_evaluation_stays_near_float32_rounding():
     """Evaluated in float32 the fractional error grows with z, where the
     rounding of the exponent's argument -z^2 + q is magnified by exp (1.5e-5
     near z = 9, on values of order 1e-35); where erfc is of order one it stays
-    below 1e-6, and the absolute error stays below 1e-8 everywhere."""
+    below 1e-6, and the absolute error (float32 rounding of the ten-term sum)
+    stays below 5e-7 everywhere."""
     z = np.linspace(0.0, 9.0, 20001)
     ref = special.erfc(z)
     got = erfcc(z.astype(np.float32), shipped_coefficients(), np.float32).astype(np.float64)
     near = z <= 2.0
     assert np.abs(got[near] / ref[near] - 1.0).max() < 1e-6
-    assert np.abs(got - ref).max() < 1e-8
+    assert np.abs(got - ref).max() < 5e-7
 
 
 def test_half_erfc_sign_handling():
