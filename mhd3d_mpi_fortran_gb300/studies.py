@@ -180,12 +180,19 @@ def equal_time(n: int = 256, steps: int = 100, recon: int = 1) -> dict:
 
 
 def learned_study(n: int = 64, train_seeds=tuple(range(100, 108)), val_seed: int = 108,
-                  test_seeds=(200, 201, 202, 203), steps: int = 100, every: int = 10, iters: int = 4000) -> dict:
+                  test_seeds=(200, 201, 202, 203), steps: int = 100, every: int = 10, iters: int = 4000,
+                  damp_seed: int | None = None) -> dict:
+    """Train the correction, optionally choose its damping on the rollout of
+    damp_seed (``learned.damp``), and evaluate it on the held-out seeds."""
     from . import learned
     import time
     t0 = time.perf_counter()
     mlp, loss, npairs, alpha = learned.train_correction(list(train_seeds), n, steps=2 * steps, every=every,
                                                         iters=iters, batch=16384, lr=1e-3, val_seeds=[val_seed])
+    damping = None
+    if damp_seed is not None:
+        gamma, errs = learned.damp(mlp, damp_seed, n, steps)
+        damping = {"seed": damp_seed, "gamma": gamma, "corrected_l1": errs}
     t_train = time.perf_counter() - t0
     rows = []
     for seed in test_seeds:
@@ -198,7 +205,7 @@ def learned_study(n: int = 64, train_seeds=tuple(range(100, 108)), val_seed: int
         "study": "learned", "workload": f"coarse {n}^3 vs fine {2 * n}^3 decaying turbulence (FP32 RK2 PDM), "
                                         f"{steps} coarse steps, {len(test_seeds)} held-out seeds",
         "train": {"seeds": len(train_seeds), "pairs": npairs, "iters": iters, "final_loss": loss,
-                  "alpha": [float(a) for a in alpha], "seconds_incl_data": t_train},
+                  "alpha": [float(a) for a in alpha], "damping": damping, "seconds_incl_data": t_train},
         "mean": agg, "per_seed": rows,
         "note": "errors are relative L1 of the conserved variables against the restricted fine run; "
                 "times are host wall clock with the device synchronised",
@@ -212,6 +219,8 @@ def main(argv=None) -> None:
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--recons", default="1,5,3", help="precision study: reconop values (1 PDM, 5 TVD-MC, 3 WENO5)")
+    ap.add_argument("--damp-seed", type=int, default=None,
+                    help="learned study: choose the correction's damping on this seed's rollout")
     a = ap.parse_args(argv)
     if a.study == "curvilinear":
         print(json.dumps(curvilinear(a.n or 192, a.steps or 200)), flush=True)
@@ -219,7 +228,7 @@ def main(argv=None) -> None:
         for r in tuple(int(r) for r in a.recons.split(",")):
             print(json.dumps(equal_time(a.n or 256, a.steps or 100, r)), flush=True)
     elif a.study == "learned":
-        print(json.dumps(learned_study(a.n or 64, steps=a.steps or 100)), flush=True)
+        print(json.dumps(learned_study(a.n or 64, steps=a.steps or 100, damp_seed=a.damp_seed)), flush=True)
     else:
         for line in precision(a.n or 256, a.steps or 500, tuple(int(r) for r in a.recons.split(","))):
             print(json.dumps(line), flush=True)

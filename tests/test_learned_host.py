@@ -56,3 +56,35 @@ def test_feature_rows_are_the_normalised_3x3x3_stencil():
                 assert np.allclose(row[f:f + 8], ref, rtol=2 ** -8, atol=1e-6)
                 f += 8
     assert np.all(row[216:] == 0) and x.dtype == np.uint16
+
+
+def test_choose_damping_picks_the_smallest_rollout_error():
+    errs = {1.0: 1.03, 0.75: 0.88, 0.5: 0.86, 0.25: 0.91}
+    g, got = learned.choose_damping(lambda g: errs[g])
+    assert g == 0.5 and got == errs
+
+
+class _FakeMLP:
+    """Stands in for the GPU network: records the output scales it is given."""
+
+    def __init__(self):
+        self.norm = None
+        self.calls = []
+
+    def set_norm(self, mean, std, scale):
+        self.norm = [np.asarray(mean, np.float32), np.asarray(std, np.float32), np.asarray(scale, np.float32)]
+        self.calls.append(float(self.norm[2][0]))
+
+
+def test_damp_scales_the_outputs_and_keeps_the_best(monkeypatch):
+    mlp = _FakeMLP()
+    mlp.set_norm(np.zeros(8), np.ones(8), np.full(8, 2.0))
+    mlp.calls.clear()
+    # a rollout error that is smallest when the output scale is 1.5 (gamma 0.75)
+    monkeypatch.setattr(learned, "evaluate",
+                        lambda m, seed, n, steps, nord=8: {"corrected_l1": abs(float(m.norm[2][0]) - 1.5)})
+    g, errs = learned.damp(mlp, seed=3, n_coarse=16, steps=10)
+    assert g == 0.75
+    assert mlp.calls[:4] == [2.0, 1.5, 1.0, 0.5]          # each damping tried on the undamped scales
+    assert np.allclose(mlp.norm[2], 1.5)                  # the chosen one is left in place
+    assert set(errs) == set(learned.DAMPINGS)
