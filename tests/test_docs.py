@@ -58,3 +58,35 @@ def test_cited_kernels_and_entry_points_exist(doc):
     names = set(re.findall(r"`((?:k|mhd|oracle)_\w+)", (ROOT / doc).read_text()))
     missing = sorted(n for n in names if not re.search(r"\b" + re.escape(n) + r"\b", src))
     assert not missing, missing
+
+
+@pytest.mark.parametrize("doc", ["README.md", "INTEGRATION.md"])
+def test_python_examples_match_the_api(doc):
+    """Each ```python block compiles, and every call to a package function or
+    class it names binds to that callable's signature."""
+    import ast
+    import inspect
+    import mhd3d_mpi_fortran_gb300 as pkg
+    from mhd3d_mpi_fortran_gb300 import abi, deck, ics, learned
+    modules = {"learned": learned, "ics": ics, "deck": deck, "abi": abi}
+    names = {"MHDSolver": pkg.MHDSolver, "ensemble_step": pkg.ensemble_step,
+             "ensemble_autotune": pkg.ensemble_autotune, "Params": abi.Params}
+    blocks = re.findall(r"```python\n(.*?)```", (ROOT / doc).read_text(), re.S)
+    for src in blocks:
+        tree = ast.parse(src)
+        for node in ast.walk(tree):
+            if not isinstance(node, ast.Call):
+                continue
+            f = node.func
+            fn = None
+            if isinstance(f, ast.Attribute) and isinstance(f.value, ast.Name) and f.value.id in modules:
+                fn = getattr(modules[f.value.id], f.attr, None)
+                assert fn is not None, f"{f.value.id}.{f.attr} does not exist"
+            elif isinstance(f, ast.Name) and f.id in names:
+                fn = names[f.id]
+            if fn is None:
+                continue
+            sig = inspect.signature(fn)
+            args = [object()] * len(node.args)
+            kwargs = {k.arg: object() for k in node.keywords if k.arg}
+            sig.bind(*args, **kwargs)  # raises TypeError on a mismatch
