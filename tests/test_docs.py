@@ -90,3 +90,22 @@ def test_python_examples_match_the_api(doc):
             args = [object()] * len(node.args)
             kwargs = {k.arg: object() for k in node.keywords if k.arg}
             sig.bind(*args, **kwargs)  # raises TypeError on a mismatch
+
+
+def test_c_example_compiles_against_the_header(tmp_path):
+    """The ```c example of INTEGRATION.md, wrapped in a function that declares
+    the host arrays it uses, compiles against include/mhd_gpu.h."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    block = re.search(r"```c\n(.*?)```", (ROOT / "INTEGRATION.md").read_text(), re.S).group(1)
+    body = "\n".join(line for line in block.splitlines() if not line.startswith("#include"))
+    arrays = ", ".join(f"double* {v}" for v in ("rho", "vx", "vy", "vz", "pr", "bi", "bj", "bk", "bx", "by", "bz",
+                                                  "dx", "dy", "dz"))
+    src = tmp_path / "example.c"
+    src.write_text(f'#include <stdio.h>\n#include "mhd_gpu.h"\nvoid example({arrays}) {{\n{body}\n}}\n')
+    r = subprocess.run([cc, "-std=c11", "-Wall", "-Werror", "-fsyntax-only", "-I", str(ROOT / "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
