@@ -61,6 +61,12 @@ module mhd_gpu_binding
          import :: c_int, c_ptr
          type(c_ptr), value :: h
       end function mhd_free
+
+      integer(c_int) function mhd_diagnostics(h, out) bind(C, name="mhd_diagnostics")
+         import :: c_int, c_double, c_ptr
+         type(c_ptr), value :: h
+         real(c_double), intent(out) :: out(*)
+      end function mhd_diagnostics
    end interface
 
    type(c_ptr), save :: gpu_handle = c_null_ptr
@@ -102,6 +108,18 @@ contains
       rc = mhd_fetch(gpu_handle, rho, vx, vy, vz, p, bx, by, bz, bi, bj, bk)
       if (rc /= 0) stop 'mhd_fetch failed'
    end subroutine gpu_fetch
+
+   !..device diagnostics for the driver's diag_* step (mhd3d3.f90:3137-3160):
+   !  mass and total energy (compensated FP64 sums), max |div B|, min rho
+   !  (diag_rho_neg) and the CFL dt (get_dt)
+   subroutine gpu_diagnostics(mass, energy, divb_max, rho_min, dt_cfl)
+      real(c_double), intent(out) :: mass, energy, divb_max, rho_min, dt_cfl
+      real(c_double) :: out(5)
+      integer(c_int) :: rc
+      rc = mhd_diagnostics(gpu_handle, out)
+      if (rc /= 0) stop 'mhd_diagnostics failed'
+      mass = out(1); energy = out(2); divb_max = out(3); rho_min = out(4); dt_cfl = out(5)
+   end subroutine gpu_diagnostics
 
    subroutine gpu_free()
       integer(c_int) :: rc

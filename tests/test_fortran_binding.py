@@ -96,7 +96,7 @@ def _c_arg_class(arg):
     a = re.sub(r"\bconst\b", "", arg)
     a = re.sub(r"\s+", " ", a).strip()
     base = a.split()[0].rstrip("*")
-    depth = a.count("*")
+    depth = a.count("*") + a.count("[")  # an array parameter is passed as a pointer
     elem = {"int32_t": "int32", "uint32_t": "int32", "int": "int32"}.get(base, base)
     return elem + "*" * depth
 
@@ -136,13 +136,13 @@ def _f90_arg_class(spec, is_array):
 def test_every_interface_names_a_declared_entry_point():
     protos = c_prototypes()
     ifaces = f90_interfaces()
-    assert set(ifaces) >= {"mhd_init", "mhd_step", "mhd_step_n", "mhd_fetch", "mhd_free"}
+    assert set(ifaces) >= {"mhd_init", "mhd_step", "mhd_step_n", "mhd_fetch", "mhd_free", "mhd_diagnostics"}
     for cname, (fname, _) in ifaces.items():
         assert fname == cname
         assert cname in protos, cname
 
 
-@pytest.mark.parametrize("name", ["mhd_init", "mhd_step", "mhd_step_n", "mhd_fetch", "mhd_free"])
+@pytest.mark.parametrize("name", ["mhd_init", "mhd_step", "mhd_step_n", "mhd_fetch", "mhd_free", "mhd_diagnostics"])
 def test_interface_arguments_match_the_prototype(name):
     _, fargs = f90_interfaces()[name]
     assert fargs == c_prototypes()[name], (name, fargs, c_prototypes()[name])
