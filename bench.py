@@ -13,12 +13,18 @@ steps (CUDA events on the solver's stream, graph replay, inputs resident);
 (D2H), all inside the timed region.
 
 ``--impl reference`` times the reference algorithm on the host cores instead
-(the oracle port: no Fortran compiler exists to build the reference itself),
-one bounded-size RK2 step per timed step.
+(the oracle port in its array-pass mode: no Fortran compiler exists to build
+the reference itself), one RK2 step of the same 256^3 workload per timed step,
+at most 20 timed steps.
+
+The line also carries ``fp64`` (the same workload in all-FP64 mode) and
+``equal_time`` (relative L1 error against the FP64 256^3 solve of FP32 and
+FP64 runs at comparable GPU time), both measured after the timed region.
 """
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -41,6 +47,35 @@ sys.path.insert(0, str(ROOT))
 #   ct: read 3 face B + 3 EMFs (+3 B^n on stage 2: 1.5), write 3 face B   10.5
 WORDS = {"flux_x": 16, "flux_y": 24, "flux_z_update": 23.5, "emf": 18, "ct": 10.5}
 LAUNCHES = {"flux_x": 1, "flux_y": 1, "flux_z_update": 1, "emf": 3, "ct": 1}
+RECON_NAMES = {1: "PDM", 2: "TVD", 3: "WENO5", 4: "MPWENO5", 5: "TVD-MC"}
+# the sources of the step kernels: counts and traffic read from profiles/
+# describe the code only while this hash matches the one stored beside them
+STEP_SOURCES = ("mhd_kernels.cuh", "mhd_state.h", "mhd_api.cu", "mhd_fp32.cu")
+
+
+def step_sources_sha16() -> str:
+    h = hashlib.sha256()
+    for name in STEP_SOURCES:
+        h.update((ROOT / "mhd3d_mpi_fortran_gb300" / "csrc" / name).read_bytes())
+    return h.hexdigest()[:16]
+
+
+def profile_file(name: str):
+    """(data, provenance) of a machine-readable profile summary; provenance
+    says whether it was captured on the current step kernels."""
+    f = ROOT / "profiles" / name
+    if not f.exists():
+        return None, None
+    d = json.loads(f.read_text())
+    sha = d.get("kernels_sha16") if isinstance(d, dict) else None
+    return d, {"file": f"profiles/{name}", "kernels_sha16": sha, "stale": sha != step_sources_sha16()}
+
+
+def bench_config(n: int, recon: int) -> dict:
+    """The workload both arms run (same keys and values in both lines)."""
+    return {"workload": f"{n}^3 periodic decaying MHD turbulence (seeded solenoidal v and B, k^-2 on "
+                        f"2<=k<=8), {RECON_NAMES[recon]} + RK2", "grid": [n, n, n], "recon": recon,
+            "stepper": "RK2", "l2": "inputs larger than L2 (state >= 0.9 GB), no flush"}
 
 
 def parse():
@@ -59,6 +94,9 @@ def parse():
                     help="launch shapes 'face_tile,ei_tile' (e.g. 8,8) instead of the autotuner's choice")
     ap.add_argument("--ensemble", type=int, default=0,
                     help="batched-ensemble mode: this many periodic OT grids of sizes {32,48,64,96}^3")
+    ap.add_argument("--no-study", action="store_true",
+                    help="skip the FP64 line and the error-at-equal-GPU-time table")
+    ap.add_argument("--study-steps", type=int, default=20)
     return ap.parse_args()
 
 
@@ -69,10 +107,9 @@ def roofs(zu_per_gpu: float, clocks: dict, recon: int, tiles) -> dict:
     profiles/counts_pdm_rk2_fp32.json.  Peaks: SMs x 128 FP32 lanes x 2 flop
     and SMs x 4 schedulers x 32 lanes per cycle, at the median SM clock seen
     during the timed region."""
-    cf = ROOT / "profiles" / "counts_pdm_rk2_fp32.json"
-    if recon != 1 or not cf.exists():
+    counts, prov = profile_file("counts_pdm_rk2_fp32.json")
+    if recon != 1 or counts is None:
         return {}
-    counts = json.loads(cf.read_text())
     key = f"td{tiles[0]}_ei{tiles[1]}"
     if key not in counts["per_zone_update"]:
         return {}
@@ -93,6 +130,7 @@ def roofs(zu_per_gpu: float, clocks: dict, recon: int, tiles) -> dict:
                        "peak_tinst_s": issue_peak / 1e12, "frac": zu_per_gpu * c["inst"] / issue_peak,
                        "peak_kind": f"nominal: {sms} SMs x 4 x 32 thread instructions x {mhz:.0f} MHz",
                        "counts_from": counts["source"]},
+        "counts_provenance": prov,
     }
 
 
@@ -212,32 +250,42 @@ def cpu_detail(recon=1):
     return rows
 
 
+REF_MAX_TIMED_STEPS = 20  # 256^3 array-pass steps take ~4.6 s on 16 Grace cores
+
+
 def run_reference(a):
+    """The reference's CPU path on the host cores: the FP64 oracle restatement
+    in its array-pass mode (the reference's own per-routine passes and
+    temporaries), all host threads, on the same workload as our arm (same
+    config); each step is one RK2 step of the whole grid.  At most
+    REF_MAX_TIMED_STEPS steps are timed so that the run stays within minutes;
+    the line's `steps` says how many."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    # bounded per-step sample so that warmup + K steps stay within minutes
-    n = 64 if a.steps > 40 else 96
+    n = a.n
     from mhd3d_mpi_fortran_gb300 import ics
     from mhd3d_mpi_fortran_gb300.abi import Params
     from oracle.oracle import OracleSolver, threads
-    s = ics.turbulence(n, seed=0)
-    prm = Params(n, n, n, reconop=a.recon, stepop=2, tau=ics.cfl_dt(s, cfl=0.3))
+    s, tau = workload(n)
+    prm = Params(n, n, n, reconop=a.recon, stepop=2, tau=tau)
     o = OracleSolver(prm, s)
-    o.step(max(1, min(a.warmup, 3)))
+    o.step(max(1, min(a.warmup, 1)))
+    k = max(1, min(a.steps, REF_MAX_TIMED_STEPS))
     t0 = time.perf_counter()
-    o.step(a.steps)
+    o.step(k)
     dt = time.perf_counter() - t0
-    v = n ** 3 * a.steps / dt
+    o.close()
+    v = n ** 3 * k / dt
     line = {
         "impl": "reference", "metric": "zone-updates/s", "value": v, "unit": "zone-updates/s",
-        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * dt / a.steps,
+        "n_gpus": a.gpus, "steps": k, "warmup": max(1, min(a.warmup, 1)), "ms_per_step": 1e3 * dt / k,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic: seeded solenoidal turbulence (same generator)",
-        "config": {"workload": f"periodic decaying MHD turbulence, PDM + RK2 (sample {n}^3 per step "
-                               f"of the 256^3 workload)", "grid": [n, n, n]},
+        "data": "synthetic: seeded solenoidal turbulence (same generator and seed as our arm)",
+        "config": bench_config(n, a.recon),
         "cpu_baseline": {"value": v, "unit": "zone-updates/s", "cores": threads(), "kind": "port",
-                         "sample": f"{a.steps} RK2 steps of a {n}^3 grid, FP64 oracle restatement (array passes, as the reference computes)"},
+                         "sample": f"{k} RK2 steps of the {n}^3 workload (requested {a.steps}), FP64 oracle "
+                                   f"restatement in array-pass mode, as the reference computes"},
         "e2e": {"value": v, "unit": "zone-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -309,10 +357,10 @@ def run_ours(a):
     bytes_per_launch = WORDS[dom] * 4 * n ** 3 / LAUNCHES[dom]
     launch_s = fam_ms[dom] * 1e-3 / LAUNCHES[dom]
     achieved = bytes_per_launch / launch_s / 1e9
-    traffic = None
-    tf = ROOT / "profiles" / "traffic.json"
-    if tf.exists():
-        traffic = json.loads(tf.read_text()).get(dom)
+    traffic, traffic_prov = None, None
+    tdat, traffic_prov = profile_file("traffic.json")
+    if tdat is not None:
+        traffic = tdat.get("per_launch", tdat).get(dom)
     # e2e through the C ABI with host buffers
     e2e = None
     if not a.no_e2e and rank == 0:
@@ -344,6 +392,13 @@ def run_ours(a):
                "split_s": {"init": t1 - t0, "steps": t2 - t1, "fetch": t3 - t2}}
         del out
     solver.close()  # after the e2e run, so that its allocation does not follow a free of the same size
+    study = None
+    if not a.no_study and rank == 0 and ws == 1:
+        # the same workload in all-FP64 mode (the reference's precision) and
+        # the error at equal GPU time (BASELINE's second metric), after the
+        # timed region: FP64 n^3 is the reference solution of the table
+        from mhd3d_mpi_fortran_gb300 import studies
+        study = studies.equal_time(n=n, steps=a.study_steps, recon=a.recon)
     cpu = None
     if not a.no_cpu_baseline and rank == 0 and ws == 1:
         v, dt, cores = cpu_rate(160, 8, a.recon)
@@ -355,18 +410,25 @@ def run_ours(a):
         return
     compute_roofs = roofs(zu / ws, clocks, a.recon, tiles)
     launches_per_step = 2 + 2 * (3 + 3 + 1 + 1)
+    fp64 = None
+    if study:
+        ref = study["runs"][0]
+        fp64 = {"value": n ** 3 * ref["steps"] / (ref["gpu_ms"] * 1e-3), "unit": "zone-updates/s",
+                "ms_per_step": ref["gpu_ms"] / ref["steps"], "steps": ref["steps"],
+                "how": "the same workload in all-FP64 mode (FP64 state, fluxes and reconstructions; the "
+                       "reference's precision), CUDA events around graph replays"}
     line = {
         "metric": "zone-updates/s", "value": zu, "unit": "zone-updates/s", "n_gpus": ws,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded Gaussian-random solenoidal turbulence, k^-2 on 2<=k<=8, 256^3 periodic",
-        "config": {"workload": f"{n}^3 periodic decaying MHD turbulence, PDM + RK2, FP32 state/fluxes, "
-                               f"FP64 metric and sums", "grid": [n, n, n], "recon": a.recon, "stepper": "RK2",
-                   "graph": graph, "tiles": {"face_tile_len": tiles[0], "ei_emf_tile": tiles[1]},
-                   "l2": "inputs larger than L2 (FP32 state ~0.9 GB), no flush",
+        "config": bench_config(n, a.recon),
+        "launch": {"precision": "FP32 state/fluxes, FP64 metric and sums", "graph": graph,
+                   "tiles": {"face_tile_len": tiles[0], "ei_emf_tile": tiles[1]},
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind},
+                     "frac": achieved / hbm, "traffic": traffic, "traffic_provenance": traffic_prov,
+                     "peak_kind": peak_kind},
         "hbm_roofline_160B": {"achieved_gbs": zu * 160 / 1e9 / ws, "peak": hbm, "frac": zu * 160 / 1e9 / ws / hbm,
                               "note": "compulsory 160 B per FP32 RK2 zone-update"},
         "family_ms_per_stage": fam_ms,
@@ -375,6 +437,8 @@ def run_ours(a):
         "clocks": clocks,
         "status": st,
         "e2e": e2e,
+        "fp64": fp64,
+        "equal_time": study,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)

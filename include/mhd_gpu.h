@@ -113,15 +113,21 @@ int mhd_init_mapped(const mhd_params* prm,
                     const double* p, const double* phi_i, const double* phi_j, const double* phi_k,
                     const double* xn, const double* yn, const double* zn, void** handle);
 
-/* One time step (replaces `call step`, mhd3d3.f90:3286).  On return *tau_out
- * (if non-NULL) holds the dt the step used (the module `tau` after the step)
- * and *status (if non-NULL) the MHD_ST_* bits of the checks made during it.
- * Synchronous with respect to the handle's stream when either pointer is
- * non-NULL. */
-int mhd_step(void* handle, double* tau_out, uint32_t* status);
+/* One time step (replaces `call step`, mhd3d3.f90:3286).  tau_inout is the
+ * driver's module `tau` (may be NULL).  On entry: an RK step with the
+ * reference dt mode takes the fixed deck dt (tau = tau0, mhd3d3.f90:3656-3661),
+ * and a positive *tau_inout that differs from the handle's fixed dt becomes
+ * that fixed dt before the step (as mhd_set_tau, in stream order); AB steps
+ * and MHD_DT_CFL take the CFL dt (get_dt) and ignore the input, as the
+ * reference overwrites tau there.  On return *tau_inout holds the dt the step
+ * used (the module `tau` after the step) and *status (if non-NULL) the
+ * MHD_ST_* bits of the checks made during it.  Synchronous with respect to
+ * the handle's stream when either pointer is non-NULL. */
+int mhd_step(void* handle, double* tau_inout, uint32_t* status);
 
 /* n steps back to back without host synchronisation in between (the driver's
- * inner `do nt=1,nts` loop, mhd3d3.f90:3284-3288).  status accumulates. */
+ * inner `do nt=1,nts` loop, mhd3d3.f90:3284-3288).  status accumulates;
+ * tau_out is output only (the dt of the last step). */
 int mhd_step_n(void* handle, int32_t nsteps, double* tau_out, uint32_t* status);
 
 /* Copy the current state back into ghost-inclusive FP64 Fortran arrays.  Any
@@ -206,8 +212,11 @@ int mhd_debug_emf(void* handle, double* ei, double* ej, double* ek);
  * diagnostics: a driver whose device memory is all owned by its own pool, a
  * latency-critical loop that must not take the implicit device
  * synchronisation of cudaMalloc/cudaFree, or a process capped by MPS/MIG
- * limits.  Same five outputs as mhd_diagnostics, computed from arrays the
- * caller already holds on the device; the call allocates nothing.
+ * limits.  Same five outputs as mhd_diagnostics on a Cartesian grid (cell
+ * widths dx, dy, dz), computed from arrays the caller already holds on the
+ * device; the call allocates nothing.  Curvilinear (mhd_init_mapped) grids
+ * are not covered: their diagnostics use cell volumes and face areas, so use
+ * mhd_diagnostics there.
  *
  * All array arguments are DEVICE pointers to FP64, ghost-inclusive, Fortran-
  * ordered arrays of the layout mhd_init takes from the host (cell arrays
@@ -222,7 +231,12 @@ int mhd_debug_emf(void* handle, double* ei, double* ej, double* ek);
  * that array, so calls whose kernels overlap on the GPU (different streams,
  * or other host threads, on the same device) race: order them on one stream.
  * The first call on each device looks up the array's device address with
- * that device current; make that first call before any stream capture. */
+ * that device current; make that first call before any stream capture.  The
+ * address is cached for the life of the process: after a cudaDeviceReset of
+ * a device, do not call this entry point on it again.
+ * Errors: a CUDA error already pending from the caller's own work is
+ * reported as MHD_E_CUDA and left pending (cudaPeekAtLastError); a failed
+ * launch of this call is reported as MHD_E_CUDA and cleared. */
 int mhd_diagnostics_noalloc(const mhd_params* prm, const double* rho, const double* vx,
                             const double* vy, const double* vz, const double* p,
                             const double* bi, const double* bj, const double* bk,

@@ -870,8 +870,26 @@ int mhd_step_n(void* handle, int32_t nsteps, double* tau_out, uint32_t* status) 
   return finish(h, tau_out, status);
 }
 
-int mhd_step(void* handle, double* tau_out, uint32_t* status) {
-  return mhd_step_n(handle, 1, tau_out, status);
+// Sets the fixed RK dt (Scal::tau, Scal::tau0) in stream order, without a host wait.
+__global__ void k_set_tau(Scal* sc, double tau) {
+  sc->tau = tau;
+  sc->tau0 = tau;
+}
+
+int mhd_step(void* handle, double* tau_inout, uint32_t* status) {
+  Handle* h = (Handle*)handle;
+  if (!h) return fail(MHD_E_ARG, "null handle");
+  // tau in: the driver's module tau.  RK steps with the reference dt take the
+  // fixed deck dt tau0 (step_rk2/3, mhd3d3.f90:3656-3661); a positive value
+  // that differs from it becomes the new fixed dt before the step.  AB steps
+  // and the CFL dt mode compute their dt on the device (get_dt) and ignore it.
+  if (tau_inout && *tau_inout > 0.0 && std::isfinite(*tau_inout) && h->prm.stepop != MHD_STEP_AB2 &&
+      h->prm.dt_mode == MHD_DT_REFERENCE && *tau_inout != h->prm.tau) {
+    k_set_tau<<<1, 1, 0, h->st>>>(h->sc, *tau_inout);
+    CK(cudaGetLastError());
+    h->prm.tau = *tau_inout;
+  }
+  return mhd_step_n(handle, 1, tau_inout, status);
 }
 
 static int graph_for(Handle* h, int nsteps, cudaGraphExec_t* out);

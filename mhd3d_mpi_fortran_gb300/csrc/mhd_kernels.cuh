@@ -1161,12 +1161,16 @@ __global__ void __launch_bounds__(128, kSweepMinB)
   T (*zs)[18][32] = szf[threadIdx.y];
   T w[8][8], nx[8], Fp[8];
   // window of the first face (cell c0): cells c0-4 .. c0+3; the loop shifts
-  // one cell in per face, so w[v][1..7] start as cells c0-4 .. c0+2
+  // one cell in per face, so w[v][1..7] start as cells c0-4 .. c0+2.  Window
+  // cells are clamped to the ghost-inclusive range [0, nD-1]: with fewer than
+  // 4 ghost layers (nord 4 or 6: TVD, WENO) the outermost taps lie outside
+  // it, and those taps are exactly the ones such a stencil never reads.
+  const int nD = (D == 1) ? g.ny : g.nz;
 #pragma unroll
   for (int v = 0; v < 8; ++v) {
 #pragma unroll
-    for (int m = 1; m < 8; ++m) w[v][m] = src[v][col + (c0 - 5 + m) * s];
-    nx[v] = src[v][col + (c0 + 3) * s];
+    for (int m = 1; m < 8; ++m) w[v][m] = src[v][col + max(c0 - 5 + m, 0) * s];
+    nx[v] = src[v][col + min(c0 + 3, nD - 1) * s];
   }
   T dx = T(0), rdx = T(0);
   if (D == 1) {
@@ -1183,7 +1187,7 @@ __global__ void __launch_bounds__(128, kSweepMinB)
     }
     if (cd < c1) {
 #pragma unroll
-      for (int v = 0; v < 8; ++v) nx[v] = src[v][col + (cd + 4) * s];
+      for (int v = 0; v < 8; ++v) nx[v] = src[v][col + min(cd + 4, nD - 1) * s];
     }
     if (D == 1) {
       __syncwarp();  // every lane is done reading the slot refilled here

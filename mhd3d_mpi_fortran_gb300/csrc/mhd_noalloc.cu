@@ -140,7 +140,9 @@ int fail_na(int code, const std::string& m) {
 }
 
 // Device address of the scratch array, looked up once per device with that
-// device current (cudaGetSymbolAddress), then cached.
+// device current (cudaGetSymbolAddress), then cached for the life of the
+// process.  A cudaDeviceReset destroys the context the address belongs to,
+// so the cache does not survive one (documented in mhd_gpu.h).
 int scratch_for_current_device(double** out) {
   static std::mutex mu;
   static double* ptr[kMaxDevices] = {};
@@ -178,13 +180,19 @@ int mhd_diagnostics_noalloc(const mhd_params* prm, const double* rho, const doub
     return fail_na(MHD_E_ARG, "grid has " + std::to_string(d.nz) + " z planes (nz0 + nord); the allocation-free "
                    "diagnostics hold at most " + std::to_string(kMaxPlanes));
   if ((long long)d.nx * d.ny >= (1LL << 31)) return fail_na(MHD_E_ARG, "z plane larger than 2^31 cells");
+  // An error the caller's own work left pending is reported, and left pending
+  // for the caller, rather than taken for a failure of these launches.
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess)
+    return fail_na(MHD_E_CUDA, std::string("an earlier CUDA error is pending (left for the caller): ") +
+                                   cudaGetErrorString(e));
   double* scratch = nullptr;
   int rc = scratch_for_current_device(&scratch);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   k_plane<<<d.nz, kThreads, 0, st>>>(d, rho, vx, vy, vz, p, bi, bj, bk, dx, dy, dz, scratch);
   k_final<<<1, 1, 0, st>>>(scratch, d.nz, out);
-  cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   if (e != cudaSuccess) return fail_na(MHD_E_CUDA, std::string("launch: ") + cudaGetErrorString(e));
   return MHD_OK;
 }

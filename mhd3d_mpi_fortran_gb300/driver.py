@@ -46,11 +46,6 @@ class RunStopped(RuntimeError):
 # three of mhd3d2 (its program calls init_ic_otv, mhd3d2.f90:3186-3188).
 ICS = ("tube", "otv", "bws", "imp")
 Z2D = 8  # z planes of a 2-D run: the smallest axis the solver's tests run
-# Ghost depth of a run.  Decks with nord = 6 (mhd3d2.in, WENO) run with 8: the
-# WENO / TVD stencils reach 3 cells, the deeper ghosts are exact copies
-# (periodic, outflow, mirror), and the CFL minimum over them is the same, so
-# the interior and dt are bit-identical (tests/test_driver.py).
-NORD_RUN = 8
 
 
 def ic_grid(deck: dict, nord: int, ic: str = "tube") -> tuple:
@@ -156,8 +151,6 @@ def run(deck, outdir, precision: int = FP64, periodic: bool = False, state: ics.
     nframes = int(lst.get("nframes", 1)) if nframes is None else nframes
     nts = int(lst.get("nts", 1)) if nts is None else nts
     prm = params_from_deck(deck, precision=precision, bc=BC_PERIODIC if periodic else None)
-    if state is None:
-        prm.nord = max(prm.nord, NORD_RUN)
     if ic != "tube" and state is None:
         _, _, nz0, bc = ic_grid(deck, prm.nord, ic)
         prm.nz0, prm.bc = nz0, bc

@@ -37,7 +37,7 @@ module mhd_gpu_binding
       integer(c_int) function mhd_step(h, tau, status) bind(C, name="mhd_step")
          import :: c_int, c_double, c_ptr, c_int32_t
          type(c_ptr), value :: h
-         real(c_double), intent(out) :: tau
+         real(c_double), intent(inout) :: tau
          integer(c_int32_t), intent(out) :: status
       end function mhd_step
 
@@ -56,6 +56,12 @@ module mhd_gpu_binding
          real(c_double), intent(out) :: rho(*), vx(*), vy(*), vz(*), p(*)
          real(c_double), intent(out) :: bx(*), by(*), bz(*), bi(*), bj(*), bk(*)
       end function mhd_fetch
+
+      integer(c_int) function mhd_set_tau(h, tau) bind(C, name="mhd_set_tau")
+         import :: c_int, c_double, c_ptr
+         type(c_ptr), value :: h
+         real(c_double), value :: tau
+      end function mhd_set_tau
 
       integer(c_int) function mhd_free(h) bind(C, name="mhd_free")
          import :: c_int, c_ptr
@@ -91,7 +97,9 @@ contains
       if (rc /= 0) stop 'mhd_init failed'
    end subroutine gpu_init
 
-   !..replaces `call step`: tau comes back as the module tau after the step
+   !..replaces `call step`: tau goes in as the driver's module tau (for RK with
+   !  the deck dt, a changed positive tau becomes the fixed dt tau0) and comes
+   !  back as the module tau after the step (AB: its CFL dt)
    subroutine gpu_step(tau)
       real(c_double), intent(inout) :: tau
       integer(c_int32_t) :: status
@@ -100,6 +108,14 @@ contains
       if (rc /= 0) stop 'mhd_step failed'
       if (iand(status, 3) /= 0) stop 'NaN or negative density (device check)'
    end subroutine gpu_step
+
+   !..sets the fixed RK dt (the module tau0) outright, e.g. after a restart
+   subroutine gpu_set_tau(tau)
+      real(c_double), intent(in) :: tau
+      integer(c_int) :: rc
+      rc = mhd_set_tau(gpu_handle, tau)
+      if (rc /= 0) stop 'mhd_set_tau failed'
+   end subroutine gpu_set_tau
 
    subroutine gpu_fetch(rho, vx, vy, vz, p, bx, by, bz, bi, bj, bk)
       real(c_double), intent(out) :: rho(*), vx(*), vy(*), vz(*), p(*), bx(*), by(*), bz(*)

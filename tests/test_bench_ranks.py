@@ -53,3 +53,20 @@ def test_reference_arm_prints_on_rank_zero_only():
                         "--warmup", "1"], env=env, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0
     assert r.stdout.strip() == ""
+
+
+def test_reference_arm_runs_the_same_config_as_ours():
+    """The reference arm times the oracle (array passes) on the same workload
+    description as our arm: identical config dicts, so the two lines compare
+    like for like."""
+    import json
+    import bench
+    env = dict(os.environ, WORLD_SIZE="1", RANK="0", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--n", "12", "--steps", "2",
+                        "--warmup", "1"], env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["steps"] == 2
+    assert line["config"] == bench.bench_config(12, 1)
+    assert line["e2e"]["value"] == line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port"

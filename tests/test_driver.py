@@ -121,10 +121,10 @@ def test_deck_run_writes_every_frame(tmp_path):
 
 
 @pytest.mark.parametrize("recon,stepop,bc", [(4, 3, "2d"), (3, 1, "walls"), (5, 2, "2d")])
-def test_nord6_decks_run_bit_identically_at_nord8(recon, stepop, bc):
-    """The driver runs nord = 6 decks with 8 ghost cells: the interior and the
-    time steps are bit-identical (WENO / TVD stencils reach 3 cells; deeper
-    ghosts are exact copies)."""
+def test_nord6_and_nord8_give_the_same_interior(recon, stepop, bc):
+    """Oracle property: WENO / TVD stencils reach 3 cells, so a 4th ghost layer
+    (an exact copy: periodic, outflow, mirror) changes neither the interior
+    nor the time steps, bit for bit."""
     from mhd3d_mpi_fortran_gb300.abi import BC_EVEN, BC_OUTFLOW, BC_PERIODIC, Params
     from oracle.oracle import OracleSolver
     bcs = (BC_PERIODIC, BC_PERIODIC, BC_OUTFLOW) if bc == "2d" else (BC_EVEN,) * 3
@@ -143,9 +143,9 @@ def test_nord6_decks_run_bit_identically_at_nord8(recon, stepop, bc):
 
 @pytest.mark.gpu
 def test_mhd3d2_otv_deck_runs_on_the_gpu(tmp_path):
-    """mhd3d2.in's scheme (MP-WENO5, RK3; its nord 6 run as 8) from init_ic_otv
-    on the lifted 2-D grid, through the driver loop: the last frame matches the
-    oracle's FP64 run, and every z plane of it is the same."""
+    """mhd3d2.in's scheme (MP-WENO5, RK3) at its own ghost depth (nord 6) from
+    init_ic_otv on the lifted 2-D grid, through the driver loop: the last frame
+    matches the oracle's FP64 run, and every z plane of it is the same."""
     from mhd3d_mpi_fortran_gb300.deck import params_from_deck
     from oracle.oracle import OracleSolver
     deck = driver.read_deck(DECK2)
@@ -154,13 +154,13 @@ def test_mhd3d2_otv_deck_runs_on_the_gpu(tmp_path):
     fr = driver.read_frames(tmp_path)
     assert fr["rho"].shape == (3, 8, 16, 16)
     prm = params_from_deck(deck)
-    prm.nord = driver.NORD_RUN
+    assert prm.nord == 6
     _, _, prm.nz0, prm.bc = driver.ic_grid(deck, prm.nord, "otv")
     o = OracleSolver(prm, driver.initial_state(deck, prm.nord, "otv"))
     o.step(6)
     ref = o.fetch()
     for v in ("rho", "vx", "vy", "p", "bx", "by"):
-        want = ref[v][4:-4, 4:-4, 4:-4].transpose(2, 1, 0)
+        want = ref[v][3:-3, 3:-3, 3:-3].transpose(2, 1, 0)
         got = fr[v][2]
         assert np.abs(got - want).max() <= 1e-11 * np.abs(want).max(), v
         for z in range(1, got.shape[0]):

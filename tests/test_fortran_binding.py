@@ -142,7 +142,8 @@ def test_every_interface_names_a_declared_entry_point():
         assert cname in protos, cname
 
 
-@pytest.mark.parametrize("name", ["mhd_init", "mhd_step", "mhd_step_n", "mhd_fetch", "mhd_free", "mhd_diagnostics"])
+@pytest.mark.parametrize("name", ["mhd_init", "mhd_step", "mhd_step_n", "mhd_fetch", "mhd_free", "mhd_diagnostics",
+                                  "mhd_set_tau"])
 def test_interface_arguments_match_the_prototype(name):
     _, fargs = f90_interfaces()[name]
     assert fargs == c_prototypes()[name], (name, fargs, c_prototypes()[name])
@@ -154,3 +155,17 @@ def test_step_stop_mask_is_nan_or_negative_density():
     bits = {m.group(1): int(m.group(2)) for m in re.finditer(r"(MHD_ST_\w+)\s*=\s*1u\s*<<\s*(\d+)", HEADER)}
     mask = int(re.search(r"iand\(status, (\d+)\)", F90).group(1))
     assert mask == (1 << bits["MHD_ST_NAN"]) | (1 << bits["MHD_ST_NEG_RHO"])
+
+
+def test_step_passes_tau_both_ways():
+    """mhd_step's tau is in/out (the driver's module tau, mhd3d3.f90:3285-3286):
+    the interface declares it intent(inout), and gpu_step hands the driver's
+    own variable through unchanged."""
+    lines = _f90_lines(F90)
+    i = lines.index('integer(c_int) function mhd_step(h, tau, status) bind(C, name="mhd_step")')
+    decl = next(x for x in lines[i:] if x.startswith("real(c_double)"))
+    assert "intent(inout)" in decl and decl.endswith(":: tau")
+    j = lines.index("subroutine gpu_step(tau)")
+    assert lines[j + 1] == "real(c_double), intent(inout) :: tau"
+    assert "rc = mhd_step(gpu_handle, tau, status)" in lines[j:j + 8]
+    assert "subroutine gpu_set_tau(tau)" in lines

@@ -502,3 +502,37 @@ def test_fetch_fills_caller_arrays_in_place():
     assert b is dst
     for k in FIELDS:
         assert np.array_equal(a[k], dst[k]), k
+
+
+def test_step_tau_inout_sets_the_fixed_rk_dt():
+    """mhd_step reads the driver's tau: for RK with the deck dt a changed
+    positive tau becomes the fixed dt before the step (bit-identical to
+    mhd_set_tau then mhd_step), an unchanged one is a no-op; AB2 takes its CFL
+    dt and ignores the input, as step_ab overwrites tau (mhd3d3.f90:3609)."""
+    s = ics.orszag_tang_3d(12, seed=3)
+    t0 = 0.4 * ics.cfl_dt(s)
+    t1 = 0.7 * t0
+    prm = Params(12, 12, 12, tau=t0)
+    with MHDSolver(prm, s) as a, MHDSolver(prm, s) as b:
+        lib = a.lib
+        tau, st = C.c_double(t0), C.c_uint32()
+        for _ in range(2):
+            assert lib.mhd_step(a.h, C.byref(tau), C.byref(st)) == E_OK
+            assert tau.value == t0
+        tau.value = t1
+        assert lib.mhd_step(a.h, C.byref(tau), C.byref(st)) == E_OK
+        assert tau.value == t1
+        assert lib.mhd_step(a.h, C.byref(tau), C.byref(st)) == E_OK
+        assert tau.value == t1
+        b.step(2)
+        b.set_tau(t1)
+        b.step(2)
+        fa, fb = a.fetch(), b.fetch()
+    for k in FIELDS:
+        assert np.array_equal(fa[k], fb[k]), k
+    pab = Params(12, 12, 12, stepop=STEP_AB2, tau=3e-4)
+    with MHDSolver(pab, s) as a, MHDSolver(pab, s) as b:
+        tau = C.c_double(123.0)
+        assert a.lib.mhd_step(a.h, C.byref(tau), None) == E_OK
+        tb, _ = b.step(1)
+        assert tau.value == tb and tau.value < 1.0
