@@ -125,7 +125,9 @@ Inp<T> half_inp(const Dev<T>& d) {
 // Launch-family recorder: in profile mode every family is bracketed by a pair
 // of CUDA events on the stream (no synchronisation); pairs are resolved after
 // the call.  Families: 0 x fluxes, 1 y fluxes (+x divergence), 2 z fluxes +
-// conserved update, 3 emf, 4 ct (face B), 5 fill+bxyz, 6 dt/save/predict.
+// conserved update, 3 emf, 4 ct (face B) with the fill + bxyz that follows it
+// (one fused family since both run in Launch::ct_fill), 5 unused, 6
+// dt/save/predict.
 struct Rec {
   Handle* h = nullptr;
   cudaStream_t st = nullptr;
@@ -159,15 +161,7 @@ Dev<double>& dev<double>(Handle* h) { return h->dd; }
 // The handle's Dev with the current half of the primitive buffers in front.
 template <typename T>
 Dev<T> at_par(const Dev<T>& base, int par) {
-  Dev<T> d = base;
-  if (par) {
-    std::swap(d.rho, d.orho);
-    std::swap(d.vx, d.ovx);
-    std::swap(d.vy, d.ovy);
-    std::swap(d.vz, d.ovz);
-    std::swap(d.p, d.op);
-  }
-  return d;
+  return par ? other_half(base) : base;
 }
 
 // The EMF families and the face-flux kernels of a stage read the same stage
@@ -208,10 +202,8 @@ void enqueue_step(Handle* h, int& par, cudaStream_t st, Rec* r = nullptr) {
     R.begin(); L::cfl(d, 2, st); L::predictor_ab(d, st); R.end(6);
     Inp<T> in = half_inp(d);
     emf_and_fluxes<T, M>(h, d, in, -1, 0.0, 1.0, true, st, R);
-    R.begin(); L::ct(d, -1, 0.0, 1.0, st); R.end(4);
+    R.begin(); L::ct_fill(d, -1, 0.0, 1.0, false, st); R.end(4);
     par ^= 1;
-    d = at_par(base, par);
-    R.begin(); L::fill_bxyz(d, false, st); R.end(5);
     return;
   }
   {
@@ -232,10 +224,8 @@ void enqueue_step(Handle* h, int& par, cudaStream_t st, Rec* r = nullptr) {
     Dev<T> d = at_par(base, par);
     Inp<T> in = state_inp(d);
     emf_and_fluxes<T, M>(h, d, in, form, c, den, false, st, R);
-    R.begin(); L::ct(d, form, c, den, st); R.end(4);
+    R.begin(); L::ct_fill(d, form, c, den, true, st); R.end(4);
     par ^= 1;
-    d = at_par(base, par);
-    R.begin(); L::fill_bxyz(d, true, st); R.end(5);
   }
 }
 
@@ -274,6 +264,7 @@ void carve(Handle* h, Dev<T>& d, char* base) {
   d.rho = next(); d.vx = next(); d.vy = next(); d.vz = next(); d.p = next();
   d.bi = next(); d.bj = next(); d.bk = next(); d.bx = next(); d.by = next(); d.bz = next();
   d.orho = next(); d.ovx = next(); d.ovy = next(); d.ovz = next(); d.op = next();
+  d.obi = next(); d.obj = next(); d.obk = next();
   for (int q = 0; q < 8; ++q) d.dU[q] = next();
   int nq = (h->prm.stepop == MHD_STEP_AB2) ? 11 : 8;
   for (int i = 0; i < 11; ++i) d.q[i] = (i < nq) ? next() : nullptr;
@@ -338,7 +329,7 @@ MetricOut metric_out(Handle* h) {
 }
 
 size_t n_arrays(const mhd_params& p, bool metric) {
-  size_t n = 11 + 5 + 8 + ((p.stepop == MHD_STEP_AB2) ? 22 : 8) + 24 + 3 + 1 + (metric ? 6 : 0) +
+  size_t n = 11 + 5 + 3 + 8 + ((p.stepop == MHD_STEP_AB2) ? 22 : 8) + 24 + 3 + 1 + (metric ? 6 : 0) +
              ((p.emf == MHD_EMF_YEE) ? 12 : 0);
   return n;
 }

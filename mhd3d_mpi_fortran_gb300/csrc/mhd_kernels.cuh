@@ -1729,7 +1729,8 @@ __global__ void k_metric_prep(Dev<T> d, Inp<T> in) {
 }
 
 // ------------------------------------------------------------------ update
-// advance_bijk (3909-3933) + B combine, interior faces of all three arrays.
+// advance_bijk (3909-3933) + B combine, interior faces of all three arrays,
+// read from the stage's half of the face B and written to the other half.
 template <typename T, bool M, bool B>
 __global__ void k_update_b(KArg<T, B> ka, int form, T cw, T den) {
   const int4 bb = ka.blk();
@@ -1751,34 +1752,34 @@ __global__ void k_update_b(KArg<T, B> ka, int form, T cw, T den) {
     if (in_y && in_z) {
       T b = d.bi[c] - tau * ((ek[c + sy] - ek[c]) - (ej[c + sz] - ej[c]));
       if (form >= 0) b = comb(form, cw, d.q[5][c], b, den);
-      d.bi[c] = b;
+      d.obi[c] = b;
     }
     if (in_x && in_z) {
       T b = d.bj[c] - tau * ((ei[c + sz] - ei[c]) - (ek[c + 1] - ek[c]));
       if (form >= 0) b = comb(form, cw, d.q[6][c], b, den);
-      d.bj[c] = b;
+      d.obj[c] = b;
     }
     if (in_x && in_y) {
       T b = d.bk[c] - tau * ((ej[c + 1] - ej[c]) - (ei[c + sy] - ei[c]));
       if (form >= 0) b = comb(form, cw, d.q[7][c], b, den);
-      d.bk[c] = b;
+      d.obk[c] = b;
     }
     return;
   }
   if (in_y && in_z) {
     T b = d.bi[c] - tau * (O::dw(ek[c + sy] - ek[c], dy, ry) - O::dw(ej[c + sz] - ej[c], dz, rz));
     if (form >= 0) b = comb(form, cw, d.q[5][c], b, den);
-    d.bi[c] = b;
+    d.obi[c] = b;
   }
   if (in_x && in_z) {
     T b = d.bj[c] - tau * (O::dw(ei[c + sz] - ei[c], dz, rz) - O::dw(ek[c + 1] - ek[c], dx, rx));
     if (form >= 0) b = comb(form, cw, d.q[6][c], b, den);
-    d.bj[c] = b;
+    d.obj[c] = b;
   }
   if (in_x && in_y) {
     T b = d.bk[c] - tau * (O::dw(ej[c + 1] - ej[c], dx, rx) - O::dw(ei[c + sy] - ei[c], dy, ry));
     if (form >= 0) b = comb(form, cw, d.q[7][c], b, den);
-    d.bk[c] = b;
+    d.obk[c] = b;
   }
 }
 
@@ -1889,23 +1890,26 @@ __device__ __forceinline__ void fill_shell_ijk(const Geom& g, int u, int& i, int
   i = ii < g.ng ? ii : ii + g.nx0;
 }
 
+// shell_only != 0: the launch covers only the shell blocks (block b is shell
+// block b), after k_ct_fill has done the interior.
 template <typename T, bool M, bool B>
-__global__ void __launch_bounds__(256) k_fill_bxyz(KArg<T, B> ka, int want_vf) {
+__global__ void __launch_bounds__(256) k_fill_bxyz(KArg<T, B> ka, int want_vf, int shell_only) {
   const int4 bb = ka.blk();
   const auto& d = ka.dev(bb);
   const Geom& g = d.g;
   const FillShape fs(g);
+  const int blk = shell_only ? bb.y + fs.nint : bb.y;
   int i, j, k;
   bool inner;
-  if (bb.y < fs.nint) {
-    const int bx = bb.y % fs.nbx, r = bb.y / fs.nbx, by = r % fs.nby, kz = r / fs.nby;
+  if (blk < fs.nint) {
+    const int bx = blk % fs.nbx, r = blk / fs.nbx, by = r % fs.nby, kz = r / fs.nby;
     i = g.ng + bx * 32 + (threadIdx.x & 31);
     j = g.ng + by * 8 + (threadIdx.x >> 5);
     k = g.ng + kz;
     if (i >= g.ng + g.nx0 || j >= g.ng + g.ny0) return;  // those cells belong to no block here
     inner = true;
   } else {
-    const int u = (bb.y - fs.nint) * 256 + threadIdx.x;
+    const int u = (blk - fs.nint) * 256 + threadIdx.x;
     if (u >= fs.nshell) return;
     fill_shell_ijk(g, u, i, j, k);
     inner = false;
@@ -1973,6 +1977,69 @@ __global__ void __launch_bounds__(256) k_fill_bxyz(KArg<T, B> ka, int want_vf) {
     const int s = sci + cyz;
     const T u = d.vx[s], v = d.vy[s], w = d.vz[s];
     d.vf[c] = sq(u * u + v * v + w * w) + sq((bx * bx + by * by + bz * bz) / d.rho[s]);
+  }
+}
+
+// CT fused with get_bxyz and vf on Cartesian meshes (advance_bijk + combine,
+// mhd3d3.f90:3909-3933, 3698-3702, 3784-3788; get_bxyz 2118-2128; vf of
+// get_eijk_LFM 1766): one thread per interior cell, blocks of 32 x 8 cells of
+// one z plane (the fill's interior tiles).  The thread advances its cell's
+// three low faces into the new half of the face B with k_update_b's
+// expressions and recomputes the new values of its three high faces from the
+// same inputs (the cell that owns such a face writes it; the last cell of an
+// axis writes the boundary face), then forms the cell-centred B from the six
+// new faces and vf from the new primitives, which the z sweep wrote into the
+// new half.  Every input here is read-only (old half of the face B, EMFs,
+// U^n, new primitives), so a recomputed face equals what its owner writes,
+// bit for bit, and the result equals k_update_b followed by the fill's
+// interior tiles.  The ghost shell of the new half follows in k_fill_bxyz
+// (shell_only).
+template <typename T, bool B>
+__global__ void __launch_bounds__(256) k_ct_fill(KArg<T, B> ka, int form, T cw, T den, int want_vf) {
+  const int4 bb = ka.blk();
+  const auto& d = ka.dev(bb);
+  const Geom& g = d.g;
+  const int i = g.ng + bb.y * 32 + (threadIdx.x & 31);
+  const int j = g.ng + bb.z * 8 + (threadIdx.x >> 5);
+  const int k = g.ng + bb.w;
+  if (i >= g.ng + g.nx0 || j >= g.ng + g.ny0) return;
+  const int px = g.px, pl = (int)g.plane;
+  const int c = i + px * j + pl * k;
+  const T tau = (T)d.sc->tau;
+  const T dx = d.wx[i], dy = d.wy[j], dz = d.wz[k];
+  const T rx = d.rwx[i], ry = d.rwy[j], rz = d.rwz[k];
+  const T *ei = d.E[0], *ej = d.E[1], *ek = d.E[2];
+  typedef Ops<T> O;
+  auto new_bi = [&](int f) {
+    T b = d.bi[f] - tau * (O::dw(ek[f + px] - ek[f], dy, ry) - O::dw(ej[f + pl] - ej[f], dz, rz));
+    return form >= 0 ? comb(form, cw, d.q[5][f], b, den) : b;
+  };
+  auto new_bj = [&](int f) {
+    T b = d.bj[f] - tau * (O::dw(ei[f + pl] - ei[f], dz, rz) - O::dw(ek[f + 1] - ek[f], dx, rx));
+    return form >= 0 ? comb(form, cw, d.q[6][f], b, den) : b;
+  };
+  auto new_bk = [&](int f) {
+    T b = d.bk[f] - tau * (O::dw(ej[f + 1] - ej[f], dx, rx) - O::dw(ei[f + px] - ei[f], dy, ry));
+    return form >= 0 ? comb(form, cw, d.q[7][f], b, den) : b;
+  };
+  const T bil = new_bi(c), bih = new_bi(c + 1);
+  const T bjl = new_bj(c), bjh = new_bj(c + px);
+  const T bkl = new_bk(c), bkh = new_bk(c + pl);
+  d.obi[c] = bil;
+  d.obj[c] = bjl;
+  d.obk[c] = bkl;
+  if (i == g.ng + g.nx0 - 1) d.obi[c + 1] = bih;
+  if (j == g.ng + g.ny0 - 1) d.obj[c + px] = bjh;
+  if (k == g.ng + g.nz0 - 1) d.obk[c + pl] = bkh;
+  const T bx = T(0.5) * (bih + bil);
+  const T by = T(0.5) * (bjh + bjl);
+  const T bz = T(0.5) * (bkh + bkl);
+  d.bx[c] = bx;
+  d.by[c] = by;
+  d.bz[c] = bz;
+  if (want_vf) {
+    const T u = d.ovx[c], v = d.ovy[c], w = d.ovz[c];
+    d.vf[c] = sq(u * u + v * v + w * w) + sq((bx * bx + by * by + bz * bz) / d.orho[c]);
   }
 }
 
@@ -2108,7 +2175,20 @@ void Launch<T, M>::bxyz_vf(const Dev<T>& d, bool want_vf, cudaStream_t st) {
 
 template <typename T, bool M>
 void Launch<T, M>::fill_bxyz(const Dev<T>& d, bool want_vf, cudaStream_t st) {
-  k_fill_bxyz<T, M, false><<<FillShape(d.g).blocks(), 256, 0, st>>>(one(d), want_vf ? 1 : 0);
+  k_fill_bxyz<T, M, false><<<FillShape(d.g).blocks(), 256, 0, st>>>(one(d), want_vf ? 1 : 0, 0);
+}
+
+template <typename T, bool M>
+void Launch<T, M>::ct_fill(const Dev<T>& d, int form, double c, double den, bool want_vf, cudaStream_t st) {
+  if constexpr (M) {  // metric mode: CT, then the fill + bxyz pass of the new half
+    ct(d, form, c, den, st);
+    fill_bxyz(other_half(d), want_vf, st);
+  } else {
+    const FillShape fs(d.g);
+    k_ct_fill<T, false><<<dim3(fs.nbx, fs.nby, d.g.nz0), 256, 0, st>>>(one(d), form, (T)c, (T)den,
+                                                                        want_vf ? 1 : 0);
+    k_fill_bxyz<T, false, false><<<(fs.nshell + 255) / 256, 256, 0, st>>>(one(other_half(d)), want_vf ? 1 : 0, 1);
+  }
 }
 
 template <typename T, bool M>
@@ -2422,8 +2502,11 @@ dim3 Batch<T>::dims(int fam, const Geom& g, int td, int ey) {
     case BF_EMF_I: return emf_grid(0, g, ei_x(Y), Y, Y);
     case BF_EMF_J: return emf_grid(1, g, 32, 1, kPT);
     case BF_EMF_K: return emf_grid(2, g, 32, kPT, 1);
-    case BF_CT: return grid3(g.nx0 + 1, g.ny0 + 1, g.nz0 + 1, dim3(32, 4, 1));
-    default: return dim3(FillShape(g).blocks(), 1, 1);  // BF_FILL
+    case BF_CT: {  // k_ct_fill: the fill's interior tiles
+      const FillShape fs(g);
+      return dim3(fs.nbx, fs.nby, g.nz0);
+    }
+    default: return dim3((FillShape(g).nshell + 255) / 256, 1, 1);  // BF_FILL: the shell of the new half
   }
 }
 
@@ -2505,11 +2588,10 @@ void Batch<T>::parts(const BatchView& v, int sel, int which, int form, double c,
     else if (F32 && v.tile_td == 16) batch_flux_t<T, F32 ? 16 : TD>(v, tab, P, form, (T)c, (T)den, st);
     else batch_flux_t<T, TD>(v, tab, P, form, (T)c, (T)den, st);
   }
-  if (which & 4) {  // face-B update, then fill + bxyz + vf of the half the stage wrote
-    k_update_b<T, false, true><<<v.nblk[BF_CT], dim3(32, 4), 0, st>>>(KArg<T, true>{tab, v.map[BF_CT]}, form, (T)c,
-                                                                       (T)den);
+  if (which & 4) {  // face-B update + bxyz + vf (interior), then the ghost shell of the half the stage wrote
+    k_ct_fill<T, true><<<v.nblk[BF_CT], 256, 0, st>>>(KArg<T, true>{tab, v.map[BF_CT]}, form, (T)c, (T)den, 1);
     KArg<T, true> fa{(const Dev<T>*)v.tab[sel ^ 1], v.map[BF_FILL]};
-    k_fill_bxyz<T, false, true><<<v.nblk[BF_FILL], 256, 0, st>>>(fa, 1);
+    k_fill_bxyz<T, false, true><<<v.nblk[BF_FILL], 256, 0, st>>>(fa, 1, 1);
   }
 }
 

@@ -74,10 +74,13 @@ struct Dev {
   int recon, stepop, tvd_shift, dt_mode;
   int bc[3];
   T gam, pdmb, eps, alpha, beta, cfl;
-  // state of the current level; the cell primitives are double-buffered:
-  // the z-flux kernel writes the new level into o* (swapped after each stage)
+  // state of the current level; the cell primitives and the face B are
+  // double-buffered: the z-flux kernel writes the new primitives into o*, the
+  // CT kernel the new face B into ob* (swapped after each stage), so no kernel
+  // reads an element another thread of it is updating
   T *rho, *vx, *vy, *vz, *p, *bi, *bj, *bk, *bx, *by, *bz;
   T *orho, *ovx, *ovy, *ovz, *op;
+  T *obi, *obj, *obk;
   T* dU[8];    // x+y flux divergence per cell {rho, rvx, rvy, rvz, eng, s_x, s_y, s_z}
   // previous level: RK {rho, rvx, rvy, rvz, eng, bi, bj, bk};
   //                 AB {rho, vx, vy, vz, p, bi, bj, bk, bx, by, bz}
@@ -106,6 +109,21 @@ struct Dev {
   T* ye[12];         // Yee split electric fields, [x, y, z edges][pp, np, pn, nn] (emf = 1)
 };
 
+// The same handle with the two halves of its double-buffered arrays exchanged.
+template <typename T>
+inline Dev<T> other_half(Dev<T> d) {
+  T* t;
+  t = d.rho; d.rho = d.orho; d.orho = t;
+  t = d.vx; d.vx = d.ovx; d.ovx = t;
+  t = d.vy; d.vy = d.ovy; d.ovy = t;
+  t = d.vz; d.vz = d.ovz; d.ovz = t;
+  t = d.p; d.p = d.op; d.op = t;
+  t = d.bi; d.bi = d.obi; d.obi = t;
+  t = d.bj; d.bj = d.obj; d.obj = t;
+  t = d.bk; d.bk = d.obk; d.obk = t;
+  return d;
+}
+
 // Stage-input view: which arrays feed the EMF and flux kernels (RK: the
 // state; AB: the predicted half step, mhd3d3.f90:3622-3624).
 template <typename T>
@@ -133,8 +151,11 @@ struct Launch {
   // form: -1 none (stage 1 / AB), 0 (Xp+X)/den, 1 (c*Xp+X)/den, 2 (Xp+c*X)/den
   static void hydro(const Dev<T>& d, const Inp<T>& in, int part, int form, double c, double den, bool ab,
                     cudaStream_t st);
-  // constrained-transport face-B update + combine
+  // constrained-transport face-B update + combine (into the other half)
   static void ct(const Dev<T>& d, int form, double c, double den, cudaStream_t st);
+  // Cartesian: CT + get_bxyz + vf over the interior cells in one pass, then
+  // the ghost fill of the new half (d is the stage's view, as for ct)
+  static void ct_fill(const Dev<T>& d, int form, double c, double den, bool want_vf, cudaStream_t st);
   static void fill(const Dev<T>& d, cudaStream_t st);
   static void diagnostics(const Dev<T>& d, double* out5_dev, cudaStream_t st);
 };

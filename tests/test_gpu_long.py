@@ -150,7 +150,8 @@ def test_fp32_budget_on_the_bench_workload_128cubed():
     turbulence, E(k) ~ k^-2 on 2 <= k <= 8, PDM + RK2, the bench's dt = 0.8 x
     the initial CFL-0.3 dt) at 128^3 over 100 steps, against the all-FP64 mode
     on the same inputs: relative L1 <= 1e-5 per field, FP32 div B at FP32
-    round-off, and mass conserved to FP32 round-off."""
+    round-off of the face field (max |div B| dx / max |B| <= 1e-5), and mass
+    conserved to FP32 round-off."""
     s = ics.turbulence(128, seed=0)
     tau = 0.8 * ics.cfl_dt(s, cfl=0.3)
     out, diag = {}, {}
@@ -166,7 +167,9 @@ def test_fp32_budget_on_the_bench_workload_128cubed():
         l1 = np.abs(a - b).sum() / np.abs(b).sum()
         assert l1 <= 1e-5, (k, l1)
     d0, d1 = diag[FP32]
-    assert d1["divb_max"] <= 1e-4
+    # max |div B| in units of max|B| / dx: a few FP32 ulps of the face field
+    bmax = max(np.abs(out[FP32][k]).max() for k in ("bi", "bj", "bk"))
+    assert d1["divb_max"] * (1.0 / 128) / bmax <= 1e-5
     assert abs(d1["mass"] - d0["mass"]) <= 1e-5 * d0["mass"]
     d0, d1 = diag[FP64]
     assert d1["divb_max"] <= 1e-12
