@@ -718,12 +718,140 @@ template <> struct Moments<float> {
   static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
 };
 
+// ------------------------------------------------ FP32 packed-pair arithmetic
+// Blackwell's packed FP32 instructions (FFMA2 / FMUL2 / FADD2) issue once for
+// two lanes, each rounded as the scalar fma / mul / add.  The FP32 path
+// evaluates the PDM face reconstruction on pairs of fields and the
+// Gaussian-split flux on the (left, right) pair of a face with them; absolute
+// values, min / max, signs and selects stay per lane, where the absolute
+// values fold into the scalar instructions that use them.  Every FP32 face
+// kernel (x faces, y / z face tiles and column sweeps, batched or not) goes
+// through these functions, so they agree bit for bit.
+namespace p2 {
+__device__ __forceinline__ float2 K(float c) { return make_float2(c, c); }
+__device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub(float2 a, float2 b) { return __ffma2_rn(b, K(-1.0f), a); }  // a - b, one rounding
+__device__ __forceinline__ float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 rcp(float2 a) { return make_float2(__fdividef(1.0f, a.x), __fdividef(1.0f, a.y)); }
+__device__ __forceinline__ float2 rsq(float2 a) { return make_float2(rsqrtf(a.x), rsqrtf(a.y)); }
+}  // namespace p2
+
+// The limiter of pdm2 for one stencil, given the clamped interpolant fii, the
+// one-sided differences dfl = fii - fm1, dfr = f0 - fii and the scaled cell
+// differences dfm, df0, dfp: (left, right) face states.
+__device__ __forceinline__ float2 pdm_lim(float fii, float dfl, float dfr, float dfm, float df0, float dfp) {
+  const float sm = sgn1(dfm), s0 = sgn1(df0), sp = sgn1(dfp);
+  const float qm = fabsf(sm + s0), qp = fabsf(s0 + sp);
+  return make_float2(fii - s0 * mx(0.0f, fabsf(dfl) - qm * fabsf(dfm)),
+                     fii + s0 * mx(0.0f, fabsf(dfr) - qp * fabsf(dfp)));
+}
+
+// PDM2 (mhd3d3.f90:1069-1172) of two stencils at once (lanes .x and .y, e.g.
+// two fields at one face) from the interpolant pair fi: the differences on
+// the packed pipe, the clamp and the limiter per lane.  lr0 / lr1 are the
+// (left, right) states of lane x / lane y.
+__device__ __forceinline__ void pdm2x2(float2 fm2, float2 fm1, float2 f0, float2 fp1, float2 fi, float pdmb,
+                                       float2& lr0, float2& lr1) {
+  const float2 kp = p2::K(pdmb);
+  const float2 dfm = p2::mul(kp, p2::sub(fm1, fm2));
+  const float2 df0 = p2::mul(kp, p2::sub(f0, fm1));
+  const float2 dfp = p2::mul(kp, p2::sub(fp1, f0));
+  float2 fii;
+  fii.x = mx(mn(fm1.x, f0.x), mn(fi.x, mx(fm1.x, f0.x)));
+  fii.y = mx(mn(fm1.y, f0.y), mn(fi.y, mx(fm1.y, f0.y)));
+  const float2 dfl = p2::sub(fii, fm1), dfr = p2::sub(f0, fii);
+  lr0 = pdm_lim(fii.x, dfl.x, dfr.x, dfm.x, df0.x, dfp.x);
+  lr1 = pdm_lim(fii.y, dfl.y, dfr.y, dfm.y, df0.y, dfp.y);
+}
+
+// PDM face states of two fields from their 8-tap windows (tap m = cell
+// c+m-4 for the face at the low side of cell c), packed as field pairs.
+__device__ __forceinline__ void pdm_pair_states(const float2* a, float pdmb, float2& lr0, float2& lr1) {
+  const float2 fi = tap8p<float>(a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7]);
+  pdm2x2(a[2], a[3], a[4], a[5], fi, pdmb, lr0, lr1);
+}
+
+// 0.5 erfc(-x.x) (left state, + moment) and 0.5 erfc(x.y) (right state, -
+// moment) with the erfcc fit of Moments<float>::erfc_pos: its polynomial is
+// evaluated with negated coefficients, so exp(z^2 - (-q)) takes the same
+// argument as erfc_pos's exp(-z^2 + q).
+__device__ __forceinline__ float2 half_erfc_lr(float2 x) {
+  const float2 z = make_float2(fabsf(x.x), fabsf(x.y));
+  const float2 t = p2::rcp(p2::fma(p2::K(0.5f), z, p2::K(1.0f)));
+  float2 nq = p2::fma(t, p2::K(-0.17087277f), p2::K(0.82215223f));
+  nq = p2::fma(t, nq, p2::K(-1.48851587f));
+  nq = p2::fma(t, nq, p2::K(1.13520398f));
+  nq = p2::fma(t, nq, p2::K(-0.27886807f));
+  nq = p2::fma(t, nq, p2::K(0.18628806f));
+  nq = p2::fma(t, nq, p2::K(-0.09678418f));
+  nq = p2::fma(t, nq, p2::K(-0.37409196f));
+  nq = p2::fma(t, nq, p2::K(-1.00002368f));
+  nq = p2::fma(t, nq, p2::K(1.26551223f));
+  const float2 y = p2::fma(z, z, nq);  // z^2 - q
+  const float2 e = make_float2(__expf(-y.x), __expf(-y.y));
+  const float2 h = p2::mul(p2::K(0.5f), p2::mul(t, e));
+  const float2 g = p2::sub(p2::K(1.0f), h);
+  return make_float2(x.x <= 0.0f ? h.x : g.x, x.y >= 0.0f ? h.y : g.y);
+}
+
+// Fluxes and magnetic stress through one face normal to axis D (the
+// formulas of face_flux) with the left state in lane x and the right state
+// in lane y of X[q] = (l[q], r[q]); out = left + right.
+template <int D>
+__device__ __forceinline__ void face_flux_lr(const float2* X, float gam, float* out) {
+  using namespace p2;
+  const float rg = __frcp_rn(gam - 1.0f);
+  const float2 r = X[0], u = X[1], v = X[2], w = X[3], pr = X[4], bx = X[5], by = X[6], bz = X[7];
+  const float2 vn = X[1 + D], bn = X[5 + D];
+  float2 ke = mul(u, u);
+  ke = fma(v, v, ke);
+  ke = fma(w, w, ke);
+  const float2 leng = fma(pr, K(rg), mul(mul(K(0.5f), r), ke));
+  // hydro moments, lam = rho / (2 p)
+  const float2 lam = mul(r, rcp(mul(K(2.0f), pr)));
+  const float2 ra = rsq(lam);
+  const float2 v0 = half_erfc_lr(mul(mul(lam, ra), vn));
+  const float2 lv = mul(mul(lam, vn), vn);
+  const float2 b = mul(mul(K(0.5f * 0.56418958354775628f), ra), make_float2(__expf(-lv.x), __expf(-lv.y)));
+  const float2 v1 = fma(vn, v0, make_float2(b.x, -b.y));
+  float2 f[8];
+  f[0] = mul(r, v1);
+  f[1] = mul(mul(r, u), v1);
+  f[2] = mul(mul(r, v), v1);
+  f[3] = mul(mul(r, w), v1);
+  f[4] = mul(fma(K(0.5f), pr, leng), v1);
+  f[1 + D] = fma(pr, v0, f[1 + D]);
+  f[4] = fma(mul(mul(K(0.5f), pr), vn), v0, f[4]);
+  // magnetic stress, lam = rho / (2 p + B^2)
+  float2 lb = mul(bx, bx);
+  lb = fma(by, by, lb);
+  lb = fma(bz, bz, lb);
+  const float2 lm = mul(r, rcp(fma(K(2.0f), pr, lb)));
+  const float2 m0 = half_erfc_lr(mul(mul(lm, rsq(lm)), vn));
+  const float2 nm0 = mul(K(-1.0f), m0);
+  const float2 hb = mul(K(0.5f), lb);
+  f[5] = (D == 0) ? mul(sub(hb, mul(bx, bx)), m0) : mul(mul(bx, bn), nm0);
+  f[6] = (D == 1) ? mul(sub(hb, mul(by, by)), m0) : mul(mul(by, bn), nm0);
+  f[7] = (D == 2) ? mul(sub(hb, mul(bz, bz)), m0) : mul(mul(bz, bn), nm0);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) out[q] = f[q].x + f[q].y;
+}
+
 // Fluxes and magnetic stress through one face normal to axis D from the
 // reconstructed left (l) and right (r) states {rho, vx, vy, vz, p, bx, by, bz}
 // (get_flux_stress, mhd3d3.f90:2385-2560): out = {rho, rvx, rvy, rvz, eng,
 // s_x, s_y, s_z}.  Left state with the + moments, right with the - moments.
+// FP32: on the packed pipe (face_flux_lr).
 template <typename T, int D>
 __device__ __forceinline__ void face_flux(const T* l, const T* r, T gam, T* out) {
+  if constexpr (std::is_same<T, float>::value) {
+    float2 X[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) X[q] = make_float2(l[q], r[q]);
+    face_flux_lr<D>(X, gam, out);
+    return;
+  }
   typedef Moments<T> M;
   const T gm1 = gam - T(1);
   {
@@ -845,6 +973,28 @@ __device__ __forceinline__ void recon_win(const T* w, const Prm<T>& P, T& fl, T&
 #undef TAP
 }
 
+// One-sided states of the 8 cell fields src[0..7] at the low face of element
+// c along stride s (recon_face per field); FP32 PDM on field pairs.
+template <typename T, int RECON, typename I>
+__device__ __forceinline__ void face_states(const T* const* src, I c, I s, const Prm<T>& P, T* L, T* R) {
+  if constexpr (std::is_same<T, float>::value && RECON == R_PDM) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float *fa = src[2 * q], *fb = src[2 * q + 1];
+      float2 a[8];
+#pragma unroll
+      for (int m = 0; m < 8; ++m) a[m] = make_float2(fa[c + (m - 4) * s], fb[c + (m - 4) * s]);
+      float2 lr0, lr1;
+      pdm_pair_states(a, P.pdmb, lr0, lr1);
+      L[2 * q] = lr0.x; R[2 * q] = lr0.y;
+      L[2 * q + 1] = lr1.x; R[2 * q + 1] = lr1.y;
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < 8; ++v) recon_face<T, RECON>(src[v], c, s, P, L[v], R[v]);
+  }
+}
+
 // Face fluxes through the low face of cell c along axis D by direct (cached)
 // loads; one face per thread.  Used for the x faces of every stage and, for
 // all three axes, by the kernel-level debug entry point.
@@ -865,8 +1015,7 @@ __global__ void k_flux(KArg<T, B> ka, Inp<T> in0, Prm<T> P) {
   const int s = (D == 0) ? 1 : (D == 1) ? g.px : (int)g.plane;
   const T* src[8] = {in.rho, in.vx, in.vy, in.vz, in.p, in.bx, in.by, in.bz};
   T L[8], R[8], out[8];
-#pragma unroll
-  for (int v = 0; v < 8; ++v) recon_face<T, RECON>(src[v], c, s, P, L[v], R[v]);
+  face_states<T, RECON>(src, c, s, P, L, R);
   any_face_flux<T, D, M>(d, c, L, R, out);
 #pragma unroll
   for (int q = 0; q < 8; ++q) d.F[D][q][c] = out[q];
@@ -1072,8 +1221,7 @@ __global__ void __launch_bounds__(32 * (TDV + 1), FluxMinB<T>::value)
       for (int v = 0; v < 8; ++v) recon_col<T, RECON, 32>(sv + (v * TROWS + r) * 32 + tx, P, L[v], R[v]);
     } else {
       const int cf = rowbase + tx + cd * s;
-#pragma unroll
-      for (int v = 0; v < 8; ++v) recon_face<T, RECON>(src[v], cf, s, P, L[v], R[v]);
+      face_states<T, RECON>(src, cf, s, P, L, R);
     }
     any_face_flux<T, D, M>(d, rowbase + tx + cd * s, L, R, F);
 #pragma unroll
@@ -1159,18 +1307,26 @@ __global__ void __launch_bounds__(128, kSweepMinB)
   // (each lane reads back only what it copied)
   __shared__ __align__(16) T szf[4][2][18][32];
   T (*zs)[18][32] = szf[threadIdx.y];
-  T w[8][8], nx[8], Fp[8];
+  // the window holds the 8 fields as pairs (rho, vx), (vy, vz), (p, bx),
+  // (by, bz), the operands of the packed FP32 reconstruction
+  typedef typename Pr<T>::V V2;
+  V2 w[4][8], nx[4];
+  T Fp[8];
   // window of the first face (cell c0): cells c0-4 .. c0+3; the loop shifts
-  // one cell in per face, so w[v][1..7] start as cells c0-4 .. c0+2.  Window
+  // one cell in per face, so w[q][1..7] start as cells c0-4 .. c0+2.  Window
   // cells are clamped to the ghost-inclusive range [0, nD-1]: with fewer than
   // 4 ghost layers (nord 4 or 6: TVD, WENO) the outermost taps lie outside
   // it, and those taps are exactly the ones such a stencil never reads.
   const int nD = (D == 1) ? g.ny : g.nz;
 #pragma unroll
-  for (int v = 0; v < 8; ++v) {
+  for (int q = 0; q < 4; ++q) {
 #pragma unroll
-    for (int m = 1; m < 8; ++m) w[v][m] = src[v][col + max(c0 - 5 + m, 0) * s];
-    nx[v] = src[v][col + min(c0 + 3, nD - 1) * s];
+    for (int m = 1; m < 8; ++m) {
+      const int x = col + max(c0 - 5 + m, 0) * s;
+      w[q][m] = Pr<T>::mk(src[2 * q][x], src[2 * q + 1][x]);
+    }
+    const int x = col + min(c0 + 3, nD - 1) * s;
+    nx[q] = Pr<T>::mk(src[2 * q][x], src[2 * q + 1][x]);
   }
   T dx = T(0), rdx = T(0);
   if (D == 1) {
@@ -1180,14 +1336,15 @@ __global__ void __launch_bounds__(128, kSweepMinB)
 #pragma unroll kSweepUnroll
   for (int cd = c0; cd <= c1; ++cd) {  // the face at the low side of cell cd
 #pragma unroll
-    for (int v = 0; v < 8; ++v) {
+    for (int q = 0; q < 4; ++q) {
 #pragma unroll
-      for (int m = 0; m < 7; ++m) w[v][m] = w[v][m + 1];
-      w[v][7] = nx[v];
+      for (int m = 0; m < 7; ++m) w[q][m] = w[q][m + 1];
+      w[q][7] = nx[q];
     }
     if (cd < c1) {
+      const int x = col + min(cd + 4, nD - 1) * s;
 #pragma unroll
-      for (int v = 0; v < 8; ++v) nx[v] = src[v][col + min(cd + 4, nD - 1) * s];
+      for (int q = 0; q < 4; ++q) nx[q] = Pr<T>::mk(src[2 * q][x], src[2 * q + 1][x]);
     }
     if (D == 1) {
       __syncwarp();  // every lane is done reading the slot refilled here
@@ -1236,8 +1393,23 @@ __global__ void __launch_bounds__(128, kSweepMinB)
       asm volatile("cp.async.commit_group;" ::: "memory");
     }
     T L[8], R[8], F[8];
+    if constexpr (std::is_same<T, float>::value && RECON == R_PDM) {
 #pragma unroll
-    for (int v = 0; v < 8; ++v) recon_win<T, RECON, 0>(w[v], P, L[v], R[v]);
+      for (int q = 0; q < 4; ++q) {
+        float2 lr0, lr1;
+        pdm_pair_states(w[q], P.pdmb, lr0, lr1);
+        L[2 * q] = lr0.x; R[2 * q] = lr0.y;
+        L[2 * q + 1] = lr1.x; R[2 * q + 1] = lr1.y;
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < 8; ++v) {
+        T wv[8];
+#pragma unroll
+        for (int m = 0; m < 8; ++m) wv[m] = (v & 1) ? w[v >> 1][m].y : w[v >> 1][m].x;
+        recon_win<T, RECON, 0>(wv, P, L[v], R[v]);
+      }
+    }
     face_flux<T, D>(L, R, d.gam, F);
     if (cd > c0) {
       const int cc = cd - 1;
