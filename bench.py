@@ -97,6 +97,8 @@ def parse():
     ap.add_argument("--no-study", action="store_true",
                     help="skip the FP64 line and the error-at-equal-GPU-time table")
     ap.add_argument("--study-steps", type=int, default=20)
+    ap.add_argument("--ensemble-key", type=int, default=256,
+                    help="grids of the batched ensemble measured after the timed region (0: skip)")
     return ap.parse_args()
 
 
@@ -399,6 +401,9 @@ def run_ours(a):
         # timed region: FP64 n^3 is the reference solution of the table
         from mhd3d_mpi_fortran_gb300 import studies
         study = studies.equal_time(n=n, steps=a.study_steps, recon=a.recon)
+    ens = None
+    if a.ensemble_key > 0 and rank == 0 and ws == 1:
+        ens = ensemble_measure(a.ensemble_key, min(a.steps, 20), a.warmup)
     cpu = None
     if not a.no_cpu_baseline and rank == 0 and ws == 1:
         v, dt, cores = cpu_rate(160, 8, a.recon)
@@ -439,6 +444,7 @@ def run_ours(a):
         "e2e": e2e,
         "fp64": fp64,
         "equal_time": study,
+        "ensemble": ens,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
@@ -456,44 +462,46 @@ def ensemble_members(ngrids: int, seed: int = 0):
     return [(int(n), float(a_), float(b_) / (10.0 / 3.0)) for n, a_, b_ in zip(sizes, amp, beta)]
 
 
-def run_ensemble(a):
-    """One CUDA graph stepping every grid (mhd_ensemble_step) against the same
-    grids stepped one after another (per-grid graph replay)."""
-    from mhd3d_mpi_fortran_gb300 import MHDSolver, ics, ensemble_step, ensemble_autotune
+def ensemble_measure(ngrids: int, steps: int, warmup: int) -> dict:
+    """The batched ensemble (mhd_ensemble_step: one CUDA graph, one launch per
+    kernel family over all grids) against the same grids stepped one after
+    another (each grid's own k-step graph), both device-timed with CUDA
+    events (mhd_ensemble_time, mhd_time_steps)."""
+    from mhd3d_mpi_fortran_gb300 import MHDSolver, ics, ensemble_step, ensemble_autotune, ensemble_time
     from mhd3d_mpi_fortran_gb300.abi import Params, FP32
-    members = ensemble_members(a.ensemble)
+    members = ensemble_members(ngrids)
     solvers, zones = [], 0
-    for i, (n, amp, bs) in enumerate(members):
-        st = ics.orszag_tang_3d(n, seed=i, amp=amp, beta_scale=bs)
-        solvers.append(MHDSolver(Params(n, n, n, precision=FP32, tau=0.5 * ics.cfl_dt(st)), st))
-        zones += n ** 3
-    k = a.steps
-    tiles = ensemble_autotune(solvers, reps=3)
-    ensemble_step(solvers, max(3, a.warmup))
-    t0 = time.perf_counter()
-    ensemble_step(solvers, k)
-    t_ens = time.perf_counter() - t0
-    import ctypes
-    for sv in solvers:  # build and warm each grid's own k-step graph
-        sv.lib.mhd_step_graph(sv.h, k, None, None)
-        sv.step(0)
-    t0 = time.perf_counter()
-    for sv in solvers:  # one grid after another: each waits for the previous
-        sv.lib.mhd_step_graph(sv.h, k, None, None)
-        sv.lib.mhd_step_n(sv.h, 0, ctypes.byref(ctypes.c_double()), ctypes.byref(ctypes.c_uint32()))
-    t_seq = time.perf_counter() - t0
-    for sv in solvers:
-        sv.close()
-    line = {"metric": "zone-updates/s (batched ensemble)", "value": zones * k / t_ens, "unit": "zone-updates/s",
-            "n_gpus": 1, "steps": k, "warmup": a.warmup, "ms_per_step": 1e3 * t_ens / k,
-            "higher_is_better": True, "dtype": "f32", "data": "synthetic: seeded OT ensemble",
-            "config": {"workload": f"{a.ensemble} periodic OT grids, N in {{32,48,64,96}}, amplitude U[0.5,1.5], "
-                                   f"beta U[0.1,10], PDM + RK2, FP32", "zones_per_step": zones,
-                       "batched": "one launch per kernel family over all grids, one CUDA graph",
-                       "tiles": {"face_tile_len": tiles[0], "ei_emf_tile": tiles[1]}},
-            "sequential": {"value": zones * k / t_seq, "ms_per_step": 1e3 * t_seq / k,
-                           "how": "per-grid CUDA-graph replay, grids one after another"},
-            "timing": "host wall clock around the graph launches, device synchronised at both ends"}
+    try:
+        for i, (n, amp, bs) in enumerate(members):
+            st = ics.orszag_tang_3d(n, seed=i, amp=amp, beta_scale=bs)
+            solvers.append(MHDSolver(Params(n, n, n, precision=FP32, tau=0.5 * ics.cfl_dt(st)), st))
+            zones += n ** 3
+        tiles = ensemble_autotune(solvers, reps=3)
+        ensemble_step(solvers, max(3, warmup))
+        ensemble_time(solvers, steps)  # the k-step graph is captured on its first use
+        ms_ens = ensemble_time(solvers, steps)
+        ms_seq = 0.0
+        for sv in solvers:
+            sv.time_steps(steps, graph=True)  # capture and warm each grid's own k-step graph
+            ms_seq += sv.time_steps(steps, graph=True)
+    finally:
+        for sv in solvers:
+            sv.close()
+    sizes = sorted({m[0] for m in members})
+    return {"metric": "zone-updates/s (batched ensemble)", "value": zones * steps / (ms_ens * 1e-3),
+            "unit": "zone-updates/s", "steps": steps, "ms_per_step": ms_ens / steps, "zones_per_step": zones,
+            "workload": f"{ngrids} periodic 3-D Orszag-Tang grids, N uniform in {sizes}, amplitude U[0.5,1.5], "
+                        f"beta U[0.1,10], PDM + RK2, FP32",
+            "tiles": {"face_tile_len": tiles[0], "ei_emf_tile": tiles[1]},
+            "sequential": {"value": zones * steps / (ms_seq * 1e-3), "ms_per_step": ms_seq / steps,
+                           "how": "each grid's own k-step CUDA graph, one grid after another"},
+            "timing": "CUDA events on the ensemble's stream around its graph (device time)"}
+
+
+def run_ensemble(a):
+    line = ensemble_measure(a.ensemble, a.steps, a.warmup)
+    line.update({"n_gpus": 1, "warmup": a.warmup, "higher_is_better": True, "dtype": "f32",
+                 "data": "synthetic: seeded OT ensemble"})
     print(json.dumps(line), flush=True)
 
 

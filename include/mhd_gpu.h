@@ -254,6 +254,11 @@ int mhd_diagnostics_noalloc(const mhd_params* prm, const double* rho, const doub
  * alone gives.  Graphs are cached per (grids, nsteps). */
 int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* status);
 
+/* The same ensemble steps as mhd_ensemble_step, with *ms the device time of
+ * the ensemble graph: two CUDA events on the stream that carries it (the
+ * first grid's), recorded right before and after its launch. */
+int mhd_ensemble_time(void** handles, int32_t ngrids, int32_t nsteps, float* ms);
+
 /* Tile autotuner (no reference counterpart).  Times the launch-shape variants
  * compiled for the FP32 Cartesian paths -- y/z face-tile length 4, 8 or 16 (8
  * only outside PDM)

@@ -7,4 +7,4 @@ Python (``MHDSolver``).  ``ics`` holds the initial-condition generators and
 """
 from .abi import Params, MHDError  # noqa: F401
 from . import abi, ics, deck  # noqa: F401
-from .solver import MHDSolver, ensemble_step, ensemble_autotune  # noqa: F401
+from .solver import MHDSolver, ensemble_step, ensemble_autotune, ensemble_time  # noqa: F401

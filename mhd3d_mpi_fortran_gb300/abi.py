@@ -27,7 +27,7 @@ EXPORTS = (
     "mhd_init", "mhd_init_mapped", "mhd_step", "mhd_step_n", "mhd_fetch", "mhd_diagnostics", "mhd_step_graph",
     "mhd_set_tau", "mhd_set_profiling", "mhd_last_timings", "mhd_free", "mhd_last_error", "mhd_set_wait_bound",
     "mhd_device_info",
-    "mhd_debug_fluxes", "mhd_debug_emf", "mhd_ensemble_step", "mhd_time_steps",
+    "mhd_debug_fluxes", "mhd_debug_emf", "mhd_ensemble_step", "mhd_ensemble_time", "mhd_time_steps",
     "mhd_diagnostics_noalloc", "mhd_checkpoint_save", "mhd_checkpoint_load",
     "mhd_autotune", "mhd_ensemble_autotune", "mhd_set_tiles", "mhd_tc_gemm_test",
     "mhd_mlp_create", "mhd_mlp_params", "mhd_mlp_set_norm", "mhd_mlp_set_data", "mhd_mlp_grad", "mhd_mlp_train",
@@ -129,6 +129,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.mhd_debug_emf.argtypes = [vp, dp, dp, dp]
     lib.mhd_time_steps.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_float)]
     lib.mhd_ensemble_step.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.POINTER(C.c_uint32)]
+    lib.mhd_ensemble_time.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.POINTER(C.c_float)]
     lib.mhd_checkpoint_save.argtypes = [vp, C.c_char_p]
     lib.mhd_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
     lib.mhd_set_tiles.argtypes = [vp, C.c_int32, C.c_int32]

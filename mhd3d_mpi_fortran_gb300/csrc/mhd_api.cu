@@ -1270,9 +1270,12 @@ static void ens_forget(unsigned long long uid) {
 
 // Ensemble: nsteps steps of every grid in one CUDA graph on the first grid's
 // stream; graphs cached per (grids, their current halves, nsteps, shapes).
-int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* status) {
+// Enqueues the graph (after the work already queued on every grid's stream)
+// and returns; ev_after (optional) is recorded right after it.
+static int ens_launch(void** handles, int32_t ngrids, int32_t nsteps, std::vector<Handle*>& hs,
+                      cudaEvent_t ev_before, cudaEvent_t ev_after) {
   if (!handles || ngrids <= 0 || nsteps <= 0) return fail(MHD_E_ARG, "bad ensemble arguments");
-  std::vector<Handle*> hs(ngrids);
+  hs.assign(ngrids, nullptr);
   for (int i = 0; i < ngrids; ++i) {
     Handle* h = (Handle*)handles[i];
     if (!h) return fail(MHD_E_ARG, "null handle in ensemble");
@@ -1309,7 +1312,16 @@ int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* 
     cudaEventDestroy(e);
   }
   for (int i = 0; i < ngrids; ++i) hs[i]->par = it->second.par_end[i];
+  if (ev_before) CK(cudaEventRecord(ev_before, h0->st));
   CK(cudaGraphLaunch(it->second.ex, h0->st));
+  if (ev_after) CK(cudaEventRecord(ev_after, h0->st));
+  return MHD_OK;
+}
+
+int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* status) {
+  std::vector<Handle*> hs;
+  int rc = ens_launch(handles, ngrids, nsteps, hs, nullptr, nullptr);
+  if (rc) return rc;
   // h0's stream carries the whole graph: waiting on it first covers every grid
   uint32_t acc = 0;
   for (int i = 0; i < ngrids; ++i) {
@@ -1319,6 +1331,24 @@ int mhd_ensemble_step(void** handles, int32_t ngrids, int32_t nsteps, uint32_t* 
     acc |= st;
   }
   if (status) *status = acc;
+  return MHD_OK;
+}
+
+// The same nsteps-step ensemble graph as mhd_ensemble_step, bracketed by two
+// CUDA events on the stream that carries it; *ms = their elapsed device time.
+int mhd_ensemble_time(void** handles, int32_t ngrids, int32_t nsteps, float* ms) {
+  if (!ms) return fail(MHD_E_ARG, "null output");
+  if (!handles || ngrids <= 0 || !handles[0]) return fail(MHD_E_ARG, "bad ensemble arguments");
+  Handle* h0 = (Handle*)handles[0];
+  std::vector<Handle*> hs;
+  int rc = ens_launch(handles, ngrids, nsteps, hs, h0->ev[2], h0->ev[3]);
+  if (rc) return rc;
+  for (Handle* h : hs) {  // read back and clear each grid's status, as mhd_ensemble_step does
+    uint32_t st = 0;
+    rc = finish(h, nullptr, &st);
+    if (rc) return rc;
+  }
+  CK(cudaEventElapsedTime(ms, h0->ev[2], h0->ev[3]));
   return MHD_OK;
 }
 

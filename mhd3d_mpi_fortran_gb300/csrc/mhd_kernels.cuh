@@ -727,6 +727,14 @@ template <> struct Moments<float> {
 // values fold into the scalar instructions that use them.  Every FP32 face
 // kernel (x faces, y / z face tiles and column sweeps, batched or not) goes
 // through these functions, so they agree bit for bit.
+// Compile-time knobs: MHD_FLUX_PACKED = 0 keeps the FP32 flux scalar (two
+// independent left / right chains), MHD_RECON_PACKED = 0 the reconstruction.
+#ifndef MHD_FLUX_PACKED
+#define MHD_FLUX_PACKED 1
+#endif
+#ifndef MHD_RECON_PACKED
+#define MHD_RECON_PACKED 1
+#endif
 namespace p2 {
 __device__ __forceinline__ float2 K(float c) { return make_float2(c, c); }
 __device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
@@ -845,7 +853,7 @@ __device__ __forceinline__ void face_flux_lr(const float2* X, float gam, float* 
 // FP32: on the packed pipe (face_flux_lr).
 template <typename T, int D>
 __device__ __forceinline__ void face_flux(const T* l, const T* r, T gam, T* out) {
-  if constexpr (std::is_same<T, float>::value) {
+  if constexpr (std::is_same<T, float>::value && MHD_FLUX_PACKED) {
     float2 X[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) X[q] = make_float2(l[q], r[q]);
@@ -977,7 +985,7 @@ __device__ __forceinline__ void recon_win(const T* w, const Prm<T>& P, T& fl, T&
 // c along stride s (recon_face per field); FP32 PDM on field pairs.
 template <typename T, int RECON, typename I>
 __device__ __forceinline__ void face_states(const T* const* src, I c, I s, const Prm<T>& P, T* L, T* R) {
-  if constexpr (std::is_same<T, float>::value && RECON == R_PDM) {
+  if constexpr (std::is_same<T, float>::value && RECON == R_PDM && MHD_RECON_PACKED) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const float *fa = src[2 * q], *fb = src[2 * q + 1];
@@ -1393,7 +1401,7 @@ __global__ void __launch_bounds__(128, kSweepMinB)
       asm volatile("cp.async.commit_group;" ::: "memory");
     }
     T L[8], R[8], F[8];
-    if constexpr (std::is_same<T, float>::value && RECON == R_PDM) {
+    if constexpr (std::is_same<T, float>::value && RECON == R_PDM && MHD_RECON_PACKED) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         float2 lr0, lr1;

@@ -202,6 +202,16 @@ def ensemble_step(solvers: list, nsteps: int) -> int:
     return st.value
 
 
+def ensemble_time(solvers: list, nsteps: int) -> float:
+    """Device time (ms) of nsteps ensemble steps (mhd_ensemble_time): CUDA
+    events around the ensemble graph on the stream that carries it."""
+    lib = solvers[0].lib
+    arr = (C.c_void_p * len(solvers))(*[s.h.value for s in solvers])
+    ms = C.c_float()
+    check(lib, lib.mhd_ensemble_time(arr, len(solvers), int(nsteps), C.byref(ms)), "mhd_ensemble_time")
+    return ms.value
+
+
 def ensemble_autotune(solvers: list, reps: int = 5) -> tuple:
     """Pick the fastest launch shapes for a batched ensemble (mhd_ensemble_autotune)."""
     lib = solvers[0].lib
