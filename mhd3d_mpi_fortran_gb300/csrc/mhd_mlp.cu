@@ -100,11 +100,19 @@ struct MlpW {
   const float* p;                                 // FP32 parameters (biases read from here)
 };
 
+// tanh on the SFU (PTX tanh.approx.f32, sm_75+; maximum relative error about
+// 2^-11, below the BF16 rounding the activations take next).
+__device__ __forceinline__ float tanh_sfu(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // GELU, tanh form (Hendrycks & Gimpel), and its derivative in dg.
 __device__ __forceinline__ float gelu_t(float z, float& dg) {
   const float c = 0.7978845608028654f, a = 0.044715f;
   const float u = c * (z + a * z * z * z);
-  const float t = tanhf(u);
+  const float t = tanh_sfu(u);
   dg = 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * c * (1.0f + 3.0f * a * z * z);
   return 0.5f * z * (1.0f + t);
 }
@@ -340,28 +348,57 @@ constexpr int I_W1 = 0, I_W2 = I_W1 + NH * FIN * 2, I_W3 = I_W2 + NH * NH * 2, I
               I_TOTAL = I_X + 128 * FIN * 2;
 static_assert(I_W3 + NO * NH * 2 <= I_X && I_X % 1024 == 0, "inference smem map");
 
+// The 8 normalised conserved variables (rho, rho v, hydro energy, cell B)
+// of every cell, ghosts included, as BF16 into one 16-byte record per cell
+// (the cell's padded index): the inference gathers a stencil row as 27 such
+// records instead of recomputing each cell's variables for the 27 rows that
+// use it.
+__global__ void k_mlp_features(Dev<float> d, MlpNorm nm, uint4* __restrict__ field) {
+  const Geom& g = d.g;
+  const long long n = (long long)g.nx * g.ny * g.nz;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = (int)(t % g.nx);
+  const long long q = t / g.nx;
+  const int j = (int)(q % g.ny), k = (int)(q / g.ny);
+  const long long c = (long long)i + (long long)g.px * ((long long)j + (long long)g.py * k);
+  const float gm1 = d.gam - 1.0f;
+  const float rho = d.rho[c], u = d.vx[c], v = d.vy[c], w = d.vz[c];
+  const float U[8] = {rho, rho * u, rho * v, rho * w, 0.5f * rho * (u * u + v * v + w * w) + d.p[c] / gm1,
+                      d.bx[c], d.by[c], d.bz[c]};
+  uint32_t pk[4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn((U[2 * a] - nm.mean[2 * a]) / nm.std[2 * a],
+                                                   (U[2 * a + 1] - nm.mean[2 * a + 1]) / nm.std[2 * a + 1]);
+    pk[a] = *reinterpret_cast<const uint32_t*>(&h);
+  }
+  field[c] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+}
+
 // Features of interior cell t of an FP32 Cartesian grid into row r of an
-// input tile: the 3x3x3 stencil of (rho, rho v, hydro energy, cell B),
-// normalised, feature ((dz+1)*9 + (dy+1)*3 + (dx+1))*8 + var; 216..255 zero.
-__device__ __forceinline__ void gather_row(const Dev<float>& d, const MlpNorm& nm, long long t, unsigned char* tile,
-                                           int r) {
+// input tile: the 3x3x3 stencil of the feature records, feature
+// ((dz+1)*9 + (dy+1)*3 + (dx+1))*8 + var; 216..255 zero.  Eight features are
+// one 16-byte core-matrix row of the K-major tile.
+__device__ __forceinline__ void gather_row(const Dev<float>& d, const uint4* __restrict__ field, long long t,
+                                           unsigned char* tile, int r) {
   const Geom& g = d.g;
   const int i = (int)(t % g.nx0) + g.ng;
   const long long q = t / g.nx0;
   const int j = (int)(q % g.ny0) + g.ng, k = (int)(q / g.ny0) + g.ng;
-  const float gm1 = d.gam - 1.0f;
+  const long long c0 = (long long)i + (long long)g.px * ((long long)j + (long long)g.py * k);
   int f = 0;
-  for (int dz = -1; dz <= 1; ++dz)
-    for (int dy = -1; dy <= 1; ++dy)
-      for (int dx = -1; dx <= 1; ++dx) {
-        const long long c = (long long)(i + dx) + (long long)g.px * ((long long)(j + dy) + (long long)g.py * (k + dz));
-        const float rho = d.rho[c], u = d.vx[c], v = d.vy[c], w = d.vz[c];
-        const float U[8] = {rho, rho * u, rho * v, rho * w, 0.5f * rho * (u * u + v * v + w * w) + d.p[c] / gm1,
-                            d.bx[c], d.by[c], d.bz[c]};
 #pragma unroll
-        for (int a = 0; a < 8; ++a) tc::st_bf16(tile, tc::kmaj(r, f + a, FIN), (U[a] - nm.mean[a]) / nm.std[a]);
+  for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+    for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+      for (int dx = -1; dx <= 1; ++dx) {
+        const long long c = c0 + dx + (long long)g.px * (dy + (long long)g.py * dz);
+        *reinterpret_cast<uint4*>(tile + tc::kmaj(r, f, FIN)) = field[c];
         f += 8;
       }
+#pragma unroll
   for (; f < FIN; f += 8) *reinterpret_cast<uint4*>(tile + tc::kmaj(r, f, FIN)) = make_uint4(0, 0, 0, 0);
 }
 
@@ -370,8 +407,8 @@ __device__ __forceinline__ void gather_row(const Dev<float>& d, const MlpNorm& n
 // grid d, gathered straight into the input tile.
 template <bool GRID>
 __global__ void __launch_bounds__(128, 2)
-    k_mlp_infer(const __nv_bfloat16* __restrict__ X, Dev<float> d, MlpNorm nm, int n, MlpW w, float* __restrict__ Y,
-                int* err) {
+    k_mlp_infer(const __nv_bfloat16* __restrict__ X, Dev<float> d, const uint4* __restrict__ field, int n, MlpW w,
+                float* __restrict__ Y, int* err) {
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tslot;
@@ -398,7 +435,7 @@ __global__ void __launch_bounds__(128, 2)
   for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     if (GRID) {
       const long long g = (long long)tile * 128 + tid;
-      if (g < n) gather_row(d, nm, g, XS, tid);
+      if (g < n) gather_row(d, field, g, XS, tid);
       else
         for (int f = 0; f < FIN; f += 8) *reinterpret_cast<uint4*>(XS + tc::kmaj(tid, f, FIN)) = make_uint4(0, 0, 0, 0);
     } else {
@@ -854,7 +891,7 @@ int mhd_mlp_forward(void* h, const uint16_t* x, int64_t n, float* y) {
   }
   cudaMemcpy(dx, x, (size_t)n * FIN * 2, cudaMemcpyHostToDevice);
   const int tiles = (int)((n + 127) / 128);
-  k_mlp_infer<false><<<tiles < 2 * m->sms ? tiles : 2 * m->sms, 128, I_TOTAL>>>(dx, Dev<float>{}, m->norm, (int)n,
+  k_mlp_infer<false><<<tiles < 2 * m->sms ? tiles : 2 * m->sms, 128, I_TOTAL>>>(dx, Dev<float>{}, nullptr, (int)n,
                                                                                  wview(m), dy, m->err);
   cudaError_t e = cudaDeviceSynchronize();
   if (e == cudaSuccess) e = cudaMemcpy(y, dy, (size_t)n * NOUT * 4, cudaMemcpyDeviceToHost);
@@ -891,8 +928,13 @@ int mhd::mlp_correct(void* h, Dev<float>& d, cudaStream_t st) {
   if (rc) return rc;
   const int nb = (int)((n + 255) / 256);
   const int tiles = (int)((n + 127) / 128);
-  k_mlp_infer<true><<<tiles < 2 * m->sms ? tiles : 2 * m->sms, 128, I_TOTAL, st>>>(nullptr, d, m->norm, (int)n, wview(m),
-                                                                                   m->ys, m->err);
+  // the feature records go to the y-face flux arrays, scratch outside a step
+  // (4 consecutive FP32 arrays = one 16-byte record per padded cell index)
+  uint4* field = reinterpret_cast<uint4*>(d.F[1][0]);
+  const long long ncell = (long long)d.g.nx * d.g.ny * d.g.nz;
+  k_mlp_features<<<(int)((ncell + 255) / 256), 256, 0, st>>>(d, m->norm, field);
+  k_mlp_infer<true><<<tiles < 2 * m->sms ? tiles : 2 * m->sms, 128, I_TOTAL, st>>>(nullptr, d, field, (int)n,
+                                                                                   wview(m), m->ys, m->err);
   if (!m->sums) MCK(cudaMalloc(&m->sums, 8 * sizeof(double)));
   MCK(cudaMemsetAsync(m->sums, 0, 8 * sizeof(double), st));
   k_mlp_sums<<<m->sms * 4, 256, 0, st>>>(m->ys, (long long)n, m->sums);
