@@ -442,6 +442,16 @@ template <typename T> struct KArg<T, true> {
 template <typename T>
 inline KArg<T, false> one(const Dev<T>& d) { return KArg<T, false>{d}; }
 
+// Resident 256-thread blocks per SM requested for the cell passes (CFL, CT +
+// bxyz, fill).  Single grid: full occupancy at 32 registers.  Batched: each
+// thread holds its grid's array pointers in registers (from the grid table,
+// not the constant bank), about 75 registers unbounded, which would leave 3
+// blocks per SM for these latency-bound passes; a budget keeps more resident.
+#ifndef MHD_BATCH_MINB
+#define MHD_BATCH_MINB 6
+#endif
+constexpr int pass_min_blocks(bool B) { return B ? MHD_BATCH_MINB : 8; }
+
 // ------------------------------------------------------------- small kernels
 template <typename T>
 __device__ __forceinline__ long long idx3(const Geom& g, int i, int j, int k) {
@@ -500,7 +510,7 @@ __device__ __forceinline__ float cfl_sqrt(float x) { return x > 0.0f ? x * rsqrt
 // 3794-3819) at interior cells and faces, the only places they are read.
 // The minimum is reduced in T and converted to FP64 once per block.
 template <typename T, bool M, bool B>
-__global__ void __launch_bounds__(256) k_cfl(KArg<T, B> ka, int save) {
+__global__ void __launch_bounds__(256, pass_min_blocks(B)) k_cfl(KArg<T, B> ka, int save) {
   const int4 bb = ka.blk();
   const auto& d = ka.dev(bb);
   const Geom& g = d.g;
@@ -2073,7 +2083,7 @@ __device__ __forceinline__ void fill_shell_ijk(const Geom& g, int u, int& i, int
 // shell_only != 0: the launch covers only the shell blocks (block b is shell
 // block b), after k_ct_fill has done the interior.
 template <typename T, bool M, bool B>
-__global__ void __launch_bounds__(256) k_fill_bxyz(KArg<T, B> ka, int want_vf, int shell_only) {
+__global__ void __launch_bounds__(256, pass_min_blocks(B)) k_fill_bxyz(KArg<T, B> ka, int want_vf, int shell_only) {
   const int4 bb = ka.blk();
   const auto& d = ka.dev(bb);
   const Geom& g = d.g;
@@ -2175,7 +2185,7 @@ __global__ void __launch_bounds__(256) k_fill_bxyz(KArg<T, B> ka, int want_vf, i
 // interior tiles.  The ghost shell of the new half follows in k_fill_bxyz
 // (shell_only).
 template <typename T, bool B>
-__global__ void __launch_bounds__(256) k_ct_fill(KArg<T, B> ka, int form, T cw, T den, int want_vf) {
+__global__ void __launch_bounds__(256, pass_min_blocks(B)) k_ct_fill(KArg<T, B> ka, int form, T cw, T den, int want_vf) {
   const int4 bb = ka.blk();
   const auto& d = ka.dev(bb);
   const Geom& g = d.g;
