@@ -117,6 +117,26 @@ __device__ __forceinline__ float gelu_t(float z, float& dg) {
   return 0.5f * z * (1.0f + t);
 }
 
+// GELU of the 16 accumulators z[0..16) of row r, columns c0.. (+ bias),
+// rounded to BF16 and stored as two 16-byte core-matrix rows of the K-major
+// [128 x NH] activation tile.
+__device__ __forceinline__ void gelu16_store(unsigned char* tile, int r, int c0, const float* z,
+                                             const float* __restrict__ bias) {
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    uint32_t pk[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      float d0, d1;
+      const int i = 8 * h + 2 * a;
+      const __nv_bfloat162 v = __floats2bfloat162_rn(gelu_t(z[i] + bias[c0 + i], d0),
+                                                     gelu_t(z[i + 1] + bias[c0 + i + 1], d1));
+      pk[a] = *reinterpret_cast<const uint32_t*>(&v);
+    }
+    *reinterpret_cast<uint4*>(tile + tc::kmaj(r, c0 + 8 * h, NH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+  }
+}
+
 // Copy a row-major [R x K] BF16 matrix into a K-major canonical tile.
 __device__ __forceinline__ void stage_w(unsigned char* dst, const __nv_bfloat16* src, int R, int K) {
   const int k8n = K / 8;
@@ -454,10 +474,7 @@ __global__ void __launch_bounds__(128, 2)
     for (int c0 = 0; c0 < NH; c0 += 16) {  // H1 over the consumed input tile
       float z[16];
       tc::tmem_ld16(tc::tmem_at(tb + T_D1, q, c0), z);
-      for (int i = 0; i < 16; ++i) {
-        float dg;
-        tc::st_bf16(XS, tc::kmaj(tid, c0 + i, NH), gelu_t(z[i] + w.p[OB1 + c0 + i], dg));
-      }
+      gelu16_store(XS, tid, c0, z, w.p + OB1);
     }
     publish();
     if (tid == 0) gemm(tb + T_D2, s0 + I_X, s0 + I_W2, NH, NH, false);
@@ -466,10 +483,7 @@ __global__ void __launch_bounds__(128, 2)
     for (int c0 = 0; c0 < NH; c0 += 16) {  // H2 over H1 (consumed)
       float z[16];
       tc::tmem_ld16(tc::tmem_at(tb + T_D2, q, c0), z);
-      for (int i = 0; i < 16; ++i) {
-        float dg;
-        tc::st_bf16(XS, tc::kmaj(tid, c0 + i, NH), gelu_t(z[i] + w.p[OB2 + c0 + i], dg));
-      }
+      gelu16_store(XS, tid, c0, z, w.p + OB2);
     }
     publish();
     if (tid == 0) gemm(tb + T_D3, s0 + I_X, s0 + I_W3, NO, NH, false);
@@ -596,10 +610,13 @@ __global__ void k_mlp_apply_b(Dev<float> d) {
   const int i0 = (int)(t % (g.nx0 + 1));
   const long long r = t / (g.nx0 + 1);
   const int j0 = (int)(r % (g.ny0 + 1)), k0 = (int)(r / (g.ny0 + 1));
-  auto at = [&](int a, int i, int j, int k) -> float {  // interior-periodic cell value of d.dU[5+a]
-    i = (i + 2 * g.nx0) % g.nx0;
-    j = (j + 2 * g.ny0) % g.ny0;
-    k = (k + 2 * g.nz0) % g.nz0;
+  // interior-periodic cell value of d.dU[5+a]; every index here lies in
+  // [-1, n0], so one conditional wrap per axis is the periodic image
+  auto wrap = [](int x, int n) { return x < 0 ? x + n : (x >= n ? x - n : x); };
+  auto at = [&](int a, int i, int j, int k) -> float {
+    i = wrap(i, g.nx0);
+    j = wrap(j, g.ny0);
+    k = wrap(k, g.nz0);
     return d.dU[5 + a][(long long)(i + g.ng) + (long long)g.px * ((long long)(j + g.ng) + (long long)g.py * (k + g.ng))];
   };
   auto ex = [&](int i, int j, int k) {

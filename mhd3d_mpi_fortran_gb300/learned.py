@@ -168,11 +168,15 @@ def curl_faces(A: np.ndarray, dx: float):
     return d(ez, 1) - d(ey, 2), d(ex, 2) - d(ez, 0), d(ey, 0) - d(ex, 1)
 
 
-def potential_from_faces(dbi, dbj, dbk, dx: float) -> np.ndarray:
-    """Cell-centred A[3, n, n, n] whose edge-averaged discrete curl (the apply
-    kernel's operator) is the least-squares fit of the face increments
-    (periodic, per wavenumber, minimum-norm solution)."""
-    n = dbi.shape[0]
+_CURL_SVD = {}
+
+
+def _curl_svd(n: int, dx: float):
+    """Per-wavenumber SVD of the apply kernel's curl operator on an n^3
+    periodic grid (cached: it depends on n and dx only)."""
+    key = (n, dx)
+    if key in _CURL_SVD:
+        return _CURL_SVD[key]
     th = 2.0 * np.pi * np.fft.fftfreq(n)
     ex = np.exp(-1j * th)                      # shift by -1
     s = 0.5 * (1.0 + ex)                        # two-cell average toward -1
@@ -186,13 +190,24 @@ def potential_from_faces(dbi, dbj, dbk, dx: float) -> np.ndarray:
         b, c = (a + 1) % 3, (a + 2) % 3
         M[..., a, c] = np.broadcast_to(D[b] * S[a] * S[b], shape)   # E_c averages over axes a, b
         M[..., a, b] = np.broadcast_to(-D[c] * S[a] * S[c], shape)  # E_b averages over axes c, a
-    B = np.stack([np.fft.fftn(dbi), np.fft.fftn(dbj), np.fft.fftn(dbk)], axis=-1)
     # minimum-norm solve; singular values below 1e-9 of the largest over all
     # wavenumbers are null directions (gauge, and the Nyquist modes that the
     # two-cell averages remove)
     u, sv, vh = np.linalg.svd(M)
     cut = 1e-9 * sv.max()
     inv = np.where(sv > cut, 1.0 / np.where(sv > cut, sv, 1.0), 0.0)
+    _CURL_SVD.clear()  # keep one grid size
+    _CURL_SVD[key] = (u, inv, vh)
+    return u, inv, vh
+
+
+def potential_from_faces(dbi, dbj, dbk, dx: float) -> np.ndarray:
+    """Cell-centred A[3, n, n, n] whose edge-averaged discrete curl (the apply
+    kernel's operator) is the least-squares fit of the face increments
+    (periodic, per wavenumber, minimum-norm solution)."""
+    n = dbi.shape[0]
+    u, inv, vh = _curl_svd(n, dx)
+    B = np.stack([np.fft.fftn(dbi), np.fft.fftn(dbj), np.fft.fftn(dbk)], axis=-1)
     uhb = np.einsum("...ji,...j->...i", u.conj(), B)
     A = np.einsum("...ji,...j->...i", vh.conj(), inv * uhb)
     return np.real(np.stack([np.fft.ifftn(A[..., i]) for i in range(3)]))
@@ -220,16 +235,18 @@ class Pairs:
 
 
 def generate(seeds, n_coarse: int, steps: int, every: int = 10, cfl: float = 0.3, nord: int = 8,
-             norm=None):
+             norm=None, precision: int = FP32):
     """Training pairs from fine runs (2 n_coarse)^3 of the turbulence state,
-    one snapshot every `every` fine steps.  Returns (raw features U list,
-    raw targets list) for normalisation, then ``build`` packs them."""
+    one snapshot every `every` fine steps; the fine runs in `precision` (the
+    coarse step that the target corrects is FP32, as the corrected solver).
+    Returns (raw features U list, raw targets list) for normalisation, then
+    ``build`` packs them."""
     nf = 2 * n_coarse
     Us, Ts = [], []
     for seed in seeds:
         s = ics.turbulence(nf, seed=seed)
         tau_f = 0.8 * ics.cfl_dt(s, cfl=cfl)
-        fine = MHDSolver(Params(nf, nf, nf, precision=FP32, stepop=STEP_RK2, tau=tau_f, nord=nord), s)
+        fine = MHDSolver(Params(nf, nf, nf, precision=precision, stepop=STEP_RK2, tau=tau_f, nord=nord), s)
         done = 0
         while done + 2 <= steps:
             f0 = fine.fetch()
@@ -273,11 +290,20 @@ def normalisation(Us, Ts):
     return mean.astype(np.float32), std.astype(np.float32), scale.astype(np.float32)
 
 
-def build(Us, Ts, mean, std, scale) -> Pairs:
+def build(Us, Ts, mean, std, scale, sample: float | None = None, seed: int = 0) -> Pairs:
+    """Feature rows and normalised targets of every snapshot; with `sample`,
+    a seeded random fraction of each snapshot's cells (bounds the pair count
+    of large grids)."""
+    rng = np.random.default_rng(seed)
     xs, ts = [], []
     for U, T in zip(Us, Ts):
-        xs.append(features(U, mean, std))
-        ts.append((T.reshape(8, -1, order="F").T / scale).astype(np.float32))
+        x = features(U, mean, std)
+        t = (T.reshape(8, -1, order="F").T / scale).astype(np.float32)
+        if sample is not None and sample < 1.0:
+            keep = np.sort(rng.choice(x.shape[0], size=max(128, int(sample * x.shape[0])), replace=False))
+            x, t = x[keep], t[keep]
+        xs.append(x)
+        ts.append(t)
     return Pairs(np.concatenate(xs), np.concatenate(ts))
 
 
@@ -389,19 +415,69 @@ def calibrate(mlp: MLP, Us, Ts, mean, std, scale) -> np.ndarray:
 
 def train_correction(train_seeds, n_coarse: int, steps: int, every: int = 10, iters: int = 2000,
                      batch: int = 16384, lr: float = 1e-3, init_seed: int = 0, nord: int = 8,
-                     val_seeds=None):
+                     val_seeds=None, sample: float | None = None, val_steps: int | None = None):
     """Generate pairs from the fine runs of train_seeds, normalise, train a
     fresh network and, with val_seeds, calibrate its outputs on their pairs.
     Returns (mlp, final minibatch loss, number of training pairs, alpha)."""
     Us, Ts = generate(train_seeds, n_coarse, steps, every=every, nord=nord)
     mean, std, scale = normalisation(Us, Ts)
-    pairs = build(Us, Ts, mean, std, scale)
+    pairs = build(Us, Ts, mean, std, scale, sample=sample, seed=init_seed)
+    del Us, Ts
     mlp = MLP(init_params(init_seed))
     mlp.set_norm(mean, std, scale)
     mlp.set_data(pairs.x, pairs.t)
     loss = mlp.train(iters, batch=min(batch, (pairs.x.shape[0] // 128) * 128), lr=lr, seed=init_seed)
     alpha = np.ones(8)
     if val_seeds:
-        Uv, Tv = generate(val_seeds, n_coarse, steps, every=every, nord=nord)
+        Uv, Tv = generate(val_seeds, n_coarse, val_steps or steps, every=every, nord=nord)
         alpha = calibrate(mlp, Uv, Tv, mean, std, scale)
     return mlp, loss, pairs.x.shape[0], alpha
+
+
+def truth_compare(mlp: MLP, seed: int, n_coarse: int, steps: int, cfl: float = 0.3, nord: int = 8) -> dict:
+    """Errors against a 4x finer truth: the (4N)^3 FP32 run over 4*steps steps,
+    restricted to N^3, judges the plain (2N)^3 FP64 run (2*steps steps from
+    the restricted truth start), the plain N^3 FP32 run and the corrected N^3
+    run (steps steps).  GPU time: CUDA events around graph replays for the
+    plain runs, host wall clock (device synchronised) for the corrected run."""
+    import time
+    n4, n2 = 4 * n_coarse, 2 * n_coarse
+    s4 = ics.turbulence(n4, seed=seed)
+    tau4 = 0.8 * ics.cfl_dt(s4, cfl=cfl)
+    ng = nord // 2
+    out = {}
+
+    def timed(prm, st, k, chunk):
+        with MHDSolver(prm, st) as sv:
+            ms, done = 0.0, 0
+            while done < k:
+                m = min(chunk, k - done)
+                ms += sv.time_steps(m, graph=True)
+                done += m
+            return ms, sv.fetch()
+
+    ms4, f4 = timed(Params(n4, n4, n4, precision=FP32, stepop=STEP_RK2, tau=tau4, nord=nord), s4, 4 * steps, 100)
+    ref = state_dict(restrict(state_dict(restrict(f4, n4, nord)), n2, nord))
+    del f4
+    with MHDSolver(Params(n4, n4, n4, precision=FP32, stepop=STEP_RK2, tau=tau4, nord=nord), s4) as sv:
+        s2 = restrict(sv.fetch(), n4, nord)
+    del s4
+    s1 = restrict(state_dict(s2), n2, nord)
+    from .abi import FP64
+    ms2, f2 = timed(Params(n2, n2, n2, precision=FP64, stepop=STEP_RK2, tau=2 * tau4, nord=nord), s2, 2 * steps, 20)
+    out["fine_fp64"] = {"n": n2, "steps": 2 * steps, "gpu_ms": ms2,
+                        "l1": l1_error(state_dict(restrict(f2, n2, nord)), ref, ng)}
+    del f2
+    pc = Params(n_coarse, n_coarse, n_coarse, precision=FP32, stepop=STEP_RK2, tau=4 * tau4, nord=nord)
+    ms1, f1 = timed(pc, s1, steps, 100)
+    out["coarse_fp32"] = {"n": n_coarse, "steps": steps, "gpu_ms": ms1, "l1": l1_error(f1, ref, ng)}
+    with MHDSolver(pc, s1) as cs:
+        cs.step(0)
+        t0 = time.perf_counter()
+        _, st = mlp.step_corrected(cs, steps)
+        t1 = time.perf_counter()
+        out["corrected_fp32"] = {"n": n_coarse, "steps": steps, "wall_ms": 1e3 * (t1 - t0),
+                                 "l1": l1_error(cs.fetch(), ref, ng), "status": st,
+                                 "divb_max": cs.diagnostics()["divb_max"]}
+    out["truth"] = {"n": n4, "steps": 4 * steps, "gpu_ms": ms4, "precision": "fp32"}
+    return out

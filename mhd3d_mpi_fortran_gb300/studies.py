@@ -212,10 +212,65 @@ def learned_study(n: int = 64, train_seeds=tuple(range(100, 108)), val_seed: int
     }
 
 
+def learned_config5(n: int = 128, train_seeds=(100, 101, 102, 103), val_seed: int = 104, damp_seed: int = 105,
+                    test_seeds=(200, 201), train_steps: int = 60, every: int = 10, sample: float = 0.125,
+                    iters: int = 3000, steps: int = 200, damp_steps: int = 50, fp64_seed: int = 100,
+                    truth_steps: int = 100) -> dict:
+    """The learned correction at the stated scale: trained on restricted fine
+    (2n)^3 FP32 runs of train_seeds (a snapshot every `every` fine steps, a
+    `sample` fraction of each snapshot's cells), calibrated on val_seed, its
+    damping chosen on damp_seed's rollout, evaluated on test_seeds over
+    `steps` coarse steps against the restricted fine run; the FP32 training
+    targets compared with FP64 ones on fp64_seed; and, on the first test seed,
+    the plain (2n)^3 FP64, plain n^3 and corrected n^3 runs against a (4n)^3
+    truth over truth_steps coarse steps."""
+    from . import learned
+    from .abi import FP64
+    import time
+    t0 = time.perf_counter()
+    mlp, loss, npairs, alpha = learned.train_correction(list(train_seeds), n, steps=train_steps, every=every,
+                                                        iters=iters, batch=16384, lr=1e-3, val_seeds=[val_seed],
+                                                        sample=sample, val_steps=2 * every)
+    t_train = time.perf_counter() - t0
+    gamma, errs = learned.damp(mlp, damp_seed, n, damp_steps)
+    # FP32 vs FP64 fine runs as the source of the targets (two snapshots)
+    mean, std, scale = mlp.norm
+    U32, T32 = learned.generate([fp64_seed], n, 2 * every, every=every, precision=FP32)
+    U64, T64 = learned.generate([fp64_seed], n, 2 * every, every=every, precision=FP64)
+    tdiff = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in
+             zip(np.concatenate(T32, axis=1), np.concatenate(T64, axis=1))]
+    p32 = learned.build(U32, T32, mean, std, scale)
+    p64 = learned.build(U64, T64, mean, std, scale)
+    y = mlp.forward(p32.x).astype(np.float64)
+    loss32 = float(np.mean((y - p32.t) ** 2))
+    y = mlp.forward(p64.x).astype(np.float64)
+    loss64 = float(np.mean((y - p64.t) ** 2))
+    del U32, T32, U64, T64, p32, p64
+    rows = [learned.evaluate(mlp, seed, n, steps) for seed in test_seeds]
+    truth = learned.truth_compare(mlp, test_seeds[0], n, truth_steps) if truth_steps else None
+    mlp.close()
+    agg = {k: float(np.mean([r[k] for r in rows])) for k in ("coarse_l1", "corrected_l1", "fine_s", "coarse_s",
+                                                            "corrected_s")}
+    return {
+        "study": "learned_config5",
+        "workload": f"coarse {n}^3 vs fine {2 * n}^3 decaying turbulence (FP32 RK2 PDM), {steps} coarse steps, "
+                    f"{len(test_seeds)} held-out seeds",
+        "train": {"seeds": list(train_seeds), "fine_steps_per_seed": train_steps, "every": every, "sample": sample,
+                  "pairs": npairs, "iters": iters, "final_loss": loss, "alpha": [float(a) for a in alpha],
+                  "seconds_incl_data": t_train},
+        "damping": {"seed": damp_seed, "steps": damp_steps, "gamma": gamma, "corrected_l1": errs},
+        "targets_fp32_vs_fp64": {"seed": fp64_seed, "rel_l2_per_output": tdiff, "loss_on_fp32_targets": loss32,
+                                 "loss_on_fp64_targets": loss64},
+        "mean": agg, "per_seed": rows, "truth": truth,
+        "note": "mean / per_seed: relative L1 of the conserved variables against the restricted fine run, host "
+                "wall clock with the device synchronised; truth: against the restricted (4n)^3 run",
+    }
+
+
 def main(argv=None) -> None:
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["curvilinear", "precision", "learned", "equal_time"])
+    ap.add_argument("study", choices=["curvilinear", "precision", "learned", "learned_config5", "equal_time"])
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--recons", default="1,5,3", help="precision study: reconop values (1 PDM, 5 TVD-MC, 3 WENO5)")
@@ -227,6 +282,8 @@ def main(argv=None) -> None:
     elif a.study == "equal_time":
         for r in tuple(int(r) for r in a.recons.split(",")):
             print(json.dumps(equal_time(a.n or 256, a.steps or 100, r)), flush=True)
+    elif a.study == "learned_config5":
+        print(json.dumps(learned_config5(a.n or 128, steps=a.steps or 200)), flush=True)
     elif a.study == "learned":
         print(json.dumps(learned_study(a.n or 64, steps=a.steps or 100, damp_seed=a.damp_seed)), flush=True)
     else:
