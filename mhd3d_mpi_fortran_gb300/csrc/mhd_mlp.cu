@@ -399,41 +399,46 @@ __global__ void k_mlp_features(Dev<float> d, MlpNorm nm, uint4* __restrict__ fie
 // Features of interior cell t of an FP32 Cartesian grid into row r of an
 // input tile: the 3x3x3 stencil of the feature records, feature
 // ((dz+1)*9 + (dy+1)*3 + (dx+1))*8 + var; 216..255 zero.  Eight features are
-// one 16-byte core-matrix row of the K-major tile.
-__device__ __forceinline__ void gather_row(const Dev<float>& d, const uint4* __restrict__ field, long long t,
-                                           unsigned char* tile, int r) {
+// one 16-byte core-matrix row of the K-major tile; this thread writes the
+// 16 of the row's 32 such chunks that start at chunk h*16 (t < 0: zeros).
+__device__ __forceinline__ void gather_half_row(const Dev<float>& d, const uint4* __restrict__ field, long long t,
+                                                unsigned char* tile, int r, int h) {
   const Geom& g = d.g;
-  const int i = (int)(t % g.nx0) + g.ng;
-  const long long q = t / g.nx0;
-  const int j = (int)(q % g.ny0) + g.ng, k = (int)(q / g.ny0) + g.ng;
-  const long long c0 = (long long)i + (long long)g.px * ((long long)j + (long long)g.py * k);
-  int f = 0;
+  long long c0 = 0;
+  if (t >= 0) {
+    const int i = (int)(t % g.nx0) + g.ng;
+    const long long q = t / g.nx0;
+    const int j = (int)(q % g.ny0) + g.ng, k = (int)(q / g.ny0) + g.ng;
+    c0 = (long long)i + (long long)g.px * ((long long)j + (long long)g.py * k);
+  }
 #pragma unroll
-  for (int dz = -1; dz <= 1; ++dz)
-#pragma unroll
-    for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-      for (int dx = -1; dx <= 1; ++dx) {
-        const long long c = c0 + dx + (long long)g.px * (dy + (long long)g.py * dz);
-        *reinterpret_cast<uint4*>(tile + tc::kmaj(r, f, FIN)) = field[c];
-        f += 8;
-      }
-#pragma unroll
-  for (; f < FIN; f += 8) *reinterpret_cast<uint4*>(tile + tc::kmaj(r, f, FIN)) = make_uint4(0, 0, 0, 0);
+  for (int u = 0; u < 16; ++u) {
+    const int ch = 16 * h + u;  // chunk = stencil point ((dz+1)*9 + (dy+1)*3 + (dx+1)), 27..31 padding
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (t >= 0 && ch < 27) {
+      const int dz = ch / 9 - 1, dy = (ch / 3) % 3 - 1, dx = ch % 3 - 1;
+      v = field[c0 + dx + (long long)g.px * (dy + (long long)g.py * dz)];
+    }
+    *reinterpret_cast<uint4*>(tile + tc::kmaj(r, 8 * ch, FIN)) = v;
+  }
 }
 
 // Inference: Y[n][8] = raw network outputs.  GRID = false: rows of the BF16
 // feature matrix X; GRID = true: the features of the n interior cells of the
 // grid d, gathered straight into the input tile.
+// 256 threads: thread (row r, half h) = (tid % 128, tid / 128) gathers half
+// of row r's input chunks and takes the activation columns [32 h, 32 h + 32)
+// of row r in the epilogues (TMEM lane quarter r / 32 = warp % 4), so two
+// warps share each TMEM lane quarter and the GELU work.
 template <bool GRID>
-__global__ void __launch_bounds__(128, 2)
+__global__ void __launch_bounds__(256, 2)
     k_mlp_infer(const __nv_bfloat16* __restrict__ X, Dev<float> d, const uint4* __restrict__ field, int n, MlpW w,
                 float* __restrict__ Y, int* err) {
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tslot;
-  const int tid = threadIdx.x, q = tid >> 5;
-  if (q == 0) tc::tmem_alloc(&tslot, 256);
+  const int tid = threadIdx.x, warp = tid >> 5, q = warp & 3, row = tid & 127, half = tid >> 7;
+  if (warp == 0) tc::tmem_alloc(&tslot, 256);
   if (tid == 0) tc::bar_init(&bar, 1);
   stage_w(sm + I_W1, w.w1, NH, FIN);
   stage_w(sm + I_W2, w.w2, NH, NH);
@@ -454,12 +459,10 @@ __global__ void __launch_bounds__(128, 2)
   const int ntiles = (n + 127) / 128;
   for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     if (GRID) {
-      const long long g = (long long)tile * 128 + tid;
-      if (g < n) gather_row(d, field, g, XS, tid);
-      else
-        for (int f = 0; f < FIN; f += 8) *reinterpret_cast<uint4*>(XS + tc::kmaj(tid, f, FIN)) = make_uint4(0, 0, 0, 0);
+      const long long g = (long long)tile * 128 + row;
+      gather_half_row(d, field, g < n ? g : -1, XS, row, half);
     } else {
-      for (int t = tid; t < 128 * (FIN / 8); t += 128) {
+      for (int t = tid; t < 128 * (FIN / 8); t += blockDim.x) {
         const int r = t >> 5, c8 = (t & 31) * 8;
         const int g = tile * 128 + r;
         uint4 v = make_uint4(0, 0, 0, 0);
@@ -471,30 +474,34 @@ __global__ void __launch_bounds__(128, 2)
     if (tid == 0) gemm(tb + T_D1, s0 + I_X, s0 + I_W1, NH, FIN, false);
     sync_mma();
     if (!ok) break;
-    for (int c0 = 0; c0 < NH; c0 += 16) {  // H1 over the consumed input tile
+    for (int c0 = 32 * half; c0 < 32 * half + 32; c0 += 16) {  // H1 over the consumed input tile
       float z[16];
       tc::tmem_ld16(tc::tmem_at(tb + T_D1, q, c0), z);
-      gelu16_store(XS, tid, c0, z, w.p + OB1);
+      gelu16_store(XS, row, c0, z, w.p + OB1);
     }
     publish();
     if (tid == 0) gemm(tb + T_D2, s0 + I_X, s0 + I_W2, NH, NH, false);
     sync_mma();
     if (!ok) break;
-    for (int c0 = 0; c0 < NH; c0 += 16) {  // H2 over H1 (consumed)
+    for (int c0 = 32 * half; c0 < 32 * half + 32; c0 += 16) {  // H2 over H1 (consumed)
       float z[16];
       tc::tmem_ld16(tc::tmem_at(tb + T_D2, q, c0), z);
-      gelu16_store(XS, tid, c0, z, w.p + OB2);
+      gelu16_store(XS, row, c0, z, w.p + OB2);
     }
     publish();
     if (tid == 0) gemm(tb + T_D3, s0 + I_X, s0 + I_W3, NO, NH, false);
     sync_mma();
     if (!ok) break;
-    float y[16];
-    tc::tmem_ld16(tc::tmem_at(tb + T_D3, q, 0), y);
-    const long long g = (long long)tile * 128 + tid;
-    if (g < n)
-      for (int o = 0; o < NOUT; ++o) Y[g * NOUT + o] = y[o] + w.p[OB3 + o];
+    if (half == 0) {
+      float y[16];
+      tc::tmem_ld16(tc::tmem_at(tb + T_D3, q, 0), y);
+      const long long g = (long long)tile * 128 + row;
+      if (g < n)
+        for (int o = 0; o < NOUT; ++o) Y[g * NOUT + o] = y[o] + w.p[OB3 + o];
+    }
+    tc::fence_before();
     __syncthreads();
+    tc::fence_after();
   }
   if (!ok) {
     if (tid == 0) atomicExch(err, 1);
@@ -502,7 +509,7 @@ __global__ void __launch_bounds__(128, 2)
   }
   tc::fence_before();
   __syncthreads();
-  if (q == 0) tc::tmem_free(tb, 256);
+  if (warp == 0) tc::tmem_free(tb, 256);
 }
 
 // Adam (Kingma & Ba, 2015) on the FP32 parameters.
@@ -552,16 +559,26 @@ __global__ void k_iota(int* idx, int count, long long off) {
 }
 
 // ------------------------------------------------------- solver coupling
-// Domain sums of the hydro increments y[0..4] (for a conservative correction).
-__global__ void k_mlp_sums(const float* __restrict__ Y, long long n, double* sums) {
+// Domain sums of the hydro increments y[0..4] (for a conservative correction):
+// FP64 per thread, then per warp and per block (256 threads), one atomic per
+// block and variable.
+__global__ void __launch_bounds__(256) k_mlp_sums(const float* __restrict__ Y, long long n, double* sums) {
+  __shared__ double part[8][5];
   double a[5] = {0, 0, 0, 0, 0};
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
 #pragma unroll
     for (int q = 0; q < 5; ++q) a[q] += (double)Y[t * NOUT + q];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int q = 0; q < 5; ++q) {
     for (int m = 16; m > 0; m >>= 1) a[q] += __shfl_xor_sync(0xffffffffu, a[q], m);
-    if ((threadIdx.x & 31) == 0) atomicAdd(sums + q, a[q]);
+    if (lane == 0) part[wid][q] = a[q];
+  }
+  __syncthreads();
+  if (threadIdx.x < 5) {
+    double b = 0.0;
+    for (int w2 = 0; w2 < 8; ++w2) b += part[w2][threadIdx.x];
+    atomicAdd(sums + threadIdx.x, b);
   }
 }
 
@@ -572,6 +589,9 @@ __global__ void k_mlp_sums(const float* __restrict__ Y, long long n, double* sum
 __global__ void k_mlp_apply_hydro(Dev<float> d, MlpNorm nm, const float* __restrict__ Y, const double* sums) {
   const Geom& g = d.g;
   const long long n = (long long)g.nx0 * g.ny0 * g.nz0;
+  __shared__ float mean[5];  // domain means of the increments, divided once per block
+  if (threadIdx.x < 5) mean[threadIdx.x] = (float)(sums[threadIdx.x] / (double)n);
+  __syncthreads();
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
   const int i = (int)(t % g.nx0) + g.ng;
@@ -583,7 +603,7 @@ __global__ void k_mlp_apply_hydro(Dev<float> d, MlpNorm nm, const float* __restr
   const float rho = d.rho[c], u = d.vx[c], v = d.vy[c], w = d.vz[c];
   float U[5] = {rho, rho * u, rho * v, rho * w, 0.5f * rho * (u * u + v * v + w * w) + d.p[c] / gm1};
 #pragma unroll
-  for (int a = 0; a < 5; ++a) U[a] += (y[a] - (float)(sums[a] / (double)n)) * nm.scale[a];
+  for (int a = 0; a < 5; ++a) U[a] += (y[a] - mean[a]) * nm.scale[a];
   const float rn = U[0];
   const float pn = gm1 * (U[4] - 0.5f * (U[1] * U[1] + U[2] * U[2] + U[3] * U[3]) / rn);
   if (rn > 0.0f && pn > 0.0f) {
@@ -908,7 +928,7 @@ int mhd_mlp_forward(void* h, const uint16_t* x, int64_t n, float* y) {
   }
   cudaMemcpy(dx, x, (size_t)n * FIN * 2, cudaMemcpyHostToDevice);
   const int tiles = (int)((n + 127) / 128);
-  k_mlp_infer<false><<<tiles < 2 * m->sms ? tiles : 2 * m->sms, 128, I_TOTAL>>>(dx, Dev<float>{}, nullptr, (int)n,
+  k_mlp_infer<false><<<tiles < 2 * m->sms ? tiles : 2 * m->sms, 256, I_TOTAL>>>(dx, Dev<float>{}, nullptr, (int)n,
                                                                                  wview(m), dy, m->err);
   cudaError_t e = cudaDeviceSynchronize();
   if (e == cudaSuccess) e = cudaMemcpy(y, dy, (size_t)n * NOUT * 4, cudaMemcpyDeviceToHost);
@@ -950,7 +970,7 @@ int mhd::mlp_correct(void* h, Dev<float>& d, cudaStream_t st) {
   uint4* field = reinterpret_cast<uint4*>(d.F[1][0]);
   const long long ncell = (long long)d.g.nx * d.g.ny * d.g.nz;
   k_mlp_features<<<(int)((ncell + 255) / 256), 256, 0, st>>>(d, m->norm, field);
-  k_mlp_infer<true><<<tiles < 2 * m->sms ? tiles : 2 * m->sms, 128, I_TOTAL, st>>>(nullptr, d, field, (int)n,
+  k_mlp_infer<true><<<tiles < 2 * m->sms ? tiles : 2 * m->sms, 256, I_TOTAL, st>>>(nullptr, d, field, (int)n,
                                                                                    wview(m), m->ys, m->err);
   if (!m->sums) MCK(cudaMalloc(&m->sums, 8 * sizeof(double)));
   MCK(cudaMemsetAsync(m->sums, 0, 8 * sizeof(double), st));
