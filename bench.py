@@ -44,8 +44,10 @@ sys.path.insert(0, str(ROOT))
 #   flux_z_update: read 8 cell fields + 8 divergences + U^n (5, stage 2
 #           only: 2.5 on average), write 5 primitives                     23.5
 #   emf: per edge family read v1, v2, b1, b2, vf, write E (3 launches)   18
-#   ct: read 3 face B + 3 EMFs (+3 B^n on stage 2: 1.5), write 3 face B   10.5
-WORDS = {"flux_x": 16, "flux_y": 24, "flux_z_update": 23.5, "emf": 18, "ct": 10.5}
+#   ct (CT fused with get_bxyz and vf, then the ghost shell): read 3 face B +
+#           3 EMFs (+3 B^n on stage 2: 1.5) + the new rho, v (4), write 3 face
+#           B + cell B and vf (4)                                            18.5
+WORDS = {"flux_x": 16, "flux_y": 24, "flux_z_update": 23.5, "emf": 18, "ct": 18.5}
 LAUNCHES = {"flux_x": 1, "flux_y": 1, "flux_z_update": 1, "emf": 3, "ct": 1}
 RECON_NAMES = {1: "PDM", 2: "TVD", 3: "WENO5", 4: "MPWENO5", 5: "TVD-MC"}
 # the sources of the step kernels: counts and traffic read from profiles/
@@ -69,6 +71,136 @@ def profile_file(name: str):
     d = json.loads(f.read_text())
     sha = d.get("kernels_sha16") if isinstance(d, dict) else None
     return d, {"file": f"profiles/{name}", "kernels_sha16": sha, "stale": sha != step_sources_sha16()}
+
+
+# kernel name -> launch family of the step (counts and traffic summaries)
+def _family(kernel: str) -> str | None:
+    k = kernel.split("(")[0]
+    if "k_cfl" in k:
+        return "dt"
+    if "k_emf_pdm" in k or "k_emf_weno" in k or "k_emf<" in k:
+        return "emf"
+    if "k_flux_sweep" in k or "k_flux_t" in k:
+        return "flux_y" if ", 1," in k.split("<", 1)[1][:12] else "flux_z_update"
+    if "k_flux<" in k:
+        return "flux_x"
+    if "k_ct_fill" in k or "k_fill_bxyz" in k or "k_update_b" in k:
+        return "ct"
+    return None
+
+
+def _ncu_rows(csv_path: str):
+    """(kernel name, {metric: value}) per launch of an ncu --csv log, in order."""
+    import csv
+    rows = list(csv.reader(open(csv_path)))
+    hi = next(i for i, r in enumerate(rows) if r and r[0] == "ID")
+    h = rows[hi]
+    ix = {k: i for i, k in enumerate(h)}
+    out, cur = [], None
+    for r in rows[hi + 1:]:
+        if len(r) < len(h):
+            continue
+        key = (r[ix["ID"]], r[ix["Kernel Name"]])
+        if cur is None or cur[0] != key:
+            cur = (key, {})
+            out.append(cur)
+        v = r[ix["Metric Value"]].replace(",", "")
+        try:
+            cur[1][r[ix["Metric Name"]]] = float(v)
+        except ValueError:
+            pass
+    return [(k[1], m) for k, m in out]
+
+
+# launches per RK2 step of each kernel class, for per-step sums of captures
+# that hold only some of a class's launches
+_PER_STEP = {"dt": 1, "emf": 6, "flux_x": 2, "flux_y": 2, "flux_z_update": 2, "ct_fill": 2, "shell": 2}
+
+
+def _class(kernel: str) -> str | None:
+    f = _family(kernel)
+    if f == "ct":
+        return "shell" if "k_fill_bxyz" in kernel else "ct_fill"
+    return f
+
+
+def _step_sums(paths, metric_fn) -> dict:
+    """Per-step sums of metric_fn(metrics) per launch family over ncu captures
+    (comma-separated csv paths, one kernel each, a few launches), each class
+    scaled from its captured launches to its launches per RK2 step."""
+    acc, cnt = {}, {}
+    for path in paths.split(","):
+        for name, m in _ncu_rows(path):
+            c = _class(name)
+            if c is None:
+                continue
+            v = metric_fn(m)
+            for key, val in v.items():
+                acc.setdefault(c, {}).setdefault(key, 0.0)
+                acc[c][key] += val
+            cnt[c] = cnt.get(c, 0) + 1
+    fam = {}
+    for c, vals in acc.items():
+        f = "ct" if c in ("ct_fill", "shell") else c
+        e = fam.setdefault(f, {})
+        for key, val in vals.items():
+            e[key] = e.get(key, 0.0) + val * _PER_STEP[c] / cnt[c]
+    return fam
+
+
+def _counts_of(m) -> dict:
+    flop = (m.get("smsp__sass_thread_inst_executed_op_fadd_pred_on.sum", 0)
+            + m.get("smsp__sass_thread_inst_executed_op_fmul_pred_on.sum", 0)
+            + 2 * m.get("smsp__sass_thread_inst_executed_op_ffma_pred_on.sum", 0)
+            + 2 * m.get("smsp__sass_thread_inst_executed_op_fadd2_pred_on.sum", 0)
+            + 2 * m.get("smsp__sass_thread_inst_executed_op_fmul2_pred_on.sum", 0)
+            + 4 * m.get("smsp__sass_thread_inst_executed_op_ffma2_pred_on.sum", 0))
+    return {"flop": flop, "inst": m.get("smsp__thread_inst_executed.sum", 0),
+            "us_ncu": m.get("gpu__time_duration.sum", 0) / 1e3,
+            "dram_bytes": m.get("dram__bytes_read.sum", 0) + m.get("dram__bytes_write.sum", 0)}
+
+
+def ingest_counts(a):
+    """profiles/counts_pdm_rk2_fp32.json and profiles/traffic.json from ncu
+    captures of `bench.py --n N --tiles T,E --profile-only`, one kernel per
+    capture (--ingest-counts a.csv,b.csv,...): FP32 flop and thread
+    instructions per zone-update of one RK2 step, per family and in total, and
+    DRAM bytes per launch; stamped with the hash of the step sources they were
+    captured on.  Traffic is scaled from the N^3 capture to a 256^3 launch by
+    the units processed (x (256/N)^3)."""
+    fam = _step_sums(a.ingest_counts, _counts_of)
+    n3 = float(a.n) ** 3
+    tot = {"flop": sum(e["flop"] for e in fam.values()) / n3, "inst": sum(e["inst"] for e in fam.values()) / n3}
+    td, ey = (int(t) for t in a.tiles.split(","))
+    key = f"td{td}_ei{ey}"
+    p = ROOT / "profiles" / "counts_pdm_rk2_fp32.json"
+    d = json.loads(p.read_text()) if p.exists() else {}
+    if d.get("kernels_sha16") != step_sources_sha16():
+        d = {}  # counts of older kernels do not mix with these
+    d["kernels_sha16"] = step_sources_sha16()
+    d["source"] = (f"ncu --metrics smsp__thread_inst_executed.sum, sm__sass_thread_inst_executed_op_"
+                   f"{{fadd,fmul,ffma,fadd2,fmul2,ffma2}}_pred_on.sum, dram__bytes_{{read,write}}.sum, one kernel "
+                   f"per capture (-k, <= 4 launches) of bench.py --n {a.n} --tiles T,E --steps 2 --warmup 3 "
+                   f"--profile-only, scaled to one RK2 step, per zone-update of the {a.n}^3 grid; T = 32 is the "
+                   f"column-sweep face shape")
+    d["units"] = {"flop": "FP32 flop (fadd + fmul + 2 ffma + 2 fadd2 + 2 fmul2 + 4 ffma2 thread instructions)",
+                  "inst": "thread instructions executed"}
+    d.setdefault("per_zone_update", {})[key] = {k: round(v, 1) for k, v in tot.items()}
+    d.setdefault("per_family_per_step", {})[key] = {
+        f: {"flop": round(e["flop"] / n3, 1), "inst": round(e["inst"] / n3, 1), "us_ncu": round(e["us_ncu"], 1)}
+        for f, e in fam.items()}
+    p.write_text(json.dumps(d, indent=1) + "\n")
+    scale = (256.0 / a.n) ** 3
+    launches = {"emf": 6, "flux_x": 2, "flux_y": 2, "flux_z_update": 2, "ct": 2, "dt": 1}
+    t = {"kernels_sha16": step_sources_sha16(),
+         "source": f"dram__bytes_read.sum + dram__bytes_write.sum of the same captures at {a.n}^3, per launch of "
+                   f"each family (CT + bxyz and its ghost shell counted as one), scaled x{scale:g} to a 256^3 launch "
+                   f"(traffic grows with the units processed: every array of these kernels exceeds L2 at 256^3)",
+         "captured_at": a.n,
+         "per_launch": {f: e["dram_bytes"] * scale / launches[f] for f, e in fam.items()},
+         "per_step_bytes_256": sum(e["dram_bytes"] for e in fam.values()) * scale}
+    (ROOT / "profiles" / "traffic.json").write_text(json.dumps(t, indent=1) + "\n")
+    print(json.dumps({"per_zone_update": d["per_zone_update"][key], "traffic": t["per_launch"]}))
 
 
 def bench_config(n: int, recon: int) -> dict:
@@ -97,6 +229,8 @@ def parse():
     ap.add_argument("--no-study", action="store_true",
                     help="skip the FP64 line and the error-at-equal-GPU-time table")
     ap.add_argument("--study-steps", type=int, default=20)
+    ap.add_argument("--ingest-counts", default=None,
+                    help="write profiles/counts_pdm_rk2_fp32.json and traffic.json from these ncu csvs (ingest_counts)")
     ap.add_argument("--ensemble-key", type=int, default=256,
                     help="grids of the batched ensemble measured after the timed region (0: skip)")
     return ap.parse_args()
@@ -507,6 +641,9 @@ def run_ensemble(a):
 
 def main():
     a = parse()
+    if a.ingest_counts:
+        ingest_counts(a)
+        return
     if a.ensemble:
         run_ensemble(a)
         return

@@ -70,3 +70,30 @@ def test_reference_arm_runs_the_same_config_as_ours():
     assert line["config"] == bench.bench_config(12, 1)
     assert line["e2e"]["value"] == line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port"
+
+
+def test_profile_ingest_maps_kernels_to_families(tmp_path):
+    """The ncu-csv reader of bench.py groups a step's launches into the launch
+    families whose counts and traffic the bench line reports."""
+    import bench
+    names = {
+        "void mhd::k_cfl<float, 0, 0>(mhd::KArg<T1, T3>, int)": "dt",
+        "void mhd::k_emf_pdm<float, 1, 32, 1, 8, 256, 0, 0>(mhd::KArg<T1, T8>)": "emf",
+        "void mhd::k_flux<float, 1, 0, 0, 0>(mhd::KArg<T1, T5>)": "flux_x",
+        "void mhd::k_flux_sweep<float, 1, 0, 1>(mhd::KArg<T1, T3>)": "flux_y",
+        "void mhd::k_flux_sweep<float, 2, 0, 1>(mhd::KArg<T1, T3>)": "flux_z_update",
+        "void mhd::k_ct_fill<float, 0>(mhd::KArg<T1, T2>, int)": "ct",
+        "void mhd::k_fill_bxyz<float, 0, 0>(mhd::KArg<T1, T3>, int, int)": "ct",
+    }
+    for k, fam in names.items():
+        assert bench._family(k) == fam, k
+    csv = tmp_path / "c.csv"
+    lines = ['"ID","Kernel Name","Metric Name","Metric Unit","Metric Value"']
+    for i, k in enumerate(names):
+        lines.append(f'"{i}","{k}","gpu__time_duration.sum","ns","1,000"')
+        lines.append(f'"{i}","{k}","smsp__thread_inst_executed.sum","inst","{100 * (i + 1)}"')
+    csv.write_text("\n".join(lines) + "\n")
+    rows = bench._ncu_rows(str(csv))
+    assert [r[0] for r in rows] == list(names)
+    assert rows[2][1]["smsp__thread_inst_executed.sum"] == 300.0
+    assert rows[0][1]["gpu__time_duration.sum"] == 1000.0
