@@ -269,8 +269,11 @@ void carve(Handle* h, Dev<T>& d, char* base) {
   int nq = (h->prm.stepop == MHD_STEP_AB2) ? 11 : 8;
   for (int i = 0; i < 11; ++i) d.q[i] = (i < nq) ? next() : nullptr;
   for (int i = 0; i < 11; ++i) d.h[i] = (h->prm.stepop == MHD_STEP_AB2) ? next() : nullptr;
-  for (int ax = 0; ax < 3; ++ax)
-    for (int q = 0; q < 8; ++q) d.F[ax][q] = next();
+  // x-face fluxes only: the y / z faces are consumed inside the sweeps / face
+  // tiles; the kernel-level debug entry point gives them scratch of its own
+  for (int q = 0; q < 8; ++q) d.F[0][q] = next();
+  for (int ax = 1; ax < 3; ++ax)
+    for (int q = 0; q < 8; ++q) d.F[ax][q] = nullptr;
   for (int e = 0; e < 3; ++e) d.E[e] = next();
   d.vf = next();
   d.dx = h->geo; d.dy = h->geo + g.nx; d.dz = h->geo + g.nx + g.ny;
@@ -329,7 +332,7 @@ MetricOut metric_out(Handle* h) {
 }
 
 size_t n_arrays(const mhd_params& p, bool metric) {
-  size_t n = 11 + 5 + 3 + 8 + ((p.stepop == MHD_STEP_AB2) ? 22 : 8) + 24 + 3 + 1 + (metric ? 6 : 0) +
+  size_t n = 11 + 5 + 3 + 8 + ((p.stepop == MHD_STEP_AB2) ? 22 : 8) + 8 + 3 + 1 + (metric ? 6 : 0) +
              ((p.emf == MHD_EMF_YEE) ? 12 : 0);
   return n;
 }
@@ -369,7 +372,7 @@ __global__ void k_to_f64(const T* __restrict__ src, int ex, int ey, int px, long
 
 template <typename T>
 double* f64_scratch(const Dev<T>& d) {
-  return reinterpret_cast<double*>(d.F[0][0]);  // 24 x vol x sizeof(T) bytes, >= one FP64 array
+  return reinterpret_cast<double*>(d.F[0][0]);  // 8 x vol x sizeof(T) bytes, >= one FP64 array
 }
 
 template <typename T>
@@ -1043,6 +1046,16 @@ template <typename T, bool M>
 static int dbg_flux_t(Handle* h, double* out) {
   const Geom& g = h->g;
   Dev<T> d = at_par(dev<T>(h), h->par);
+  // the y / z face fluxes go to scratch of this call (the handle keeps none)
+  T* yz = nullptr;
+  if (cudaMalloc(&yz, 16 * (size_t)g.vol * sizeof(T)) != cudaSuccess)
+    return fail(MHD_E_NOMEM, "debug fluxes: device allocation failed");
+  for (int ax = 1; ax < 3; ++ax)
+    for (int q = 0; q < 8; ++q) d.F[ax][q] = yz + (size_t)((ax - 1) * 8 + q) * (size_t)g.vol;
+  struct Free {
+    T* p;
+    ~Free() { cudaFree(p); }
+  } release{yz};
   Launch<T, M>::fluxes(d, state_inp(d), h->st);
   CK(cudaGetLastError());
   std::vector<T> host((size_t)g.vol);

@@ -345,9 +345,6 @@ __device__ __forceinline__ typename Pr<T>::V tap8p(typename Pr<T>::V a0, typenam
 #ifndef MHD_RECON_PACKED
 #define MHD_RECON_PACKED 1
 #endif
-#ifndef MHD_EMF_PACKED  // the EMF corner limiter on (v_a1, v_a2) pairs
-#define MHD_EMF_PACKED 1
-#endif
 namespace p2 {
 __device__ __forceinline__ float2 K(float c) { return make_float2(c, c); }
 __device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
@@ -358,50 +355,6 @@ __device__ __forceinline__ float2 rcp(float2 a) { return make_float2(__fdividef(
 __device__ __forceinline__ float2 rsq(float2 a) { return make_float2(rsqrtf(a.x), rsqrtf(a.y)); }
 }  // namespace p2
 
-// The PDM part of the corner velocity (corner_pdm_vals) for both components at
-// once (lanes .x = v_a1, .y = v_a2, from the pair-interleaved tile), FP32:
-// the differences, scalings and the 4-quadrant mean on the packed pipe; the
-// quadrant choices, clamps, signs and limiter per lane, as pdm_half does,
-// with the same rounding per lane.
-__device__ __forceinline__ float2 pdm_half_x2(float2 lo, float2 hi, float2 outer, bool lx, bool ly, float2 fi,
-                                              float pdmb) {
-  const float2 kp = p2::K(pdmb);
-  float2 fii;
-  fii.x = mx(mn(lo.x, hi.x), mn(fi.x, mx(lo.x, hi.x)));
-  fii.y = mx(mn(lo.y, hi.y), mn(fi.y, mx(lo.y, hi.y)));
-  const float2 a = p2::sub(lo, outer), b = p2::sub(outer, hi);
-  const float2 dn = p2::mul(kp, make_float2(lx ? a.x : b.x, ly ? a.y : b.y));
-  const float2 hl = p2::mul(kp, p2::sub(hi, lo));
-  const float2 t = p2::sub(make_float2(lx ? lo.x : hi.x, ly ? lo.y : hi.y), fii);
-  const float sx = sgn1(hl.x), sy = sgn1(hl.y);
-  const float qx = fabsf(sgn1(dn.x) + sx), qy = fabsf(sgn1(dn.y) + sy);
-  const float xx = sx * mx(0.0f, fabsf(t.x) - qx * fabsf(dn.x));
-  const float xy = sy * mx(0.0f, fabsf(t.y) - qy * fabsf(dn.y));
-  return make_float2(lx ? fii.x - xx : fii.x + xx, ly ? fii.y - xy : fii.y + xy);
-}
-
-__device__ __forceinline__ float2 corner_pdm_x2(float2 m11, float2 m21, float2 m12, float2 m01, float2 p11,
-                                                float2 m02, float2 m10, float2 m20, float2 m1p, float2 c0,
-                                                float2 p10, float2 p01, float2 vi, float pd) {
-  // dif signs per quadrant: |a - b| - |c - b| (the absolute values fold into the lane's add)
-  float2 u = p2::sub(m21, m11), w = p2::sub(m12, m11);
-  const bool b00x = fabsf(u.x) - fabsf(w.x) >= 0.0f, b00y = fabsf(u.y) - fabsf(w.y) >= 0.0f;
-  u = p2::sub(p11, m01); w = p2::sub(m02, m01);
-  const bool b10x = fabsf(u.x) - fabsf(w.x) >= 0.0f, b10y = fabsf(u.y) - fabsf(w.y) >= 0.0f;
-  u = p2::sub(m20, m10); w = p2::sub(m1p, m10);
-  const bool b01x = fabsf(u.x) - fabsf(w.x) >= 0.0f, b01y = fabsf(u.y) - fabsf(w.y) >= 0.0f;
-  u = p2::sub(p10, c0); w = p2::sub(p01, c0);
-  const bool b11x = fabsf(u.x) - fabsf(w.x) >= 0.0f, b11y = fabsf(u.y) - fabsf(w.y) >= 0.0f;
-  auto sel = [](bool bx, bool by, float2 a, float2 b) { return make_float2(bx ? a.x : b.x, by ? a.y : b.y); };
-  const float2 v00 = pdm_half_x2(m11, sel(b00x, b00y, m01, m10), sel(b00x, b00y, m21, m12), true, true, vi, pd);
-  const float2 v10 = pdm_half_x2(sel(b10x, b10y, m11, m01), sel(b10x, b10y, m01, c0), sel(b10x, b10y, p11, m02),
-                                 !b10x, !b10y, vi, pd);
-  const float2 v01 = pdm_half_x2(sel(b01x, b01y, m10, m11), sel(b01x, b01y, c0, m10), sel(b01x, b01y, m20, m1p),
-                                 b01x, b01y, vi, pd);
-  const float2 v11 = pdm_half_x2(sel(b11x, b11y, m10, m01), c0, sel(b11x, b11y, p10, p01), false, false, vi, pd);
-  return p2::mul(p2::K(0.25f), p2::add(p2::add(p2::add(v00, v01), v10), v11));
-}
-
 // corner_pdm of both components from pair-interleaved shared memory.
 template <typename T>
 __device__ __forceinline__ void corner_pdm_pair(const typename Pr<T>::V* __restrict__ v, int c, int s1, int s2,
@@ -410,14 +363,8 @@ __device__ __forceinline__ void corner_pdm_pair(const typename Pr<T>::V* __restr
   const V m11 = v[c - s1 - s2], m21 = v[c - 2 * s1 - s2], m12 = v[c - s1 - 2 * s2], m01 = v[c - s2];
   const V p11 = v[c + s1 - s2], m02 = v[c - 2 * s2], m10 = v[c - s1], m20 = v[c - 2 * s1];
   const V m1p = v[c - s1 + s2], c0 = v[c], p10 = v[c + s1], p01 = v[c + s2];
-  if constexpr (std::is_same<T, float>::value && MHD_EMF_PACKED) {
-    const float2 r = corner_pdm_x2(m11, m21, m12, m01, p11, m02, m10, m20, m1p, c0, p10, p01, vi, pd);
-    r0 = r.x;
-    r1 = r.y;
-  } else {
-    r0 = corner_pdm_vals(m11.x, m21.x, m12.x, m01.x, p11.x, m02.x, m10.x, m20.x, m1p.x, c0.x, p10.x, p01.x, vi.x, pd);
-    r1 = corner_pdm_vals(m11.y, m21.y, m12.y, m01.y, p11.y, m02.y, m10.y, m20.y, m1p.y, c0.y, p10.y, p01.y, vi.y, pd);
-  }
+  r0 = corner_pdm_vals(m11.x, m21.x, m12.x, m01.x, p11.x, m02.x, m10.x, m20.x, m1p.x, c0.x, p10.x, p01.x, vi.x, pd);
+  r1 = corner_pdm_vals(m11.y, m21.y, m12.y, m01.y, p11.y, m02.y, m10.y, m20.y, m1p.y, c0.y, p10.y, p01.y, vi.y, pd);
 }
 
 // Limited corner value of v at the edge whose two transverse axes have
@@ -514,14 +461,14 @@ template <typename T>
 inline KArg<T, false> one(const Dev<T>& d) { return KArg<T, false>{d}; }
 
 // Resident 256-thread blocks per SM requested for the cell passes (CFL, CT +
-// bxyz, fill).  Single grid: full occupancy at 32 registers.  Batched: each
+// bxyz, fill).  Single grid: none (0; they take 32 registers).  Batched: each
 // thread holds its grid's array pointers in registers (from the grid table,
 // not the constant bank), about 75 registers unbounded, which would leave 3
 // blocks per SM for these latency-bound passes; a budget keeps more resident.
 #ifndef MHD_BATCH_MINB
 #define MHD_BATCH_MINB 6
 #endif
-constexpr int pass_min_blocks(bool B) { return B ? MHD_BATCH_MINB : 8; }
+constexpr int pass_min_blocks(bool B) { return B ? MHD_BATCH_MINB : 0; }
 
 // ------------------------------------------------------------- small kernels
 template <typename T>

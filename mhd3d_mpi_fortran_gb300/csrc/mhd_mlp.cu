@@ -965,9 +965,9 @@ int mhd::mlp_correct(void* h, Dev<float>& d, cudaStream_t st) {
   if (rc) return rc;
   const int nb = (int)((n + 255) / 256);
   const int tiles = (int)((n + 127) / 128);
-  // the feature records go to the y-face flux arrays, scratch outside a step
+  // the feature records go to the x-face flux arrays, scratch outside a step
   // (4 consecutive FP32 arrays = one 16-byte record per padded cell index)
-  uint4* field = reinterpret_cast<uint4*>(d.F[1][0]);
+  uint4* field = reinterpret_cast<uint4*>(d.F[0][0]);
   const long long ncell = (long long)d.g.nx * d.g.ny * d.g.nz;
   k_mlp_features<<<(int)((ncell + 255) / 256), 256, 0, st>>>(d, m->norm, field);
   k_mlp_infer<true><<<tiles < 2 * m->sms ? tiles : 2 * m->sms, 256, I_TOTAL, st>>>(nullptr, d, field, (int)n,

@@ -212,6 +212,31 @@ def learned_study(n: int = 64, train_seeds=tuple(range(100, 108)), val_seed: int
     }
 
 
+def learned_cost(n: int = 128, steps: int = 50) -> dict:
+    """Cost of the learned correction: `steps` plain FP32 RK2 steps of the n^3
+    turbulence state against `steps` corrected steps (mhd_step_corrected, a
+    network with its outputs scaled to 1e-6 so the state stays that of the
+    plain run), host wall clock with the device synchronised at both ends."""
+    from . import learned
+    import time
+    s = ics.turbulence(n, seed=0)
+    prm = Params(n, n, n, precision=FP32, stepop=STEP_RK2, tau=0.8 * ics.cfl_dt(s, cfl=0.3))
+    mlp = learned.MLP(learned.init_params(0))
+    mlp.set_norm(np.zeros(8, np.float32), np.ones(8, np.float32), np.full(8, 1e-6, np.float32))
+    with MHDSolver(prm, s) as a:
+        a.step(5)
+        t0 = time.perf_counter()
+        a.step(steps)
+        plain = (time.perf_counter() - t0) / steps * 1e3
+        mlp.step_corrected(a, 5)
+        t0 = time.perf_counter()
+        mlp.step_corrected(a, steps)
+        corr = (time.perf_counter() - t0) / steps * 1e3
+    mlp.close()
+    return {"study": "learned_cost", "n": n, "steps": steps, "plain_ms_per_step": plain,
+            "corrected_ms_per_step": corr, "ratio": corr / plain}
+
+
 def learned_config5(n: int = 128, train_seeds=(100, 101, 102, 103), val_seed: int = 104, damp_seed: int = 105,
                     test_seeds=(200, 201), train_steps: int = 60, every: int = 10, sample: float = 0.125,
                     iters: int = 3000, steps: int = 200, damp_steps: int = 50, fp64_seed: int = 100,
@@ -270,7 +295,8 @@ def learned_config5(n: int = 128, train_seeds=(100, 101, 102, 103), val_seed: in
 def main(argv=None) -> None:
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["curvilinear", "precision", "learned", "learned_config5", "equal_time"])
+    ap.add_argument("study", choices=["curvilinear", "precision", "learned", "learned_config5", "learned_cost",
+                                      "equal_time"])
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--recons", default="1,5,3", help="precision study: reconop values (1 PDM, 5 TVD-MC, 3 WENO5)")
@@ -282,6 +308,8 @@ def main(argv=None) -> None:
     elif a.study == "equal_time":
         for r in tuple(int(r) for r in a.recons.split(",")):
             print(json.dumps(equal_time(a.n or 256, a.steps or 100, r)), flush=True)
+    elif a.study == "learned_cost":
+        print(json.dumps(learned_cost(a.n or 128, a.steps or 50)), flush=True)
     elif a.study == "learned_config5":
         print(json.dumps(learned_config5(a.n or 128, steps=a.steps or 200)), flush=True)
     elif a.study == "learned":
