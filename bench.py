@@ -78,7 +78,7 @@ def _family(kernel: str) -> str | None:
     k = kernel.split("(")[0]
     if "k_cfl" in k:
         return "dt"
-    if "k_emf_pdm" in k or "k_emf_weno" in k or "k_emf<" in k:
+    if "k_emf_pdm" in k or "k_emf_weno" in k or "k_emf<" in k or "k_emf_stream" in k or "k_emf_rows" in k:
         return "emf"
     if "k_flux_sweep" in k or "k_flux_t" in k:
         return "flux_y" if ", 1," in k.split("<", 1)[1][:12] else "flux_z_update"
@@ -114,13 +114,16 @@ def _ncu_rows(csv_path: str):
 
 # launches per RK2 step of each kernel class, for per-step sums of captures
 # that hold only some of a class's launches
-_PER_STEP = {"dt": 1, "emf": 6, "flux_x": 2, "flux_y": 2, "flux_z_update": 2, "ct_fill": 2, "shell": 2}
+_PER_STEP = {"dt": 1, "emf": 6, "emf_rows": 2, "flux_x": 2, "flux_y": 2, "flux_z_update": 2, "ct_fill": 2,
+             "shell": 2}
 
 
 def _class(kernel: str) -> str | None:
     f = _family(kernel)
     if f == "ct":
         return "shell" if "k_fill_bxyz" in kernel else "ct_fill"
+    if f == "emf" and "k_emf_rows" in kernel:
+        return "emf_rows"
     return f
 
 
@@ -141,7 +144,7 @@ def _step_sums(paths, metric_fn) -> dict:
             cnt[c] = cnt.get(c, 0) + 1
     fam = {}
     for c, vals in acc.items():
-        f = "ct" if c in ("ct_fill", "shell") else c
+        f = "ct" if c in ("ct_fill", "shell") else "emf" if c == "emf_rows" else c
         e = fam.setdefault(f, {})
         for key, val in vals.items():
             e[key] = e.get(key, 0.0) + val * _PER_STEP[c] / cnt[c]
@@ -194,7 +197,8 @@ def ingest_counts(a):
     launches = {"emf": 6, "flux_x": 2, "flux_y": 2, "flux_z_update": 2, "ct": 2, "dt": 1}
     t = {"kernels_sha16": step_sources_sha16(),
          "source": f"dram__bytes_read.sum + dram__bytes_write.sum of the same captures at {a.n}^3, per launch of "
-                   f"each family (CT + bxyz and its ghost shell counted as one), scaled x{scale:g} to a 256^3 launch "
+                   f"each family (CT + bxyz and its ghost shell counted as one, an EMF family with its share of the "
+                   f"boundary-row launch), scaled x{scale:g} to a 256^3 launch "
                    f"(traffic grows with the units processed: every array of these kernels exceeds L2 at 256^3)",
          "captured_at": a.n,
          "per_launch": {f: e["dram_bytes"] * scale / launches[f] for f, e in fam.items()},
@@ -528,8 +532,9 @@ def run_ours(a):
     fam_ms = {k: v / stages for k, v in fam.items()}  # per stage
     dom = max(WORDS, key=lambda k: fam_ms[k])
     hbm, peak_kind = peaks()
-    bytes_per_launch = WORDS[dom] * 4 * n ** 3 / LAUNCHES[dom]
-    launch_s = fam_ms[dom] * 1e-3 / LAUNCHES[dom]
+    nl = LAUNCHES[dom] + (1 if dom == "emf" and tiles[1] == 1 else 0)
+    bytes_per_launch = WORDS[dom] * 4 * n ** 3 / nl
+    launch_s = fam_ms[dom] * 1e-3 / nl
     achieved = bytes_per_launch / launch_s / 1e9
     traffic, traffic_prov = None, None
     tdat, traffic_prov = profile_file("traffic.json")
@@ -556,7 +561,8 @@ def run_ours(a):
     if rank != 0:
         return
     compute_roofs = roofs(zu / ws, clocks, a.recon, tiles)
-    launches_per_step = 2 + 2 * (3 + 3 + 1 + 1)
+    emf_launches = 4 if tiles[1] == 1 else 3  # slice streams: three families plus their boundary rows
+    launches_per_step = 2 + 2 * (emf_launches + 3 + 1 + 1)
     fp64 = None
     if study:
         ref = study["runs"][0]

@@ -263,10 +263,12 @@ int mhd_ensemble_time(void** handles, int32_t ngrids, int32_t nsteps, float* ms)
  * compiled for the FP32 Cartesian paths -- y/z face-tile length 4, 8 or 16 (8
  * only outside PDM)
  * or 32 (32: column sweeps of 32-cell segments with a register window) and
- * ei EMF tile 4x4 or 8x8 edges -- on the handle's own grid, `reps` timed
- * runs each, keeps the fastest and writes it to out[0] (tile length) and
- * out[1] (EMF tile).  The timed launches touch only scratch arrays, so the
- * state is unchanged, and every choice gives bit-identical steps.  Other
+ * the PDM EMF shape: 4 or 8 (shared-memory tiles, ei tile 4x4 or 8x8 edges)
+ * or 1 (slice streams: one edge column per thread, the default) -- on the
+ * handle's own grid, `reps` timed runs each, keeps the fastest and writes it
+ * to out[0] (tile length) and out[1] (EMF shape).  The timed launches touch
+ * only scratch arrays, so the state is unchanged, and every choice gives
+ * bit-identical steps.  Other
  * handles keep their fixed shapes (returned in out). */
 int mhd_autotune(void* handle, int32_t reps, int32_t out[2]);
 
@@ -275,7 +277,7 @@ int mhd_autotune(void* handle, int32_t reps, int32_t out[2]);
 int mhd_ensemble_autotune(void** handles, int32_t ngrids, int32_t reps, int32_t out[2]);
 
 /* Sets the launch shapes directly (no timing): face-tile length 4, 8, 16 or
- * 32 and ei EMF tile 4 or 8, for a reproducible configuration (profiling, or
+ * 32 and EMF shape 4, 8 or 1, for a reproducible configuration (profiling, or
  * shapes found by an earlier mhd_autotune).  Handles outside the tunable
  * path (FP64, metric mode, other reconstructions) accept only their fixed
  * shapes.  Every choice gives bit-identical steps. */

@@ -529,8 +529,9 @@ static int create_handle(const mhd_params* prm, const double* dx, const double* 
   h->prm = *prm;
   h->fp32 = (prm->precision == MHD_FP32);
   h->metric = metric;
-  h->tile_ey = h->fp32 ? 8 : 4;
-  // the column sweeps are the fastest face shape at production sizes (the autotuner may still pick a tile)
+  // the column sweeps and the slice-streamed EMF are the fastest FP32 shapes at
+  // production sizes (the autotuner may still pick tiles)
+  h->tile_ey = (h->fp32 && !metric) ? kEmfStream : h->fp32 ? 8 : 4;
   h->tile_td = (h->fp32 && !metric) ? kSweepTile : 8;
   Geom& g = h->g;
   g.nx0 = prm->nx0; g.ny0 = prm->ny0; g.nz0 = prm->nz0;
@@ -1451,7 +1452,7 @@ int mhd_set_tiles(void* handle, int32_t face_tile, int32_t ei_tile) {
   bool ok_td = false, ok_ey = false;
   for (int td : kTileTD) ok_td |= td == face_tile;
   for (int ey : kTileEY) ok_ey |= ey == ei_tile;
-  if (!ok_td || !ok_ey) return fail(MHD_E_ARG, "face tile must be 4, 8, 16 or 32 and ei tile 4 or 8");
+  if (!ok_td || !ok_ey) return fail(MHD_E_ARG, "face tile must be 4, 8, 16 or 32 and EMF shape 4, 8 (ei tile) or 1 (slice streams)");
   int rc = wait_stream(h);
   if (rc) return rc;
   h->tile_td = face_tile;

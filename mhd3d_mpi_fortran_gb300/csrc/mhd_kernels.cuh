@@ -206,13 +206,19 @@ struct Prm {
 
 // One-sided face states of f at the low face of element c along stride s
 // (reconstruct_3d for dirs 1-3, mhd3d3.f90:833-860).
+// PDM face states from the 8 taps a0..a7 (cells c-4 .. c+3 along the
+// reconstruction axis; the face at the low side of c).
+template <typename T>
+__device__ __forceinline__ void recon_pdm8(T a0, T a1, T a2, T a3, T a4, T a5, T a6, T a7, T pdmb, T& fl, T& fr) {
+  const T fi = tap8(a0, a1, a2, a3, a4, a5, a6, a7);
+  pdm2(a2, a3, a4, a5, fi, pdmb, fl, fr);
+}
+
 template <typename T, int RECON, typename I>
 __device__ __forceinline__ void recon_face(const T* __restrict__ f, I c, I s, const Prm<T>& P, T& fl, T& fr) {
   if (RECON == R_PDM) {
-    T a0 = f[c - 4 * s], a1 = f[c - 3 * s], a2 = f[c - 2 * s], a3 = f[c - s];
-    T a4 = f[c], a5 = f[c + s], a6 = f[c + 2 * s], a7 = f[c + 3 * s];
-    T fi = tap8(a0, a1, a2, a3, a4, a5, a6, a7);
-    pdm2(a2, a3, a4, a5, fi, P.pdmb, fl, fr);
+    recon_pdm8(f[c - 4 * s], f[c - 3 * s], f[c - 2 * s], f[c - s], f[c], f[c + s], f[c + 2 * s], f[c + 3 * s], P.pdmb,
+               fl, fr);
   } else if (RECON == R_TVD || RECON == R_TVDMC) {
     T fm2 = f[c - 2 * s], fm1 = f[c - s], f0 = f[c], fp1 = f[c + s];
     T fi = (fm1 + f0) / T(2);
@@ -1473,6 +1479,41 @@ __global__ void __launch_bounds__(128, kSweepMinB)
 // edge whose upper cell is c (get_eijk_LFM, 1754-1856).  a1 = E+1, a2 = E+2
 // (cyclic): v1 = v_a1, v2 = v_a2; b1 = B_a1 reconstructed along a2 and
 // upwinded by sign(v2); b2 = B_a2 reconstructed along a1, upwinded by sign(v1).
+// E of an edge from its corner velocities, the one-sided face states of b1
+// and b2 and eta = 0.25 (vf[c-s1-s2] + vf[c-s2] + vf[c] + vf[c-s1]): the
+// upwinded convective term plus the resistive term (metric: g_e and |dl_e|).
+template <typename T>
+__device__ __forceinline__ T eta4(T a, T b, T c, T e) {
+  return T(0.25) * (a + b + c + e);
+}
+template <typename T, int E, bool M, typename I>
+__device__ __forceinline__ T emf_value(const Dev<T>& d, I c, T v1av, T v2av, T b1l, T b1r, T b2l, T b2r, T eta) {
+  const T b1u = (v2av >= T(0)) ? b1l : b1r;
+  const T b2u = (v1av >= T(0)) ? b2l : b2r;
+  const T e = -v1av * b2u + v2av * b1u;
+  if (M)  // E.dl: g_e * (convective term) + eta |dl_e| * (resistive term)
+    return (T)d.m.ge[E][c] * e + eta * (T)d.m.dl[E][c] * (b1l + b2r - b1r - b2l);
+  return e + eta * (b1l + b2r - b1r - b2l);
+}
+
+// One edge of family E from global memory (upper cell index c).
+template <typename T, int RECON, int E, bool M>
+__device__ __forceinline__ void emf_edge(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, long long c) {
+  const long long st[3] = {1, (long long)d.g.px, d.g.plane};
+  constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
+  const long long s1 = st[A1], s2 = st[A2];
+  const T* vel[3] = {in.vx, in.vy, in.vz};
+  const T* fb[3] = {in.bi, in.bj, in.bk};
+  const T v1av = corner_vel<T, RECON>(vel[A1], c, s1, s2, P);
+  const T v2av = corner_vel<T, RECON>(vel[A2], c, s1, s2, P);
+  T b1l, b1r, b2l, b2r;
+  recon_face<T, RECON>(fb[A1], c, s2, P, b1l, b1r);
+  recon_face<T, RECON>(fb[A2], c, s1, P, b2l, b2r);
+  const T* vf = d.vf;
+  const T eta = eta4(vf[c - s1 - s2], vf[c - s2], vf[c], vf[c - s1]);
+  d.E[E][c] = emf_value<T, E, M>(d, c, v1av, v2av, b1l, b1r, b2l, b2r, eta);
+}
+
 template <typename T, int RECON, int E, bool M>
 __global__ void k_emf(Dev<T> d, Inp<T> in, Prm<T> P) {
   const Geom& g = d.g;
@@ -1481,27 +1522,7 @@ __global__ void k_emf(Dev<T> d, Inp<T> in, Prm<T> P) {
   int k = blockIdx.z + g.ng;
   int ni = g.nx0 + (E != 0), nj = g.ny0 + (E != 1), nk = g.nz0 + (E != 2);
   if (i >= g.ng + ni || j >= g.ng + nj || k >= g.ng + nk) return;
-  long long c = idx3<T>(g, i, j, k);
-  const long long st[3] = {1, (long long)g.px, g.plane};
-  constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
-  const long long s1 = st[A1], s2 = st[A2];
-  const T* vel[3] = {in.vx, in.vy, in.vz};
-  const T* fb[3] = {in.bi, in.bj, in.bk};
-  T v1av = corner_vel<T, RECON>(vel[A1], c, s1, s2, P);
-  T v2av = corner_vel<T, RECON>(vel[A2], c, s1, s2, P);
-  T b1l, b1r, b2l, b2r;
-  recon_face<T, RECON>(fb[A1], c, s2, P, b1l, b1r);
-  recon_face<T, RECON>(fb[A2], c, s1, P, b2l, b2r);
-  T b1u = (v2av >= T(0)) ? b1l : b1r;
-  T b2u = (v1av >= T(0)) ? b2l : b2r;
-  T e = -v1av * b2u + v2av * b1u;
-  const T* vf = d.vf;
-  T eta = T(0.25) * (vf[c - s1 - s2] + vf[c - s2] + vf[c] + vf[c - s1]);
-  if (M)  // E.dl: g_e * (convective term) + eta |dl_e| * (resistive term)
-    e = (T)d.m.ge[E][c] * e + eta * (T)d.m.dl[E][c] * (b1l + b2r - b1r - b2l);
-  else
-    e = e + eta * (b1l + b2r - b1r - b2l);
-  d.E[E][c] = e;
+  emf_edge<T, RECON, E, M>(d, in, P, idx3<T>(g, i, j, k));
 }
 
 // Shared-memory tiled EMF of family E for PDM (the default deck's
@@ -1634,16 +1655,9 @@ __device__ __forceinline__ void emf_pdm_tile(const Dev<T>& d, const Inp<T>& in, 
     T b1l, b1r, b2l, b2r;
     recon_face<T, R_PDM>(fb[A1], c, s2, P, b1l, b1r);
     recon_face<T, R_PDM>(fb[A2], c, s1, P, b2l, b2r);
-    T b1u = (v2av >= T(0)) ? b1l : b1r;
-    T b2u = (v1av >= T(0)) ? b2l : b2r;
-    T ee = -v1av * b2u + v2av * b1u;
     const T* vf = d.vf;
-    T eta = T(0.25) * (vf[c - s1 - s2] + vf[c - s2] + vf[c] + vf[c - s1]);
-    if (M)
-      ee = (T)d.m.ge[E][c] * ee + eta * (T)d.m.dl[E][c] * (b1l + b2r - b1r - b2l);
-    else
-      ee = ee + eta * (b1l + b2r - b1r - b2l);
-    d.E[E][c] = ee;
+    const T eta = eta4(vf[c - s1 - s2], vf[c - s2], vf[c], vf[c - s1]);
+    d.E[E][c] = emf_value<T, E, M>(d, c, v1av, v2av, b1l, b1r, b2l, b2r, eta);
   }
 }
 
@@ -1699,6 +1713,296 @@ void launch_emf_pdm(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStre
     attr.mark(bit);
   }
   k_emf_pdm<T, E, TX, TY, TZ, NT, M, false><<<emf_grid(E, d.g, TX, TY, TZ), NT, bytes, st>>>(one(d), in, P);
+}
+
+// ------------------------------------------------------ streamed PDM EMF
+// The PDM EMF of one family as slice streams.  A block owns a patch of edges
+// across the stream axis S (32 lanes along x times NW warps) and walks S over
+// a segment of edge positions.  Each step copies one new cell slice of
+// (v_a1, v_a2), of the face-B component that is reconstructed across the
+// slice and of vf into shared-memory rings, asynchronously and a step ahead,
+// and each thread computes the edge of its column at the current position:
+// every cell is staged once per segment (no halo re-reads along S, no
+// per-tap index arithmetic), and the taps along S come from a register window
+// or the ring.
+//   ei (E = 0): lanes along x (the edge axis), warps along y = a1, S = z = a2.
+//   ek (E = 2): lanes along x = a1, warps along z (the edge axis), S = y = a2.
+//   ej (E = 1): lanes along x = a2, warps along y (the edge axis), S = z = a1.
+// With S = a2 the first pass of interp2_pdm (8 taps along a1) runs inside
+// the new slice and the second pass (along S) on a register window of eight
+// first-pass values; with S = a1 the first pass runs across eight ring slices
+// into a per-warp row (32 columns plus the 8-column halo) and the second pass
+// along x reads that row.  The face-B component reconstructed along S is a
+// register window of eight values of the thread's own column.  The
+// arithmetic per edge is emf_pdm_tile's and k_emf's (same operands, same
+// order), so all three give the same bits.  The in-slice transverse axis
+// holds n0 + 1 edges; the tiles cover the first n0 and k_emf_rows the last.
+template <typename T, int E, int NW>
+struct EmfStream {
+  static constexpr bool SA2 = (E != 1);             // S = a2 (ei, ek) or S = a1 (ej)
+  static constexpr int NT = 32 * NW;
+  static constexpr int C = (E == 0) ? 32 : 40;      // slice columns (x), with the x halo for ek / ej
+  static constexpr int R = (E == 0) ? NW + 8 : NW;  // slice rows, with the y halo for ei
+  static constexpr int NS = R * C;                  // cells per slice
+  static constexpr int NE = (NS + NT - 1) / NT;     // slice cells each thread copies
+  static constexpr int TS = (E == 0) ? C : 1;       // in-slice stride of the transverse axis
+  static constexpr int DV = SA2 ? 8 : 16;           // (v_a1, v_a2) ring depth
+  static constexpr size_t smem =
+      sizeof(typename Pr<T>::V) * (DV * NS + (SA2 ? 0 : NW * C)) + sizeof(T) * (2 * NS + 4 * NS);
+};
+
+// Segments along S: nseg of seg edge positions, the last one taking the rest.
+__host__ __device__ inline int emf_stream_segs(int nS0, int seg) { return max(1, (nS0 + 1) / seg); }
+
+template <typename T>
+__device__ __forceinline__ void cp_async_zfill(uint32_t dst, const T* src, bool ok) {
+  const int n = ok ? (int)sizeof(T) : 0;  // 0: nothing is read, the element is zeroed
+  if (sizeof(T) == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(n) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(n) : "memory");
+}
+
+#ifndef MHD_EMF_STREAM_MINB
+#define MHD_EMF_STREAM_MINB 3
+#endif
+template <typename T, int E, int NW, bool M>
+__global__ void __launch_bounds__(32 * NW, MHD_EMF_STREAM_MINB)
+    k_emf_stream(Dev<T> d, Inp<T> in, Prm<T> P, int seg) {
+  typedef EmfStream<T, E, NW> K;
+  typedef Pr<T> Q;
+  typedef typename Q::V V;
+  constexpr int A1 = (E + 1) % 3, A2 = (E + 2) % 3;
+  constexpr int C = K::C, NS = K::NS, TS = K::TS, DV = K::DV, NT = K::NT, NE = K::NE;
+  constexpr bool SA2 = K::SA2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* vr = reinterpret_cast<V*>(smem_raw);              // [DV][NS] (v_a1, v_a2)
+  V* gr = vr + DV * NS;                                // ej: [NW][C] first-pass rows
+  T* br = reinterpret_cast<T*>(gr + (SA2 ? 0 : NW * C));  // [2][NS] face B across the slice
+  T* fr = br + 2 * NS;                                 // [4][NS] vf
+  const Geom& g = d.g;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int x0 = g.ng + 32 * (int)blockIdx.x;   // first x of the tile (edge or cell index)
+  const int w0 = g.ng + NW * (int)blockIdx.y;   // first index along the warp axis (y, z, y)
+  const int nS0 = (E == 2) ? g.ny0 : g.nz0;     // interior cells along S
+  const int nSg = (E == 2) ? g.ny : g.nz;
+  const int nW0 = (E == 2) ? g.nz0 : g.ny0;
+  const int s_lo = g.ng + seg * (int)blockIdx.z;
+  const int s_hi = ((int)blockIdx.z == emf_stream_segs(nS0, seg) - 1) ? g.ng + nS0 : s_lo + seg - 1;
+  const int SS = (E == 2) ? g.px : (int)g.plane;  // global stride along S
+  const int ox = x0 + lane, ow = w0 + warp;
+  const bool own = ox < g.ng + g.nx0 && ow < g.ng + nW0;
+  const int obase = ox + ((E == 2) ? (int)g.plane * ow : g.px * ow);  // own column at S = 0
+  const int oi = (E == 0) ? (warp + 4) * C + lane : warp * C + lane + 4;  // own cell in a slice
+  // the slice cells this thread copies: global offset at S = 0 and bounds
+  int go[NE];
+  bool gok[NE];
+#pragma unroll
+  for (int k = 0; k < NE; ++k) {
+    const int idx = tid + k * NT, r = idx / C, q = idx - r * C;
+    int x, w;
+    if (E == 0) { x = x0 + q; w = w0 - 4 + r; }
+    else { x = x0 - 4 + q; w = w0 + r; }
+    const int nw = (E == 2) ? g.nz : g.ny;
+    gok[k] = idx < NS && (unsigned)x < (unsigned)g.nx && (unsigned)w < (unsigned)nw;
+    go[k] = x + ((E == 2) ? (int)g.plane * w : g.px * w);
+  }
+  const T* vel[3] = {in.vx, in.vy, in.vz};
+  const T* fb[3] = {in.bi, in.bj, in.bk};
+  const T* v1 = vel[A1];
+  const T* v2 = vel[A2];
+  const T* bst = SA2 ? fb[A2] : fb[A1];  // reconstructed across the slice (staged)
+  const T* bwn = SA2 ? fb[A1] : fb[A2];  // reconstructed along S (own-column window)
+  const T* vf = d.vf;
+  const uint32_t vr_s = (uint32_t)__cvta_generic_to_shared(vr);
+  const uint32_t br_s = (uint32_t)__cvta_generic_to_shared(br);
+  const uint32_t fr_s = (uint32_t)__cvta_generic_to_shared(fr);
+  auto vslot = [&](int s) { return (s - s_lo + 4) & (DV - 1); };
+  // copy slice s of the selected arrays into their ring slots
+  auto stage = [&](int s, bool with_v, bool with_bf) {
+    const bool sok = (unsigned)s < (unsigned)nSg;
+#pragma unroll
+    for (int k = 0; k < NE; ++k) {
+      if (k * NT + tid < NS) {
+        const int idx = tid + k * NT;
+        const bool ok = gok[k] && sok;
+        const int o = ok ? go[k] + s * SS : 0;
+        if (with_v) {
+          const uint32_t a = vr_s + (uint32_t)((vslot(s) * NS + idx) * sizeof(V));
+          cp_async_zfill<T>(a, v1 + o, ok);
+          cp_async_zfill<T>(a + sizeof(T), v2 + o, ok);
+        }
+        if (with_bf) {
+          cp_async_zfill<T>(br_s + (uint32_t)(((s & 1) * NS + idx) * sizeof(T)), bst + o, ok);
+          cp_async_zfill<T>(fr_s + (uint32_t)(((s & 3) * NS + idx) * sizeof(T)), vf + o, ok);
+        }
+      }
+    }
+  };
+  // prologue: v slices s_lo-4 .. s_lo+3, face B at s_lo, vf at s_lo-1 and s_lo
+#pragma unroll 1
+  for (int m = 0; m < 8; ++m) stage(s_lo - 4 + m, true, m == 3 || m == 4);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  T bw[8];
+#pragma unroll
+  for (int m = 0; m < 8; ++m) bw[m] = own ? bwn[obase + (s_lo - 4 + m) * SS] : T(0);
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  __syncthreads();
+  // first pass along a1 inside slice s (S = a2)
+  auto first_a1 = [&](int s) {
+    const V* a = vr + vslot(s) * NS + oi;
+    return tap8p<T>(a[-4 * TS], a[-3 * TS], a[-2 * TS], a[-TS], a[0], a[TS], a[2 * TS], a[3 * TS]);
+  };
+  V gw[8];
+  if constexpr (SA2) {
+#pragma unroll
+    for (int m = 0; m < 8; ++m) gw[m] = first_a1(s_lo - 4 + m);
+    __syncthreads();  // the first step refills the slot of slice s_lo - 4
+  }
+#pragma unroll 1
+  for (int s = s_lo; s <= s_hi; ++s) {
+    const bool more = s < s_hi;
+    T bnext = T(0);
+    if (more) {  // inputs of the next step
+      stage(s + 4, true, false);
+      stage(s + 1, false, true);
+      if (own) bnext = bwn[obase + (s + 4) * SS];
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    V vi;
+    if constexpr (SA2) {
+      vi = tap8p<T>(gw[0], gw[1], gw[2], gw[3], gw[4], gw[5], gw[6], gw[7]);
+    } else {
+      // first pass along a1 = S across the ring into this warp's row
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r2 = lane + 32 * h;
+        if (r2 < C) {
+          const int col = warp * C + r2;
+          gr[col] = tap8p<T>(vr[vslot(s - 4) * NS + col], vr[vslot(s - 3) * NS + col], vr[vslot(s - 2) * NS + col],
+                             vr[vslot(s - 1) * NS + col], vr[vslot(s) * NS + col], vr[vslot(s + 1) * NS + col],
+                             vr[vslot(s + 2) * NS + col], vr[vslot(s + 3) * NS + col]);
+        }
+      }
+      __syncwarp();
+      const V* gg = gr + warp * C + lane;
+      vi = tap8p<T>(gg[0], gg[1], gg[2], gg[3], gg[4], gg[5], gg[6], gg[7]);
+    }
+    // the 12 corner cells, (d1, d2) from the upper cell
+    const V* sm2 = vr + vslot(s - 2) * NS + oi;
+    const V* sm1 = vr + vslot(s - 1) * NS + oi;
+    const V* s00 = vr + vslot(s) * NS + oi;
+    const V* sp1 = vr + vslot(s + 1) * NS + oi;
+    V m11, m21, m12, m01, p11, m02, m10, m20, m1p, c0, p10, p01;
+    if constexpr (SA2) {  // d1 in the slice (stride TS), d2 across slices
+      m11 = sm1[-TS]; m21 = sm1[-2 * TS]; m12 = sm2[-TS]; m01 = sm1[0]; p11 = sm1[TS]; m02 = sm2[0];
+      m10 = s00[-TS]; m20 = s00[-2 * TS]; m1p = sp1[-TS]; c0 = s00[0]; p10 = s00[TS]; p01 = sp1[0];
+    } else {  // d1 across slices, d2 in the slice (stride 1)
+      m11 = sm1[-1]; m21 = sm2[-1]; m12 = sm1[-2]; m01 = s00[-1]; p11 = sp1[-1]; m02 = s00[-2];
+      m10 = sm1[0]; m20 = sm2[0]; m1p = sm1[1]; c0 = s00[0]; p10 = sp1[0]; p01 = s00[1];
+    }
+    const T v1av = corner_pdm_vals(m11.x, m21.x, m12.x, m01.x, p11.x, m02.x, m10.x, m20.x, m1p.x, c0.x, p10.x, p01.x,
+                                   vi.x, P.pdmb);
+    const T v2av = corner_pdm_vals(m11.y, m21.y, m12.y, m01.y, p11.y, m02.y, m10.y, m20.y, m1p.y, c0.y, p10.y, p01.y,
+                                   vi.y, P.pdmb);
+    // face B: across the slice from the staged slice, along S from the window
+    constexpr int BS = SA2 ? TS : 1;
+    const T* bb = br + (s & 1) * NS + oi;
+    T sl, sr, wl, wr;
+    recon_pdm8(bb[-4 * BS], bb[-3 * BS], bb[-2 * BS], bb[-BS], bb[0], bb[BS], bb[2 * BS], bb[3 * BS], P.pdmb, sl, sr);
+    recon_pdm8(bw[0], bw[1], bw[2], bw[3], bw[4], bw[5], bw[6], bw[7], P.pdmb, wl, wr);
+    const T* f0 = fr + (s & 3) * NS + oi;
+    const T* fm = fr + ((s - 1) & 3) * NS + oi;
+    T eta;
+    if constexpr (SA2) eta = eta4(fm[-TS], fm[0], f0[0], f0[-TS]);  // s1 in the slice, s2 = S
+    else eta = eta4(fm[-1], f0[-1], f0[0], fm[0]);                  // s1 = S, s2 in the slice
+    if (own) {
+      const int c = obase + s * SS;
+      // b1 = B_a1 along a2, b2 = B_a2 along a1
+      d.E[E][c] = SA2 ? emf_value<T, E, M>(d, c, v1av, v2av, wl, wr, sl, sr, eta)
+                      : emf_value<T, E, M>(d, c, v1av, v2av, sl, sr, wl, wr, eta);
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
+    if (more) {
+#pragma unroll
+      for (int m = 0; m < 7; ++m) bw[m] = bw[m + 1];
+      bw[7] = bnext;
+      if constexpr (SA2) {
+#pragma unroll
+        for (int m = 0; m < 7; ++m) gw[m] = gw[m + 1];
+        gw[7] = first_a1(s + 4);
+      }
+    }
+  }
+}
+
+// The (n0+1)-th edge row of the in-slice transverse axis of each streamed
+// family, as thin shared-memory tiles of emf_pdm_tile in one launch of
+// 256-thread blocks: ei at y = ny0 in 32 x 1 x 8 tiles (x, y, z edges), ek
+// at x = nx0 in 1 x 32 x 8 tiles, ej at x = nx0 in 1 x 8 x 32 tiles.
+struct EmfRows {
+  int bi, bk, bj;  // blocks of the three planes
+  __host__ __device__ explicit EmfRows(const Geom& g)
+      : bi(((g.nx0 + 31) / 32) * ((g.nz0 + 8) / 8)), bk(((g.ny0 + 32) / 32) * ((g.nz0 + 7) / 8)),
+        bj(((g.ny0 + 7) / 8) * ((g.nz0 + 32) / 32)) {}
+  __host__ __device__ int blocks() const { return bi + bk + bj; }
+};
+template <typename T>
+constexpr size_t emf_rows_smem() {
+  constexpr size_t a = emf_pdm_smem<T, 0, 32, 1, 8>(), b = emf_pdm_smem<T, 2, 1, 32, 8>(),
+                   c = emf_pdm_smem<T, 1, 1, 8, 32>();
+  return a > b ? (a > c ? a : c) : (b > c ? b : c);
+}
+template <typename T, bool M>
+__global__ void __launch_bounds__(256) k_emf_rows(Dev<T> d, Inp<T> in, Prm<T> P) {
+  const Geom& g = d.g;
+  const EmfRows r(g);
+  int b = blockIdx.x;
+  if (b < r.bi) {
+    const int nbx = (g.nx0 + 31) / 32, bx = b % nbx, bz = b / nbx;
+    emf_pdm_tile<T, 0, 32, 1, 8, M>(d, in, P, g.ng + 32 * bx, g.ng + g.ny0, g.ng + 8 * bz);
+    return;
+  }
+  b -= r.bi;
+  if (b < r.bk) {
+    const int nby = (g.ny0 + 32) / 32, by = b % nby, bz = b / nby;
+    emf_pdm_tile<T, 2, 1, 32, 8, M>(d, in, P, g.ng + g.nx0, g.ng + 32 * by, g.ng + 8 * bz);
+    return;
+  }
+  b -= r.bk;
+  const int nby = (g.ny0 + 7) / 8, by = b % nby, bz = b / nby;
+  emf_pdm_tile<T, 1, 1, 8, 32, M>(d, in, P, g.ng + g.nx0, g.ng + 8 * by, g.ng + 32 * bz);
+}
+
+#ifndef MHD_EMF_SEG
+#define MHD_EMF_SEG 32
+#endif
+template <typename T, int E, int NW, bool M>
+void launch_emf_stream(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStream_t st) {
+  typedef EmfStream<T, E, NW> K;
+  static PerDevice attr;
+  unsigned long long bit = 0;
+  if (attr.need(bit)) {
+    cudaFuncSetAttribute(k_emf_stream<T, E, NW, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::smem);
+    attr.mark(bit);
+  }
+  const Geom& g = d.g;
+  const int nS0 = (E == 2) ? g.ny0 : g.nz0, nW0 = (E == 2) ? g.nz0 : g.ny0;
+  const dim3 grid((g.nx0 + 31) / 32, (nW0 + NW - 1) / NW, emf_stream_segs(nS0, MHD_EMF_SEG));
+  k_emf_stream<T, E, NW, M><<<grid, K::NT, K::smem, st>>>(d, in, P, MHD_EMF_SEG);
+}
+
+#ifndef MHD_EMF_NW
+#define MHD_EMF_NW 8
+#endif
+template <typename T, bool M>
+void emf_pdm_stream(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStream_t st) {
+  launch_emf_stream<T, 0, MHD_EMF_NW, M>(d, in, P, st);
+  launch_emf_stream<T, 1, MHD_EMF_NW, M>(d, in, P, st);
+  launch_emf_stream<T, 2, MHD_EMF_NW, M>(d, in, P, st);
+  static_assert(emf_rows_smem<T>() <= 48 * 1024, "k_emf_rows fits the default shared-memory limit");
+  k_emf_rows<T, M><<<EmfRows(d.g).blocks(), 256, emf_rows_smem<T>(), st>>>(d, in, P);
 }
 
 // ------------------------------------------------------------- WENO EMF
@@ -2651,6 +2955,12 @@ void Launch<T, M>::emf(const Dev<T>& d, const Inp<T>& in0, cudaStream_t st) {
   }
   if (d.recon == R_PDM) {
     Prm<T> P = prm_of(d);
+    if constexpr (std::is_same<T, float>::value && !M) {
+      if (d.tile_ey == kEmfStream) {
+        emf_pdm_stream<T, M>(d, in, P, st);
+        return;
+      }
+    }
     if (std::is_same<T, float>::value && !M && d.tile_ey == 4)
       launch_emf_pdm<T, 0, 32, 4, 4, 512, M>(d, in, P, st);
     else
@@ -2683,7 +2993,8 @@ void Launch<T, M>::fill(const Dev<T>& d, cudaStream_t st) {
 // ------------------------------------------------------------ batched ensemble
 template <typename T>
 dim3 Batch<T>::dims(int fam, const Geom& g, int td, int ey) {
-  const int Y = std::is_same<T, float>::value ? ey : EiTile<T>::Y;
+  // the batch runs the 8 x 8 ei tile where the single grid streams its EMF (same bits)
+  const int Y = std::is_same<T, float>::value && ey != kEmfStream ? ey : EiTile<T>::Y;
   if (!std::is_same<T, float>::value) td = TD;
   switch (fam) {
     case BF_CFL: return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + 7) / 8);

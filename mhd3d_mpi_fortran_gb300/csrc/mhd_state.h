@@ -204,6 +204,7 @@ int mlp_status(void* h);
 // Tile lengths the autotuner tries (FP32 Cartesian PDM).
 constexpr int kSweepTile = 32;  // face-shape value of the column sweeps
 constexpr int kTileTD[4] = {4, 8, 16, kSweepTile};
-constexpr int kTileEY[2] = {4, 8};
+constexpr int kEmfStream = 1;   // EMF-shape value of the slice-streamed EMF families
+constexpr int kTileEY[3] = {4, 8, kEmfStream};
 
 }  // namespace mhd

@@ -327,7 +327,7 @@ def test_autotuned_shapes_give_identical_steps():
         a.step(2)
         b.step(2)
         td, ey = b.autotune(reps=2)
-        assert td in (4, 8, 16, 32) and ey in (4, 8)
+        assert td in (4, 8, 16, 32) and ey in (1, 4, 8)
         a.step(3, graph=True)
         b.step(3, graph=True)
         fa, fb = a.fetch(), b.fetch()
@@ -336,10 +336,10 @@ def test_autotuned_shapes_give_identical_steps():
 
 
 def test_set_tiles_every_shape_gives_identical_steps():
-    """mhd_set_tiles: all eight FP32 PDM launch-shape pairs (face tiles 4, 8,
-    16 and the 32-cell column sweeps; ei tiles 4x4, 8x8) step to the same
-    bits; fixed-shape handles refuse other shapes; mhd_device_info reports
-    the device."""
+    """mhd_set_tiles: all twelve FP32 PDM launch-shape pairs (face tiles 4,
+    8, 16 and the 32-cell column sweeps; EMF as ei tiles 4x4, 8x8 or as slice
+    streams) step to the same bits; fixed-shape handles refuse other shapes;
+    mhd_device_info reports the device."""
     import ctypes as C
     from mhd3d_mpi_fortran_gb300 import abi
     from mhd3d_mpi_fortran_gb300.abi import MHDError
@@ -347,7 +347,7 @@ def test_set_tiles_every_shape_gives_identical_steps():
     prm = Params(40, 40, 40, precision=FP32, tau=0.5 * ics.cfl_dt(s))
     ref = None
     for td in (4, 8, 16, 32):
-        for ey in (4, 8):
+        for ey in (4, 8, 1):
             with MHDSolver(prm, s) as g:
                 g.set_tiles(td, ey)
                 g.step(2)
@@ -363,6 +363,29 @@ def test_set_tiles_every_shape_gives_identical_steps():
     info = (C.c_int32 * 4)()
     assert abi.load().mhd_device_info(info) == 0
     assert info[0] > 0 and info[1] >= 10 and info[3] > 0
+
+
+@pytest.mark.parametrize("shape", [(33, 17, 9), (64, 40, 24), (16, 64, 33), (8, 8, 8)])
+def test_streamed_emf_equals_tiles(shape):
+    """The slice-streamed EMF families (one edge column per thread along z for
+    ei and ej, along y for ek; the last edge row of the in-slice transverse
+    axis in a separate launch) against the shared-memory tiles: every EMF,
+    and the state after RK2 steps, bit-identical on ragged grids whose x
+    extent is not a multiple of the 32-lane tile, whose stream axis spans one
+    or several segments, and a grid smaller than one tile."""
+    s = rand_state(*shape, seed=sum(shape) + 1)
+    prm = Params(*shape, precision=FP32, tau=2e-4)
+    out = {}
+    for ey in (8, 1):
+        with MHDSolver(prm, s) as g:
+            g.set_tiles(8, ey)
+            e = g.debug_emf()
+            g.step(3)
+            out[ey] = (e, g.fetch())
+    for k in range(3):
+        assert np.array_equal(out[8][0][k], out[1][0][k]), k
+    for k in FIELDS:
+        assert np.array_equal(out[8][1][k], out[1][1][k]), k
 
 
 @pytest.mark.parametrize("stepop", [STEP_AB2, STEP_RK3])
@@ -431,7 +454,7 @@ def test_ensemble_autotune_then_step_equals_sequential():
             seq.append(g.fetch())
     ens = [MHDSolver(p, st) for p, st in zip(prms, states)]
     td, ey = ensemble_autotune(ens, reps=2)
-    assert td in (4, 8, 16) and ey in (4, 8)
+    assert td in (4, 8, 16) and ey in (1, 4, 8)
     ensemble_step(ens, 3)
     for e, ref in zip(ens, seq):
         got = e.fetch()
