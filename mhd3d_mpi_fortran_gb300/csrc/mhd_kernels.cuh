@@ -45,6 +45,24 @@ struct PerDevice {
   void mark(unsigned long long bit) { done.fetch_or(bit, std::memory_order_release); }
 };
 
+// Preferred shared-memory carveout (percent of the SM's maximum) of a kernel,
+// set once per device.  The L1-reliant step passes ask for the shared memory
+// they need and no more, so that the configuration a preceding
+// shared-memory-heavy launch (the EMF slice rings) leaves behind does not
+// shrink their L1.
+#ifndef MHD_L1_PREF
+#define MHD_L1_PREF 0
+#endif
+template <typename K>
+inline void prefer_carveout(K kernel, int pct, PerDevice& attr) {
+  if (!MHD_L1_PREF) return;
+  unsigned long long bit = 0;
+  if (attr.need(bit)) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+    attr.mark(bit);
+  }
+}
+
 inline dim3 grid3(int ni, int nj, int nk, dim3 b) {
   return dim3((ni + b.x - 1) / b.x, (nj + b.y - 1) / b.y, nk);
 }
@@ -1766,9 +1784,12 @@ __device__ __forceinline__ void cp_async_zfill(uint32_t dst, const T* src, bool 
 #ifndef MHD_EMF_STREAM_MINB
 #define MHD_EMF_STREAM_MINB 3
 #endif
-template <typename T, int E, int NW, bool M>
+template <typename T, int E, int NW, bool M, bool B>
 __global__ void __launch_bounds__(32 * NW, MHD_EMF_STREAM_MINB)
-    k_emf_stream(Dev<T> d, Inp<T> in, Prm<T> P, int seg) {
+    k_emf_stream(KArg<T, B> ka, Inp<T> in0, Prm<T> P, int seg) {
+  const int4 bb = ka.blk();
+  const auto& d = ka.dev(bb);
+  const Inp<T> in = B ? state_view(d) : in0;
   typedef EmfStream<T, E, NW> K;
   typedef Pr<T> Q;
   typedef typename Q::V V;
@@ -1782,13 +1803,13 @@ __global__ void __launch_bounds__(32 * NW, MHD_EMF_STREAM_MINB)
   T* fr = br + 2 * NS;                                 // [4][NS] vf
   const Geom& g = d.g;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int x0 = g.ng + 32 * (int)blockIdx.x;   // first x of the tile (edge or cell index)
-  const int w0 = g.ng + NW * (int)blockIdx.y;   // first index along the warp axis (y, z, y)
+  const int x0 = g.ng + 32 * bb.y;   // first x of the tile (edge or cell index)
+  const int w0 = g.ng + NW * bb.z;   // first index along the warp axis (y, z, y)
   const int nS0 = (E == 2) ? g.ny0 : g.nz0;     // interior cells along S
   const int nSg = (E == 2) ? g.ny : g.nz;
   const int nW0 = (E == 2) ? g.nz0 : g.ny0;
-  const int s_lo = g.ng + seg * (int)blockIdx.z;
-  const int s_hi = ((int)blockIdx.z == emf_stream_segs(nS0, seg) - 1) ? g.ng + nS0 : s_lo + seg - 1;
+  const int s_lo = g.ng + seg * bb.w;
+  const int s_hi = (bb.w == emf_stream_segs(nS0, seg) - 1) ? g.ng + nS0 : s_lo + seg - 1;
   const int SS = (E == 2) ? g.px : (int)g.plane;  // global stride along S
   const int ox = x0 + lane, ow = w0 + warp;
   const bool own = ox < g.ng + g.nx0 && ow < g.ng + nW0;
@@ -1954,11 +1975,14 @@ constexpr size_t emf_rows_smem() {
                    c = emf_pdm_smem<T, 1, 1, 8, 32>();
   return a > b ? (a > c ? a : c) : (b > c ? b : c);
 }
-template <typename T, bool M>
-__global__ void __launch_bounds__(256) k_emf_rows(Dev<T> d, Inp<T> in, Prm<T> P) {
+template <typename T, bool M, bool B>
+__global__ void __launch_bounds__(256) k_emf_rows(KArg<T, B> ka, Inp<T> in0, Prm<T> P) {
+  const int4 bb = ka.blk();
+  const auto& d = ka.dev(bb);
+  const Inp<T> in = B ? state_view(d) : in0;
   const Geom& g = d.g;
   const EmfRows r(g);
-  int b = blockIdx.x;
+  int b = bb.y;
   if (b < r.bi) {
     const int nbx = (g.nx0 + 31) / 32, bx = b % nbx, bz = b / nbx;
     emf_pdm_tile<T, 0, 32, 1, 8, M>(d, in, P, g.ng + 32 * bx, g.ng + g.ny0, g.ng + 8 * bz);
@@ -1978,31 +2002,43 @@ __global__ void __launch_bounds__(256) k_emf_rows(Dev<T> d, Inp<T> in, Prm<T> P)
 #ifndef MHD_EMF_SEG
 #define MHD_EMF_SEG 32
 #endif
-template <typename T, int E, int NW, bool M>
-void launch_emf_stream(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStream_t st) {
-  typedef EmfStream<T, E, NW> K;
-  static PerDevice attr;
-  unsigned long long bit = 0;
-  if (attr.need(bit)) {
-    cudaFuncSetAttribute(k_emf_stream<T, E, NW, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::smem);
-    attr.mark(bit);
-  }
-  const Geom& g = d.g;
-  const int nS0 = (E == 2) ? g.ny0 : g.nz0, nW0 = (E == 2) ? g.nz0 : g.ny0;
-  const dim3 grid((g.nx0 + 31) / 32, (nW0 + NW - 1) / NW, emf_stream_segs(nS0, MHD_EMF_SEG));
-  k_emf_stream<T, E, NW, M><<<grid, K::NT, K::smem, st>>>(d, in, P, MHD_EMF_SEG);
-}
-
 #ifndef MHD_EMF_NW
 #define MHD_EMF_NW 8
 #endif
+// blocks of streamed family E on one grid (x tiles, warp-axis tiles, segments)
+inline dim3 emf_stream_grid(int E, const Geom& g) {
+  const int nS0 = (E == 2) ? g.ny0 : g.nz0, nW0 = (E == 2) ? g.nz0 : g.ny0;
+  return dim3((g.nx0 + 31) / 32, (nW0 + MHD_EMF_NW - 1) / MHD_EMF_NW, emf_stream_segs(nS0, MHD_EMF_SEG));
+}
+template <typename T, int E, bool M, bool B>
+void stream_attr() {
+  static PerDevice attr;
+  unsigned long long bit = 0;
+  if (attr.need(bit)) {
+    cudaFuncSetAttribute(k_emf_stream<T, E, MHD_EMF_NW, M, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)EmfStream<T, E, MHD_EMF_NW>::smem);
+#ifdef MHD_EMF_CARVEOUT
+    cudaFuncSetAttribute(k_emf_stream<T, E, MHD_EMF_NW, M, B>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         MHD_EMF_CARVEOUT);
+#endif
+    attr.mark(bit);
+  }
+}
+template <typename T, int E, bool M>
+void launch_emf_stream(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStream_t st) {
+  typedef EmfStream<T, E, MHD_EMF_NW> K;
+  stream_attr<T, E, M, false>();
+  k_emf_stream<T, E, MHD_EMF_NW, M, false><<<emf_stream_grid(E, d.g), K::NT, K::smem, st>>>(one(d), in, P,
+                                                                                          MHD_EMF_SEG);
+}
+
 template <typename T, bool M>
 void emf_pdm_stream(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStream_t st) {
-  launch_emf_stream<T, 0, MHD_EMF_NW, M>(d, in, P, st);
-  launch_emf_stream<T, 1, MHD_EMF_NW, M>(d, in, P, st);
-  launch_emf_stream<T, 2, MHD_EMF_NW, M>(d, in, P, st);
+  launch_emf_stream<T, 0, M>(d, in, P, st);
+  launch_emf_stream<T, 1, M>(d, in, P, st);
+  launch_emf_stream<T, 2, M>(d, in, P, st);
   static_assert(emf_rows_smem<T>() <= 48 * 1024, "k_emf_rows fits the default shared-memory limit");
-  k_emf_rows<T, M><<<EmfRows(d.g).blocks(), 256, emf_rows_smem<T>(), st>>>(d, in, P);
+  k_emf_rows<T, M, false><<<EmfRows(d.g).blocks(), 256, emf_rows_smem<T>(), st>>>(one(d), in, P);
 }
 
 // ------------------------------------------------------------- WENO EMF
@@ -2680,6 +2716,9 @@ void Launch<T, M>::ct_fill(const Dev<T>& d, int form, double c, double den, bool
     fill_bxyz(other_half(d), want_vf, st);
   } else {
     const FillShape fs(d.g);
+    static PerDevice pref_ct, pref_fill;
+    prefer_carveout(k_ct_fill<T, false>, 0, pref_ct);
+    prefer_carveout(k_fill_bxyz<T, false, false>, 0, pref_fill);
     k_ct_fill<T, false><<<dim3(fs.nbx, fs.nby, d.g.nz0), 256, 0, st>>>(one(d), form, (T)c, (T)den,
                                                                         want_vf ? 1 : 0);
     k_fill_bxyz<T, false, false><<<(fs.nshell + 255) / 256, 256, 0, st>>>(one(other_half(d)), want_vf ? 1 : 0, 1);
@@ -2689,6 +2728,8 @@ void Launch<T, M>::ct_fill(const Dev<T>& d, int form, double c, double den, bool
 template <typename T, bool M>
 void Launch<T, M>::cfl(const Dev<T>& d, int mode, cudaStream_t st, bool save) {
   dim3 grid((d.g.nx + 31) / 32, (d.g.ny + 7) / 8, (d.g.nz + 7) / 8);
+  static PerDevice pref;
+  prefer_carveout(k_cfl<T, M, false>, 0, pref);
   k_cfl<T, M, false><<<grid, 256, 0, st>>>(one(d), save ? 1 : 0);
   k_cfl_final<T><<<1, 1, 0, st>>>(d, mode);
 }
@@ -2757,6 +2798,8 @@ template <typename T, int RECON, int D, bool M>
 void flux_t_any(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, int form, T c, T den, int ab, cudaStream_t st) {
   if constexpr (std::is_same<T, float>::value && !M) {
     if (d.tile_td == kSweepTile) {  // column sweeps (every FP32 Cartesian reconstruction with a register window)
+      static PerDevice pref;  // 4 blocks of 27 KB static shared memory
+      prefer_carveout(k_flux_sweep<T, D, false, RECON>, 50, pref);
       k_flux_sweep<T, D, false, RECON><<<sweep_grid(D, d.g), dim3(32, 4), 0, st>>>(one(d), in, P, form, c, den);
       return;
     }
@@ -2775,6 +2818,8 @@ void hydro_r(const Dev<T>& d, const Inp<T>& in, int part, int form, double c, do
   const Geom& g = d.g;
   if (part == 0) {
     const int n0 = (g.nx0 + 1) * g.ny0 * g.nz0;
+    static PerDevice pref;
+    prefer_carveout(k_flux<T, RECON, 0, M, false>, 0, pref);
     k_flux<T, RECON, 0, M, false><<<(n0 + 127) / 128, 128, 0, st>>>(one(d), in, P);
   } else if (part == 1) {
     flux_t_any<T, RECON, 1, M>(d, in, P, -1, T(0), T(1), 0, st);
@@ -2993,17 +3038,18 @@ void Launch<T, M>::fill(const Dev<T>& d, cudaStream_t st) {
 // ------------------------------------------------------------ batched ensemble
 template <typename T>
 dim3 Batch<T>::dims(int fam, const Geom& g, int td, int ey) {
-  // the batch runs the 8 x 8 ei tile where the single grid streams its EMF (same bits)
-  const int Y = std::is_same<T, float>::value && ey != kEmfStream ? ey : EiTile<T>::Y;
+  const bool stream = std::is_same<T, float>::value && ey == kEmfStream;
+  const int Y = std::is_same<T, float>::value && !stream ? ey : EiTile<T>::Y;
   if (!std::is_same<T, float>::value) td = TD;
   switch (fam) {
     case BF_CFL: return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + 7) / 8);
     case BF_FLUX_X: return dim3(((g.nx0 + 1) * g.ny0 * g.nz0 + 127) / 128, 1, 1);
     case BF_FLUX_Y: return td == kSweepTile ? sweep_grid(1, g) : dim3((g.nx0 + 31) / 32, (g.ny0 + td - 1) / td, g.nz0);
     case BF_FLUX_Z: return td == kSweepTile ? sweep_grid(2, g) : dim3((g.nx0 + 31) / 32, (g.nz0 + td - 1) / td, g.ny0);
-    case BF_EMF_I: return emf_grid(0, g, ei_x(Y), Y, Y);
-    case BF_EMF_J: return emf_grid(1, g, 32, 1, kPT);
-    case BF_EMF_K: return emf_grid(2, g, 32, kPT, 1);
+    case BF_EMF_I: return stream ? emf_stream_grid(0, g) : emf_grid(0, g, ei_x(Y), Y, Y);
+    case BF_EMF_J: return stream ? emf_stream_grid(1, g) : emf_grid(1, g, 32, 1, kPT);
+    case BF_EMF_K: return stream ? emf_stream_grid(2, g) : emf_grid(2, g, 32, kPT, 1);
+    case BF_EMF_R: return stream ? dim3(EmfRows(g).blocks(), 1, 1) : dim3(0, 0, 0);
     case BF_CT: {  // k_ct_fill: the fill's interior tiles
       const FillShape fs(g);
       return dim3(fs.nbx, fs.nby, g.nz0);
@@ -3048,6 +3094,24 @@ void batch_emf(const BatchView& v, const Dev<T>* tab, const Prm<T>& P, cudaStrea
       KArg<T, true>{tab, v.map[BF_EMF_K]}, none, P);
 }
 
+// Batched slice-streamed EMF families and their boundary rows.
+template <typename T>
+void batch_emf_stream(const BatchView& v, const Dev<T>* tab, const Prm<T>& P, cudaStream_t st) {
+  stream_attr<T, 0, false, true>();
+  stream_attr<T, 1, false, true>();
+  stream_attr<T, 2, false, true>();
+  const Inp<T> none{};
+  constexpr int NT = 32 * MHD_EMF_NW;
+  k_emf_stream<T, 0, MHD_EMF_NW, false, true><<<v.nblk[BF_EMF_I], NT, EmfStream<T, 0, MHD_EMF_NW>::smem, st>>>(
+      KArg<T, true>{tab, v.map[BF_EMF_I]}, none, P, MHD_EMF_SEG);
+  k_emf_stream<T, 1, MHD_EMF_NW, false, true><<<v.nblk[BF_EMF_J], NT, EmfStream<T, 1, MHD_EMF_NW>::smem, st>>>(
+      KArg<T, true>{tab, v.map[BF_EMF_J]}, none, P, MHD_EMF_SEG);
+  k_emf_stream<T, 2, MHD_EMF_NW, false, true><<<v.nblk[BF_EMF_K], NT, EmfStream<T, 2, MHD_EMF_NW>::smem, st>>>(
+      KArg<T, true>{tab, v.map[BF_EMF_K]}, none, P, MHD_EMF_SEG);
+  k_emf_rows<T, false, true><<<v.nblk[BF_EMF_R], 256, emf_rows_smem<T>(), st>>>(
+      KArg<T, true>{tab, v.map[BF_EMF_R]}, none, P);
+}
+
 // Batched y / z face tiles of length TDV.
 template <typename T, int TDV>
 void batch_flux_t(const BatchView& v, const Dev<T>* tab, const Prm<T>& P, int form, T c, T den, cudaStream_t st) {
@@ -3074,6 +3138,12 @@ void Batch<T>::parts(const BatchView& v, int sel, int which, int form, double c,
   P.pdmb = (T)v.pdmb; P.eps = (T)v.eps; P.alpha = (T)v.alpha; P.beta = (T)v.beta; P.tvd_shift = v.tvd_shift;
   constexpr bool F32 = std::is_same<T, float>::value;
   if (which & 1) {  // EMF families
+    if constexpr (F32) {
+      if (v.tile_ey == kEmfStream) {
+        batch_emf_stream<T>(v, tab, P, st);
+        return parts(v, sel, which & ~1, form, c, den, st);
+      }
+    }
     if (F32 && v.tile_ey == 4) batch_emf<T, 4>(v, tab, P, st);
     else batch_emf<T, EiTile<T>::Y>(v, tab, P, st);
   }

@@ -164,7 +164,9 @@ struct Launch {
 // grid of the batch in one flattened 1-D launch.  A family's per-grid block
 // grid is exactly the one its single-grid launcher uses; map[f] lists
 // {grid, bx, by, bz} for every block of the launch, grid after grid.
-enum BatchFam { BF_CFL, BF_FLUX_X, BF_FLUX_Y, BF_FLUX_Z, BF_EMF_I, BF_EMF_J, BF_EMF_K, BF_CT, BF_FILL, BF_COUNT };
+enum BatchFam {
+  BF_CFL, BF_FLUX_X, BF_FLUX_Y, BF_FLUX_Z, BF_EMF_I, BF_EMF_J, BF_EMF_K, BF_EMF_R, BF_CT, BF_FILL, BF_COUNT
+};
 
 struct BatchView {
   const void* tab[2];       // device Dev<T>[ngrids] for the two halves of the primitive buffers

@@ -420,9 +420,11 @@ def test_weno_column_sweeps_equal_face_tiles(recon):
         assert np.array_equal(out[8][k], out[32][k]), k
 
 
-def test_batched_column_sweeps_equal_sequential_tiles():
-    """Batched ensemble on the column-sweep face kernels (tile 32) against each
-    grid stepped alone on the default face tiles: bit-identical."""
+@pytest.mark.parametrize("ey", [8, 1])
+def test_batched_column_sweeps_equal_sequential_tiles(ey):
+    """Batched ensemble on the column-sweep face kernels (tile 32) and the
+    8x8 ei EMF tiles or the slice-streamed EMF against each grid stepped
+    alone on its default shapes: bit-identical."""
     sizes = (16, 40, 24)
     states = [ics.turbulence(n, seed=10 + i) for i, n in enumerate(sizes)]
     prms = [Params(n, n, n, precision=FP32, tau=0.4 * ics.cfl_dt(st)) for n, st in zip(sizes, states)]
@@ -433,7 +435,7 @@ def test_batched_column_sweeps_equal_sequential_tiles():
             seq.append(g.fetch())
     ens = [MHDSolver(p, st) for p, st in zip(prms, states)]
     for e in ens:
-        e.set_tiles(32, 8)
+        e.set_tiles(32, ey)
     ensemble_step(ens, 4)
     for e, ref in zip(ens, seq):
         got = e.fetch()
