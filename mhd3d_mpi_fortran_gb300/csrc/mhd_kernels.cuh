@@ -1769,8 +1769,6 @@ struct EmfStream {
       sizeof(typename Pr<T>::V) * (DV * NS + (SA2 ? 0 : NW * C)) + sizeof(T) * (2 * NS + 4 * NS);
 };
 
-// Segments along S: nseg of seg edge positions, the last one taking the rest.
-__host__ __device__ inline int emf_stream_segs(int nS0, int seg) { return max(1, (nS0 + 1) / seg); }
 
 template <typename T>
 __device__ __forceinline__ void cp_async_zfill(uint32_t dst, const T* src, bool ok) {
@@ -1999,12 +1997,6 @@ __global__ void __launch_bounds__(256) k_emf_rows(KArg<T, B> ka, Inp<T> in0, Prm
   emf_pdm_tile<T, 1, 1, 8, 32, M>(d, in, P, g.ng + g.nx0, g.ng + 8 * by, g.ng + 32 * bz);
 }
 
-#ifndef MHD_EMF_SEG
-#define MHD_EMF_SEG 32
-#endif
-#ifndef MHD_EMF_NW
-#define MHD_EMF_NW 8
-#endif
 // blocks of streamed family E on one grid (x tiles, warp-axis tiles, segments)
 inline dim3 emf_stream_grid(int E, const Geom& g) {
   const int nS0 = (E == 2) ? g.ny0 : g.nz0, nW0 = (E == 2) ? g.nz0 : g.ny0;
@@ -2472,43 +2464,59 @@ __global__ void __launch_bounds__(256, pass_min_blocks(B)) k_fill_bxyz(KArg<T, B
   const int* fx = cz + g.nz + 2;
   const int* fy = fx + g.nx + 2;
   const int* fz = fy + g.ny + 2;
+  // every image index first, then every load, then every store: the loads of
+  // one thread are in flight together (no store sits between them)
   const int sci = cx[i], scj = cy[j], sck = cz[k];  // cell images (entries n, n+1 unused)
   const int sfi = fx[i], sfj = fy[j], sfk = fz[k];  // face images
+  const int sfi1 = fx[i + 1], sfj1 = fy[j + 1], sfk1 = fz[k + 1];
   const bool cin = i < g.nx && j < g.ny && k < g.nz;
-  // ghost copies: cell arrays (rho, vx, vy, vz, p), then bi, bj, bk
   const bool gx = sci != i, gy = scj != j, gz = sck != k;
-  if (cin && (gx || gy || gz)) {
-    const int sc = sci + px * scj + pl * sck;
-    d.rho[c] = d.rho[sc];
-    d.p[c] = d.p[sc];
-    const T ux = d.vx[sc], uy = d.vy[sc], uz = d.vz[sc];
+  const bool cell_copy = cin && (gx || gy || gz);
+  const bool bi_copy = j < g.ny && k < g.nz && (sfi != i || gy || gz);
+  const bool bj_copy = i < g.nx && k < g.nz && (gx || sfj != j || gz);
+  const bool bk_copy = i < g.nx && j < g.ny && (gx || gy || sfk != k);
+  const bool need_cell = cell_copy || (cin && want_vf);
+  const int sc = sci + px * scj + pl * sck;
+  const int fi0 = sfi + px * scj + pl * sck, fi1 = sfi1 + px * scj + pl * sck;  // faces of the image cell
+  const int fj0 = sci + px * sfj + pl * sck, fj1 = sci + px * sfj1 + pl * sck;
+  const int fk0 = sci + px * scj + pl * sfk, fk1 = sci + px * scj + pl * sfk1;
+  T r0 = T(0), p0 = T(0), ux = T(0), uy = T(0), uz = T(0);
+  if (need_cell) {
+    r0 = d.rho[sc]; p0 = d.p[sc]; ux = d.vx[sc]; uy = d.vy[sc]; uz = d.vz[sc];
+  }
+  T bi0 = T(0), bi1 = T(0), bj0 = T(0), bj1 = T(0), bk0 = T(0), bk1 = T(0);
+  if (bi_copy || cin) bi0 = d.bi[fi0];
+  if (bj_copy || cin) bj0 = d.bj[fj0];
+  if (bk_copy || cin) bk0 = d.bk[fk0];
+  if (cin) {
+    bi1 = d.bi[fi1];
+    bj1 = d.bj[fj1];
+    bk1 = d.bk[fk1];
+  }
+  // ghost copies: cell arrays (rho, vx, vy, vz, p), then bi, bj, bk
+  if (cell_copy) {
+    d.rho[c] = r0;
+    d.p[c] = p0;
     d.vx[c] = (gx && d.bc[0] == BC_REFLECT) ? -ux : ux;
     d.vy[c] = (gy && d.bc[1] == BC_REFLECT) ? -uy : uy;
     d.vz[c] = (gz && d.bc[2] == BC_REFLECT) ? -uz : uz;
   }
-  if (j < g.ny && k < g.nz && (sfi != i || gy || gz)) d.bi[c] = d.bi[sfi + px * scj + pl * sck];
-  if (i < g.nx && k < g.nz && (gx || sfj != j || gz)) d.bj[c] = d.bj[sci + px * sfj + pl * sck];
-  if (i < g.nx && j < g.ny && (gx || gy || sfk != k)) d.bk[c] = d.bk[sci + px * scj + pl * sfk];
+  if (bi_copy) d.bi[c] = bi0;
+  if (bj_copy) d.bj[c] = bj0;
+  if (bk_copy) d.bk[c] = bk0;
   if (!cin) return;
-  const int cyz = px * scj + pl * sck;
   T bx, by, bz;
   if (M) {  // face fluxes of the images, geometry of this cell (as fill then get_bxyz)
-    cell_b_metric<T>(d.m, c, d.bi[sfi + cyz], d.bi[fx[i + 1] + cyz], d.bj[sci + px * sfj + pl * sck],
-                     d.bj[sci + px * fy[j + 1] + pl * sck], d.bk[sci + px * scj + pl * sfk],
-                     d.bk[sci + px * scj + pl * fz[k + 1]], bx, by, bz);
+    cell_b_metric<T>(d.m, c, bi0, bi1, bj0, bj1, bk0, bk1, bx, by, bz);
   } else {
-    bx = T(0.5) * (d.bi[fx[i + 1] + cyz] + d.bi[sfi + cyz]);
-    by = T(0.5) * (d.bj[sci + px * fy[j + 1] + pl * sck] + d.bj[sci + px * sfj + pl * sck]);
-    bz = T(0.5) * (d.bk[sci + px * scj + pl * fz[k + 1]] + d.bk[sci + px * scj + pl * sfk]);
+    bx = T(0.5) * (bi1 + bi0);
+    by = T(0.5) * (bj1 + bj0);
+    bz = T(0.5) * (bk1 + bk0);
   }
   d.bx[c] = bx;
   d.by[c] = by;
   d.bz[c] = bz;
-  if (want_vf) {
-    const int s = sci + cyz;
-    const T u = d.vx[s], v = d.vy[s], w = d.vz[s];
-    d.vf[c] = sq(u * u + v * v + w * w) + sq((bx * bx + by * by + bz * bz) / d.rho[s]);
-  }
+  if (want_vf) d.vf[c] = sq(ux * ux + uy * uy + uz * uz) + sq((bx * bx + by * by + bz * bz) / r0);
 }
 
 // CT fused with get_bxyz and vf on Cartesian meshes (advance_bijk + combine,

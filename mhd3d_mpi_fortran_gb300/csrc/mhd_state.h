@@ -207,6 +207,16 @@ int mlp_status(void* h);
 constexpr int kSweepTile = 32;  // face-shape value of the column sweeps
 constexpr int kTileTD[4] = {4, 8, 16, kSweepTile};
 constexpr int kEmfStream = 1;   // EMF-shape value of the slice-streamed EMF families
+// Slice-streamed EMF launch shape: warps per block (edges along the warp
+// axis) and edge positions per segment of the stream axis (compile-time knobs).
+#ifndef MHD_EMF_NW
+#define MHD_EMF_NW 8
+#endif
+#ifndef MHD_EMF_SEG
+#define MHD_EMF_SEG 32
+#endif
+// Segments along the stream axis: nseg of seg edge positions, the last one taking the rest.
+__host__ __device__ inline int emf_stream_segs(int nS0, int seg) { return (nS0 + 1) / seg > 1 ? (nS0 + 1) / seg : 1; }
 constexpr int kTileEY[3] = {4, 8, kEmfStream};
 
 }  // namespace mhd
