@@ -562,7 +562,10 @@ def run_ours(a):
         return
     compute_roofs = roofs(zu / ws, clocks, a.recon, tiles)
     emf_launches = 4 if tiles[1] == 1 else 3  # slice streams: three families plus their boundary rows
-    launches_per_step = 2 + 2 * (emf_launches + 3 + 1 + 1)
+    # per RK2 step: the tau selection (the CFL dt comes from the previous step's
+    # last stage), then per stage EMF, x faces, y and z sweeps, CT + bxyz + vf
+    # and the ghost shell
+    launches_per_step = 1 + 2 * (emf_launches + 3 + 1 + 1)
     fp64 = None
     if study:
         ref = study["runs"][0]

@@ -77,13 +77,17 @@ struct Handle {
   std::vector<cudaEvent_t> pool;
   std::vector<int> fam;
   int par = 0;                 // which half of the double-buffered primitives is current
+  // the previous RK step left the CFL dt and status of the current state in
+  // Scal::dtnext_bits / pend_status (cleared whenever the state changes
+  // between steps: init, load, learned correction, batched steps)
+  bool prepared = false;
   int tile_td = 8, tile_ey = 8;  // launch shapes (autotuned for FP32 Cartesian PDM)
   float* geoT = nullptr;       // FP32 copy of the cell widths
   int* gmap = nullptr;         // ghost-image tables
   bool metric = false;         // curvilinear metric mode (mhd_init_mapped)
   double* met = nullptr;       // FP64 metric arrays (kMetricArrays x vol)
   std::vector<double> nodes;   // host copy of the node coordinates (checkpoints)
-  // graphs keyed by (nsteps, starting parity) -> (exec, parity after replay)
+  // graphs keyed by (nsteps, starting parity + 2 prepared) -> (exec, parity + 2 prepared after replay)
   std::map<std::pair<int, int>, std::pair<cudaGraphExec_t, int>> graphs;
 };
 
@@ -204,17 +208,23 @@ void enqueue_step(Handle* h, int& par, cudaStream_t st, Rec* r = nullptr) {
     emf_and_fluxes<T, M>(h, d, in, -1, 0.0, 1.0, true, st, R);
     R.begin(); L::ct_fill(d, -1, 0.0, 1.0, false, st); R.end(4);
     par ^= 1;
+    h->prepared = false;
     return;
   }
+  // Cartesian RK: U^n is stored by the first stage and the CFL dt of the next
+  // step's state accumulated by the last one (no separate pass over the
+  // state); the metric mode keeps the CFL pass that also stores U^n.
+  constexpr bool fold = !M;
   {
     Dev<T> d = at_par(base, par);
     R.begin();
-    L::cfl(d, p.dt_mode == MHD_DT_CFL ? 1 : 0, st, true);
+    if (fold) L::cfl_folded(d, p.dt_mode == MHD_DT_CFL ? 1 : 0, !h->prepared, st);
+    else L::cfl(d, p.dt_mode == MHD_DT_CFL ? 1 : 0, st, true);
     R.end(6);
   }
   int nst = (p.stepop == MHD_STEP_RK2) ? 2 : 3;
   for (int s = 1; s <= nst; ++s) {
-    int form = -1;
+    int form = fold ? FORM_SAVE : -1;
     double c = 0.0, den = 1.0;
     if (s > 1) {
       if (nst == 2) { form = 0; den = 2.0; }
@@ -224,9 +234,10 @@ void enqueue_step(Handle* h, int& par, cudaStream_t st, Rec* r = nullptr) {
     Dev<T> d = at_par(base, par);
     Inp<T> in = state_inp(d);
     emf_and_fluxes<T, M>(h, d, in, form, c, den, false, st, R);
-    R.begin(); L::ct_fill(d, form, c, den, true, st); R.end(4);
+    R.begin(); L::ct_fill(d, form, c, den, true, st, fold && s == nst); R.end(4);
     par ^= 1;
   }
+  h->prepared = fold;
 }
 
 // Cartesian or metric step of a handle.
@@ -604,7 +615,9 @@ static int create_handle(const mhd_params* prm, const double* dx, const double* 
   s.ab_coef = 0.0;
   double inf = INFINITY;
   std::memcpy(&s.dtmin_bits, &inf, sizeof(double));
+  std::memcpy(&s.dtnext_bits, &inf, sizeof(double));
   s.status = 0;
+  s.pend_status = 0;
   if (cudaMemcpy(h->sc, &s, sizeof(Scal), cudaMemcpyHostToDevice) != cudaSuccess)
     return bail(MHD_E_CUDA, "scalar upload failed");
   if (h->fp32) carve<float>(h, h->df, (char*)h->buf);
@@ -835,6 +848,7 @@ int mhd_checkpoint_load(const char* path, void** handle) {
   s.tau = sc4[0]; s.tau0 = sc4[1]; s.dt_cfl = sc4[2]; s.ab_coef = sc4[3];
   double inf = INFINITY;
   std::memcpy(&s.dtmin_bits, &inf, sizeof(double));
+  std::memcpy(&s.dtnext_bits, &inf, sizeof(double));
   if (cudaMemcpy(h->sc, &s, sizeof(Scal), cudaMemcpyHostToDevice) != cudaSuccess) {
     mhd_free(h);
     return fail(MHD_E_CUDA, "scalar upload failed");
@@ -907,11 +921,13 @@ int mhd_step_graph(void* handle, int32_t nsteps, double* tau_out, uint32_t* stat
 }
 
 static int graph_for(Handle* h, int nsteps, cudaGraphExec_t* out) {
-  auto key = std::make_pair(nsteps, h->par);
+  // the first captured step differs when the state was changed between steps
+  auto key = std::make_pair(nsteps, h->par + (h->prepared ? 2 : 0));
   auto it = h->graphs.find(key);
   if (it != h->graphs.end()) {
     *out = it->second.first;
-    h->par = it->second.second;  // the replay leaves this half current
+    h->par = it->second.second & 1;  // the replay leaves this half current
+    h->prepared = (it->second.second & 2) != 0;
     return MHD_OK;
   }
   cudaGraph_t gr;
@@ -925,7 +941,7 @@ static int graph_for(Handle* h, int nsteps, cudaGraphExec_t* out) {
   CK(cudaStreamEndCapture(h->st, &gr));
   CK(cudaGraphInstantiate(&ex, gr, 0));
   cudaGraphDestroy(gr);
-  h->graphs[key] = std::make_pair(ex, par);
+  h->graphs[key] = std::make_pair(ex, par + (h->prepared ? 2 : 0));
   h->par = par;
   *out = ex;
   return MHD_OK;
@@ -1331,7 +1347,10 @@ static int ens_launch(void** handles, int32_t ngrids, int32_t nsteps, std::vecto
     CK(cudaStreamWaitEvent(h0->st, e, 0));
     cudaEventDestroy(e);
   }
-  for (int i = 0; i < ngrids; ++i) hs[i]->par = it->second.par_end[i];
+  for (int i = 0; i < ngrids; ++i) {
+    hs[i]->par = it->second.par_end[i];
+    hs[i]->prepared = false;  // batched steps run their own CFL pass
+  }
   if (ev_before) CK(cudaEventRecord(ev_before, h0->st));
   CK(cudaGraphLaunch(it->second.ex, h0->st));
   if (ev_after) CK(cudaEventRecord(ev_after, h0->st));
@@ -1531,6 +1550,7 @@ int mhd_mlp_apply(void* handle, void* mlp) {
   Dev<float> d = at_par(h->df, h->par);
   int rc = mlp_correct(mlp, d, h->st);
   if (rc) return rc;
+  h->prepared = false;  // the corrected state needs its own CFL dt
   Launch<float>::fill_bxyz(d, true, h->st);
   CK(cudaGetLastError());
   return MHD_OK;

@@ -548,11 +548,56 @@ __global__ void k_bxyz_vf(Dev<T> d, int want_vf) {
 __device__ __forceinline__ double cfl_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float cfl_sqrt(float x) { return x > 0.0f ? x * rsqrtf(x) : 0.0f; }
 
+// get_dt of one cell (mhd3d3.f90:1608-1639) from its primitives and cell B,
+// with the status bits of its values.
+template <typename T, bool M>
+__device__ __forceinline__ T cell_dt(const Dev<T>& d, int c, int i, int j, int k, T r0, T p0, T u, T v, T w, T a,
+                                     T b, T cc, unsigned& st) {
+  typedef Ops<T> O;
+  T vv = cfl_sqrt(u * u + v * v + w * w);
+  T btot = cfl_sqrt(a * a + b * b + cc * cc);
+  T valf = O::dv(btot, cfl_sqrt(r0));
+  T vs = cfl_sqrt(O::dv(d.gam * p0, r0));
+  T vcfl = vv + cfl_sqrt(valf * valf + vs * vs);
+  T dt;
+  if (M)  // metric mode: 1/dx_a -> |mean area vector of the a-faces| / V
+    dt = O::dv(d.cfl, O::dw(vcfl * (T)d.m.sa[c], (T)d.m.vol[c], (T)d.m.rvol[c]));
+  else
+    dt = O::dv(d.cfl, O::dw(vcfl, d.wx[i], d.rwx[i]) + O::dw(vcfl, d.wy[j], d.rwy[j]) +
+                          O::dw(vcfl, d.wz[k], d.rwz[k]));
+  if (isnan(r0) || isnan(p0) || isnan(u) || isnan(v) || isnan(w)) st |= ST_NAN;
+  if (r0 < T(0)) st |= ST_NEG_RHO;
+  if (p0 < T(0)) st |= ST_NEG_P;
+  if (isnan(dt)) st |= ST_NAN;
+  return dt;
+}
+
+// Fold a thread's (dt, status) into the accumulators of the next step's
+// state: warp minimum, then one atomic per warp that lowers the running
+// minimum (a plain read first skips the rest).  Every lane of the warp calls it.
+template <typename T>
+__device__ __forceinline__ void dt_next_accumulate(Scal* sc, T m, unsigned st) {
+  for (int o = 16; o > 0; o >>= 1) {
+    T y = __shfl_xor_sync(0xffffffffu, m, o);
+    m = (y < m) ? y : m;
+    st |= __shfl_xor_sync(0xffffffffu, st, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    const double md = (double)m;
+    if (md >= 0.0) {
+      const unsigned long long bits = (unsigned long long)__double_as_longlong(md);
+      if (bits < *(volatile unsigned long long*)&sc->dtnext_bits) atomicMin(&sc->dtnext_bits, bits);
+    }
+    if (st) atomicOr(&sc->pend_status, st);
+  }
+}
+
 // save != 0 also stores U^n of the RK stage combines (advance_previous,
 // 3794-3819) at interior cells and faces, the only places they are read.
+// next != 0: the dt and status go to the next-step accumulators.
 // The minimum is reduced in T and converted to FP64 once per block.
 template <typename T, bool M, bool B>
-__global__ void __launch_bounds__(256, pass_min_blocks(B)) k_cfl(KArg<T, B> ka, int save) {
+__global__ void __launch_bounds__(256, pass_min_blocks(B)) k_cfl(KArg<T, B> ka, int save, int next) {
   const int4 bb = ka.blk();
   const auto& d = ka.dev(bb);
   const Geom& g = d.g;
@@ -583,24 +628,8 @@ __global__ void __launch_bounds__(256, pass_min_blocks(B)) k_cfl(KArg<T, B> ka, 
       if (ix && fy && iz) d.q[6][c] = d.bj[c];
       if (ix && iy && fz) d.q[7][c] = d.bk[c];
     }
-    // get_dt (mhd3d3.f90:1608-1639)
-    T a = d.bx[c], b = d.by[c], cc = d.bz[c];
-    T vv = cfl_sqrt(u * u + v * v + w * w);
-    T btot = cfl_sqrt(a * a + b * b + cc * cc);
-    T valf = O::dv(btot, cfl_sqrt(r0));
-    T vs = cfl_sqrt(O::dv(d.gam * p0, r0));
-    T vcfl = vv + cfl_sqrt(valf * valf + vs * vs);
-    T dt;
-    if (M)  // metric mode: 1/dx_a -> |mean area vector of the a-faces| / V
-      dt = O::dv(d.cfl, O::dw(vcfl * (T)d.m.sa[c], (T)d.m.vol[c], (T)d.m.rvol[c]));
-    else
-      dt = O::dv(d.cfl, O::dw(vcfl, d.wx[i], d.rwx[i]) + O::dw(vcfl, d.wy[j], d.rwy[j]) +
-                            O::dw(vcfl, d.wz[k], d.rwz[k]));
+    const T dt = cell_dt<T, M>(d, c, i, j, k, r0, p0, u, v, w, d.bx[c], d.by[c], d.bz[c], st);
     m = (dt < m) ? dt : m;
-    if (isnan(r0) || isnan(p0) || isnan(u) || isnan(v) || isnan(w)) st |= ST_NAN;
-    if (r0 < T(0)) st |= ST_NEG_RHO;
-    if (p0 < T(0)) st |= ST_NEG_P;
-    if (isnan(dt)) st |= ST_NAN;
   }
   for (int o = 16; o > 0; o >>= 1) {
     T y = __shfl_xor_sync(0xffffffffu, m, o);
@@ -618,19 +647,36 @@ __global__ void __launch_bounds__(256, pass_min_blocks(B)) k_cfl(KArg<T, B> ka, 
       st |= ss[w2];
     }
     const double md = (double)m;
-    if (md >= 0.0) atomicMin(&d.sc->dtmin_bits, (unsigned long long)__double_as_longlong(md));
-    if (st) atomicOr(&d.sc->status, st);
+    if (md >= 0.0) atomicMin(next ? &d.sc->dtnext_bits : &d.sc->dtmin_bits, (unsigned long long)__double_as_longlong(md));
+    if (st) atomicOr(next ? &d.sc->pend_status : &d.sc->status, st);
   }
+}
+
+// Empties the next-step accumulators before a dt pass refills them.
+__global__ inline void k_next_reset(Scal* sc) {
+  sc->dtnext_bits = (unsigned long long)__double_as_longlong(INFINITY);
+  sc->pend_status = 0;
 }
 
 // tau selection of step_ab (3609) / step_rk2,3 (3656-3661, 3723-3728).
 // mode 0: RK with fixed deck dt; 1: CFL dt every step; 2: AB (CFL dt and the
 // predictor coefficient tau/tau0/2, then tau0=tau).
+// mode | 4: take the dt and status accumulated for this state by the
+// previous step (dtnext_bits, pend_status) and empty them.
 template <typename T>
 __global__ void k_cfl_final(Dev<T> d, int mode) {
   Scal* s = d.sc;
-  double dt = __longlong_as_double((long long)s->dtmin_bits);
-  s->dtmin_bits = (unsigned long long)__double_as_longlong(INFINITY);
+  double dt;
+  if (mode & 4) {
+    dt = __longlong_as_double((long long)s->dtnext_bits);
+    s->dtnext_bits = (unsigned long long)__double_as_longlong(INFINITY);
+    s->status |= s->pend_status;
+    s->pend_status = 0;
+    mode &= 3;
+  } else {
+    dt = __longlong_as_double((long long)s->dtmin_bits);
+    s->dtmin_bits = (unsigned long long)__double_as_longlong(INFINITY);
+  }
   s->dt_cfl = dt;
   if (mode == 0) {
     if (dt < s->tau0) s->status |= ST_CFL;
@@ -1158,6 +1204,13 @@ __device__ __forceinline__ void cell_update_vals(const Dev<T>& d, int c, int cd,
   T rr = pv[0], u = pv[1], v = pv[2], ww = pv[3], pr = pv[4];
   T rvx0 = rr * u, rvy0 = rr * v, rvz0 = rr * ww;
   T eng0 = T(0.5) * rr * (u * u + v * v + ww * ww) + Ops<T>::dv(pr, gm1);
+  if (form == FORM_SAVE) {  // U^n of the step (this first stage's input), read by the later stages' combines
+    d.q[0][c] = rr;
+    d.q[1][c] = rvx0;
+    d.q[2][c] = rvy0;
+    d.q[3][c] = rvz0;
+    d.q[4][c] = eng0;
+  }
   T rho1 = rr - tau * dv[0];
   T eng1 = eng0 - tau * dv[4];
   T rx = rvx0 - tau * dv[1], ry = rvy0 - tau * dv[2], rz = rvz0 - tau * dv[3];
@@ -2413,12 +2466,12 @@ __device__ __forceinline__ void fill_shell_ijk(const Geom& g, int u, int& i, int
   i = ii < g.ng ? ii : ii + g.nx0;
 }
 
-// shell_only != 0: the launch covers only the shell blocks (block b is shell
-// block b), after k_ct_fill has done the interior.
-template <typename T, bool M, bool B>
-__global__ void __launch_bounds__(256, pass_min_blocks(B)) k_fill_bxyz(KArg<T, B> ka, int want_vf, int shell_only) {
-  const int4 bb = ka.blk();
-  const auto& d = ka.dev(bb);
+// One element of k_fill_bxyz; returns the CFL dt of its cell when want_dt
+// (a ghost cell of the shell: its values and widths, as get_dt sees them
+// after the fill), else +inf.
+template <typename T, bool M>
+__device__ __forceinline__ T fill_bxyz_elem(const Dev<T>& d, int4 bb, int want_vf, int shell_only, int want_dt,
+                                            unsigned& st) {
   const Geom& g = d.g;
   const FillShape fs(g);
   const int blk = shell_only ? bb.y + fs.nint : bb.y;
@@ -2429,11 +2482,11 @@ __global__ void __launch_bounds__(256, pass_min_blocks(B)) k_fill_bxyz(KArg<T, B
     i = g.ng + bx * 32 + (threadIdx.x & 31);
     j = g.ng + by * 8 + (threadIdx.x >> 5);
     k = g.ng + kz;
-    if (i >= g.ng + g.nx0 || j >= g.ng + g.ny0) return;  // those cells belong to no block here
+    if (i >= g.ng + g.nx0 || j >= g.ng + g.ny0) return T(INFINITY);  // those cells belong to no block here
     inner = true;
   } else {
     const int u = (blk - fs.nint) * 256 + threadIdx.x;
-    if (u >= fs.nshell) return;
+    if (u >= fs.nshell) return T(INFINITY);
     fill_shell_ijk(g, u, i, j, k);
     inner = false;
   }
@@ -2456,7 +2509,7 @@ __global__ void __launch_bounds__(256, pass_min_blocks(B)) k_fill_bxyz(KArg<T, B
       const T u = d.vx[c], v = d.vy[c], w = d.vz[c];
       d.vf[c] = sq(u * u + v * v + w * w) + sq((bx * bx + by * by + bz * bz) / d.rho[c]);
     }
-    return;
+    return T(INFINITY);
   }
   const int* cx = d.gmap;
   const int* cy = cx + g.nx + 2;
@@ -2475,7 +2528,7 @@ __global__ void __launch_bounds__(256, pass_min_blocks(B)) k_fill_bxyz(KArg<T, B
   const bool bi_copy = j < g.ny && k < g.nz && (sfi != i || gy || gz);
   const bool bj_copy = i < g.nx && k < g.nz && (gx || sfj != j || gz);
   const bool bk_copy = i < g.nx && j < g.ny && (gx || gy || sfk != k);
-  const bool need_cell = cell_copy || (cin && want_vf);
+  const bool need_cell = cell_copy || (cin && (want_vf || want_dt));
   const int sc = sci + px * scj + pl * sck;
   const int fi0 = sfi + px * scj + pl * sck, fi1 = sfi1 + px * scj + pl * sck;  // faces of the image cell
   const int fj0 = sci + px * sfj + pl * sck, fj1 = sci + px * sfj1 + pl * sck;
@@ -2504,7 +2557,7 @@ __global__ void __launch_bounds__(256, pass_min_blocks(B)) k_fill_bxyz(KArg<T, B
   if (bi_copy) d.bi[c] = bi0;
   if (bj_copy) d.bj[c] = bj0;
   if (bk_copy) d.bk[c] = bk0;
-  if (!cin) return;
+  if (!cin) return T(INFINITY);
   T bx, by, bz;
   if (M) {  // face fluxes of the images, geometry of this cell (as fill then get_bxyz)
     cell_b_metric<T>(d.m, c, bi0, bi1, bj0, bj1, bk0, bk1, bx, by, bz);
@@ -2517,6 +2570,21 @@ __global__ void __launch_bounds__(256, pass_min_blocks(B)) k_fill_bxyz(KArg<T, B
   d.by[c] = by;
   d.bz[c] = bz;
   if (want_vf) d.vf[c] = sq(ux * ux + uy * uy + uz * uz) + sq((bx * bx + by * by + bz * bz) / r0);
+  return want_dt ? cell_dt<T, M>(d, c, i, j, k, r0, p0, ux, uy, uz, bx, by, bz, st) : T(INFINITY);
+}
+
+// shell_only != 0: the launch covers only the shell blocks (block b is shell
+// block b), after k_ct_fill has done the interior.  dt_next != 0 (shell
+// only): the ghost cells' CFL dt and status go to the next-step accumulators.
+template <typename T, bool M, bool B>
+__global__ void __launch_bounds__(256, pass_min_blocks(B))
+    k_fill_bxyz(KArg<T, B> ka, int want_vf, int shell_only, int dt_next) {
+  const int4 bb = ka.blk();
+  const auto& d = ka.dev(bb);
+  unsigned st = 0;
+  const bool want_dt = !B && dt_next;  // single grids only (a batch runs its own CFL pass)
+  const T m = fill_bxyz_elem<T, M>(d, bb, want_vf, shell_only, want_dt, st);
+  if (want_dt) dt_next_accumulate(d.sc, m, st);
 }
 
 // CT fused with get_bxyz and vf on Cartesian meshes (advance_bijk + combine,
@@ -2532,54 +2600,74 @@ __global__ void __launch_bounds__(256, pass_min_blocks(B)) k_fill_bxyz(KArg<T, B
 // U^n, new primitives), so a recomputed face equals what its owner writes,
 // bit for bit, and the result equals k_update_b followed by the fill's
 // interior tiles.  The ghost shell of the new half follows in k_fill_bxyz
-// (shell_only).
+// (shell_only).  An RK first stage (form FORM_SAVE) also stores its input
+// face B as U^n of the later combines; dt_next (the last stage) accumulates
+// the CFL dt and status of the new cells for the next step, as k_cfl would
+// compute them at its start.
 template <typename T, bool B>
-__global__ void __launch_bounds__(256, pass_min_blocks(B)) k_ct_fill(KArg<T, B> ka, int form, T cw, T den, int want_vf) {
+__global__ void __launch_bounds__(256, pass_min_blocks(B))
+    k_ct_fill(KArg<T, B> ka, int form, T cw, T den, int want_vf, int dt_next) {
   const int4 bb = ka.blk();
   const auto& d = ka.dev(bb);
   const Geom& g = d.g;
   const int i = g.ng + bb.y * 32 + (threadIdx.x & 31);
   const int j = g.ng + bb.z * 8 + (threadIdx.x >> 5);
   const int k = g.ng + bb.w;
-  if (i >= g.ng + g.nx0 || j >= g.ng + g.ny0) return;
-  const int px = g.px, pl = (int)g.plane;
-  const int c = i + px * j + pl * k;
-  const T tau = (T)d.sc->tau;
-  const T dx = d.wx[i], dy = d.wy[j], dz = d.wz[k];
-  const T rx = d.rwx[i], ry = d.rwy[j], rz = d.rwz[k];
-  const T *ei = d.E[0], *ej = d.E[1], *ek = d.E[2];
-  typedef Ops<T> O;
-  auto new_bi = [&](int f) {
-    T b = d.bi[f] - tau * (O::dw(ek[f + px] - ek[f], dy, ry) - O::dw(ej[f + pl] - ej[f], dz, rz));
-    return form >= 0 ? comb(form, cw, d.q[5][f], b, den) : b;
-  };
-  auto new_bj = [&](int f) {
-    T b = d.bj[f] - tau * (O::dw(ei[f + pl] - ei[f], dz, rz) - O::dw(ek[f + 1] - ek[f], dx, rx));
-    return form >= 0 ? comb(form, cw, d.q[6][f], b, den) : b;
-  };
-  auto new_bk = [&](int f) {
-    T b = d.bk[f] - tau * (O::dw(ej[f + 1] - ej[f], dx, rx) - O::dw(ei[f + px] - ei[f], dy, ry));
-    return form >= 0 ? comb(form, cw, d.q[7][f], b, den) : b;
-  };
-  const T bil = new_bi(c), bih = new_bi(c + 1);
-  const T bjl = new_bj(c), bjh = new_bj(c + px);
-  const T bkl = new_bk(c), bkh = new_bk(c + pl);
-  d.obi[c] = bil;
-  d.obj[c] = bjl;
-  d.obk[c] = bkl;
-  if (i == g.ng + g.nx0 - 1) d.obi[c + 1] = bih;
-  if (j == g.ng + g.ny0 - 1) d.obj[c + px] = bjh;
-  if (k == g.ng + g.nz0 - 1) d.obk[c + pl] = bkh;
-  const T bx = T(0.5) * (bih + bil);
-  const T by = T(0.5) * (bjh + bjl);
-  const T bz = T(0.5) * (bkh + bkl);
-  d.bx[c] = bx;
-  d.by[c] = by;
-  d.bz[c] = bz;
-  if (want_vf) {
-    const T u = d.ovx[c], v = d.ovy[c], w = d.ovz[c];
-    d.vf[c] = sq(u * u + v * v + w * w) + sq((bx * bx + by * by + bz * bz) / d.orho[c]);
+  // batched stages neither store U^n nor accumulate the next dt (their CFL pass does both)
+  const bool save = !B && form == FORM_SAVE, want_dt = !B && dt_next;
+  T m = T(INFINITY);
+  unsigned st = 0;
+  if (i < g.ng + g.nx0 && j < g.ng + g.ny0) {
+    const int px = g.px, pl = (int)g.plane;
+    const int c = i + px * j + pl * k;
+    const T tau = (T)d.sc->tau;
+    const T dx = d.wx[i], dy = d.wy[j], dz = d.wz[k];
+    const T rx = d.rwx[i], ry = d.rwy[j], rz = d.rwz[k];
+    const T *ei = d.E[0], *ej = d.E[1], *ek = d.E[2];
+    typedef Ops<T> O;
+    auto new_bi = [&](int f) {
+      T b = d.bi[f] - tau * (O::dw(ek[f + px] - ek[f], dy, ry) - O::dw(ej[f + pl] - ej[f], dz, rz));
+      return form >= 0 ? comb(form, cw, d.q[5][f], b, den) : b;
+    };
+    auto new_bj = [&](int f) {
+      T b = d.bj[f] - tau * (O::dw(ei[f + pl] - ei[f], dz, rz) - O::dw(ek[f + 1] - ek[f], dx, rx));
+      return form >= 0 ? comb(form, cw, d.q[6][f], b, den) : b;
+    };
+    auto new_bk = [&](int f) {
+      T b = d.bk[f] - tau * (O::dw(ej[f + 1] - ej[f], dx, rx) - O::dw(ei[f + px] - ei[f], dy, ry));
+      return form >= 0 ? comb(form, cw, d.q[7][f], b, den) : b;
+    };
+    const bool lx = i == g.ng + g.nx0 - 1, ly = j == g.ng + g.ny0 - 1, lz = k == g.ng + g.nz0 - 1;
+    if (save) {  // face B^n of the step (this first stage's input) for the later combines
+      d.q[5][c] = d.bi[c];
+      d.q[6][c] = d.bj[c];
+      d.q[7][c] = d.bk[c];
+      if (lx) d.q[5][c + 1] = d.bi[c + 1];
+      if (ly) d.q[6][c + px] = d.bj[c + px];
+      if (lz) d.q[7][c + pl] = d.bk[c + pl];
+    }
+    const T bil = new_bi(c), bih = new_bi(c + 1);
+    const T bjl = new_bj(c), bjh = new_bj(c + px);
+    const T bkl = new_bk(c), bkh = new_bk(c + pl);
+    d.obi[c] = bil;
+    d.obj[c] = bjl;
+    d.obk[c] = bkl;
+    if (lx) d.obi[c + 1] = bih;
+    if (ly) d.obj[c + px] = bjh;
+    if (lz) d.obk[c + pl] = bkh;
+    const T bx = T(0.5) * (bih + bil);
+    const T by = T(0.5) * (bjh + bjl);
+    const T bz = T(0.5) * (bkh + bkl);
+    d.bx[c] = bx;
+    d.by[c] = by;
+    d.bz[c] = bz;
+    if (want_vf || want_dt) {
+      const T u = d.ovx[c], v = d.ovy[c], w = d.ovz[c], r0 = d.orho[c];
+      if (want_vf) d.vf[c] = sq(u * u + v * v + w * w) + sq((bx * bx + by * by + bz * bz) / r0);
+      if (want_dt) m = cell_dt<T, false>(d, c, i, j, k, r0, d.op[c], u, v, w, bx, by, bz, st);
+    }
   }
+  if (want_dt) dt_next_accumulate(d.sc, m, st);
 }
 
 // ------------------------------------------------------------ diagnostics
@@ -2714,11 +2802,12 @@ void Launch<T, M>::bxyz_vf(const Dev<T>& d, bool want_vf, cudaStream_t st) {
 
 template <typename T, bool M>
 void Launch<T, M>::fill_bxyz(const Dev<T>& d, bool want_vf, cudaStream_t st) {
-  k_fill_bxyz<T, M, false><<<FillShape(d.g).blocks(), 256, 0, st>>>(one(d), want_vf ? 1 : 0, 0);
+  k_fill_bxyz<T, M, false><<<FillShape(d.g).blocks(), 256, 0, st>>>(one(d), want_vf ? 1 : 0, 0, 0);
 }
 
 template <typename T, bool M>
-void Launch<T, M>::ct_fill(const Dev<T>& d, int form, double c, double den, bool want_vf, cudaStream_t st) {
+void Launch<T, M>::ct_fill(const Dev<T>& d, int form, double c, double den, bool want_vf, cudaStream_t st,
+                           bool dt_next) {
   if constexpr (M) {  // metric mode: CT, then the fill + bxyz pass of the new half
     ct(d, form, c, den, st);
     fill_bxyz(other_half(d), want_vf, st);
@@ -2728,8 +2817,9 @@ void Launch<T, M>::ct_fill(const Dev<T>& d, int form, double c, double den, bool
     prefer_carveout(k_ct_fill<T, false>, 0, pref_ct);
     prefer_carveout(k_fill_bxyz<T, false, false>, 0, pref_fill);
     k_ct_fill<T, false><<<dim3(fs.nbx, fs.nby, d.g.nz0), 256, 0, st>>>(one(d), form, (T)c, (T)den,
-                                                                        want_vf ? 1 : 0);
-    k_fill_bxyz<T, false, false><<<(fs.nshell + 255) / 256, 256, 0, st>>>(one(other_half(d)), want_vf ? 1 : 0, 1);
+                                                                        want_vf ? 1 : 0, dt_next ? 1 : 0);
+    k_fill_bxyz<T, false, false><<<(fs.nshell + 255) / 256, 256, 0, st>>>(one(other_half(d)), want_vf ? 1 : 0, 1,
+                                                                         dt_next ? 1 : 0);
   }
 }
 
@@ -2738,8 +2828,18 @@ void Launch<T, M>::cfl(const Dev<T>& d, int mode, cudaStream_t st, bool save) {
   dim3 grid((d.g.nx + 31) / 32, (d.g.ny + 7) / 8, (d.g.nz + 7) / 8);
   static PerDevice pref;
   prefer_carveout(k_cfl<T, M, false>, 0, pref);
-  k_cfl<T, M, false><<<grid, 256, 0, st>>>(one(d), save ? 1 : 0);
+  k_cfl<T, M, false><<<grid, 256, 0, st>>>(one(d), save ? 1 : 0, 0);
   k_cfl_final<T><<<1, 1, 0, st>>>(d, mode);
+}
+
+template <typename T, bool M>
+void Launch<T, M>::cfl_folded(const Dev<T>& d, int mode, bool recompute, cudaStream_t st) {
+  if (recompute) {
+    k_next_reset<<<1, 1, 0, st>>>(d.sc);
+    dim3 grid((d.g.nx + 31) / 32, (d.g.ny + 7) / 8, (d.g.nz + 7) / 8);
+    k_cfl<T, M, false><<<grid, 256, 0, st>>>(one(d), 0, 1);
+  }
+  k_cfl_final<T><<<1, 1, 0, st>>>(d, mode | 4);
 }
 
 template <typename T, bool M>
@@ -3069,7 +3169,7 @@ dim3 Batch<T>::dims(int fam, const Geom& g, int td, int ey) {
 template <typename T>
 void Batch<T>::cfl(const BatchView& v, int sel, int mode, cudaStream_t st) {
   KArg<T, true> a{(const Dev<T>*)v.tab[sel], v.map[BF_CFL]};
-  k_cfl<T, false, true><<<v.nblk[BF_CFL], 256, 0, st>>>(a, 1);
+  k_cfl<T, false, true><<<v.nblk[BF_CFL], 256, 0, st>>>(a, 1, 0);
   k_cfl_final_batch<T><<<(v.ngrids + 127) / 128, 128, 0, st>>>((const Dev<T>*)v.tab[sel], v.ngrids, mode);
 }
 
@@ -3169,9 +3269,9 @@ void Batch<T>::parts(const BatchView& v, int sel, int which, int form, double c,
     else batch_flux_t<T, TD>(v, tab, P, form, (T)c, (T)den, st);
   }
   if (which & 4) {  // face-B update + bxyz + vf (interior), then the ghost shell of the half the stage wrote
-    k_ct_fill<T, true><<<v.nblk[BF_CT], 256, 0, st>>>(KArg<T, true>{tab, v.map[BF_CT]}, form, (T)c, (T)den, 1);
+    k_ct_fill<T, true><<<v.nblk[BF_CT], 256, 0, st>>>(KArg<T, true>{tab, v.map[BF_CT]}, form, (T)c, (T)den, 1, 0);
     KArg<T, true> fa{(const Dev<T>*)v.tab[sel ^ 1], v.map[BF_FILL]};
-    k_fill_bxyz<T, false, true><<<v.nblk[BF_FILL], 256, 0, st>>>(fa, 1, 1);
+    k_fill_bxyz<T, false, true><<<v.nblk[BF_FILL], 256, 0, st>>>(fa, 1, 1, 0);
   }
 }
 

@@ -37,8 +37,12 @@ struct Scal {
   double ab_coef;                // tau/tau0/2 of advance_predictor_ab
   unsigned long long dtmin_bits; // running min of the CFL reduction (+inf between steps)
   unsigned int status;           // MHD_ST_* bits
-  unsigned int pad;
+  unsigned int pend_status;      // status bits of the state the next step starts from
+  unsigned long long dtnext_bits; // CFL dt of that state (min over cells, +inf when empty)
 };
+// form of an RK first stage that also stores U^n (the input state) for the
+// later stages' combines
+constexpr int FORM_SAVE = -2;
 
 // Curvilinear metric (metric mode only; FP64 in both precisions), computed
 // once on the device from the node coordinates.  Same padded layout as the
@@ -141,6 +145,11 @@ struct Launch {
   static void fill_bxyz(const Dev<T>& d, bool want_vf, cudaStream_t st);
   // mode: 0 RK fixed, 1 CFL, 2 AB, 3 read only; save: also store RK U^n
   static void cfl(const Dev<T>& d, int mode, cudaStream_t st, bool save = false);
+  // tau selection from the CFL dt and status that the previous step's last
+  // stage accumulated for this state (Scal::dtnext_bits, pend_status); with
+  // recompute, from a dt pass over the current state instead (first step,
+  // or after the state changed between steps)
+  static void cfl_folded(const Dev<T>& d, int mode, bool recompute, cudaStream_t st);
   static void save_prev(const Dev<T>& d, cudaStream_t st);
   static void predictor_ab(const Dev<T>& d, cudaStream_t st);
   // face fluxes of all three axes into F (kernel-level debug entry point)
@@ -155,7 +164,10 @@ struct Launch {
   static void ct(const Dev<T>& d, int form, double c, double den, cudaStream_t st);
   // Cartesian: CT + get_bxyz + vf over the interior cells in one pass, then
   // the ghost fill of the new half (d is the stage's view, as for ct)
-  static void ct_fill(const Dev<T>& d, int form, double c, double den, bool want_vf, cudaStream_t st);
+  // dt_next: also accumulate the CFL dt and status of the new state (all
+  // cells, ghosts included) for the next step
+  static void ct_fill(const Dev<T>& d, int form, double c, double den, bool want_vf, cudaStream_t st,
+                      bool dt_next = false);
   static void fill(const Dev<T>& d, cudaStream_t st);
   static void diagnostics(const Dev<T>& d, double* out5_dev, cudaStream_t st);
 };

@@ -140,6 +140,43 @@ def test_cfl_dt_mode_and_diagnostics():
     assert dg["rho_min"] == pytest.approx(do["rho_min"], rel=1e-12)
 
 
+@pytest.mark.parametrize("stepop", [STEP_RK2, STEP_RK3])
+def test_cfl_dt_sequence_across_graphs_diagnostics_and_batched_steps(stepop):
+    """Cartesian RK steps take the CFL dt that the previous step's last stage
+    accumulated for their starting state, and the first stage stores U^n;
+    the first step, a step after a batched ensemble step (which runs its own
+    CFL pass) and graph replays recompute or reuse it.  Every step's CFL dt
+    (dt_mode = CFL) and the final fields match the oracle stepped alongside."""
+    s = ics.turbulence(16, seed=11)
+    prm = Params(16, 16, 16, stepop=stepop, dt_mode=DT_CFL, tau=1.0)
+    o = OracleSolver(prm, s)
+    with MHDSolver(prm, s) as gpu:
+        seq = []
+        for n in range(3):
+            tg, sg = gpu.step(1)
+            to, so = o.step(1)
+            seq.append((tg, to))
+            assert sg == so == 0
+        gpu.diagnostics()  # a peek at the CFL dt between steps leaves the pending one alone
+        tg, _ = gpu.step(2, graph=True)
+        to, _ = o.step(2)
+        seq.append((tg, to))
+        ensemble_step([gpu], 1)
+        o.step(1)
+        tg, _ = gpu.step(1)
+        to, _ = o.step(1)
+        seq.append((tg, to))
+        tg, _ = gpu.step(2, graph=True)
+        to, _ = o.step(2)
+        seq.append((tg, to))
+        fg = gpu.fetch()
+    fo = o.fetch()
+    for tg, to in seq:
+        assert tg == pytest.approx(to, rel=1e-12)
+    for k in FIELDS:
+        assert relmax(fg[k], fo[k]) <= 1e-11, k
+
+
 @pytest.mark.slow
 def test_whole_step_parity_64cubed_100_steps():
     """All-FP64 mode vs the oracle: 64^3 periodic 3-D Orszag-Tang, PDM + RK2,
