@@ -541,16 +541,16 @@ static int create_handle(const mhd_params* prm, const double* dx, const double* 
   h->fp32 = (prm->precision == MHD_FP32);
   h->metric = metric;
   // the column sweeps are the fastest FP32 face shape at production sizes; the
-  // slice-streamed EMF when its ei launch has a block for every SM (about
-  // 128^3 and up), the 8x8 ei tiles on smaller grids (the autotuner may still
-  // pick others)
+  // slice-streamed EMF when its ei launch has at least 256 blocks (about
+  // 128^3 and up; 96^3 measured even), the 8x8 ei tiles on smaller grids (the
+  // autotuner may still pick others)
   h->tile_td = (h->fp32 && !metric) ? kSweepTile : 8;
   Geom& g = h->g;
   g.nx0 = prm->nx0; g.ny0 = prm->ny0; g.nz0 = prm->nz0;
   {
     const long long eb = (long long)((g.nx0 + 31) / 32) * ((g.ny0 + MHD_EMF_NW - 1) / MHD_EMF_NW) *
-                         emf_stream_segs(g.nz0, MHD_EMF_SEG);
-    h->tile_ey = (h->fp32 && !metric) ? (eb >= 152 ? kEmfStream : 8) : h->fp32 ? 8 : 4;
+                         emf_stream_segs(g.nz0, emf_stream_seg(g.nx0, g.ny0, g.nz0));
+    h->tile_ey = (h->fp32 && !metric) ? (eb >= 256 ? kEmfStream : 8) : h->fp32 ? 8 : 4;
   }
   g.nord = prm->nord; g.ng = prm->nord / 2;
   g.nx = g.nx0 + g.nord; g.ny = g.ny0 + g.nord; g.nz = g.nz0 + g.nord;

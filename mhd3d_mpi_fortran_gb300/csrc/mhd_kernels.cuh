@@ -1837,7 +1837,7 @@ __device__ __forceinline__ void cp_async_zfill(uint32_t dst, const T* src, bool 
 #endif
 template <typename T, int E, int NW, bool M, bool B>
 __global__ void __launch_bounds__(32 * NW, MHD_EMF_STREAM_MINB)
-    k_emf_stream(KArg<T, B> ka, Inp<T> in0, Prm<T> P, int seg) {
+    k_emf_stream(KArg<T, B> ka, Inp<T> in0, Prm<T> P) {
   const int4 bb = ka.blk();
   const auto& d = ka.dev(bb);
   const Inp<T> in = B ? state_view(d) : in0;
@@ -1859,6 +1859,7 @@ __global__ void __launch_bounds__(32 * NW, MHD_EMF_STREAM_MINB)
   const int nS0 = (E == 2) ? g.ny0 : g.nz0;     // interior cells along S
   const int nSg = (E == 2) ? g.ny : g.nz;
   const int nW0 = (E == 2) ? g.nz0 : g.ny0;
+  const int seg = emf_stream_seg(g.nx0, nW0, nS0);
   const int s_lo = g.ng + seg * bb.w;
   const int s_hi = (bb.w == emf_stream_segs(nS0, seg) - 1) ? g.ng + nS0 : s_lo + seg - 1;
   const int SS = (E == 2) ? g.px : (int)g.plane;  // global stride along S
@@ -2053,7 +2054,8 @@ __global__ void __launch_bounds__(256) k_emf_rows(KArg<T, B> ka, Inp<T> in0, Prm
 // blocks of streamed family E on one grid (x tiles, warp-axis tiles, segments)
 inline dim3 emf_stream_grid(int E, const Geom& g) {
   const int nS0 = (E == 2) ? g.ny0 : g.nz0, nW0 = (E == 2) ? g.nz0 : g.ny0;
-  return dim3((g.nx0 + 31) / 32, (nW0 + MHD_EMF_NW - 1) / MHD_EMF_NW, emf_stream_segs(nS0, MHD_EMF_SEG));
+  return dim3((g.nx0 + 31) / 32, (nW0 + MHD_EMF_NW - 1) / MHD_EMF_NW,
+              emf_stream_segs(nS0, emf_stream_seg(g.nx0, nW0, nS0)));
 }
 template <typename T, int E, bool M, bool B>
 void stream_attr() {
@@ -2073,8 +2075,7 @@ template <typename T, int E, bool M>
 void launch_emf_stream(const Dev<T>& d, const Inp<T>& in, const Prm<T>& P, cudaStream_t st) {
   typedef EmfStream<T, E, MHD_EMF_NW> K;
   stream_attr<T, E, M, false>();
-  k_emf_stream<T, E, MHD_EMF_NW, M, false><<<emf_stream_grid(E, d.g), K::NT, K::smem, st>>>(one(d), in, P,
-                                                                                          MHD_EMF_SEG);
+  k_emf_stream<T, E, MHD_EMF_NW, M, false><<<emf_stream_grid(E, d.g), K::NT, K::smem, st>>>(one(d), in, P);
 }
 
 template <typename T, bool M>
@@ -3211,11 +3212,11 @@ void batch_emf_stream(const BatchView& v, const Dev<T>* tab, const Prm<T>& P, cu
   const Inp<T> none{};
   constexpr int NT = 32 * MHD_EMF_NW;
   k_emf_stream<T, 0, MHD_EMF_NW, false, true><<<v.nblk[BF_EMF_I], NT, EmfStream<T, 0, MHD_EMF_NW>::smem, st>>>(
-      KArg<T, true>{tab, v.map[BF_EMF_I]}, none, P, MHD_EMF_SEG);
+      KArg<T, true>{tab, v.map[BF_EMF_I]}, none, P);
   k_emf_stream<T, 1, MHD_EMF_NW, false, true><<<v.nblk[BF_EMF_J], NT, EmfStream<T, 1, MHD_EMF_NW>::smem, st>>>(
-      KArg<T, true>{tab, v.map[BF_EMF_J]}, none, P, MHD_EMF_SEG);
+      KArg<T, true>{tab, v.map[BF_EMF_J]}, none, P);
   k_emf_stream<T, 2, MHD_EMF_NW, false, true><<<v.nblk[BF_EMF_K], NT, EmfStream<T, 2, MHD_EMF_NW>::smem, st>>>(
-      KArg<T, true>{tab, v.map[BF_EMF_K]}, none, P, MHD_EMF_SEG);
+      KArg<T, true>{tab, v.map[BF_EMF_K]}, none, P);
   k_emf_rows<T, false, true><<<v.nblk[BF_EMF_R], 256, emf_rows_smem<T>(), st>>>(
       KArg<T, true>{tab, v.map[BF_EMF_R]}, none, P);
 }

@@ -219,14 +219,28 @@ int mlp_status(void* h);
 constexpr int kSweepTile = 32;  // face-shape value of the column sweeps
 constexpr int kTileTD[4] = {4, 8, 16, kSweepTile};
 constexpr int kEmfStream = 1;   // EMF-shape value of the slice-streamed EMF families
-// Slice-streamed EMF launch shape: warps per block (edges along the warp
-// axis) and edge positions per segment of the stream axis (compile-time knobs).
+// Slice-streamed EMF launch shape (compile-time knobs): warps per block
+// (edges along the warp axis), the blocks a family's launch aims at, and the
+// shortest segment of the stream axis.  The EMF families run beside the face
+// fluxes on a second stream, so a launch of about two blocks per SM, each
+// streaming a long segment, leaves the flux kernels room.
 #ifndef MHD_EMF_NW
 #define MHD_EMF_NW 8
 #endif
-#ifndef MHD_EMF_SEG
-#define MHD_EMF_SEG 32
+#ifndef MHD_EMF_BLOCKS
+#define MHD_EMF_BLOCKS 304
 #endif
+#ifndef MHD_EMF_SEG_MIN
+#define MHD_EMF_SEG_MIN 16
+#endif
+// Edge positions per segment for a family with nx0 x nW0 edge columns and
+// nS0 + 1 edge positions along the stream axis.
+__host__ __device__ inline int emf_stream_seg(int nx0, int nW0, int nS0) {
+  const int cols = ((nx0 + 31) / 32) * ((nW0 + MHD_EMF_NW - 1) / MHD_EMF_NW);
+  const int nseg = (MHD_EMF_BLOCKS + cols / 2) / cols;
+  const int seg = (nS0 + 1) / (nseg > 1 ? nseg : 1);
+  return seg > MHD_EMF_SEG_MIN ? seg : MHD_EMF_SEG_MIN;
+}
 // Segments along the stream axis: nseg of seg edge positions, the last one taking the rest.
 __host__ __device__ inline int emf_stream_segs(int nS0, int seg) { return (nS0 + 1) / seg > 1 ? (nS0 + 1) / seg : 1; }
 constexpr int kTileEY[3] = {4, 8, kEmfStream};
