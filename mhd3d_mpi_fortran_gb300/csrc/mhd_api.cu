@@ -1432,32 +1432,27 @@ int mhd_autotune(void* handle, int32_t reps, int32_t out[2]) {
     if (rc) return rc;
     // The timed launches (EMF, face fluxes + update) write only scratch (E,
     // F, dU) and the other half of the double buffer, so the state a step
-    // starts from is untouched; every tile choice gives the same bits.
+    // starts from is untouched; every tile choice gives the same bits.  Each
+    // (face shape, EMF shape) pair is timed as a stage runs it: the EMF
+    // families on the side stream beside the face fluxes (a shape that is
+    // faster alone is not always the faster one there).
     float best = INFINITY;
-    int pick = h->tile_td;
+    int pick_td = h->tile_td, pick_ey = h->tile_ey;
     for (int td : kTileTD) {
-      h->tile_td = td;
-      carve<float>(h, h->df, (char*)h->buf);
-      Dev<float> d = at_par(h->df, h->par);
-      const Inp<float> in = state_inp(d);
-      Launch<float>::hydro(d, in, 0, -1, 0.0, 1.0, false, h->st);
-      const float ms = time_min(h->st, reps, [&] {
-        Launch<float>::hydro(d, in, 1, -1, 0.0, 1.0, false, h->st);
-        Launch<float>::hydro(d, in, 2, -1, 0.0, 1.0, false, h->st);
-      });
-      if (ms < best) { best = ms; pick = td; }
+      for (int ey : kTileEY) {
+        h->tile_td = td;
+        h->tile_ey = ey;
+        carve<float>(h, h->df, (char*)h->buf);
+        Dev<float> d = at_par(h->df, h->par);
+        const Inp<float> in = state_inp(d);
+        Rec none;
+        const float ms =
+            time_min(h->st, reps, [&] { emf_and_fluxes<float, false>(h, d, in, -1, 0.0, 1.0, false, h->st, none); });
+        if (ms < best) { best = ms; pick_td = td; pick_ey = ey; }
+      }
     }
-    h->tile_td = pick;
-    best = INFINITY;
-    pick = h->tile_ey;
-    for (int ey : kTileEY) {
-      h->tile_ey = ey;
-      carve<float>(h, h->df, (char*)h->buf);
-      Dev<float> d = at_par(h->df, h->par);
-      const float ms = time_min(h->st, reps, [&] { Launch<float>::emf(d, state_inp(d), h->st); });
-      if (ms < best) { best = ms; pick = ey; }
-    }
-    h->tile_ey = pick;
+    h->tile_td = pick_td;
+    h->tile_ey = pick_ey;
     carve<float>(h, h->df, (char*)h->buf);
     drop_graphs(h);
     CK(cudaGetLastError());
@@ -1477,7 +1472,8 @@ int mhd_set_tiles(void* handle, int32_t face_tile, int32_t ei_tile) {
   bool ok_td = false, ok_ey = false;
   for (int td : kTileTD) ok_td |= td == face_tile;
   for (int ey : kTileEY) ok_ey |= ey == ei_tile;
-  if (!ok_td || !ok_ey) return fail(MHD_E_ARG, "face tile must be 4, 8, 16 or 32 and EMF shape 4, 8 (ei tile) or 1 (slice streams)");
+  if (!ok_td || !ok_ey)
+    return fail(MHD_E_ARG, "face tile must be 4, 8, 16 or 32 and EMF shape 4, 8 (ei tile) or 1 (slice streams)");
   int rc = wait_stream(h);
   if (rc) return rc;
   h->tile_td = face_tile;
