@@ -573,8 +573,9 @@ __device__ __forceinline__ T cell_dt(const Dev<T>& d, int c, int i, int j, int k
 }
 
 // Fold a thread's (dt, status) into the accumulators of the next step's
-// state: warp minimum, then one atomic per warp that lowers the running
-// minimum (a plain read first skips the rest).  Every lane of the warp calls it.
+// state: block minimum (warp shuffles, then shared memory), then one atomic
+// per block that lowers the running minimum (a plain read first skips the
+// rest).  Every thread of the 256-thread block calls it.
 template <typename T>
 __device__ __forceinline__ void dt_next_accumulate(Scal* sc, T m, unsigned st) {
   for (int o = 16; o > 0; o >>= 1) {
@@ -582,7 +583,16 @@ __device__ __forceinline__ void dt_next_accumulate(Scal* sc, T m, unsigned st) {
     m = (y < m) ? y : m;
     st |= __shfl_xor_sync(0xffffffffu, st, o);
   }
-  if ((threadIdx.x & 31) == 0) {
+  __shared__ T bm[8];
+  __shared__ unsigned bs[8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { bm[wid] = m; bs[wid] = st; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < 8; ++w) {
+      m = (bm[w] < m) ? bm[w] : m;
+      st |= bs[w];
+    }
     const double md = (double)m;
     if (md >= 0.0) {
       const unsigned long long bits = (unsigned long long)__double_as_longlong(md);
