@@ -1201,8 +1201,12 @@ static int build_batch(Handle* const* hs, int n, BatchBufs& b) {
 }
 
 // nsteps RK steps of every grid of a batch; returns the number of half swaps.
+// The EMF families of a stage run on the side stream st2 beside the face
+// fluxes (they read the same stage input and write disjoint arrays), joined
+// before CT, as a single grid's stage runs them.
 template <typename T>
-static int enqueue_batch(const BatchView& v, int stepop, int dt_mode, int nsteps, cudaStream_t st) {
+static int enqueue_batch(const BatchView& v, int stepop, int dt_mode, int nsteps, cudaStream_t st,
+                         cudaStream_t st2, cudaEvent_t fork, cudaEvent_t join) {
   int flips = 0;
   const int nst = (stepop == MHD_STEP_RK2) ? 2 : 3;
   for (int s = 0; s < nsteps; ++s) {
@@ -1215,7 +1219,15 @@ static int enqueue_batch(const BatchView& v, int stepop, int dt_mode, int nsteps
         else if (k == 2) { form = 1; c = 3.0; den = 4.0; }
         else { form = 2; c = 2.0; den = 3.0; }
       }
-      Batch<T>::stage(v, flips & 1, form, c, den, st);
+      const int sel = flips & 1;
+      // (a failed record or wait surfaces when the capture ends)
+      cudaEventRecord(fork, st);
+      cudaStreamWaitEvent(st2, fork, 0);
+      Batch<T>::parts(v, sel, 1, form, c, den, st2);
+      Batch<T>::parts(v, sel, 2, form, c, den, st);
+      cudaEventRecord(join, st2);
+      cudaStreamWaitEvent(st, join, 0);
+      Batch<T>::parts(v, sel, 4, form, c, den, st);
       ++flips;
     }
   }
@@ -1234,8 +1246,11 @@ static int capture_ensemble(const std::vector<Handle*>& hs, int nsteps, cudaGrap
     int rc = h0->fp32 ? build_batch<float>(hs.data(), n, bufs) : build_batch<double>(hs.data(), n, bufs);
     if (rc) return rc;
     CK(cudaStreamBeginCapture(h0->st, cudaStreamCaptureModeThreadLocal));
-    const int flips = h0->fp32 ? enqueue_batch<float>(bufs.view, h0->prm.stepop, h0->prm.dt_mode, nsteps, h0->st)
-                               : enqueue_batch<double>(bufs.view, h0->prm.stepop, h0->prm.dt_mode, nsteps, h0->st);
+    const int flips =
+        h0->fp32 ? enqueue_batch<float>(bufs.view, h0->prm.stepop, h0->prm.dt_mode, nsteps, h0->st, h0->st2,
+                                        h0->ev_fork, h0->ev_join)
+                 : enqueue_batch<double>(bufs.view, h0->prm.stepop, h0->prm.dt_mode, nsteps, h0->st, h0->st2,
+                                         h0->ev_fork, h0->ev_join);
     CK(cudaStreamEndCapture(h0->st, &gr));
     for (int i = 0; i < n; ++i) pars[i] = hs[i]->par ^ (flips & 1);
   } else {
@@ -1496,32 +1511,30 @@ int mhd_ensemble_autotune(void** handles, int32_t ngrids, int32_t reps, int32_t 
       int rc = wait_stream(h);
       if (rc) return rc;
     }
+    // each (face shape, EMF shape) pair timed as a batched stage runs it: the
+    // EMF families on the side stream beside the face fluxes
     int best_td = h0->tile_td, best_ey = h0->tile_ey;
     float best = INFINITY;
     for (int td : kTileTD) {
-      for (Handle* h : hs) h->tile_td = td;
-      BatchBufs b;
-      int rc = build_batch<float>(hs.data(), ngrids, b);
-      if (rc == MHD_OK) {
-        const float ms = time_min(h0->st, reps, [&] { Batch<float>::parts(b.view, 0, 2, -1, 0.0, 1.0, h0->st); });
-        if (ms < best) { best = ms; best_td = td; }
+      for (int ey : kTileEY) {
+        for (Handle* h : hs) { h->tile_td = td; h->tile_ey = ey; }
+        BatchBufs b;
+        int rc = build_batch<float>(hs.data(), ngrids, b);
+        if (rc == MHD_OK) {
+          const float ms = time_min(h0->st, reps, [&] {
+            cudaEventRecord(h0->ev_fork, h0->st);
+            cudaStreamWaitEvent(h0->st2, h0->ev_fork, 0);
+            Batch<float>::parts(b.view, 0, 1, -1, 0.0, 1.0, h0->st2);
+            Batch<float>::parts(b.view, 0, 2, -1, 0.0, 1.0, h0->st);
+            cudaEventRecord(h0->ev_join, h0->st2);
+            cudaStreamWaitEvent(h0->st, h0->ev_join, 0);
+          });
+          if (ms < best) { best = ms; best_td = td; best_ey = ey; }
+        }
+        cudaFree(b.tabs);
+        cudaFree(b.maps);
+        if (rc) return rc;
       }
-      cudaFree(b.tabs);
-      cudaFree(b.maps);
-      if (rc) return rc;
-    }
-    best = INFINITY;
-    for (int ey : kTileEY) {
-      for (Handle* h : hs) { h->tile_td = best_td; h->tile_ey = ey; }
-      BatchBufs b;
-      int rc = build_batch<float>(hs.data(), ngrids, b);
-      if (rc == MHD_OK) {
-        const float ms = time_min(h0->st, reps, [&] { Batch<float>::parts(b.view, 0, 1, -1, 0.0, 1.0, h0->st); });
-        if (ms < best) { best = ms; best_ey = ey; }
-      }
-      cudaFree(b.tabs);
-      cudaFree(b.maps);
-      if (rc) return rc;
     }
     for (Handle* h : hs) {
       h->tile_td = best_td;
