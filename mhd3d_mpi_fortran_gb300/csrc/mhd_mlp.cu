@@ -137,6 +137,35 @@ __device__ __forceinline__ void gelu16_store(unsigned char* tile, int r, int c0,
   }
 }
 
+// The inference epilogue of gelu16_store on the packed FP32 pipe: GELU (tanh
+// form) of two accumulators plus their biases (bias pairs from shared memory),
+// rounded to BF16 as one pair.  Same operations as gelu_t's value.
+__device__ __forceinline__ uint32_t gelu2_bf16(float2 z, float2 b) {
+  const float2 c = make_float2(0.7978845608028654f, 0.7978845608028654f);
+  const float2 a = make_float2(0.044715f, 0.044715f), h = make_float2(0.5f, 0.5f);
+  z = __fadd2_rn(z, b);
+  const float2 z3 = __fmul2_rn(__fmul2_rn(__fmul2_rn(a, z), z), z);  // a z^3
+  const float2 u = __fmul2_rn(c, __fadd2_rn(z, z3));
+  const float2 t = make_float2(tanh_sfu(u.x), tanh_sfu(u.y));
+  const float2 g = __fmul2_rn(__fmul2_rn(h, z), __fadd2_rn(make_float2(1.0f, 1.0f), t));
+  const __nv_bfloat162 v = __floats2bfloat162_rn(g.x, g.y);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+__device__ __forceinline__ void gelu16_store_sm(unsigned char* tile, int r, int c0, const float* z,
+                                                const float* sbias) {
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const float4 b0 = *reinterpret_cast<const float4*>(sbias + c0 + 8 * h);
+    const float4 b1 = *reinterpret_cast<const float4*>(sbias + c0 + 8 * h + 4);
+    const float* zz = z + 8 * h;
+    const uint32_t p0 = gelu2_bf16(make_float2(zz[0], zz[1]), make_float2(b0.x, b0.y));
+    const uint32_t p1 = gelu2_bf16(make_float2(zz[2], zz[3]), make_float2(b0.z, b0.w));
+    const uint32_t p2 = gelu2_bf16(make_float2(zz[4], zz[5]), make_float2(b1.x, b1.y));
+    const uint32_t p3 = gelu2_bf16(make_float2(zz[6], zz[7]), make_float2(b1.z, b1.w));
+    *reinterpret_cast<uint4*>(tile + tc::kmaj(r, c0 + 8 * h, NH)) = make_uint4(p0, p1, p2, p3);
+  }
+}
+
 // Copy a row-major [R x K] BF16 matrix into a K-major canonical tile.
 __device__ __forceinline__ void stage_w(unsigned char* dst, const __nv_bfloat16* src, int R, int K) {
   const int k8n = K / 8;
@@ -437,9 +466,11 @@ __global__ void __launch_bounds__(256, 2)
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tslot;
+  __shared__ __align__(16) float sbias[2 * NH];  // hidden-layer biases (b1, b2)
   const int tid = threadIdx.x, warp = tid >> 5, q = warp & 3, row = tid & 127, half = tid >> 7;
   if (warp == 0) tc::tmem_alloc(&tslot, 256);
   if (tid == 0) tc::bar_init(&bar, 1);
+  if (tid < 2 * NH) sbias[tid] = tid < NH ? w.p[OB1 + tid] : w.p[OB2 + tid - NH];
   stage_w(sm + I_W1, w.w1, NH, FIN);
   stage_w(sm + I_W2, w.w2, NH, NH);
   stage_w(sm + I_W3, w.w3, NO, NH);
@@ -477,7 +508,7 @@ __global__ void __launch_bounds__(256, 2)
     for (int c0 = 32 * half; c0 < 32 * half + 32; c0 += 16) {  // H1 over the consumed input tile
       float z[16];
       tc::tmem_ld16(tc::tmem_at(tb + T_D1, q, c0), z);
-      gelu16_store(XS, row, c0, z, w.p + OB1);
+      gelu16_store_sm(XS, row, c0, z, sbias);
     }
     publish();
     if (tid == 0) gemm(tb + T_D2, s0 + I_X, s0 + I_W2, NH, NH, false);
@@ -486,7 +517,7 @@ __global__ void __launch_bounds__(256, 2)
     for (int c0 = 32 * half; c0 < 32 * half + 32; c0 += 16) {  // H2 over H1 (consumed)
       float z[16];
       tc::tmem_ld16(tc::tmem_at(tb + T_D2, q, c0), z);
-      gelu16_store(XS, row, c0, z, w.p + OB2);
+      gelu16_store_sm(XS, row, c0, z, sbias + NH);
     }
     publish();
     if (tid == 0) gemm(tb + T_D3, s0 + I_X, s0 + I_W3, NO, NH, false);
@@ -564,10 +595,21 @@ __global__ void k_iota(int* idx, int count, long long off) {
 // block and variable.
 __global__ void __launch_bounds__(256) k_mlp_sums(const float* __restrict__ Y, long long n, double* sums) {
   __shared__ double part[8][5];
-  double a[5] = {0, 0, 0, 0, 0};
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+  // a thread's own few rows in FP32 with compensation (Neumaier), then FP64
+  float s[5] = {0, 0, 0, 0, 0}, e[5] = {0, 0, 0, 0, 0};
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const float4 y0 = *reinterpret_cast<const float4*>(Y + t * NOUT);
+    const float y[5] = {y0.x, y0.y, y0.z, y0.w, Y[t * NOUT + 4]};
 #pragma unroll
-    for (int q = 0; q < 5; ++q) a[q] += (double)Y[t * NOUT + q];
+    for (int q = 0; q < 5; ++q) {
+      const float u = s[q] + y[q];
+      e[q] += fabsf(s[q]) >= fabsf(y[q]) ? (s[q] - u) + y[q] : (y[q] - u) + s[q];
+      s[q] = u;
+    }
+  }
+  double a[5];
+#pragma unroll
+  for (int q = 0; q < 5; ++q) a[q] = (double)s[q] + (double)e[q];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int q = 0; q < 5; ++q) {
@@ -633,12 +675,18 @@ __global__ void k_mlp_apply_b(Dev<float> d) {
   // interior-periodic cell value of d.dU[5+a]; every index here lies in
   // [-1, n0], so one conditional wrap per axis is the periodic image
   auto wrap = [](int x, int n) { return x < 0 ? x + n : (x >= n ? x - n : x); };
-  auto at = [&](int a, int i, int j, int k) -> float {
-    i = wrap(i, g.nx0);
-    j = wrap(j, g.ny0);
-    k = wrap(k, g.nz0);
-    return d.dU[5 + a][(long long)(i + g.ng) + (long long)g.px * ((long long)(j + g.ng) + (long long)g.py * (k + g.ng))];
-  };
+  const int iw = i0 % g.nx0, jw = j0 % g.ny0, kw = k0 % g.nz0;  // the periodic face this one images
+  // padded offsets of the wrapped indices iw-1, iw, iw+1 (and likewise j, k):
+  // the edges below read cells at offsets -1 .. +1 of (iw, jw, kw) only
+  int ox[3], oy[3], oz[3];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    ox[m] = wrap(iw + m - 1, g.nx0) + g.ng;
+    oy[m] = g.px * (wrap(jw + m - 1, g.ny0) + g.ng);
+    oz[m] = (int)g.plane * (wrap(kw + m - 1, g.nz0) + g.ng);
+  }
+  // cell value of d.dU[5+a] at (iw + di, jw + dj, kw + dk), di, dj, dk in -1..1
+  auto at = [&](int a, int di, int dj, int dk) -> float { return d.dU[5 + a][ox[di + 1] + oy[dj + 1] + oz[dk + 1]]; };
   auto ex = [&](int i, int j, int k) {
     return 0.25f * (at(0, i, j, k) + at(0, i, j - 1, k) + at(0, i, j, k - 1) + at(0, i, j - 1, k - 1));
   };
@@ -650,15 +698,14 @@ __global__ void k_mlp_apply_b(Dev<float> d) {
   };
   const int i = i0 + g.ng, j = j0 + g.ng, k = k0 + g.ng;
   const long long c = (long long)i + (long long)g.px * ((long long)j + (long long)g.py * k);
-  const int iw = i0 % g.nx0, jw = j0 % g.ny0, kw = k0 % g.nz0;  // the periodic face this one images
   const float rdx = d.rwx[g.ng + iw], rdy = d.rwy[g.ng + jw], rdz = d.rwz[g.ng + kw];
   const bool in_x = i0 < g.nx0, in_y = j0 < g.ny0, in_z = k0 < g.nz0;
   if (in_y && in_z)
-    d.bi[c] += (ez(iw, jw + 1, kw) - ez(iw, jw, kw)) * rdy - (ey(iw, jw, kw + 1) - ey(iw, jw, kw)) * rdz;
+    d.bi[c] += (ez(0, 1, 0) - ez(0, 0, 0)) * rdy - (ey(0, 0, 1) - ey(0, 0, 0)) * rdz;
   if (in_x && in_z)
-    d.bj[c] += (ex(iw, jw, kw + 1) - ex(iw, jw, kw)) * rdz - (ez(iw + 1, jw, kw) - ez(iw, jw, kw)) * rdx;
+    d.bj[c] += (ex(0, 0, 1) - ex(0, 0, 0)) * rdz - (ez(1, 0, 0) - ez(0, 0, 0)) * rdx;
   if (in_x && in_y)
-    d.bk[c] += (ey(iw + 1, jw, kw) - ey(iw, jw, kw)) * rdx - (ex(iw, jw + 1, kw) - ex(iw, jw, kw)) * rdy;
+    d.bk[c] += (ey(1, 0, 0) - ey(0, 0, 0)) * rdx - (ex(0, 1, 0) - ex(0, 0, 0)) * rdy;
 }
 
 int mfail(int code, const std::string& m) {
