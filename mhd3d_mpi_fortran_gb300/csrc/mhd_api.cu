@@ -1434,9 +1434,10 @@ static void drop_graphs(Handle* h) {
   h->graphs.clear();
 }
 
-// FP32 Cartesian PDM: face tiles 4/8/16 or the column sweeps, ei tile 4x4/8x8;
-// the other FP32 Cartesian reconstructions: face tile 8 (4 and 16 run as 8) or
-// the column sweeps (their EMF launch shapes are fixed, the ei value is ignored).
+// FP32 Cartesian PDM: face tiles 4/8/16 or the column sweeps, EMF as ei tiles
+// 4x4/8x8 or slice streams; the other FP32 Cartesian reconstructions: face tile
+// 8 (4 and 16 run as 8) or the column sweeps (their EMF launch shapes are
+// fixed, the EMF value is ignored).
 static bool tunable(const Handle* h) { return h->fp32 && !h->metric; }
 
 int mhd_autotune(void* handle, int32_t reps, int32_t out[2]) {

@@ -1832,7 +1832,6 @@ struct EmfStream {
       sizeof(typename Pr<T>::V) * (DV * NS + (SA2 ? 0 : NW * C)) + sizeof(T) * (2 * NS + 4 * NS);
 };
 
-
 template <typename T>
 __device__ __forceinline__ void cp_async_zfill(uint32_t dst, const T* src, bool ok) {
   const int n = ok ? (int)sizeof(T) : 0;  // 0: nothing is read, the element is zeroed
@@ -2074,10 +2073,6 @@ void stream_attr() {
   if (attr.need(bit)) {
     cudaFuncSetAttribute(k_emf_stream<T, E, MHD_EMF_NW, M, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)EmfStream<T, E, MHD_EMF_NW>::smem);
-#ifdef MHD_EMF_CARVEOUT
-    cudaFuncSetAttribute(k_emf_stream<T, E, MHD_EMF_NW, M, B>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                         MHD_EMF_CARVEOUT);
-#endif
     attr.mark(bit);
   }
 }

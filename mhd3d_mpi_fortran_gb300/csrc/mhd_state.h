@@ -106,8 +106,9 @@ struct Dev {
   Metric m;
   T* mw[3];
   T* mbn[3];
-  // launch shapes (host side only): y/z face-tile length and ei EMF tile,
-  // chosen by the autotuner for the FP32 Cartesian PDM path
+  // launch shapes (host side only): y/z face-tile length and EMF shape (ei
+  // tile 4 or 8, or kEmfStream), chosen by the autotuner for the FP32 Cartesian
+  // PDM path
   int tile_td, tile_ey;
   int emf;           // edge EMF scheme: 0 LFM, 1 Yee
   T* ye[12];         // Yee split electric fields, [x, y, z edges][pp, np, pn, nn] (emf = 1)

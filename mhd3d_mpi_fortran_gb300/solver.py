@@ -97,7 +97,7 @@ class MHDSolver:
 
     def autotune(self, reps: int = 5) -> tuple:
         """Pick the fastest compiled launch shapes for this grid (mhd_autotune);
-        returns (face-tile length, EMF tile)."""
+        returns (face-tile length, EMF shape: 4 or 8 = ei tile, 1 = slice streams)."""
         out = (C.c_int32 * 2)()
         check(self.lib, self.lib.mhd_autotune(self.h, int(reps), out), "mhd_autotune")
         return out[0], out[1]
