@@ -100,6 +100,26 @@ struct MlpW {
   const float* p;                                 // FP32 parameters (biases read from here)
 };
 
+// Division by a grid extent d >= 1 with a multiplier and shift computed on
+// the host (the round-up method of Granlund & Montgomery, 1994): q =
+// (umulhi(n, m) + n) >> l with l = ceil(log2 d) and m = 2^32 (2^l - d) / d + 1,
+// exact for 0 <= n < 2^31 (the sum then stays below 2^32).
+struct FastDiv {
+  uint32_t m = 0;
+  int l = 0;
+  FastDiv() = default;
+  explicit FastDiv(int d) {
+    while ((1ull << l) < (unsigned long long)d) ++l;
+    m = (uint32_t)(((1ull << 32) * ((1ull << l) - (unsigned long long)d)) / (unsigned long long)d + 1ull);
+  }
+  __device__ __forceinline__ uint32_t div(uint32_t n) const { return (__umulhi(n, m) + n) >> l; }
+};
+// interior cell index t -> (i, j, k) of an nx0 x ny0 x nz0 grid
+struct CellMap {
+  FastDiv by_nx, by_ny;
+};
+inline CellMap cell_map(const Geom& g) { return CellMap{FastDiv(g.nx0), FastDiv(g.ny0)}; }
+
 // tanh on the SFU (PTX tanh.approx.f32, sm_75+; maximum relative error about
 // 2^-11, below the BF16 rounding the activations take next).
 __device__ __forceinline__ float tanh_sfu(float x) {
@@ -429,24 +449,29 @@ __global__ void k_mlp_features(Dev<float> d, MlpNorm nm, uint4* __restrict__ fie
 // input tile: the 3x3x3 stencil of the feature records, feature
 // ((dz+1)*9 + (dy+1)*3 + (dx+1))*8 + var; 216..255 zero.  Eight features are
 // one 16-byte core-matrix row of the K-major tile; this thread writes the
-// 16 of the row's 32 such chunks that start at chunk h*16 (t < 0: zeros).
-__device__ __forceinline__ void gather_half_row(const Dev<float>& d, const uint4* __restrict__ field, long long t,
-                                                unsigned char* tile, int r, int h) {
+// 16 of the row's 32 such chunks that start at chunk H*16 (t < 0: zeros).
+// H is a template argument, so every chunk's stencil offset is a constant.
+template <int H>
+__device__ __forceinline__ void gather_half_row(const Dev<float>& d, const CellMap& cm,
+                                                const uint4* __restrict__ field, long long t, unsigned char* tile,
+                                                int r) {
   const Geom& g = d.g;
   long long c0 = 0;
   if (t >= 0) {
-    const int i = (int)(t % g.nx0) + g.ng;
-    const long long q = t / g.nx0;
-    const int j = (int)(q % g.ny0) + g.ng, k = (int)(q / g.ny0) + g.ng;
-    c0 = (long long)i + (long long)g.px * ((long long)j + (long long)g.py * k);
+    const uint32_t q = cm.by_nx.div((uint32_t)t), k = cm.by_ny.div(q);
+    const int i = (int)((uint32_t)t - q * (uint32_t)g.nx0) + g.ng;
+    const int j = (int)(q - k * (uint32_t)g.ny0) + g.ng;
+    c0 = (long long)i + (long long)g.px * ((long long)j + (long long)g.py * ((int)k + g.ng));
   }
+  const long long px = g.px, pl = g.plane;
 #pragma unroll
   for (int u = 0; u < 16; ++u) {
-    const int ch = 16 * h + u;  // chunk = stencil point ((dz+1)*9 + (dy+1)*3 + (dx+1)), 27..31 padding
+    constexpr int base = 16 * H;
+    const int ch = base + u;  // chunk = stencil point ((dz+1)*9 + (dy+1)*3 + (dx+1)), 27..31 padding
     uint4 v = make_uint4(0, 0, 0, 0);
     if (t >= 0 && ch < 27) {
       const int dz = ch / 9 - 1, dy = (ch / 3) % 3 - 1, dx = ch % 3 - 1;
-      v = field[c0 + dx + (long long)g.px * (dy + (long long)g.py * dz)];
+      v = field[c0 + dx + px * dy + pl * dz];
     }
     *reinterpret_cast<uint4*>(tile + tc::kmaj(r, 8 * ch, FIN)) = v;
   }
@@ -461,16 +486,17 @@ __device__ __forceinline__ void gather_half_row(const Dev<float>& d, const uint4
 // warps share each TMEM lane quarter and the GELU work.
 template <bool GRID>
 __global__ void __launch_bounds__(256, 2)
-    k_mlp_infer(const __nv_bfloat16* __restrict__ X, Dev<float> d, const uint4* __restrict__ field, int n, MlpW w,
-                float* __restrict__ Y, int* err) {
+    k_mlp_infer(const __nv_bfloat16* __restrict__ X, Dev<float> d, CellMap cm, const uint4* __restrict__ field, int n,
+                MlpW w, float* __restrict__ Y, int* err) {
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tslot;
-  __shared__ __align__(16) float sbias[2 * NH];  // hidden-layer biases (b1, b2)
+  __shared__ __align__(16) float sbias[2 * NH + NOUT];  // biases b1, b2 and the used outputs of b3
   const int tid = threadIdx.x, warp = tid >> 5, q = warp & 3, row = tid & 127, half = tid >> 7;
   if (warp == 0) tc::tmem_alloc(&tslot, 256);
   if (tid == 0) tc::bar_init(&bar, 1);
-  if (tid < 2 * NH) sbias[tid] = tid < NH ? w.p[OB1 + tid] : w.p[OB2 + tid - NH];
+  if (tid < 2 * NH + NOUT)
+    sbias[tid] = tid < NH ? w.p[OB1 + tid] : tid < 2 * NH ? w.p[OB2 + tid - NH] : w.p[OB3 + tid - 2 * NH];
   stage_w(sm + I_W1, w.w1, NH, FIN);
   stage_w(sm + I_W2, w.w2, NH, NH);
   stage_w(sm + I_W3, w.w3, NO, NH);
@@ -491,7 +517,8 @@ __global__ void __launch_bounds__(256, 2)
   for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     if (GRID) {
       const long long g = (long long)tile * 128 + row;
-      gather_half_row(d, field, g < n ? g : -1, XS, row, half);
+      if (half == 0) gather_half_row<0>(d, cm, field, g < n ? g : -1, XS, row);
+      else gather_half_row<1>(d, cm, field, g < n ? g : -1, XS, row);
     } else {
       for (int t = tid; t < 128 * (FIN / 8); t += blockDim.x) {
         const int r = t >> 5, c8 = (t & 31) * 8;
@@ -527,8 +554,12 @@ __global__ void __launch_bounds__(256, 2)
       float y[16];
       tc::tmem_ld16(tc::tmem_at(tb + T_D3, q, 0), y);
       const long long g = (long long)tile * 128 + row;
-      if (g < n)
-        for (int o = 0; o < NOUT; ++o) Y[g * NOUT + o] = y[o] + w.p[OB3 + o];
+      if (g < n) {
+        const float* b3 = sbias + 2 * NH;
+        float4* yo = reinterpret_cast<float4*>(Y + g * NOUT);
+        yo[0] = make_float4(y[0] + b3[0], y[1] + b3[1], y[2] + b3[2], y[3] + b3[3]);
+        yo[1] = make_float4(y[4] + b3[4], y[5] + b3[5], y[6] + b3[6], y[7] + b3[7]);
+      }
     }
     tc::fence_before();
     __syncthreads();
@@ -700,12 +731,17 @@ __global__ void k_mlp_apply_b(Dev<float> d) {
   const long long c = (long long)i + (long long)g.px * ((long long)j + (long long)g.py * k);
   const float rdx = d.rwx[g.ng + iw], rdy = d.rwy[g.ng + jw], rdz = d.rwz[g.ng + kw];
   const bool in_x = i0 < g.nx0, in_y = j0 < g.ny0, in_z = k0 < g.nz0;
-  if (in_y && in_z)
-    d.bi[c] += (ez(0, 1, 0) - ez(0, 0, 0)) * rdy - (ey(0, 0, 1) - ey(0, 0, 0)) * rdz;
-  if (in_x && in_z)
-    d.bj[c] += (ex(0, 0, 1) - ex(0, 0, 0)) * rdz - (ez(1, 0, 0) - ez(0, 0, 0)) * rdx;
-  if (in_x && in_y)
-    d.bk[c] += (ey(1, 0, 0) - ey(0, 0, 0)) * rdx - (ex(0, 1, 0) - ex(0, 0, 0)) * rdy;
+  // the nine edge potentials (every cell load ahead of the stores, so loads
+  // shared between edges are issued once), then the three face increments
+  const float ex0 = ex(0, 0, 0), ex_z = ex(0, 0, 1), ex_y = ex(0, 1, 0);
+  const float ey0 = ey(0, 0, 0), ey_z = ey(0, 0, 1), ey_x = ey(1, 0, 0);
+  const float ez0 = ez(0, 0, 0), ez_y = ez(0, 1, 0), ez_x = ez(1, 0, 0);
+  const float dbi = (ez_y - ez0) * rdy - (ey_z - ey0) * rdz;
+  const float dbj = (ex_z - ex0) * rdz - (ez_x - ez0) * rdx;
+  const float dbk = (ey_x - ey0) * rdx - (ex_y - ex0) * rdy;
+  if (in_y && in_z) d.bi[c] += dbi;
+  if (in_x && in_z) d.bj[c] += dbj;
+  if (in_x && in_y) d.bk[c] += dbk;
 }
 
 int mfail(int code, const std::string& m) {
@@ -975,8 +1011,8 @@ int mhd_mlp_forward(void* h, const uint16_t* x, int64_t n, float* y) {
   }
   cudaMemcpy(dx, x, (size_t)n * FIN * 2, cudaMemcpyHostToDevice);
   const int tiles = (int)((n + 127) / 128);
-  k_mlp_infer<false><<<tiles < 2 * m->sms ? tiles : 2 * m->sms, 256, I_TOTAL>>>(dx, Dev<float>{}, nullptr, (int)n,
-                                                                                 wview(m), dy, m->err);
+  k_mlp_infer<false><<<tiles < 2 * m->sms ? tiles : 2 * m->sms, 256, I_TOTAL>>>(dx, Dev<float>{}, CellMap{}, nullptr,
+                                                                                 (int)n, wview(m), dy, m->err);
   cudaError_t e = cudaDeviceSynchronize();
   if (e == cudaSuccess) e = cudaMemcpy(y, dy, (size_t)n * NOUT * 4, cudaMemcpyDeviceToHost);
   cudaFree(dx);
@@ -1017,8 +1053,8 @@ int mhd::mlp_correct(void* h, Dev<float>& d, cudaStream_t st) {
   uint4* field = reinterpret_cast<uint4*>(d.F[0][0]);
   const long long ncell = (long long)d.g.nx * d.g.ny * d.g.nz;
   k_mlp_features<<<(int)((ncell + 255) / 256), 256, 0, st>>>(d, m->norm, field);
-  k_mlp_infer<true><<<tiles < 2 * m->sms ? tiles : 2 * m->sms, 256, I_TOTAL, st>>>(nullptr, d, field, (int)n,
-                                                                                   wview(m), m->ys, m->err);
+  k_mlp_infer<true><<<tiles < 2 * m->sms ? tiles : 2 * m->sms, 256, I_TOTAL, st>>>(nullptr, d, cell_map(d.g), field,
+                                                                                   (int)n, wview(m), m->ys, m->err);
   if (!m->sums) MCK(cudaMalloc(&m->sums, 8 * sizeof(double)));
   MCK(cudaMemsetAsync(m->sums, 0, 8 * sizeof(double), st));
   k_mlp_sums<<<m->sms * 4, 256, 0, st>>>(m->ys, (long long)n, m->sums);
