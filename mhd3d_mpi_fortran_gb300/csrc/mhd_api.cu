@@ -1560,8 +1560,9 @@ int mhd_mlp_apply(void* handle, void* mlp) {
   Dev<float> d = at_par(h->df, h->par);
   int rc = mlp_correct(mlp, d, h->st);
   if (rc) return rc;
-  h->prepared = false;  // the corrected state needs its own CFL dt
-  Launch<float>::fill_bxyz(d, true, h->st);
+  // the refill of the corrected state also gives the next step its CFL dt
+  Launch<float>::fill_bxyz(d, true, h->st, true);
+  h->prepared = true;
   CK(cudaGetLastError());
   return MHD_OK;
 }

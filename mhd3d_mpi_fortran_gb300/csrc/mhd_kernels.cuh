@@ -2473,8 +2473,7 @@ __device__ __forceinline__ void fill_shell_ijk(const Geom& g, int u, int& i, int
 }
 
 // One element of k_fill_bxyz; returns the CFL dt of its cell when want_dt
-// (a ghost cell of the shell: its values and widths, as get_dt sees them
-// after the fill), else +inf.
+// (its values and widths, as get_dt sees them after the fill), else +inf.
 template <typename T, bool M>
 __device__ __forceinline__ T fill_bxyz_elem(const Dev<T>& d, int4 bb, int want_vf, int shell_only, int want_dt,
                                             unsigned& st) {
@@ -2511,9 +2510,10 @@ __device__ __forceinline__ T fill_bxyz_elem(const Dev<T>& d, int4 bb, int want_v
     d.bx[c] = bx;
     d.by[c] = by;
     d.bz[c] = bz;
-    if (want_vf) {
-      const T u = d.vx[c], v = d.vy[c], w = d.vz[c];
-      d.vf[c] = sq(u * u + v * v + w * w) + sq((bx * bx + by * by + bz * bz) / d.rho[c]);
+    if (want_vf || want_dt) {
+      const T u = d.vx[c], v = d.vy[c], w = d.vz[c], r0 = d.rho[c];
+      if (want_vf) d.vf[c] = sq(u * u + v * v + w * w) + sq((bx * bx + by * by + bz * bz) / r0);
+      if (want_dt) return cell_dt<T, M>(d, c, i, j, k, r0, d.p[c], u, v, w, bx, by, bz, st);
     }
     return T(INFINITY);
   }
@@ -2580,8 +2580,8 @@ __device__ __forceinline__ T fill_bxyz_elem(const Dev<T>& d, int4 bb, int want_v
 }
 
 // shell_only != 0: the launch covers only the shell blocks (block b is shell
-// block b), after k_ct_fill has done the interior.  dt_next != 0 (shell
-// only): the ghost cells' CFL dt and status go to the next-step accumulators.
+// block b), after k_ct_fill has done the interior.  dt_next != 0: the CFL dt
+// and status of the cells the launch covers go to the next-step accumulators.
 template <typename T, bool M, bool B>
 __global__ void __launch_bounds__(256, pass_min_blocks(B))
     k_fill_bxyz(KArg<T, B> ka, int want_vf, int shell_only, int dt_next) {
@@ -2807,8 +2807,10 @@ void Launch<T, M>::bxyz_vf(const Dev<T>& d, bool want_vf, cudaStream_t st) {
 }
 
 template <typename T, bool M>
-void Launch<T, M>::fill_bxyz(const Dev<T>& d, bool want_vf, cudaStream_t st) {
-  k_fill_bxyz<T, M, false><<<FillShape(d.g).blocks(), 256, 0, st>>>(one(d), want_vf ? 1 : 0, 0, 0);
+void Launch<T, M>::fill_bxyz(const Dev<T>& d, bool want_vf, cudaStream_t st, bool dt_next) {
+  const bool dt = dt_next && !M;
+  if (dt) k_next_reset<<<1, 1, 0, st>>>(d.sc);
+  k_fill_bxyz<T, M, false><<<FillShape(d.g).blocks(), 256, 0, st>>>(one(d), want_vf ? 1 : 0, 0, dt ? 1 : 0);
 }
 
 template <typename T, bool M>

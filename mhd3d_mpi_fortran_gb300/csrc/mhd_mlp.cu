@@ -159,15 +159,17 @@ __device__ __forceinline__ void gelu16_store(unsigned char* tile, int r, int c0,
 
 // The inference epilogue of gelu16_store on the packed FP32 pipe: GELU (tanh
 // form) of two accumulators plus their biases (bias pairs from shared memory),
-// rounded to BF16 as one pair.  Same operations as gelu_t's value.
+// rounded to BF16 as one pair.  gelu_t's value with its constants folded:
+// u = c z + (c a) z^3 = z (c + (c a) z^2), GELU = h z + h z t (h = 1/2).
 __device__ __forceinline__ uint32_t gelu2_bf16(float2 z, float2 b) {
   const float2 c = make_float2(0.7978845608028654f, 0.7978845608028654f);
-  const float2 a = make_float2(0.044715f, 0.044715f), h = make_float2(0.5f, 0.5f);
+  const float2 ca = make_float2(0.7978845608028654f * 0.044715f, 0.7978845608028654f * 0.044715f);
+  const float2 h = make_float2(0.5f, 0.5f);
   z = __fadd2_rn(z, b);
-  const float2 z3 = __fmul2_rn(__fmul2_rn(__fmul2_rn(a, z), z), z);  // a z^3
-  const float2 u = __fmul2_rn(c, __fadd2_rn(z, z3));
+  const float2 u = __fmul2_rn(z, __ffma2_rn(ca, __fmul2_rn(z, z), c));
   const float2 t = make_float2(tanh_sfu(u.x), tanh_sfu(u.y));
-  const float2 g = __fmul2_rn(__fmul2_rn(h, z), __fadd2_rn(make_float2(1.0f, 1.0f), t));
+  const float2 hz = __fmul2_rn(h, z);
+  const float2 g = __ffma2_rn(hz, t, hz);
   const __nv_bfloat162 v = __floats2bfloat162_rn(g.x, g.y);
   return *reinterpret_cast<const uint32_t*>(&v);
 }

@@ -143,7 +143,9 @@ template <typename T, bool M = false>
 struct Launch {
   static void bxyz_vf(const Dev<T>& d, bool want_vf, cudaStream_t st);
   // ghost fill + get_bxyz + vf in one pass
-  static void fill_bxyz(const Dev<T>& d, bool want_vf, cudaStream_t st);
+  // dt_next (Cartesian): also the CFL dt and status of every cell for the
+  // next step (the accumulators emptied first), as the step's dt pass gives them
+  static void fill_bxyz(const Dev<T>& d, bool want_vf, cudaStream_t st, bool dt_next = false);
   // mode: 0 RK fixed, 1 CFL, 2 AB, 3 read only; save: also store RK U^n
   static void cfl(const Dev<T>& d, int mode, cudaStream_t st, bool save = false);
   // tau selection from the CFL dt and status that the previous step's last
