@@ -77,9 +77,10 @@ struct Handle {
   std::vector<cudaEvent_t> pool;
   std::vector<int> fam;
   int par = 0;                 // which half of the double-buffered primitives is current
-  // the previous RK step left the CFL dt and status of the current state in
-  // Scal::dtnext_bits / pend_status (cleared whenever the state changes
-  // between steps: init, load, learned correction, batched steps)
+  // the previous RK step (or the learned correction's refill) left the CFL dt
+  // and status of the current state in Scal::dtnext_bits / pend_status;
+  // cleared when the state changes otherwise between steps (init, load,
+  // batched steps)
   bool prepared = false;
   int tile_td = 8, tile_ey = 8;  // launch shapes (autotuned for FP32 Cartesian PDM)
   float* geoT = nullptr;       // FP32 copy of the cell widths
