@@ -402,16 +402,18 @@ def test_set_tiles_every_shape_gives_identical_steps():
     assert info[0] > 0 and info[1] >= 10 and info[3] > 0
 
 
-@pytest.mark.parametrize("shape", [(33, 17, 9), (64, 40, 24), (16, 64, 33), (8, 8, 8)])
-def test_streamed_emf_equals_tiles(shape):
+@pytest.mark.parametrize("shape,nord", [((33, 17, 9), 8), ((64, 40, 24), 8), ((16, 64, 33), 8), ((8, 8, 8), 8),
+                                        ((40, 24, 20), 10)])
+def test_streamed_emf_equals_tiles(shape, nord):
     """The slice-streamed EMF families (one edge column per thread along z for
     ei and ej, along y for ek; the last edge row of the in-slice transverse
     axis in a separate launch) against the shared-memory tiles: every EMF,
     and the state after RK2 steps, bit-identical on ragged grids whose x
     extent is not a multiple of the 32-lane tile, whose stream axis spans one
-    or several segments, and a grid smaller than one tile."""
-    s = rand_state(*shape, seed=sum(shape) + 1)
-    prm = Params(*shape, precision=FP32, tau=2e-4)
+    or several segments, a grid smaller than one tile, and 5 ghost layers
+    (the slices keep the 4-cell stencil halo whatever the ghost depth)."""
+    s = rand_state(*shape, seed=sum(shape) + 1, nord=nord)
+    prm = Params(*shape, precision=FP32, tau=2e-4, nord=nord)
     out = {}
     for ey in (8, 1):
         with MHDSolver(prm, s) as g:
