@@ -116,3 +116,59 @@ def test_trained_correction_reduces_coarse_error():
     assert ev["corrected_status"] == 0 and ev["corrected_divb"] <= 1e-4
     assert ev["corrected_l1"] < ev["coarse_l1"], ev
     mlp.close()
+
+
+def test_grid_inference_equals_matrix_inference_on_a_ragged_grid():
+    """The correction's in-grid inference (each row gathers its 3x3x3 stencil
+    of feature records by padded cell index, the cell index split by
+    host-computed multipliers) against the matrix inference on feature rows
+    built on the host, on a periodic 20 x 12 x 24 grid: the hydro increments
+    (zero-mean, times the output scale) and the face-B curl of the vector
+    potential that one application adds agree with the host's to the BF16
+    rounding of the features; a wrong gather would move them by O(1)."""
+    nx, ny, nz = 20, 12, 24
+    s = ics.orszag_tang_3d(nx, seed=3, ny0=ny, nz0=nz)
+    prm = Params(nx, ny, nz, precision=FP32, tau=1e-3)
+    ng = prm.nord // 2
+    mlp = learned.MLP(learned.init_params(4) * 0.3)
+    mean = np.array([0.2, 0.01, -0.01, 0.0, 0.5, 0.0, 0.0, 0.0], np.float32)
+    std = np.array([0.1, 0.2, 0.2, 0.1, 0.3, 0.2, 0.2, 0.1], np.float32)
+    scale = np.full(8, 1e-3, np.float32)
+    mlp.set_norm(mean, std, scale)
+    with MHDSolver(prm, s) as g:
+        f0 = g.fetch()
+        mlp.apply(g)
+        f1 = g.fetch()
+    U0, U1 = learned.conserved(f0, ng), learned.conserved(f1, ng)
+    Un = (U0 - mean[:, None, None, None].astype(np.float64)) / std[:, None, None, None]
+    cols = []
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                sh = np.roll(Un, shift=(-dx, -dy, -dz), axis=(1, 2, 3))
+                cols.append(sh.reshape(8, -1, order="F").T)
+    x = np.zeros((nx * ny * nz, learned.FIN), dtype=np.float32)
+    x[:, :216] = np.concatenate(cols, axis=1)
+    y = mlp.forward(learned.bf16_bits(x)).astype(np.float64)  # [cells, 8], x fastest
+    mlp.close()
+    # hydro increments: zero-mean outputs times the scale
+    dh = (y[:, :5] - y[:, :5].mean(axis=0)) * scale[:5]
+    dU = (U1[:5] - U0[:5]).reshape(5, -1, order="F").T
+    for q in range(5):
+        ref = dh[:, q]
+        assert np.abs(dU[:, q] - ref).max() <= 2e-2 * np.abs(ref).max() + 1e-7, q
+    # face B: the curl of the edge means of the cell potentials A = y[5:8] * scale
+    A = (y[:, 5:8] * scale[5:8]).T.reshape(3, nx, ny, nz, order="F")
+    r = np.roll
+
+    def edge(a, ax1, ax2):
+        v = A[a]
+        return 0.25 * (v + r(v, 1, ax1) + r(v, 1, ax2) + r(r(v, 1, ax1), 1, ax2))
+    ex, ey, ez = edge(0, 1, 2), edge(1, 0, 2), edge(2, 0, 1)
+    hx, hy, hz = 1.0 / nx, 1.0 / ny, 1.0 / nz
+    d = lambda e, ax, h: (r(e, -1, ax) - e) / h
+    ref = {"bi": d(ez, 1, hy) - d(ey, 2, hz), "bj": d(ex, 2, hz) - d(ez, 0, hx), "bk": d(ey, 0, hx) - d(ex, 1, hy)}
+    sl = (slice(ng, ng + nx), slice(ng, ng + ny), slice(ng, ng + nz))
+    for k in ("bi", "bj", "bk"):
+        got = f1[k][sl] - f0[k][sl]
+        assert np.abs(got - ref[k]).max() <= 2e-2 * np.abs(ref[k]).max() + 1e-6, k
