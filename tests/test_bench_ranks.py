@@ -84,9 +84,19 @@ def test_profile_ingest_maps_kernels_to_families(tmp_path):
         "void mhd::k_flux_sweep<float, 2, 0, 1>(mhd::KArg<T1, T3>)": "flux_z_update",
         "void mhd::k_ct_fill<float, 0>(mhd::KArg<T1, T2>, int)": "ct",
         "void mhd::k_fill_bxyz<float, 0, 0>(mhd::KArg<T1, T3>, int, int)": "ct",
+        "void mhd::k_emf_stream<float, 0, 8, 0, 0>(mhd::KArg<T1, T5>, mhd::Inp<T1>, mhd::Prm<T1>)": "emf",
+        "void mhd::k_emf_rows<float, 0, 0>(mhd::KArg<T1, T3>, mhd::Inp<T1>, mhd::Prm<T1>)": "emf",
+        "void mhd::k_cfl_final<float>(mhd::Dev<T1>, int)": "dt",
     }
     for k, fam in names.items():
         assert bench._family(k) == fam, k
+    # classes with their own launches per RK2 step: the boundary-row launch and
+    # the ghost shell are counted apart from their families' main kernels
+    assert bench._class("void mhd::k_emf_rows<float, 0, 0>(x)") == "emf_rows"
+    assert bench._class("void mhd::k_emf_stream<float, 2, 8, 0, 0>(x)") == "emf"
+    assert bench._class("void mhd::k_fill_bxyz<float, 0, 0>(x)") == "shell"
+    assert bench._class("void mhd::k_ct_fill<float, 0>(x)") == "ct_fill"
+    assert bench._PER_STEP["emf"] == 6 and bench._PER_STEP["emf_rows"] == 2
     csv = tmp_path / "c.csv"
     lines = ['"ID","Kernel Name","Metric Name","Metric Unit","Metric Value"']
     for i, k in enumerate(names):
@@ -97,3 +107,11 @@ def test_profile_ingest_maps_kernels_to_families(tmp_path):
     assert [r[0] for r in rows] == list(names)
     assert rows[2][1]["smsp__thread_inst_executed.sum"] == 300.0
     assert rows[0][1]["gpu__time_duration.sum"] == 1000.0
+    # per-step sums: each class scaled from its captured launches to its
+    # launches per RK2 step, then summed into its family
+    fam = bench._step_sums(str(csv), lambda m: {"inst": m["smsp__thread_inst_executed.sum"]})
+    inst = {k: 100 * (i + 1) for i, k in enumerate(names)}
+    ks = list(names)
+    assert fam["emf"]["inst"] == 6 * (inst[ks[1]] + inst[ks[7]]) / 2 + 2 * inst[ks[8]]
+    assert fam["ct"]["inst"] == 2 * inst[ks[5]] + 2 * inst[ks[6]]
+    assert fam["dt"]["inst"] == (inst[ks[0]] + inst[ks[9]]) / 2
